@@ -1,0 +1,94 @@
+"""Seeded synthetic DEM states and the material-table derivation.
+
+The tables follow the reference's property registry:
+  Yeff    = 1/((1-nu_i^2)/E_i + (1-nu_j^2)/E_j)        src/global_properties.cpp:449
+  Geff    = 1/(2(2-nu_i)(1+nu_i)/E_i + 2(2-nu_j)(1+nu_j)/E_j)   :480
+  betaeff = ln e / sqrt(ln^2 e + pi^2)                   :556
+  coeffRestLog = ln e                                    :518
+with the same operand order, so on the same libm the values are bit-identical
+to the reference's MatrixProperty data.  Matrices are (ntypes+1)^2 with types
+starting at 1 (row/column 0 unused).
+
+A "case" is a plain dict describing one system: box, periodicity, dt, skin,
+contact-model switches, material tables, primitive planes and the initial
+atoms (tag, type, x, v, omega, radius, rmass).  The same dict drives the GPU
+handle, the CPU oracle and the reference input scripts.
+"""
+import math
+
+import numpy as np
+
+MY_PI = 3.14159265358979323846
+
+
+def derive_tables(E, nu, rest, frict, rollfrict=None):
+    """E, nu: per type (length nt); rest, frict, rollfrict: nt x nt."""
+    nt = len(E)
+    Y = np.zeros((nt + 1, nt + 1))
+    G = np.zeros((nt + 1, nt + 1))
+    B = np.zeros((nt + 1, nt + 1))
+    RL = np.zeros((nt + 1, nt + 1))
+    MU = np.zeros((nt + 1, nt + 1))
+    MUR = np.zeros((nt + 1, nt + 1))
+    for i in range(1, nt + 1):
+        for j in range(1, nt + 1):
+            Yi, Yj, vi, vj = float(E[i - 1]), float(E[j - 1]), float(nu[i - 1]), float(nu[j - 1])
+            Y[i, j] = 1. / ((1. - math.pow(vi, 2.)) / Yi + (1. - math.pow(vj, 2.)) / Yj)
+            G[i, j] = 1. / (2. * (2. - vi) * (1. + vi) / Yi + 2. * (2. - vj) * (1. + vj) / Yj)
+            lg = math.log(float(rest[i - 1][j - 1]))
+            RL[i, j] = lg
+            B[i, j] = lg / math.sqrt(math.pow(lg, 2.) + math.pow(math.pi, 2.))
+            MU[i, j] = float(frict[i - 1][j - 1])
+            MUR[i, j] = float(rollfrict[i - 1][j - 1]) if rollfrict is not None else 0.0
+    return dict(Yeff=Y, Geff=G, betaeff=B, coeffRestLog=RL, coeffFrict=MU, coeffRollFrict=MUR)
+
+
+def sphere_mass(radius, density):
+    """rmass of atom_style granular, src/atom_vec_sphere.cpp:1076-1080."""
+    r = np.asarray(radius, dtype=np.float64)
+    return 4.0 * MY_PI / 3.0 * r * r * r * np.asarray(density, dtype=np.float64)
+
+
+def lattice_case(seed, nx, ny, nz, spacing, radius=(1e-3, 1e-3), density=2500.0,
+                 z0=None, jitter=0.0, vmax=0.0, wmax=0.0, ntypes=1, E=(5e6,), nu=(0.45,),
+                 rest=((0.9,),), frict=((0.5,),), rollfrict=None, periodic=(1, 1, 0),
+                 zhi=None, dt=1e-6, skin=5e-4, gravity=(0.0, 0.0, -9.81), plane_z=0.0,
+                 normal_model=0, rolling_model=0, charVel=0.0, pad=(0.0, 0.0)):
+    """Jittered cubic lattice of spheres in a box periodic in x/y with a floor.
+
+    Box x/y extents are nx*spacing, ny*spacing (exactly periodic lattice);
+    z starts at z0 (default: radius_max) and the box top is zhi.
+    """
+    rng = np.random.default_rng(seed)
+    n = nx * ny * nz
+    Lx, Ly = nx * spacing + pad[0], ny * spacing + pad[1]
+    rmax = radius[1]
+    if z0 is None:
+        z0 = rmax
+    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    x = np.stack([(ii.ravel() + 0.5) * spacing, (jj.ravel() + 0.5) * spacing,
+                  z0 + kk.ravel() * spacing], axis=1).astype(np.float64)
+    if jitter > 0:
+        x += rng.uniform(-jitter, jitter, size=x.shape)
+        x[:, 2] = np.maximum(x[:, 2], z0 - jitter)
+    if zhi is None:
+        zhi = z0 + nz * spacing + 4 * rmax
+    r = rng.uniform(radius[0], radius[1], size=n) if radius[0] != radius[1] else np.full(n, radius[0])
+    typ = rng.integers(1, ntypes + 1, size=n).astype(np.int32)
+    v = rng.uniform(-vmax, vmax, size=(n, 3)) if vmax > 0 else np.zeros((n, 3))
+    w = rng.uniform(-wmax, wmax, size=(n, 3)) if wmax > 0 else np.zeros((n, 3))
+    rmass = sphere_mass(r, density)
+    case = dict(
+        boxlo=(0.0, 0.0, 0.0), boxhi=(Lx, Ly, float(zhi)), periodic=tuple(periodic),
+        dt=dt, skin=skin, cdf=1.0, neigh=(1, 0, 1), normal_model=normal_model,
+        rolling_model=rolling_model, gravity=gravity, ntypes=ntypes, charVel=charVel,
+        planes=[(2, plane_z, 1, rolling_model)] if plane_z is not None else [],
+        material=dict(E=list(E), nu=list(nu), rest=[list(r_) for r_ in rest],
+                      frict=[list(f_) for f_ in frict],
+                      rollfrict=[list(f_) for f_ in rollfrict] if rollfrict is not None else None,
+                      density=density),
+        atoms=dict(tag=np.arange(1, n + 1, dtype=np.int32), type=typ, x=x, v=v, omega=w,
+                   radius=r, rmass=rmass),
+    )
+    case.update(derive_tables(E, nu, rest, frict, rollfrict))
+    return case

@@ -1,0 +1,165 @@
+"""ORACLE — TEST INFRASTRUCTURE ONLY.
+
+ctypes binding of ``dem_oracle.c`` (the CPU restatement of the reference's
+sphere timestep).  ``build()`` compiles it with ``-ffp-contract=off`` so that
+the arithmetic is plain IEEE double on x86-64 and on aarch64 alike.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle_dem.so")
+
+NORMAL_HERTZ, NORMAL_HOOKE = 0, 1
+ROLLING_OFF, ROLLING_CDT = 0, 1
+COHESION_OFF, COHESION_BOND_NONLINEAR = 0, 1
+
+
+def build(force=False):
+    src = os.path.join(HERE, "dem_oracle.c")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp"
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", src,
+                           "-o", tmp, "-lm"])
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class OrcConfig(ctypes.Structure):
+    _fields_ = [("boxlo", ctypes.c_double * 3), ("boxhi", ctypes.c_double * 3),
+                ("periodic", ctypes.c_int * 3), ("dt", ctypes.c_double),
+                ("skin", ctypes.c_double), ("contact_distance_factor", ctypes.c_double),
+                ("neigh_every", ctypes.c_int), ("neigh_delay", ctypes.c_int),
+                ("neigh_check", ctypes.c_int), ("normal_model", ctypes.c_int),
+                ("rolling_model", ctypes.c_int), ("cohesion_model", ctypes.c_int),
+                ("tangential_damping", ctypes.c_int), ("limit_force", ctypes.c_int),
+                ("gravity_on", ctypes.c_int), ("gravity", ctypes.c_double * 3)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        P = ctypes.c_void_p
+        L.orc_create.restype = P
+        L.orc_create.argtypes = [ctypes.POINTER(OrcConfig)]
+        L.orc_destroy.argtypes = [P]
+        L.orc_last_error.restype = ctypes.c_char_p
+        L.orc_last_error.argtypes = [P]
+        L.orc_set_pair_params.argtypes = [P, ctypes.c_int] + [P] * 6 + [ctypes.c_double]
+        L.orc_add_plane.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.orc_set_atoms.argtypes = [P, ctypes.c_int] + [P] * 7
+        L.orc_setup.argtypes = [P]
+        L.orc_run.argtypes = [P, ctypes.c_int]
+        for fn in ("orc_natoms", "orc_npairs", "orc_dnum"):
+            getattr(L, fn).argtypes = [P]
+        L.orc_nrebuilds.restype = ctypes.c_long
+        L.orc_nrebuilds.argtypes = [P]
+        L.orc_ntimestep.restype = ctypes.c_long
+        L.orc_ntimestep.argtypes = [P]
+        L.orc_get_atoms.argtypes = [P] + [P] * 9
+        L.orc_get_pairs.argtypes = [P] + [P] * 5
+        L.orc_get_wall_history.argtypes = [P, ctypes.c_int, P]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+class Oracle:
+    """One system of the CPU restatement; mirrors the GPU handle's methods."""
+
+    def __init__(self, case):
+        L = lib()
+        c = OrcConfig()
+        c.boxlo[:] = case["boxlo"]
+        c.boxhi[:] = case["boxhi"]
+        c.periodic[:] = case["periodic"]
+        c.dt = case["dt"]
+        c.skin = case["skin"]
+        c.contact_distance_factor = case.get("cdf", 1.0)
+        c.neigh_every, c.neigh_delay, c.neigh_check = case.get("neigh", (1, 0, 1))
+        c.normal_model = case.get("normal_model", NORMAL_HERTZ)
+        c.rolling_model = case.get("rolling_model", ROLLING_OFF)
+        c.cohesion_model = case.get("cohesion_model", COHESION_OFF)
+        c.tangential_damping = 1
+        c.limit_force = 0
+        g = case.get("gravity")
+        c.gravity_on = 1 if g is not None else 0
+        c.gravity[:] = g if g is not None else (0.0, 0.0, 0.0)
+        self._keep = []
+        self.h = L.orc_create(ctypes.byref(c))
+        nt = int(case["ntypes"])
+        tabs = []
+        for k in ("Yeff", "Geff", "betaeff", "coeffFrict", "coeffRollFrict", "coeffRestLog"):
+            a = np.ascontiguousarray(case[k], dtype=np.float64).reshape(nt + 1, nt + 1)
+            tabs.append(a)
+        self._keep += tabs
+        L.orc_set_pair_params(self.h, nt, *[_p(a) for a in tabs], float(case.get("charVel", 0.0)))
+        for (axis, pos, wtype, roll) in case.get("planes", []):
+            L.orc_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll))
+        a = case["atoms"]
+        n = len(a["tag"])
+        arrs = [np.ascontiguousarray(a[k], dtype=t) for k, t in
+                (("tag", np.int32), ("type", np.int32), ("x", np.float64), ("v", np.float64),
+                 ("omega", np.float64), ("radius", np.float64), ("rmass", np.float64))]
+        L.orc_set_atoms(self.h, n, *[_p(x) for x in arrs])
+
+    def _check(self, rc):
+        if rc != 0:
+            raise RuntimeError(lib().orc_last_error(self.h).decode())
+
+    def setup(self):
+        self._check(lib().orc_setup(self.h))
+
+    def run(self, n):
+        self._check(lib().orc_run(self.h, int(n)))
+
+    @property
+    def nrebuilds(self):
+        return lib().orc_nrebuilds(self.h)
+
+    def atoms(self):
+        L = lib()
+        n = L.orc_natoms(self.h)
+        out = dict(tag=np.zeros(n, np.int32), type=np.zeros(n, np.int32),
+                   x=np.zeros((n, 3)), v=np.zeros((n, 3)), omega=np.zeros((n, 3)),
+                   f=np.zeros((n, 3)), torque=np.zeros((n, 3)), radius=np.zeros(n),
+                   rmass=np.zeros(n))
+        L.orc_get_atoms(self.h, *[_p(out[k]) for k in
+                                  ("tag", "type", "x", "v", "omega", "f", "torque", "radius", "rmass")])
+        return out
+
+    def pairs(self):
+        L = lib()
+        n = L.orc_npairs(self.h)
+        d = L.orc_dnum(self.h)
+        out = dict(tag_i=np.zeros(n, np.int32), tag_j=np.zeros(n, np.int32),
+                   shift=np.zeros((n, 3), np.int32), flag=np.zeros(n, np.int32),
+                   hist=np.zeros((n, d)))
+        L.orc_get_pairs(self.h, *[_p(out[k]) for k in ("tag_i", "tag_j", "shift", "flag", "hist")])
+        return out
+
+    def wall_history(self, w):
+        L = lib()
+        n = L.orc_natoms(self.h)
+        h = np.zeros((n, 3))
+        L.orc_get_wall_history(self.h, int(w), _p(h))
+        return h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None

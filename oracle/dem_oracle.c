@@ -1,0 +1,947 @@
+/* ORACLE — TEST INFRASTRUCTURE ONLY (see dem_oracle.h).
+ *
+ * Single-threaded C restatement of the LIGGGHTS-INL timestep for spheres:
+ *   Verlet::setup / Verlet::run          src/verlet.cpp:264-431
+ *   FixNVESphere initial/final_integrate src/fix_nve_sphere.cpp:134-244
+ *   Neighbor::decide / check_distance    src/neighbor.cpp:1362-1466
+ *   Domain::pbc, CommBrick::exchange     src/domain.cpp:550-650, src/comm_brick.cpp:732-808
+ *   ghost images x_j + pbc*prd           src/atom_vec_sphere.cpp:203-225
+ *   Neighbor::granular_bin_no_newton     src/neigh_gran.cpp:485-644
+ *   FixContactHistory::pre_exchange      src/fix_contact_history.cpp:305-425
+ *   Granular<CM>::compute_force          src/pair_gran_base.h:187-503
+ *   SurfaceModel<SURFACE_DEFAULT>        src/surface_model_default.h:146-211
+ *   NormalModel<HERTZ>                   src/normal_model_hertz.h:205-408
+ *   NormalModel<HOOKE>                   src/normal_model_hooke.h:230-400
+ *   TangentialModel<TANGENTIAL_HISTORY>  src/tangential_model_history.h:135-439
+ *   RollingModel<ROLLING_CDT>            src/rolling_model_cdt.h:89-167
+ *   FixGravity::post_force               src/fix_gravity.cpp:301-352
+ *   FixWallGran::post_force_primitive    src/fix_wall_gran.cpp:988-1119
+ *   Walls::Granular::compute_force       src/fix_wall_gran_base.h:159-372
+ *   PrimitiveWall plane contact/neighbour src/primitive_wall_definitions.h:123-150
+ * Every arithmetic expression keeps the reference's operand order, and the
+ * file must be compiled with -ffp-contract=off so that no FMA is formed
+ * (the reference is x86-64 SSE2 code without contraction).
+ *
+ * Not restated: the reference's bin geometry, so the ORDER of j inside one
+ * atom's neighbour list (and hence the summation order of forces) differs;
+ * the pair SET and every per-pair value are the reference's.
+ */
+#include "dem_oracle.h"
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define MAXTYPE_ERR "type out of range"
+#define CONTACT_NORMAL_MODEL (1 << 0)
+#define CONTACT_TANGENTIAL_MODEL (1 << 2)
+
+typedef struct {
+  int axis;
+  double pos;
+  int wall_type;
+  int rolling_model;
+  int *nlist;        /* PrimitiveWall neighbour list (atom indices) */
+  int nn, nncap;
+  double *hist;      /* 3 doubles per atom: shearx, sheary, shearz */
+} orc_plane;
+
+struct orc_sys {
+  orc_config cfg;
+  char err[256];
+  int ntypes;
+  double *Yeff, *Geff, *betaeff, *frict, *rollfrict, *restlog;
+  double charVel;
+
+  int n, nmax;
+  int *tag, *type;
+  double *x, *v, *omega, *f, *torque, *radius, *rmass, *xhold;
+  int *prow; /* row of this atom in the partner table */
+
+  /* half neighbour list, CSR by owner i */
+  int *nstart, *nj, *nshift, *nflag;
+  double *nhist;
+  int np, npcap;
+  int dnum;
+  int list_valid;
+
+  /* partner table (FixContactHistory npartner_/partner_/contacthistory_) */
+  int *pstart, *ptag;
+  double *phist;
+  int prows;
+
+  orc_plane planes[8];
+  int nplanes;
+
+  double cutneighmax;
+  long ntimestep, nrebuilds;
+  int ago;
+  int computeflag;   /* FixContactHistory computeflag_: a pair compute ran */
+};
+
+static void *xrealloc(void *p, size_t n) {
+  void *q = realloc(p, n ? n : 1);
+  if (!q) { fprintf(stderr, "oracle: out of memory\n"); abort(); }
+  return q;
+}
+
+orc_sys *orc_create(const orc_config *cfg) {
+  orc_sys *s = (orc_sys *)calloc(1, sizeof(orc_sys));
+  s->cfg = *cfg;
+  s->dnum = 3; /* shearx, sheary, shearz: src/tangential_model_history.h:79-81 */
+  return s;
+}
+
+void orc_destroy(orc_sys *s) {
+  if (!s) return;
+  free(s->Yeff); free(s->Geff); free(s->betaeff); free(s->frict); free(s->rollfrict);
+  free(s->restlog);
+  free(s->tag); free(s->type); free(s->x); free(s->v); free(s->omega); free(s->f);
+  free(s->torque); free(s->radius); free(s->rmass); free(s->xhold); free(s->prow);
+  free(s->nstart); free(s->nj); free(s->nshift); free(s->nflag); free(s->nhist);
+  free(s->pstart); free(s->ptag); free(s->phist);
+  for (int w = 0; w < s->nplanes; w++) { free(s->planes[w].nlist); free(s->planes[w].hist); }
+  free(s);
+}
+
+const char *orc_last_error(const orc_sys *s) { return s->err; }
+
+static double *dupm(const double *a, int nt) {
+  if (!a) return NULL;
+  size_t m = (size_t)(nt + 1) * (nt + 1);
+  double *b = (double *)xrealloc(NULL, m * sizeof(double));
+  memcpy(b, a, m * sizeof(double));
+  return b;
+}
+
+int orc_set_pair_params(orc_sys *s, int ntypes, const double *Yeff, const double *Geff,
+                        const double *betaeff, const double *coeffFrict,
+                        const double *coeffRollFrict, const double *coeffRestLog,
+                        double charVel) {
+  s->ntypes = ntypes;
+  s->Yeff = dupm(Yeff, ntypes);
+  s->Geff = dupm(Geff, ntypes);
+  s->betaeff = dupm(betaeff, ntypes);
+  s->frict = dupm(coeffFrict, ntypes);
+  s->rollfrict = dupm(coeffRollFrict, ntypes);
+  s->restlog = dupm(coeffRestLog, ntypes);
+  s->charVel = charVel;
+  return 0;
+}
+
+int orc_add_plane(orc_sys *s, int axis, double pos, int wall_type, int rolling_model) {
+  if (s->nplanes >= 8) { snprintf(s->err, sizeof s->err, "too many planes"); return -1; }
+  orc_plane *w = &s->planes[s->nplanes++];
+  memset(w, 0, sizeof *w);
+  w->axis = axis; w->pos = pos; w->wall_type = wall_type; w->rolling_model = rolling_model;
+  return 0;
+}
+
+static void grow_atoms(orc_sys *s, int n) {
+  if (n <= s->nmax) return;
+  s->nmax = n;
+  size_t n3 = 3 * (size_t)n * sizeof(double), n1 = (size_t)n * sizeof(double);
+  s->tag = (int *)xrealloc(s->tag, n * sizeof(int));
+  s->type = (int *)xrealloc(s->type, n * sizeof(int));
+  s->prow = (int *)xrealloc(s->prow, n * sizeof(int));
+  s->x = (double *)xrealloc(s->x, n3); s->v = (double *)xrealloc(s->v, n3);
+  s->omega = (double *)xrealloc(s->omega, n3); s->f = (double *)xrealloc(s->f, n3);
+  s->torque = (double *)xrealloc(s->torque, n3); s->xhold = (double *)xrealloc(s->xhold, n3);
+  s->radius = (double *)xrealloc(s->radius, n1); s->rmass = (double *)xrealloc(s->rmass, n1);
+  for (int w = 0; w < s->nplanes; w++) s->planes[w].hist = (double *)xrealloc(s->planes[w].hist, n3);
+}
+
+int orc_set_atoms(orc_sys *s, int n, const int *tag, const int *type, const double *x,
+                  const double *v, const double *omega, const double *radius,
+                  const double *rmass) {
+  grow_atoms(s, n);
+  s->n = n;
+  memcpy(s->tag, tag, n * sizeof(int));
+  memcpy(s->type, type, n * sizeof(int));
+  memcpy(s->x, x, 3 * (size_t)n * sizeof(double));
+  memcpy(s->v, v, 3 * (size_t)n * sizeof(double));
+  memcpy(s->omega, omega, 3 * (size_t)n * sizeof(double));
+  memcpy(s->radius, radius, (size_t)n * sizeof(double));
+  memcpy(s->rmass, rmass, (size_t)n * sizeof(double));
+  memset(s->f, 0, 3 * (size_t)n * sizeof(double));
+  memset(s->torque, 0, 3 * (size_t)n * sizeof(double));
+  for (int w = 0; w < s->nplanes; w++) memset(s->planes[w].hist, 0, 3 * (size_t)n * sizeof(double));
+  for (int i = 0; i < n; i++) s->prow[i] = -1;
+  s->list_valid = 0;
+  s->computeflag = 0;
+  s->prows = 0;
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Parameters                                                          */
+/* ------------------------------------------------------------------ */
+
+static inline double M(const orc_sys *s, const double *m, int i, int j) {
+  return m[(size_t)i * (s->ntypes + 1) + j];
+}
+
+/* cutneighmax = max over type pairs of (maxrad_i + maxrad_j)*cdf + skin,
+ * src/pair_gran.cpp:591-602, src/neighbor.cpp:316-337 */
+static void compute_cutneighmax(orc_sys *s) {
+  double maxrad = 0.0;
+  for (int i = 0; i < s->n; i++) if (s->radius[i] > maxrad) maxrad = s->radius[i];
+  double cutoff = (maxrad + maxrad) * s->cfg.contact_distance_factor;
+  double cutsq = cutoff * cutoff;
+  s->cutneighmax = sqrt(cutsq) + s->cfg.skin;
+}
+
+/* ------------------------------------------------------------------ */
+/* Domain::pbc + CommBrick::exchange (atom deletion in non-periodic dims) */
+/* ------------------------------------------------------------------ */
+
+static void copy_atom(orc_sys *s, int from, int to) {
+  s->tag[to] = s->tag[from]; s->type[to] = s->type[from]; s->prow[to] = s->prow[from];
+  for (int d = 0; d < 3; d++) {
+    s->x[3 * to + d] = s->x[3 * from + d]; s->v[3 * to + d] = s->v[3 * from + d];
+    s->omega[3 * to + d] = s->omega[3 * from + d]; s->f[3 * to + d] = s->f[3 * from + d];
+    s->torque[3 * to + d] = s->torque[3 * from + d];
+    for (int w = 0; w < s->nplanes; w++) s->planes[w].hist[3 * to + d] = s->planes[w].hist[3 * from + d];
+  }
+  s->radius[to] = s->radius[from]; s->rmass[to] = s->rmass[from];
+}
+
+static void pbc_and_exchange(orc_sys *s) {
+  const double *lo = s->cfg.boxlo, *hi = s->cfg.boxhi;
+  for (int i = 0; i < s->n; i++) {
+    for (int d = 0; d < 3; d++) {
+      if (!s->cfg.periodic[d]) continue;
+      double prd = hi[d] - lo[d];
+      double *xd = &s->x[3 * i + d];
+      if (*xd < lo[d]) *xd += prd;
+      if (*xd >= hi[d]) { *xd -= prd; if (*xd < lo[d]) *xd = lo[d]; }
+    }
+  }
+  for (int dim = 0; dim < 3; dim++) {
+    int i = 0;
+    while (i < s->n) {
+      double xd = s->x[3 * i + dim];
+      if (xd < lo[dim] || xd >= hi[dim]) { copy_atom(s, s->n - 1, i); s->n--; }
+      else i++;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* FixContactHistory::pre_exchange: neighbour list -> per-atom partners  */
+/* ------------------------------------------------------------------ */
+
+static void pre_exchange(orc_sys *s) {
+  const int n = s->n, dnum = s->dnum;
+  int *cnt = (int *)calloc(n + 1, sizeof(int));
+  if (s->list_valid) {
+    for (int i = 0; i < n; i++)
+      for (int p = s->nstart[i]; p < s->nstart[i + 1]; p++)
+        if (s->nflag[p]) {
+          cnt[i]++;
+          int sh = s->nshift[p];
+          if (sh == 0) cnt[s->nj[p]]++;  /* j < nlocal_neigh */
+        }
+  }
+  s->pstart = (int *)xrealloc(s->pstart, (n + 1) * sizeof(int));
+  s->pstart[0] = 0;
+  for (int i = 0; i < n; i++) s->pstart[i + 1] = s->pstart[i] + cnt[i];
+  int tot = s->pstart[n];
+  s->ptag = (int *)xrealloc(s->ptag, (tot + 1) * sizeof(int));
+  s->phist = (double *)xrealloc(s->phist, ((size_t)tot * dnum + 1) * sizeof(double));
+  memset(cnt, 0, (n + 1) * sizeof(int));
+  if (s->list_valid) {
+    for (int i = 0; i < n; i++)
+      for (int p = s->nstart[i]; p < s->nstart[i + 1]; p++)
+        if (s->nflag[p]) {
+          const double *hist = &s->nhist[(size_t)p * dnum];
+          int j = s->nj[p];
+          int m = s->pstart[i] + cnt[i]++;
+          s->ptag[m] = s->tag[j];
+          for (int d = 0; d < dnum; d++) s->phist[(size_t)m * dnum + d] = hist[d];
+          if (s->nshift[p] == 0) {
+            m = s->pstart[j] + cnt[j]++;
+            s->ptag[m] = s->tag[i];
+            /* every history value of tangential history has newtonflag 1 */
+            for (int d = 0; d < dnum; d++) s->phist[(size_t)m * dnum + d] = -hist[d];
+          }
+        }
+  }
+  for (int i = 0; i < n; i++) s->prow[i] = i;
+  s->prows = n;
+  free(cnt);
+  s->computeflag = 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Neighbour build                                                     */
+/* ------------------------------------------------------------------ */
+
+static inline int shift_code(int sx, int sy, int sz) { return (sx + 1) + 3 * (sy + 1) + 9 * (sz + 1) - 13; }
+static inline void shift_decode(int c, int *sx, int *sy, int *sz) {
+  c += 13; *sx = c % 3 - 1; *sy = (c / 3) % 3 - 1; *sz = c / 9 - 1;
+}
+
+typedef struct { int j, sh; } cand_t;
+static int cand_cmp(const void *a, const void *b) {
+  const cand_t *p = (const cand_t *)a, *q = (const cand_t *)b;
+  if (p->j != q->j) return p->j < q->j ? -1 : 1;
+  return (p->sh > q->sh) - (p->sh < q->sh);
+}
+
+/* ghost coordinate x_j + pbc*prd exactly as CommBrick::borders/forward_comm */
+static inline void image_x(const orc_sys *s, int j, int sh, double *xj) {
+  int sx, sy, sz; shift_decode(sh, &sx, &sy, &sz);
+  int sv[3] = {sx, sy, sz};
+  for (int d = 0; d < 3; d++) {
+    double dx = sv[d] * (s->cfg.boxhi[d] - s->cfg.boxlo[d]);
+    xj[d] = sv[d] ? s->x[3 * j + d] + dx : s->x[3 * j + d];
+  }
+}
+
+static int neighbor_build(orc_sys *s) {
+  const int n = s->n, dnum = s->dnum;
+  const double cdf = s->cfg.contact_distance_factor, skin = s->cfg.skin;
+  compute_cutneighmax(s);
+  int nc[3];
+  double csz[3];
+  for (int d = 0; d < 3; d++) {
+    double L = s->cfg.boxhi[d] - s->cfg.boxlo[d];
+    nc[d] = (int)floor(L / s->cutneighmax);
+    if (nc[d] < 1) nc[d] = 1;
+    if (s->cfg.periodic[d] && nc[d] < 3) {
+      snprintf(s->err, sizeof s->err, "periodic box dimension %d shorter than 3 neighbour cutoffs", d);
+      return -1;
+    }
+    if (nc[d] > 1024) nc[d] = 1024;
+    csz[d] = L / nc[d];
+  }
+  size_t ncell = (size_t)nc[0] * nc[1] * nc[2];
+  int *head = (int *)malloc(ncell * sizeof(int));
+  int *next = (int *)malloc((n + 1) * sizeof(int));
+  int *cell = (int *)malloc((n + 1) * sizeof(int));
+  for (size_t c = 0; c < ncell; c++) head[c] = -1;
+  for (int i = n - 1; i >= 0; i--) {
+    int ci[3];
+    for (int d = 0; d < 3; d++) {
+      int c = (int)((s->x[3 * i + d] - s->cfg.boxlo[d]) / csz[d]);
+      if (c < 0) c = 0;
+      if (c >= nc[d]) c = nc[d] - 1;
+      ci[d] = c;
+    }
+    int c = ci[0] + nc[0] * (ci[1] + nc[1] * ci[2]);
+    cell[i] = c;
+    next[i] = head[c];
+    head[c] = i;
+  }
+
+  /* new list */
+  int *nstart = (int *)malloc((n + 1) * sizeof(int));
+  int cap = s->npcap > 16 ? s->npcap : 16 * (n + 1);
+  int *nj = (int *)malloc(cap * sizeof(int));
+  int *nsh = (int *)malloc(cap * sizeof(int));
+  int *nfl = (int *)malloc(cap * sizeof(int));
+  double *nh = (double *)malloc((size_t)cap * dnum * sizeof(double));
+  int np = 0;
+  cand_t *cand = (cand_t *)malloc(4096 * sizeof(cand_t));
+  int candcap = 4096;
+
+  for (int i = 0; i < n; i++) {
+    nstart[i] = np;
+    const double xtmp = s->x[3 * i], ytmp = s->x[3 * i + 1], ztmp = s->x[3 * i + 2];
+    const double radi = s->radius[i];
+    int c = cell[i];
+    int ci[3] = {c % nc[0], (c / nc[0]) % nc[1], c / (nc[0] * nc[1])};
+    int nca = 0;
+    for (int oz = -1; oz <= 1; oz++)
+      for (int oy = -1; oy <= 1; oy++)
+        for (int ox = -1; ox <= 1; ox++) {
+          int o[3] = {ox, oy, oz}, cc[3], sv[3] = {0, 0, 0}, skip = 0;
+          for (int d = 0; d < 3; d++) {
+            cc[d] = ci[d] + o[d];
+            if (nc[d] == 1 && o[d] != 0) { skip = 1; break; }
+            if (cc[d] < 0) { if (!s->cfg.periodic[d]) { skip = 1; break; } cc[d] += nc[d]; sv[d] = -1; }
+            if (cc[d] >= nc[d]) { if (!s->cfg.periodic[d]) { skip = 1; break; } cc[d] -= nc[d]; sv[d] = 1; }
+          }
+          if (skip) continue;
+          int sh = shift_code(sv[0], sv[1], sv[2]);
+          for (int j = head[cc[0] + nc[0] * (cc[1] + nc[1] * cc[2])]; j >= 0; j = next[j]) {
+            if (sh == 0 && j <= i) continue;
+            double xj[3];
+            image_x(s, j, sh, xj);
+            const double delx = xtmp - xj[0];
+            const double dely = ytmp - xj[1];
+            const double delz = ztmp - xj[2];
+            const double rsq = delx * delx + dely * dely + delz * delz;
+            const double radsum = (radi + s->radius[j]) * cdf;
+            const double cutsq = (radsum + skin) * (radsum + skin);
+            if (rsq <= cutsq) {
+              if (nca == candcap) { candcap *= 2; cand = (cand_t *)xrealloc(cand, candcap * sizeof(cand_t)); }
+              cand[nca].j = j; cand[nca].sh = sh; nca++;
+            }
+          }
+        }
+    qsort(cand, nca, sizeof(cand_t), cand_cmp);
+    for (int k = 0; k < nca; k++) {
+      if (np == cap) {
+        cap *= 2;
+        nj = (int *)xrealloc(nj, cap * sizeof(int)); nsh = (int *)xrealloc(nsh, cap * sizeof(int));
+        nfl = (int *)xrealloc(nfl, cap * sizeof(int));
+        nh = (double *)xrealloc(nh, (size_t)cap * dnum * sizeof(double));
+      }
+      int j = cand[k].j, sh = cand[k].sh;
+      double xj[3];
+      image_x(s, j, sh, xj);
+      const double delx = xtmp - xj[0];
+      const double dely = ytmp - xj[1];
+      const double delz = ztmp - xj[2];
+      const double rsq = delx * delx + dely * dely + delz * delz;
+      const double radsum = (radi + s->radius[j]) * cdf;
+      nj[np] = j; nsh[np] = sh;
+      double *h = &nh[(size_t)np * dnum];
+      int found = -1;
+      if (rsq < radsum * radsum && s->prow[i] >= 0) {
+        int r = s->prow[i];
+        for (int m = s->pstart[r]; m < s->pstart[r + 1]; m++)
+          if (s->ptag[m] == s->tag[j]) { found = m; break; }
+      }
+      if (found >= 0) {
+        nfl[np] = 1;
+        for (int d = 0; d < dnum; d++) h[d] = s->phist[(size_t)found * dnum + d];
+      } else {
+        nfl[np] = 0;
+        for (int d = 0; d < dnum; d++) h[d] = 0.0;
+      }
+      np++;
+    }
+  }
+  nstart[n] = np;
+  free(cand); free(head); free(next); free(cell);
+  free(s->nstart); free(s->nj); free(s->nshift); free(s->nflag); free(s->nhist);
+  s->nstart = nstart; s->nj = nj; s->nshift = nsh; s->nflag = nfl; s->nhist = nh;
+  s->np = np; s->npcap = cap;
+  s->list_valid = 1;
+  memcpy(s->xhold, s->x, 3 * (size_t)n * sizeof(double));
+  s->ago = 0;
+  s->nrebuilds++;
+  /* partner rows are stale once the list owns the history */
+  for (int i = 0; i < n; i++) s->prow[i] = -1;
+  return 0;
+}
+
+/* PrimitiveWall::buildNeighList, src/primitive_wall.h:129-138, threshold = skin */
+static void plane_neighbors(orc_sys *s) {
+  for (int w = 0; w < s->nplanes; w++) {
+    orc_plane *pl = &s->planes[w];
+    if (pl->nncap < s->n) { pl->nncap = s->n; pl->nlist = (int *)xrealloc(pl->nlist, s->n * sizeof(int)); }
+    pl->nn = 0;
+    for (int i = 0; i < s->n; i++) {
+      double dMax = s->radius[i] + s->cfg.skin;
+      double dist = s->x[3 * i + pl->axis] - pl->pos;
+      double absdist = (dist > 0.0) ? dist : -dist;
+      if (absdist <= dMax) pl->nlist[pl->nn++] = i;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Contact law                                                         */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+  double dF[3], dT[3];
+} fdata;
+
+typedef struct {
+  int is_wall, itype, jtype, update_history;
+  double radi, radj, radsum, r, rinv, rsq, meff;
+  double en[3], delta[3];
+  const double *v_i, *v_j, *omega_i, *omega_j;
+  double vn, deltan, cri, crj, wr1, wr2, wr3, vtr1, vtr2, vtr3;
+  double Fn, kn, kt, gamman, gammat;
+  double *shear;
+  int *contact_flags;
+} sidata_t;
+
+static void surface_default(sidata_t *sd) {
+  const double enx = sd->en[0], eny = sd->en[1], enz = sd->en[2];
+  const double vr1 = sd->v_i[0] - sd->v_j[0];
+  const double vr2 = sd->v_i[1] - sd->v_j[1];
+  const double vr3 = sd->v_i[2] - sd->v_j[2];
+  const double vn = vr1 * enx + vr2 * eny + vr3 * enz;
+  const double vn1 = vn * enx, vn2 = vn * eny, vn3 = vn * enz;
+  const double vt1 = vr1 - vn1, vt2 = vr2 - vn2, vt3 = vr3 - vn3;
+  const double deltan = sd->radsum - sd->r;
+  const double dx = sd->delta[0], dy = sd->delta[1], dz = sd->delta[2];
+  const double rinv = sd->rinv;
+  double wr1, wr2, wr3;
+  if (sd->is_wall) {
+    const double cr = sd->radi - 0.5 * sd->deltan;
+    wr1 = cr * sd->omega_i[0] * rinv;
+    wr2 = cr * sd->omega_i[1] * rinv;
+    wr3 = cr * sd->omega_i[2] * rinv;
+    sd->cri = cr;
+  } else {
+    const double cri = sd->radi - 0.5 * deltan;
+    const double crj = sd->radj - 0.5 * deltan;
+    wr1 = (cri * sd->omega_i[0] + crj * sd->omega_j[0]) * rinv;
+    wr2 = (cri * sd->omega_i[1] + crj * sd->omega_j[1]) * rinv;
+    wr3 = (cri * sd->omega_i[2] + crj * sd->omega_j[2]) * rinv;
+    sd->cri = cri;
+    sd->crj = crj;
+  }
+  sd->vtr1 = vt1 - (dz * wr2 - dy * wr3);
+  sd->vtr2 = vt2 - (dx * wr3 - dz * wr1);
+  sd->vtr3 = vt3 - (dy * wr1 - dx * wr2);
+  sd->vn = vn;
+  sd->deltan = deltan;
+  sd->wr1 = wr1; sd->wr2 = wr2; sd->wr3 = wr3;
+}
+
+static void normal_hertz(const orc_sys *s, sidata_t *sd, fdata *fi, fdata *fj) {
+  if (sd->contact_flags) *sd->contact_flags |= CONTACT_NORMAL_MODEL;
+  const int it = sd->itype, jt = sd->jtype;
+  const double radi = sd->radi, radj = sd->radj;
+  double reff = sd->is_wall ? radi : (radi * radj / (radi + radj));
+  const double meff = sd->meff;
+  const double sqrtval = sqrt(reff * sd->deltan);
+  const double deltan = sd->deltan;
+  const double Y = M(s, s->Yeff, it, jt), G = M(s, s->Geff, it, jt), be = M(s, s->betaeff, it, jt);
+  const double Sn = 2. * Y * sqrtval;
+  const double St = 8. * G * sqrtval;
+  double kn = 4. / 3. * Y * sqrtval;
+  double kt = St;
+  const double sqrtFiveOverSix = 0.91287092917527685576161630466800355658790782499663875;
+  const double gamman = -2. * sqrtFiveOverSix * be * sqrt(Sn * meff);
+  const double gammat = s->cfg.tangential_damping ? -2. * sqrtFiveOverSix * be * sqrt(St * meff) : 0.0;
+  kn /= 1.0; /* force->nktv2p, 1 in SI */
+  kt /= 1.0;
+  const double Fn_damping = -gamman * sd->vn;
+  const double Fn_contact = kn * deltan;
+  double Fn = Fn_damping + Fn_contact;
+  if (s->cfg.limit_force && Fn < 0.0) Fn = 0.0;
+  sd->Fn = Fn; sd->kn = kn; sd->kt = kt; sd->gamman = gamman; sd->gammat = gammat;
+  if (sd->is_wall) {
+    const double Fn_ = Fn * 1.0; /* area_ratio */
+    fi->dF[0] += Fn_ * sd->en[0]; fi->dF[1] += Fn_ * sd->en[1]; fi->dF[2] += Fn_ * sd->en[2];
+  } else {
+    fi->dF[0] += sd->Fn * sd->en[0]; fi->dF[1] += sd->Fn * sd->en[1]; fi->dF[2] += sd->Fn * sd->en[2];
+    fj->dF[0] += -fi->dF[0]; fj->dF[1] += -fi->dF[1]; fj->dF[2] += -fi->dF[2];
+  }
+}
+
+static void normal_hooke(const orc_sys *s, sidata_t *sd, fdata *fi, fdata *fj) {
+  if (sd->contact_flags) *sd->contact_flags |= CONTACT_NORMAL_MODEL;
+  const int it = sd->itype, jt = sd->jtype;
+  const double radi = sd->radi, radj = sd->radj;
+  double reff = sd->is_wall ? radi : (radi * radj / (radi + radj));
+  const double meff = sd->meff;
+  const double sqrtval = sqrt(reff);
+  const double Y = M(s, s->Yeff, it, jt);
+  const double coeffRestLogChosen = M(s, s->restlog, it, jt);
+  const double charVel = s->charVel;
+  double kn = 16. / 15. * sqrtval * (Y) * pow(15. * meff * charVel * charVel / (16. * sqrtval * Y), 0.2);
+  double kt = kn;
+  const double coeffRestLogChosenSq = coeffRestLogChosen * coeffRestLogChosen;
+  const double gamman = sqrt(4. * meff * kn * coeffRestLogChosenSq / (coeffRestLogChosenSq + M_PI * M_PI));
+  const double gammat = s->cfg.tangential_damping ? gamman : 0.0;
+  kn /= 1.0;
+  kt /= 1.0;
+  const double Fn_damping = -gamman * sd->vn;
+  const double deltan = sd->deltan;
+  const double Fn_contact = kn * deltan;
+  double Fn = Fn_damping + Fn_contact;
+  if (s->cfg.limit_force && Fn < 0.0) Fn = 0.0;
+  sd->Fn = Fn; sd->kn = kn; sd->kt = kt; sd->gamman = gamman; sd->gammat = gammat;
+  if (sd->is_wall) {
+    const double Fn_ = Fn * 1.0;
+    fi->dF[0] += Fn_ * sd->en[0]; fi->dF[1] += Fn_ * sd->en[1]; fi->dF[2] += Fn_ * sd->en[2];
+  } else {
+    fi->dF[0] += sd->Fn * sd->en[0]; fi->dF[1] += sd->Fn * sd->en[1]; fi->dF[2] += sd->Fn * sd->en[2];
+    fj->dF[0] += -fi->dF[0]; fj->dF[1] += -fi->dF[1]; fj->dF[2] += -fi->dF[2];
+  }
+}
+
+static void tangential_history(const orc_sys *s, sidata_t *sd, fdata *fi, fdata *fj) {
+  const double enx = sd->en[0], eny = sd->en[1], enz = sd->en[2];
+  if (sd->contact_flags) *sd->contact_flags |= CONTACT_TANGENTIAL_MODEL;
+  double *const shear = sd->shear;
+  if (sd->update_history) {
+    const double dt = s->cfg.dt;
+    shear[0] += sd->vtr1 * dt;
+    shear[1] += sd->vtr2 * dt;
+    shear[2] += sd->vtr3 * dt;
+    double rsht = shear[0] * enx + shear[1] * eny + shear[2] * enz;
+    shear[0] -= rsht * enx;
+    shear[1] -= rsht * eny;
+    shear[2] -= rsht * enz;
+  }
+  const double shrmag = sqrt(shear[0] * shear[0] + shear[1] * shear[1] + shear[2] * shear[2]);
+  const double kt = sd->kt;
+  const double xmu = M(s, s->frict, sd->itype, sd->jtype);
+  double Ft1 = -(kt * shear[0]);
+  double Ft2 = -(kt * shear[1]);
+  double Ft3 = -(kt * shear[2]);
+  const double Ft_shear = kt * shrmag;
+  const double Ft_friction = xmu * fabs(sd->Fn);
+  if (Ft_shear > Ft_friction) {
+    if (shrmag != 0.0) {
+      const double ratio = Ft_friction / Ft_shear;
+      Ft1 *= ratio; Ft2 *= ratio; Ft3 *= ratio;
+      if (sd->update_history) {
+        shear[0] = -Ft1 / kt;
+        shear[1] = -Ft2 / kt;
+        shear[2] = -Ft3 / kt;
+      }
+    } else
+      Ft1 = Ft2 = Ft3 = 0.0;
+  } else {
+    const double gammat = sd->gammat;
+    Ft1 -= (gammat * sd->vtr1);
+    Ft2 -= (gammat * sd->vtr2);
+    Ft3 -= (gammat * sd->vtr3);
+  }
+  const double Tn_shear = 0.;
+  const double tor1 = eny * Ft3 - enz * Ft2;
+  const double tor2 = enz * Ft1 - enx * Ft3;
+  const double tor3 = enx * Ft2 - eny * Ft1;
+  double torque_i[3], torque_j[3] = {0., 0., 0.};
+  torque_i[0] = -sd->cri * tor1 + Tn_shear * enx;
+  torque_i[1] = -sd->cri * tor2 + Tn_shear * eny;
+  torque_i[2] = -sd->cri * tor3 + Tn_shear * enz;
+  if (!sd->is_wall) {
+    torque_j[0] = -sd->crj * tor1 - Tn_shear * enx;
+    torque_j[1] = -sd->crj * tor2 - Tn_shear * eny;
+    torque_j[2] = -sd->crj * tor3 - Tn_shear * enz;
+  }
+  if (sd->is_wall) {
+    const double area_ratio = 1.0;
+    fi->dF[0] += Ft1 * area_ratio; fi->dF[1] += Ft2 * area_ratio; fi->dF[2] += Ft3 * area_ratio;
+    fi->dT[0] += torque_i[0] * area_ratio; fi->dT[1] += torque_i[1] * area_ratio;
+    fi->dT[2] += torque_i[2] * area_ratio;
+  } else {
+    fi->dF[0] += Ft1; fi->dF[1] += Ft2; fi->dF[2] += Ft3;
+    fj->dF[0] += -Ft1; fj->dF[1] += -Ft2; fj->dF[2] += -Ft3;
+    fi->dT[0] += torque_i[0]; fi->dT[1] += torque_i[1]; fi->dT[2] += torque_i[2];
+    fj->dT[0] += torque_j[0]; fj->dT[1] += torque_j[1]; fj->dT[2] += torque_j[2];
+  }
+}
+
+static void rolling_cdt(const orc_sys *s, sidata_t *sd, fdata *fi, fdata *fj) {
+  const double rmu = M(s, s->rollfrict, sd->itype, sd->jtype);
+  double r_torque[3] = {0., 0., 0.}, wr_roll[3];
+  const double radi = sd->radi, radj = sd->radj;
+  double reff = sd->is_wall ? radi : (radi * radj / (radi + radj));
+  if (sd->is_wall) {
+    const double wr1 = sd->wr1, wr2 = sd->wr2, wr3 = sd->wr3;
+    const double wrmag = sqrt(wr1 * wr1 + wr2 * wr2 + wr3 * wr3);
+    if (wrmag > 0.) {
+      const double kn = sd->kn;
+      const double enx = sd->en[0], eny = sd->en[1], enz = sd->en[2];
+      const double Fn = sd->deltan * kn;
+      r_torque[0] = rmu * Fn * wr1 / wrmag * reff;
+      r_torque[1] = rmu * Fn * wr2 / wrmag * reff;
+      r_torque[2] = rmu * Fn * wr3 / wrmag * reff;
+      double rtd = r_torque[0] * enx + r_torque[1] * eny + r_torque[2] * enz;
+      double rn[3] = {enx * rtd, eny * rtd, enz * rtd};
+      r_torque[0] = r_torque[0] - rn[0];
+      r_torque[1] = r_torque[1] - rn[1];
+      r_torque[2] = r_torque[2] - rn[2];
+    }
+  } else {
+    wr_roll[0] = sd->omega_i[0] - sd->omega_j[0];
+    wr_roll[1] = sd->omega_i[1] - sd->omega_j[1];
+    wr_roll[2] = sd->omega_i[2] - sd->omega_j[2];
+    const double wr_rollmag = sqrt(wr_roll[0] * wr_roll[0] + wr_roll[1] * wr_roll[1] + wr_roll[2] * wr_roll[2]);
+    if (wr_rollmag > 0.) {
+      const double enx = sd->en[0], eny = sd->en[1], enz = sd->en[2];
+      const double fac = rmu * sd->kn * sd->deltan * reff / wr_rollmag;
+      r_torque[0] = fac * wr_roll[0];
+      r_torque[1] = fac * wr_roll[1];
+      r_torque[2] = fac * wr_roll[2];
+      const double rtd = r_torque[0] * enx + r_torque[1] * eny + r_torque[2] * enz;
+      double rn[3] = {enx * rtd, eny * rtd, enz * rtd};
+      r_torque[0] = r_torque[0] - rn[0];
+      r_torque[1] = r_torque[1] - rn[1];
+      r_torque[2] = r_torque[2] - rn[2];
+    }
+  }
+  fi->dT[0] -= r_torque[0]; fi->dT[1] -= r_torque[1]; fi->dT[2] -= r_torque[2];
+  fj->dT[0] += r_torque[0]; fj->dT[1] += r_torque[1]; fj->dT[2] += r_torque[2];
+}
+
+static void surfaces_intersect(const orc_sys *s, sidata_t *sd, fdata *fi, fdata *fj, int rolling) {
+  surface_default(sd);
+  if (s->cfg.normal_model == ORC_NORMAL_HOOKE) normal_hooke(s, sd, fi, fj);
+  else normal_hertz(s, sd, fi, fj);
+  tangential_history(s, sd, fi, fj);
+  if (rolling == ORC_ROLLING_CDT) rolling_cdt(s, sd, fi, fj);
+}
+
+/* TangentialModel<TANGENTIAL_HISTORY>::surfacesClose */
+static void surfaces_close(sidata_t *sd) {
+  if (sd->contact_flags) *sd->contact_flags &= ~CONTACT_TANGENTIAL_MODEL;
+  if (!sd->shear) return;
+  sd->shear[0] = 0.0; sd->shear[1] = 0.0; sd->shear[2] = 0.0;
+}
+
+/* Granular<CM>::compute_force, half list, newton off */
+static void pair_compute(orc_sys *s, int shearupdate) {
+  const double cdm = s->cfg.contact_distance_factor * s->cfg.contact_distance_factor;
+  for (int i = 0; i < s->n; i++) {
+    const double xtmp = s->x[3 * i], ytmp = s->x[3 * i + 1], ztmp = s->x[3 * i + 2];
+    const double radi = s->radius[i];
+    for (int p = s->nstart[i]; p < s->nstart[i + 1]; p++) {
+      const int j = s->nj[p], sh = s->nshift[p];
+      double xj[3];
+      image_x(s, j, sh, xj);
+      const double delx = xtmp - xj[0];
+      const double dely = ytmp - xj[1];
+      const double delz = ztmp - xj[2];
+      const double rsq = delx * delx + dely * dely + delz * delz;
+      const double radj = s->radius[j];
+      const double radsum = radi + radj;
+      sidata_t sd;
+      memset(&sd, 0, sizeof sd);
+      sd.is_wall = 0;
+      sd.update_history = shearupdate;
+      sd.radi = radi; sd.radj = radj; sd.radsum = radsum; sd.rsq = rsq;
+      sd.delta[0] = delx; sd.delta[1] = dely; sd.delta[2] = delz;
+      sd.contact_flags = &s->nflag[p];
+      sd.shear = &s->nhist[(size_t)p * s->dnum];
+      sd.v_i = &s->v[3 * i]; sd.v_j = &s->v[3 * j];
+      sd.omega_i = &s->omega[3 * i]; sd.omega_j = &s->omega[3 * j];
+      sd.itype = s->type[i]; sd.jtype = s->type[j];
+      fdata fi, fj;
+      memset(&fi, 0, sizeof fi); memset(&fj, 0, sizeof fj);
+      int has_force = 0;
+      if (rsq < radsum * radsum) {
+        const double r = sqrt(rsq);
+        const double rinv = 1.0 / r;
+        const double mi = s->rmass[i], mj = s->rmass[j];
+        const double meff = mi * mj / (mi + mj);
+        sd.r = r; sd.rinv = rinv; sd.meff = meff;
+        sd.en[0] = delx * rinv; sd.en[1] = dely * rinv; sd.en[2] = delz * rinv;
+        surfaces_intersect(s, &sd, &fi, &fj, s->cfg.rolling_model);
+        has_force = 1;
+      } else if (rsq < cdm * radsum * radsum) {
+        surfaces_close(&sd);
+      }
+      if (has_force) {
+        for (int d = 0; d < 3; d++) {
+          s->f[3 * i + d] += 1.0 * fi.dF[d];
+          s->torque[3 * i + d] += 1.0 * fi.dT[d];
+        }
+        if (sh == 0) {
+          for (int d = 0; d < 3; d++) {
+            s->f[3 * j + d] += 1.0 * fj.dF[d];
+            s->torque[3 * j + d] += 1.0 * fj.dT[d];
+          }
+        }
+      }
+    }
+  }
+  s->computeflag = 1;
+}
+
+static void gravity_post_force(orc_sys *s) {
+  if (!s->cfg.gravity_on) return;
+  for (int i = 0; i < s->n; i++) {
+    const double massone = s->rmass[i] * 1.;
+    s->f[3 * i] += massone * s->cfg.gravity[0];
+    s->f[3 * i + 1] += massone * s->cfg.gravity[1];
+    s->f[3 * i + 2] += massone * s->cfg.gravity[2];
+  }
+}
+
+static void plane_post_force(orc_sys *s, orc_plane *pl, int shearupdate) {
+  const double cdm1 = s->cfg.contact_distance_factor - 1.0;
+  const double vwall[3] = {0., 0., 0.};
+  for (int k = 0; k < pl->nn; k++) {
+    const int ip = pl->nlist[k];
+    sidata_t sd;
+    memset(&sd, 0, sizeof sd);
+    sd.is_wall = 1;
+    sd.radi = s->radius[ip];
+    /* Plane<dim>::resolveContact */
+    double delta[3];
+    double deltan;
+    const double *pos = &s->x[3 * ip];
+    const int ax = pl->axis, ay = (ax + 1) % 3, az = (ax + 2) % 3;
+    if (pos[ax] > pl->pos) {
+      delta[ax] = pl->pos - pos[ax]; delta[ay] = 0.; delta[az] = 0.;
+      deltan = pos[ax] - pl->pos - sd.radi;
+    } else {
+      delta[ax] = pl->pos - pos[ax]; delta[ay] = 0.; delta[az] = 0.;
+      deltan = pl->pos - pos[ax] - sd.radi;
+    }
+    if (deltan > s->cutneighmax) continue;
+    double *hist = &pl->hist[3 * ip];
+    if (deltan <= 0 || deltan < cdm1 * s->radius[ip]) {
+      const int intersectflag = (deltan <= 0);
+      sd.deltan = -deltan;
+      sd.delta[0] = -delta[0]; sd.delta[1] = -delta[1]; sd.delta[2] = -delta[2];
+      sd.shear = hist;
+      /* Walls::Granular::compute_force */
+      sd.v_i = &s->v[3 * ip]; sd.v_j = vwall; sd.omega_i = &s->omega[3 * ip];
+      sd.r = sd.radi - sd.deltan;
+      sd.rsq = sd.r * sd.r;
+      const double rinv = 1.0 / sd.r;
+      sd.rinv = rinv;
+      sd.contact_flags = NULL;
+      sd.itype = s->type[ip];
+      sd.meff = s->rmass[ip];
+      sd.update_history = shearupdate;
+      sd.jtype = pl->wall_type;
+      sd.en[0] = sd.delta[0] * rinv; sd.en[1] = sd.delta[1] * rinv; sd.en[2] = sd.delta[2] * rinv;
+      sd.radsum = sd.radi;
+      fdata fi, fj;
+      memset(&fi, 0, sizeof fi); memset(&fj, 0, sizeof fj);
+      if (intersectflag) {
+        surfaces_intersect(s, &sd, &fi, &fj, pl->rolling_model);
+        for (int d = 0; d < 3; d++) {
+          s->f[3 * ip + d] += fi.dF[d];
+          s->torque[3 * ip + d] += fi.dT[d];
+        }
+      } else {
+        surfaces_close(&sd);
+      }
+    } else {
+      hist[0] = 0.; hist[1] = 0.; hist[2] = 0.;
+    }
+  }
+}
+
+static void force_clear(orc_sys *s) {
+  memset(s->f, 0, 3 * (size_t)s->n * sizeof(double));
+  memset(s->torque, 0, 3 * (size_t)s->n * sizeof(double));
+}
+
+static void initial_integrate(orc_sys *s) {
+  const double dtf = 0.5 * s->cfg.dt * 1.0; /* force->ftm2v = 1 in SI */
+  const double dtv = s->cfg.dt;
+  const double dtfrotate = dtf / 0.4;
+  for (int i = 0; i < s->n; i++) {
+    const double dtfm = dtf / (s->rmass[i] * (1. + 0.0));
+    double *v = &s->v[3 * i], *x = &s->x[3 * i], *w = &s->omega[3 * i];
+    const double *f = &s->f[3 * i], *t = &s->torque[3 * i];
+    v[0] += dtfm * f[0]; v[1] += dtfm * f[1]; v[2] += dtfm * f[2];
+    x[0] += dtv * v[0]; x[1] += dtv * v[1]; x[2] += dtv * v[2];
+    const double dtirotate = dtfrotate / (s->radius[i] * s->radius[i] * s->rmass[i]);
+    w[0] += dtirotate * t[0]; w[1] += dtirotate * t[1]; w[2] += dtirotate * t[2];
+  }
+}
+
+static void final_integrate(orc_sys *s) {
+  const double dtf = 0.5 * s->cfg.dt * 1.0;
+  const double dtfrotate = dtf / 0.4;
+  for (int i = 0; i < s->n; i++) {
+    const double dtfm = dtf / (s->rmass[i] * (1. + 0.0));
+    double *v = &s->v[3 * i], *w = &s->omega[3 * i];
+    const double *f = &s->f[3 * i], *t = &s->torque[3 * i];
+    v[0] += dtfm * f[0]; v[1] += dtfm * f[1]; v[2] += dtfm * f[2];
+    const double dtirotate = dtfrotate / (s->radius[i] * s->radius[i] * s->rmass[i]);
+    w[0] += dtirotate * t[0]; w[1] += dtirotate * t[1]; w[2] += dtirotate * t[2];
+  }
+}
+
+static int check_distance(orc_sys *s) {
+  const double skin = s->cfg.skin;
+  const double deltasq = 0.25 * skin * skin;
+  int flag = 0;
+  for (int i = 0; i < s->n; i++) {
+    const double delx = s->x[3 * i] - s->xhold[3 * i];
+    const double dely = s->x[3 * i + 1] - s->xhold[3 * i + 1];
+    const double delz = s->x[3 * i + 2] - s->xhold[3 * i + 2];
+    const double rsq = delx * delx + dely * dely + delz * delz;
+    if (rsq > deltasq) flag = 1;
+  }
+  return flag;
+}
+
+static int decide(orc_sys *s) {
+  s->ago++;
+  if (s->ago >= s->cfg.neigh_delay && s->ago % s->cfg.neigh_every == 0) {
+    if (s->cfg.neigh_check == 0) return 1;
+    return check_distance(s);
+  }
+  return 0;
+}
+
+static int rebuild(orc_sys *s) {
+  if (s->computeflag) pre_exchange(s);
+  pbc_and_exchange(s);
+  if (neighbor_build(s)) return -1;
+  plane_neighbors(s);
+  return 0;
+}
+
+static void compute_forces(orc_sys *s, int shearupdate) {
+  force_clear(s);
+  pair_compute(s, shearupdate);
+  gravity_post_force(s);
+  for (int w = 0; w < s->nplanes; w++) plane_post_force(s, &s->planes[w], shearupdate);
+}
+
+int orc_setup(orc_sys *s) {
+  if (!s->Yeff) { snprintf(s->err, sizeof s->err, "pair parameters not set"); return -1; }
+  if (rebuild(s)) return -1;
+  compute_forces(s, 0);
+  return 0;
+}
+
+int orc_run(orc_sys *s, int nsteps) {
+  for (int k = 0; k < nsteps; k++) {
+    s->ntimestep++;
+    initial_integrate(s);
+    if (decide(s)) {
+      if (rebuild(s)) return -1;
+    }
+    compute_forces(s, 1);
+    final_integrate(s);
+  }
+  return 0;
+}
+
+int orc_natoms(const orc_sys *s) { return s->n; }
+int orc_npairs(const orc_sys *s) { return s->list_valid ? s->np : 0; }
+int orc_dnum(const orc_sys *s) { return s->dnum; }
+long orc_nrebuilds(const orc_sys *s) { return s->nrebuilds; }
+long orc_ntimestep(const orc_sys *s) { return s->ntimestep; }
+
+int orc_get_atoms(const orc_sys *s, int *tag, int *type, double *x, double *v, double *omega,
+                  double *f, double *torque, double *radius, double *rmass) {
+  const int n = s->n;
+  size_t n3 = 3 * (size_t)n * sizeof(double);
+  if (tag) memcpy(tag, s->tag, n * sizeof(int));
+  if (type) memcpy(type, s->type, n * sizeof(int));
+  if (x) memcpy(x, s->x, n3);
+  if (v) memcpy(v, s->v, n3);
+  if (omega) memcpy(omega, s->omega, n3);
+  if (f) memcpy(f, s->f, n3);
+  if (torque) memcpy(torque, s->torque, n3);
+  if (radius) memcpy(radius, s->radius, n * sizeof(double));
+  if (rmass) memcpy(rmass, s->rmass, n * sizeof(double));
+  return n;
+}
+
+int orc_get_pairs(const orc_sys *s, int *tag_i, int *tag_j, int *shift, int *flag, double *hist) {
+  if (!s->list_valid) return 0;
+  for (int i = 0; i < s->n; i++)
+    for (int p = s->nstart[i]; p < s->nstart[i + 1]; p++) {
+      int sx, sy, sz;
+      shift_decode(s->nshift[p], &sx, &sy, &sz);
+      if (tag_i) tag_i[p] = s->tag[i];
+      if (tag_j) tag_j[p] = s->tag[s->nj[p]];
+      if (shift) { shift[3 * p] = sx; shift[3 * p + 1] = sy; shift[3 * p + 2] = sz; }
+      if (flag) flag[p] = s->nflag[p];
+      if (hist) for (int d = 0; d < s->dnum; d++) hist[(size_t)p * s->dnum + d] = s->nhist[(size_t)p * s->dnum + d];
+    }
+  return s->np;
+}
+
+int orc_get_wall_history(const orc_sys *s, int wall, double *hist) {
+  if (wall < 0 || wall >= s->nplanes) return -1;
+  memcpy(hist, s->planes[wall].hist, 3 * (size_t)s->n * sizeof(double));
+  return s->n;
+}

@@ -1,0 +1,81 @@
+/* ORACLE — TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C, single-threaded restatement of LIGGGHTS-INL's per-timestep DEM
+ * path for spheres.  It exists to check the GPU product: only tests/, the
+ * smoke check and the CPU-baseline leg of bench.py may load it.  The product
+ * never links or calls it.
+ *
+ * Parity pin: tests/golden/ holds snapshots of the reference binary itself
+ * (built from the reference sources by oracle/ref/Makefile) on seeded inputs;
+ * tests/test_oracle_golden.py checks this restatement against them.
+ *
+ * Arrays follow the reference's per-atom layout: x[3*i+d] is atom->x[i][d].
+ * Per-type-pair matrices are (ntypes+1)*(ntypes+1), row-major, index [i][j]
+ * with types starting at 1, as MatrixProperty in src/global_properties.cpp.
+ */
+#ifndef DEM_ORACLE_H
+#define DEM_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_NORMAL_HERTZ = 0, ORC_NORMAL_HOOKE = 1 };
+enum { ORC_ROLLING_OFF = 0, ORC_ROLLING_CDT = 1 };
+enum { ORC_COHESION_OFF = 0, ORC_COHESION_BOND_NONLINEAR = 1 };
+
+typedef struct orc_config {
+  double boxlo[3], boxhi[3];
+  int periodic[3];
+  double dt;
+  double skin;                 /* neighbor SKIN bin */
+  double contact_distance_factor; /* neigh_modify contact_distance_factor */
+  int neigh_every, neigh_delay, neigh_check; /* neigh_modify every/delay/check */
+  int normal_model;            /* ORC_NORMAL_* */
+  int rolling_model;           /* ORC_ROLLING_* */
+  int cohesion_model;          /* ORC_COHESION_* */
+  int tangential_damping;      /* model option, default 1 */
+  int limit_force;             /* model option limitForce, default 0 */
+  int gravity_on;
+  double gravity[3];           /* xacc, yacc, zacc of fix gravity */
+} orc_config;
+
+typedef struct orc_sys orc_sys;
+
+orc_sys *orc_create(const orc_config *cfg);
+void orc_destroy(orc_sys *s);
+
+/* Per-type-pair tables, (ntypes+1)^2 each.  coeffRestLog and charVel are only
+ * read by the Hooke law, coeffRollFrict only with CDT rolling. */
+int orc_set_pair_params(orc_sys *s, int ntypes, const double *Yeff, const double *Geff,
+                        const double *betaeff, const double *coeffFrict,
+                        const double *coeffRollFrict, const double *coeffRestLog,
+                        double charVel);
+
+/* fix wall/gran ... primitive type WTYPE {x,y,z}plane POS (axis 0/1/2). */
+int orc_add_plane(orc_sys *s, int axis, double pos, int wall_type, int rolling_model);
+
+int orc_set_atoms(orc_sys *s, int n, const int *tag, const int *type, const double *x,
+                  const double *v, const double *omega, const double *radius,
+                  const double *rmass);
+
+int orc_setup(orc_sys *s);            /* Verlet::setup */
+int orc_run(orc_sys *s, int nsteps);  /* nsteps iterations of Verlet::run */
+
+int orc_natoms(const orc_sys *s);
+int orc_get_atoms(const orc_sys *s, int *tag, int *type, double *x, double *v, double *omega,
+                  double *f, double *torque, double *radius, double *rmass);
+int orc_npairs(const orc_sys *s);
+int orc_dnum(const orc_sys *s);
+/* shift[3*p+d] is the periodic image of j: j's coordinate is x_j + shift*L. */
+int orc_get_pairs(const orc_sys *s, int *tag_i, int *tag_j, int *shift, int *flag,
+                  double *hist);
+int orc_get_wall_history(const orc_sys *s, int wall, double *hist);
+long orc_nrebuilds(const orc_sys *s);
+long orc_ntimestep(const orc_sys *s);
+const char *orc_last_error(const orc_sys *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,181 @@
+"""Generate the golden fixtures in this folder from the reference itself.
+
+Runs the LIGGGHTS-INL binary that oracle/ref/Makefile builds from the
+reference sources (oracle/_ref/lmp_ref) on seeded synthetic inputs, with the
+snapshot fix of oracle/ref registered, and stores tag-sorted per-atom state,
+the granular half neighbour list (pair set, contact flags, shear history) and
+the primitive-wall histories at selected steps as compressed .npz files.
+
+This runs only where the reference sources are present (not on the GPU
+machine); the .npz files it writes are committed and travel instead.
+
+    python tests/golden/make_golden.py            # all cases
+    python tests/golden/make_golden.py dense_hertz
+"""
+import json
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "liggghts-inl_gb300", "python"))
+from gb300dem import workloads  # noqa: E402
+
+LMP = os.path.join(ROOT, "oracle", "_ref", "lmp_ref")
+
+
+def cases():
+    c = {}
+    c["dense_hertz"] = (workloads.lattice_case(
+        seed=11, nx=8, ny=8, nz=5, spacing=1.96e-3, radius=(1e-3, 1e-3), z0=0.99e-3,
+        jitter=2e-5, vmax=2.0, wmax=100.0), 500, [0, 1, 2, 10, 50, 100, 200, 300, 500])
+    c["poly_cdt"] = (workloads.lattice_case(
+        seed=23, nx=7, ny=7, nz=5, spacing=2.1e-3, radius=(0.8e-3, 1.2e-3), z0=1.0e-3,
+        jitter=3e-5, vmax=2.0, wmax=200.0, ntypes=2, E=(5e6, 1e7), nu=(0.45, 0.3),
+        rest=((0.9, 0.7), (0.7, 0.5)), frict=((0.5, 0.4), (0.4, 0.6)),
+        rollfrict=((0.3, 0.2), (0.2, 0.1)), rolling_model=1, density=1500.0),
+        400, [0, 1, 2, 10, 50, 100, 200, 400])
+    c["hooke"] = (workloads.lattice_case(
+        seed=5, nx=6, ny=6, nz=4, spacing=1.97e-3, radius=(1e-3, 1e-3), z0=0.995e-3,
+        jitter=2e-5, vmax=1.5, wmax=80.0, normal_model=1, charVel=0.5),
+        300, [0, 1, 10, 100, 300])
+    return c
+
+
+def fmt(v):
+    return "%.17g" % v
+
+
+def write_inputs(case, d, nsteps, snaps):
+    a = case["atoms"]
+    n = len(a["tag"])
+    mat = case["material"]
+    nt = case["ntypes"]
+    lines = ["LIGGGHTS data file (seeded synthetic)", "", "%d atoms" % n, "%d atom types" % nt, ""]
+    for k, ax in enumerate("xyz"):
+        lines.append("%s %s %slo %shi" % (fmt(case["boxlo"][k]), fmt(case["boxhi"][k]), ax, ax))
+    lines += ["", "Atoms", ""]
+    for i in range(n):
+        lines.append("%d %d %s %s %s %s %s" % (a["tag"][i], a["type"][i], fmt(2 * a["radius"][i]),
+                                               fmt(mat["density"]), fmt(a["x"][i, 0]),
+                                               fmt(a["x"][i, 1]), fmt(a["x"][i, 2])))
+    lines += ["", "Velocities", ""]
+    for i in range(n):
+        lines.append("%d %s" % (a["tag"][i], " ".join(fmt(t) for t in
+                                                       list(a["v"][i]) + list(a["omega"][i]))))
+    open(os.path.join(d, "data.case"), "w").write("\n".join(lines) + "\n")
+
+    bnd = " ".join("p" if p else "f" for p in case["periodic"])
+    model = "model %s tangential history" % ("hooke" if case["normal_model"] == 1 else "hertz")
+    if case["rolling_model"] == 1:
+        model += " rolling_friction cdt"
+    tpl = lambda m: " ".join(fmt(m[i][j]) for i in range(nt) for j in range(nt))  # noqa: E731
+    s = ["atom_style granular", "atom_modify map array sort 0 0", "boundary %s" % bnd,
+         "newton off", "communicate single vel yes", "units si",
+         "read_data data.case", "neighbor %s bin" % fmt(case["skin"]), "neigh_modify delay 0",
+         "fix m1 all property/global youngsModulus peratomtype %s" % " ".join(fmt(e) for e in mat["E"]),
+         "fix m2 all property/global poissonsRatio peratomtype %s" % " ".join(fmt(e) for e in mat["nu"]),
+         "fix m3 all property/global coefficientRestitution peratomtypepair %d %s" % (nt, tpl(mat["rest"])),
+         "fix m4 all property/global coefficientFriction peratomtypepair %d %s" % (nt, tpl(mat["frict"]))]
+    if case["rolling_model"] == 1:
+        s.append("fix m5 all property/global coefficientRollingFriction peratomtypepair %d %s"
+                 % (nt, tpl(mat["rollfrict"])))
+    if case["normal_model"] == 1:
+        s.append("fix m6 all property/global characteristicVelocity scalar %s" % fmt(case["charVel"]))
+    s += ["pair_style gran %s" % model, "pair_coeff * *", "timestep %s" % fmt(case["dt"])]
+    g = case["gravity"]
+    s.append("fix gravi all gravity 9.81 vector 0.0 0.0 -1.0")
+    assert tuple(g) == (0.0, 0.0, -9.81)
+    for k, (axis, pos, wtype, roll) in enumerate(case["planes"]):
+        wm = "model %s tangential history" % ("hooke" if case["normal_model"] == 1 else "hertz")
+        if roll == 1:
+            wm += " rolling_friction cdt"
+        s.append("fix wall%d all wall/gran %s primitive type %d %splane %s"
+                 % (k, wm, wtype, "xyz"[axis], fmt(pos)))
+    s += ["fix integr all nve/sphere",
+          "fix snap all oracle/snapshot snap %s" % " ".join(str(t) for t in snaps),
+          "thermo 100", "run %d" % nsteps]
+    open(os.path.join(d, "in.case"), "w").write("\n".join(s) + "\n")
+
+
+def read_snapshot(path):
+    b = open(path, "rb").read()
+    assert b[:8] == b"DEMSNAP1"
+    off = 8
+    def take(dt, cnt):
+        nonlocal off
+        a = np.frombuffer(b, dtype=dt, count=cnt, offset=off)
+        off += a.nbytes
+        return a
+    step = int(take(np.int64, 1)[0])
+    nlocal, nghost, dnum, nwall = [int(t) for t in take(np.int32, 4)]
+    boxlo, boxhi = take(np.float64, 3), take(np.float64, 3)
+    per = take(np.int32, 4)[:3]
+    nall = nlocal + nghost
+    tag, typ = take(np.int32, nall), take(np.int32, nall)
+    vec = {k: take(np.float64, 3 * nall).reshape(nall, 3) for k in ("x", "v", "omega", "f", "torque")}
+    radius, rmass = take(np.float64, nall), take(np.float64, nall)
+    np_ = int(take(np.int32, 1)[0])
+    pi, pj, pf = take(np.int32, np_), take(np.int32, np_), take(np.int32, np_)
+    ph = take(np.float64, np_ * dnum).reshape(np_, dnum)
+    walls = {}
+    for _ in range(nwall):
+        ln = int(take(np.int32, 1)[0])
+        name = b[off:off + ln].decode(); off += ln
+        wd = int(take(np.int32, 1)[0])
+        walls[name] = take(np.float64, nlocal * wd).reshape(nlocal, wd)
+    # canonical pairs: tags plus periodic image of j
+    L = boxhi - boxlo
+    owner = {int(t): i for i, t in enumerate(tag[:nlocal])}
+    shift = np.zeros((np_, 3), np.int32)
+    for p in range(np_):
+        j = pj[p]
+        if j >= nlocal:
+            o = owner[int(tag[j])]
+            shift[p] = np.rint((vec["x"][j] - vec["x"][o]) / L).astype(np.int32)
+    order = np.argsort(tag[:nlocal], kind="stable")
+    snap = dict(step=step, tag=tag[:nlocal][order], type=typ[:nlocal][order],
+                radius=radius[:nlocal][order], rmass=rmass[:nlocal][order],
+                pair_tag_i=tag[pi], pair_tag_j=tag[pj], pair_shift=shift, pair_flag=pf,
+                pair_hist=ph)
+    for k in vec:
+        snap[k] = vec[k][:nlocal][order]
+    for k, (name, w) in enumerate(sorted(walls.items())):
+        snap["wall%d_hist" % k] = w[order]
+    return snap
+
+
+def run_case(name, case, nsteps, snaps):
+    with tempfile.TemporaryDirectory() as d:
+        write_inputs(case, d, nsteps, snaps)
+        subprocess.check_call([LMP, "-in", "in.case", "-log", "log.case", "-screen", "none"], cwd=d)
+        out = {}
+        for st in snaps:
+            sn = read_snapshot(os.path.join(d, "snap.%d.bin" % st))
+            for k, v in sn.items():
+                if k != "step":
+                    out["s%d_%s" % (st, k)] = v
+        loop = [l for l in open(os.path.join(d, "log.case")) if l.startswith("Loop time")]
+    meta = {k: v for k, v in case.items() if k != "atoms" and not isinstance(v, np.ndarray)}
+    meta.update(nsteps=nsteps, snaps=snaps, loop=loop)
+    a = case["atoms"]
+    # the reference's rmass (identical formula) is what the runs start from
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta),
+                        init_tag=a["tag"], init_type=a["type"], init_x=a["x"], init_v=a["v"],
+                        init_omega=a["omega"], init_radius=a["radius"],
+                        init_rmass=out["s0_rmass"], Yeff=case["Yeff"], Geff=case["Geff"],
+                        betaeff=case["betaeff"], coeffFrict=case["coeffFrict"],
+                        coeffRollFrict=case["coeffRollFrict"], coeffRestLog=case["coeffRestLog"],
+                        **out)
+    print(name, "atoms", len(a["tag"]), "pairs@0", len(out["s0_pair_flag"]), loop)
+
+
+if __name__ == "__main__":
+    allc = cases()
+    sel = sys.argv[1:] or list(allc)
+    for nm in sel:
+        run_case(nm, *allc[nm])

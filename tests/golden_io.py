@@ -1,0 +1,88 @@
+"""Loading of the golden fixtures and the comparison rules shared by tests.
+
+Comparison rules (the parity contract):
+  * pair sets: bit-exact as sets of (owner tag, partner tag, image shift);
+    a pair of two owned atoms is canonicalised to (min tag, max tag) with its
+    history negated when the orientation flips (the reference stores the
+    j-side copy negated, src/fix_contact_history.cpp:400-413);
+  * forces and torques: |a - b| <= FORCE_RTOL * max|F| per component
+    (per-step, relative to the force norm);
+  * trajectories: positions within TRAJ_ATOL_REL of the box size.
+"""
+import json
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+
+FORCE_RTOL = 1e-11      # per-step forces/torques, relative to max |F| (|T|)
+HIST_RTOL = 1e-9        # shear history, relative to max |shear|
+TRAJ_RTOL = 1e-9        # positions/velocities over <= 100 steps, relative
+
+
+def load_golden(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(z["meta"]))
+    case = dict(meta)
+    case["boxlo"] = tuple(meta["boxlo"])
+    case["boxhi"] = tuple(meta["boxhi"])
+    case["periodic"] = tuple(meta["periodic"])
+    case["neigh"] = tuple(meta["neigh"])
+    case["gravity"] = tuple(meta["gravity"]) if meta["gravity"] is not None else None
+    case["planes"] = [tuple(p) for p in meta["planes"]]
+    for k in ("Yeff", "Geff", "betaeff", "coeffFrict", "coeffRollFrict", "coeffRestLog"):
+        case[k] = z[k]
+    case["atoms"] = dict(tag=z["init_tag"], type=z["init_type"], x=z["init_x"], v=z["init_v"],
+                         omega=z["init_omega"], radius=z["init_radius"], rmass=z["init_rmass"])
+    snaps = {}
+    for st in meta["snaps"]:
+        pre = "s%d_" % st
+        snaps[st] = {k[len(pre):]: z[k] for k in z.files if k.startswith(pre)}
+    return case, snaps
+
+
+def canonical_pairs(tag_i, tag_j, shift, flag, hist):
+    """dict key -> (flag, hist) with owned-owned pairs as (min, max) tags."""
+    out = {}
+    for p in range(len(tag_i)):
+        ti, tj = int(tag_i[p]), int(tag_j[p])
+        sh = tuple(int(t) for t in shift[p])
+        h = np.asarray(hist[p], dtype=np.float64)
+        if sh == (0, 0, 0) and ti > tj:
+            ti, tj, h = tj, ti, -h
+        key = (ti, tj, sh)
+        assert key not in out, "duplicate pair %r" % (key,)
+        out[key] = (int(flag[p]), h)
+    return out
+
+
+def sort_by_tag(atoms):
+    o = np.argsort(atoms["tag"], kind="stable")
+    return {k: (v[o] if isinstance(v, np.ndarray) and v.shape[:1] == o.shape else v)
+            for k, v in atoms.items()}
+
+
+def max_rel(a, b, scale=None):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    s = np.max(np.abs(b)) if scale is None else scale
+    if s == 0:
+        return float(np.max(np.abs(a - b)))
+    return float(np.max(np.abs(a - b)) / s)
+
+
+def compare_pairs(got, ref, hist_rtol=HIST_RTOL):
+    """Returns (missing, extra, flag_mismatch, max_hist_rel)."""
+    ks_g, ks_r = set(got), set(ref)
+    missing = ks_r - ks_g
+    extra = ks_g - ks_r
+    common = ks_g & ks_r
+    flagmis = [k for k in common if (got[k][0] != 0) != (ref[k][0] != 0)]
+    hs = max([np.max(np.abs(ref[k][1])) for k in common] + [0.0])
+    hm = 0.0
+    for k in common:
+        d = np.max(np.abs(got[k][1] - ref[k][1]))
+        hm = max(hm, d / hs if hs > 0 else d)
+    return missing, extra, flagmis, hm
