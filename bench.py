@@ -1,0 +1,306 @@
+"""Benchmark of the GB300 sphere-DEM timestep (particle-steps/s).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload column1m|...]
+
+One bench step = one DEM timestep (Verlet iteration) of the whole system.
+value: device-timed throughput with the state resident in HBM (CUDA events
+on the library's stream around dem_step(K)).  e2e: the same metric through
+the C ABI with host buffers: upload + setup + K steps + download, host
+copies inside the timed region.  --impl reference times the CPU oracle
+(restatement of the reference's path; the reference binary itself is not
+built on the GPU machine) on all host cores.  N>1: independent replicas,
+one per rank (the path has no exchange step), "scaling": "weak".
+"""
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "liggghts-inl_gb300", "python"))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s (1M Hertz/history spheres)"
+
+
+# ----------------------------------------------------------------------------
+# workloads
+# ----------------------------------------------------------------------------
+
+def workload(name, scale=1.0, seed=2024):
+    from gb300dem import workloads
+    if name == "column1m":
+        # configs[1] materials (r U[0.8,1.2] mm, rho 1500, E 1e7, e 0.5, mu 0.6,
+        # CDT 0.3), dense jittered lattice in a periodic column with a floor.
+        nx = max(4, int(round(100 * scale ** (1 / 3))))
+        case = workloads.lattice_case(
+            seed=seed, nx=nx, ny=nx, nz=nx, spacing=2.2e-3, radius=(0.8e-3, 1.2e-3),
+            density=1500.0, z0=1.2e-3, jitter=5e-5, vmax=0.2, wmax=20.0, E=(1e7,), nu=(0.3,),
+            rest=((0.5,),), frict=((0.6,),), rollfrict=((0.3,),), rolling_model=1, dt=5e-7,
+            skin=5e-4)
+        desc = dict(workload="column1m", atoms=int(len(case["atoms"]["tag"])),
+                    description="polydisperse Hertz/history + CDT rolling spheres, dense jittered "
+                                "lattice (2.2 mm, r 0.8-1.2 mm) in a periodic x/y column with a "
+                                "floor plane; configs[1] materials, dt 5e-7",
+                    l2="state + neighbour list > L2 (129 MB); no flush needed")
+        return case, desc
+    raise SystemExit("unknown workload %s" % name)
+
+
+# ----------------------------------------------------------------------------
+# helpers
+# ----------------------------------------------------------------------------
+
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.p = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.close()
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            c = [t.strip() for t in line.split(",")]
+            if len(c) < 9:
+                continue
+            try:
+                sm.append(float(c[1]))
+                mx = max(mx, float(c[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if c[5 + k].lower() in ("active", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def _oracle_sample_worker(args):
+    name, scale, seed, warm, steps = args
+    sys.path.insert(0, os.path.join(ROOT, "liggghts-inl_gb300", "python"))
+    sys.path.insert(0, ROOT)
+    from oracle.binding import Oracle
+    case, _ = workload(name, scale=scale, seed=seed)
+    o = Oracle(case)
+    o.setup()
+    o.run(warm)
+    t0 = time.perf_counter()
+    o.run(steps)
+    dt = time.perf_counter() - t0
+    return len(case["atoms"]["tag"]), steps, dt
+
+
+def cpu_sample(name, cores, steps, warm=2, scale=0.01):
+    """Times the oracle on a bounded sample (10k-atom slice of the workload)."""
+    from oracle import binding
+    binding.build()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_oracle_sample_worker, [(name, scale, 100 + k, warm, steps) for k in range(cores)])
+    tot = sum(n * s for n, s, _ in res)
+    tmax = max(dt for _, _, dt in res)
+    return tot / tmax, res
+
+
+# ----------------------------------------------------------------------------
+# arms
+# ----------------------------------------------------------------------------
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    steps = max(1, args.steps)
+    t0 = time.perf_counter()
+    val, res = cpu_sample(args.workload, cores, steps, warm=max(1, args.warmup))
+    wall = time.perf_counter() - t0
+    _, desc = workload(args.workload, scale=0.01)
+    sample = ("%d independent replicas (one per core) of a %d-atom slice of %s, %d timed steps each"
+              % (cores, res[0][0], args.workload, steps))
+    line = {"metric": METRIC, "value": val, "unit": "particle-steps/s", "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * max(r[2] for r in res) / steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "impl": "reference",
+            "config": {"workload": args.workload, "sample_atoms": res[0][0], "replicas": cores},
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "CPU restatement of the reference path (oracle/dem_oracle.c, pinned to the "
+                    "reference binary by tests/golden); the reference binary is built only where its "
+                    "sources are present", "wall_s": wall}
+    print(json.dumps(line))
+
+
+def run_gb300(args):
+    from gb300dem import api
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    case, desc = workload(args.workload, seed=2024 + rank)
+    n = len(case["atoms"]["tag"])
+    g = api.DemSystem(case)
+    g.setup()
+    g.step(args.warmup)
+    # ---- headline: device-timed K steps, state resident
+    if dist:
+        dist.barrier()
+    clocks = Clocks()
+    clocks.start()
+    g.profile(False)
+    t0 = time.perf_counter()
+    g.step(args.steps)
+    wall = time.perf_counter() - t0
+    cl = clocks.stop()
+    st = g.stats()
+    kt = g.kernel_times()
+    dev_ms = st["last_step_ms"]
+    if dist:
+        import torch
+        tt = torch.tensor([dev_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        dev_ms = float(tt.item())
+    value = world * n * args.steps / (dev_ms * 1e-3)
+    # ---- per-kernel times (separate profiled run of the same length)
+    g.profile(True)
+    g.step(args.steps)
+    kp = g.kernel_times()
+    g.profile(False)
+    # ---- e2e through the C ABI with host buffers
+    a = case["atoms"]
+    host = {k: np.ascontiguousarray(v) for k, v in a.items()}
+    g2 = api.DemSystem({k: v for k, v in case.items() if k != "atoms"})
+    t0 = time.perf_counter()
+    g2.upload(host)
+    g2.setup()
+    g2.step(args.steps)
+    out = g2.atoms()
+    e2e_s = time.perf_counter() - t0
+    h2d = n * (3 * 3 * 8 + 2 * 8 + 2 * 4)
+    d2h = n * (5 * 3 * 8 + 2 * 8 + 2 * 4)
+    assert out["x"].shape == (n, 3)
+    e2e = world * n * args.steps / e2e_s
+    g2.close()
+    # ---- roofline of the dominant kernel
+    peaks = measured_peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    npairs = st["npairs"]
+    pair_ms = kp["pair_ms"] / max(1, kp["pair_launches"])
+    part_ms = kp["particle_ms"] / max(1, kp["particle_launches"])
+    neigh_ms = kp["neigh_ms"] / max(1, kp["neigh_stages"])
+    tot_ms = pair_ms + part_ms + neigh_ms
+    # algorithmic bytes: pair kernel reads each atom's x,r,v,omega,type once
+    # (92 B), each list entry's i,j,shift (9 B) + active flag write (1 B);
+    # each touching entry: meff,reff (16 B), history r/w (48 B), flags r/w
+    # (8 B), results (72 B).
+    ncontact = int(kp.get("ncontacts", 0)) or None
+    fp64 = None
+    try:
+        fp64_peak = api.fp64_peak_tflops()
+    except Exception:
+        fp64_peak = None
+    frac_touch = 0.5
+    pair_bytes = n * 92 + npairs * 10 + frac_touch * npairs * 144
+    part_bytes = n * (15 * 8 * 2 + 8 * 4 + 1) + npairs * (4 + 1 + 72) + frac_touch * npairs * 4
+    dom = "pair" if pair_ms >= part_ms else "particle"
+    dom_bytes = pair_bytes if dom == "pair" else part_bytes
+    dom_ms = pair_ms if dom == "pair" else part_ms
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    roof = {"kernel": "k_pair" if dom == "pair" else "k_particle", "bound": "hbm",
+            "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+            "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
+            "algorithmic_bytes_per_launch": dom_bytes,
+            "avg_launch_ms": dom_ms,
+            "shares": {"pair": pair_ms / tot_ms, "particle": part_ms / tot_ms, "neigh": neigh_ms / tot_ms}}
+    if fp64_peak:
+        roof["fp64_peak_tflops_measured"] = fp64_peak
+    # ---- CPU baseline (oracle port, bounded sample, rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cores = 1
+        v, res = cpu_sample(args.workload, cores, steps=args.cpu_steps, warm=1)
+        cpu = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+               "sample": "oracle (CPU restatement, pinned to the reference binary) on a %d-atom slice "
+                         "of %s, %d steps, 1 thread" % (res[0][0], args.workload, args.cpu_steps)}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded)", "impl": "gb300",
+                "config": dict(desc, parallelism="replicas" if world > 1 else "single",
+                               pairs=npairs, rebuilds_total=st["nrebuilds"]),
+                "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d / args.steps,
+                        "d2h_bytes_per_step": d2h / args.steps,
+                        "note": "upload+setup+K steps+download through the C ABI, host buffers"},
+                "gpu_launches": kt["kernel_launches"],
+                "roofline": roof, "cpu_baseline": cpu, "clocks": cl, "wall_s": wall,
+                "kernel_ms_per_step": {"pair": pair_ms, "particle": part_ms, "neigh": neigh_ms}}
+        print(json.dumps(line))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="column1m")
+    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+/* liggghts_gb300.h — C ABI of the GB300 sphere-DEM timestep (libdemgpu.so).
+ *
+ * One handle holds one granular system resident on the GPU: particle state,
+ * the granular half neighbour list with its contact history, primitive-wall
+ * histories.  Every call returns a dem_status code; no exception crosses the
+ * ABI.  One handle per host thread; each handle owns one CUDA stream.
+ *
+ * Reference interfaces each entry point replaces (LIGGGHTS-INL source paths):
+ *   dem_create            PairGran::settings/init_style + Neighbor::init
+ *                         (src/pair_gran_proxy.cpp:63-79, src/pair_gran.cpp:229-330,
+ *                          src/neighbor.cpp:258-337)
+ *   dem_set_pair_params   ContactModel::connectToProperties -> PropertyRegistry
+ *                         matrices Yeff/Geff/betaeff/coeffFrict/coeffRollFrict/
+ *                         coeffRestLog/charVel (src/global_properties.cpp:428-561,
+ *                         src/normal_model_hertz.h:172-183, src/rolling_model_cdt.h:83-86)
+ *   dem_add_plane         FixWallGran "primitive type T {x,y,z}plane P"
+ *                         (src/fix_wall_gran.cpp:176-215, src/primitive_wall_definitions.h:123-150)
+ *   dem_upload_atoms      Atom arrays x v omega radius rmass type tag
+ *                         (src/atom_vec_sphere.cpp:1060-1090, src/library.h:59-74)
+ *   dem_setup             Verlet::setup (src/verlet.cpp setup(); src/pair_gran.cpp:633-635)
+ *   dem_step              Verlet::run loop body (src/verlet.cpp:281-389): nve/sphere
+ *                         initial/final_integrate, Neighbor::decide/build with history
+ *                         carry-over, PairGran::compute, FixGravity and FixWallGran post_force
+ *   dem_download_atoms    lammps_gather_atoms / Atom::extract (src/library.h:59-74)
+ *   dem_download_contacts compute pair/gran/local id force history (src/compute_pair_gran_local.cpp:100-116)
+ *   dem_download_wall_history  fix property/atom history_<wallid> (src/fix_wall_gran.cpp:477-500)
+ *   dem_get_stats         Timer / Finish breakdown, Neighbor::ncalls (src/timer.h:51-52)
+ */
+#ifndef LIGGGHTS_GB300_H
+#define LIGGGHTS_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum dem_status {
+  DEM_OK = 0,
+  DEM_ERR_BAD_ARG = 1,        /* invalid argument or call order */
+  DEM_ERR_CUDA = 2,           /* a CUDA runtime call failed; see dem_last_error */
+  DEM_ERR_NEIGH_OVERFLOW = 3, /* neighbour list capacity could not be grown */
+  DEM_ERR_NAN = 4,            /* non-finite particle state detected */
+  DEM_ERR_TIMEOUT = 5,        /* a bounded device wait gave up */
+  DEM_ERR_BOX = 6,            /* periodic box shorter than 3 neighbour cutoffs */
+  DEM_ERR_UNSUPPORTED = 7,    /* contact-model combination not on the GPU path */
+  DEM_ERR_NO_DEVICE = 8       /* no CUDA device / kernel image */
+} dem_status;
+
+enum { DEM_NORMAL_HERTZ = 0, DEM_NORMAL_HOOKE = 1 };
+enum { DEM_ROLLING_OFF = 0, DEM_ROLLING_CDT = 1 };
+enum { DEM_COHESION_OFF = 0, DEM_COHESION_BOND_NONLINEAR = 1 };
+
+/* Same meaning as the input-script settings of the reference. */
+typedef struct dem_config {
+  double boxlo[3], boxhi[3];
+  int periodic[3];             /* boundary p (1) or f (0) per dimension */
+  double dt;                   /* timestep */
+  double skin;                 /* neighbor SKIN bin */
+  double contact_distance_factor; /* neigh_modify contact_distance_factor (1.0) */
+  int neigh_every, neigh_delay, neigh_check; /* neigh_modify every/delay/check */
+  int normal_model;            /* DEM_NORMAL_* of pair_style gran model ... */
+  int rolling_model;           /* DEM_ROLLING_* (rolling_friction cdt) */
+  int cohesion_model;          /* DEM_COHESION_* */
+  int tangential_damping;      /* model option tangential_damping (default 1) */
+  int limit_force;             /* model option limitForce (default 0) */
+  int gravity_on;              /* fix gravity present */
+  double gravity[3];           /* xacc, yacc, zacc as FixGravity::set_acceleration */
+} dem_config;
+
+typedef struct dem_stats {
+  long long ntimestep;         /* update->ntimestep */
+  long long nrebuilds;         /* neighbour list builds (Neighbor::ncalls) */
+  long long npairs;            /* entries in the granular half list */
+  long long nlost;             /* atoms removed at non-periodic boundaries */
+  long long natoms;
+  int device;                  /* CUDA ordinal */
+  int pair_capacity;
+  double last_step_ms;         /* device time of the last dem_step call */
+} dem_stats;
+
+typedef struct dem_handle dem_handle;
+
+int dem_create(const dem_config *cfg, dem_handle **out);
+int dem_destroy(dem_handle *h);
+
+/* Matrices are (ntypes+1)^2, row-major, types start at 1 (row/col 0 unused),
+ * the layout of the reference's MatrixProperty.  coeffRollFrict may be NULL
+ * without rolling friction; coeffRestLog/charVel are read by the Hooke law. */
+int dem_set_pair_params(dem_handle *h, int ntypes, const double *Yeff, const double *Geff,
+                        const double *betaeff, const double *coeffFrict,
+                        const double *coeffRollFrict, const double *coeffRestLog,
+                        double charVel);
+
+/* Helper: the reference's derivations of Yeff, Geff, betaeff, coeffRestLog from
+ * youngsModulus/poissonsRatio (per type) and coefficientRestitution (per type
+ * pair), src/global_properties.cpp:428-561.  Host-only arithmetic. */
+int dem_derive_hertz_tables(int ntypes, const double *youngs, const double *poisson,
+                            const double *restitution, double *Yeff, double *Geff,
+                            double *betaeff, double *coeffRestLog);
+
+/* axis 0/1/2 = xplane/yplane/zplane, rolling_model = DEM_ROLLING_* for this wall.
+ * Returns the wall id through *wall_id (may be NULL). */
+int dem_add_plane(dem_handle *h, int axis, double pos, int wall_type, int rolling_model,
+                  int *wall_id);
+
+/* x, v, omega are n*3 (x[3*i+d] == atom->x[i][d]). Resets contact history. */
+int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, const double *x,
+                     const double *v, const double *omega, const double *radius,
+                     const double *rmass);
+
+int dem_setup(dem_handle *h);
+int dem_step(dem_handle *h, int nsteps);
+
+/* Atoms come back in the device's current (cell-sorted) order with their tags. */
+int dem_natoms(dem_handle *h, int *n);
+int dem_download_atoms(dem_handle *h, int *tag, int *type, double *x, double *v, double *omega,
+                       double *f, double *torque, double *radius, double *rmass);
+
+/* Granular half list: owner tag, partner tag, periodic image of the partner
+ * (shift[3*p+d] in {-1,0,1}), contact flags (reference bit layout) and the
+ * dnum history doubles per pair (dnum = 3: shear x,y,z). */
+int dem_npairs(dem_handle *h, int *npairs, int *dnum);
+int dem_download_contacts(dem_handle *h, int *tag_i, int *tag_j, int *shift, int *flag,
+                          double *hist);
+/* 3 doubles per atom in dem_download_atoms order. */
+int dem_download_wall_history(dem_handle *h, int wall_id, double *hist);
+
+int dem_get_stats(dem_handle *h, dem_stats *out);
+
+/* Per-kernel device timing with CUDA events on the handle's stream (the
+ * reference's Timer buckets, src/timer.h:51-52).  Enabling resets counters.
+ * kernel_launches counts every kernel the library launched since the reset. */
+typedef struct dem_kernel_times {
+  double pair_ms;              /* pair force kernel (PairGran::compute) */
+  long long pair_launches;
+  double particle_ms;          /* gather + walls + gravity + nve/sphere kernel */
+  long long particle_launches;
+  double neigh_ms;             /* decide + rebuild stage (Neighbor::decide/build) */
+  long long neigh_stages;
+  long long kernel_launches;
+} dem_kernel_times;
+int dem_profile(dem_handle *h, int enable);
+int dem_get_kernel_times(dem_handle *h, dem_kernel_times *out);
+
+/* Diagnostic without a reference counterpart: FP64 FMA throughput of the
+ * current device in TFLOP/s (dependent-chain-free DFMA loop), used as the
+ * FP64 roofline denominator. */
+int dem_measure_fp64_peak(double *tflops);
+const char *dem_last_error(dem_handle *h);
+const char *dem_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

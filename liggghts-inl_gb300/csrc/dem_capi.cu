@@ -1,0 +1,631 @@
+// Host runtime of one resident granular system and the C ABI of
+// include/liggghts_gb300.h.  The host owns device buffers and one stream per
+// handle, queues whole timesteps without synchronising (rebuild decisions are
+// taken on the device), and checks the device control block every
+// kCheckEvery steps and at the end of each call.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/liggghts_gb300.h"
+#include "dem_device.cuh"
+#include "dem_kernels.h"
+
+using namespace gb300;
+
+namespace {
+constexpr int kCheckEvery = 256;
+constexpr long kMaxCells = 1L << 26;
+}  // namespace
+
+struct dem_handle {
+  dem_config cfg{};
+  Sys s{};
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int device = 0;
+  std::string err;
+  bool have_params = false, have_atoms = false, setup_done = false;
+  std::vector<void *> allocs_atoms, allocs_pairs, allocs_misc;
+  LaunchCfg lc{152 * 8};
+  float last_ms = 0.f;
+  Ctrl host_ctrl{};
+  // per-kernel timing (dem_profile)
+  bool profile = false;
+  std::vector<cudaEvent_t> evpool;
+  int evused = 0;
+  std::vector<int> evkind;  // 0 particle, 1 neigh, 2 pair: kind of interval ending at event k
+  dem_kernel_times kt{};
+};
+
+// Records an event closing an interval of the given kind (profiling only).
+static void mark(dem_handle *h, int kind) {
+  if (!h->profile) return;
+  if (h->evused >= (int)h->evpool.size()) return;
+  cudaEventRecord(h->evpool[h->evused], h->st);
+  h->evkind[h->evused] = kind;
+  h->evused++;
+}
+
+static void mark_start(dem_handle *h) { mark(h, -1); }
+
+// Folds the recorded intervals into the totals (the stream must be idle).
+static void harvest(dem_handle *h) {
+  if (!h->profile || h->evused == 0) return;
+  for (int k = 1; k < h->evused; k++) {
+    if (h->evkind[k] < 0) continue;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->evpool[k - 1], h->evpool[k]);
+    if (h->evkind[k] == 0) { h->kt.particle_ms += ms; h->kt.particle_launches++; }
+    if (h->evkind[k] == 1) { h->kt.neigh_ms += ms; h->kt.neigh_stages++; }
+    if (h->evkind[k] == 2) { h->kt.pair_ms += ms; h->kt.pair_launches++; }
+  }
+  h->evused = 0;
+}
+
+#define CUDA_TRY(h, call)                                                                  \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) {                                                               \
+      (h)->err = std::string(#call) + ": " + cudaGetErrorString(e_);                       \
+      return DEM_ERR_CUDA;                                                                 \
+    }                                                                                      \
+  } while (0)
+
+static int fail(dem_handle *h, int code, const std::string &msg) {
+  if (h) h->err = msg;
+  return code;
+}
+
+template <typename T>
+static cudaError_t dalloc(std::vector<void *> &list, T **p, size_t n) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+  if (e == cudaSuccess) {
+    list.push_back(q);
+    *p = static_cast<T *>(q);
+  }
+  return e;
+}
+
+static void free_list(std::vector<void *> &l) {
+  for (void *p : l) cudaFree(p);
+  l.clear();
+}
+
+static int alloc_atoms(dem_handle *h, int nmax) {
+  Sys &s = h->s;
+  free_list(h->allocs_atoms);
+  s.nmax = nmax;
+  auto &L = h->allocs_atoms;
+  for (int b = 0; b < 2; b++) {
+    AtomArrays &A = s.atoms[b];
+    double **d[] = {&A.x, &A.y, &A.z, &A.vx, &A.vy, &A.vz, &A.wx, &A.wy, &A.wz, &A.fx, &A.fy,
+                    &A.fz, &A.tx, &A.ty, &A.tz, &A.r, &A.m, &A.dtfm, &A.dtir, &A.xh, &A.yh, &A.zh};
+    for (double **pp : d) CUDA_TRY(h, dalloc(L, pp, nmax));
+    CUDA_TRY(h, dalloc(L, &A.type, nmax));
+    CUDA_TRY(h, dalloc(L, &A.tag, nmax));
+    CUDA_TRY(h, dalloc(L, &A.whist, (size_t)3 * kMaxPlanes * nmax));
+    CUDA_TRY(h, dalloc(L, &A.wbits, nmax));
+  }
+  for (int b = 0; b < 2; b++) {
+    PairArrays &P = s.pairs[b];
+    CUDA_TRY(h, dalloc(L, &P.row, nmax + 1));
+    CUDA_TRY(h, dalloc(L, &P.rev_start, nmax + 1));
+    CUDA_TRY(h, cudaMemset(P.row, 0, (nmax + 1) * sizeof(int)));
+    CUDA_TRY(h, cudaMemset(P.rev_start, 0, (nmax + 1) * sizeof(int)));
+  }
+  CUDA_TRY(h, dalloc(L, &s.perm, nmax));
+  CUDA_TRY(h, dalloc(L, &s.order, nmax));
+  CUDA_TRY(h, dalloc(L, &s.pcount, nmax + 1));
+  CUDA_TRY(h, dalloc(L, &s.rev_count, nmax + 1));
+  CUDA_TRY(h, dalloc(L, &s.rev_fill, nmax + 1));
+  CUDA_TRY(h, dalloc(L, &s.cell_count, (size_t)s.ncell + 2));
+  CUDA_TRY(h, dalloc(L, &s.cell_start, (size_t)s.ncell + 2));
+  CUDA_TRY(h, dalloc(L, &s.cell_fill, (size_t)s.ncell + 2));
+  long maxlen = std::max<long>(nmax + 1, s.ncell + 2);
+  CUDA_TRY(h, dalloc(L, &s.scan_tmp, (maxlen + 4095) / 4096 + 1));
+  return DEM_OK;
+}
+
+// (Re)allocates every pcap-sized array; keeps the current list (pairs[0]).
+static int alloc_pairs(dem_handle *h, int pcap, int keep_np) {
+  Sys &s = h->s;
+  std::vector<void *> nl;
+  PairArrays np_[2];
+  for (int b = 0; b < 2; b++) {
+    PairArrays &P = np_[b];
+    P = s.pairs[b];
+    CUDA_TRY(h, dalloc(nl, &P.i, pcap));
+    CUDA_TRY(h, dalloc(nl, &P.j, pcap));
+    CUDA_TRY(h, dalloc(nl, &P.sh, pcap));
+    CUDA_TRY(h, dalloc(nl, &P.flag, pcap));
+    CUDA_TRY(h, dalloc(nl, &P.hist, (size_t)3 * pcap));
+    CUDA_TRY(h, dalloc(nl, &P.meff, pcap));
+    CUDA_TRY(h, dalloc(nl, &P.reff, pcap));
+    CUDA_TRY(h, dalloc(nl, &P.rev, pcap));
+  }
+  double *rF, *rTi, *rTj;
+  uint8_t *act;
+  CUDA_TRY(h, dalloc(nl, &rF, (size_t)3 * pcap));
+  CUDA_TRY(h, dalloc(nl, &rTi, (size_t)3 * pcap));
+  CUDA_TRY(h, dalloc(nl, &rTj, (size_t)3 * pcap));
+  CUDA_TRY(h, dalloc(nl, &act, pcap));
+  if (keep_np > 0 && s.pcap > 0) {
+    const PairArrays &O = s.pairs[0];
+    PairArrays &N = np_[0];
+    const size_t k = keep_np;
+    CUDA_TRY(h, cudaMemcpy(N.i, O.i, k * sizeof(int), cudaMemcpyDeviceToDevice));
+    CUDA_TRY(h, cudaMemcpy(N.j, O.j, k * sizeof(int), cudaMemcpyDeviceToDevice));
+    CUDA_TRY(h, cudaMemcpy(N.sh, O.sh, k, cudaMemcpyDeviceToDevice));
+    CUDA_TRY(h, cudaMemcpy(N.flag, O.flag, k * sizeof(int), cudaMemcpyDeviceToDevice));
+    for (int d = 0; d < 3; d++)
+      CUDA_TRY(h, cudaMemcpy(N.hist + (size_t)d * pcap, O.hist + (size_t)d * s.pcap,
+                             k * sizeof(double), cudaMemcpyDeviceToDevice));
+    CUDA_TRY(h, cudaMemcpy(N.meff, O.meff, k * sizeof(double), cudaMemcpyDeviceToDevice));
+    CUDA_TRY(h, cudaMemcpy(N.reff, O.reff, k * sizeof(double), cudaMemcpyDeviceToDevice));
+    CUDA_TRY(h, cudaMemcpy(N.rev, O.rev, k * sizeof(int), cudaMemcpyDeviceToDevice));
+  }
+  free_list(h->allocs_pairs);
+  h->allocs_pairs = nl;
+  s.pairs[0] = np_[0];
+  s.pairs[1] = np_[1];
+  s.resF = rF;
+  s.resTi = rTi;
+  s.resTj = rTj;
+  s.active = act;
+  s.pcap = pcap;
+  return DEM_OK;
+}
+
+static int read_ctrl(dem_handle *h) {
+  CUDA_TRY(h, cudaMemcpyAsync(&h->host_ctrl, h->s.ctrl, sizeof(Ctrl), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  harvest(h);
+  return DEM_OK;
+}
+
+// If the device halted on a pair-capacity overflow: grow, clear the halt and
+// finish the interrupted rebuild.  Returns DEM_OK when nothing is pending.
+static int recover(dem_handle *h, bool *resumed) {
+  *resumed = false;
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  Ctrl &c = h->host_ctrl;
+  if (c.status == kStatNan) return fail(h, DEM_ERR_NAN, "non-finite particle position");
+  if (!c.halt) return DEM_OK;
+  if (c.status != kStatPairOverflow) return fail(h, DEM_ERR_CUDA, "device halted");
+  const int want = (int)std::min<long>(2147000000L, std::max<long>((long)c.np_new * 5 / 4 + 1024, 2L * h->s.pcap));
+  rc = alloc_pairs(h, want, c.np);
+  if (rc) return fail(h, DEM_ERR_NEIGH_OVERFLOW, "cannot grow neighbour list: " + h->err);
+  c.halt = 0;
+  c.status = kStatOk;
+  CUDA_TRY(h, cudaMemcpyAsync(h->s.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice, h->st));
+  h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 1);
+  *resumed = true;
+  return DEM_OK;
+}
+
+extern "C" {
+
+const char *dem_version(void) { return "liggghts-inl-gb300 0.1 (sm_103a)"; }
+
+int dem_create(const dem_config *cfg, dem_handle **out) {
+  if (!cfg || !out) return DEM_ERR_BAD_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DEM_ERR_NO_DEVICE;
+  if (cfg->cohesion_model != DEM_COHESION_OFF) return DEM_ERR_UNSUPPORTED;
+  if (cfg->normal_model != DEM_NORMAL_HERTZ && cfg->normal_model != DEM_NORMAL_HOOKE)
+    return DEM_ERR_UNSUPPORTED;
+  if (cfg->dt <= 0 || cfg->skin < 0 || cfg->neigh_every < 1 || cfg->contact_distance_factor < 1.0)
+    return DEM_ERR_BAD_ARG;
+  dem_handle *h = new dem_handle();
+  h->cfg = *cfg;
+  cudaGetDevice(&h->device);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, h->device) == cudaSuccess)
+    h->lc.max_grid = prop.multiProcessorCount * 8;
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
+    delete h;
+    return DEM_ERR_CUDA;
+  }
+  Sys &s = h->s;
+  if (cudaMalloc(&s.ctrl, sizeof(Ctrl)) != cudaSuccess) {
+    delete h;
+    return DEM_ERR_CUDA;
+  }
+  h->allocs_misc.push_back(s.ctrl);
+  cudaMemset(s.ctrl, 0, sizeof(Ctrl));
+  for (int d = 0; d < 3; d++) {
+    s.boxlo[d] = cfg->boxlo[d];
+    s.boxhi[d] = cfg->boxhi[d];
+    s.prd[d] = cfg->boxhi[d] - cfg->boxlo[d];
+    s.periodic[d] = cfg->periodic[d] ? 1 : 0;
+    s.g[d] = cfg->gravity[d];
+  }
+  s.dt = cfg->dt;
+  s.skin = cfg->skin;
+  s.cdf = cfg->contact_distance_factor;
+  s.neigh_every = cfg->neigh_every;
+  s.neigh_delay = cfg->neigh_delay;
+  s.neigh_check = cfg->neigh_check;
+  s.normal = cfg->normal_model;
+  s.rolling = cfg->rolling_model;
+  s.tdamp = cfg->tangential_damping;
+  s.limitf = cfg->limit_force;
+  s.gravity_on = cfg->gravity_on;
+  *out = h;
+  return DEM_OK;
+}
+
+int dem_destroy(dem_handle *h) {
+  if (!h) return DEM_ERR_BAD_ARG;
+  if (h->st) cudaStreamSynchronize(h->st);
+  free_list(h->allocs_pairs);
+  free_list(h->allocs_atoms);
+  free_list(h->allocs_misc);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  for (auto &e : h->evpool) cudaEventDestroy(e);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return DEM_OK;
+}
+
+int dem_derive_hertz_tables(int nt, const double *Y, const double *v, const double *e,
+                            double *Yeff, double *Geff, double *betaeff, double *restlog) {
+  if (nt < 1 || !Y || !v || !e) return DEM_ERR_BAD_ARG;
+  const int m = nt + 1;
+  for (int k = 0; k < m * m; k++) {
+    if (Yeff) Yeff[k] = 0.0;
+    if (Geff) Geff[k] = 0.0;
+    if (betaeff) betaeff[k] = 0.0;
+    if (restlog) restlog[k] = 0.0;
+  }
+  for (int i = 1; i <= nt; i++)
+    for (int j = 1; j <= nt; j++) {
+      const double Yi = Y[i - 1], Yj = Y[j - 1], vi = v[i - 1], vj = v[j - 1];
+      // src/global_properties.cpp:449, :480, :518, :556
+      if (Yeff) Yeff[i * m + j] = 1. / ((1. - pow(vi, 2.)) / Yi + (1. - pow(vj, 2.)) / Yj);
+      if (Geff) Geff[i * m + j] = 1. / (2. * (2. - vi) * (1. + vi) / Yi + 2. * (2. - vj) * (1. + vj) / Yj);
+      const double lg = log(e[(i - 1) * nt + (j - 1)]);
+      if (restlog) restlog[i * m + j] = lg;
+      if (betaeff) betaeff[i * m + j] = lg / sqrt(pow(lg, 2.) + pow(M_PI, 2.));
+    }
+  return DEM_OK;
+}
+
+int dem_set_pair_params(dem_handle *h, int ntypes, const double *Yeff, const double *Geff,
+                        const double *betaeff, const double *coeffFrict,
+                        const double *coeffRollFrict, const double *coeffRestLog, double charVel) {
+  if (!h || ntypes < 1 || !Yeff || !Geff || !coeffFrict) return DEM_ERR_BAD_ARG;
+  if (h->cfg.normal_model == DEM_NORMAL_HERTZ && !betaeff) return fail(h, DEM_ERR_BAD_ARG, "betaeff required");
+  if (h->cfg.normal_model == DEM_NORMAL_HOOKE && !coeffRestLog) return fail(h, DEM_ERR_BAD_ARG, "coeffRestLog required");
+  const int m = (ntypes + 1) * (ntypes + 1);
+  std::vector<double> tab(6 * (size_t)m, 0.0);
+  const double *src[6] = {Yeff, Geff, betaeff, coeffFrict, coeffRollFrict, coeffRestLog};
+  for (int k = 0; k < 6; k++)
+    if (src[k]) std::memcpy(&tab[(size_t)k * m], src[k], m * sizeof(double));
+  if (h->s.params) {
+    cudaFree(h->s.params);
+    h->allocs_misc.erase(std::remove(h->allocs_misc.begin(), h->allocs_misc.end(), (void *)h->s.params),
+                         h->allocs_misc.end());
+  }
+  CUDA_TRY(h, dalloc(h->allocs_misc, &h->s.params, tab.size()));
+  CUDA_TRY(h, cudaMemcpy(h->s.params, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+  h->s.ntypes = ntypes;
+  h->s.charVel = charVel;
+  h->have_params = true;
+  return DEM_OK;
+}
+
+int dem_add_plane(dem_handle *h, int axis, double pos, int wall_type, int rolling_model, int *wall_id) {
+  if (!h || axis < 0 || axis > 2 || wall_type < 1) return DEM_ERR_BAD_ARG;
+  if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "add walls before uploading atoms");
+  if (h->s.nplanes >= kMaxPlanes) return fail(h, DEM_ERR_BAD_ARG, "too many primitive walls");
+  Plane &p = h->s.planes[h->s.nplanes];
+  p.axis = axis;
+  p.pos = pos;
+  p.wall_type = wall_type;
+  p.rolling = rolling_model == DEM_ROLLING_CDT ? 1 : 0;
+  if (wall_id) *wall_id = h->s.nplanes;
+  h->s.nplanes++;
+  return DEM_OK;
+}
+
+int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, const double *x,
+                     const double *v, const double *omega, const double *radius,
+                     const double *rmass) {
+  if (!h || n < 1 || !tag || !type || !x || !v || !omega || !radius || !rmass) return DEM_ERR_BAD_ARG;
+  if (!h->have_params) return fail(h, DEM_ERR_BAD_ARG, "set pair parameters first");
+  Sys &s = h->s;
+  for (int i = 0; i < n; i++)
+    if (type[i] < 1 || type[i] > s.ntypes) return fail(h, DEM_ERR_BAD_ARG, "atom type out of range");
+  // cutneighmax = (maxrad_i + maxrad_j)*cdf + skin, src/pair_gran.cpp:591-602,
+  // src/neighbor.cpp:316-337
+  double maxrad = 0.0;
+  for (int i = 0; i < n; i++) maxrad = std::max(maxrad, radius[i]);
+  const double cutoff = (maxrad + maxrad) * s.cdf;
+  s.cutneighmax = std::sqrt(cutoff * cutoff) + s.skin;
+  long ncell = 1;
+  for (int d = 0; d < 3; d++) {
+    long nc = (long)std::floor(s.prd[d] / (s.cutneighmax * (1.0 + 1e-9)));
+    if (nc < 1) nc = 1;
+    if (s.periodic[d] && nc < 3)
+      return fail(h, DEM_ERR_BOX, "periodic box dimension shorter than 3 neighbour cutoffs");
+    s.nc[d] = (int)std::min<long>(nc, 4096);
+    ncell *= s.nc[d];
+  }
+  while (ncell > kMaxCells) {  // very sparse boxes: coarser cells stay conservative
+    int d = (s.nc[0] >= s.nc[1] && s.nc[0] >= s.nc[2]) ? 0 : (s.nc[1] >= s.nc[2] ? 1 : 2);
+    if (s.periodic[d] && s.nc[d] <= 3) break;
+    s.nc[d] = std::max(s.periodic[d] ? 3 : 1, s.nc[d] / 2);
+    ncell = (long)s.nc[0] * s.nc[1] * s.nc[2];
+  }
+  for (int d = 0; d < 3; d++) s.csz[d] = s.prd[d] / s.nc[d];
+  s.ncell = (int)ncell;
+  int rc = alloc_atoms(h, n);
+  if (rc) return rc;
+  rc = alloc_pairs(h, std::max(16 * n, 4096), 0);
+  if (rc) return rc;
+  // host-side per-atom constants of FixNVESphere (src/fix_nve_sphere.cpp:150-178)
+  const double dtf = 0.5 * s.dt * 1.0;
+  const double dtfrotate = dtf / 0.4;
+  std::vector<double> buf(n);
+  AtomArrays &A = s.atoms[0];
+  auto up3 = [&](const double *src, double *dx, double *dy, double *dz) -> int {
+    double *dst[3] = {dx, dy, dz};
+    for (int d = 0; d < 3; d++) {
+      for (int i = 0; i < n; i++) buf[i] = src[3 * i + d];
+      CUDA_TRY(h, cudaMemcpy(dst[d], buf.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    return DEM_OK;
+  };
+  if ((rc = up3(x, A.x, A.y, A.z))) return rc;
+  if ((rc = up3(v, A.vx, A.vy, A.vz))) return rc;
+  if ((rc = up3(omega, A.wx, A.wy, A.wz))) return rc;
+  CUDA_TRY(h, cudaMemcpy(A.r, radius, n * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpy(A.m, rmass, n * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpy(A.type, type, n * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpy(A.tag, tag, n * sizeof(int), cudaMemcpyHostToDevice));
+  for (int i = 0; i < n; i++) buf[i] = dtf / (rmass[i] * (1. + 0.0));
+  CUDA_TRY(h, cudaMemcpy(A.dtfm, buf.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  for (int i = 0; i < n; i++) buf[i] = dtfrotate / (radius[i] * radius[i] * rmass[i]);
+  CUDA_TRY(h, cudaMemcpy(A.dtir, buf.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+  double *z3[] = {A.fx, A.fy, A.fz, A.tx, A.ty, A.tz, A.xh, A.yh, A.zh};
+  for (double *p : z3) CUDA_TRY(h, cudaMemset(p, 0, n * sizeof(double)));
+  CUDA_TRY(h, cudaMemset(A.whist, 0, (size_t)3 * kMaxPlanes * n * sizeof(double)));
+  CUDA_TRY(h, cudaMemset(A.wbits, 0, n));
+  Ctrl c{};
+  c.n = n;
+  h->host_ctrl = c;
+  CUDA_TRY(h, cudaMemcpy(s.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice));
+  h->have_atoms = true;
+  h->setup_done = false;
+  return DEM_OK;
+}
+
+int dem_setup(dem_handle *h) {
+  if (!h || !h->have_atoms) return DEM_ERR_BAD_ARG;
+  cudaGetLastError();
+  h->kt.kernel_launches += launch_set_rebuild(h->s, 1, h->st);
+  h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);
+  bool resumed = true;
+  while (resumed) {
+    int rc = recover(h, &resumed);
+    if (rc) return rc;
+  }
+  h->kt.kernel_launches += launch_pair(h->s, h->lc, 0, h->st);
+  h->kt.kernel_launches += launch_particle(h->s, h->lc, kModeGather, 0, h->st);
+  CUDA_TRY(h, cudaGetLastError());
+  bool dummy;
+  int rc = recover(h, &dummy);
+  if (rc) return rc;
+  h->setup_done = true;
+  return DEM_OK;
+}
+
+int dem_step(dem_handle *h, int nsteps) {
+  if (!h || nsteps < 0) return DEM_ERR_BAD_ARG;
+  if (!h->setup_done) return fail(h, DEM_ERR_BAD_ARG, "dem_setup must precede dem_step");
+  if (nsteps == 0) return DEM_OK;
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  const long long ts0 = h->host_ctrl.ntimestep;
+  CUDA_TRY(h, cudaEventRecord(h->ev0, h->st));
+  long long done = 0;  // steps whose rebuild+pair stage has been queued
+  bool first = true;
+  while (done < nsteps) {
+    const long long chunk = std::min<long long>(kCheckEvery, nsteps - done);
+    mark_start(h);
+    for (long long k = 0; k < chunk; k++) {
+      h->kt.kernel_launches +=
+          launch_particle(h->s, h->lc, first ? kModeInitial : kModeGatherFinalInitial, 1, h->st);
+      mark(h, 0);
+      first = false;
+      h->kt.kernel_launches += launch_decide(h->s, h->st);
+      h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);
+      mark(h, 1);
+      h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
+      mark(h, 2);
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    bool resumed = false;
+    rc = recover(h, &resumed);
+    if (rc) return rc;
+    if (resumed) {
+      // the halted step's rebuild is now finished; compute its forces and
+      // continue after it (later queued kernels were no-ops)
+      h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
+      bool again = true;
+      while (again) {
+        rc = recover(h, &again);
+        if (rc) return rc;
+        if (again) h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
+      }
+      rc = read_ctrl(h);
+      if (rc) return rc;
+      done = h->host_ctrl.ntimestep - ts0;
+    } else {
+      done += chunk;
+    }
+  }
+  mark_start(h);
+  h->kt.kernel_launches += launch_particle(h->s, h->lc, kModeGatherFinal, 1, h->st);
+  mark(h, 0);
+  CUDA_TRY(h, cudaEventRecord(h->ev1, h->st));
+  CUDA_TRY(h, cudaGetLastError());
+  bool dummy;
+  rc = recover(h, &dummy);
+  if (rc) return rc;
+  cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+  return DEM_OK;
+}
+
+int dem_natoms(dem_handle *h, int *n) {
+  if (!h || !n) return DEM_ERR_BAD_ARG;
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  *n = h->host_ctrl.n;
+  return DEM_OK;
+}
+
+int dem_download_atoms(dem_handle *h, int *tag, int *type, double *x, double *v, double *omega,
+                       double *f, double *torque, double *radius, double *rmass) {
+  if (!h || !h->have_atoms) return DEM_ERR_BAD_ARG;
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  const int n = h->host_ctrl.n;
+  const AtomArrays &A = h->s.atoms[0];
+  std::vector<double> buf(n);
+  auto down3 = [&](double *dst, const double *sx, const double *sy, const double *sz) -> int {
+    if (!dst) return DEM_OK;
+    const double *src[3] = {sx, sy, sz};
+    for (int d = 0; d < 3; d++) {
+      CUDA_TRY(h, cudaMemcpy(buf.data(), src[d], n * sizeof(double), cudaMemcpyDeviceToHost));
+      for (int i = 0; i < n; i++) dst[3 * i + d] = buf[i];
+    }
+    return DEM_OK;
+  };
+  if ((rc = down3(x, A.x, A.y, A.z))) return rc;
+  if ((rc = down3(v, A.vx, A.vy, A.vz))) return rc;
+  if ((rc = down3(omega, A.wx, A.wy, A.wz))) return rc;
+  if ((rc = down3(f, A.fx, A.fy, A.fz))) return rc;
+  if ((rc = down3(torque, A.tx, A.ty, A.tz))) return rc;
+  if (radius) CUDA_TRY(h, cudaMemcpy(radius, A.r, n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (rmass) CUDA_TRY(h, cudaMemcpy(rmass, A.m, n * sizeof(double), cudaMemcpyDeviceToHost));
+  if (tag) CUDA_TRY(h, cudaMemcpy(tag, A.tag, n * sizeof(int), cudaMemcpyDeviceToHost));
+  if (type) CUDA_TRY(h, cudaMemcpy(type, A.type, n * sizeof(int), cudaMemcpyDeviceToHost));
+  return DEM_OK;
+}
+
+int dem_npairs(dem_handle *h, int *npairs, int *dnum) {
+  if (!h) return DEM_ERR_BAD_ARG;
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  if (npairs) *npairs = h->host_ctrl.np;
+  if (dnum) *dnum = kDnumShear;
+  return DEM_OK;
+}
+
+int dem_download_contacts(dem_handle *h, int *tag_i, int *tag_j, int *shift, int *flag, double *hist) {
+  if (!h || !h->have_atoms) return DEM_ERR_BAD_ARG;
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  const int n = h->host_ctrl.n, np = h->host_ctrl.np;
+  const PairArrays &L = h->s.pairs[0];
+  std::vector<int> pi(np), pj(np), tags(n), fl(np);
+  std::vector<uint8_t> sh(np);
+  if (np) {
+    CUDA_TRY(h, cudaMemcpy(pi.data(), L.i, np * sizeof(int), cudaMemcpyDeviceToHost));
+    CUDA_TRY(h, cudaMemcpy(pj.data(), L.j, np * sizeof(int), cudaMemcpyDeviceToHost));
+    CUDA_TRY(h, cudaMemcpy(sh.data(), L.sh, np, cudaMemcpyDeviceToHost));
+    CUDA_TRY(h, cudaMemcpy(fl.data(), L.flag, np * sizeof(int), cudaMemcpyDeviceToHost));
+  }
+  CUDA_TRY(h, cudaMemcpy(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost));
+  for (int p = 0; p < np; p++) {
+    if (tag_i) tag_i[p] = tags[pi[p]];
+    if (tag_j) tag_j[p] = tags[pj[p]];
+    if (shift) {
+      const int c = sh[p];
+      shift[3 * p] = c % 3 - 1;
+      shift[3 * p + 1] = (c / 3) % 3 - 1;
+      shift[3 * p + 2] = c / 9 - 1;
+    }
+    if (flag) flag[p] = fl[p];
+  }
+  if (hist && np) {
+    std::vector<double> hb(np);
+    for (int d = 0; d < kDnumShear; d++) {
+      CUDA_TRY(h, cudaMemcpy(hb.data(), L.hist + (size_t)d * h->s.pcap, np * sizeof(double),
+                             cudaMemcpyDeviceToHost));
+      for (int p = 0; p < np; p++) hist[(size_t)p * kDnumShear + d] = hb[p];
+    }
+  }
+  return DEM_OK;
+}
+
+int dem_download_wall_history(dem_handle *h, int wall_id, double *hist) {
+  if (!h || !h->have_atoms || !hist || wall_id < 0 || wall_id >= h->s.nplanes) return DEM_ERR_BAD_ARG;
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  const int n = h->host_ctrl.n;
+  std::vector<double> hb(n);
+  for (int d = 0; d < 3; d++) {
+    CUDA_TRY(h, cudaMemcpy(hb.data(), h->s.atoms[0].whist + (size_t)(wall_id * 3 + d) * h->s.nmax,
+                           n * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < n; i++) hist[3 * (size_t)i + d] = hb[i];
+  }
+  return DEM_OK;
+}
+
+int dem_get_stats(dem_handle *h, dem_stats *out) {
+  if (!h || !out) return DEM_ERR_BAD_ARG;
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  const Ctrl &c = h->host_ctrl;
+  out->ntimestep = c.ntimestep;
+  out->nrebuilds = c.nrebuilds;
+  out->npairs = c.np;
+  out->nlost = c.lost;
+  out->natoms = c.n;
+  out->device = h->device;
+  out->pair_capacity = h->s.pcap;
+  out->last_step_ms = h->last_ms;
+  return DEM_OK;
+}
+
+int dem_profile(dem_handle *h, int enable) {
+  if (!h) return DEM_ERR_BAD_ARG;
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  harvest(h);
+  h->kt = dem_kernel_times{};
+  h->profile = enable != 0;
+  if (h->profile && h->evpool.empty()) {
+    const int nev = 3 * kCheckEvery + 8;
+    h->evpool.resize(nev);
+    h->evkind.resize(nev);
+    for (auto &e : h->evpool) CUDA_TRY(h, cudaEventCreate(&e));
+  }
+  h->evused = 0;
+  return DEM_OK;
+}
+
+int dem_get_kernel_times(dem_handle *h, dem_kernel_times *out) {
+  if (!h || !out) return DEM_ERR_BAD_ARG;
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  harvest(h);
+  *out = h->kt;
+  return DEM_OK;
+}
+
+const char *dem_last_error(dem_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+}  // extern "C"

@@ -1,0 +1,773 @@
+// GB300 kernels of the sphere-DEM timestep.
+//
+// One step = k_particle (force gather of the previous step + walls + gravity +
+// nve/sphere final and initial half-kicks + skin check) -> k_decide ->
+// [rebuild kernels, no-ops unless ctrl->rebuild] -> k_pair.  All decisions
+// live in device memory (Ctrl), so many steps are queued without a host sync.
+//
+// Determinism: every force is the sum of per-pair results in a fixed order
+// (owner row ascending, then partner list ascending); no floating-point
+// atomics anywhere.  Integer atomics are only used for counting; each
+// resulting order is made canonical by a per-cell / per-atom sort.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "contact_law.cuh"
+#include "dem_device.cuh"
+#include "dem_kernels.h"
+
+namespace gb300 {
+
+#define GRID_STRIDE(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
+
+__device__ __forceinline__ bool gated(const Ctrl *c) { return c->halt != 0 || c->rebuild == 0; }
+
+// Exact reference arithmetic (no contraction) for everything that decides
+// membership of the pair set.
+__device__ __forceinline__ double rsq_rn(double dx, double dy, double dz) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+}
+
+__device__ __forceinline__ void shift_decode(int c, int &sx, int &sy, int &sz) {
+  sx = c % 3 - 1;
+  sy = (c / 3) % 3 - 1;
+  sz = c / 9 - 1;
+}
+
+// ghost image x_j + pbc*prd exactly as CommBrick::borders/forward_comm
+// (src/atom_vec_sphere.cpp:213-223): fl(x + (+-prd)) per shifted dimension.
+__device__ __forceinline__ void image(const Sys &s, int code, double &xj, double &yj, double &zj) {
+  if (code == kNoShift) return;
+  int sx, sy, sz;
+  shift_decode(code, sx, sy, sz);
+  if (sx) xj = __dadd_rn(xj, sx * s.prd[0]);
+  if (sy) yj = __dadd_rn(yj, sy * s.prd[1]);
+  if (sz) zj = __dadd_rn(zj, sz * s.prd[2]);
+}
+
+__device__ __forceinline__ int cell_coord(const Sys &s, double x, int d) {
+  int c = (int)((x - s.boxlo[d]) / s.csz[d]);
+  c = c < 0 ? 0 : c;
+  c = c >= s.nc[d] ? s.nc[d] - 1 : c;
+  return c;
+}
+
+// ----------------------------------------------------------------------------
+// step control
+// ----------------------------------------------------------------------------
+
+__global__ void k_decide(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (c->halt) return;
+  c->ntimestep++;
+  c->ago++;
+  int reb = 0;
+  if (c->ago >= s.neigh_delay && c->ago % s.neigh_every == 0) reb = s.neigh_check ? c->moved : 1;
+  c->rebuild = reb;
+  c->moved = 0;
+}
+
+__global__ void k_set_rebuild(Sys s, int v) {
+  if (s.ctrl->halt) return;
+  s.ctrl->rebuild = v;
+  s.ctrl->moved = 0;
+}
+
+__global__ void k_zero_gated(Sys s, int *a, int n) {
+  if (gated(s.ctrl)) return;
+  GRID_STRIDE(i, n) a[i] = 0;
+}
+
+// ----------------------------------------------------------------------------
+// exclusive scan (warp-shuffle prefix sums), 4096 items per block
+// ----------------------------------------------------------------------------
+
+__device__ __forceinline__ int warp_incl_scan(int x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= off) x += y;
+  }
+  return x;
+}
+
+// out[k] = sum(in[0..k-1]) within the block's 4096 items; bsum[block] = total.
+__global__ void __launch_bounds__(1024) k_scan_blocks(Sys s, const int *__restrict__ in, int *out,
+                                                      int len, int *bsum, int gate) {
+  if (gate && gated(s.ctrl)) return;
+  __shared__ int wsum[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const long base = (long)blockIdx.x * 4096 + 4 * t;
+  int v[4], tot = 0;
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    v[k] = (base + k < len) ? in[base + k] : 0;
+    tot += v[k];
+  }
+  int incl = warp_incl_scan(tot);
+  if (lane == 31) wsum[w] = incl;
+  __syncthreads();
+  if (w == 0) wsum[lane] = warp_incl_scan(wsum[lane]);
+  __syncthreads();
+  int run = incl - tot + (w ? wsum[w - 1] : 0);
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    if (base + k < len) out[base + k] = run;
+    run += v[k];
+  }
+  if (t == 1023 && bsum) bsum[blockIdx.x] = run;
+}
+
+__global__ void k_scan_add(Sys s, int *out, int len, const int *__restrict__ bsum, int gate) {
+  if (gate && gated(s.ctrl)) return;
+  const int add = bsum[blockIdx.x];
+  const long base = (long)blockIdx.x * 4096;
+  for (int k = threadIdx.x; k < 4096; k += blockDim.x)
+    if (base + k < len) out[base + k] += add;
+}
+
+// ----------------------------------------------------------------------------
+// rebuild: pbc wrap, cell sort, permutation
+// ----------------------------------------------------------------------------
+
+// Domain::pbc (src/domain.cpp:550-600) then CommBrick::exchange deletion of
+// atoms outside the box in any dimension (src/comm_brick.cpp:784-808).
+__global__ void k_cell_count(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const AtomArrays &A = s.atoms[0];
+  const int n = c->n;
+  GRID_STRIDE(i, n) {
+    double xv[3] = {A.x[i], A.y[i], A.z[i]};
+    bool lost = false;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      if (s.periodic[d]) {
+        if (xv[d] < s.boxlo[d]) xv[d] = __dadd_rn(xv[d], s.prd[d]);
+        if (xv[d] >= s.boxhi[d]) {
+          xv[d] = __dadd_rn(xv[d], -s.prd[d]);
+          if (xv[d] < s.boxlo[d]) xv[d] = s.boxlo[d];
+        }
+      }
+      if (xv[d] < s.boxlo[d] || xv[d] >= s.boxhi[d]) lost = true;
+    }
+    A.x[i] = xv[0];
+    A.y[i] = xv[1];
+    A.z[i] = xv[2];
+    int cell = s.ncell;
+    if (!lost) {
+      const int cx = cell_coord(s, xv[0], 0), cy = cell_coord(s, xv[1], 1), cz = cell_coord(s, xv[2], 2);
+      cell = cx + s.nc[0] * (cy + s.nc[1] * cz);
+    }
+    s.pcount[i] = cell;  // reused as per-atom cell id until the pair count
+    atomicAdd(&s.cell_count[cell], 1);
+  }
+}
+
+__global__ void k_cell_scatter(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const int n = c->n;
+  GRID_STRIDE(i, n) {
+    const int cell = s.pcount[i];
+    const int slot = s.cell_start[cell] + atomicAdd(&s.cell_fill[cell], 1);
+    s.order[slot] = i;
+  }
+}
+
+// canonical order inside every cell: ascending previous index
+__global__ void k_cell_sort(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  GRID_STRIDE(cell, s.ncell) {
+    const int b = s.cell_start[cell], e = s.cell_start[cell + 1];
+    for (int k = b + 1; k < e; k++) {
+      const int v = s.order[k];
+      int m = k - 1;
+      while (m >= b && s.order[m] > v) {
+        s.order[m + 1] = s.order[m];
+        m--;
+      }
+      s.order[m + 1] = v;
+    }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    c->n_new = s.cell_start[s.ncell];
+    c->lost_step = c->n - c->n_new;
+  }
+}
+
+// gather atoms into the new order (buffer 1), xhold = x, primitive-wall
+// neighbour lists (PrimitiveWall::buildNeighList, src/primitive_wall.h:129-138)
+__global__ void k_permute(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const AtomArrays &A = s.atoms[0];
+  const AtomArrays &B = s.atoms[1];
+  const int n = c->n_new;
+  GRID_STRIDE(i, n) {
+    const int o = s.order[i];
+    s.perm[i] = o;
+    const double x = A.x[o], y = A.y[o], z = A.z[o];
+    B.x[i] = x; B.y[i] = y; B.z[i] = z;
+    B.xh[i] = x; B.yh[i] = y; B.zh[i] = z;
+    B.vx[i] = A.vx[o]; B.vy[i] = A.vy[o]; B.vz[i] = A.vz[o];
+    B.wx[i] = A.wx[o]; B.wy[i] = A.wy[o]; B.wz[i] = A.wz[o];
+    B.fx[i] = A.fx[o]; B.fy[i] = A.fy[o]; B.fz[i] = A.fz[o];
+    B.tx[i] = A.tx[o]; B.ty[i] = A.ty[o]; B.tz[i] = A.tz[o];
+    const double r = A.r[o];
+    B.r[i] = r; B.m[i] = A.m[o]; B.dtfm[i] = A.dtfm[o]; B.dtir[i] = A.dtir[o];
+    B.type[i] = A.type[o]; B.tag[i] = A.tag[o];
+    uint8_t bits = 0;
+    for (int w = 0; w < s.nplanes; w++) {
+      for (int d = 0; d < 3; d++)
+        B.whist[(size_t)(w * 3 + d) * s.nmax + i] = A.whist[(size_t)(w * 3 + d) * s.nmax + o];
+      const double pos = s.planes[w].axis == 0 ? x : (s.planes[w].axis == 1 ? y : z);
+      const double dMax = r + s.skin;
+      const double dist = pos - s.planes[w].pos;
+      const double absdist = (dist > 0.0) ? dist : -dist;
+      if (absdist <= dMax) bits |= (uint8_t)(1u << w);
+    }
+    B.wbits[i] = bits;
+  }
+}
+
+__global__ void k_copy_atoms(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const AtomArrays &A = s.atoms[0];
+  const AtomArrays &B = s.atoms[1];
+  const int n = c->n_new;
+  GRID_STRIDE(i, n) {
+    A.x[i] = B.x[i]; A.y[i] = B.y[i]; A.z[i] = B.z[i];
+    A.xh[i] = B.xh[i]; A.yh[i] = B.yh[i]; A.zh[i] = B.zh[i];
+    A.vx[i] = B.vx[i]; A.vy[i] = B.vy[i]; A.vz[i] = B.vz[i];
+    A.wx[i] = B.wx[i]; A.wy[i] = B.wy[i]; A.wz[i] = B.wz[i];
+    A.fx[i] = B.fx[i]; A.fy[i] = B.fy[i]; A.fz[i] = B.fz[i];
+    A.tx[i] = B.tx[i]; A.ty[i] = B.ty[i]; A.tz[i] = B.tz[i];
+    A.r[i] = B.r[i]; A.m[i] = B.m[i]; A.dtfm[i] = B.dtfm[i]; A.dtir[i] = B.dtir[i];
+    A.type[i] = B.type[i]; A.tag[i] = B.tag[i];
+    for (int w = 0; w < s.nplanes; w++)
+      for (int d = 0; d < 3; d++)
+        A.whist[(size_t)(w * 3 + d) * s.nmax + i] = B.whist[(size_t)(w * 3 + d) * s.nmax + i];
+    A.wbits[i] = B.wbits[i];
+  }
+}
+
+// ----------------------------------------------------------------------------
+// rebuild: granular half list (Neighbor::granular_bin_no_newton,
+// src/neigh_gran.cpp:485-644), 27-cell stencil with periodic images.
+// ----------------------------------------------------------------------------
+
+template <bool FILL>
+__global__ void k_pairs(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const AtomArrays &A = s.atoms[0];
+  const PairArrays &L = s.pairs[0];  // old list (old atom order)
+  const PairArrays &M = s.pairs[1];  // new list
+  const int n = c->n_new;
+  const int total = FILL ? n : s.nmax + 1;
+  GRID_STRIDE(i, total) {
+    if (!FILL && i >= n) {
+      s.pcount[i] = 0;
+      continue;
+    }
+    const double xi = A.x[i], yi = A.y[i], zi = A.z[i];
+    const double radi = A.r[i];
+    const double mi = A.m[i];
+    const int ci[3] = {cell_coord(s, xi, 0), cell_coord(s, yi, 1), cell_coord(s, zi, 2)};
+    int cnt = 0;
+    int out = FILL ? M.row[i] : 0;
+    for (int oz = -1; oz <= 1; oz++) {
+      for (int oy = -1; oy <= 1; oy++) {
+        for (int ox = -1; ox <= 1; ox++) {
+          const int o[3] = {ox, oy, oz};
+          int cc[3], sv[3] = {0, 0, 0};
+          bool skip = false;
+#pragma unroll
+          for (int d = 0; d < 3; d++) {
+            cc[d] = ci[d] + o[d];
+            if (s.nc[d] == 1 && o[d] != 0) skip = true;
+            if (cc[d] < 0) {
+              if (!s.periodic[d]) skip = true;
+              cc[d] += s.nc[d];
+              sv[d] = -1;
+            } else if (cc[d] >= s.nc[d]) {
+              if (!s.periodic[d]) skip = true;
+              cc[d] -= s.nc[d];
+              sv[d] = 1;
+            }
+          }
+          if (skip) continue;
+          const int code = (sv[0] + 1) + 3 * (sv[1] + 1) + 9 * (sv[2] + 1);
+          const int cell = cc[0] + s.nc[0] * (cc[1] + s.nc[1] * cc[2]);
+          const int jb = s.cell_start[cell], je = s.cell_start[cell + 1];
+          for (int j = jb; j < je; j++) {
+            if (code == kNoShift && j <= i) continue;
+            double xj = A.x[j], yj = A.y[j], zj = A.z[j];
+            image(s, code, xj, yj, zj);
+            const double delx = __dadd_rn(xi, -xj);
+            const double dely = __dadd_rn(yi, -yj);
+            const double delz = __dadd_rn(zi, -zj);
+            const double rsq = rsq_rn(delx, dely, delz);
+            const double radj = A.r[j];
+            const double radsum = __dmul_rn(__dadd_rn(radi, radj), s.cdf);
+            const double cs = __dadd_rn(radsum, s.skin);
+            if (!(rsq <= __dmul_rn(cs, cs))) continue;
+            if (!FILL) {
+              cnt++;
+              continue;
+            }
+            // history carry-over: partner lookup by identity in the old list
+            // (FixContactHistory::pre_exchange + the partner search of
+            // src/neigh_gran.cpp:590-620); j-side copies are negated.
+            double h0 = 0.0, h1 = 0.0, h2 = 0.0;
+            int flag = 0;
+            if (rsq < __dmul_rn(radsum, radsum)) {
+              const int oi = s.perm[i], oj = s.perm[j];
+              bool found = false;
+              for (int q = L.row[oi]; q < L.row[oi + 1]; q++) {
+                if (L.j[q] == oj && L.flag[q] != 0) {
+                  h0 = L.hist[q];
+                  h1 = L.hist[(size_t)s.pcap + q];
+                  h2 = L.hist[2 * (size_t)s.pcap + q];
+                  found = true;
+                  break;
+                }
+              }
+              if (!found) {
+                for (int k = L.rev_start[oi]; k < L.rev_start[oi + 1]; k++) {
+                  const int q = L.rev[k];
+                  if (L.i[q] == oj && L.flag[q] != 0) {
+                    h0 = -L.hist[q];
+                    h1 = -L.hist[(size_t)s.pcap + q];
+                    h2 = -L.hist[2 * (size_t)s.pcap + q];
+                    found = true;
+                    break;
+                  }
+                }
+              }
+              flag = found ? 1 : 0;
+            }
+            const int p = out++;
+            M.i[p] = i;
+            M.j[p] = j;
+            M.sh[p] = (uint8_t)code;
+            M.flag[p] = flag;
+            M.hist[p] = h0;
+            M.hist[(size_t)s.pcap + p] = h1;
+            M.hist[2 * (size_t)s.pcap + p] = h2;
+            const double mj = A.m[j];
+            M.meff[p] = mi * mj / (mi + mj);
+            M.reff[p] = radi * radj / (radi + radj);
+            if (code == kNoShift) atomicAdd(&s.rev_count[j], 1);
+          }
+        }
+      }
+    }
+    if (!FILL) s.pcount[i] = cnt;
+  }
+}
+
+// after the pair-count scan: capacity check; halts on overflow
+__global__ void k_pairs_total(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const int np = s.pairs[1].row[s.nmax];
+  c->np_new = np;
+  if (np > s.pcap) {
+    c->status = kStatPairOverflow;
+    c->halt = 1;
+    c->halt_step = 1;
+  }
+}
+
+__global__ void k_rev_fill(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const PairArrays &M = s.pairs[1];
+  const int np = c->np_new;
+  GRID_STRIDE(p, np) {
+    if (M.sh[p] != kNoShift) continue;
+    const int j = M.j[p];
+    M.rev[M.rev_start[j] + atomicAdd(&s.rev_fill[j], 1)] = p;
+  }
+}
+
+__global__ void k_rev_sort(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const PairArrays &M = s.pairs[1];
+  const int n = c->n_new;
+  GRID_STRIDE(i, n) {
+    const int b = M.rev_start[i], e = M.rev_start[i + 1];
+    for (int k = b + 1; k < e; k++) {
+      const int v = M.rev[k];
+      int m = k - 1;
+      while (m >= b && M.rev[m] > v) {
+        M.rev[m + 1] = M.rev[m];
+        m--;
+      }
+      M.rev[m + 1] = v;
+    }
+  }
+}
+
+__global__ void k_copy_pairs(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const PairArrays &L = s.pairs[0];
+  const PairArrays &M = s.pairs[1];
+  const int np = c->np_new;
+  const int nrow = s.nmax + 1;
+  const int tot = np > nrow ? np : nrow;
+  GRID_STRIDE(p, tot) {
+    if (p < np) {
+      L.i[p] = M.i[p];
+      L.j[p] = M.j[p];
+      L.sh[p] = M.sh[p];
+      L.flag[p] = M.flag[p];
+      L.hist[p] = M.hist[p];
+      L.hist[(size_t)s.pcap + p] = M.hist[(size_t)s.pcap + p];
+      L.hist[2 * (size_t)s.pcap + p] = M.hist[2 * (size_t)s.pcap + p];
+      L.meff[p] = M.meff[p];
+      L.reff[p] = M.reff[p];
+      L.rev[p] = M.rev[p];
+    }
+    if (p < nrow) {
+      L.row[p] = M.row[p];
+      L.rev_start[p] = M.rev_start[p];
+    }
+  }
+}
+
+__global__ void k_finish_rebuild(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  c->lost += c->lost_step;
+  c->n = c->n_new;
+  c->np = c->np_new;
+  c->nrebuilds++;
+  c->ago = 0;
+}
+
+// ----------------------------------------------------------------------------
+// pair forces: one thread per half-list entry, results to the pair buffer
+// ----------------------------------------------------------------------------
+
+template <int NORMAL, bool ROLL>
+__global__ void __launch_bounds__(256) k_pair(Sys s, int shearupdate) {
+  Ctrl *c = s.ctrl;
+  if (c->halt) return;
+  const AtomArrays &A = s.atoms[0];
+  const PairArrays &L = s.pairs[0];
+  const int np = c->np;
+  const size_t P = s.pcap;
+  const double cdm = s.cdf * s.cdf;
+  GRID_STRIDE(p, np) {
+    const int i = L.i[p], j = L.j[p];
+    const int code = L.sh[p];
+    const double xi = A.x[i], yi = A.y[i], zi = A.z[i];
+    double xj = A.x[j], yj = A.y[j], zj = A.z[j];
+    image(s, code, xj, yj, zj);
+    const double delx = __dadd_rn(xi, -xj);
+    const double dely = __dadd_rn(yi, -yj);
+    const double delz = __dadd_rn(zi, -zj);
+    const double rsq = rsq_rn(delx, dely, delz);
+    const double radi = A.r[i], radj = A.r[j];
+    const double radsum = __dadd_rn(radi, radj);
+    const double rs2 = __dmul_rn(radsum, radsum);
+    if (rsq < rs2) {
+      ContactIn ci;
+      ci.radi = radi;
+      ci.radj = radj;
+      ci.radsum = radsum;
+      ci.r = sqrt(rsq);
+      ci.rinv = 1.0 / ci.r;
+      ci.meff = L.meff[p];
+      ci.reff = L.reff[p];
+      ci.d[0] = delx;
+      ci.d[1] = dely;
+      ci.d[2] = delz;
+      ci.en[0] = delx * ci.rinv;
+      ci.en[1] = dely * ci.rinv;
+      ci.en[2] = delz * ci.rinv;
+      ci.vr[0] = A.vx[i] - A.vx[j];
+      ci.vr[1] = A.vy[i] - A.vy[j];
+      ci.vr[2] = A.vz[i] - A.vz[j];
+      ci.wi[0] = A.wx[i]; ci.wi[1] = A.wy[i]; ci.wi[2] = A.wz[i];
+      ci.wj[0] = A.wx[j]; ci.wj[1] = A.wy[j]; ci.wj[2] = A.wz[j];
+      ci.deltan_wall = 0.0;
+      const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], A.type[j]);
+      double sh3[3] = {L.hist[p], L.hist[P + p], L.hist[2 * P + p]};
+      ContactOut o;
+      contact_law<NORMAL, false>(ci, tp, s.dt, s.charVel, s.tdamp, s.limitf, ROLL,
+                                 shearupdate != 0, sh3, o);
+      if (shearupdate) {
+        L.hist[p] = sh3[0];
+        L.hist[P + p] = sh3[1];
+        L.hist[2 * P + p] = sh3[2];
+      }
+      L.flag[p] |= (kContactNormal | kContactTangential);
+      s.resF[p] = o.F[0]; s.resF[P + p] = o.F[1]; s.resF[2 * P + p] = o.F[2];
+      s.resTi[p] = o.Ti[0]; s.resTi[P + p] = o.Ti[1]; s.resTi[2 * P + p] = o.Ti[2];
+      s.resTj[p] = o.Tj[0]; s.resTj[P + p] = o.Tj[1]; s.resTj[2 * P + p] = o.Tj[2];
+      s.active[p] = 1;
+    } else {
+      s.active[p] = 0;
+      if (rsq < __dmul_rn(__dmul_rn(cdm, radsum), radsum)) {
+        // TangentialModel<TANGENTIAL_HISTORY>::surfacesClose
+        L.flag[p] &= ~kContactTangential;
+        L.hist[p] = 0.0;
+        L.hist[P + p] = 0.0;
+        L.hist[2 * P + p] = 0.0;
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// per-atom kernel: force gather + gravity + primitive walls + nve/sphere
+// ----------------------------------------------------------------------------
+
+template <int NORMAL>
+__device__ __forceinline__ void plane_contact(const Sys &s, const AtomArrays &A, int i, int w,
+                                              int shearupdate, double v[3], double om[3],
+                                              double xv[3], double &fx, double &fy, double &fz,
+                                              double &tx, double &ty, double &tz) {
+  const Plane &pl = s.planes[w];
+  const int ax = pl.axis, ay = (ax + 1) % 3, az = (ax + 2) % 3;
+  const double radi = A.r[i];
+  double delta[3];
+  double deltan;
+  // Plane<dim>::resolveContact, src/primitive_wall_definitions.h:123-140
+  if (xv[ax] > pl.pos) {
+    delta[ax] = pl.pos - xv[ax];
+    deltan = xv[ax] - pl.pos - radi;
+  } else {
+    delta[ax] = pl.pos - xv[ax];
+    deltan = pl.pos - xv[ax] - radi;
+  }
+  delta[ay] = 0.;
+  delta[az] = 0.;
+  if (deltan > s.cutneighmax) return;
+  double *h = A.whist + (size_t)(w * 3) * s.nmax + i;
+  const size_t hs = s.nmax;
+  const double cdm1 = s.cdf - 1.0;
+  if (deltan <= 0 || deltan < cdm1 * radi) {
+    if (deltan <= 0) {
+      ContactIn ci;
+      ci.radi = radi;
+      ci.radj = 0.0;
+      ci.deltan_wall = -deltan;
+      ci.d[0] = -delta[0];
+      ci.d[1] = -delta[1];
+      ci.d[2] = -delta[2];
+      ci.r = radi - ci.deltan_wall;
+      ci.rinv = 1.0 / ci.r;
+      ci.en[0] = ci.d[0] * ci.rinv;
+      ci.en[1] = ci.d[1] * ci.rinv;
+      ci.en[2] = ci.d[2] * ci.rinv;
+      ci.radsum = radi;
+      ci.meff = A.m[i];
+      ci.reff = radi;
+      ci.vr[0] = v[0] - 0.0;
+      ci.vr[1] = v[1] - 0.0;
+      ci.vr[2] = v[2] - 0.0;
+      ci.wi[0] = om[0]; ci.wi[1] = om[1]; ci.wi[2] = om[2];
+      ci.wj[0] = ci.wj[1] = ci.wj[2] = 0.0;
+      const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], pl.wall_type);
+      double sh3[3] = {h[0], h[hs], h[2 * hs]};
+      ContactOut o;
+      contact_law<NORMAL, true>(ci, tp, s.dt, s.charVel, s.tdamp, s.limitf, pl.rolling != 0,
+                                shearupdate != 0, sh3, o);
+      if (shearupdate) {
+        h[0] = sh3[0];
+        h[hs] = sh3[1];
+        h[2 * hs] = sh3[2];
+      }
+      fx += o.F[0]; fy += o.F[1]; fz += o.F[2];
+      tx += o.Ti[0]; ty += o.Ti[1]; tz += o.Ti[2];
+    } else {
+      h[0] = 0.0; h[hs] = 0.0; h[2 * hs] = 0.0;  // surfacesClose
+    }
+  } else {
+    h[0] = 0.0; h[hs] = 0.0; h[2 * hs] = 0.0;
+  }
+}
+
+template <int NORMAL, bool GATHER, bool FINAL, bool INITIAL>
+__global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
+  Ctrl *c = s.ctrl;
+  if (c->halt) return;
+  const AtomArrays &A = s.atoms[0];
+  const PairArrays &L = s.pairs[0];
+  const int n = c->n;
+  const size_t P = s.pcap;
+  const double dtv = s.dt;
+  const double trigger = 0.25 * s.skin * s.skin;
+  bool moved = false, bad = false;
+  GRID_STRIDE(i, n) {
+    double fx, fy, fz, tx, ty, tz;
+    double v[3] = {A.vx[i], A.vy[i], A.vz[i]};
+    double om[3] = {A.wx[i], A.wy[i], A.wz[i]};
+    double xv[3] = {A.x[i], A.y[i], A.z[i]};
+    if (GATHER) {
+      fx = fy = fz = tx = ty = tz = 0.0;
+      const int pb = L.row[i], pe = L.row[i + 1];
+      for (int p = pb; p < pe; p++) {
+        if (!s.active[p]) continue;
+        fx += s.resF[p]; fy += s.resF[P + p]; fz += s.resF[2 * P + p];
+        tx += s.resTi[p]; ty += s.resTi[P + p]; tz += s.resTi[2 * P + p];
+      }
+      const int rb = L.rev_start[i], re = L.rev_start[i + 1];
+      for (int k = rb; k < re; k++) {
+        const int p = L.rev[k];
+        if (!s.active[p]) continue;
+        fx -= s.resF[p]; fy -= s.resF[P + p]; fz -= s.resF[2 * P + p];
+        tx += s.resTj[p]; ty += s.resTj[P + p]; tz += s.resTj[2 * P + p];
+      }
+      if (s.gravity_on) {
+        const double massone = A.m[i] * 1.;
+        fx += massone * s.g[0];
+        fy += massone * s.g[1];
+        fz += massone * s.g[2];
+      }
+      const uint8_t bits = A.wbits[i];
+      if (bits) {
+        for (int w = 0; w < s.nplanes; w++)
+          if (bits & (1u << w))
+            plane_contact<NORMAL>(s, A, i, w, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz);
+      }
+      A.fx[i] = fx; A.fy[i] = fy; A.fz[i] = fz;
+      A.tx[i] = tx; A.ty[i] = ty; A.tz[i] = tz;
+    } else {
+      fx = A.fx[i]; fy = A.fy[i]; fz = A.fz[i];
+      tx = A.tx[i]; ty = A.ty[i]; tz = A.tz[i];
+    }
+    if (FINAL || INITIAL) {
+      const double dtfm = A.dtfm[i], dtir = A.dtir[i];
+      if (FINAL) {
+        v[0] += dtfm * fx; v[1] += dtfm * fy; v[2] += dtfm * fz;
+        om[0] += dtir * tx; om[1] += dtir * ty; om[2] += dtir * tz;
+      }
+      if (INITIAL) {
+        v[0] += dtfm * fx; v[1] += dtfm * fy; v[2] += dtfm * fz;
+        xv[0] += dtv * v[0]; xv[1] += dtv * v[1]; xv[2] += dtv * v[2];
+        om[0] += dtir * tx; om[1] += dtir * ty; om[2] += dtir * tz;
+        A.x[i] = xv[0]; A.y[i] = xv[1]; A.z[i] = xv[2];
+        const double dx = __dadd_rn(xv[0], -A.xh[i]);
+        const double dy = __dadd_rn(xv[1], -A.yh[i]);
+        const double dz = __dadd_rn(xv[2], -A.zh[i]);
+        if (rsq_rn(dx, dy, dz) > trigger) moved = true;
+        if (!isfinite(xv[0] + xv[1] + xv[2])) bad = true;
+      }
+      A.vx[i] = v[0]; A.vy[i] = v[1]; A.vz[i] = v[2];
+      A.wx[i] = om[0]; A.wy[i] = om[1]; A.wz[i] = om[2];
+    }
+  }
+  if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(&c->moved, 1);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) {
+    atomicExch(&c->status, kStatNan);
+  }
+}
+
+// ----------------------------------------------------------------------------
+// launchers
+// ----------------------------------------------------------------------------
+
+static inline int grid_for(long n, int block, int cap) {
+  long g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > cap) g = cap;
+  return (int)g;
+}
+
+int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, bool gate,
+                   cudaStream_t st) {
+  const int nb = (len + 4095) / 4096;
+  k_scan_blocks<<<nb, 1024, 0, st>>>(s, in, out, len, tmp, gate);
+  if (nb > 1) {
+    // nb <= 4096: one block scans the block totals in place
+    k_scan_blocks<<<1, 1024, 0, st>>>(s, tmp, tmp, nb, nullptr, gate);
+    k_scan_add<<<nb, 256, 0, st>>>(s, out, len, tmp, gate);
+    return 3;
+  }
+  return 1;
+}
+
+int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage) {
+  int nl = 0;
+  const int B = 256;
+  const int gN = grid_for(s.nmax + 1, B, lc.max_grid);
+  const int gC = grid_for(s.ncell + 2, B, lc.max_grid);
+  const int gP = grid_for(s.pcap, B, lc.max_grid);
+  if (stage <= 0) {
+    k_zero_gated<<<gC, B, 0, st>>>(s, s.cell_count, s.ncell + 2);
+    k_zero_gated<<<gC, B, 0, st>>>(s, s.cell_fill, s.ncell + 2);
+    k_cell_count<<<gN, B, 0, st>>>(s);
+    nl += 3 + scan_exclusive(s, s.cell_count, s.cell_start, s.ncell + 2, s.scan_tmp, true, st);
+    k_cell_scatter<<<gN, B, 0, st>>>(s);
+    k_cell_sort<<<gC, B, 0, st>>>(s);
+    k_permute<<<gN, B, 0, st>>>(s);
+    k_copy_atoms<<<gN, B, 0, st>>>(s);
+    k_pairs<false><<<gN, B, 0, st>>>(s);
+    nl += 5 + scan_exclusive(s, s.pcount, s.pairs[1].row, s.nmax + 1, s.scan_tmp, true, st);
+    k_pairs_total<<<1, 1, 0, st>>>(s);
+    nl += 1;
+  }
+  // stage 1: resumes here after a pair-capacity overflow was fixed by the host
+  k_zero_gated<<<gN, B, 0, st>>>(s, s.rev_count, s.nmax + 1);
+  k_zero_gated<<<gN, B, 0, st>>>(s, s.rev_fill, s.nmax + 1);
+  k_pairs<true><<<gN, B, 0, st>>>(s);
+  nl += 3 + scan_exclusive(s, s.rev_count, s.pairs[1].rev_start, s.nmax + 1, s.scan_tmp, true, st);
+  k_rev_fill<<<gP, B, 0, st>>>(s);
+  k_rev_sort<<<gN, B, 0, st>>>(s);
+  k_copy_pairs<<<grid_for((long)s.pcap > s.nmax + 1 ? s.pcap : s.nmax + 1, B, lc.max_grid), B, 0, st>>>(s);
+  k_finish_rebuild<<<1, 1, 0, st>>>(s);
+  return nl + 4;
+}
+
+int launch_decide(const Sys &s, cudaStream_t st) {
+  k_decide<<<1, 1, 0, st>>>(s);
+  return 1;
+}
+int launch_set_rebuild(const Sys &s, int v, cudaStream_t st) {
+  k_set_rebuild<<<1, 1, 0, st>>>(s, v);
+  return 1;
+}
+
+int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t st) {
+  const int B = 256;
+  const int g = grid_for(s.pcap, B, lc.max_grid);
+  if (s.normal == kHertz) {
+    if (s.rolling) k_pair<kHertz, true><<<g, B, 0, st>>>(s, shearupdate);
+    else k_pair<kHertz, false><<<g, B, 0, st>>>(s, shearupdate);
+  } else {
+    if (s.rolling) k_pair<kHooke, true><<<g, B, 0, st>>>(s, shearupdate);
+    else k_pair<kHooke, false><<<g, B, 0, st>>>(s, shearupdate);
+  }
+  return 1;
+}
+
+template <int NORMAL>
+static void launch_particle_n(const Sys &s, int g, int mode, int shearupdate, cudaStream_t st) {
+  const int B = 256;
+  switch (mode) {
+    case kModeInitial: k_particle<NORMAL, false, false, true><<<g, B, 0, st>>>(s, shearupdate); break;
+    case kModeGather: k_particle<NORMAL, true, false, false><<<g, B, 0, st>>>(s, shearupdate); break;
+    case kModeGatherFinal: k_particle<NORMAL, true, true, false><<<g, B, 0, st>>>(s, shearupdate); break;
+    case kModeGatherFinalInitial: k_particle<NORMAL, true, true, true><<<g, B, 0, st>>>(s, shearupdate); break;
+  }
+}
+
+int launch_particle(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, cudaStream_t st) {
+  const int g = grid_for(s.nmax, 256, lc.max_grid);
+  if (s.normal == kHertz) launch_particle_n<kHertz>(s, g, mode, shearupdate, st);
+  else launch_particle_n<kHooke>(s, g, mode, shearupdate, st);
+  return 1;
+}
+
+}  // namespace gb300

@@ -1,0 +1,27 @@
+// Host-side launchers of the sphere-DEM kernels (dem_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "dem_device.cuh"
+
+namespace gb300 {
+
+struct LaunchCfg {
+  int max_grid;  // grid-stride kernels never launch more blocks than this
+};
+
+enum {
+  kModeInitial = 0,             // nve/sphere initial_integrate only (first step of a call)
+  kModeGather = 1,              // sum forces only (setup)
+  kModeGatherFinal = 2,         // sum forces + final_integrate (last step of a call)
+  kModeGatherFinalInitial = 3,  // sum forces + final(n) + initial(n+1) (steady state)
+};
+
+int launch_decide(const Sys &s, cudaStream_t st);
+int launch_set_rebuild(const Sys &s, int v, cudaStream_t st);
+// stage 0: full rebuild; stage 1: resume after a pair-capacity overflow
+int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage);
+int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t st);
+int launch_particle(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, cudaStream_t st);
+
+}  // namespace gb300

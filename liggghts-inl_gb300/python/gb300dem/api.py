@@ -1,0 +1,214 @@
+"""ctypes binding of the C ABI in include/liggghts_gb300.h (libdemgpu.so).
+
+``DemSystem`` mirrors the reference's run semantics: ``setup()`` is
+Verlet::setup (neighbour build + forces without history update) and
+``step(n)`` runs n Verlet iterations.  It raises if the CUDA library is not
+built or no GPU is present: there is no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import build as _build
+
+HEADER = os.path.join(os.path.dirname(_build.PKG), "include", "liggghts_gb300.h")
+
+STATUS = {0: "DEM_OK", 1: "DEM_ERR_BAD_ARG", 2: "DEM_ERR_CUDA", 3: "DEM_ERR_NEIGH_OVERFLOW",
+          4: "DEM_ERR_NAN", 5: "DEM_ERR_TIMEOUT", 6: "DEM_ERR_BOX", 7: "DEM_ERR_UNSUPPORTED",
+          8: "DEM_ERR_NO_DEVICE"}
+
+
+class DemConfig(ctypes.Structure):
+    _fields_ = [("boxlo", ctypes.c_double * 3), ("boxhi", ctypes.c_double * 3),
+                ("periodic", ctypes.c_int * 3), ("dt", ctypes.c_double),
+                ("skin", ctypes.c_double), ("contact_distance_factor", ctypes.c_double),
+                ("neigh_every", ctypes.c_int), ("neigh_delay", ctypes.c_int),
+                ("neigh_check", ctypes.c_int), ("normal_model", ctypes.c_int),
+                ("rolling_model", ctypes.c_int), ("cohesion_model", ctypes.c_int),
+                ("tangential_damping", ctypes.c_int), ("limit_force", ctypes.c_int),
+                ("gravity_on", ctypes.c_int), ("gravity", ctypes.c_double * 3)]
+
+
+class DemStats(ctypes.Structure):
+    _fields_ = [("ntimestep", ctypes.c_longlong), ("nrebuilds", ctypes.c_longlong),
+                ("npairs", ctypes.c_longlong), ("nlost", ctypes.c_longlong),
+                ("natoms", ctypes.c_longlong), ("device", ctypes.c_int),
+                ("pair_capacity", ctypes.c_int), ("last_step_ms", ctypes.c_double)]
+
+
+class DemKernelTimes(ctypes.Structure):
+    _fields_ = [("pair_ms", ctypes.c_double), ("pair_launches", ctypes.c_longlong),
+                ("particle_ms", ctypes.c_double), ("particle_launches", ctypes.c_longlong),
+                ("neigh_ms", ctypes.c_double), ("neigh_stages", ctypes.c_longlong),
+                ("kernel_launches", ctypes.c_longlong)]
+
+
+_lib = None
+P = ctypes.c_void_p
+
+
+def load(build=True):
+    """Loads libdemgpu.so (building it first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.build() if build else _build.LIB
+    L = ctypes.CDLL(path)
+    I = ctypes.c_int
+    L.dem_create.argtypes = [ctypes.POINTER(DemConfig), ctypes.POINTER(P)]
+    L.dem_destroy.argtypes = [P]
+    L.dem_set_pair_params.argtypes = [P, I] + [P] * 6 + [ctypes.c_double]
+    L.dem_derive_hertz_tables.argtypes = [I] + [P] * 7
+    L.dem_add_plane.argtypes = [P, I, ctypes.c_double, I, I, P]
+    L.dem_upload_atoms.argtypes = [P, I] + [P] * 7
+    L.dem_setup.argtypes = [P]
+    L.dem_step.argtypes = [P, I]
+    L.dem_natoms.argtypes = [P, P]
+    L.dem_download_atoms.argtypes = [P] + [P] * 9
+    L.dem_npairs.argtypes = [P, P, P]
+    L.dem_download_contacts.argtypes = [P] + [P] * 5
+    L.dem_download_wall_history.argtypes = [P, I, P]
+    L.dem_get_stats.argtypes = [P, ctypes.POINTER(DemStats)]
+    L.dem_last_error.argtypes = [P]
+    L.dem_last_error.restype = ctypes.c_char_p
+    L.dem_version.restype = ctypes.c_char_p
+    L.dem_profile.argtypes = [P, I]
+    L.dem_get_kernel_times.argtypes = [P, ctypes.POINTER(DemKernelTimes)]
+    L.dem_measure_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    _lib = L
+    return L
+
+
+def fp64_peak_tflops():
+    """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
+    v = ctypes.c_double()
+    rc = load().dem_measure_fp64_peak(ctypes.byref(v))
+    if rc != 0:
+        raise DemError("dem_measure_fp64_peak: %s" % STATUS.get(rc, rc))
+    return v.value
+
+
+def _p(a):
+    return a.ctypes.data_as(P) if a is not None else None
+
+
+class DemError(RuntimeError):
+    pass
+
+
+class DemSystem:
+    """One resident granular system on the GPU (one C-ABI handle)."""
+
+    def __init__(self, case):
+        L = load()
+        c = DemConfig()
+        c.boxlo[:] = case["boxlo"]
+        c.boxhi[:] = case["boxhi"]
+        c.periodic[:] = case["periodic"]
+        c.dt = case["dt"]
+        c.skin = case["skin"]
+        c.contact_distance_factor = case.get("cdf", 1.0)
+        c.neigh_every, c.neigh_delay, c.neigh_check = case.get("neigh", (1, 0, 1))
+        c.normal_model = case.get("normal_model", 0)
+        c.rolling_model = case.get("rolling_model", 0)
+        c.cohesion_model = case.get("cohesion_model", 0)
+        c.tangential_damping = 1
+        c.limit_force = 0
+        g = case.get("gravity")
+        c.gravity_on = 1 if g is not None else 0
+        c.gravity[:] = g if g is not None else (0.0, 0.0, 0.0)
+        h = P()
+        rc = L.dem_create(ctypes.byref(c), ctypes.byref(h))
+        if rc != 0:
+            raise DemError("dem_create: %s" % STATUS.get(rc, rc))
+        self.h = h
+        nt = int(case["ntypes"])
+        tabs = [np.ascontiguousarray(case[k], dtype=np.float64).reshape(nt + 1, nt + 1)
+                for k in ("Yeff", "Geff", "betaeff", "coeffFrict", "coeffRollFrict", "coeffRestLog")]
+        self._check(L.dem_set_pair_params(self.h, nt, *[_p(a) for a in tabs],
+                                          float(case.get("charVel", 0.0))))
+        for (axis, pos, wtype, roll) in case.get("planes", []):
+            self._check(L.dem_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll), None))
+        if "atoms" in case:
+            self.upload(case["atoms"])
+
+    def _check(self, rc):
+        if rc != 0:
+            msg = load().dem_last_error(self.h).decode() if getattr(self, "h", None) else ""
+            raise DemError("%s: %s" % (STATUS.get(rc, rc), msg))
+
+    def upload(self, a):
+        n = len(a["tag"])
+        arrs = [np.ascontiguousarray(a[k], dtype=t) for k, t in
+                (("tag", np.int32), ("type", np.int32), ("x", np.float64), ("v", np.float64),
+                 ("omega", np.float64), ("radius", np.float64), ("rmass", np.float64))]
+        self._check(load().dem_upload_atoms(self.h, n, *[_p(x) for x in arrs]))
+
+    def setup(self):
+        self._check(load().dem_setup(self.h))
+
+    def step(self, n):
+        self._check(load().dem_step(self.h, int(n)))
+
+    run = step
+
+    def natoms(self):
+        n = ctypes.c_int()
+        self._check(load().dem_natoms(self.h, ctypes.byref(n)))
+        return n.value
+
+    def atoms(self):
+        n = self.natoms()
+        out = dict(tag=np.zeros(n, np.int32), type=np.zeros(n, np.int32),
+                   x=np.zeros((n, 3)), v=np.zeros((n, 3)), omega=np.zeros((n, 3)),
+                   f=np.zeros((n, 3)), torque=np.zeros((n, 3)), radius=np.zeros(n),
+                   rmass=np.zeros(n))
+        self._check(load().dem_download_atoms(self.h, *[_p(out[k]) for k in (
+            "tag", "type", "x", "v", "omega", "f", "torque", "radius", "rmass")]))
+        return out
+
+    def pairs(self):
+        L = load()
+        n, d = ctypes.c_int(), ctypes.c_int()
+        self._check(L.dem_npairs(self.h, ctypes.byref(n), ctypes.byref(d)))
+        n, d = n.value, d.value
+        out = dict(tag_i=np.zeros(n, np.int32), tag_j=np.zeros(n, np.int32),
+                   shift=np.zeros((n, 3), np.int32), flag=np.zeros(n, np.int32),
+                   hist=np.zeros((n, d)))
+        self._check(L.dem_download_contacts(self.h, *[_p(out[k]) for k in
+                                                      ("tag_i", "tag_j", "shift", "flag", "hist")]))
+        return out
+
+    def wall_history(self, w):
+        h = np.zeros((self.natoms(), 3))
+        self._check(load().dem_download_wall_history(self.h, int(w), _p(h)))
+        return h
+
+    def stats(self):
+        s = DemStats()
+        self._check(load().dem_get_stats(self.h, ctypes.byref(s)))
+        return {k: getattr(s, k) for k, _ in DemStats._fields_}
+
+    def profile(self, enable=True):
+        self._check(load().dem_profile(self.h, 1 if enable else 0))
+
+    def kernel_times(self):
+        t = DemKernelTimes()
+        self._check(load().dem_get_kernel_times(self.h, ctypes.byref(t)))
+        return {k: getattr(t, k) for k, _ in DemKernelTimes._fields_}
+
+    @property
+    def nrebuilds(self):
+        return self.stats()["nrebuilds"]
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().dem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
