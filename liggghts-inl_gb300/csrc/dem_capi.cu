@@ -20,7 +20,9 @@ using namespace gb300;
 
 namespace {
 constexpr int kCheckEvery = 256;
-constexpr long kMaxCells = 1L << 26;
+// the two-level exclusive scan covers 4096 * 4096 items
+constexpr long kMaxScan = 4096L * 4096L - 2;
+constexpr long kMaxCells = 16000000L;
 }  // namespace
 
 struct dem_handle {
@@ -346,8 +348,13 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
   if (!h || n < 1 || !tag || !type || !x || !v || !omega || !radius || !rmass) return DEM_ERR_BAD_ARG;
   if (!h->have_params) return fail(h, DEM_ERR_BAD_ARG, "set pair parameters first");
   Sys &s = h->s;
+  if ((long)n > kMaxScan) return fail(h, DEM_ERR_BAD_ARG, "too many atoms for one handle");
   for (int i = 0; i < n; i++)
     if (type[i] < 1 || type[i] > s.ntypes) return fail(h, DEM_ERR_BAD_ARG, "atom type out of range");
+  for (int w = 0; w < s.nplanes; w++)
+    if (s.planes[w].wall_type > s.ntypes) return fail(h, DEM_ERR_BAD_ARG, "wall type out of range");
+  for (int i = 0; i < n; i++)
+    if (!(radius[i] > 0.0) || !(rmass[i] > 0.0)) return fail(h, DEM_ERR_BAD_ARG, "radius and rmass must be > 0");
   // cutneighmax = (maxrad_i + maxrad_j)*cdf + skin, src/pair_gran.cpp:591-602,
   // src/neighbor.cpp:316-337
   double maxrad = 0.0;

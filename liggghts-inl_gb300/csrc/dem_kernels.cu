@@ -280,6 +280,7 @@ __global__ void k_pairs(Sys s) {
     const int ci[3] = {cell_coord(s, xi, 0), cell_coord(s, yi, 1), cell_coord(s, zi, 2)};
     int cnt = 0;
     int out = FILL ? M.row[i] : 0;
+    const int out_end = FILL ? M.row[i + 1] : 0;
     for (int oz = -1; oz <= 1; oz++) {
       for (int oy = -1; oy <= 1; oy++) {
         for (int ox = -1; ox <= 1; ox++) {
@@ -320,6 +321,7 @@ __global__ void k_pairs(Sys s) {
               cnt++;
               continue;
             }
+            if (out >= out_end) continue;  // count and fill passes agree; guard only
             // history carry-over: partner lookup by identity in the old list
             // (FixContactHistory::pre_exchange + the partner search of
             // src/neigh_gran.cpp:590-620); j-side copies are negated.
