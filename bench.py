@@ -180,7 +180,7 @@ def run_gb300(args):
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-    case, desc = workload(args.workload, seed=2024 + rank)
+    case, desc = workload(args.workload, scale=args.scale, seed=2024 + rank)
     n = len(case["atoms"]["tag"])
     g = api.DemSystem(case)
     g.setup()
@@ -293,6 +293,8 @@ def main():
     ap.add_argument("--workload", default="column1m")
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0,
+                    help="fraction of the workload's atoms (small cases for ncu captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -107,6 +107,19 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
                      const double *v, const double *omega, const double *radius,
                      const double *rmass);
 
+/* Restart data, valid between dem_upload_atoms and dem_setup (atoms indexed in
+ * upload order).  Contact history as the reference keeps it per atom
+ * (FixContactHistory npartner/partner/contacthistory, restored by
+ * FixContactHistory::unpack_restart, src/fix_contact_history.cpp:554-659):
+ * one entry per (owner atom, partner atom) with the owner's dnum history
+ * doubles; a contact between two atoms has one entry per side.  The next
+ * neighbour build carries an entry over when the pair touches at that time,
+ * exactly as after read_restart.  Wall history: 3 doubles per atom, the
+ * fix property/atom history_<wallid> restart data. */
+int dem_upload_contact_history(dem_handle *h, int nentries, const int *tag_owner,
+                               const int *tag_partner, const double *hist);
+int dem_upload_wall_history(dem_handle *h, int wall_id, const double *hist);
+
 int dem_setup(dem_handle *h);
 int dem_step(dem_handle *h, int nsteps);
 

@@ -419,6 +419,67 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
   return DEM_OK;
 }
 
+int dem_upload_contact_history(dem_handle *h, int ne, const int *towner, const int *tpartner,
+                               const double *hist) {
+  if (!h || !h->have_atoms || ne < 0 || (ne > 0 && (!towner || !tpartner || !hist)))
+    return DEM_ERR_BAD_ARG;
+  if (h->setup_done) return fail(h, DEM_ERR_BAD_ARG, "contact history must precede dem_setup");
+  const int n = h->host_ctrl.n;
+  std::vector<int> tags(n);
+  CUDA_TRY(h, cudaMemcpy(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<std::pair<int, int>> t2i(n);
+  for (int i = 0; i < n; i++) t2i[i] = {tags[i], i};
+  std::sort(t2i.begin(), t2i.end());
+  auto find = [&](int t) -> int {
+    auto it = std::lower_bound(t2i.begin(), t2i.end(), std::make_pair(t, -1));
+    return (it != t2i.end() && it->first == t) ? it->second : -1;
+  };
+  std::vector<int> oi(ne), oj(ne), row(n + 1, 0);
+  for (int k = 0; k < ne; k++) {
+    oi[k] = find(towner[k]);
+    oj[k] = find(tpartner[k]);
+    if (oi[k] < 0 || oj[k] < 0) return fail(h, DEM_ERR_BAD_ARG, "contact history names an unknown tag");
+    row[oi[k] + 1]++;
+  }
+  for (int i = 0; i < n; i++) row[i + 1] += row[i];
+  if (ne > h->s.pcap) {
+    int rc = alloc_pairs(h, ne + 1024, 0);
+    if (rc) return rc;
+  }
+  const size_t P = h->s.pcap;
+  std::vector<int> pi(ne), pj(ne), fl(ne, 1), fill(row.begin(), row.end() - 1);
+  std::vector<double> hh(3 * P, 0.0);
+  for (int k = 0; k < ne; k++) {
+    const int p = fill[oi[k]]++;
+    pi[p] = oi[k];
+    pj[p] = oj[k];
+    for (int d = 0; d < kDnumShear; d++) hh[d * P + p] = hist[(size_t)k * kDnumShear + d];
+  }
+  const PairArrays &L = h->s.pairs[0];
+  if (ne) {
+    CUDA_TRY(h, cudaMemcpy(L.i, pi.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(L.j, pj.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(L.flag, fl.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(L.hist, hh.data(), 3 * P * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  CUDA_TRY(h, cudaMemcpy(L.row, row.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemset(L.rev_start, 0, (h->s.nmax + 1) * sizeof(int)));
+  return DEM_OK;
+}
+
+int dem_upload_wall_history(dem_handle *h, int wall_id, const double *hist) {
+  if (!h || !h->have_atoms || !hist || wall_id < 0 || wall_id >= h->s.nplanes) return DEM_ERR_BAD_ARG;
+  if (h->setup_done) return fail(h, DEM_ERR_BAD_ARG, "wall history must precede dem_setup");
+  const int n = h->host_ctrl.n;
+  std::vector<double> hb(n);
+  for (int d = 0; d < 3; d++) {
+    for (int i = 0; i < n; i++) hb[i] = hist[3 * (size_t)i + d];
+    CUDA_TRY(h, cudaMemcpy(h->s.atoms[0].whist + (size_t)(wall_id * 3 + d) * h->s.nmax, hb.data(),
+                           n * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  return DEM_OK;
+}
+
 int dem_setup(dem_handle *h) {
   if (!h || !h->have_atoms) return DEM_ERR_BAD_ARG;
   cudaGetLastError();

@@ -631,11 +631,11 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
         fx -= s.resF[p]; fy -= s.resF[P + p]; fz -= s.resF[2 * P + p];
         tx += s.resTj[p]; ty += s.resTj[P + p]; tz += s.resTj[2 * P + p];
       }
-      if (s.gravity_on) {
+      if (s.gravity_on) {  // FixGravity::post_force, src/fix_gravity.cpp:329-337
         const double massone = A.m[i] * 1.;
-        fx += massone * s.g[0];
-        fy += massone * s.g[1];
-        fz += massone * s.g[2];
+        fx = __dadd_rn(fx, __dmul_rn(massone, s.g[0]));
+        fy = __dadd_rn(fy, __dmul_rn(massone, s.g[1]));
+        fz = __dadd_rn(fz, __dmul_rn(massone, s.g[2]));
       }
       const uint8_t bits = A.wbits[i];
       if (bits) {
@@ -650,15 +650,27 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
       tx = A.tx[i]; ty = A.ty[i]; tz = A.tz[i];
     }
     if (FINAL || INITIAL) {
+      // FixNVESphere updates with the reference's rounding (no contraction):
+      // positions then match the reference bit for bit whenever forces do.
       const double dtfm = A.dtfm[i], dtir = A.dtir[i];
       if (FINAL) {
-        v[0] += dtfm * fx; v[1] += dtfm * fy; v[2] += dtfm * fz;
-        om[0] += dtir * tx; om[1] += dtir * ty; om[2] += dtir * tz;
+        v[0] = __dadd_rn(v[0], __dmul_rn(dtfm, fx));
+        v[1] = __dadd_rn(v[1], __dmul_rn(dtfm, fy));
+        v[2] = __dadd_rn(v[2], __dmul_rn(dtfm, fz));
+        om[0] = __dadd_rn(om[0], __dmul_rn(dtir, tx));
+        om[1] = __dadd_rn(om[1], __dmul_rn(dtir, ty));
+        om[2] = __dadd_rn(om[2], __dmul_rn(dtir, tz));
       }
       if (INITIAL) {
-        v[0] += dtfm * fx; v[1] += dtfm * fy; v[2] += dtfm * fz;
-        xv[0] += dtv * v[0]; xv[1] += dtv * v[1]; xv[2] += dtv * v[2];
-        om[0] += dtir * tx; om[1] += dtir * ty; om[2] += dtir * tz;
+        v[0] = __dadd_rn(v[0], __dmul_rn(dtfm, fx));
+        v[1] = __dadd_rn(v[1], __dmul_rn(dtfm, fy));
+        v[2] = __dadd_rn(v[2], __dmul_rn(dtfm, fz));
+        xv[0] = __dadd_rn(xv[0], __dmul_rn(dtv, v[0]));
+        xv[1] = __dadd_rn(xv[1], __dmul_rn(dtv, v[1]));
+        xv[2] = __dadd_rn(xv[2], __dmul_rn(dtv, v[2]));
+        om[0] = __dadd_rn(om[0], __dmul_rn(dtir, tx));
+        om[1] = __dadd_rn(om[1], __dmul_rn(dtir, ty));
+        om[2] = __dadd_rn(om[2], __dmul_rn(dtir, tz));
         A.x[i] = xv[0]; A.y[i] = xv[1]; A.z[i] = xv[2];
         const double dx = __dadd_rn(xv[0], -A.xh[i]);
         const double dy = __dadd_rn(xv[1], -A.yh[i]);

@@ -62,6 +62,8 @@ def load(build=True):
     L.dem_derive_hertz_tables.argtypes = [I] + [P] * 7
     L.dem_add_plane.argtypes = [P, I, ctypes.c_double, I, I, P]
     L.dem_upload_atoms.argtypes = [P, I] + [P] * 7
+    L.dem_upload_contact_history.argtypes = [P, I, P, P, P]
+    L.dem_upload_wall_history.argtypes = [P, I, P]
     L.dem_setup.argtypes = [P]
     L.dem_step.argtypes = [P, I]
     L.dem_natoms.argtypes = [P, P]
@@ -144,6 +146,16 @@ class DemSystem:
                 (("tag", np.int32), ("type", np.int32), ("x", np.float64), ("v", np.float64),
                  ("omega", np.float64), ("radius", np.float64), ("rmass", np.float64))]
         self._check(load().dem_upload_atoms(self.h, n, *[_p(x) for x in arrs]))
+
+    def set_restart(self, tag_owner, tag_partner, hist, wall_hist=()):
+        """Restart contact/wall history (between upload and setup)."""
+        to = np.ascontiguousarray(tag_owner, dtype=np.int32)
+        tp = np.ascontiguousarray(tag_partner, dtype=np.int32)
+        h = np.ascontiguousarray(hist, dtype=np.float64)
+        self._check(load().dem_upload_contact_history(self.h, len(to), _p(to), _p(tp), _p(h)))
+        for w, wh in enumerate(wall_hist):
+            wh = np.ascontiguousarray(wh, dtype=np.float64)
+            self._check(load().dem_upload_wall_history(self.h, w, _p(wh)))
 
     def setup(self):
         self._check(load().dem_setup(self.h))

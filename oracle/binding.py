@@ -70,6 +70,8 @@ def lib():
         L.orc_get_atoms.argtypes = [P] + [P] * 9
         L.orc_get_pairs.argtypes = [P] + [P] * 5
         L.orc_get_wall_history.argtypes = [P, ctypes.c_int, P]
+        L.orc_set_contact_history.argtypes = [P, ctypes.c_int, P, P, P]
+        L.orc_set_wall_history.argtypes = [P, ctypes.c_int, P]
         _lib = L
     return _lib
 
@@ -116,6 +118,16 @@ class Oracle:
                 (("tag", np.int32), ("type", np.int32), ("x", np.float64), ("v", np.float64),
                  ("omega", np.float64), ("radius", np.float64), ("rmass", np.float64))]
         L.orc_set_atoms(self.h, n, *[_p(x) for x in arrs])
+
+    def set_restart(self, tag_owner, tag_partner, hist, wall_hist=()):
+        """Contact/wall history as restored by read_restart (see dem_oracle.h)."""
+        to = np.ascontiguousarray(tag_owner, dtype=np.int32)
+        tp = np.ascontiguousarray(tag_partner, dtype=np.int32)
+        h = np.ascontiguousarray(hist, dtype=np.float64)
+        self._check(lib().orc_set_contact_history(self.h, len(to), _p(to), _p(tp), _p(h)))
+        for w, wh in enumerate(wall_hist):
+            wh = np.ascontiguousarray(wh, dtype=np.float64)
+            self._check(lib().orc_set_wall_history(self.h, w, _p(wh)))
 
     def _check(self, rc):
         if rc != 0:

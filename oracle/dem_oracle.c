@@ -173,6 +173,44 @@ int orc_set_atoms(orc_sys *s, int n, const int *tag, const int *type, const doub
   return 0;
 }
 
+/* Restart data: per-atom partner lists as FixContactHistory::unpack_restart
+ * leaves them (src/fix_contact_history.cpp:554-659).  Entries are directed
+ * (owner tag, partner tag, owner's history). */
+int orc_set_contact_history(orc_sys *s, int ne, const int *towner, const int *tpartner,
+                            const double *hist) {
+  const int n = s->n, dnum = s->dnum;
+  int *cnt = (int *)calloc(n + 1, sizeof(int));
+  int *own = (int *)malloc((ne + 1) * sizeof(int));
+  for (int k = 0; k < ne; k++) {
+    own[k] = -1;
+    for (int i = 0; i < n; i++) if (s->tag[i] == towner[k]) { own[k] = i; break; }
+    if (own[k] < 0) { free(cnt); free(own); snprintf(s->err, sizeof s->err, "unknown tag"); return -1; }
+    cnt[own[k]]++;
+  }
+  s->pstart = (int *)xrealloc(s->pstart, (n + 1) * sizeof(int));
+  s->pstart[0] = 0;
+  for (int i = 0; i < n; i++) s->pstart[i + 1] = s->pstart[i] + cnt[i];
+  s->ptag = (int *)xrealloc(s->ptag, (ne + 1) * sizeof(int));
+  s->phist = (double *)xrealloc(s->phist, ((size_t)ne * dnum + 1) * sizeof(double));
+  memset(cnt, 0, (n + 1) * sizeof(int));
+  for (int k = 0; k < ne; k++) {
+    int m = s->pstart[own[k]] + cnt[own[k]]++;
+    s->ptag[m] = tpartner[k];
+    for (int d = 0; d < dnum; d++) s->phist[(size_t)m * dnum + d] = hist[(size_t)k * dnum + d];
+  }
+  for (int i = 0; i < n; i++) s->prow[i] = i;
+  s->prows = n;
+  free(cnt);
+  free(own);
+  return 0;
+}
+
+int orc_set_wall_history(orc_sys *s, int wall, const double *hist) {
+  if (wall < 0 || wall >= s->nplanes) return -1;
+  memcpy(s->planes[wall].hist, hist, 3 * (size_t)s->n * sizeof(double));
+  return 0;
+}
+
 /* ------------------------------------------------------------------ */
 /* Parameters                                                          */
 /* ------------------------------------------------------------------ */

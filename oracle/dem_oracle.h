@@ -59,6 +59,12 @@ int orc_set_atoms(orc_sys *s, int n, const int *tag, const int *type, const doub
                   const double *v, const double *omega, const double *radius,
                   const double *rmass);
 
+/* Restart data (between orc_set_atoms and orc_setup): directed contact
+ * history entries and per-atom wall history, as after read_restart. */
+int orc_set_contact_history(orc_sys *s, int nentries, const int *tag_owner,
+                            const int *tag_partner, const double *hist);
+int orc_set_wall_history(orc_sys *s, int wall, const double *hist);
+
 int orc_setup(orc_sys *s);            /* Verlet::setup */
 int orc_run(orc_sys *s, int nsteps);  /* nsteps iterations of Verlet::run */
 

@@ -43,6 +43,33 @@ def load_golden(name):
     return case, snaps
 
 
+DIVERGED_RTOL = 1e-7    # forces after >10 steps of independently rounded trajectories
+
+
+def restart_from_snapshot(case, snap):
+    """The reference's state at one snapshot as restart data.
+
+    Returns (case_k, tag_owner, tag_partner, hist, wall_hists): atoms at that
+    step plus the per-atom partner lists FixContactHistory::pre_exchange would
+    write from the snapshot's neighbour list (src/fix_contact_history.cpp:
+    305-425): every flagged pair gives an owner entry and, when both atoms are
+    owned (no periodic image), a partner entry with negated history.
+    """
+    ck = dict(case)
+    ck["atoms"] = dict(tag=snap["tag"], type=snap["type"], x=snap["x"], v=snap["v"],
+                       omega=snap["omega"], radius=snap["radius"], rmass=snap["rmass"])
+    to, tp, hs = [], [], []
+    for p in range(len(snap["pair_flag"])):
+        if snap["pair_flag"][p] == 0:
+            continue
+        ti, tj, h = int(snap["pair_tag_i"][p]), int(snap["pair_tag_j"][p]), snap["pair_hist"][p]
+        to.append(ti); tp.append(tj); hs.append(h)
+        if not np.any(snap["pair_shift"][p]):
+            to.append(tj); tp.append(ti); hs.append(-h)
+    walls = [snap[k] for k in sorted(k for k in snap if k.startswith("wall") and k.endswith("_hist"))]
+    return ck, np.array(to, np.int32), np.array(tp, np.int32), np.array(hs).reshape(-1, 3), walls
+
+
 def canonical_pairs(tag_i, tag_j, shift, flag, hist):
     """dict key -> (flag, hist) with owned-owned pairs as (min, max) tags."""
     out = {}
