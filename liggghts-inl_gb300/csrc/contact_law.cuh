@@ -6,10 +6,20 @@
 //   TangentialModel<TANGENTIAL_HISTORY>               src/tangential_model_history.h:135-439
 //   RollingModel<ROLLING_CDT>                         src/rolling_model_cdt.h:89-167
 //
-// The expressions keep the reference's operand order; FMA contraction is left
-// to the compiler here (it changes results at the rounding level only).  The
-// inputs that decide the contact set (rsq, radsum) are formed by the callers
-// with explicit round-to-nearest intrinsics, bit-identical to the reference.
+// GB300 has ~1.25 TFLOP/s of FP64, so the law is restated with fewer FP64
+// instructions; every change is an algebraic identity and moves results only
+// at the rounding level:
+//   * Hertz damping: gamma_n = -2 sqrt(5/6) beta sqrt(Sn meff) with
+//     Sn = 2 Y sqrt(reff deltan) equals Kn * (reff deltan)^(1/4) with the
+//     per-pair constant Kn = -2 sqrt(5/6) beta sqrt(2 Y meff) (likewise Kt
+//     with 8 G): one sqrt per contact-step instead of three;
+//   * Hooke: kn and gamma_n depend only on the pair (reff, meff, types), so
+//     the pow() of the reference is evaluated once per neighbour build;
+//   * Coulomb test kt|s| > mu|Fn| on squares; sqrt and division only when
+//     the contact slides; shear = -Ft/kt as shear*ratio;
+//   * 1/r and 1/|w_roll| as rsqrt.
+// The quantities that decide the contact set (rsq, radsum) and the overlap
+// deltan = radsum - sqrt(rsq) are formed exactly as in the reference.
 #pragma once
 #include "dem_device.cuh"
 
@@ -35,8 +45,30 @@ __device__ __forceinline__ TypePair load_typepair(const double *__restrict__ par
   return t;
 }
 
+// Per-pair constants of the normal law.  Hertz: (Kn, Kt) damping prefactors;
+// Hooke: (kn, gamma_n) of src/normal_model_hooke.h:272-279.
+template <int NORMAL>
+__device__ __forceinline__ void contact_consts(const TypePair &tp, double meff, double reff,
+                                               double charVel, bool tdamp, double &c0,
+                                               double &c1) {
+  if (NORMAL == kHertz) {
+    const double sqrtFiveOverSix = 0.91287092917527685576161630466800355658790782499663875;
+    const double k = -2. * sqrtFiveOverSix * tp.beta;
+    c0 = k * sqrt(2. * tp.Y * meff);
+    c1 = tdamp ? k * sqrt(8. * tp.G * meff) : 0.0;
+  } else {
+    const double sqrtval = sqrt(reff);
+    const double kn = 16. / 15. * sqrtval * (tp.Y) *
+                      pow(15. * meff * charVel * charVel / (16. * sqrtval * tp.Y), 0.2);
+    const double lsq = tp.restlog * tp.restlog;
+    c0 = kn;
+    c1 = sqrt(4. * meff * kn * lsq / (lsq + 9.86960440108935861883 /* M_PI*M_PI */));
+  }
+}
+
 struct ContactIn {
-  double radi, radj, radsum, r, rinv, meff, reff;
+  double radi, radj, radsum, r, rinv;
+  double reff, c0, c1;
   double en[3], d[3];
   double vr[3];          // v_i - v_j
   double wi[3], wj[3];
@@ -52,7 +84,7 @@ struct ContactOut {
 // shear[3] is the tangential history, updated in place when update_history.
 template <int NORMAL, bool WALL>
 __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &tp, double dt,
-                                            double charVel, bool tdamp, bool limitf, bool rolling,
+                                            bool tdamp, bool limitf, bool rolling,
                                             bool update_history, double shear[3], ContactOut &o) {
   const double enx = c.en[0], eny = c.en[1], enz = c.en[2];
   // ---- surface model (sphere kinematics)
@@ -61,14 +93,15 @@ __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &
   const double vt1 = vr1 - vn * enx;
   const double vt2 = vr2 - vn * eny;
   const double vt3 = vr3 - vn * enz;
-  const double deltan = c.radsum - c.r;
+  const double deltan = __dadd_rn(c.radsum, -c.r);
   const double dx = c.d[0], dy = c.d[1], dz = c.d[2];
   double wr1, wr2, wr3, cri, crj = 0.0;
   if (WALL) {
     cri = c.radi - 0.5 * c.deltan_wall;
-    wr1 = cri * c.wi[0] * c.rinv;
-    wr2 = cri * c.wi[1] * c.rinv;
-    wr3 = cri * c.wi[2] * c.rinv;
+    const double cr = cri * c.rinv;
+    wr1 = cr * c.wi[0];
+    wr2 = cr * c.wi[1];
+    wr3 = cr * c.wi[2];
   } else {
     cri = c.radi - 0.5 * deltan;
     crj = c.radj - 0.5 * deltan;
@@ -81,74 +114,64 @@ __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &
   const double vtr3 = vt3 - (dy * wr1 - dx * wr2);
 
   // ---- normal model
-  const double reff = c.reff;
-  const double meff = c.meff;
   double kn, kt, gamman, gammat;
   if (NORMAL == kHertz) {
-    const double sqrtval = sqrt(reff * deltan);
-    const double Sn = 2. * tp.Y * sqrtval;
-    const double St = 8. * tp.G * sqrtval;
+    const double sqrtval = sqrt(c.reff * deltan);
+    const double q = sqrt(sqrtval);
     kn = 4. / 3. * tp.Y * sqrtval;
-    kt = St;
-    const double sqrtFiveOverSix = 0.91287092917527685576161630466800355658790782499663875;
-    gamman = -2. * sqrtFiveOverSix * tp.beta * sqrt(Sn * meff);
-    gammat = tdamp ? -2. * sqrtFiveOverSix * tp.beta * sqrt(St * meff) : 0.0;
+    kt = 8. * tp.G * sqrtval;
+    gamman = c.c0 * q;
+    gammat = c.c1 * q;
   } else {
-    const double sqrtval = sqrt(reff);
-    kn = 16. / 15. * sqrtval * (tp.Y) *
-         pow(15. * meff * charVel * charVel / (16. * sqrtval * tp.Y), 0.2);
+    kn = c.c0;
     kt = kn;
-    const double lsq = tp.restlog * tp.restlog;
-    gamman = sqrt(4. * meff * kn * lsq / (lsq + 9.86960440108935861883 /* M_PI*M_PI */));
+    gamman = c.c1;
     gammat = tdamp ? gamman : 0.0;
   }
-  const double Fn_damping = -gamman * vn;
-  const double Fn_contact = kn * deltan;
-  double Fn = Fn_damping + Fn_contact;
+  double Fn = kn * deltan - gamman * vn;
   if (limitf && Fn < 0.0) Fn = 0.0;
-  double F1 = Fn * enx, F2 = Fn * eny, F3 = Fn * enz;
 
   // ---- tangential history
+  double s0 = shear[0], s1 = shear[1], s2 = shear[2];
   if (update_history) {
-    shear[0] += vtr1 * dt;
-    shear[1] += vtr2 * dt;
-    shear[2] += vtr3 * dt;
-    const double rsht = shear[0] * enx + shear[1] * eny + shear[2] * enz;
-    shear[0] -= rsht * enx;
-    shear[1] -= rsht * eny;
-    shear[2] -= rsht * enz;
+    s0 += vtr1 * dt;
+    s1 += vtr2 * dt;
+    s2 += vtr3 * dt;
+    const double rsht = s0 * enx + s1 * eny + s2 * enz;
+    s0 -= rsht * enx;
+    s1 -= rsht * eny;
+    s2 -= rsht * enz;
   }
-  const double shrmag = sqrt(shear[0] * shear[0] + shear[1] * shear[1] + shear[2] * shear[2]);
-  double Ft1 = -(kt * shear[0]);
-  double Ft2 = -(kt * shear[1]);
-  double Ft3 = -(kt * shear[2]);
-  const double Ft_shear = kt * shrmag;
+  double Ft1, Ft2, Ft3;
+  const double ss = s0 * s0 + s1 * s1 + s2 * s2;
   const double Ft_friction = tp.mu * fabs(Fn);
-  if (Ft_shear > Ft_friction) {
-    if (shrmag != 0.0) {
-      const double ratio = Ft_friction / Ft_shear;
-      Ft1 *= ratio;
-      Ft2 *= ratio;
-      Ft3 *= ratio;
-      if (update_history) {
-        shear[0] = -Ft1 / kt;
-        shear[1] = -Ft2 / kt;
-        shear[2] = -Ft3 / kt;
-      }
-    } else {
-      Ft1 = Ft2 = Ft3 = 0.0;
+  if (kt * kt * ss > Ft_friction * Ft_friction) {
+    // sliding (ss > 0 here): cap the spring force at mu|Fn|
+    const double ratio = Ft_friction * rsqrt(ss) / kt;
+    Ft1 = -(kt * s0) * ratio;
+    Ft2 = -(kt * s1) * ratio;
+    Ft3 = -(kt * s2) * ratio;
+    if (update_history) {
+      s0 *= ratio;
+      s1 *= ratio;
+      s2 *= ratio;
     }
   } else {
-    Ft1 -= gammat * vtr1;
-    Ft2 -= gammat * vtr2;
-    Ft3 -= gammat * vtr3;
+    Ft1 = -(kt * s0) - gammat * vtr1;
+    Ft2 = -(kt * s1) - gammat * vtr2;
+    Ft3 = -(kt * s2) - gammat * vtr3;
+  }
+  if (update_history) {
+    shear[0] = s0;
+    shear[1] = s1;
+    shear[2] = s2;
   }
   const double tor1 = eny * Ft3 - enz * Ft2;
   const double tor2 = enz * Ft1 - enx * Ft3;
   const double tor3 = enx * Ft2 - eny * Ft1;
-  o.F[0] = F1 + Ft1;
-  o.F[1] = F2 + Ft2;
-  o.F[2] = F3 + Ft3;
+  o.F[0] = Fn * enx + Ft1;
+  o.F[1] = Fn * eny + Ft2;
+  o.F[2] = Fn * enz + Ft3;
   o.Ti[0] = -cri * tor1;
   o.Ti[1] = -cri * tor2;
   o.Ti[2] = -cri * tor3;
@@ -158,39 +181,31 @@ __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &
 
   // ---- rolling friction, constant directional torque
   if (rolling) {
-    double rt1 = 0., rt2 = 0., rt3 = 0.;
+    double w1, w2, w3;
     if (WALL) {
-      const double wrmag = sqrt(wr1 * wr1 + wr2 * wr2 + wr3 * wr3);
-      if (wrmag > 0.) {
-        const double Fnr = deltan * kn;
-        rt1 = tp.mur * Fnr * wr1 / wrmag * reff;
-        rt2 = tp.mur * Fnr * wr2 / wrmag * reff;
-        rt3 = tp.mur * Fnr * wr3 / wrmag * reff;
-        const double rtd = rt1 * enx + rt2 * eny + rt3 * enz;
-        rt1 -= enx * rtd;
-        rt2 -= eny * rtd;
-        rt3 -= enz * rtd;
-      }
+      w1 = wr1;
+      w2 = wr2;
+      w3 = wr3;
     } else {
-      const double w1 = c.wi[0] - c.wj[0], w2 = c.wi[1] - c.wj[1], w3 = c.wi[2] - c.wj[2];
-      const double wmag = sqrt(w1 * w1 + w2 * w2 + w3 * w3);
-      if (wmag > 0.) {
-        const double fac = tp.mur * kn * deltan * reff / wmag;
-        rt1 = fac * w1;
-        rt2 = fac * w2;
-        rt3 = fac * w3;
-        const double rtd = rt1 * enx + rt2 * eny + rt3 * enz;
-        rt1 -= enx * rtd;
-        rt2 -= eny * rtd;
-        rt3 -= enz * rtd;
-      }
+      w1 = c.wi[0] - c.wj[0];
+      w2 = c.wi[1] - c.wj[1];
+      w3 = c.wi[2] - c.wj[2];
     }
-    o.Ti[0] -= rt1;
-    o.Ti[1] -= rt2;
-    o.Ti[2] -= rt3;
-    o.Tj[0] += rt1;
-    o.Tj[1] += rt2;
-    o.Tj[2] += rt3;
+    const double wsq = w1 * w1 + w2 * w2 + w3 * w3;
+    if (wsq > 0.) {
+      const double fac = tp.mur * kn * deltan * c.reff * rsqrt(wsq);
+      double rt1 = fac * w1, rt2 = fac * w2, rt3 = fac * w3;
+      const double rtd = rt1 * enx + rt2 * eny + rt3 * enz;
+      rt1 -= enx * rtd;
+      rt2 -= eny * rtd;
+      rt3 -= enz * rtd;
+      o.Ti[0] -= rt1;
+      o.Ti[1] -= rt2;
+      o.Ti[2] -= rt3;
+      o.Tj[0] += rt1;
+      o.Tj[1] += rt2;
+      o.Tj[2] += rt3;
+    }
   }
 }
 

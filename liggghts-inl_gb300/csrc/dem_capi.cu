@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -43,7 +44,28 @@ struct dem_handle {
   int evused = 0;
   std::vector<int> evkind;  // 0 particle, 1 neigh, 2 pair: kind of interval ending at event k
   dem_kernel_times kt{};
+  // graph-resident step loop
+  bool use_graph = true;
+  cudaStream_t st2 = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  long long graph_gen = -1, sys_gen = 0;  // rebuilt when device pointers change
+  int graph_kps = 0, graph_kpr = 0;
 };
+
+static int ensure_graph(dem_handle *h) {
+  if (h->gexec && h->graph_gen == h->sys_gen) return DEM_OK;
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  cudaError_t e = build_step_graph(h->s, h->lc, h->st, h->st2, &h->gexec, &h->graph_kps, &h->graph_kpr);
+  if (e != cudaSuccess) {
+    h->err = std::string("build_step_graph: ") + cudaGetErrorString(e);
+    return DEM_ERR_CUDA;
+  }
+  h->graph_gen = h->sys_gen;
+  return DEM_OK;
+}
 
 // Records an event closing an interval of the given kind (profiling only).
 static void mark(dem_handle *h, int kind) {
@@ -103,6 +125,7 @@ static void free_list(std::vector<void *> &l) {
 static int alloc_atoms(dem_handle *h, int nmax) {
   Sys &s = h->s;
   free_list(h->allocs_atoms);
+  h->sys_gen++;
   s.nmax = nmax;
   auto &L = h->allocs_atoms;
   for (int b = 0; b < 2; b++) {
@@ -148,8 +171,9 @@ static int alloc_pairs(dem_handle *h, int pcap, int keep_np) {
     CUDA_TRY(h, dalloc(nl, &P.sh, pcap));
     CUDA_TRY(h, dalloc(nl, &P.flag, pcap));
     CUDA_TRY(h, dalloc(nl, &P.hist, (size_t)3 * pcap));
-    CUDA_TRY(h, dalloc(nl, &P.meff, pcap));
     CUDA_TRY(h, dalloc(nl, &P.reff, pcap));
+    CUDA_TRY(h, dalloc(nl, &P.c0, pcap));
+    CUDA_TRY(h, dalloc(nl, &P.c1, pcap));
     CUDA_TRY(h, dalloc(nl, &P.rev, pcap));
   }
   double *rF, *rTi, *rTj;
@@ -169,8 +193,9 @@ static int alloc_pairs(dem_handle *h, int pcap, int keep_np) {
     for (int d = 0; d < 3; d++)
       CUDA_TRY(h, cudaMemcpy(N.hist + (size_t)d * pcap, O.hist + (size_t)d * s.pcap,
                              k * sizeof(double), cudaMemcpyDeviceToDevice));
-    CUDA_TRY(h, cudaMemcpy(N.meff, O.meff, k * sizeof(double), cudaMemcpyDeviceToDevice));
     CUDA_TRY(h, cudaMemcpy(N.reff, O.reff, k * sizeof(double), cudaMemcpyDeviceToDevice));
+    CUDA_TRY(h, cudaMemcpy(N.c0, O.c0, k * sizeof(double), cudaMemcpyDeviceToDevice));
+    CUDA_TRY(h, cudaMemcpy(N.c1, O.c1, k * sizeof(double), cudaMemcpyDeviceToDevice));
     CUDA_TRY(h, cudaMemcpy(N.rev, O.rev, k * sizeof(int), cudaMemcpyDeviceToDevice));
   }
   free_list(h->allocs_pairs);
@@ -182,6 +207,7 @@ static int alloc_pairs(dem_handle *h, int pcap, int keep_np) {
   s.resTj = rTj;
   s.active = act;
   s.pcap = pcap;
+  h->sys_gen++;
   return DEM_OK;
 }
 
@@ -234,10 +260,15 @@ int dem_create(const dem_config *cfg, dem_handle **out) {
   if (cudaGetDeviceProperties(&prop, h->device) == cudaSuccess)
     h->lc.max_grid = prop.multiProcessorCount * 8;
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
     delete h;
     return DEM_ERR_CUDA;
   }
+  // LIGGGHTS_GB300_NO_GRAPH=1 queues every kernel from the host instead of
+  // running the step loop as one graph (same results; for debugging)
+  const char *ng = getenv("LIGGGHTS_GB300_NO_GRAPH");
+  h->use_graph = !(ng && ng[0] == '1');
   Sys &s = h->s;
   if (cudaMalloc(&s.ctrl, sizeof(Ctrl)) != cudaSuccess) {
     delete h;
@@ -276,7 +307,9 @@ int dem_destroy(dem_handle *h) {
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (auto &e : h->evpool) cudaEventDestroy(e);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
   if (h->st) cudaStreamDestroy(h->st);
+  if (h->st2) cudaStreamDestroy(h->st2);
   delete h;
   return DEM_OK;
 }
@@ -325,6 +358,7 @@ int dem_set_pair_params(dem_handle *h, int ntypes, const double *Yeff, const dou
   h->s.ntypes = ntypes;
   h->s.charVel = charVel;
   h->have_params = true;
+  h->sys_gen++;
   return DEM_OK;
 }
 
@@ -339,6 +373,7 @@ int dem_add_plane(dem_handle *h, int axis, double pos, int wall_type, int rollin
   p.rolling = rolling_model == DEM_ROLLING_CDT ? 1 : 0;
   if (wall_id) *wall_id = h->s.nplanes;
   h->s.nplanes++;
+  h->sys_gen++;
   return DEM_OK;
 }
 
@@ -380,7 +415,12 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
   s.ncell = (int)ncell;
   int rc = alloc_atoms(h, n);
   if (rc) return rc;
-  rc = alloc_pairs(h, std::max(16 * n, 4096), 0);
+  // Initial pair capacity: 16 entries per atom.  LIGGGHTS_GB300_PAIRS_PER_ATOM
+  // overrides it; a deliberately small value exercises the overflow path
+  // (device halt, host growth, resumed rebuild) in tests.
+  long ppa = 16;
+  if (const char *e = getenv("LIGGGHTS_GB300_PAIRS_PER_ATOM")) ppa = std::max(0L, atol(e));
+  rc = alloc_pairs(h, (int)std::max<long>(ppa * n, ppa >= 16 ? 4096 : 1), 0);
   if (rc) return rc;
   // host-side per-atom constants of FixNVESphere (src/fix_nve_sphere.cpp:150-178)
   const double dtf = 0.5 * s.dt * 1.0;
@@ -510,19 +550,44 @@ int dem_step(dem_handle *h, int nsteps) {
   CUDA_TRY(h, cudaEventRecord(h->ev0, h->st));
   long long done = 0;  // steps whose rebuild+pair stage has been queued
   bool first = true;
+  const bool graph = h->use_graph && !h->profile;
   while (done < nsteps) {
-    const long long chunk = std::min<long long>(kCheckEvery, nsteps - done);
+    const long long chunk = graph ? nsteps - done : std::min<long long>(kCheckEvery, nsteps - done);
+    long long k0 = 0;
     mark_start(h);
-    for (long long k = 0; k < chunk; k++) {
-      h->kt.kernel_launches +=
-          launch_particle(h->s, h->lc, first ? kModeInitial : kModeGatherFinalInitial, 1, h->st);
+    if (first) {  // step 1 starts from stored forces: initial_integrate only
+      h->kt.kernel_launches += launch_particle(h->s, h->lc, kModeInitial, 1, h->st);
       mark(h, 0);
-      first = false;
       h->kt.kernel_launches += launch_decide(h->s, h->st);
       h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);
       mark(h, 1);
       h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
       mark(h, 2);
+      first = false;
+      k0 = 1;
+    }
+    if (graph && chunk > k0) {
+      rc = ensure_graph(h);
+      if (rc) return rc;
+      rc = read_ctrl(h);
+      if (rc) return rc;
+      const long long rb0 = h->host_ctrl.nrebuilds;
+      h->kt.kernel_launches += launch_set_loop(h->s, (int)(chunk - k0), h->st);
+      CUDA_TRY(h, cudaGraphLaunch(h->gexec, h->st));
+      rc = read_ctrl(h);
+      if (rc) return rc;
+      const long long iters = std::min<long long>(chunk - k0, h->host_ctrl.ntimestep - (ts0 + done + k0));
+      h->kt.kernel_launches += iters * h->graph_kps + (h->host_ctrl.nrebuilds - rb0) * h->graph_kpr;
+    } else {
+      for (long long k = k0; k < chunk; k++) {
+        h->kt.kernel_launches += launch_particle(h->s, h->lc, kModeGatherFinalInitial, 1, h->st);
+        mark(h, 0);
+        h->kt.kernel_launches += launch_decide(h->s, h->st);
+        h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);
+        mark(h, 1);
+        h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
+        mark(h, 2);
+      }
     }
     CUDA_TRY(h, cudaGetLastError());
     bool resumed = false;

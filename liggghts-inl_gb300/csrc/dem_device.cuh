@@ -2,13 +2,13 @@
 //
 // HBM layout (all SoA, FP64 unless noted; nmax = atom capacity, pcap = pair
 // capacity):
-//   atoms[2]   double-buffered per-atom arrays; a rebuild gathers the cell-
-//              sorted order into the inactive buffer and flips ctrl->cur_a.
-//   pairs[2]   double-buffered granular half list (CSR by owner) with contact
-//              flags, history hist[d*pcap + p], and per-pair constants
-//              meff = mi*mj/(mi+mj), reff = ri*rj/(ri+rj); the rebuild builds
-//              the new list beside the old one (history remap reads the old
-//              one) and flips ctrl->cur_p.
+//   atoms[2]   per-atom arrays; a rebuild gathers the cell-sorted order into
+//              atoms[1] and copies it back into atoms[0].
+//   pairs[2]   granular half list (CSR by owner) with contact flags, history
+//              hist[d*pcap + p] and per-pair constants (reff and the two
+//              contact constants of contact_consts()); pairs[1] is where a
+//              rebuild builds the new list while the history remap still
+//              reads the old one in pairs[0].
 //   scratch    cell counts/starts, sort permutation, per-pair force results.
 //   ctrl       device control block: atom/pair counts, rebuild decision,
 //              halt/status words.  Kernels read it, so no host round trip is
@@ -47,7 +47,8 @@ struct PairArrays {
   uint8_t *sh;              // periodic image code of j, 13 = none
   int *flag;                // contact flags (reference bits)
   double *hist;             // [d*pcap + p]
-  double *meff, *reff;
+  double *reff;             // ri*rj/(ri+rj)
+  double *c0, *c1;          // contact constants, see contact_consts()
   int *row;                 // [nmax+1] CSR offsets by owner
   int *rev_start;           // [nmax+1] offsets of pairs where the atom is partner
   int *rev;                 // pair ids, ascending per partner
@@ -67,7 +68,7 @@ struct Ctrl {
   long long lost;
   long long ntimestep, nrebuilds;
   int halt_step;
-  int pad;
+  int loop_left;    // steps left for the device-side step loop (graph WHILE node)
 };
 
 struct Plane {

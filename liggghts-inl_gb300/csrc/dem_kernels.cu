@@ -67,6 +67,28 @@ __global__ void k_decide(Sys s) {
   c->moved = 0;
 }
 
+// k_decide for the graph-resident step loop: also drives the IF node around
+// the rebuild and the WHILE node around the whole step.
+__global__ void k_decide_loop(Sys s, cudaGraphConditionalHandle hreb, cudaGraphConditionalHandle hloop) {
+  Ctrl *c = s.ctrl;
+  if (c->halt) {
+    cudaGraphSetConditional(hreb, 0);
+    cudaGraphSetConditional(hloop, 0);
+    return;
+  }
+  c->ntimestep++;
+  c->ago++;
+  int reb = 0;
+  if (c->ago >= s.neigh_delay && c->ago % s.neigh_every == 0) reb = s.neigh_check ? c->moved : 1;
+  c->rebuild = reb;
+  c->moved = 0;
+  c->loop_left--;
+  cudaGraphSetConditional(hreb, reb ? 1u : 0u);
+  cudaGraphSetConditional(hloop, c->loop_left > 0 ? 1u : 0u);
+}
+
+__global__ void k_set_loop(Sys s, int n) { s.ctrl->loop_left = n; }
+
 __global__ void k_set_rebuild(Sys s, int v) {
   if (s.ctrl->halt) return;
   s.ctrl->rebuild = v;
@@ -362,8 +384,15 @@ __global__ void k_pairs(Sys s) {
             M.hist[(size_t)s.pcap + p] = h1;
             M.hist[2 * (size_t)s.pcap + p] = h2;
             const double mj = A.m[j];
-            M.meff[p] = mi * mj / (mi + mj);
-            M.reff[p] = radi * radj / (radi + radj);
+            const double meff = mi * mj / (mi + mj);
+            const double reff = radi * radj / (radi + radj);
+            const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], A.type[j]);
+            double c0, c1;
+            if (s.normal == kHertz) contact_consts<kHertz>(tp, meff, reff, s.charVel, s.tdamp, c0, c1);
+            else contact_consts<kHooke>(tp, meff, reff, s.charVel, s.tdamp, c0, c1);
+            M.reff[p] = reff;
+            M.c0[p] = c0;
+            M.c1[p] = c1;
             if (code == kNoShift) atomicAdd(&s.rev_count[j], 1);
           }
         }
@@ -434,8 +463,9 @@ __global__ void k_copy_pairs(Sys s) {
       L.hist[p] = M.hist[p];
       L.hist[(size_t)s.pcap + p] = M.hist[(size_t)s.pcap + p];
       L.hist[2 * (size_t)s.pcap + p] = M.hist[2 * (size_t)s.pcap + p];
-      L.meff[p] = M.meff[p];
       L.reff[p] = M.reff[p];
+      L.c0[p] = M.c0[p];
+      L.c1[p] = M.c1[p];
       L.rev[p] = M.rev[p];
     }
     if (p < nrow) {
@@ -459,8 +489,18 @@ __global__ void k_finish_rebuild(Sys s) {
 // pair forces: one thread per half-list entry, results to the pair buffer
 // ----------------------------------------------------------------------------
 
+// Each block walks tiles of 256 list entries.  Phase 1 (all lanes): the exact
+// contact test rsq < radsum^2.  Touching entries are compacted into a shared
+// queue (warp ballots + block prefix), so phase 2 runs the FP64 contact law
+// on dense warps: non-touching entries cost no FP64 issue slots.  Results go
+// to the entry's own slot p, so the processing order never changes a value.
+constexpr int kPairTile = 256;
+
 template <int NORMAL, bool ROLL>
-__global__ void __launch_bounds__(256) k_pair(Sys s, int shearupdate) {
+__global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
+  __shared__ int q_p[kPairTile];
+  __shared__ double q_d[4][kPairTile];
+  __shared__ int wcnt[kPairTile / 32];
   Ctrl *c = s.ctrl;
   if (c->halt) return;
   const AtomArrays &A = s.atoms[0];
@@ -468,34 +508,71 @@ __global__ void __launch_bounds__(256) k_pair(Sys s, int shearupdate) {
   const int np = c->np;
   const size_t P = s.pcap;
   const double cdm = s.cdf * s.cdf;
-  GRID_STRIDE(p, np) {
-    const int i = L.i[p], j = L.j[p];
-    const int code = L.sh[p];
-    const double xi = A.x[i], yi = A.y[i], zi = A.z[i];
-    double xj = A.x[j], yj = A.y[j], zj = A.z[j];
-    image(s, code, xj, yj, zj);
-    const double delx = __dadd_rn(xi, -xj);
-    const double dely = __dadd_rn(yi, -yj);
-    const double delz = __dadd_rn(zi, -zj);
-    const double rsq = rsq_rn(delx, dely, delz);
-    const double radi = A.r[i], radj = A.r[j];
-    const double radsum = __dadd_rn(radi, radj);
-    const double rs2 = __dmul_rn(radsum, radsum);
-    if (rsq < rs2) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int base = blockIdx.x * kPairTile; base < np; base += gridDim.x * kPairTile) {
+    const int p = base + threadIdx.x;
+    bool touch = false;
+    double delx = 0., dely = 0., delz = 0., rsq = 0.;
+    if (p < np) {
+      const int i = L.i[p], j = L.j[p];
+      const int code = L.sh[p];
+      double xj = A.x[j], yj = A.y[j], zj = A.z[j];
+      image(s, code, xj, yj, zj);
+      delx = __dadd_rn(A.x[i], -xj);
+      dely = __dadd_rn(A.y[i], -yj);
+      delz = __dadd_rn(A.z[i], -zj);
+      rsq = rsq_rn(delx, dely, delz);
+      const double radsum = __dadd_rn(A.r[i], A.r[j]);
+      touch = rsq < __dmul_rn(radsum, radsum);
+      if (!touch) {
+        s.active[p] = 0;
+        if (rsq < __dmul_rn(__dmul_rn(cdm, radsum), radsum)) {
+          // TangentialModel<TANGENTIAL_HISTORY>::surfacesClose
+          L.flag[p] &= ~kContactTangential;
+          L.hist[p] = 0.0;
+          L.hist[P + p] = 0.0;
+          L.hist[2 * P + p] = 0.0;
+        }
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, touch);
+    if (lane == 0) wcnt[warp] = __popc(m);
+    __syncthreads();
+    int off = 0, tot = 0;
+#pragma unroll
+    for (int k = 0; k < kPairTile / 32; k++) {
+      const int v = wcnt[k];
+      off += (k < warp) ? v : 0;
+      tot += v;
+    }
+    if (touch) {
+      const int slot = off + __popc(m & ((1u << lane) - 1u));
+      q_p[slot] = p;
+      q_d[0][slot] = delx;
+      q_d[1][slot] = dely;
+      q_d[2][slot] = delz;
+      q_d[3][slot] = rsq;
+    }
+    __syncthreads();
+    if (threadIdx.x < tot) {
+      const int q = q_p[threadIdx.x];
+      const int i = L.i[q], j = L.j[q];
       ContactIn ci;
-      ci.radi = radi;
-      ci.radj = radj;
-      ci.radsum = radsum;
-      ci.r = sqrt(rsq);
-      ci.rinv = 1.0 / ci.r;
-      ci.meff = L.meff[p];
-      ci.reff = L.reff[p];
-      ci.d[0] = delx;
-      ci.d[1] = dely;
-      ci.d[2] = delz;
-      ci.en[0] = delx * ci.rinv;
-      ci.en[1] = dely * ci.rinv;
-      ci.en[2] = delz * ci.rinv;
+      ci.d[0] = q_d[0][threadIdx.x];
+      ci.d[1] = q_d[1][threadIdx.x];
+      ci.d[2] = q_d[2][threadIdx.x];
+      const double rsq_q = q_d[3][threadIdx.x];
+      ci.radi = A.r[i];
+      ci.radj = A.r[j];
+      ci.radsum = __dadd_rn(ci.radi, ci.radj);
+      ci.r = sqrt(rsq_q);
+      ci.rinv = rsqrt(rsq_q);
+      ci.reff = L.reff[q];
+      ci.c0 = L.c0[q];
+      ci.c1 = L.c1[q];
+      ci.en[0] = ci.d[0] * ci.rinv;
+      ci.en[1] = ci.d[1] * ci.rinv;
+      ci.en[2] = ci.d[2] * ci.rinv;
       ci.vr[0] = A.vx[i] - A.vx[j];
       ci.vr[1] = A.vy[i] - A.vy[j];
       ci.vr[2] = A.vz[i] - A.vz[j];
@@ -503,30 +580,21 @@ __global__ void __launch_bounds__(256) k_pair(Sys s, int shearupdate) {
       ci.wj[0] = A.wx[j]; ci.wj[1] = A.wy[j]; ci.wj[2] = A.wz[j];
       ci.deltan_wall = 0.0;
       const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], A.type[j]);
-      double sh3[3] = {L.hist[p], L.hist[P + p], L.hist[2 * P + p]};
+      double sh3[3] = {L.hist[q], L.hist[P + q], L.hist[2 * P + q]};
       ContactOut o;
-      contact_law<NORMAL, false>(ci, tp, s.dt, s.charVel, s.tdamp, s.limitf, ROLL,
-                                 shearupdate != 0, sh3, o);
+      contact_law<NORMAL, false>(ci, tp, s.dt, s.tdamp, s.limitf, ROLL, shearupdate != 0, sh3, o);
       if (shearupdate) {
-        L.hist[p] = sh3[0];
-        L.hist[P + p] = sh3[1];
-        L.hist[2 * P + p] = sh3[2];
+        L.hist[q] = sh3[0];
+        L.hist[P + q] = sh3[1];
+        L.hist[2 * P + q] = sh3[2];
       }
-      L.flag[p] |= (kContactNormal | kContactTangential);
-      s.resF[p] = o.F[0]; s.resF[P + p] = o.F[1]; s.resF[2 * P + p] = o.F[2];
-      s.resTi[p] = o.Ti[0]; s.resTi[P + p] = o.Ti[1]; s.resTi[2 * P + p] = o.Ti[2];
-      s.resTj[p] = o.Tj[0]; s.resTj[P + p] = o.Tj[1]; s.resTj[2 * P + p] = o.Tj[2];
-      s.active[p] = 1;
-    } else {
-      s.active[p] = 0;
-      if (rsq < __dmul_rn(__dmul_rn(cdm, radsum), radsum)) {
-        // TangentialModel<TANGENTIAL_HISTORY>::surfacesClose
-        L.flag[p] &= ~kContactTangential;
-        L.hist[p] = 0.0;
-        L.hist[P + p] = 0.0;
-        L.hist[2 * P + p] = 0.0;
-      }
+      L.flag[q] |= (kContactNormal | kContactTangential);
+      s.resF[q] = o.F[0]; s.resF[P + q] = o.F[1]; s.resF[2 * P + q] = o.F[2];
+      s.resTi[q] = o.Ti[0]; s.resTi[P + q] = o.Ti[1]; s.resTi[2 * P + q] = o.Ti[2];
+      s.resTj[q] = o.Tj[0]; s.resTj[P + q] = o.Tj[1]; s.resTj[2 * P + q] = o.Tj[2];
+      s.active[q] = 1;
     }
+    __syncthreads();
   }
 }
 
@@ -573,7 +641,6 @@ __device__ __forceinline__ void plane_contact(const Sys &s, const AtomArrays &A,
       ci.en[1] = ci.d[1] * ci.rinv;
       ci.en[2] = ci.d[2] * ci.rinv;
       ci.radsum = radi;
-      ci.meff = A.m[i];
       ci.reff = radi;
       ci.vr[0] = v[0] - 0.0;
       ci.vr[1] = v[1] - 0.0;
@@ -581,9 +648,10 @@ __device__ __forceinline__ void plane_contact(const Sys &s, const AtomArrays &A,
       ci.wi[0] = om[0]; ci.wi[1] = om[1]; ci.wi[2] = om[2];
       ci.wj[0] = ci.wj[1] = ci.wj[2] = 0.0;
       const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], pl.wall_type);
+      contact_consts<NORMAL>(tp, A.m[i], radi, s.charVel, s.tdamp, ci.c0, ci.c1);
       double sh3[3] = {h[0], h[hs], h[2 * hs]};
       ContactOut o;
-      contact_law<NORMAL, true>(ci, tp, s.dt, s.charVel, s.tdamp, s.limitf, pl.rolling != 0,
+      contact_law<NORMAL, true>(ci, tp, s.dt, s.tdamp, s.limitf, pl.rolling != 0,
                                 shearupdate != 0, sh3, o);
       if (shearupdate) {
         h[0] = sh3[0];
@@ -742,6 +810,65 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
   k_copy_pairs<<<grid_for((long)s.pcap > s.nmax + 1 ? s.pcap : s.nmax + 1, B, lc.max_grid), B, 0, st>>>(s);
   k_finish_rebuild<<<1, 1, 0, st>>>(s);
   return nl + 4;
+}
+
+// Builds the executable graph of `steps 2..n` of dem_step:
+//   WHILE(loop) { k_particle(gather+final+initial) -> k_decide_loop ->
+//                 IF(rebuild) { rebuild kernels } -> k_pair }
+// The host sets ctrl->loop_left with launch_set_loop() before each launch.
+cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st, cudaStream_t st2,
+                             cudaGraphExec_t *exec, int *kernels_per_step, int *kernels_per_rebuild) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle hloop, hreb;
+  if ((e = cudaGraphConditionalHandleCreate(&hloop, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+  if ((e = cudaGraphConditionalHandleCreate(&hreb, g, 0, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+  cudaGraphNodeParams wp = {};
+  wp.type = cudaGraphNodeTypeConditional;
+  wp.conditional.handle = hloop;
+  wp.conditional.type = cudaGraphCondTypeWhile;
+  wp.conditional.size = 1;
+  cudaGraphNode_t wnode;
+  if ((e = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp)) != cudaSuccess) return e;
+  cudaGraph_t body = wp.conditional.phGraph_out[0];
+  if ((e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+    return e;
+  int k = launch_particle(s, lc, kModeGatherFinalInitial, 1, st);
+  k_decide_loop<<<1, 1, 0, st>>>(s, hreb, hloop);
+  k++;
+  cudaStreamCaptureStatus cs;
+  const cudaGraphNode_t *deps = nullptr;
+  size_t nd = 0;
+  cudaGraph_t cg;
+  if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &nd)) != cudaSuccess) return e;
+  cudaGraphNodeParams ip = {};
+  ip.type = cudaGraphNodeTypeConditional;
+  ip.conditional.handle = hreb;
+  ip.conditional.type = cudaGraphCondTypeIf;
+  ip.conditional.size = 1;
+  cudaGraphNode_t inode;
+  if ((e = cudaGraphAddNode(&inode, cg, deps, nullptr, nd, &ip)) != cudaSuccess) return e;
+  cudaGraph_t rbody = ip.conditional.phGraph_out[0];
+  if ((e = cudaStreamUpdateCaptureDependencies(st, &inode, nullptr, 1, cudaStreamSetCaptureDependencies)) != cudaSuccess)
+    return e;
+  k += launch_pair(s, lc, 1, st);
+  cudaGraph_t out = nullptr;
+  if ((e = cudaStreamEndCapture(st, &out)) != cudaSuccess) return e;
+  if ((e = cudaStreamBeginCaptureToGraph(st2, rbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+    return e;
+  const int kr = launch_rebuild(s, lc, st2, 0);
+  if ((e = cudaStreamEndCapture(st2, &out)) != cudaSuccess) return e;
+  e = cudaGraphInstantiate(exec, g, 0);
+  cudaGraphDestroy(g);
+  *kernels_per_step = k;
+  *kernels_per_rebuild = kr;
+  return e;
+}
+
+int launch_set_loop(const Sys &s, int n, cudaStream_t st) {
+  k_set_loop<<<1, 1, 0, st>>>(s, n);
+  return 1;
 }
 
 int launch_decide(const Sys &s, cudaStream_t st) {

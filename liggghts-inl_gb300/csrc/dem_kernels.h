@@ -23,5 +23,10 @@ int launch_set_rebuild(const Sys &s, int v, cudaStream_t st);
 int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage);
 int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t st);
 int launch_particle(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, cudaStream_t st);
+int launch_set_loop(const Sys &s, int n, cudaStream_t st);
+// Executable graph of the steady-state step loop (WHILE node over steps, IF
+// node around the rebuild); see dem_kernels.cu.
+cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st, cudaStream_t st2,
+                             cudaGraphExec_t *exec, int *kernels_per_step, int *kernels_per_rebuild);
 
 }  // namespace gb300
