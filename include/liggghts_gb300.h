@@ -154,6 +154,33 @@ typedef struct dem_kernel_times {
 int dem_profile(dem_handle *h, int enable);
 int dem_get_kernel_times(dem_handle *h, dem_kernel_times *out);
 
+/* No counterpart in the reference.  Contact forces and torques of one setup
+ * force pass (history read, not updated) for a caller-supplied neighbour list,
+ * allocating nothing on the device: for callers that cannot call cudaMalloc
+ * while they run (GPU memory owned by another allocator or pool, loops that
+ * must not allocate after start-up).  All array arguments except the material
+ * tables are DEVICE pointers owned by the caller: x, v, omega n*3; radius,
+ * rmass, type n; pair_i, pair_j npairs (pair_i non-decreasing, as
+ * dem_download_contacts returns the list); shift, hist npairs*3; f, torque
+ * n*3 (written).  The material tables are host arrays as in
+ * dem_set_pair_params; cfg supplies the box, model and option switches.
+ * stream is a cudaStream_t (NULL: legacy default stream); the call
+ * synchronises it before returning.
+ * Scratch lives in one fixed static device array (about 11 MB per GPU that
+ * loads the library, kept until exit); limits: n <= 32768 atoms,
+ * npairs <= 131072, ntypes <= 15, else DEM_ERR_BAD_ARG.  The first call on a
+ * device looks up that array's device address and should come before any
+ * stream capture on that device.  Calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+int dem_contact_forces_noalloc(int n, const double *x, const double *v, const double *omega,
+                               const double *radius, const double *rmass, const int *type,
+                               int npairs, const int *pair_i, const int *pair_j, const int *shift,
+                               const double *hist, const dem_config *cfg, int ntypes,
+                               const double *Yeff, const double *Geff, const double *betaeff,
+                               const double *coeffFrict, const double *coeffRollFrict,
+                               const double *coeffRestLog, double charVel, double *f,
+                               double *torque, void *stream);
+
 /* Diagnostic without a reference counterpart: FP64 FMA throughput of the
  * current device in TFLOP/s (dependent-chain-free DFMA loop), used as the
  * FP64 roofline denominator. */

@@ -16,7 +16,7 @@ LIB = os.path.join(BUILD, "libdemgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
                   "-Xptxas", "-warn-spills"]
-SOURCES = ["dem_kernels.cu", "dem_capi.cu", "dem_probe.cu"]
+SOURCES = ["dem_kernels.cu", "dem_capi.cu", "dem_probe.cu", "dem_noalloc.cu"]
 
 
 def nvcc():
