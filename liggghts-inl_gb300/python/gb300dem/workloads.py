@@ -49,6 +49,106 @@ def sphere_mass(radius, density):
     return 4.0 * MY_PI / 3.0 * r * r * r * np.asarray(density, dtype=np.float64)
 
 
+def cone_mesh(r_out, r_top, half_angle_deg, n_az, n_ax, z_out=0.0):
+    """Triangles of a conical hopper wall (axis z, outlet at z_out).
+
+    n_az x n_ax quads between rings of radius r(z) = r_out + (z - z_out) tan(a),
+    each split into two triangles; returns nodes[ntri, 3, 3].
+    """
+    ta = math.tan(math.radians(half_angle_deg))
+    z_top = z_out + (r_top - r_out) / ta
+    zs = np.linspace(z_out, z_top, n_ax + 1)
+    th = np.linspace(0.0, 2.0 * math.pi, n_az + 1)
+    tri = []
+    for k in range(n_ax):
+        r0 = r_out + (zs[k] - z_out) * ta
+        r1 = r_out + (zs[k + 1] - z_out) * ta
+        for j in range(n_az):
+            jn = (j + 1) % n_az  # the seam reuses the nodes of column 0 exactly
+            c0, s0 = math.cos(th[j]), math.sin(th[j])
+            c1, s1 = math.cos(th[jn]), math.sin(th[jn])
+            a = (r0 * c0, r0 * s0, zs[k])
+            b = (r0 * c1, r0 * s1, zs[k])
+            c = (r1 * c1, r1 * s1, zs[k + 1])
+            d = (r1 * c0, r1 * s0, zs[k + 1])
+            tri.append((a, b, c))
+            tri.append((a, c, d))
+    return np.array(tri, dtype=np.float64), z_top
+
+
+def write_stl(path, nodes):
+    """ASCII STL of nodes[ntri, 3, 3] (facet normals from the node order)."""
+    with open(path, "w") as f:
+        f.write("solid mesh\n")
+        for t in nodes:
+            n = np.cross(t[1] - t[0], t[2] - t[0])
+            nn = np.linalg.norm(n)
+            n = n / nn if nn > 0 else n
+            f.write("  facet normal %.17g %.17g %.17g\n    outer loop\n" % tuple(n))
+            for p in t:
+                f.write("      vertex %.17g %.17g %.17g\n" % tuple(p))
+            f.write("    endloop\n  endfacet\n")
+        f.write("endsolid mesh\n")
+
+
+def hopper_case(seed, r_out, r_top, half_angle_deg, n_az, n_ax, spacing, radius=(1e-3, 1e-3),
+                density=2500.0, fill_height=None, vmax=0.0, wmax=0.0, E=(5e6,), nu=(0.45,),
+                rest=((0.9,),), frict=((0.5,),), rollfrict=None, rolling_model=0, dt=1e-6,
+                skin=5e-4, gravity=(0.0, 0.0, -9.81), jitter=0.0, z_below=None, normal_model=0,
+                charVel=0.0, max_atoms=None, clearance=None):
+    """Conical hopper (triangle mesh, outlet open) filled with a jittered lattice.
+
+    The box is non-periodic; atoms falling below z_below are lost at the next
+    neighbour rebuild, as with `thermo_modify lost ignore` in the reference.
+    """
+    rng = np.random.default_rng(seed)
+    nodes, z_top = cone_mesh(r_out, r_top, half_angle_deg, n_az, n_ax)
+    ta = math.tan(math.radians(half_angle_deg))
+    rmax = radius[1]
+    if clearance is None:
+        clearance = 0.25 * spacing  # negative: the outer ring overlaps the wall
+    zf = z_top if fill_height is None else fill_height
+    pts = []
+    nxy = int(2 * r_top / spacing) + 2
+    nz = int((zf - rmax) / spacing) + 1
+    for k in range(nz):
+        z = rmax * 1.5 + k * spacing
+        for i in range(nxy):
+            for j in range(nxy):
+                x = -r_top + (i + 0.5) * spacing
+                y = -r_top + (j + 0.5) * spacing
+                # inside the cone with one radius of clearance measured normal to the wall
+                R = r_out + z * ta
+                if (math.hypot(x, y) + rmax / math.cos(math.radians(half_angle_deg))) < R - clearance:
+                    pts.append((x, y, z))
+    x = np.array(pts, dtype=np.float64)
+    if max_atoms is not None and len(x) > max_atoms:
+        x = x[np.argsort(x[:, 2], kind="stable")[:max_atoms]]
+    n = len(x)
+    if jitter > 0:
+        x += rng.uniform(-jitter, jitter, size=x.shape)
+    r = rng.uniform(radius[0], radius[1], size=n) if radius[0] != radius[1] else np.full(n, radius[0])
+    v = rng.uniform(-vmax, vmax, size=(n, 3)) if vmax > 0 else np.zeros((n, 3))
+    w = rng.uniform(-wmax, wmax, size=(n, 3)) if wmax > 0 else np.zeros((n, 3))
+    if z_below is None:
+        z_below = -4 * rmax
+    pad = 4 * rmax
+    case = dict(
+        boxlo=(-r_top - pad, -r_top - pad, z_below), boxhi=(r_top + pad, r_top + pad, z_top + pad),
+        periodic=(0, 0, 0), dt=dt, skin=skin, cdf=1.0, neigh=(1, 0, 1), normal_model=normal_model,
+        rolling_model=rolling_model, gravity=gravity, ntypes=1, charVel=charVel, planes=[],
+        meshes=[dict(nodes=nodes, wall_type=1, rolling=rolling_model)],
+        material=dict(E=list(E), nu=list(nu), rest=[list(q) for q in rest],
+                      frict=[list(q) for q in frict],
+                      rollfrict=[list(q) for q in rollfrict] if rollfrict is not None else None,
+                      density=density),
+        atoms=dict(tag=np.arange(1, n + 1, dtype=np.int32), type=np.ones(n, np.int32), x=x, v=v,
+                   omega=w, radius=r, rmass=sphere_mass(r, density)),
+    )
+    case.update(derive_tables(E, nu, rest, frict, rollfrict))
+    return case
+
+
 def lattice_case(seed, nx, ny, nz, spacing, radius=(1e-3, 1e-3), density=2500.0,
                  z0=None, jitter=0.0, vmax=0.0, wmax=0.0, ntypes=1, E=(5e6,), nu=(0.45,),
                  rest=((0.9,),), frict=((0.5,),), rollfrict=None, periodic=(1, 1, 0),

@@ -21,7 +21,8 @@ COHESION_OFF, COHESION_BOND_NONLINEAR = 0, 1
 
 def build(force=False):
     src = os.path.join(HERE, "dem_oracle.c")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    deps = [os.path.join(HERE, f) for f in os.listdir(HERE) if f.endswith((".c", ".h"))]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(map(os.path.getmtime, deps)):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp"
@@ -72,6 +73,9 @@ def lib():
         L.orc_get_wall_history.argtypes = [P, ctypes.c_int, P]
         L.orc_set_contact_history.argtypes = [P, ctypes.c_int, P, P, P]
         L.orc_set_wall_history.argtypes = [P, ctypes.c_int, P]
+        L.orc_add_mesh.argtypes = [P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int, P, P]
+        L.orc_get_mesh_flags.argtypes = [P, ctypes.c_int, P, P]
+        L.orc_get_mesh_contacts.argtypes = [P, ctypes.c_int, P, P, P, P]
         _lib = L
     return _lib
 
@@ -112,6 +116,17 @@ class Oracle:
         L.orc_set_pair_params(self.h, nt, *[_p(a) for a in tabs], float(case.get("charVel", 0.0)))
         for (axis, pos, wtype, roll) in case.get("planes", []):
             L.orc_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll))
+        self.nmesh = 0
+        for m in case.get("meshes", []):
+            nodes = np.ascontiguousarray(m["nodes"], dtype=np.float64)
+            ea = m.get("edge_active")
+            ca = m.get("corner_active")
+            ea = np.ascontiguousarray(ea, dtype=np.uint8) if ea is not None else None
+            ca = np.ascontiguousarray(ca, dtype=np.uint8) if ca is not None else None
+            self._keep += [nodes, ea, ca]
+            self._check(L.orc_add_mesh(self.h, len(nodes), _p(nodes), int(m["wall_type"]),
+                                       int(m.get("rolling", 0)), _p(ea), _p(ca)))
+            self.nmesh += 1
         a = case["atoms"]
         n = len(a["tag"])
         arrs = [np.ascontiguousarray(a[k], dtype=t) for k, t in
@@ -162,6 +177,24 @@ class Oracle:
                    shift=np.zeros((n, 3), np.int32), flag=np.zeros(n, np.int32),
                    hist=np.zeros((n, d)))
         L.orc_get_pairs(self.h, *[_p(out[k]) for k in ("tag_i", "tag_j", "shift", "flag", "hist")])
+        return out
+
+    def mesh_flags(self, k):
+        ntri = len(self._keep_mesh_nodes(k))
+        ea = np.zeros((ntri, 3), np.uint8)
+        ca = np.zeros((ntri, 3), np.uint8)
+        lib().orc_get_mesh_flags(self.h, int(k), _p(ea), _p(ca))
+        return ea, ca
+
+    def _keep_mesh_nodes(self, k):
+        return [a for a in self._keep if isinstance(a, np.ndarray) and a.ndim == 3][k]
+
+    def mesh_contacts(self, k):
+        L = lib()
+        n = L.orc_get_mesh_contacts(self.h, int(k), None, None, None, None)
+        out = dict(tag=np.zeros(n, np.int32), tri=np.zeros(n, np.int32), slot=np.zeros(n, np.int32),
+                   hist=np.zeros((n, 3)))
+        L.orc_get_mesh_contacts(self.h, int(k), *[_p(out[q]) for q in ("tag", "tri", "slot", "hist")])
         return out
 
     def wall_history(self, w):

@@ -36,6 +36,8 @@
 #define CONTACT_NORMAL_MODEL (1 << 0)
 #define CONTACT_TANGENTIAL_MODEL (1 << 2)
 
+#include "oracle_mesh.h"
+
 typedef struct {
   int axis;
   double pos;
@@ -72,6 +74,8 @@ struct orc_sys {
 
   orc_plane planes[8];
   int nplanes;
+  orc_mesh meshes[4];
+  int nmeshes;
 
   double cutneighmax;
   long ntimestep, nrebuilds;
@@ -101,6 +105,13 @@ void orc_destroy(orc_sys *s) {
   free(s->nstart); free(s->nj); free(s->nshift); free(s->nflag); free(s->nhist);
   free(s->pstart); free(s->ptag); free(s->phist);
   for (int w = 0; w < s->nplanes; w++) { free(s->planes[w].nlist); free(s->planes[w].hist); }
+  for (int k = 0; k < s->nmeshes; k++) {
+    orc_mesh *m = &s->meshes[k];
+    free(m->node); free(m->nodev); free(m->edgeVec); free(m->edgeLen); free(m->edgeNorm);
+    free(m->surfNorm); free(m->center); free(m->rBound); free(m->obtuse); free(m->edgeActive);
+    free(m->cornerActive); free(m->nNeighs); free(m->neighFaces); free(m->cstart); free(m->cand);
+    free(m->nslot); free(m->npartner); free(m->partner); free(m->keep); free(m->inter); free(m->hist);
+  }
   free(s);
 }
 
@@ -149,6 +160,74 @@ static void grow_atoms(orc_sys *s, int n) {
   s->torque = (double *)xrealloc(s->torque, n3); s->xhold = (double *)xrealloc(s->xhold, n3);
   s->radius = (double *)xrealloc(s->radius, n1); s->rmass = (double *)xrealloc(s->rmass, n1);
   for (int w = 0; w < s->nplanes; w++) s->planes[w].hist = (double *)xrealloc(s->planes[w].hist, n3);
+  for (int k = 0; k < s->nmeshes; k++) {
+    orc_mesh *m = &s->meshes[k];
+    const size_t ns = (size_t)n * MESH_MAXSLOT;
+    m->nslot = (int *)xrealloc(m->nslot, n * sizeof(int));
+    m->npartner = (int *)xrealloc(m->npartner, n * sizeof(int));
+    m->partner = (int *)xrealloc(m->partner, ns * sizeof(int));
+    m->keep = (unsigned char *)xrealloc(m->keep, ns);
+    m->inter = (unsigned char *)xrealloc(m->inter, ns);
+    m->hist = (double *)xrealloc(m->hist, 3 * ns * sizeof(double));
+  }
+}
+
+/* fix mesh/surface + fix wall/gran ... mesh: nodes[ntri][3][3] in element
+ * order (element id = index).  edge/corner activity: given (the reference's
+ * own flags) or NULL to derive them as SurfaceMesh::buildNeighbours does. */
+int orc_add_mesh(orc_sys *s, int ntri, const double *nodes, int wall_type, int rolling_model,
+                 const unsigned char *edge_active, const unsigned char *corner_active) {
+  if (s->nmeshes >= 4 || s->n > 0) { snprintf(s->err, sizeof s->err, "add meshes before atoms (max 4)"); return -1; }
+  orc_mesh *m = &s->meshes[s->nmeshes++];
+  memset(m, 0, sizeof *m);
+  m->ntri = ntri;
+  m->wall_type = wall_type;
+  m->rolling = rolling_model;
+  const size_t t9 = 9 * (size_t)ntri, t3 = 3 * (size_t)ntri;
+  m->node = (double *)xrealloc(NULL, t9 * sizeof(double));
+  memcpy(m->node, nodes, t9 * sizeof(double));
+  m->edgeVec = (double *)xrealloc(NULL, t9 * sizeof(double));
+  m->edgeNorm = (double *)xrealloc(NULL, t9 * sizeof(double));
+  m->edgeLen = (double *)xrealloc(NULL, t3 * sizeof(double));
+  m->surfNorm = (double *)xrealloc(NULL, t3 * sizeof(double));
+  m->center = (double *)xrealloc(NULL, t3 * sizeof(double));
+  m->rBound = (double *)xrealloc(NULL, ntri * sizeof(double));
+  m->obtuse = (int *)xrealloc(NULL, ntri * sizeof(int));
+  m->edgeActive = (unsigned char *)xrealloc(NULL, t3);
+  m->cornerActive = (unsigned char *)xrealloc(NULL, t3);
+  m->nNeighs = (int *)xrealloc(NULL, ntri * sizeof(int));
+  m->neighFaces = (int *)xrealloc(NULL, 5 * (size_t)ntri * sizeof(int));
+  mesh_geometry(m);
+  mesh_topology(m);
+  if (edge_active) memcpy(m->edgeActive, edge_active, t3);
+  if (corner_active) memcpy(m->cornerActive, corner_active, t3);
+  return 0;
+}
+
+int orc_get_mesh_flags(const orc_sys *s, int k, unsigned char *edge_active, unsigned char *corner_active) {
+  if (k < 0 || k >= s->nmeshes) return -1;
+  const orc_mesh *m = &s->meshes[k];
+  memcpy(edge_active, m->edgeActive, 3 * (size_t)m->ntri);
+  memcpy(corner_active, m->cornerActive, 3 * (size_t)m->ntri);
+  return m->ntri;
+}
+
+/* Mesh contacts: (atom tag, triangle index, slot, history[3]) per occupied slot */
+int orc_get_mesh_contacts(const orc_sys *s, int k, int *tag, int *tri, int *slot, double *hist) {
+  if (k < 0 || k >= s->nmeshes) return -1;
+  const orc_mesh *m = &s->meshes[k];
+  int c = 0;
+  for (int i = 0; i < s->n; i++)
+    for (int q = 0; q < m->nslot[i]; q++) {
+      const int p = m->partner[(size_t)i * MESH_MAXSLOT + q];
+      if (p < 0) continue;
+      if (tag) tag[c] = s->tag[i];
+      if (tri) tri[c] = p;
+      if (slot) slot[c] = q;
+      if (hist) for (int d = 0; d < 3; d++) hist[3 * c + d] = m->hist[3 * ((size_t)i * MESH_MAXSLOT + q) + d];
+      c++;
+    }
+  return c;
 }
 
 int orc_set_atoms(orc_sys *s, int n, const int *tag, const int *type, const double *x,
@@ -166,6 +245,12 @@ int orc_set_atoms(orc_sys *s, int n, const int *tag, const int *type, const doub
   memset(s->f, 0, 3 * (size_t)n * sizeof(double));
   memset(s->torque, 0, 3 * (size_t)n * sizeof(double));
   for (int w = 0; w < s->nplanes; w++) memset(s->planes[w].hist, 0, 3 * (size_t)n * sizeof(double));
+  for (int k = 0; k < s->nmeshes; k++) {
+    orc_mesh *m = &s->meshes[k];
+    for (int i = 0; i < n; i++) { m->nslot[i] = 0; m->npartner[i] = 0; }
+    for (size_t q = 0; q < (size_t)n * MESH_MAXSLOT; q++) { m->partner[q] = -1; m->keep[q] = 0; m->inter[q] = 0; }
+    memset(m->hist, 0, 3 * (size_t)n * MESH_MAXSLOT * sizeof(double));
+  }
   for (int i = 0; i < n; i++) s->prow[i] = -1;
   s->list_valid = 0;
   s->computeflag = 0;
@@ -240,6 +325,18 @@ static void copy_atom(orc_sys *s, int from, int to) {
     s->omega[3 * to + d] = s->omega[3 * from + d]; s->f[3 * to + d] = s->f[3 * from + d];
     s->torque[3 * to + d] = s->torque[3 * from + d];
     for (int w = 0; w < s->nplanes; w++) s->planes[w].hist[3 * to + d] = s->planes[w].hist[3 * from + d];
+  }
+  for (int k = 0; k < s->nmeshes; k++) {
+    orc_mesh *m = &s->meshes[k];
+    m->nslot[to] = m->nslot[from];
+    m->npartner[to] = m->npartner[from];
+    for (int q = 0; q < MESH_MAXSLOT; q++) {
+      m->partner[(size_t)to * MESH_MAXSLOT + q] = m->partner[(size_t)from * MESH_MAXSLOT + q];
+      m->keep[(size_t)to * MESH_MAXSLOT + q] = m->keep[(size_t)from * MESH_MAXSLOT + q];
+      m->inter[(size_t)to * MESH_MAXSLOT + q] = m->inter[(size_t)from * MESH_MAXSLOT + q];
+      for (int d = 0; d < 3; d++)
+        m->hist[3 * ((size_t)to * MESH_MAXSLOT + q) + d] = m->hist[3 * ((size_t)from * MESH_MAXSLOT + q) + d];
+    }
   }
   s->radius[to] = s->radius[from]; s->rmass[to] = s->rmass[from];
 }
@@ -792,6 +889,43 @@ static void gravity_post_force(orc_sys *s) {
   }
 }
 
+/* Walls::Granular::compute_force for one wall contact with overlap -deltan,
+ * wall-to-particle vector -delta (src/fix_wall_gran_base.h:159-372) */
+static void wall_contact(orc_sys *s, int ip, double deltan, const double *delta, double *hist,
+                         const double *vwall, int wall_type, int rolling, int shearupdate) {
+  sidata_t sd;
+  memset(&sd, 0, sizeof sd);
+  sd.is_wall = 1;
+  sd.radi = s->radius[ip];
+  const int intersectflag = (deltan <= 0);
+  sd.deltan = -deltan;
+  sd.delta[0] = -delta[0]; sd.delta[1] = -delta[1]; sd.delta[2] = -delta[2];
+  sd.shear = hist;
+  sd.v_i = &s->v[3 * ip]; sd.v_j = vwall; sd.omega_i = &s->omega[3 * ip];
+  sd.r = sd.radi - sd.deltan;
+  sd.rsq = sd.r * sd.r;
+  const double rinv = 1.0 / sd.r;
+  sd.rinv = rinv;
+  sd.contact_flags = NULL;
+  sd.itype = s->type[ip];
+  sd.meff = s->rmass[ip];
+  sd.update_history = shearupdate;
+  sd.jtype = wall_type;
+  sd.en[0] = sd.delta[0] * rinv; sd.en[1] = sd.delta[1] * rinv; sd.en[2] = sd.delta[2] * rinv;
+  sd.radsum = sd.radi;
+  fdata fi, fj;
+  memset(&fi, 0, sizeof fi); memset(&fj, 0, sizeof fj);
+  if (intersectflag) {
+    surfaces_intersect(s, &sd, &fi, &fj, rolling);
+    for (int d = 0; d < 3; d++) {
+      s->f[3 * ip + d] += fi.dF[d];
+      s->torque[3 * ip + d] += fi.dT[d];
+    }
+  } else {
+    surfaces_close(&sd);
+  }
+}
+
 static void plane_post_force(orc_sys *s, orc_plane *pl, int shearupdate) {
   const double cdm1 = s->cfg.contact_distance_factor - 1.0;
   const double vwall[3] = {0., 0., 0.};
@@ -816,38 +950,207 @@ static void plane_post_force(orc_sys *s, orc_plane *pl, int shearupdate) {
     if (deltan > s->cutneighmax) continue;
     double *hist = &pl->hist[3 * ip];
     if (deltan <= 0 || deltan < cdm1 * s->radius[ip]) {
-      const int intersectflag = (deltan <= 0);
-      sd.deltan = -deltan;
-      sd.delta[0] = -delta[0]; sd.delta[1] = -delta[1]; sd.delta[2] = -delta[2];
-      sd.shear = hist;
-      /* Walls::Granular::compute_force */
-      sd.v_i = &s->v[3 * ip]; sd.v_j = vwall; sd.omega_i = &s->omega[3 * ip];
-      sd.r = sd.radi - sd.deltan;
-      sd.rsq = sd.r * sd.r;
-      const double rinv = 1.0 / sd.r;
-      sd.rinv = rinv;
-      sd.contact_flags = NULL;
-      sd.itype = s->type[ip];
-      sd.meff = s->rmass[ip];
-      sd.update_history = shearupdate;
-      sd.jtype = pl->wall_type;
-      sd.en[0] = sd.delta[0] * rinv; sd.en[1] = sd.delta[1] * rinv; sd.en[2] = sd.delta[2] * rinv;
-      sd.radsum = sd.radi;
-      fdata fi, fj;
-      memset(&fi, 0, sizeof fi); memset(&fj, 0, sizeof fj);
-      if (intersectflag) {
-        surfaces_intersect(s, &sd, &fi, &fj, pl->rolling_model);
-        for (int d = 0; d < 3; d++) {
-          s->f[3 * ip + d] += fi.dF[d];
-          s->torque[3 * ip + d] += fi.dT[d];
-        }
-      } else {
-        surfaces_close(&sd);
-      }
+      wall_contact(s, ip, deltan, delta, hist, vwall, pl->wall_type, pl->rolling_model, shearupdate);
     } else {
       hist[0] = 0.; hist[1] = 0.; hist[2] = 0.;
     }
   }
+}
+
+/* ------------------------------------------------------------------ */
+/* mesh walls                                                           */
+/* ------------------------------------------------------------------ */
+
+#define SLOT(m, i, q) ((size_t)(i) * MESH_MAXSLOT + (q))
+
+static void mesh_swap(orc_mesh *m, int i, int a, int b, int keepflag) {
+  int t = m->partner[SLOT(m, i, a)];
+  m->partner[SLOT(m, i, a)] = m->partner[SLOT(m, i, b)];
+  m->partner[SLOT(m, i, b)] = t;
+  for (int d = 0; d < 3; d++) {
+    double h = m->hist[3 * SLOT(m, i, a) + d];
+    m->hist[3 * SLOT(m, i, a) + d] = m->hist[3 * SLOT(m, i, b) + d];
+    m->hist[3 * SLOT(m, i, b) + d] = h;
+  }
+  if (keepflag) {
+    unsigned char k = m->keep[SLOT(m, i, a)];
+    m->keep[SLOT(m, i, a)] = m->keep[SLOT(m, i, b)];
+    m->keep[SLOT(m, i, b)] = k;
+    k = m->inter[SLOT(m, i, a)];
+    m->inter[SLOT(m, i, a)] = m->inter[SLOT(m, i, b)];
+    m->inter[SLOT(m, i, b)] = k;
+  }
+}
+
+/* FixContactHistoryMesh::sort_contacts (pre_exchange) */
+static void mesh_sort_contacts(orc_sys *s, orc_mesh *m) {
+  for (int i = 0; i < s->n; i++) {
+    const int nn = m->nslot[i];
+    if (nn == 0) continue;
+    int fe, lf;
+    do {
+      fe = lf = -1;
+      for (int j = 0; j < nn; j++) {
+        if (fe == -1 && m->partner[SLOT(m, i, j)] == -1) fe = j;
+        if (m->partner[SLOT(m, i, j)] >= 0) lf = j;
+      }
+      if (fe > -1 && lf > -1 && fe < lf) mesh_swap(m, i, fe, lf, 1);
+    } while (fe > -1 && lf > -1 && fe < lf);
+  }
+}
+
+static int in_candidates(const orc_mesh *m, int t, int i) {
+  for (int k = m->cstart[t]; k < m->cstart[t + 1]; k++)
+    if (m->cand[k] == i) return 1;
+  return 0;
+}
+
+/* FixNeighlistMesh::pre_force then FixContactHistoryMesh::pre_force */
+static int mesh_neighbors(orc_sys *s, orc_mesh *m) {
+  const int moving = m->nodev != NULL;
+  const double cnm = s->cutneighmax, skin = s->cfg.skin;
+  const double rmax = 0.5 * (cnm - skin);
+  const double small_delta = skin / (70. * M_PI);
+  const double tskin = moving ? skin : 0.5 * skin;
+  const double distmax = moving ? cnm + small_delta : cnm - rmax + small_delta;
+  const double cdf = s->cfg.contact_distance_factor;
+  int *cnt = (int *)calloc(s->n + 1, sizeof(int));
+  free(m->cstart);
+  m->cstart = (int *)malloc((m->ntri + 1) * sizeof(int));
+  int cap = 1024, np = 0;
+  int *cand = (int *)malloc(cap * sizeof(int));
+  for (int t = 0; t < m->ntri; t++) {
+    m->cstart[t] = np;
+    double lo[3], hi[3];
+    for (int d = 0; d < 3; d++) {
+      lo[d] = hi[d] = MN(m, t, 0)[d];
+      for (int q = 1; q < 3; q++) {
+        const double v = MN(m, t, q)[d];
+        lo[d] = v < lo[d] ? v : lo[d];
+        hi[d] = v > hi[d] ? v : hi[d];
+      }
+      lo[d] -= distmax;
+      hi[d] += distmax;
+    }
+    for (int i = 0; i < s->n; i++) {
+      const double *x = &s->x[3 * i];
+      if (x[0] < lo[0] || x[0] > hi[0] || x[1] < lo[1] || x[1] > hi[1] || x[2] < lo[2] || x[2] > hi[2])
+        continue;
+      if (!tri_sphere_neighbuild(m, t, s->radius[i] * cdf, x, tskin)) continue;
+      if (np == cap) { cap *= 2; cand = (int *)xrealloc(cand, cap * sizeof(int)); }
+      cand[np++] = i;
+      cnt[i]++;
+    }
+  }
+  m->cstart[m->ntri] = np;
+  free(m->cand);
+  m->cand = cand;
+  for (int i = 0; i < s->n; i++) {
+    if (cnt[i] > MESH_MAXSLOT) {
+      snprintf(s->err, sizeof s->err, "mesh slot overflow");
+      free(cnt);
+      return -1;
+    }
+    /* cleanUpContactJumps */
+    int ip = 0;
+    while (ip < m->npartner[i]) {
+      const int t = m->partner[SLOT(m, i, ip)];
+      if (!in_candidates(m, t, i)) {
+        m->partner[SLOT(m, i, ip)] = -1;
+        for (int d = 0; d < 3; d++) m->hist[3 * SLOT(m, i, ip) + d] = 0.0;
+        mesh_swap(m, i, ip, m->npartner[i] - 1, 0);
+        m->npartner[i]--;
+      } else
+        ip++;
+    }
+    /* new pages: partners keep their slots, the rest is empty */
+    for (int q = m->npartner[i]; q < MESH_MAXSLOT; q++) {
+      m->partner[SLOT(m, i, q)] = -1;
+      for (int d = 0; d < 3; d++) m->hist[3 * SLOT(m, i, q) + d] = 0.0;
+    }
+    m->nslot[i] = cnt[i];
+  }
+  free(cnt);
+  return 0;
+}
+
+static int mesh_coplanar_already(const orc_mesh *m, int i, int t) {
+  for (int q = 0; q < m->nslot[i]; q++) {
+    const int p = m->partner[SLOT(m, i, q)];
+    if (p >= 0 && p != t && coplanar_node_neighs(m, p, t) && m->keep[SLOT(m, i, q)]) return 1;
+  }
+  return 0;
+}
+
+/* FixContactHistoryMesh::handleContact; returns the slot or -1 (no contact) */
+static int mesh_handle_contact(orc_sys *s, orc_mesh *m, int i, int t, int intersect, int faceflag) {
+  for (int q = 0; q < m->nslot[i]; q++)
+    if (m->partner[SLOT(m, i, q)] == t) {
+      m->keep[SLOT(m, i, q)] = 1;
+      m->inter[SLOT(m, i, q)] = (unsigned char)intersect;
+      return q;
+    }
+  if (faceflag && mesh_coplanar_already(m, i, t)) return -1;
+  if (m->npartner[i] >= m->nslot[i]) {
+    snprintf(s->err, sizeof s->err, "mesh contact slots exhausted");
+    return -1;
+  }
+  int slot = -1;
+  for (int q = 0; q < m->nslot[i]; q++)
+    if (m->partner[SLOT(m, i, q)] == -1) { slot = q; break; }
+  m->partner[SLOT(m, i, slot)] = t;
+  m->keep[SLOT(m, i, slot)] = 1;
+  m->inter[SLOT(m, i, slot)] = (unsigned char)intersect;
+  for (int d = 0; d < 3; d++) m->hist[3 * SLOT(m, i, slot) + d] = 0.0;
+  m->npartner[i]++;
+  if (faceflag)
+    for (int q = 0; q < m->nslot[i]; q++) {
+      const int p = m->partner[SLOT(m, i, q)];
+      if (p >= 0 && p != t && coplanar_node_neighs(m, p, t))
+        for (int d = 0; d < 3; d++) m->hist[3 * SLOT(m, i, slot) + d] = m->hist[3 * SLOT(m, i, q) + d];
+    }
+  return slot;
+}
+
+/* FixWallGran::post_force_mesh */
+static void mesh_post_force(orc_sys *s, orc_mesh *m, int shearupdate) {
+  const double cdm1 = s->cfg.contact_distance_factor - 1.0;
+  for (int i = 0; i < s->n; i++)
+    for (int q = 0; q < m->nslot[i]; q++) {
+      m->keep[SLOT(m, i, q)] = 0;
+      m->inter[SLOT(m, i, q)] = 0;
+    }
+  for (int t = 0; t < m->ntri; t++) {
+    for (int k = m->cstart[t]; k < m->cstart[t + 1]; k++) {
+      const int ip = m->cand[k];
+      double delta[3], bary[3];
+      int bs;
+      const double deltan = resolve_tri_sphere(m, t, s->radius[ip], &s->x[3 * ip], delta, bary, &bs);
+      if (deltan > s->cutneighmax) continue;
+      const int intersect = deltan <= 0;
+      if (deltan <= 0 || deltan < cdm1 * s->radius[ip]) {
+        const int slot = mesh_handle_contact(s, m, ip, t, intersect, bs == 7);
+        if (slot < 0) continue;
+        double vwall[3] = {0., 0., 0.};
+        if (m->nodev) {
+          const double *vn = &m->nodev[9 * (size_t)t];
+          for (int d = 0; d < 3; d++)
+            vwall[d] = (bary[0] * vn[d] + bary[1] * vn[3 + d] + bary[2] * vn[6 + d]);
+        }
+        wall_contact(s, ip, deltan, delta, &m->hist[3 * SLOT(m, ip, slot)], vwall, m->wall_type,
+                     m->rolling, shearupdate);
+      }
+    }
+  }
+  /* cleanUpContacts */
+  for (int i = 0; i < s->n; i++)
+    for (int q = 0; q < m->nslot[i]; q++)
+      if (!m->keep[SLOT(m, i, q)]) {
+        if (m->partner[SLOT(m, i, q)] > -1) m->npartner[i]--;
+        m->partner[SLOT(m, i, q)] = -1;
+        m->inter[SLOT(m, i, q)] = 0;
+        for (int d = 0; d < 3; d++) m->hist[3 * SLOT(m, i, q) + d] = 0.0;
+      }
 }
 
 static void force_clear(orc_sys *s) {
@@ -908,9 +1211,12 @@ static int decide(orc_sys *s) {
 
 static int rebuild(orc_sys *s) {
   if (s->computeflag) pre_exchange(s);
+  for (int k = 0; k < s->nmeshes; k++) mesh_sort_contacts(s, &s->meshes[k]);
   pbc_and_exchange(s);
   if (neighbor_build(s)) return -1;
   plane_neighbors(s);
+  for (int k = 0; k < s->nmeshes; k++)
+    if (mesh_neighbors(s, &s->meshes[k])) return -1;
   return 0;
 }
 
@@ -919,6 +1225,7 @@ static void compute_forces(orc_sys *s, int shearupdate) {
   pair_compute(s, shearupdate);
   gravity_post_force(s);
   for (int w = 0; w < s->nplanes; w++) plane_post_force(s, &s->planes[w], shearupdate);
+  for (int k = 0; k < s->nmeshes; k++) mesh_post_force(s, &s->meshes[k], shearupdate);
 }
 
 int orc_setup(orc_sys *s) {

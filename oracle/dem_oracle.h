@@ -55,6 +55,15 @@ int orc_set_pair_params(orc_sys *s, int ntypes, const double *Yeff, const double
 /* fix wall/gran ... primitive type WTYPE {x,y,z}plane POS (axis 0/1/2). */
 int orc_add_plane(orc_sys *s, int axis, double pos, int wall_type, int rolling_model);
 
+/* fix mesh/surface + fix wall/gran mesh: nodes[ntri*9], element id = index.
+ * edge_active/corner_active[ntri*3]: the reference's flags, or NULL to derive
+ * them as SurfaceMesh::buildNeighbours does.  Add meshes before atoms. */
+int orc_add_mesh(orc_sys *s, int ntri, const double *nodes, int wall_type, int rolling_model,
+                 const unsigned char *edge_active, const unsigned char *corner_active);
+int orc_get_mesh_flags(const orc_sys *s, int mesh, unsigned char *edge_active,
+                       unsigned char *corner_active);
+int orc_get_mesh_contacts(const orc_sys *s, int mesh, int *tag, int *tri, int *slot, double *hist);
+
 int orc_set_atoms(orc_sys *s, int n, const int *tag, const int *type, const double *x,
                   const double *v, const double *omega, const double *radius,
                   const double *rmass);

@@ -27,6 +27,9 @@
 #include "pair_gran.h"
 #include "update.h"
 #include "fix_property_atom.h"
+#include "fix_mesh_surface.h"
+#include "fix_contact_history_mesh.h"
+#include "tri_mesh.h"
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -143,6 +146,61 @@ void FixOracleSnapshot::write_snapshot()
         w[(size_t)i * wd + d] = (wd == 1 && fpa->vector_atom) ? fpa->vector_atom[i]
                                                               : fpa->array_atom[i][d];
     put(fp, w.data(), w.size());
+  }
+
+  // triangle meshes of fix mesh/surface: geometry, edge/corner activity
+  // (SurfaceMesh::buildNeighbours) and the per-atom mesh contact slots of
+  // FixContactHistoryMesh (partner triangle id or -1, history)
+  std::vector<FixMeshSurface*> meshes;
+  for (int k = 0; k < modify->nfix; k++)
+    if (strcmp(modify->fix[k]->style, "mesh/surface") == 0)
+      meshes.push_back(static_cast<FixMeshSurface*>(modify->fix[k]));
+  int32_t nm = (int32_t)meshes.size();
+  put(fp, &nm, 1);
+  for (size_t k = 0; k < meshes.size(); k++) {
+    FixMeshSurface *fm = meshes[k];
+    TriMesh *mesh = fm->triMesh();
+    int32_t len = (int32_t)strlen(fm->id);
+    put(fp, &len, 1);
+    fwrite(fm->id, 1, len, fp);
+    int32_t ntri = mesh->sizeLocal();
+    put(fp, &ntri, 1);
+    std::vector<int32_t> ids(ntri);
+    std::vector<double> nodes(9 * (size_t)ntri);
+    std::vector<uint8_t> act(6 * (size_t)ntri);
+    for (int t = 0; t < ntri; t++) {
+      ids[t] = mesh->id(t);
+      for (int q = 0; q < 3; q++) {
+        mesh->node(t, q, &nodes[9 * (size_t)t + 3 * q]);
+        act[6 * (size_t)t + q] = mesh->edgeActive(t, q) ? 1 : 0;
+        act[6 * (size_t)t + 3 + q] = mesh->cornerActive(t, q) ? 1 : 0;
+      }
+    }
+    put(fp, ids.data(), ntri);
+    put(fp, nodes.data(), nodes.size());
+    put(fp, act.data(), act.size());
+    FixContactHistoryMesh *ch = fm->contactHistory();
+    int32_t md = ch ? ch->get_dnum() : 0;
+    put(fp, &md, 1);
+    std::vector<int32_t> nslot(nlocal, 0), npart(nlocal, 0), part;
+    std::vector<double> mh;
+    if (ch) {
+      for (int i = 0; i < nlocal; i++) {
+        nslot[i] = ch->nneighs(i);
+        npart[i] = ch->n_partner(i);
+        for (int s = 0; s < nslot[i]; s++) {
+          part.push_back(ch->get_partner_idTri(i, s));
+          const double *h = ch->contacthistory(i, s);
+          for (int d = 0; d < md; d++) mh.push_back(h[d]);
+        }
+      }
+    }
+    put(fp, nslot.data(), nlocal);
+    put(fp, npart.data(), nlocal);
+    int32_t ns = (int32_t)part.size();
+    put(fp, &ns, 1);
+    put(fp, part.data(), part.size());
+    put(fp, mh.data(), mh.size());
   }
   fclose(fp);
 }

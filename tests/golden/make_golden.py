@@ -43,6 +43,17 @@ def cases():
         seed=5, nx=6, ny=6, nz=4, spacing=1.97e-3, radius=(1e-3, 1e-3), z0=0.995e-3,
         jitter=2e-5, vmax=1.5, wmax=80.0, normal_model=1, charVel=0.5),
         300, [0, 1, 10, 100, 300])
+    # conical hopper wall (triangle mesh), outlet open: atoms leave the box
+    c["hopper_mesh"] = (workloads.hopper_case(
+        seed=31, r_out=3e-3, r_top=14e-3, half_angle_deg=30.0, n_az=24, n_ax=5,
+        spacing=2.05e-3, radius=(0.9e-3, 1.0e-3), jitter=3e-5, vmax=1.5, wmax=100.0,
+        fill_height=12e-3, clearance=-0.6e-3), 600, [0, 1, 2, 10, 50, 100, 200, 400, 600])
+    c["hopper_mesh_cdt"] = (workloads.hopper_case(
+        seed=37, r_out=3e-3, r_top=14e-3, half_angle_deg=30.0, n_az=16, n_ax=4,
+        spacing=2.05e-3, radius=(0.9e-3, 1.0e-3), jitter=3e-5, vmax=1.5, wmax=100.0,
+        fill_height=12e-3, rollfrict=((0.3,),), rolling_model=1, density=1500.0, E=(1e7,),
+        nu=(0.3,), rest=((0.5,),), frict=((0.6,),), clearance=-0.6e-3),
+        400, [0, 1, 10, 100, 200, 400])
     return c
 
 
@@ -96,6 +107,15 @@ def write_inputs(case, d, nsteps, snaps):
             wm += " rolling_friction cdt"
         s.append("fix wall%d all wall/gran %s primitive type %d %splane %s"
                  % (k, wm, wtype, "xyz"[axis], fmt(pos)))
+    for k, m in enumerate(case.get("meshes", [])):
+        workloads.write_stl(os.path.join(d, "mesh%d.stl" % k), m["nodes"])
+        s.append("fix cad%d all mesh/surface file mesh%d.stl type %d" % (k, k, m["wall_type"]))
+        wm = "model %s tangential history" % ("hooke" if case["normal_model"] == 1 else "hertz")
+        if m.get("rolling", 0) == 1:
+            wm += " rolling_friction cdt"
+        s.append("fix mwall%d all wall/gran %s mesh n_meshes 1 meshes cad%d" % (k, wm, k))
+    if not all(case["periodic"]):
+        s.append("thermo_modify lost ignore")
     s += ["fix integr all nve/sphere",
           "fix snap all oracle/snapshot snap %s" % " ".join(str(t) for t in snaps),
           "thermo 100", "run %d" % nsteps]
@@ -128,6 +148,26 @@ def read_snapshot(path):
         name = b[off:off + ln].decode(); off += ln
         wd = int(take(np.int32, 1)[0])
         walls[name] = take(np.float64, nlocal * wd).reshape(nlocal, wd)
+    meshes = []
+    if off < len(b):
+        nm = int(take(np.int32, 1)[0])
+        for _ in range(nm):
+            ln = int(take(np.int32, 1)[0])
+            name = b[off:off + ln].decode(); off += ln
+            ntri = int(take(np.int32, 1)[0])
+            ids = take(np.int32, ntri)
+            mnodes = take(np.float64, 9 * ntri).reshape(ntri, 3, 3)
+            act = np.frombuffer(b, dtype=np.uint8, count=6 * ntri, offset=off).reshape(ntri, 6)
+            off += 6 * ntri
+            md = int(take(np.int32, 1)[0])
+            nslot = take(np.int32, nlocal)
+            npart = take(np.int32, nlocal)
+            ns = int(take(np.int32, 1)[0])
+            part = take(np.int32, ns)
+            mh = take(np.float64, ns * md).reshape(ns, md)
+            meshes.append(dict(name=name, ids=ids, nodes=mnodes, edge_active=act[:, :3].copy(),
+                               corner_active=act[:, 3:].copy(), nslot=nslot, npart=npart,
+                               part=part, hist=mh))
     # canonical pairs: tags plus periodic image of j
     L = boxhi - boxlo
     owner = {int(t): i for i, t in enumerate(tag[:nlocal])}
@@ -146,13 +186,33 @@ def read_snapshot(path):
         snap[k] = vec[k][:nlocal][order]
     for k, (name, w) in enumerate(sorted(walls.items())):
         snap["wall%d_hist" % k] = w[order]
+    # mesh contacts as (atom tag, triangle id, history) triples, plus the
+    # per-atom slot layout (for slot-order checks) and the mesh topology
+    starts = None
+    for k, m in enumerate(meshes):
+        starts = np.concatenate([[0], np.cumsum(m["nslot"])])
+        mt, mtri, mhist, mslot = [], [], [], []
+        for i in range(nlocal):
+            for s_ in range(m["nslot"][i]):
+                pidx = starts[i] + s_
+                if m["part"][pidx] >= 0:
+                    mt.append(int(tag[i])); mtri.append(int(m["part"][pidx]))
+                    mhist.append(m["hist"][pidx]); mslot.append(s_)
+        snap["mesh%d_contact_tag" % k] = np.array(mt, np.int32)
+        snap["mesh%d_contact_tri" % k] = np.array(mtri, np.int32)
+        snap["mesh%d_contact_hist" % k] = np.array(mhist, np.float64).reshape(-1, 3)
+        snap["mesh%d_contact_slot" % k] = np.array(mslot, np.int32)
+        snap["mesh%d_nslot" % k] = m["nslot"][order]
+        snap["mesh%d_ids" % k] = m["ids"]
+        snap["mesh%d_edge_active" % k] = m["edge_active"]
+        snap["mesh%d_corner_active" % k] = m["corner_active"]
     return snap
 
 
 def run_case(name, case, nsteps, snaps):
     with tempfile.TemporaryDirectory() as d:
         write_inputs(case, d, nsteps, snaps)
-        subprocess.check_call([LMP, "-in", "in.case", "-log", "log.case", "-screen", "none"], cwd=d)
+        subprocess.check_call([LMP, "-in", "in.case", "-log", "log.case", "-screen", "screen.case"], cwd=d)
         out = {}
         for st in snaps:
             sn = read_snapshot(os.path.join(d, "snap.%d.bin" % st))
@@ -160,8 +220,12 @@ def run_case(name, case, nsteps, snaps):
                 if k != "step":
                     out["s%d_%s" % (st, k)] = v
         loop = [l for l in open(os.path.join(d, "log.case")) if l.startswith("Loop time")]
-    meta = {k: v for k, v in case.items() if k != "atoms" and not isinstance(v, np.ndarray)}
+    meta = {k: v for k, v in case.items() if k not in ("atoms", "meshes") and not isinstance(v, np.ndarray)}
     meta.update(nsteps=nsteps, snaps=snaps, loop=loop)
+    meta["meshes"] = [dict(wall_type=m["wall_type"], rolling=m.get("rolling", 0))
+                      for m in case.get("meshes", [])]
+    for k, m in enumerate(case.get("meshes", [])):
+        out["mesh%d_nodes" % k] = m["nodes"]
     a = case["atoms"]
     # the reference's rmass (identical formula) is what the runs start from
     np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta),

@@ -32,6 +32,7 @@ def load_golden(name):
     case["neigh"] = tuple(meta["neigh"])
     case["gravity"] = tuple(meta["gravity"]) if meta["gravity"] is not None else None
     case["planes"] = [tuple(p) for p in meta["planes"]]
+    case["meshes"] = [dict(m, nodes=z["mesh%d_nodes" % k]) for k, m in enumerate(meta.get("meshes", []))]
     for k in ("Yeff", "Geff", "betaeff", "coeffFrict", "coeffRollFrict", "coeffRestLog"):
         case[k] = z[k]
     case["atoms"] = dict(tag=z["init_tag"], type=z["init_type"], x=z["init_x"], v=z["init_v"],

@@ -47,6 +47,45 @@ def test_oracle_matches_reference(name):
     assert o.nrebuilds >= 2, "fixture must exercise history carry-over across rebuilds"
 
 
+MESH_CASES = ["hopper_mesh", "hopper_mesh_cdt"]
+
+
+def mesh_contact_map(tags, tris, slots, hists):
+    return {(int(t), int(tr)): (int(sl), np.asarray(h)) for t, tr, sl, h in zip(tags, tris, slots, hists)}
+
+
+@pytest.mark.parametrize("name", MESH_CASES)
+def test_oracle_mesh_walls_match_reference(name):
+    """Triangle-mesh walls: the derived edge/corner activity equals the
+    reference's, and the mesh contact set, slot layout and histories match at
+    every snapshot (including atoms leaving through the outlet)."""
+    case, snaps = load_golden(name)
+    o = Oracle(case)
+    ea, ca = o.mesh_flags(0)
+    assert np.array_equal(ea, snaps[0]["mesh0_edge_active"])
+    assert np.array_equal(ca, snaps[0]["mesh0_corner_active"])
+    o.setup()
+    prev = 0
+    for st in sorted(snaps):
+        if st > prev:
+            o.run(st - prev)
+            prev = st
+        g = sort_by_tag(o.atoms())
+        r = snaps[st]
+        assert np.array_equal(g["tag"], r["tag"])
+        tol = FORCE_RTOL if st <= 100 else 1e-9
+        assert max_rel(g["f"], r["f"]) < tol and max_rel(g["torque"], r["torque"]) < tol, (name, st)
+        mc = o.mesh_contacts(0)
+        gm = mesh_contact_map(mc["tag"], mc["tri"], mc["slot"], mc["hist"])
+        rm = mesh_contact_map(r["mesh0_contact_tag"], r["mesh0_contact_tri"], r["mesh0_contact_slot"],
+                              r["mesh0_contact_hist"])
+        assert set(gm) == set(rm), (name, st)
+        assert all(gm[k][0] == rm[k][0] for k in rm), "slot layout differs"
+        hs = max([np.abs(v[1]).max() for v in rm.values()] + [1e-300])
+        assert max([np.abs(gm[k][1] - rm[k][1]).max() for k in rm] + [0.0]) / hs < HIST_RTOL
+    assert len(snaps[0]["mesh0_contact_tag"]) > 20, "fixture must start with wall contacts"
+
+
 def test_fixture_has_periodic_and_wall_contacts():
     case, snaps = load_golden("dense_hertz")
     s0 = snaps[0]
