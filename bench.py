@@ -36,6 +36,24 @@ METRIC = "particle-steps/s (1M Hertz/history spheres)"
 
 def workload(name, scale=1.0, seed=2024):
     from gb300dem import workloads
+    if name == "hopper1m":
+        # configs[1]: conical hopper (half-angle 30 deg, top radius 0.25 m,
+        # outlet radius 0.03 m, 256 x 64 quads = 32,768 triangles), outlet open,
+        # radii U[0.8, 1.2] mm, rho 1500, E 1e7, e 0.5, mu 0.6, CDT rolling 0.3
+        # on pairs and wall, dt 5e-7; the lowest 1M sites of a jittered lattice
+        case = workloads.hopper_case(
+            seed=seed, r_out=0.03, r_top=0.25, half_angle_deg=30.0, n_az=256, n_ax=64,
+            spacing=2.2e-3, radius=(0.8e-3, 1.2e-3), density=1500.0, jitter=1e-4, E=(1e7,),
+            nu=(0.45,), rest=((0.5,),), frict=((0.6,),), rollfrict=((0.3,),), rolling_model=1,
+            dt=5e-7, skin=5e-4, max_atoms=max(1000, int(round(1_000_000 * scale))),
+            clearance=-1e-4, z_below=-0.02)
+        desc = dict(workload="hopper1m", atoms=int(len(case["atoms"]["tag"])), triangles=32768,
+                    description="configs[1] conical hopper discharge: triangle-mesh cone "
+                                "(32,768 triangles), outlet open, polydisperse Hertz/history + CDT "
+                                "rolling (pair and wall), jittered lattice (2.2 mm) filling the "
+                                "cone from the outlet up, dt 5e-7",
+                    l2="state + neighbour list > L2 (129 MB); no flush needed")
+        return case, desc
     if name == "column1m":
         # configs[1] materials (r U[0.8,1.2] mm, rho 1500, E 1e7, e 0.5, mu 0.6,
         # CDT 0.3), dense jittered lattice in a periodic column with a floor.
@@ -290,7 +308,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="column1m")
+    ap.add_argument("--workload", default="hopper1m", choices=["hopper1m", "column1m"])
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0,

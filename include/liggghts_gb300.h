@@ -42,7 +42,8 @@ typedef enum dem_status {
   DEM_ERR_TIMEOUT = 5,        /* a bounded device wait gave up */
   DEM_ERR_BOX = 6,            /* periodic box shorter than 3 neighbour cutoffs */
   DEM_ERR_UNSUPPORTED = 7,    /* contact-model combination not on the GPU path */
-  DEM_ERR_NO_DEVICE = 8       /* no CUDA device / kernel image */
+  DEM_ERR_NO_DEVICE = 8,      /* no CUDA device / kernel image */
+  DEM_ERR_CAPACITY = 9        /* a fixed capacity was exceeded (mesh candidates per atom) */
 } dem_status;
 
 enum { DEM_NORMAL_HERTZ = 0, DEM_NORMAL_HOOKE = 1 };
@@ -101,6 +102,28 @@ int dem_derive_hertz_tables(int ntypes, const double *youngs, const double *pois
  * Returns the wall id through *wall_id (may be NULL). */
 int dem_add_plane(dem_handle *h, int axis, double pos, int wall_type, int rolling_model,
                   int *wall_id);
+
+/* fix mesh/surface FILE type WALL_TYPE + fix wall/gran ... mesh n_meshes 1
+ * meshes ID (src/fix_mesh_surface.cpp, src/fix_wall_gran.cpp:803-982):
+ * nodes is ntri*9 (triangle t, node q, coordinate d at 9*t+3*q+d) in element
+ * order, element id = index.  edge_active/corner_active (ntri*3, may be NULL)
+ * are the mesh topology flags the reference's SurfaceMesh::buildNeighbours
+ * produces; NULL derives them the same way (see dem_mesh_topology).
+ * Returns the mesh id through *mesh_id (may be NULL).  Add before atoms. */
+int dem_add_mesh(dem_handle *h, int ntri, const double *nodes, int wall_type, int rolling_model,
+                 const unsigned char *edge_active, const unsigned char *corner_active,
+                 int *mesh_id);
+
+/* Host-only: edge/corner activity of a triangle mesh as SurfaceMesh::buildNeighbours
+ * computes it (src/surface_mesh_I.h:473-1236), ntri*3 flags each. */
+int dem_mesh_topology(int ntri, const double *nodes, unsigned char *edge_active,
+                      unsigned char *corner_active);
+
+/* Mesh contact history as FixContactHistoryMesh keeps it: one entry per
+ * occupied slot (atom tag, triangle id, slot index, 3 history doubles). */
+int dem_mesh_ncontacts(dem_handle *h, int mesh_id, int *ncontacts);
+int dem_download_mesh_contacts(dem_handle *h, int mesh_id, int *tag, int *tri, int *slot,
+                               double *hist);
 
 /* x, v, omega are n*3 (x[3*i+d] == atom->x[i][d]). Resets contact history. */
 int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, const double *x,

@@ -16,6 +16,7 @@
 #include "../../include/liggghts_gb300.h"
 #include "dem_device.cuh"
 #include "dem_kernels.h"
+#include "dem_mesh_host.h"
 
 using namespace gb300;
 
@@ -50,6 +51,7 @@ struct dem_handle {
   cudaGraphExec_t gexec = nullptr;
   long long graph_gen = -1, sys_gen = 0;  // rebuilt when device pointers change
   int graph_kps = 0, graph_kpr = 0;
+  std::vector<MeshHost> mesh_host;
 };
 
 static int ensure_graph(dem_handle *h) {
@@ -155,6 +157,26 @@ static int alloc_atoms(dem_handle *h, int nmax) {
   CUDA_TRY(h, dalloc(L, &s.cell_fill, (size_t)s.ncell + 2));
   long maxlen = std::max<long>(nmax + 1, s.ncell + 2);
   CUDA_TRY(h, dalloc(L, &s.scan_tmp, (maxlen + 4095) / 4096 + 1));
+  for (int k = 0; k < s.nmeshes; k++) {
+    MeshDev &M = s.meshes[k];
+    CUDA_TRY(h, dalloc(L, &M.tc_count, (size_t)s.ncell + 2));
+    CUDA_TRY(h, dalloc(L, &M.tc_start, (size_t)s.ncell + 2));
+    CUDA_TRY(h, dalloc(L, &M.tc_fill, (size_t)s.ncell + 2));
+    CUDA_TRY(h, dalloc(L, &M.tc_list, (size_t)M.tc_cap));
+    CUDA_TRY(h, dalloc(L, &M.cand_n, nmax));
+    CUDA_TRY(h, dalloc(L, &M.cand, (size_t)kMeshMaxCand * nmax));
+    for (int b = 0; b < 2; b++) {
+      CUDA_TRY(h, dalloc(L, &M.nslot[b], nmax));
+      CUDA_TRY(h, dalloc(L, &M.npart[b], nmax));
+      CUDA_TRY(h, dalloc(L, &M.slot_tri[b], (size_t)kMeshMaxCand * nmax));
+      CUDA_TRY(h, dalloc(L, &M.slot_hist[b], (size_t)3 * kMeshMaxCand * nmax));
+    }
+    CUDA_TRY(h, cudaMemset(M.cand_n, 0, nmax * sizeof(int)));
+    CUDA_TRY(h, cudaMemset(M.nslot[0], 0, nmax * sizeof(int)));
+    CUDA_TRY(h, cudaMemset(M.npart[0], 0, nmax * sizeof(int)));
+    CUDA_TRY(h, cudaMemset(M.slot_tri[0], 0xff, (size_t)kMeshMaxCand * nmax * sizeof(int)));
+    CUDA_TRY(h, cudaMemset(M.slot_hist[0], 0, (size_t)3 * kMeshMaxCand * nmax * sizeof(double)));
+  }
   return DEM_OK;
 }
 
@@ -226,6 +248,9 @@ static int recover(dem_handle *h, bool *resumed) {
   if (rc) return rc;
   Ctrl &c = h->host_ctrl;
   if (c.status == kStatNan) return fail(h, DEM_ERR_NAN, "non-finite particle position");
+  if (c.status == kStatMeshSlots)
+    return fail(h, DEM_ERR_CAPACITY, "an atom has more candidate mesh triangles than the per-atom capacity");
+  if (c.status == kStatMeshReg) return fail(h, DEM_ERR_CAPACITY, "mesh triangle-cell registrations overflowed");
   if (!c.halt) return DEM_OK;
   if (c.status != kStatPairOverflow) return fail(h, DEM_ERR_CUDA, "device halted");
   const int want = (int)std::min<long>(2147000000L, std::max<long>((long)c.np_new * 5 / 4 + 1024, 2L * h->s.pcap));
@@ -377,6 +402,77 @@ int dem_add_plane(dem_handle *h, int axis, double pos, int wall_type, int rollin
   return DEM_OK;
 }
 
+int dem_add_mesh(dem_handle *h, int ntri, const double *nodes, int wall_type, int rolling_model,
+                 const unsigned char *edge_active, const unsigned char *corner_active, int *mesh_id) {
+  if (!h || ntri < 1 || !nodes || wall_type < 1) return DEM_ERR_BAD_ARG;
+  if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "add meshes before uploading atoms");
+  if (h->s.nmeshes >= kMaxMeshes) return fail(h, DEM_ERR_BAD_ARG, "too many mesh walls");
+  MeshHost mh;
+  int rc = mesh_prepare(ntri, nodes, edge_active, corner_active, mh);
+  if (rc) return fail(h, rc, "degenerate mesh element");
+  MeshDev &M = h->s.meshes[h->s.nmeshes];
+  M = MeshDev{};
+  M.ntri = ntri;
+  M.wall_type = wall_type;
+  M.rolling = rolling_model == DEM_ROLLING_CDT ? 1 : 0;
+  auto &L = h->allocs_misc;
+  CUDA_TRY(h, dalloc(L, &M.tri, mh.tri.size()));
+  CUDA_TRY(h, cudaMemcpy(M.tri, mh.tri.data(), mh.tri.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, dalloc(L, &M.meta, mh.meta.size()));
+  CUDA_TRY(h, cudaMemcpy(M.meta, mh.meta.data(), mh.meta.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, dalloc(L, &M.cn_start, mh.cn_start.size()));
+  CUDA_TRY(h, cudaMemcpy(M.cn_start, mh.cn_start.data(), mh.cn_start.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, dalloc(L, &M.cn_list, std::max<size_t>(1, mh.cn_list.size())));
+  if (!mh.cn_list.empty())
+    CUDA_TRY(h, cudaMemcpy(M.cn_list, mh.cn_list.data(), mh.cn_list.size() * sizeof(int), cudaMemcpyHostToDevice));
+  if (mesh_id) *mesh_id = h->s.nmeshes;
+  h->mesh_host.push_back(std::move(mh));
+  h->s.nmeshes++;
+  h->sys_gen++;
+  return DEM_OK;
+}
+
+int dem_mesh_ncontacts(dem_handle *h, int mesh_id, int *nc) {
+  if (!h || !h->have_atoms || !nc || mesh_id < 0 || mesh_id >= h->s.nmeshes) return DEM_ERR_BAD_ARG;
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  const int n = h->host_ctrl.n;
+  std::vector<int> np(n);
+  CUDA_TRY(h, cudaMemcpy(np.data(), h->s.meshes[mesh_id].npart[0], n * sizeof(int), cudaMemcpyDeviceToHost));
+  long t = 0;
+  for (int v : np) t += v;
+  *nc = (int)t;
+  return DEM_OK;
+}
+
+int dem_download_mesh_contacts(dem_handle *h, int mesh_id, int *tag, int *tri, int *slot, double *hist) {
+  if (!h || !h->have_atoms || mesh_id < 0 || mesh_id >= h->s.nmeshes) return DEM_ERR_BAD_ARG;
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  const int n = h->host_ctrl.n;
+  const size_t nmax = h->s.nmax;
+  const MeshDev &M = h->s.meshes[mesh_id];
+  std::vector<int> ns(n), st((size_t)kMeshMaxCand * nmax), tags(n);
+  std::vector<double> sh((size_t)3 * kMeshMaxCand * nmax);
+  CUDA_TRY(h, cudaMemcpy(ns.data(), M.nslot[0], n * sizeof(int), cudaMemcpyDeviceToHost));
+  CUDA_TRY(h, cudaMemcpy(st.data(), M.slot_tri[0], st.size() * sizeof(int), cudaMemcpyDeviceToHost));
+  CUDA_TRY(h, cudaMemcpy(sh.data(), M.slot_hist[0], sh.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(h, cudaMemcpy(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost));
+  int c = 0;
+  for (int i = 0; i < n; i++)
+    for (int q = 0; q < ns[i]; q++) {
+      const int t = st[(size_t)q * nmax + i];
+      if (t < 0) continue;
+      if (tag) tag[c] = tags[i];
+      if (tri) tri[c] = t;
+      if (slot) slot[c] = q;
+      if (hist)
+        for (int d = 0; d < 3; d++) hist[3 * (size_t)c + d] = sh[(size_t)(3 * q + d) * nmax + i];
+      c++;
+    }
+  return DEM_OK;
+}
+
 int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, const double *x,
                      const double *v, const double *omega, const double *radius,
                      const double *rmass) {
@@ -388,6 +484,8 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
     if (type[i] < 1 || type[i] > s.ntypes) return fail(h, DEM_ERR_BAD_ARG, "atom type out of range");
   for (int w = 0; w < s.nplanes; w++)
     if (s.planes[w].wall_type > s.ntypes) return fail(h, DEM_ERR_BAD_ARG, "wall type out of range");
+  for (int k = 0; k < s.nmeshes; k++)
+    if (s.meshes[k].wall_type > s.ntypes) return fail(h, DEM_ERR_BAD_ARG, "mesh wall type out of range");
   for (int i = 0; i < n; i++)
     if (!(radius[i] > 0.0) || !(rmass[i] > 0.0)) return fail(h, DEM_ERR_BAD_ARG, "radius and rmass must be > 0");
   // cutneighmax = (maxrad_i + maxrad_j)*cdf + skin, src/pair_gran.cpp:591-602,
@@ -413,6 +511,34 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
   }
   for (int d = 0; d < 3; d++) s.csz[d] = s.prd[d] / s.nc[d];
   s.ncell = (int)ncell;
+  // FixNeighlistMesh::pre_force distmax/skin (static meshes), src/fix_neighlist_mesh.cpp:249-264
+  for (int k = 0; k < s.nmeshes; k++) {
+    MeshDev &M = s.meshes[k];
+    const double rmax = 0.5 * (s.cutneighmax - s.skin);
+    const double small_delta = s.skin / (70. * M_PI);
+    M.distmax = M.moving ? s.cutneighmax + small_delta : s.cutneighmax - rmax + small_delta;
+    M.tskin = M.moving ? s.skin : 0.5 * s.skin;
+    // capacity of the triangle-to-cell registrations, from the initial mesh
+    const MeshHost &mh = h->mesh_host[k];
+    long tot = 0;
+    for (int t = 0; t < mh.ntri; t++) {
+      long cells = 1;
+      for (int d = 0; d < 3; d++) {
+        double a = mh.tri[(size_t)t * kTriStride + d], b = a;
+        for (int q = 1; q < 3; q++) {
+          a = std::min(a, mh.tri[(size_t)t * kTriStride + 3 * q + d]);
+          b = std::max(b, mh.tri[(size_t)t * kTriStride + 3 * q + d]);
+        }
+        auto cc = [&](double x) {
+          long c = (long)((x - s.boxlo[d]) / s.csz[d]);
+          return std::min<long>(std::max<long>(c, 0), s.nc[d] - 1);
+        };
+        cells *= cc(b + M.distmax) - cc(a - M.distmax) + 1 + (M.moving ? 2 : 0);
+      }
+      tot += cells;
+    }
+    M.tc_cap = (int)std::min<long>(2147000000L, 2 * tot + 4096);
+  }
   int rc = alloc_atoms(h, n);
   if (rc) return rc;
   // Initial pair capacity: 16 entries per atom.  LIGGGHTS_GB300_PAIRS_PER_ATOM

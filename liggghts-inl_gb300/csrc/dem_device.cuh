@@ -69,6 +69,8 @@ struct Ctrl {
   long long ntimestep, nrebuilds;
   int halt_step;
   int loop_left;    // steps left for the device-side step loop (graph WHILE node)
+  int mesh_moved;   // a moving mesh node travelled > skin/2 since the last build
+  int force_rebuild;  // rebuild at the next decide (FixMesh next_reneighbor)
 };
 
 struct Plane {
@@ -76,6 +78,32 @@ struct Plane {
   double pos;
   int wall_type;
   int rolling;
+};
+
+// Triangle-mesh wall (fix mesh/surface + fix wall/gran mesh).
+constexpr int kMaxMeshes = 4;
+constexpr int kMeshMaxCand = 24;   // candidate triangles (= history slots) per atom
+constexpr int kTriStride = 40;     // doubles of geometry per triangle, see below
+constexpr int kStatMeshSlots = 5;  // Ctrl::status: an atom exceeded kMeshMaxCand
+constexpr int kStatMeshReg = 6;    // Ctrl::status: triangle-cell registrations overflowed
+// geometry layout per triangle: node[9] | edgeVec[9] | edgeNorm[9] |
+// edgeLen[3] | surfaceNorm[3] | center[3] | rBound | pad[3]
+// meta per triangle: bits 0-1 obtuse node+1 (0 none), bits 2-4 edge active,
+// bits 5-7 corner active
+struct MeshDev {
+  int ntri, wall_type, rolling, moving;
+  double distmax, tskin;  // FixNeighlistMesh: bounding-box growth and neighbuild threshold
+  double *tri;        // [t*kTriStride]
+  int *meta;          // [t]
+  double *nodev;      // node velocities [t*9] (moving mesh) or nullptr
+  double vel[3];      // move/mesh linear velocity
+  int *cn_start, *cn_list;          // coplanar node-neighbours (areCoplanarNodeNeighs)
+  int *tc_count, *tc_start, *tc_fill, *tc_list;  // triangles registered per atom cell
+  int tc_cap;
+  int *cand_n, *cand;               // per atom: count, [c*nmax + a] ascending
+  int *nslot[2], *npart[2];         // per atom (buffer 0 live, 1 permute scratch)
+  int *slot_tri[2];                 // [s*nmax + a], -1 empty
+  double *slot_hist[2];             // [(s*3+d)*nmax + a]
 };
 
 struct Sys {
@@ -107,6 +135,8 @@ struct Sys {
   double charVel;
   int nplanes;
   Plane planes[kMaxPlanes];
+  int nmeshes;
+  MeshDev meshes[kMaxMeshes];
 };
 
 }  // namespace gb300

@@ -15,6 +15,7 @@
 #include "contact_law.cuh"
 #include "dem_device.cuh"
 #include "dem_kernels.h"
+#include "mesh_device.cuh"
 
 namespace gb300 {
 
@@ -252,6 +253,17 @@ __global__ void k_permute(Sys s) {
       if (absdist <= dMax) bits |= (uint8_t)(1u << w);
     }
     B.wbits[i] = bits;
+    for (int k = 0; k < s.nmeshes; k++) {  // FixContactHistoryMesh per-atom slots travel too
+      const MeshDev &M = s.meshes[k];
+      const int ns = M.nslot[0][o];
+      M.nslot[1][i] = ns;
+      M.npart[1][i] = M.npart[0][o];
+      for (int q = 0; q < ns; q++) {
+        M.slot_tri[1][(size_t)q * s.nmax + i] = M.slot_tri[0][(size_t)q * s.nmax + o];
+        for (int d = 0; d < 3; d++)
+          M.slot_hist[1][(size_t)(3 * q + d) * s.nmax + i] = M.slot_hist[0][(size_t)(3 * q + d) * s.nmax + o];
+      }
+    }
   }
 }
 
@@ -274,6 +286,158 @@ __global__ void k_copy_atoms(Sys s) {
       for (int d = 0; d < 3; d++)
         A.whist[(size_t)(w * 3 + d) * s.nmax + i] = B.whist[(size_t)(w * 3 + d) * s.nmax + i];
     A.wbits[i] = B.wbits[i];
+    for (int k = 0; k < s.nmeshes; k++) {
+      const MeshDev &M = s.meshes[k];
+      const int ns = M.nslot[1][i];
+      M.nslot[0][i] = ns;
+      M.npart[0][i] = M.npart[1][i];
+      for (int q = 0; q < ns; q++) {
+        M.slot_tri[0][(size_t)q * s.nmax + i] = M.slot_tri[1][(size_t)q * s.nmax + i];
+        for (int d = 0; d < 3; d++)
+          M.slot_hist[0][(size_t)(3 * q + d) * s.nmax + i] = M.slot_hist[1][(size_t)(3 * q + d) * s.nmax + i];
+      }
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
+// rebuild: triangle-mesh candidate lists (FixNeighlistMesh::pre_force) and
+// history slot maintenance (FixContactHistoryMesh::pre_exchange/pre_force)
+// ----------------------------------------------------------------------------
+
+__device__ __forceinline__ void mslot_swap(const MeshDev &M, size_t nmax, int i, int a, int b) {
+  const int t = M.slot_tri[0][a * nmax + i];
+  M.slot_tri[0][a * nmax + i] = M.slot_tri[0][b * nmax + i];
+  M.slot_tri[0][b * nmax + i] = t;
+  for (int d = 0; d < 3; d++) {
+    const double h = M.slot_hist[0][(3 * a + d) * nmax + i];
+    M.slot_hist[0][(3 * a + d) * nmax + i] = M.slot_hist[0][(3 * b + d) * nmax + i];
+    M.slot_hist[0][(3 * b + d) * nmax + i] = h;
+  }
+}
+
+// sort_contacts: move filled slots forward (swap first empty <-> last filled)
+__global__ void k_mesh_sort(Sys s, int k) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const MeshDev &M = s.meshes[k];
+  const int n = c->n_new;
+  const size_t nmax = s.nmax;
+  GRID_STRIDE(i, n) {
+    const int nn = M.nslot[0][i];
+    int fe, lf;
+    do {
+      fe = lf = -1;
+      for (int j = 0; j < nn; j++) {
+        const int p = M.slot_tri[0][j * nmax + i];
+        if (fe == -1 && p == -1) fe = j;
+        if (p >= 0) lf = j;
+      }
+      if (fe > -1 && lf > -1 && fe < lf) mslot_swap(M, nmax, i, fe, lf);
+    } while (fe > -1 && lf > -1 && fe < lf);
+  }
+}
+
+__device__ __forceinline__ void tri_cell_range(const Sys &s, const MeshDev &M, int t, int lo[3], int hi[3]) {
+  const double *g = M.tri + (size_t)t * kTriStride;
+  for (int d = 0; d < 3; d++) {
+    double a = g[d], b = g[d];
+    for (int q = 1; q < 3; q++) {
+      a = fmin(a, g[3 * q + d]);
+      b = fmax(b, g[3 * q + d]);
+    }
+    lo[d] = cell_coord(s, a - M.distmax, d);
+    hi[d] = cell_coord(s, b + M.distmax, d);
+  }
+}
+
+__global__ void k_tri_count(Sys s, int k) {
+  if (gated(s.ctrl)) return;
+  const MeshDev &M = s.meshes[k];
+  GRID_STRIDE(t, M.ntri) {
+    int lo[3], hi[3];
+    tri_cell_range(s, M, t, lo, hi);
+    for (int z = lo[2]; z <= hi[2]; z++)
+      for (int y = lo[1]; y <= hi[1]; y++)
+        for (int x = lo[0]; x <= hi[0]; x++) atomicAdd(&M.tc_count[x + s.nc[0] * (y + s.nc[1] * z)], 1);
+  }
+}
+
+__global__ void k_tri_fill(Sys s, int k) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const MeshDev &M = s.meshes[k];
+  if (M.tc_start[s.ncell] > M.tc_cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      c->status = kStatMeshReg;
+      c->halt = 1;
+    }
+    return;
+  }
+  GRID_STRIDE(t, M.ntri) {
+    int lo[3], hi[3];
+    tri_cell_range(s, M, t, lo, hi);
+    for (int z = lo[2]; z <= hi[2]; z++)
+      for (int y = lo[1]; y <= hi[1]; y++)
+        for (int x = lo[0]; x <= hi[0]; x++) {
+          const int cell = x + s.nc[0] * (y + s.nc[1] * z);
+          M.tc_list[M.tc_start[cell] + atomicAdd(&M.tc_fill[cell], 1)] = t;
+        }
+  }
+}
+
+// per atom: candidate triangles of its cell that pass resolveTriSphereNeighbuild,
+// ascending; then cleanUpContactJumps and the re-paging of the slots
+__global__ void k_mesh_cand(Sys s, int k) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const MeshDev &M = s.meshes[k];
+  const AtomArrays &A = s.atoms[0];
+  const int n = c->n_new;
+  const size_t nmax = s.nmax;
+  bool over = false;
+  GRID_STRIDE(i, n) {
+    const double xv[3] = {A.x[i], A.y[i], A.z[i]};
+    const int cell = cell_coord(s, xv[0], 0) + s.nc[0] * (cell_coord(s, xv[1], 1) + s.nc[1] * cell_coord(s, xv[2], 2));
+    const double rS = __dmul_rn(A.r[i], s.cdf);
+    int cand[kMeshMaxCand];
+    int nc = 0;
+    for (int q = M.tc_start[cell]; q < M.tc_start[cell + 1]; q++) {
+      const int t = M.tc_list[q];
+      if (!tri_sphere_neighbuild(M.tri + (size_t)t * kTriStride, rS, xv, M.tskin)) continue;
+      if (nc == kMeshMaxCand) { over = true; break; }
+      int m = nc++;
+      while (m > 0 && cand[m - 1] > t) { cand[m] = cand[m - 1]; m--; }
+      cand[m] = t;
+    }
+    M.cand_n[i] = nc;
+    for (int q = 0; q < nc; q++) M.cand[(size_t)q * nmax + i] = cand[q];
+    // cleanUpContactJumps: drop partners whose triangle no longer lists the atom
+    int np = M.npart[0][i];
+    int ip = 0;
+    while (ip < np) {
+      const int t = M.slot_tri[0][ip * nmax + i];
+      bool listed = false;
+      for (int q = 0; q < nc; q++) listed |= (cand[q] == t);
+      if (!listed) {
+        M.slot_tri[0][ip * nmax + i] = -1;
+        for (int d = 0; d < 3; d++) M.slot_hist[0][(3 * ip + d) * nmax + i] = 0.0;
+        mslot_swap(M, nmax, i, ip, np - 1);
+        np--;
+      } else {
+        ip++;
+      }
+    }
+    for (int q = np; q < nc; q++) {
+      M.slot_tri[0][q * nmax + i] = -1;
+      for (int d = 0; d < 3; d++) M.slot_hist[0][(3 * q + d) * nmax + i] = 0.0;
+    }
+    M.npart[0][i] = np;
+    M.nslot[0][i] = nc;
+  }
+  if (over) {
+    c->status = kStatMeshSlots;
+    c->halt = 1;
   }
 }
 
@@ -602,6 +766,54 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
 // per-atom kernel: force gather + gravity + primitive walls + nve/sphere
 // ----------------------------------------------------------------------------
 
+// Walls::Granular::compute_force (src/fix_wall_gran_base.h:159-372) for one
+// wall contact: overlap -deltan, delta = closest wall point - centre, wall
+// velocity vwall; h points at the history (stride hs between components)
+template <int NORMAL>
+__device__ __forceinline__ void wall_force(const Sys &s, const AtomArrays &A, int i, double deltan,
+                                           const double delta[3], const double vwall[3],
+                                           int wall_type, bool rolling, double *h, size_t hs,
+                                           int shearupdate, const double v[3], const double om[3],
+                                           double &fx, double &fy, double &fz, double &tx,
+                                           double &ty, double &tz) {
+  const double radi = A.r[i];
+  if (deltan <= 0) {
+    ContactIn ci;
+    ci.radi = radi;
+    ci.radj = 0.0;
+    ci.deltan_wall = -deltan;
+    ci.d[0] = -delta[0];
+    ci.d[1] = -delta[1];
+    ci.d[2] = -delta[2];
+    ci.r = radi - ci.deltan_wall;
+    ci.rinv = 1.0 / ci.r;
+    ci.en[0] = ci.d[0] * ci.rinv;
+    ci.en[1] = ci.d[1] * ci.rinv;
+    ci.en[2] = ci.d[2] * ci.rinv;
+    ci.radsum = radi;
+    ci.reff = radi;
+    ci.vr[0] = v[0] - vwall[0];
+    ci.vr[1] = v[1] - vwall[1];
+    ci.vr[2] = v[2] - vwall[2];
+    ci.wi[0] = om[0]; ci.wi[1] = om[1]; ci.wi[2] = om[2];
+    ci.wj[0] = ci.wj[1] = ci.wj[2] = 0.0;
+    const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], wall_type);
+    contact_consts<NORMAL>(tp, A.m[i], radi, s.charVel, s.tdamp, ci.c0, ci.c1);
+    double sh3[3] = {h[0], h[hs], h[2 * hs]};
+    ContactOut o;
+    contact_law<NORMAL, true>(ci, tp, s.dt, s.tdamp, s.limitf, rolling, shearupdate != 0, sh3, o);
+    if (shearupdate) {
+      h[0] = sh3[0];
+      h[hs] = sh3[1];
+      h[2 * hs] = sh3[2];
+    }
+    fx += o.F[0]; fy += o.F[1]; fz += o.F[2];
+    tx += o.Ti[0]; ty += o.Ti[1]; tz += o.Ti[2];
+  } else {
+    h[0] = 0.0; h[hs] = 0.0; h[2 * hs] = 0.0;  // surfacesClose
+  }
+}
+
 template <int NORMAL>
 __device__ __forceinline__ void plane_contact(const Sys &s, const AtomArrays &A, int i, int w,
                                               int shearupdate, double v[3], double om[3],
@@ -627,45 +839,90 @@ __device__ __forceinline__ void plane_contact(const Sys &s, const AtomArrays &A,
   const size_t hs = s.nmax;
   const double cdm1 = s.cdf - 1.0;
   if (deltan <= 0 || deltan < cdm1 * radi) {
-    if (deltan <= 0) {
-      ContactIn ci;
-      ci.radi = radi;
-      ci.radj = 0.0;
-      ci.deltan_wall = -deltan;
-      ci.d[0] = -delta[0];
-      ci.d[1] = -delta[1];
-      ci.d[2] = -delta[2];
-      ci.r = radi - ci.deltan_wall;
-      ci.rinv = 1.0 / ci.r;
-      ci.en[0] = ci.d[0] * ci.rinv;
-      ci.en[1] = ci.d[1] * ci.rinv;
-      ci.en[2] = ci.d[2] * ci.rinv;
-      ci.radsum = radi;
-      ci.reff = radi;
-      ci.vr[0] = v[0] - 0.0;
-      ci.vr[1] = v[1] - 0.0;
-      ci.vr[2] = v[2] - 0.0;
-      ci.wi[0] = om[0]; ci.wi[1] = om[1]; ci.wi[2] = om[2];
-      ci.wj[0] = ci.wj[1] = ci.wj[2] = 0.0;
-      const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], pl.wall_type);
-      contact_consts<NORMAL>(tp, A.m[i], radi, s.charVel, s.tdamp, ci.c0, ci.c1);
-      double sh3[3] = {h[0], h[hs], h[2 * hs]};
-      ContactOut o;
-      contact_law<NORMAL, true>(ci, tp, s.dt, s.tdamp, s.limitf, pl.rolling != 0,
-                                shearupdate != 0, sh3, o);
-      if (shearupdate) {
-        h[0] = sh3[0];
-        h[hs] = sh3[1];
-        h[2 * hs] = sh3[2];
-      }
-      fx += o.F[0]; fy += o.F[1]; fz += o.F[2];
-      tx += o.Ti[0]; ty += o.Ti[1]; tz += o.Ti[2];
-    } else {
-      h[0] = 0.0; h[hs] = 0.0; h[2 * hs] = 0.0;  // surfacesClose
-    }
+    const double vwall[3] = {0., 0., 0.};
+    wall_force<NORMAL>(s, A, i, deltan, delta, vwall, pl.wall_type, pl.rolling != 0, h, hs,
+                       shearupdate, v, om, fx, fy, fz, tx, ty, tz);
   } else {
     h[0] = 0.0; h[hs] = 0.0; h[2 * hs] = 0.0;
   }
+}
+
+// SurfaceMesh::areCoplanarNodeNeighs from the precomputed lists
+__device__ __forceinline__ bool mesh_coplanar(const MeshDev &M, int a, int b) {
+  for (int q = M.cn_start[a]; q < M.cn_start[a + 1]; q++)
+    if (M.cn_list[q] == b) return true;
+  return false;
+}
+
+// FixWallGran::post_force_mesh for one atom: its candidate triangles in
+// ascending order with FixContactHistoryMesh's slot semantics (mark, handle,
+// coplanar de-duplication and history copy, clean-up)
+template <int NORMAL>
+__device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, int shearupdate,
+                              double v[3], double om[3], double xv[3], double &fx, double &fy,
+                              double &fz, double &tx, double &ty, double &tz, bool &bad) {
+  const MeshDev &M = s.meshes[k];
+  const int nc = M.cand_n[i];
+  if (nc == 0) return;
+  const size_t nmax = s.nmax;
+  int *st = M.slot_tri[0];
+  double *sh = M.slot_hist[0];
+  unsigned keep = 0;
+  int np = M.npart[0][i];
+  const double radi = A.r[i];
+  const double cdm1 = s.cdf - 1.0;
+  for (int q = 0; q < nc; q++) {
+    const int t = M.cand[(size_t)q * nmax + i];
+    const double *g = M.tri + (size_t)t * kTriStride;
+    double delta[3], bary[3];
+    int bs;
+    const double deltan = resolve_tri_sphere(g, M.meta[t], radi, xv, delta, bary, bs);
+    if (deltan > s.cutneighmax) continue;
+    if (!(deltan <= 0 || deltan < cdm1 * radi)) continue;
+    int slot = -1;
+    for (int u = 0; u < nc; u++)
+      if (st[u * nmax + i] == t) { slot = u; break; }
+    if (slot >= 0) {
+      keep |= 1u << slot;
+    } else {
+      const bool face = bs == 7;
+      if (face) {  // coplanarContactAlready
+        bool already = false;
+        for (int u = 0; u < nc; u++) {
+          const int p = st[u * nmax + i];
+          if (p >= 0 && p != t && ((keep >> u) & 1u) && mesh_coplanar(M, p, t)) already = true;
+        }
+        if (already) continue;
+      }
+      if (np >= nc) { bad = true; continue; }
+      for (int u = 0; u < nc; u++)
+        if (st[u * nmax + i] == -1) { slot = u; break; }
+      st[slot * nmax + i] = t;
+      keep |= 1u << slot;
+      for (int d = 0; d < 3; d++) sh[(3 * slot + d) * nmax + i] = 0.0;
+      np++;
+      if (face)  // checkCoplanarContactHistory
+        for (int u = 0; u < nc; u++) {
+          const int p = st[u * nmax + i];
+          if (p >= 0 && p != t && mesh_coplanar(M, p, t))
+            for (int d = 0; d < 3; d++) sh[(3 * slot + d) * nmax + i] = sh[(3 * u + d) * nmax + i];
+        }
+    }
+    double vwall[3] = {0., 0., 0.};
+    if (M.nodev) {
+      const double *vn = M.nodev + 9 * (size_t)t;
+      for (int d = 0; d < 3; d++) vwall[d] = (bary[0] * vn[d] + bary[1] * vn[3 + d] + bary[2] * vn[6 + d]);
+    }
+    wall_force<NORMAL>(s, A, i, deltan, delta, vwall, M.wall_type, M.rolling != 0,
+                       sh + (size_t)(3 * slot) * nmax + i, nmax, shearupdate, v, om, fx, fy, fz, tx, ty, tz);
+  }
+  for (int u = 0; u < nc; u++)  // cleanUpContacts
+    if (!((keep >> u) & 1u)) {
+      if (st[u * nmax + i] > -1) np--;
+      st[u * nmax + i] = -1;
+      for (int d = 0; d < 3; d++) sh[(3 * u + d) * nmax + i] = 0.0;
+    }
+  M.npart[0][i] = np;
 }
 
 template <int NORMAL, bool GATHER, bool FINAL, bool INITIAL>
@@ -678,7 +935,7 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
   const size_t P = s.pcap;
   const double dtv = s.dt;
   const double trigger = 0.25 * s.skin * s.skin;
-  bool moved = false, bad = false;
+  bool moved = false, bad = false, meshbad = false;
   GRID_STRIDE(i, n) {
     double fx, fy, fz, tx, ty, tz;
     double v[3] = {A.vx[i], A.vy[i], A.vz[i]};
@@ -711,6 +968,8 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
           if (bits & (1u << w))
             plane_contact<NORMAL>(s, A, i, w, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz);
       }
+      for (int k = 0; k < s.nmeshes; k++)
+        mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad);
       A.fx[i] = fx; A.fy[i] = fy; A.fz[i] = fz;
       A.tx[i] = tx; A.ty[i] = ty; A.tz[i] = tz;
     } else {
@@ -753,6 +1012,9 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
   if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(&c->moved, 1);
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) {
     atomicExch(&c->status, kStatNan);
+  }
+  if (__any_sync(0xffffffffu, meshbad) && (threadIdx.x & 31) == 0) {
+    atomicExch(&c->status, kStatMeshSlots);
   }
 }
 
@@ -808,6 +1070,17 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
   k_rev_fill<<<gP, B, 0, st>>>(s);
   k_rev_sort<<<gN, B, 0, st>>>(s);
   k_copy_pairs<<<grid_for((long)s.pcap > s.nmax + 1 ? s.pcap : s.nmax + 1, B, lc.max_grid), B, 0, st>>>(s);
+  for (int k = 0; k < s.nmeshes; k++) {
+    const MeshDev &M = s.meshes[k];
+    const int gT = grid_for(M.ntri, B, lc.max_grid);
+    k_mesh_sort<<<gN, B, 0, st>>>(s, k);
+    k_zero_gated<<<gC, B, 0, st>>>(s, M.tc_count, s.ncell + 2);
+    k_zero_gated<<<gC, B, 0, st>>>(s, M.tc_fill, s.ncell + 2);
+    k_tri_count<<<gT, B, 0, st>>>(s, k);
+    nl += 6 + scan_exclusive(s, M.tc_count, M.tc_start, s.ncell + 2, s.scan_tmp, true, st);
+    k_tri_fill<<<gT, B, 0, st>>>(s, k);
+    k_mesh_cand<<<gN, B, 0, st>>>(s, k);
+  }
   k_finish_rebuild<<<1, 1, 0, st>>>(s);
   return nl + 4;
 }

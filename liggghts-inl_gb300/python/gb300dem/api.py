@@ -16,7 +16,18 @@ HEADER = os.path.join(os.path.dirname(_build.PKG), "include", "liggghts_gb300.h"
 
 STATUS = {0: "DEM_OK", 1: "DEM_ERR_BAD_ARG", 2: "DEM_ERR_CUDA", 3: "DEM_ERR_NEIGH_OVERFLOW",
           4: "DEM_ERR_NAN", 5: "DEM_ERR_TIMEOUT", 6: "DEM_ERR_BOX", 7: "DEM_ERR_UNSUPPORTED",
-          8: "DEM_ERR_NO_DEVICE"}
+          8: "DEM_ERR_NO_DEVICE", 9: "DEM_ERR_CAPACITY"}
+
+
+def mesh_topology(nodes):
+    """Edge/corner activity flags of a triangle mesh (host-only C++ of the library)."""
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    ea = np.zeros((len(nodes), 3), np.uint8)
+    ca = np.zeros((len(nodes), 3), np.uint8)
+    rc = load().dem_mesh_topology(len(nodes), _p(nodes), _p(ea), _p(ca))
+    if rc != 0:
+        raise DemError("dem_mesh_topology: %s" % STATUS.get(rc, rc))
+    return ea, ca
 
 
 class DemConfig(ctypes.Structure):
@@ -62,6 +73,10 @@ def load(build=True):
     L.dem_derive_hertz_tables.argtypes = [I] + [P] * 7
     L.dem_add_plane.argtypes = [P, I, ctypes.c_double, I, I, P]
     L.dem_upload_atoms.argtypes = [P, I] + [P] * 7
+    L.dem_add_mesh.argtypes = [P, I, P, I, I, P, P, P]
+    L.dem_mesh_topology.argtypes = [I, P, P, P]
+    L.dem_mesh_ncontacts.argtypes = [P, I, P]
+    L.dem_download_mesh_contacts.argtypes = [P, I, P, P, P, P]
     L.dem_upload_contact_history.argtypes = [P, I, P, P, P]
     L.dem_upload_wall_history.argtypes = [P, I, P]
     L.dem_setup.argtypes = [P]
@@ -132,6 +147,15 @@ class DemSystem:
                                           float(case.get("charVel", 0.0))))
         for (axis, pos, wtype, roll) in case.get("planes", []):
             self._check(L.dem_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll), None))
+        self._meshkeep = []
+        for m in case.get("meshes", []):
+            nodes = np.ascontiguousarray(m["nodes"], dtype=np.float64)
+            ea, ca = m.get("edge_active"), m.get("corner_active")
+            ea = np.ascontiguousarray(ea, dtype=np.uint8) if ea is not None else None
+            ca = np.ascontiguousarray(ca, dtype=np.uint8) if ca is not None else None
+            self._meshkeep += [nodes, ea, ca]
+            self._check(L.dem_add_mesh(self.h, len(nodes), _p(nodes), int(m["wall_type"]),
+                                       int(m.get("rolling", 0)), _p(ea), _p(ca), None))
         if "atoms" in case:
             self.upload(case["atoms"])
 
@@ -190,6 +214,17 @@ class DemSystem:
                    hist=np.zeros((n, d)))
         self._check(L.dem_download_contacts(self.h, *[_p(out[k]) for k in
                                                       ("tag_i", "tag_j", "shift", "flag", "hist")]))
+        return out
+
+    def mesh_contacts(self, k):
+        L = load()
+        n = ctypes.c_int()
+        self._check(L.dem_mesh_ncontacts(self.h, int(k), ctypes.byref(n)))
+        n = n.value
+        out = dict(tag=np.zeros(n, np.int32), tri=np.zeros(n, np.int32), slot=np.zeros(n, np.int32),
+                   hist=np.zeros((n, 3)))
+        self._check(L.dem_download_mesh_contacts(self.h, int(k), *[_p(out[q]) for q in
+                                                                  ("tag", "tri", "slot", "hist")]))
         return out
 
     def wall_history(self, w):

@@ -108,20 +108,15 @@ def hopper_case(seed, r_out, r_top, half_angle_deg, n_az, n_ax, spacing, radius=
     if clearance is None:
         clearance = 0.25 * spacing  # negative: the outer ring overlaps the wall
     zf = z_top if fill_height is None else fill_height
-    pts = []
     nxy = int(2 * r_top / spacing) + 2
     nz = int((zf - rmax) / spacing) + 1
-    for k in range(nz):
-        z = rmax * 1.5 + k * spacing
-        for i in range(nxy):
-            for j in range(nxy):
-                x = -r_top + (i + 0.5) * spacing
-                y = -r_top + (j + 0.5) * spacing
-                # inside the cone with one radius of clearance measured normal to the wall
-                R = r_out + z * ta
-                if (math.hypot(x, y) + rmax / math.cos(math.radians(half_angle_deg))) < R - clearance:
-                    pts.append((x, y, z))
-    x = np.array(pts, dtype=np.float64)
+    gx = -r_top + (np.arange(nxy) + 0.5) * spacing
+    gz = rmax * 1.5 + np.arange(nz) * spacing
+    zz, xx, yy = np.meshgrid(gz, gx, gx, indexing="ij")  # z-major, then x, then y
+    R = r_out + zz * ta
+    # inside the cone with one radius of clearance measured normal to the wall
+    inside = (np.hypot(xx, yy) + rmax / math.cos(math.radians(half_angle_deg))) < R - clearance
+    x = np.stack([xx[inside], yy[inside], zz[inside]], axis=1).astype(np.float64)
     if max_atoms is not None and len(x) > max_atoms:
         x = x[np.argsort(x[:, 2], kind="stable")[:max_atoms]]
     n = len(x)

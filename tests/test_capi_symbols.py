@@ -42,6 +42,18 @@ def test_no_device_is_an_error_not_a_fallback():
     assert rc == 8  # DEM_ERR_NO_DEVICE
 
 
+def test_library_mesh_topology_matches_reference_flags():
+    """Edge/corner activity derived by the library's host code (used when a
+    caller uploads a bare mesh) equals the reference's own flags."""
+    import numpy as np
+    from golden_io import load_golden
+    for name in ("hopper_mesh", "hopper_mesh_cdt"):
+        case, snaps = load_golden(name)
+        ea, ca = api.mesh_topology(case["meshes"][0]["nodes"])
+        assert np.array_equal(ea, snaps[0]["mesh0_edge_active"]), name
+        assert np.array_equal(ca, snaps[0]["mesh0_corner_active"]), name
+
+
 def test_host_table_derivation_matches_reference_formulas():
     L = api.load()
     E = [5e6, 1e7]

@@ -97,6 +97,39 @@ def test_gpu_per_step_from_reference_state(name):
         g.close()
 
 
+@pytest.mark.parametrize("name", ["hopper_mesh", "hopper_mesh_cdt"])
+def test_gpu_mesh_walls_match_reference(name):
+    """Conical triangle-mesh hopper: forces, and the mesh contact set, slot
+    layout and histories of FixContactHistoryMesh at every snapshot."""
+    case, snaps = load_golden(name)
+    g = _gpu(case)
+    g.setup()
+    prev = 0
+    for st in sorted(snaps):
+        if st > prev:
+            g.step(st - prev)
+            prev = st
+        a = sort_by_tag(g.atoms())
+        r = snaps[st]
+        assert np.array_equal(a["tag"], r["tag"])
+        ftol = FORCE_RTOL if st <= 10 else DIVERGED_RTOL
+        assert max_rel(a["f"], r["f"]) < ftol, (name, st, max_rel(a["f"], r["f"]))
+        assert max_rel(a["torque"], r["torque"]) < ftol, (name, st)
+        if st <= 100:
+            assert max_rel(a["x"], r["x"], scale=_box(case)) < TRAJ_RTOL, (name, st)
+        mc = g.mesh_contacts(0)
+        gm = {(int(t), int(tr)): (int(sl), h) for t, tr, sl, h in
+              zip(mc["tag"], mc["tri"], mc["slot"], mc["hist"])}
+        rm = {(int(t), int(tr)): (int(sl), h) for t, tr, sl, h in
+              zip(r["mesh0_contact_tag"], r["mesh0_contact_tri"], r["mesh0_contact_slot"],
+                  r["mesh0_contact_hist"])}
+        assert set(gm) == set(rm), (name, st, set(rm) ^ set(gm))
+        assert all(gm[k][0] == rm[k][0] for k in rm), "slot layout differs"
+        hs = max([np.abs(v[1]).max() for v in rm.values()] + [1e-300])
+        hm = max([np.abs(gm[k][1] - rm[k][1]).max() for k in rm] + [0.0]) / hs
+        assert hm < (HIST_RTOL if st <= 100 else 1e-6), (name, st, hm)
+
+
 def _bigger_case(seed=3, rolling=0):
     from gb300dem import workloads
     return workloads.lattice_case(seed=seed, nx=24, ny=24, nz=12, spacing=1.97e-3,
