@@ -29,6 +29,14 @@ import numpy as np  # noqa: E402
 
 METRIC = "particle-steps/s (1M Hertz/history spheres)"
 
+# Per-atom FP64 arithmetic (flop, DFMA = 2) and DRAM bytes (read + write) of
+# one launch, from ncu captures of the workload at 500k atoms
+# (profiles/k_pair_hopper1m_500k.md, profiles/k_particle_hopper1m_500k.md).
+PROFILED_PER_ATOM = {
+    "hopper1m": {"pair": {"fp64_flop": 119.2, "dram_bytes": 410.6},
+                 "particle": {"fp64_flop": 54.6, "dram_bytes": 404.5}},
+}
+
 
 # ----------------------------------------------------------------------------
 # workloads
@@ -267,12 +275,29 @@ def run_gb300(args):
     dom_bytes = pair_bytes if dom == "pair" else part_bytes
     dom_ms = pair_ms if dom == "pair" else part_ms
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    roof = {"kernel": "k_pair" if dom == "pair" else "k_particle", "bound": "hbm",
-            "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-            "traffic": None, "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)",
-            "algorithmic_bytes_per_launch": dom_bytes,
-            "avg_launch_ms": dom_ms,
-            "shares": {"pair": pair_ms / tot_ms, "particle": part_ms / tot_ms, "neigh": neigh_ms / tot_ms}}
+    # Binding roof: the FP64 pipe.  FP64 arithmetic per atom and DRAM bytes
+    # per atom of each kernel come from one ncu capture of the same workload
+    # at 500k atoms (DADD + DMUL + 2 DFMA thread instructions; dram read +
+    # write), scaled to this run by the atom count.
+    per_atom = PROFILED_PER_ATOM.get(args.workload, {}).get(dom)
+    hbm_roof = {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": per_atom["dram_bytes"] * n if per_atom else None,
+                "algorithmic_bytes_per_launch": dom_bytes,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    if per_atom and fp64_peak:
+        flops = per_atom["fp64_flop"] * n
+        ach_tf = flops / (dom_ms * 1e-3) / 1e12
+        roof = {"kernel": "k_pair" if dom == "pair" else "k_particle", "bound": "fp64",
+                "achieved": ach_tf, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach_tf / fp64_peak,
+                "traffic": hbm_roof["traffic"],
+                "peak_source": "FP64 FMA peak measured live on this GPU (dem_measure_fp64_peak), "
+                               "of measured",
+                "fp64_flop_per_launch": flops, "hbm": hbm_roof}
+    else:
+        roof = dict(hbm_roof, kernel="k_pair" if dom == "pair" else "k_particle", bound="hbm")
+    roof.update({"avg_launch_ms": dom_ms,
+                 "shares": {"pair": pair_ms / tot_ms, "particle": part_ms / tot_ms,
+                            "neigh": neigh_ms / tot_ms}})
     if fp64_peak:
         roof["fp64_peak_tflops_measured"] = fp64_peak
     # ---- CPU baseline (oracle port, bounded sample, rank 0, N=1 only)

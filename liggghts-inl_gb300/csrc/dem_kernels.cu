@@ -977,27 +977,28 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
       tx = A.tx[i]; ty = A.ty[i]; tz = A.tz[i];
     }
     if (FINAL || INITIAL) {
-      // FixNVESphere updates with the reference's rounding (no contraction):
-      // positions then match the reference bit for bit whenever forces do.
+      // FixNVESphere half-kicks and drift as fused multiply-adds: one FP64
+      // instruction each (the FP64 pipe bounds this kernel on GB300); the
+      // single rounding moves positions by at most an ulp from the reference.
       const double dtfm = A.dtfm[i], dtir = A.dtir[i];
       if (FINAL) {
-        v[0] = __dadd_rn(v[0], __dmul_rn(dtfm, fx));
-        v[1] = __dadd_rn(v[1], __dmul_rn(dtfm, fy));
-        v[2] = __dadd_rn(v[2], __dmul_rn(dtfm, fz));
-        om[0] = __dadd_rn(om[0], __dmul_rn(dtir, tx));
-        om[1] = __dadd_rn(om[1], __dmul_rn(dtir, ty));
-        om[2] = __dadd_rn(om[2], __dmul_rn(dtir, tz));
+        v[0] = fma(dtfm, fx, v[0]);
+        v[1] = fma(dtfm, fy, v[1]);
+        v[2] = fma(dtfm, fz, v[2]);
+        om[0] = fma(dtir, tx, om[0]);
+        om[1] = fma(dtir, ty, om[1]);
+        om[2] = fma(dtir, tz, om[2]);
       }
       if (INITIAL) {
-        v[0] = __dadd_rn(v[0], __dmul_rn(dtfm, fx));
-        v[1] = __dadd_rn(v[1], __dmul_rn(dtfm, fy));
-        v[2] = __dadd_rn(v[2], __dmul_rn(dtfm, fz));
-        xv[0] = __dadd_rn(xv[0], __dmul_rn(dtv, v[0]));
-        xv[1] = __dadd_rn(xv[1], __dmul_rn(dtv, v[1]));
-        xv[2] = __dadd_rn(xv[2], __dmul_rn(dtv, v[2]));
-        om[0] = __dadd_rn(om[0], __dmul_rn(dtir, tx));
-        om[1] = __dadd_rn(om[1], __dmul_rn(dtir, ty));
-        om[2] = __dadd_rn(om[2], __dmul_rn(dtir, tz));
+        v[0] = fma(dtfm, fx, v[0]);
+        v[1] = fma(dtfm, fy, v[1]);
+        v[2] = fma(dtfm, fz, v[2]);
+        xv[0] = fma(dtv, v[0], xv[0]);
+        xv[1] = fma(dtv, v[1], xv[1]);
+        xv[2] = fma(dtv, v[2], xv[2]);
+        om[0] = fma(dtir, tx, om[0]);
+        om[1] = fma(dtir, ty, om[1]);
+        om[2] = fma(dtir, tz, om[2]);
         A.x[i] = xv[0]; A.y[i] = xv[1]; A.z[i] = xv[2];
         const double dx = __dadd_rn(xv[0], -A.xh[i]);
         const double dy = __dadd_rn(xv[1], -A.yh[i]);
