@@ -13,6 +13,8 @@
  *                         matrices Yeff/Geff/betaeff/coeffFrict/coeffRollFrict/
  *                         coeffRestLog/charVel (src/global_properties.cpp:428-561,
  *                         src/normal_model_hertz.h:172-183, src/rolling_model_cdt.h:83-86)
+ *   dem_set_bond_params   CohesionModel<COHESION_BOND_NONLINEAR>::registerSettings +
+ *                         connectToProperties (src/cohesion_model_bond_nonlinear.h:231-381)
  *   dem_add_plane         FixWallGran "primitive type T {x,y,z}plane P"
  *                         (src/fix_wall_gran.cpp:176-215, src/primitive_wall_definitions.h:123-150)
  *   dem_upload_atoms      Atom arrays x v omega radius rmass type tag
@@ -97,6 +99,41 @@ int dem_set_pair_params(dem_handle *h, int ntypes, const double *Yeff, const dou
 int dem_derive_hertz_tables(int ntypes, const double *youngs, const double *poisson,
                             const double *restitution, double *Yeff, double *Geff,
                             double *betaeff, double *coeffRestLog);
+
+/* cohesion bond/nonlinear (pair_style gran ... cohesion bond/nonlinear;
+ * CohesionModel<COHESION_BOND_NONLINEAR>::connectToProperties,
+ * src/cohesion_model_bond_nonlinear.h:246-381).  tables stacks the 23
+ * per-type-pair property/global matrices, each (ntypes+1)^2 as in
+ * dem_set_pair_params, in this order: */
+enum {
+  DEM_BOND_RADIUS_MULTIPLIER = 0, /* radiusMultiplierBondnonlinear */
+  DEM_BOND_K_FN1, DEM_BOND_KU_FN1, DEM_BOND_KC_FN1, /* stiffnessPerUnitAreaK/Ku/Kc_fn1 (compression) */
+  DEM_BOND_K_FN2, DEM_BOND_KU_FN2, DEM_BOND_KC_FN2, /* stiffnessPerUnitAreaK/Ku/Kc_fn2 (tension) */
+  DEM_BOND_K_FT,                                    /* stiffnessPerUnitAreaK_ft */
+  DEM_BOND_K_TN, DEM_BOND_KU_TN, DEM_BOND_KC_TN,    /* stiffnessPerUnitAreaK/Ku/Kc_tn (twisting) */
+  DEM_BOND_K_TT, DEM_BOND_KU_TT, DEM_BOND_KC_TT,    /* stiffnessPerUnitAreaK/Ku/Kc_tt (bending) */
+  DEM_BOND_DAMP_FN, DEM_BOND_DAMP_FT, DEM_BOND_DAMP_TN, DEM_BOND_DAMP_TT, /* damping*Bondnonlinear */
+  DEM_BOND_MAX_DIST,                                /* maxDistanceBondnonlinear */
+  DEM_BOND_MAX_SIGMA, DEM_BOND_MAX_TAU,             /* maxSigma/maxTauBondnonlinear */
+  DEM_BOND_RATIO_TC,                                /* ratioTensionCompressionBondnonlinear */
+  DEM_BOND_CREATE_DIST,                             /* createDistanceBondnonlinear */
+  DEM_BOND_NTABLES
+};
+/* The model's on/off settings (registerSettings, :231-243; defaults: all
+ * *Stress and dampingBond on, the others off) and the scalar
+ * tsCreateBondnonlinear. */
+typedef struct dem_bond_settings {
+  double tsCreate;
+  int stressBreak, tensionStress, compressionStress, shearStress, normalTorqueStress,
+      shearTorqueStress, createBondAlways, dampingBond, dampingBondSmooth, ratioTCBond;
+} dem_bond_settings;
+/* After dem_set_pair_params and before dem_upload_atoms, with
+ * cfg.cohesion_model = DEM_COHESION_BOND_NONLINEAR.  Pairs then carry dnum = 31
+ * history values in the reference's order (28 bond values, then shear[3]);
+ * the contact distance factor grows as the model registers it.  Wall
+ * contacts use their own model without cohesion (fix wall/gran model hertz
+ * tangential history ...). */
+int dem_set_bond_params(dem_handle *h, const double *tables, const dem_bond_settings *st);
 
 /* axis 0/1/2 = xplane/yplane/zplane, rolling_model = DEM_ROLLING_* for this wall.
  * Returns the wall id through *wall_id (may be NULL). */

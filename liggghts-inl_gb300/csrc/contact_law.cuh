@@ -82,10 +82,14 @@ struct ContactOut {
 };
 
 // shear[3] is the tangential history, updated in place when update_history.
+// base: forces and torques of a bonded pair (cohesion bond/nonlinear), which
+// replace the normal model's force before the tangential and rolling models
+// add theirs (src/contact_models.h:228-238); nullptr otherwise.
 template <int NORMAL, bool WALL>
 __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &tp, double dt,
                                             bool tdamp, bool limitf, bool rolling,
-                                            bool update_history, double shear[3], ContactOut &o) {
+                                            bool update_history, double shear[3], ContactOut &o,
+                                            const ContactOut *base = nullptr) {
   const double enx = c.en[0], eny = c.en[1], enz = c.en[2];
   // ---- surface model (sphere kinematics)
   const double vr1 = c.vr[0], vr2 = c.vr[1], vr3 = c.vr[2];
@@ -169,15 +173,27 @@ __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &
   const double tor1 = eny * Ft3 - enz * Ft2;
   const double tor2 = enz * Ft1 - enx * Ft3;
   const double tor3 = enx * Ft2 - eny * Ft1;
-  o.F[0] = Fn * enx + Ft1;
-  o.F[1] = Fn * eny + Ft2;
-  o.F[2] = Fn * enz + Ft3;
-  o.Ti[0] = -cri * tor1;
-  o.Ti[1] = -cri * tor2;
-  o.Ti[2] = -cri * tor3;
-  o.Tj[0] = -crj * tor1;
-  o.Tj[1] = -crj * tor2;
-  o.Tj[2] = -crj * tor3;
+  if (base) {
+    o.F[0] = base->F[0] + Ft1;
+    o.F[1] = base->F[1] + Ft2;
+    o.F[2] = base->F[2] + Ft3;
+    o.Ti[0] = base->Ti[0] + -cri * tor1;
+    o.Ti[1] = base->Ti[1] + -cri * tor2;
+    o.Ti[2] = base->Ti[2] + -cri * tor3;
+    o.Tj[0] = base->Tj[0] + -crj * tor1;
+    o.Tj[1] = base->Tj[1] + -crj * tor2;
+    o.Tj[2] = base->Tj[2] + -crj * tor3;
+  } else {
+    o.F[0] = Fn * enx + Ft1;
+    o.F[1] = Fn * eny + Ft2;
+    o.F[2] = Fn * enz + Ft3;
+    o.Ti[0] = -cri * tor1;
+    o.Ti[1] = -cri * tor2;
+    o.Ti[2] = -cri * tor3;
+    o.Tj[0] = -crj * tor1;
+    o.Tj[1] = -crj * tor2;
+    o.Tj[2] = -crj * tor3;
+  }
 
   // ---- rolling friction, constant directional torque
   if (rolling) {

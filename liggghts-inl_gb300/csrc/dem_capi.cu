@@ -52,6 +52,8 @@ struct dem_handle {
   long long graph_gen = -1, sys_gen = 0;  // rebuilt when device pointers change
   int graph_kps = 0, graph_kpr = 0;
   std::vector<MeshHost> mesh_host;
+  std::vector<double> bond_tables;  // host copy for the cutoff derivation
+  dem_bond_settings bond_settings{};
 };
 
 static int ensure_graph(dem_handle *h) {
@@ -192,7 +194,7 @@ static int alloc_pairs(dem_handle *h, int pcap, int keep_np) {
     CUDA_TRY(h, dalloc(nl, &P.j, pcap));
     CUDA_TRY(h, dalloc(nl, &P.sh, pcap));
     CUDA_TRY(h, dalloc(nl, &P.flag, pcap));
-    CUDA_TRY(h, dalloc(nl, &P.hist, (size_t)3 * pcap));
+    CUDA_TRY(h, dalloc(nl, &P.hist, (size_t)s.dnum * pcap));
     CUDA_TRY(h, dalloc(nl, &P.reff, pcap));
     CUDA_TRY(h, dalloc(nl, &P.c0, pcap));
     CUDA_TRY(h, dalloc(nl, &P.c1, pcap));
@@ -212,7 +214,7 @@ static int alloc_pairs(dem_handle *h, int pcap, int keep_np) {
     CUDA_TRY(h, cudaMemcpy(N.j, O.j, k * sizeof(int), cudaMemcpyDeviceToDevice));
     CUDA_TRY(h, cudaMemcpy(N.sh, O.sh, k, cudaMemcpyDeviceToDevice));
     CUDA_TRY(h, cudaMemcpy(N.flag, O.flag, k * sizeof(int), cudaMemcpyDeviceToDevice));
-    for (int d = 0; d < 3; d++)
+    for (int d = 0; d < s.dnum; d++)
       CUDA_TRY(h, cudaMemcpy(N.hist + (size_t)d * pcap, O.hist + (size_t)d * s.pcap,
                              k * sizeof(double), cudaMemcpyDeviceToDevice));
     CUDA_TRY(h, cudaMemcpy(N.reff, O.reff, k * sizeof(double), cudaMemcpyDeviceToDevice));
@@ -273,7 +275,8 @@ int dem_create(const dem_config *cfg, dem_handle **out) {
   *out = nullptr;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DEM_ERR_NO_DEVICE;
-  if (cfg->cohesion_model != DEM_COHESION_OFF) return DEM_ERR_UNSUPPORTED;
+  if (cfg->cohesion_model != DEM_COHESION_OFF && cfg->cohesion_model != DEM_COHESION_BOND_NONLINEAR)
+    return DEM_ERR_UNSUPPORTED;
   if (cfg->normal_model != DEM_NORMAL_HERTZ && cfg->normal_model != DEM_NORMAL_HOOKE)
     return DEM_ERR_UNSUPPORTED;
   if (cfg->dt <= 0 || cfg->skin < 0 || cfg->neigh_every < 1 || cfg->contact_distance_factor < 1.0)
@@ -319,8 +322,17 @@ int dem_create(const dem_config *cfg, dem_handle **out) {
   s.tdamp = cfg->tangential_damping;
   s.limitf = cfg->limit_force;
   s.gravity_on = cfg->gravity_on;
+  s.bond = cfg->cohesion_model == DEM_COHESION_BOND_NONLINEAR ? 1 : 0;
+  s.dnum = s.bond ? kDnumBond : kDnumShear;
   *out = h;
   return DEM_OK;
+}
+
+// Device history index of the reference's history value r (bond values
+// first, then shear; device: shear first).
+static inline int dev_hist_index(const Sys &s, int r) {
+  if (!s.bond) return r;
+  return r < kBondValues ? kDnumShear + r : r - kBondValues;
 }
 
 int dem_destroy(dem_handle *h) {
@@ -384,6 +396,74 @@ int dem_set_pair_params(dem_handle *h, int ntypes, const double *Yeff, const dou
   h->s.charVel = charVel;
   h->have_params = true;
   h->sys_gen++;
+  return DEM_OK;
+}
+
+int dem_set_bond_params(dem_handle *h, const double *tables, const dem_bond_settings *st) {
+  if (!h || !tables || !st) return DEM_ERR_BAD_ARG;
+  if (!h->s.bond) return fail(h, DEM_ERR_BAD_ARG, "cohesion_model is not DEM_COHESION_BOND_NONLINEAR");
+  if (!h->have_params) return fail(h, DEM_ERR_BAD_ARG, "set pair parameters first");
+  if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "set bond parameters before uploading atoms");
+  const size_t m = (size_t)(h->s.ntypes + 1) * (h->s.ntypes + 1);
+  for (size_t q = 0; q < (size_t)kBondTables * m; q++)
+    if (!std::isfinite(tables[q])) return fail(h, DEM_ERR_BAD_ARG, "non-finite bond parameter");
+  // sanity range of the damping tables, createPerTypePairProperty(..., 0.0, 1.0)
+  for (int t = kBondDampFn; t <= kBondDampTt; t++)
+    for (size_t q = 0; q < m; q++)
+      if (tables[t * m + q] < 0.0 || tables[t * m + q] > 1.0)
+        return fail(h, DEM_ERR_BAD_ARG, "bond damping coefficients must lie in [0, 1]");
+  if (h->s.bondp) {
+    cudaFree(h->s.bondp);
+    h->allocs_misc.erase(std::remove(h->allocs_misc.begin(), h->allocs_misc.end(), (void *)h->s.bondp),
+                         h->allocs_misc.end());
+  }
+  CUDA_TRY(h, dalloc(h->allocs_misc, &h->s.bondp, (size_t)kBondTables * m));
+  CUDA_TRY(h, cudaMemcpy(h->s.bondp, tables, (size_t)kBondTables * m * sizeof(double), cudaMemcpyHostToDevice));
+  h->bond_tables.assign(tables, tables + (size_t)kBondTables * m);
+  h->bond_settings = *st;
+  int fl = 0;
+  if (st->stressBreak) fl |= kBondStressBreak;
+  if (st->tensionStress) fl |= kBondTension;
+  if (st->compressionStress) fl |= kBondCompression;
+  if (st->shearStress) fl |= kBondShear;
+  if (st->normalTorqueStress) fl |= kBondNormalTorque;
+  if (st->shearTorqueStress) fl |= kBondShearTorque;
+  if (st->createBondAlways) fl |= kBondCreateAlways;
+  // dampingBondSmooth implies dampingBond (connectToProperties, :285)
+  if (st->dampingBond || st->dampingBondSmooth) fl |= kBondDamping;
+  if (st->dampingBondSmooth) fl |= kBondDampingSmooth;
+  if (st->ratioTCBond) fl |= kBondUseRatioTC;
+  h->s.bond_flags = fl;
+  h->s.bond_ts_create = (long long)(int)st->tsCreate;
+  h->sys_gen++;
+  return DEM_OK;
+}
+
+// neighbor->register_contact_dist_factor of cohesion bond/nonlinear
+// (connectToProperties, src/cohesion_model_bond_nonlinear.h:330-380): the
+// cutoff grows with the largest breakage distance relative to the smallest
+// radius.  Returns 0 or a DEM_ERR_*.
+static int bond_contact_distance_factor(dem_handle *h, double minrad, double *cdf) {
+  const int nt = h->s.ntypes;
+  const size_t m = (size_t)(nt + 1) * (nt + 1);
+  auto T = [&](int t, int i, int j) { return h->bond_tables[t * m + (size_t)i * (nt + 1) + j]; };
+  const dem_bond_settings &st = h->bond_settings;
+  double cdf_all = 1.;
+  for (int i = 1; i < nt + 1; i++)
+    for (int j = 1; j < nt + 1; j++) {
+      double one;
+      if (!st.stressBreak) {
+        one = 1.1 * 0.5 * T(kBondMaxDist, i, j) / minrad;
+      } else {
+        double stress = T(kBondMaxSigma, i, j);
+        if (st.ratioTCBond) stress = std::fmax(stress, stress * T(kBondRatioTC, i, j));
+        if (T(kBondKfn2, i, j) <= 1e-15) return fail(h, DEM_ERR_BAD_ARG, "stress breakage needs K_fn2 > 0");
+        one = 0.5 * 1.1 * T(kBondCreateDist, i, j) / minrad + 0.5 * 1.1 * stress / (T(kBondKfn2, i, j) * minrad);
+      }
+      cdf_all = one > cdf_all ? one : cdf_all;
+    }
+  if (cdf_all > 10.) return fail(h, DEM_ERR_BAD_ARG, "bond distance above 10 particle diameters");
+  *cdf = cdf_all;
   return DEM_OK;
 }
 
@@ -490,10 +570,22 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
     if (!(radius[i] > 0.0) || !(rmass[i] > 0.0)) return fail(h, DEM_ERR_BAD_ARG, "radius and rmass must be > 0");
   // cutneighmax = (maxrad_i + maxrad_j)*cdf + skin, src/pair_gran.cpp:591-602,
   // src/neighbor.cpp:316-337
-  double maxrad = 0.0;
-  for (int i = 0; i < n; i++) maxrad = std::max(maxrad, radius[i]);
+  double maxrad = 0.0, minrad = 1e99;
+  for (int i = 0; i < n; i++) {
+    maxrad = std::max(maxrad, radius[i]);
+    minrad = std::min(minrad, radius[i]);
+  }
+  s.cdf = h->cfg.contact_distance_factor;
+  if (s.bond) {
+    if (!s.bondp) return fail(h, DEM_ERR_BAD_ARG, "cohesion bond/nonlinear needs dem_set_bond_params");
+    double cdf_bond = 1.0;
+    int rcb = bond_contact_distance_factor(h, minrad, &cdf_bond);
+    if (rcb) return rcb;
+    s.cdf = std::max(s.cdf, cdf_bond);
+  }
   const double cutoff = (maxrad + maxrad) * s.cdf;
   s.cutneighmax = std::sqrt(cutoff * cutoff) + s.skin;
+  s.ghost_slab = s.cutneighmax / 2. + s.skin / 2.;
   long ncell = 1;
   for (int d = 0; d < 3; d++) {
     long nc = (long)std::floor(s.prd[d] / (s.cutneighmax * (1.0 + 1e-9)));
@@ -613,20 +705,21 @@ int dem_upload_contact_history(dem_handle *h, int ne, const int *towner, const i
     if (rc) return rc;
   }
   const size_t P = h->s.pcap;
+  const int dnum = h->s.dnum;
   std::vector<int> pi(ne), pj(ne), fl(ne, 1), fill(row.begin(), row.end() - 1);
-  std::vector<double> hh(3 * P, 0.0);
+  std::vector<double> hh((size_t)dnum * P, 0.0);
   for (int k = 0; k < ne; k++) {
     const int p = fill[oi[k]]++;
     pi[p] = oi[k];
     pj[p] = oj[k];
-    for (int d = 0; d < kDnumShear; d++) hh[d * P + p] = hist[(size_t)k * kDnumShear + d];
+    for (int r = 0; r < dnum; r++) hh[dev_hist_index(h->s, r) * P + p] = hist[(size_t)k * dnum + r];
   }
   const PairArrays &L = h->s.pairs[0];
   if (ne) {
     CUDA_TRY(h, cudaMemcpy(L.i, pi.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemcpy(L.j, pj.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemcpy(L.flag, fl.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
-    CUDA_TRY(h, cudaMemcpy(L.hist, hh.data(), 3 * P * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(L.hist, hh.data(), hh.size() * sizeof(double), cudaMemcpyHostToDevice));
   }
   CUDA_TRY(h, cudaMemcpy(L.row, row.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
   CUDA_TRY(h, cudaMemset(L.rev_start, 0, (h->s.nmax + 1) * sizeof(int)));
@@ -790,7 +883,7 @@ int dem_npairs(dem_handle *h, int *npairs, int *dnum) {
   int rc = read_ctrl(h);
   if (rc) return rc;
   if (npairs) *npairs = h->host_ctrl.np;
-  if (dnum) *dnum = kDnumShear;
+  if (dnum) *dnum = h->s.dnum;
   return DEM_OK;
 }
 
@@ -822,10 +915,12 @@ int dem_download_contacts(dem_handle *h, int *tag_i, int *tag_j, int *shift, int
   }
   if (hist && np) {
     std::vector<double> hb(np);
-    for (int d = 0; d < kDnumShear; d++) {
+    const int dnum = h->s.dnum;
+    for (int r = 0; r < dnum; r++) {
+      const int d = dev_hist_index(h->s, r);
       CUDA_TRY(h, cudaMemcpy(hb.data(), L.hist + (size_t)d * h->s.pcap, np * sizeof(double),
                              cudaMemcpyDeviceToHost));
-      for (int p = 0; p < np; p++) hist[(size_t)p * kDnumShear + d] = hb[p];
+      for (int p = 0; p < np; p++) hist[(size_t)p * dnum + r] = hb[p];
     }
   }
   return DEM_OK;

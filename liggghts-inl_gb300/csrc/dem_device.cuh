@@ -21,8 +21,34 @@ namespace gb300 {
 constexpr int kMaxPlanes = 8;
 constexpr int kDnumShear = 3;
 constexpr int kContactNormal = 1 << 0;      // CONTACT_NORMAL_MODEL
+constexpr int kContactCohesion = 1 << 1;    // CONTACT_COHESION_MODEL
 constexpr int kContactTangential = 1 << 2;  // CONTACT_TANGENTIAL_MODEL
 constexpr int kNoShift = 13;                // shift code of (0,0,0)
+
+// cohesion bond/nonlinear.  A pair then carries kDnumBond history values; on
+// the device the shear comes first (d = 0..2) and the bond's 28 values follow
+// (d = 3 + b, b in the reference's order: bondFlag, initial_dist,
+// contactPos[3], ft[3], thetan[3], thetat[3], deltan_max, thetan_max[3],
+// thetat_max[3], thetan_min[3], thetat_min[3], deltan_min).  The C ABI uses
+// the reference's order (bond values first).
+constexpr int kBondValues = 28;
+constexpr int kDnumBond = kDnumShear + kBondValues;
+constexpr int kBondTables = 23;  // per-type-pair tables, DEM_BOND_* order
+enum {
+  kBondLambda = 0, kBondKfn1, kBondKufn1, kBondKcfn1, kBondKfn2, kBondKufn2, kBondKcfn2, kBondKft,
+  kBondKtn, kBondKutn, kBondKctn, kBondKtt, kBondKutt, kBondKctt, kBondDampFn, kBondDampFt,
+  kBondDampTn, kBondDampTt, kBondMaxDist, kBondMaxSigma, kBondMaxTau, kBondRatioTC, kBondCreateDist
+};
+// Sys::bond_flags bits (the model's on/off settings)
+enum {
+  kBondStressBreak = 1 << 0, kBondTension = 1 << 1, kBondCompression = 1 << 2, kBondShear = 1 << 3,
+  kBondNormalTorque = 1 << 4, kBondShearTorque = 1 << 5, kBondCreateAlways = 1 << 6,
+  kBondDamping = 1 << 7, kBondDampingSmooth = 1 << 8, kBondUseRatioTC = 1 << 9
+};
+// newtonflag of device history value d (sign flips in the partner's copy)
+__host__ __device__ __forceinline__ bool hist_newton(int d) {
+  return d < kDnumShear || (d >= kDnumShear + 5 && d <= kDnumShear + 13);
+}
 
 // status words in Ctrl::status
 constexpr int kStatOk = 0;
@@ -128,6 +154,12 @@ struct Sys {
   double boxlo[3], boxhi[3], prd[3];
   int periodic[3];
   double dt, skin, cdf, cutneighmax;
+  double ghost_slab;  // cutneighmax/2 + skin/2: CommBrick slab_offset of the ghost band
+  // cohesion bond/nonlinear (bond = 0: off, dnum = 3)
+  int bond, dnum;
+  double *bondp;      // kBondTables matrices of (nt+1)^2
+  int bond_flags;
+  long long bond_ts_create;  // static_cast<int>(tsCreateBondnonlinear)
   int neigh_every, neigh_delay, neigh_check;
   int normal, rolling, tdamp, limitf;
   int gravity_on;

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "bond_law.cuh"
 #include "contact_law.cuh"
 #include "dem_device.cuh"
 #include "dem_kernels.h"
@@ -44,6 +45,23 @@ __device__ __forceinline__ void image(const Sys &s, int code, double &xj, double
   if (sx) xj = __dadd_rn(xj, sx * s.prd[0]);
   if (sy) yj = __dadd_rn(yj, sy * s.prd[1]);
   if (sz) zj = __dadd_rn(zj, sz * s.prd[2]);
+}
+
+// Whether the periodic image of j (shift sv) exists as a ghost atom:
+// CommBrick::borders sends an atom across a periodic boundary only when it
+// lies within slab_offset + its radius of that boundary (the granular
+// criterion of CommBrick::decide, src/comm_brick.cpp:443,1613-1624).  With a
+// contact distance factor above 1 this band is narrower than the pair cutoff
+// and some periodic pairs near the cutoff do not exist in the reference.
+__device__ __forceinline__ bool ghost_exists(const Sys &s, const AtomArrays &A, int j, const int sv[3]) {
+  const double rad = A.r[j];
+  const double pos[3] = {A.x[j], A.y[j], A.z[j]};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (sv[d] > 0 && !(pos[d] <= __dadd_rn(__dadd_rn(s.boxlo[d], s.ghost_slab), rad))) return false;
+    if (sv[d] < 0 && !(pos[d] >= __dadd_rn(__dadd_rn(s.boxhi[d], -s.ghost_slab), -rad))) return false;
+  }
+  return true;
 }
 
 __device__ __forceinline__ int cell_coord(const Sys &s, double x, int d) {
@@ -493,6 +511,7 @@ __global__ void k_pairs(Sys s) {
           const int jb = s.cell_start[cell], je = s.cell_start[cell + 1];
           for (int j = jb; j < je; j++) {
             if (code == kNoShift && j <= i) continue;
+            if (code != kNoShift && !ghost_exists(s, A, j, sv)) continue;
             double xj = A.x[j], yj = A.y[j], zj = A.z[j];
             image(s, code, xj, yj, zj);
             const double delx = __dadd_rn(xi, -xj);
@@ -510,43 +529,42 @@ __global__ void k_pairs(Sys s) {
             if (out >= out_end) continue;  // count and fill passes agree; guard only
             // history carry-over: partner lookup by identity in the old list
             // (FixContactHistory::pre_exchange + the partner search of
-            // src/neigh_gran.cpp:590-620); j-side copies are negated.
-            double h0 = 0.0, h1 = 0.0, h2 = 0.0;
-            int flag = 0;
+            // src/neigh_gran.cpp:590-620); in the j-side copy the values
+            // registered with newtonflag 1 change sign.
+            int src = -1;
+            bool flip = false;
             if (rsq < __dmul_rn(radsum, radsum)) {
               const int oi = s.perm[i], oj = s.perm[j];
-              bool found = false;
               for (int q = L.row[oi]; q < L.row[oi + 1]; q++) {
                 if (L.j[q] == oj && L.flag[q] != 0) {
-                  h0 = L.hist[q];
-                  h1 = L.hist[(size_t)s.pcap + q];
-                  h2 = L.hist[2 * (size_t)s.pcap + q];
-                  found = true;
+                  src = q;
                   break;
                 }
               }
-              if (!found) {
+              if (src < 0) {
                 for (int k = L.rev_start[oi]; k < L.rev_start[oi + 1]; k++) {
                   const int q = L.rev[k];
                   if (L.i[q] == oj && L.flag[q] != 0) {
-                    h0 = -L.hist[q];
-                    h1 = -L.hist[(size_t)s.pcap + q];
-                    h2 = -L.hist[2 * (size_t)s.pcap + q];
-                    found = true;
+                    src = q;
+                    flip = true;
                     break;
                   }
                 }
               }
-              flag = found ? 1 : 0;
             }
             const int p = out++;
             M.i[p] = i;
             M.j[p] = j;
             M.sh[p] = (uint8_t)code;
-            M.flag[p] = flag;
-            M.hist[p] = h0;
-            M.hist[(size_t)s.pcap + p] = h1;
-            M.hist[2 * (size_t)s.pcap + p] = h2;
+            M.flag[p] = src >= 0 ? 1 : 0;
+            for (int d = 0; d < s.dnum; d++) {
+              double hv = 0.0;
+              if (src >= 0) {
+                hv = L.hist[(size_t)d * s.pcap + src];
+                if (flip && hist_newton(d)) hv = -hv;
+              }
+              M.hist[(size_t)d * s.pcap + p] = hv;
+            }
             const double mj = A.m[j];
             const double meff = mi * mj / (mi + mj);
             const double reff = radi * radj / (radi + radj);
@@ -624,9 +642,7 @@ __global__ void k_copy_pairs(Sys s) {
       L.j[p] = M.j[p];
       L.sh[p] = M.sh[p];
       L.flag[p] = M.flag[p];
-      L.hist[p] = M.hist[p];
-      L.hist[(size_t)s.pcap + p] = M.hist[(size_t)s.pcap + p];
-      L.hist[2 * (size_t)s.pcap + p] = M.hist[2 * (size_t)s.pcap + p];
+      for (int d = 0; d < s.dnum; d++) L.hist[(size_t)d * s.pcap + p] = M.hist[(size_t)d * s.pcap + p];
       L.reff[p] = M.reff[p];
       L.c0[p] = M.c0[p];
       L.c1[p] = M.c1[p];
@@ -660,7 +676,7 @@ __global__ void k_finish_rebuild(Sys s) {
 // to the entry's own slot p, so the processing order never changes a value.
 constexpr int kPairTile = 256;
 
-template <int NORMAL, bool ROLL>
+template <int NORMAL, bool ROLL, bool BOND>
 __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
   __shared__ int q_p[kPairTile];
   __shared__ double q_d[4][kPairTile];
@@ -673,9 +689,13 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
   const size_t P = s.pcap;
   const double cdm = s.cdf * s.cdf;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // cohesion bond/nonlinear: a bond can be created in this pass
+  const long long ntimestep = BOND ? c->ntimestep : 0;
+  const bool may_create = BOND && shearupdate &&
+                          ((s.bond_flags & kBondCreateAlways) || ntimestep == s.bond_ts_create);
   for (int base = blockIdx.x * kPairTile; base < np; base += gridDim.x * kPairTile) {
     const int p = base + threadIdx.x;
-    bool touch = false;
+    bool queue = false;
     double delx = 0., dely = 0., delz = 0., rsq = 0.;
     if (p < np) {
       const int i = L.i[p], j = L.j[p];
@@ -687,8 +707,8 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
       delz = __dadd_rn(A.z[i], -zj);
       rsq = rsq_rn(delx, dely, delz);
       const double radsum = __dadd_rn(A.r[i], A.r[j]);
-      touch = rsq < __dmul_rn(radsum, radsum);
-      if (!touch) {
+      queue = rsq < __dmul_rn(radsum, radsum);
+      if (!queue) {
         s.active[p] = 0;
         if (rsq < __dmul_rn(__dmul_rn(cdm, radsum), radsum)) {
           // TangentialModel<TANGENTIAL_HISTORY>::surfacesClose
@@ -696,10 +716,16 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
           L.hist[p] = 0.0;
           L.hist[P + p] = 0.0;
           L.hist[2 * P + p] = 0.0;
+          // CohesionModel::surfacesClose: bonded pairs (and pairs that may
+          // bond in this pass) are evaluated in phase 2
+          if (BOND && (may_create || L.hist[3 * P + p] >= 1.e-15)) {
+            const int tp = A.type[i] * (s.ntypes + 1) + A.type[j];
+            queue = __ldg(s.bondp + tp) >= 1.e-15;
+          }
         }
       }
     }
-    const unsigned m = __ballot_sync(0xffffffffu, touch);
+    const unsigned m = __ballot_sync(0xffffffffu, queue);
     if (lane == 0) wcnt[warp] = __popc(m);
     __syncthreads();
     int off = 0, tot = 0;
@@ -709,7 +735,7 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
       off += (k < warp) ? v : 0;
       tot += v;
     }
-    if (touch) {
+    if (queue) {
       const int slot = off + __popc(m & ((1u << lane) - 1u));
       q_p[slot] = p;
       q_d[0][slot] = delx;
@@ -729,34 +755,61 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
       ci.radi = A.r[i];
       ci.radj = A.r[j];
       ci.radsum = __dadd_rn(ci.radi, ci.radj);
-      ci.r = sqrt(rsq_q);
-      ci.rinv = rsqrt(rsq_q);
-      ci.reff = L.reff[q];
-      ci.c0 = L.c0[q];
-      ci.c1 = L.c1[q];
-      ci.en[0] = ci.d[0] * ci.rinv;
-      ci.en[1] = ci.d[1] * ci.rinv;
-      ci.en[2] = ci.d[2] * ci.rinv;
       ci.vr[0] = A.vx[i] - A.vx[j];
       ci.vr[1] = A.vy[i] - A.vy[j];
       ci.vr[2] = A.vz[i] - A.vz[j];
       ci.wi[0] = A.wx[i]; ci.wi[1] = A.wy[i]; ci.wi[2] = A.wz[i];
       ci.wj[0] = A.wx[j]; ci.wj[1] = A.wy[j]; ci.wj[2] = A.wz[j];
-      ci.deltan_wall = 0.0;
-      const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], A.type[j]);
-      double sh3[3] = {L.hist[q], L.hist[P + q], L.hist[2 * P + q]};
-      ContactOut o;
-      contact_law<NORMAL, false>(ci, tp, s.dt, s.tdamp, s.limitf, ROLL, shearupdate != 0, sh3, o);
-      if (shearupdate) {
-        L.hist[q] = sh3[0];
-        L.hist[P + q] = sh3[1];
-        L.hist[2 * P + q] = sh3[2];
+      const bool touch = !BOND || rsq_q < __dmul_rn(ci.radsum, ci.radsum);
+      ContactOut bo;
+      bool bonded = false;
+      if (BOND) {
+        BondIn bi;
+        bi.d[0] = ci.d[0]; bi.d[1] = ci.d[1]; bi.d[2] = ci.d[2];
+        bi.rsq = rsq_q;
+        bi.radi = ci.radi;
+        bi.radj = ci.radj;
+        bi.vi[0] = A.vx[i]; bi.vi[1] = A.vy[i]; bi.vi[2] = A.vz[i];
+        bi.vj[0] = A.vx[j]; bi.vj[1] = A.vy[j]; bi.vj[2] = A.vz[j];
+        for (int k = 0; k < 3; k++) { bi.wi[k] = ci.wi[k]; bi.wj[k] = ci.wj[k]; }
+        bi.xi[0] = A.x[i]; bi.xi[1] = A.y[i]; bi.xi[2] = A.z[i];
+        bi.tp = A.type[i] * (s.ntypes + 1) + A.type[j];
+        bonded = bond_nonlinear(s, bi, L.hist + 3 * P + q, P, L.flag + q, shearupdate != 0, ntimestep, bo);
       }
-      L.flag[q] |= (kContactNormal | kContactTangential);
-      s.resF[q] = o.F[0]; s.resF[P + q] = o.F[1]; s.resF[2 * P + q] = o.F[2];
-      s.resTi[q] = o.Ti[0]; s.resTi[P + q] = o.Ti[1]; s.resTi[2 * P + q] = o.Ti[2];
-      s.resTj[q] = o.Tj[0]; s.resTj[P + q] = o.Tj[1]; s.resTj[2 * P + q] = o.Tj[2];
-      s.active[q] = 1;
+      ContactOut o;
+      if (touch) {
+        ci.r = sqrt(rsq_q);
+        ci.rinv = rsqrt(rsq_q);
+        ci.reff = L.reff[q];
+        ci.c0 = L.c0[q];
+        ci.c1 = L.c1[q];
+        ci.en[0] = ci.d[0] * ci.rinv;
+        ci.en[1] = ci.d[1] * ci.rinv;
+        ci.en[2] = ci.d[2] * ci.rinv;
+        ci.deltan_wall = 0.0;
+        const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], A.type[j]);
+        double sh3[3] = {L.hist[q], L.hist[P + q], L.hist[2 * P + q]};
+        contact_law<NORMAL, false>(ci, tp, s.dt, s.tdamp, s.limitf, ROLL, shearupdate != 0, sh3, o,
+                                   (BOND && bonded) ? &bo : nullptr);
+        if (shearupdate) {
+          L.hist[q] = sh3[0];
+          L.hist[P + q] = sh3[1];
+          L.hist[2 * P + q] = sh3[2];
+        }
+        L.flag[q] |= (kContactNormal | kContactTangential);
+      } else {
+        for (int k = 0; k < 3; k++) {
+          o.F[k] = bo.F[k];
+          o.Ti[k] = bo.Ti[k];
+          o.Tj[k] = bo.Tj[k];
+        }
+      }
+      if (touch || bonded) {
+        s.resF[q] = o.F[0]; s.resF[P + q] = o.F[1]; s.resF[2 * P + q] = o.F[2];
+        s.resTi[q] = o.Ti[0]; s.resTi[P + q] = o.Ti[1]; s.resTi[2 * P + q] = o.Ti[2];
+        s.resTj[q] = o.Tj[0]; s.resTj[P + q] = o.Tj[1]; s.resTj[2 * P + q] = o.Tj[2];
+        s.active[q] = 1;
+      }
     }
     __syncthreads();
   }
@@ -1157,12 +1210,22 @@ int launch_set_rebuild(const Sys &s, int v, cudaStream_t st) {
 int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t st) {
   const int B = 256;
   const int g = grid_for(s.pcap, B, lc.max_grid);
+  if (s.bond) {
+    if (s.normal == kHertz) {
+      if (s.rolling) k_pair<kHertz, true, true><<<g, B, 0, st>>>(s, shearupdate);
+      else k_pair<kHertz, false, true><<<g, B, 0, st>>>(s, shearupdate);
+    } else {
+      if (s.rolling) k_pair<kHooke, true, true><<<g, B, 0, st>>>(s, shearupdate);
+      else k_pair<kHooke, false, true><<<g, B, 0, st>>>(s, shearupdate);
+    }
+    return 1;
+  }
   if (s.normal == kHertz) {
-    if (s.rolling) k_pair<kHertz, true><<<g, B, 0, st>>>(s, shearupdate);
-    else k_pair<kHertz, false><<<g, B, 0, st>>>(s, shearupdate);
+    if (s.rolling) k_pair<kHertz, true, false><<<g, B, 0, st>>>(s, shearupdate);
+    else k_pair<kHertz, false, false><<<g, B, 0, st>>>(s, shearupdate);
   } else {
-    if (s.rolling) k_pair<kHooke, true><<<g, B, 0, st>>>(s, shearupdate);
-    else k_pair<kHooke, false><<<g, B, 0, st>>>(s, shearupdate);
+    if (s.rolling) k_pair<kHooke, true, false><<<g, B, 0, st>>>(s, shearupdate);
+    else k_pair<kHooke, false, false><<<g, B, 0, st>>>(s, shearupdate);
   }
   return 1;
 }

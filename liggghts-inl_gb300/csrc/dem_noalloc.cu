@@ -255,6 +255,7 @@ extern "C" int dem_contact_forces_noalloc(int n, const double *x, const double *
   if (cfg->normal_model == DEM_NORMAL_HERTZ && !betaeff) return DEM_ERR_BAD_ARG;
   if (cfg->normal_model == DEM_NORMAL_HOOKE && !coeffRestLog) return DEM_ERR_BAD_ARG;
   if (cfg->normal_model != DEM_NORMAL_HERTZ && cfg->normal_model != DEM_NORMAL_HOOKE) return DEM_ERR_UNSUPPORTED;
+  if (cfg->cohesion_model != DEM_COHESION_OFF) return DEM_ERR_UNSUPPORTED;  // 3 history values per pair
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DEM_ERR_NO_DEVICE;
   unsigned char *base = nullptr;

@@ -41,6 +41,16 @@ class DemConfig(ctypes.Structure):
                 ("gravity_on", ctypes.c_int), ("gravity", ctypes.c_double * 3)]
 
 
+# on/off settings of cohesion bond/nonlinear, dem_bond_settings order
+BOND_FLAGS = ("stressBreak", "tensionStress", "compressionStress", "shearStress",
+              "normalTorqueStress", "shearTorqueStress", "createBondAlways", "dampingBond",
+              "dampingBondSmooth", "ratioTCBond")
+
+
+class DemBondSettings(ctypes.Structure):
+    _fields_ = [("tsCreate", ctypes.c_double)] + [(k, ctypes.c_int) for k in BOND_FLAGS]
+
+
 class DemStats(ctypes.Structure):
     _fields_ = [("ntimestep", ctypes.c_longlong), ("nrebuilds", ctypes.c_longlong),
                 ("npairs", ctypes.c_longlong), ("nlost", ctypes.c_longlong),
@@ -70,6 +80,7 @@ def load(build=True):
     L.dem_create.argtypes = [ctypes.POINTER(DemConfig), ctypes.POINTER(P)]
     L.dem_destroy.argtypes = [P]
     L.dem_set_pair_params.argtypes = [P, I] + [P] * 6 + [ctypes.c_double]
+    L.dem_set_bond_params.argtypes = [P, P, ctypes.POINTER(DemBondSettings)]
     L.dem_derive_hertz_tables.argtypes = [I] + [P] * 7
     L.dem_add_plane.argtypes = [P, I, ctypes.c_double, I, I, P]
     L.dem_upload_atoms.argtypes = [P, I] + [P] * 7
@@ -145,6 +156,15 @@ class DemSystem:
                 for k in ("Yeff", "Geff", "betaeff", "coeffFrict", "coeffRollFrict", "coeffRestLog")]
         self._check(L.dem_set_pair_params(self.h, nt, *[_p(a) for a in tabs],
                                           float(case.get("charVel", 0.0))))
+        if c.cohesion_model == 1:
+            b = case["bond"]
+            bt = np.ascontiguousarray(b["tables"], dtype=np.float64)
+            assert bt.shape == (23, nt + 1, nt + 1)
+            st = DemBondSettings()
+            st.tsCreate = float(b["settings"]["tsCreate"])
+            for k in BOND_FLAGS:
+                setattr(st, k, int(b["settings"][k]))
+            self._check(L.dem_set_bond_params(self.h, _p(bt), ctypes.byref(st)))
         for (axis, pos, wtype, roll) in case.get("planes", []):
             self._check(L.dem_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll), None))
         self._meshkeep = []

@@ -144,6 +144,147 @@ def hopper_case(seed, r_out, r_top, half_angle_deg, n_az, n_ax, spacing, radius=
     return case
 
 
+# property/global names of the 23 per-type-pair tables of cohesion
+# bond/nonlinear (src/cohesion_model_bond_nonlinear.h:70-147), in the order
+# the C ABI stacks them (DEM_BOND_* / ORC_BOND_*)
+BOND_TABLES = ("radiusMultiplierBondnonlinear", "stiffnessPerUnitAreaK_fn1",
+               "stiffnessPerUnitAreaKu_fn1", "stiffnessPerUnitAreaKc_fn1",
+               "stiffnessPerUnitAreaK_fn2", "stiffnessPerUnitAreaKu_fn2",
+               "stiffnessPerUnitAreaKc_fn2", "stiffnessPerUnitAreaK_ft",
+               "stiffnessPerUnitAreaK_tn", "stiffnessPerUnitAreaKu_tn", "stiffnessPerUnitAreaKc_tn",
+               "stiffnessPerUnitAreaK_tt", "stiffnessPerUnitAreaKu_tt", "stiffnessPerUnitAreaKc_tt",
+               "dampingNormalForceBondnonlinear", "dampingTangentialForceBondnonlinear",
+               "dampingNormalTorqueBondnonlinear", "dampingTangentialTorqueBondnonlinear",
+               "maxDistanceBondnonlinear", "maxSigmaBondnonlinear", "maxTauBondnonlinear",
+               "ratioTensionCompressionBondnonlinear", "createDistanceBondnonlinear")
+BOND_FLAGS = ("stressBreak", "tensionStress", "compressionStress", "shearStress",
+              "normalTorqueStress", "shearTorqueStress", "createBondAlways", "dampingBond",
+              "dampingBondSmooth", "ratioTCBond")
+# the model's defaults (registerSettings, src/cohesion_model_bond_nonlinear.h:231-243)
+BOND_DEFAULTS = dict(stressBreak=0, tensionStress=1, compressionStress=1, shearStress=1,
+                     normalTorqueStress=1, shearTorqueStress=1, createBondAlways=0,
+                     dampingBond=1, dampingBondSmooth=0, ratioTCBond=0)
+# the keywords of those settings on the pair_style line
+BOND_KEYWORDS = dict(stressBreak="stressBreak", tensionStress="tensionStress",
+                     compressionStress="compressionStress", shearStress="shearStress",
+                     normalTorqueStress="normalTorqueStress", shearTorqueStress="shearTorqueStress",
+                     createBondAlways="createBondAlways", dampingBond="dampingBond",
+                     dampingBondSmooth="dampingBondSmooth", ratioTCBond="ratioTensionCompressionBond")
+
+
+def bond_params(ntypes, bonded_types, tsCreate=1.0, **kw):
+    """Tables for cohesion bond/nonlinear: every property takes one value for
+    all type pairs, except radiusMultiplier, which is 0 outside the type
+    pairs within ``bonded_types`` (so walls of other types never bond).  Keyword names are the property/global names without
+    the common prefixes, e.g. K_fn1=..., radiusMultiplier=..., maxDistance=...;
+    on/off settings by their names in BOND_FLAGS."""
+    damp = {"dampingNormalForceBondnonlinear": "damp_fn", "dampingTangentialForceBondnonlinear": "damp_ft",
+            "dampingNormalTorqueBondnonlinear": "damp_tn",
+            "dampingTangentialTorqueBondnonlinear": "damp_tt"}
+    short = {n: damp.get(n) or n.replace("stiffnessPerUnitArea", "").replace("Bondnonlinear", "")
+             .replace("ratioTensionCompression", "ratioTC") for n in BOND_TABLES}
+    tabs = np.zeros((len(BOND_TABLES), ntypes + 1, ntypes + 1))
+    for k, n in enumerate(BOND_TABLES):
+        v = kw.pop(short[n], 0.0)
+        if k == 0:  # radiusMultiplier: 0 switches the model off for a type pair
+            for i in bonded_types:
+                for j in bonded_types:
+                    tabs[k, i, j] = v
+        else:
+            tabs[k, 1:, 1:] = v
+    settings = dict(BOND_DEFAULTS, tsCreate=float(tsCreate))
+    for f in BOND_FLAGS:
+        if f in kw:
+            settings[f] = int(kw.pop(f))
+    assert not kw, "unknown bond parameters: %s" % sorted(kw)
+    return dict(tables=tabs, settings=settings)
+
+
+def fibre_case(seed, nfib, nper, radius, box, spacing=(0.999, 1.001), density=1000.0,
+               E=(5e7, 5e7), nu=(0.3, 0.3), rest=((0.5, 0.5), (0.5, 0.5)),
+               frict=((0.3, 0.3), (0.3, 0.3)), vmax=0.0, wmax=0.0, dt=1e-7, skin=2e-4,
+               gravity=(0.0, 0.0, -9.81), bond=None, gap=1.3, max_tries=200000, z0=None,
+               max_fail=None):
+    """Straight fibres of nper touching spheres (type 1) with directions
+    uniform on the sphere, centres uniform in the box; a floor plane of wall
+    type 2 at z = 0, periodic in x and y.  Sphere spacing along a fibre is
+    spacing[0..1] x 2r (per fibre, uniform); spheres of different fibres stay
+    more than gap x 2r apart, so only intra-fibre pairs bond at creation.
+    Placement stops after max_tries trials or max_fail trials in a row
+    without success.
+    ``bond`` is a bond_params(...) dict (cohesion bond/nonlinear)."""
+    rng = np.random.default_rng(seed)
+    Lx, Ly, Lz = box
+    d = 2.0 * radius
+    pts = []
+    # spatial hash of placed spheres (cell >= gap*d), periodic in x and y
+    cs = gap * d
+    ncx, ncy = max(1, int(Lx // cs)), max(1, int(Ly // cs))
+    csx, csy = Lx / ncx, Ly / ncy
+    grid = {}
+
+    def key(p):
+        return (int(p[0] // csx) % ncx, int(p[1] // csy) % ncy, int(p[2] // cs))
+
+    def clear(chain):
+        for p in chain:
+            kx, ky, kz = key(p)
+            for ox in (-1, 0, 1):
+                for oy in (-1, 0, 1):
+                    for oz in (-1, 0, 1):
+                        for q in grid.get(((kx + ox) % ncx, (ky + oy) % ncy, kz + oz), ()):
+                            dx = p[0] - q[0]
+                            dx -= Lx * round(dx / Lx)
+                            dy = p[1] - q[1]
+                            dy -= Ly * round(dy / Ly)
+                            dz = p[2] - q[2]
+                            if dx * dx + dy * dy + dz * dz < (gap * d) ** 2:
+                                return False
+        return True
+
+    tries = fails = 0
+    while len(pts) < nfib and tries < max_tries and (max_fail is None or fails < max_fail):
+        tries += 1
+        fails += 1
+        u = rng.normal(size=3)
+        u /= np.linalg.norm(u)
+        sp = d * rng.uniform(*spacing)
+        half = 0.5 * (nper - 1) * sp
+        lo = np.array([0.0, 0.0, (z0 if z0 is not None else radius) + half * abs(u[2]) + radius])
+        hi = np.array([Lx, Ly, Lz - half * abs(u[2]) - radius])
+        if np.any(hi <= lo):
+            continue
+        c = rng.uniform(lo, hi)
+        chain = c + (np.arange(nper) - 0.5 * (nper - 1))[:, None] * sp * u
+        chain[:, 0] %= Lx
+        chain[:, 1] %= Ly
+        if not clear(chain):
+            continue
+        for p in chain:
+            grid.setdefault(key(p), []).append(p)
+        pts.append(chain)
+        fails = 0
+    x = np.concatenate(pts).astype(np.float64)
+    n = len(x)
+    r = np.full(n, radius)
+    v = rng.uniform(-vmax, vmax, size=(n, 3)) if vmax > 0 else np.zeros((n, 3))
+    w = rng.uniform(-wmax, wmax, size=(n, 3)) if wmax > 0 else np.zeros((n, 3))
+    case = dict(
+        boxlo=(0.0, 0.0, 0.0), boxhi=(Lx, Ly, Lz), periodic=(1, 1, 0), dt=dt, skin=skin, cdf=1.0,
+        neigh=(1, 0, 1), normal_model=0, rolling_model=0, gravity=gravity, ntypes=2, charVel=0.0,
+        planes=[(2, 0.0, 2, 0)], cohesion_model=1 if bond is not None else 0,
+        material=dict(E=list(E), nu=list(nu), rest=[list(q) for q in rest],
+                      frict=[list(q) for q in frict], rollfrict=None, density=density),
+        atoms=dict(tag=np.arange(1, n + 1, dtype=np.int32), type=np.ones(n, np.int32), x=x, v=v,
+                   omega=w, radius=r, rmass=sphere_mass(r, density)),
+        nfibres=len(pts), nper=nper,
+    )
+    if bond is not None:
+        case["bond"] = bond
+    case.update(derive_tables(E, nu, rest, frict, None))
+    return case
+
+
 def lattice_case(seed, nx, ny, nz, spacing, radius=(1e-3, 1e-3), density=2500.0,
                  z0=None, jitter=0.0, vmax=0.0, wmax=0.0, ntypes=1, E=(5e6,), nu=(0.45,),
                  rest=((0.9,),), frict=((0.5,),), rollfrict=None, periodic=(1, 1, 0),

@@ -17,6 +17,10 @@ LIB = os.path.join(BUILD, "liboracle_dem.so")
 NORMAL_HERTZ, NORMAL_HOOKE = 0, 1
 ROLLING_OFF, ROLLING_CDT = 0, 1
 COHESION_OFF, COHESION_BOND_NONLINEAR = 0, 1
+# on/off settings of cohesion bond/nonlinear, in orc_bond_settings order
+BOND_FLAGS = ("stressBreak", "tensionStress", "compressionStress", "shearStress",
+              "normalTorqueStress", "shearTorqueStress", "createBondAlways", "dampingBond",
+              "dampingBondSmooth", "ratioTCBond")
 
 
 def build(force=False):
@@ -43,6 +47,10 @@ class OrcConfig(ctypes.Structure):
                 ("gravity_on", ctypes.c_int), ("gravity", ctypes.c_double * 3)]
 
 
+class OrcBondSettings(ctypes.Structure):
+    _fields_ = [("tsCreate", ctypes.c_double)] + [(k, ctypes.c_int) for k in BOND_FLAGS]
+
+
 _lib = None
 
 
@@ -58,6 +66,7 @@ def lib():
         L.orc_last_error.restype = ctypes.c_char_p
         L.orc_last_error.argtypes = [P]
         L.orc_set_pair_params.argtypes = [P, ctypes.c_int] + [P] * 6 + [ctypes.c_double]
+        L.orc_set_bond_params.argtypes = [P, P, ctypes.POINTER(OrcBondSettings)]
         L.orc_add_plane.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int]
         L.orc_set_atoms.argtypes = [P, ctypes.c_int] + [P] * 7
         L.orc_setup.argtypes = [P]
@@ -114,6 +123,16 @@ class Oracle:
             tabs.append(a)
         self._keep += tabs
         L.orc_set_pair_params(self.h, nt, *[_p(a) for a in tabs], float(case.get("charVel", 0.0)))
+        if c.cohesion_model == COHESION_BOND_NONLINEAR:
+            b = case["bond"]
+            bt = np.ascontiguousarray(b["tables"], dtype=np.float64)
+            assert bt.shape == (23, nt + 1, nt + 1)
+            st = OrcBondSettings()
+            st.tsCreate = float(b["settings"]["tsCreate"])
+            for k in BOND_FLAGS:
+                setattr(st, k, int(b["settings"][k]))
+            self._keep.append(bt)
+            self._check(L.orc_set_bond_params(self.h, _p(bt), ctypes.byref(st)))
         for (axis, pos, wtype, roll) in case.get("planes", []):
             L.orc_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll))
         self.nmesh = 0

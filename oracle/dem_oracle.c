@@ -14,6 +14,7 @@
  *   NormalModel<HOOKE>                   src/normal_model_hooke.h:230-400
  *   TangentialModel<TANGENTIAL_HISTORY>  src/tangential_model_history.h:135-439
  *   RollingModel<ROLLING_CDT>            src/rolling_model_cdt.h:89-167
+ *   CohesionModel<BOND_NONLINEAR>        src/cohesion_model_bond_nonlinear.h:330-992
  *   FixGravity::post_force               src/fix_gravity.cpp:301-352
  *   FixWallGran::post_force_primitive    src/fix_wall_gran.cpp:988-1119
  *   Walls::Granular::compute_force       src/fix_wall_gran_base.h:159-372
@@ -77,6 +78,12 @@ struct orc_sys {
   orc_mesh meshes[4];
   int nmeshes;
 
+  /* cohesion bond/nonlinear: ORC_BOND_NTABLES tables of (ntypes+1)^2 */
+  int bond_on;
+  double *bond;
+  orc_bond_settings bset;
+  int shear_off;     /* offset of shear[3] inside a pair's history */
+
   double cutneighmax;
   long ntimestep, nrebuilds;
   int ago;
@@ -92,14 +99,20 @@ static void *xrealloc(void *p, size_t n) {
 orc_sys *orc_create(const orc_config *cfg) {
   orc_sys *s = (orc_sys *)calloc(1, sizeof(orc_sys));
   s->cfg = *cfg;
-  s->dnum = 3; /* shearx, sheary, shearz: src/tangential_model_history.h:79-81 */
+  /* history values in the order the models register them (normal, cohesion,
+   * tangential, rolling: src/contact_models.h:142-157): the bond's 28
+   * (src/cohesion_model_bond_nonlinear.h:198-226) before the shear's 3
+   * (src/tangential_model_history.h:79-81) */
+  s->bond_on = cfg->cohesion_model == ORC_COHESION_BOND_NONLINEAR;
+  s->dnum = s->bond_on ? 31 : 3;
+  s->shear_off = s->bond_on ? 28 : 0;
   return s;
 }
 
 void orc_destroy(orc_sys *s) {
   if (!s) return;
   free(s->Yeff); free(s->Geff); free(s->betaeff); free(s->frict); free(s->rollfrict);
-  free(s->restlog);
+  free(s->restlog); free(s->bond);
   free(s->tag); free(s->type); free(s->x); free(s->v); free(s->omega); free(s->f);
   free(s->torque); free(s->radius); free(s->rmass); free(s->xhold); free(s->prow);
   free(s->nstart); free(s->nj); free(s->nshift); free(s->nflag); free(s->nhist);
@@ -137,6 +150,20 @@ int orc_set_pair_params(orc_sys *s, int ntypes, const double *Yeff, const double
   s->rollfrict = dupm(coeffRollFrict, ntypes);
   s->restlog = dupm(coeffRestLog, ntypes);
   s->charVel = charVel;
+  return 0;
+}
+
+int orc_set_bond_params(orc_sys *s, const double *tables, const orc_bond_settings *st) {
+  if (!s->bond_on || s->ntypes < 1) {
+    snprintf(s->err, sizeof s->err, "bond parameters need cohesion bond/nonlinear and pair params");
+    return -1;
+  }
+  const size_t m = (size_t)(s->ntypes + 1) * (s->ntypes + 1) * ORC_BOND_NTABLES;
+  s->bond = (double *)xrealloc(s->bond, m * sizeof(double));
+  memcpy(s->bond, tables, m * sizeof(double));
+  s->bset = *st;
+  /* CohesionModel::connectToProperties: dampingBondSmooth implies dampingBond */
+  if (s->bset.dampingBondSmooth) s->bset.dampingBond = 1;
   return 0;
 }
 
@@ -366,6 +393,12 @@ static void pbc_and_exchange(orc_sys *s) {
 /* FixContactHistory::pre_exchange: neighbour list -> per-atom partners  */
 /* ------------------------------------------------------------------ */
 
+/* newtonflag of history value d (add_history_value's second argument) */
+static inline int hist_newton(const orc_sys *s, int d) {
+  if (!s->bond_on) return 1;
+  return (d >= 5 && d <= 13) || d >= 28;
+}
+
 static void pre_exchange(orc_sys *s) {
   const int n = s->n, dnum = s->dnum;
   int *cnt = (int *)calloc(n + 1, sizeof(int));
@@ -397,8 +430,10 @@ static void pre_exchange(orc_sys *s) {
           if (s->nshift[p] == 0) {
             m = s->pstart[j] + cnt[j]++;
             s->ptag[m] = s->tag[i];
-            /* every history value of tangential history has newtonflag 1 */
-            for (int d = 0; d < dnum; d++) s->phist[(size_t)m * dnum + d] = -hist[d];
+            /* j's copy: values registered with newtonflag 1 change sign —
+             * all of shear[3]; of the bond's, ft[3], thetan[3], thetat[3] */
+            for (int d = 0; d < dnum; d++)
+              s->phist[(size_t)m * dnum + d] = hist_newton(s, d) ? -hist[d] : hist[d];
           }
         }
   }
@@ -432,6 +467,27 @@ static inline void image_x(const orc_sys *s, int j, int sh, double *xj) {
     double dx = sv[d] * (s->cfg.boxhi[d] - s->cfg.boxlo[d]);
     xj[d] = sv[d] ? s->x[3 * j + d] + dx : s->x[3 * j + d];
   }
+}
+
+/* Whether the periodic image of j with shift sh exists as a ghost atom.
+ * CommBrick::borders sends an atom across a periodic boundary when it lies
+ * within slab_offset + its radius of that boundary (the granular criterion
+ * of CommBrick::decide, src/comm_brick.cpp:443,1613-1624, with
+ * slab_offset = cutghost/2 + skin/2 and cutghost = cutneighmax).  With a
+ * contact distance factor above 1 this band is narrower than the pair
+ * cutoff, so the reference misses some periodic pairs near the cutoff;
+ * they are left out here as well. */
+static int ghost_exists(const orc_sys *s, int j, int sh) {
+  int sv[3];
+  shift_decode(sh, &sv[0], &sv[1], &sv[2]);
+  const double slab_offset = s->cutneighmax / 2. + s->cfg.skin / 2.;
+  const double rad = s->radius[j];
+  for (int d = 0; d < 3; d++) {
+    const double pos = s->x[3 * j + d];
+    if (sv[d] > 0 && !(pos <= (s->cfg.boxlo[d] + slab_offset) + rad)) return 0;
+    if (sv[d] < 0 && !(pos >= (s->cfg.boxhi[d] - slab_offset) - rad)) return 0;
+  }
+  return 1;
 }
 
 static int neighbor_build(orc_sys *s) {
@@ -502,6 +558,7 @@ static int neighbor_build(orc_sys *s) {
           int sh = shift_code(sv[0], sv[1], sv[2]);
           for (int j = head[cc[0] + nc[0] * (cc[1] + nc[1] * cc[2])]; j >= 0; j = next[j]) {
             if (sh == 0 && j <= i) continue;
+            if (sh != 0 && !ghost_exists(s, j, sh)) continue;
             double xj[3];
             image_x(s, j, sh, xj);
             const double delx = xtmp - xj[0];
@@ -596,6 +653,9 @@ typedef struct {
   double Fn, kn, kt, gamman, gammat;
   double *shear;
   int *contact_flags;
+  double *bondhist;        /* the bond's 28 history values, NULL without the model */
+  const double *x_i;
+  int has_force_update;
 } sidata_t;
 
 static void surface_default(sidata_t *sd) {
@@ -805,10 +865,293 @@ static void rolling_cdt(const orc_sys *s, sidata_t *sd, fdata *fi, fdata *fj) {
   fj->dT[0] += r_torque[0]; fj->dT[1] += r_torque[1]; fj->dT[2] += r_torque[2];
 }
 
+/* ------------------------------------------------------------------ */
+/* CohesionModel<COHESION_BOND_NONLINEAR>                              */
+/* src/cohesion_model_bond_nonlinear.h:394-992 (particle pairs)        */
+/* ------------------------------------------------------------------ */
+
+#define CONTACT_COHESION_MODEL (1 << 1)
+
+static inline double BT(const orc_sys *s, int table, int i, int j) {
+  const size_t m = (size_t)(s->ntypes + 1) * (s->ntypes + 1);
+  return s->bond[table * m + (size_t)i * (s->ntypes + 1) + j];
+}
+
+/* MathExtraLiggghts::sgn, src/math_extra_liggghts.h:120-123 */
+static inline int sgn_d(double v) { return (0.0 < v) - (v < 0.0); }
+
+/* vectorProject3D with vectorNormalize3D, src/vector_liggghts.h:63-70,437-442 */
+static void project3(const double *v, const double *on, double *res) {
+  double nrm[3] = {on[0], on[1], on[2]};
+  const double norm = sqrt(nrm[0] * nrm[0] + nrm[1] * nrm[1] + nrm[2] * nrm[2]);
+  const double invnorm = (norm == 0.) ? 0. : 1. / norm;
+  nrm[0] *= invnorm; nrm[1] *= invnorm; nrm[2] *= invnorm;
+  const double dot = v[0] * nrm[0] + v[1] * nrm[1] + v[2] * nrm[2];
+  res[0] = dot * nrm[0]; res[1] = dot * nrm[1]; res[2] = dot * nrm[2];
+}
+
+/* one component of the hysteretic twisting/bending torque,
+ * src/cohesion_model_bond_nonlinear.h:677-761 (normal), :792-866 (tangential):
+ * sign-driven reset of the opposite extreme, piecewise law, new extremes */
+static double bond_hyst(double th, double *hmax, double *hmin, double k, double ku, double kc,
+                        double JI) {
+  if (th > 0.0) *hmin = 0.0;
+  else if (th < 0.0) *hmax = 0.0;
+  const double c1 = (ku - k) / (ku + kc) * *hmax;
+  const double c2 = (ku - k) / (ku + kc) * *hmin;
+  double t;
+  if ((th >= *hmax) || (th <= *hmin)) t = -k * JI * th;
+  else if (th > c1) t = -ku * JI * th + (ku - k) * JI * *hmax;
+  else if (th >= c2) t = kc * JI * th;
+  else t = -ku * JI * th + (ku - k) * JI * *hmin;
+  if (th > *hmax) *hmax = th;
+  if (th < *hmin) *hmin = th;
+  return t;
+}
+
+/* breakBondnonlinear, :980-992 */
+static void bond_break(sidata_t *sd) {
+  if (sd->contact_flags) *sd->contact_flags &= ~CONTACT_COHESION_MODEL;
+  sd->bondhist[0] = 0.;
+  sd->bondhist[1] = 0.;
+}
+
+/* surfacesClose (also reached from surfacesIntersect once lambda > 0) for a
+ * particle pair; ASSIGNS i/j forces and torques when the pair is bonded
+ * (the override of :917-939). */
+static void bond_nonlinear(const orc_sys *s, sidata_t *sd, fdata *fi, fdata *fj) {
+  const orc_bond_settings *bs = &s->bset;
+  const int it = sd->itype, jt = sd->jtype;
+  const double radi = sd->radi, radj = sd->radj;
+  const double lambda = BT(s, ORC_BOND_RADIUS_MULTIPLIER, it, jt);
+  if (lambda < 1.e-15) return;
+  double *const h = sd->bondhist;
+  const int update_history = sd->update_history;
+  const double r_centers = 1.0 * sqrt(sd->rsq);
+  const double r = r_centers;
+  if (update_history) {
+    if (h[0] < 1.e-15) {
+      const int create = (bs->createBondAlways || s->ntimestep == (long)(int)bs->tsCreate) &&
+                         (r_centers < BT(s, ORC_BOND_CREATE_DIST, it, jt));
+      if (!create) return;
+      /* createBondnonlinear, :961-978 */
+      if (sd->contact_flags) *sd->contact_flags |= CONTACT_COHESION_MODEL;
+      h[0] = 1.0;
+      h[1] = r;
+      for (int d = 0; d < 3; d++) h[2 + d] = sd->x_i[d] - sd->delta[d];
+      for (int d = 5; d < 14; d++) h[d] = 0.0;
+    }
+  } else if (h[0] < 1.e-15) {
+    return;
+  }
+  double delta[3] = {sd->delta[0], sd->delta[1], sd->delta[2]};
+  double force_tang[3] = {h[5], h[6], h[7]};
+  double theta_normal[3] = {h[8], h[9], h[10]};
+  double theta_tang[3] = {h[11], h[12], h[13]};
+  if (!bs->stressBreak && r > BT(s, ORC_BOND_MAX_DIST, it, jt) && update_history) {
+    bond_break(sd);
+    return;
+  }
+  if (sd->contact_flags) *sd->contact_flags |= CONTACT_COHESION_MODEL;
+  const double rinv = 1. / r;
+  const double en[3] = {rinv * delta[0], rinv * delta[1], rinv * delta[2]};
+  const double *vi = sd->v_i, *vj = sd->v_j, *omegai = sd->omega_i, *omegaj = sd->omega_j;
+  const double k_fn1 = BT(s, ORC_BOND_K_FN1, it, jt), ku_fn1 = BT(s, ORC_BOND_KU_FN1, it, jt);
+  const double kc_fn1 = BT(s, ORC_BOND_KC_FN1, it, jt), k_fn2 = BT(s, ORC_BOND_K_FN2, it, jt);
+  const double ku_fn2 = BT(s, ORC_BOND_KU_FN2, it, jt), kc_fn2 = BT(s, ORC_BOND_KC_FN2, it, jt);
+  const double k_ft = BT(s, ORC_BOND_K_FT, it, jt);
+  const double k_tn = BT(s, ORC_BOND_K_TN, it, jt), ku_tn = BT(s, ORC_BOND_KU_TN, it, jt);
+  const double kc_tn = BT(s, ORC_BOND_KC_TN, it, jt);
+  const double k_tt = BT(s, ORC_BOND_K_TT, it, jt), ku_tt = BT(s, ORC_BOND_KU_TT, it, jt);
+  const double kc_tt = BT(s, ORC_BOND_KC_TT, it, jt);
+  const double rb = lambda * (radi < radj ? radi : radj);
+  const double A = M_PI * rb * rb;
+  const double J = 0.5 * A * rb * rb;
+  const double I = 0.5 * J;
+  const double dt = s->cfg.dt;
+  const double radsuminv = 1. / (radi + radj);
+  const double cri = r * radi * radsuminv;
+  const double crj = r * radj * radsuminv;
+  double tmp1[3], tmp2[3];
+  double vr[3] = {vi[0] - vj[0], vi[1] - vj[1], vi[2] - vj[2]};
+  double vn[3], vt[3], wr[3], vtr[3], wn[3], wt[3];
+  project3(vr, en, vn);
+  for (int d = 0; d < 3; d++) vt[d] = vr[d] - vn[d];
+  for (int d = 0; d < 3; d++) {
+    tmp1[d] = (radi * radsuminv) * omegai[d];
+    tmp2[d] = (radj * radsuminv) * omegaj[d];
+    wr[d] = tmp1[d] + tmp2[d];
+  }
+  tmp1[0] = delta[1] * wr[2] - delta[2] * wr[1];
+  tmp1[1] = delta[2] * wr[0] - delta[0] * wr[2];
+  tmp1[2] = delta[0] * wr[1] - delta[1] * wr[0];
+  for (int d = 0; d < 3; d++) vtr[d] = vt[d] + tmp1[d];
+  for (int d = 0; d < 3; d++) wr[d] = omegai[d] - omegaj[d];
+  project3(wr, en, wn);
+  for (int d = 0; d < 3; d++) wt[d] = wr[d] - wn[d];
+
+  /* normal force, :582-636 */
+  double nforce[3] = {0., 0., 0.}, dtforce[3] = {0., 0., 0.};
+  double nfd[3] = {0., 0., 0.}, tfd[3] = {0., 0., 0.}, ntd[3] = {0., 0., 0.}, ttd[3] = {0., 0., 0.};
+  const double displacement = (h[1] - r);
+  double dmax, dmin;
+  if (displacement > h[14]) { h[14] = displacement; dmax = displacement; }
+  else dmax = h[14];
+  if (displacement < h[27]) { h[27] = displacement; dmin = displacement; }
+  else dmin = h[27];
+  if (displacement < 0.0) h[14] = 0.0;
+  if (displacement > 0.0) h[27] = 0.0;
+  const double minvel = 1e-5 * (radi < radj ? radi : radj) / dt;
+  if (bs->tensionStress || bs->compressionStress) {
+    if ((bs->tensionStress && displacement < -1.e-15) ||
+        (bs->compressionStress && displacement > 1.e-15)) {
+      const double dc1 = pow((ku_fn1 - k_fn1) / (ku_fn1 + kc_fn1), 2.0) * dmax;
+      const double dc2 = pow((ku_fn2 - k_fn2) / (ku_fn2 + kc_fn2), 1.0) * dmin;
+      double frcmag;
+      if (displacement < dmin) frcmag = k_fn2 * A * displacement;
+      else if (displacement < dc2) frcmag = ku_fn2 * A * displacement + (k_fn2 - ku_fn2) * A * dmin;
+      else if (displacement < 0.0) frcmag = -kc_fn2 * A * displacement;
+      else if (displacement < dc1) frcmag = -kc_fn1 * pow(fabs(displacement), 0.5);
+      else if (displacement < dmax)
+        frcmag = ku_fn1 * pow(fabs(displacement), 0.5) + (k_fn1 - ku_fn1) * pow(fabs(dmax), 0.5);
+      else frcmag = k_fn1 * pow(fabs(displacement), 0.5);
+      for (int d = 0; d < 3; d++) nforce[d] = frcmag * en[d];
+      if (bs->dampingBond) {
+        const double dfn = BT(s, ORC_BOND_DAMP_FN, it, jt);
+        for (int d = 0; d < 3; d++) {
+          const double dv = 0.01 * nforce[d] * dt;
+          const double mult = bs->dampingBondSmooth ? fmin(1.0, fmax(-1.0, vn[d] / fmax(minvel, dv)))
+                                                    : (double)sgn_d(vn[d]);
+          nfd[d] = nforce[d] - dfn * fabs(nforce[d]) * mult;
+        }
+      } else {
+        for (int d = 0; d < 3; d++) nfd[d] = nforce[d];
+      }
+    }
+  }
+  /* shear force, :639-664 */
+  if (bs->shearStress) {
+    const double sc = -k_ft * A * dt;
+    for (int d = 0; d < 3; d++) dtforce[d] = sc * vtr[d];
+    project3(force_tang, en, tmp1);
+    for (int d = 0; d < 3; d++) force_tang[d] = force_tang[d] - tmp1[d];
+    for (int d = 0; d < 3; d++) force_tang[d] = force_tang[d] + dtforce[d];
+    if (bs->dampingBond) {
+      const double dft = BT(s, ORC_BOND_DAMP_FT, it, jt);
+      for (int d = 0; d < 3; d++) {
+        const double dv = 0.01 * force_tang[d] * dt;
+        const double mult = bs->dampingBondSmooth ? fmin(1.0, fmax(-1.0, vtr[d] / fmax(minvel, dv)))
+                                                  : (double)sgn_d(vtr[d]);
+        tfd[d] = force_tang[d] - dft * fabs(force_tang[d]) * mult;
+      }
+    } else {
+      for (int d = 0; d < 3; d++) tfd[d] = force_tang[d];
+    }
+  }
+  /* twisting torque, :666-771 (the projected elastic torque formed first at
+   * :673-674 is overwritten component-wise below and is not restated) */
+  double torque_normal[3] = {0., 0., 0.}, torque_tang[3] = {0., 0., 0.};
+  if (bs->normalTorqueStress) {
+    for (int d = 0; d < 3; d++) theta_normal[d] = theta_normal[d] + dt * wn[d];
+    for (int d = 0; d < 3; d++)
+      torque_normal[d] = bond_hyst(theta_normal[d], &h[15 + d], &h[21 + d], k_tn, ku_tn, kc_tn, J);
+    if (bs->dampingBond) {
+      const double dtn = BT(s, ORC_BOND_DAMP_TN, it, jt);
+      for (int d = 0; d < 3; d++)
+        ntd[d] = torque_normal[d] - dtn * fabs(torque_normal[d]) * (double)sgn_d(wn[d]);
+    } else {
+      for (int d = 0; d < 3; d++) ntd[d] = torque_normal[d];
+    }
+  }
+  /* bending torque, :774-873 */
+  if (bs->shearTorqueStress) {
+    for (int d = 0; d < 3; d++) theta_tang[d] = theta_tang[d] + dt * wt[d];
+    for (int d = 0; d < 3; d++)
+      torque_tang[d] = bond_hyst(theta_tang[d], &h[18 + d], &h[24 + d], k_tt, ku_tt, kc_tt, I);
+    if (bs->dampingBond) {
+      const double dtt = BT(s, ORC_BOND_DAMP_TT, it, jt);
+      for (int d = 0; d < 3; d++)
+        ttd[d] = torque_tang[d] - dtt * fabs(torque_tang[d]) * (double)sgn_d(wt[d]);
+    } else {
+      for (int d = 0; d < 3; d++) ttd[d] = torque_tang[d];
+    }
+  }
+  /* stress breakage on undamped values, :876-891 */
+  if (bs->stressBreak) {
+    const double nfm = sqrt(nforce[0] * nforce[0] + nforce[1] * nforce[1] + nforce[2] * nforce[2]);
+    const double tfm = sqrt(force_tang[0] * force_tang[0] + force_tang[1] * force_tang[1] +
+                            force_tang[2] * force_tang[2]);
+    const double ntm = sqrt(torque_normal[0] * torque_normal[0] + torque_normal[1] * torque_normal[1] +
+                            torque_normal[2] * torque_normal[2]);
+    const double ttm = sqrt(torque_tang[0] * torque_tang[0] + torque_tang[1] * torque_tang[1] +
+                            torque_tang[2] * torque_tang[2]);
+    const double maxSigma = BT(s, ORC_BOND_MAX_SIGMA, it, jt) *
+                            ((bs->ratioTCBond && displacement < -1.e-15) ? BT(s, ORC_BOND_RATIO_TC, it, jt) : 1.0);
+    const int nstress = maxSigma < (nfm / A + ttm * rb / I);
+    const double maxTau = BT(s, ORC_BOND_MAX_TAU, it, jt);
+    const int tstress = maxTau < (tfm / A + ntm * rb / J);
+    if ((nstress || tstress) && update_history) {
+      bond_break(sd);
+      return;
+    }
+  }
+  double tor[3];
+  tor[0] = tfd[1] * en[2] - tfd[2] * en[1];
+  tor[1] = tfd[2] * en[0] - tfd[0] * en[2];
+  tor[2] = tfd[0] * en[1] - tfd[1] * en[0];
+  sd->has_force_update = 1;
+  if (update_history) {
+    for (int d = 0; d < 3; d++) {
+      h[5 + d] = force_tang[d];
+      h[8 + d] = theta_normal[d];
+      h[11 + d] = theta_tang[d];
+    }
+  }
+  for (int d = 0; d < 3; d++) {
+    const double F = nfd[d] + tfd[d];
+    fi->dF[d] = F;
+    fi->dT[d] = cri * tor[d] + ntd[d] + ttd[d];
+    fj->dF[d] = -F;
+    fj->dT[d] = crj * tor[d] - ntd[d] - ttd[d];
+  }
+}
+
+/* the cohesion bond/nonlinear cutoff: neighbor->register_contact_dist_factor
+ * from connectToProperties, :330-380 (minimum radius over the atoms) */
+static int bond_contact_distance_factor(orc_sys *s) {
+  if (!s->bond_on) return 0;
+  if (!s->bond) { snprintf(s->err, sizeof s->err, "bond parameters not set"); return -1; }
+  double minrad = 1e99;
+  for (int i = 0; i < s->n; i++) minrad = fmin(minrad, s->radius[i]);
+  double cdf_all = 1.;
+  const int nt = s->ntypes;
+  for (int i = 1; i < nt + 1; i++)
+    for (int j = 1; j < nt + 1; j++) {
+      double cdf_one;
+      if (!s->bset.stressBreak) {
+        cdf_one = 1.1 * 0.5 * BT(s, ORC_BOND_MAX_DIST, i, j) / minrad;
+      } else {
+        double stress = BT(s, ORC_BOND_MAX_SIGMA, i, j);
+        if (s->bset.ratioTCBond) stress = fmax(stress, stress * BT(s, ORC_BOND_RATIO_TC, i, j));
+        if (BT(s, ORC_BOND_K_FN2, i, j) <= 1e-15) {
+          snprintf(s->err, sizeof s->err, "stress breakage needs stiffnessPerUnitAreaK_fn2 > 0");
+          return -1;
+        }
+        cdf_one = 0.5 * 1.1 * BT(s, ORC_BOND_CREATE_DIST, i, j) / minrad +
+                  0.5 * 1.1 * stress / (BT(s, ORC_BOND_K_FN2, i, j) * minrad);
+      }
+      cdf_all = cdf_one > cdf_all ? cdf_one : cdf_all;
+    }
+  if (cdf_all > 10.) { snprintf(s->err, sizeof s->err, "bond distance above 10 diameters"); return -1; }
+  if (cdf_all > s->cfg.contact_distance_factor) s->cfg.contact_distance_factor = cdf_all;
+  return 0;
+}
+
 static void surfaces_intersect(const orc_sys *s, sidata_t *sd, fdata *fi, fdata *fj, int rolling) {
   surface_default(sd);
   if (s->cfg.normal_model == ORC_NORMAL_HOOKE) normal_hooke(s, sd, fi, fj);
   else normal_hertz(s, sd, fi, fj);
+  if (sd->bondhist) bond_nonlinear(s, sd, fi, fj);
   tangential_history(s, sd, fi, fj);
   if (rolling == ORC_ROLLING_CDT) rolling_cdt(s, sd, fi, fj);
 }
@@ -843,7 +1186,9 @@ static void pair_compute(orc_sys *s, int shearupdate) {
       sd.radi = radi; sd.radj = radj; sd.radsum = radsum; sd.rsq = rsq;
       sd.delta[0] = delx; sd.delta[1] = dely; sd.delta[2] = delz;
       sd.contact_flags = &s->nflag[p];
-      sd.shear = &s->nhist[(size_t)p * s->dnum];
+      sd.shear = &s->nhist[(size_t)p * s->dnum + s->shear_off];
+      sd.bondhist = s->bond_on ? &s->nhist[(size_t)p * s->dnum] : NULL;
+      sd.x_i = &s->x[3 * i];
       sd.v_i = &s->v[3 * i]; sd.v_j = &s->v[3 * j];
       sd.omega_i = &s->omega[3 * i]; sd.omega_j = &s->omega[3 * j];
       sd.itype = s->type[i]; sd.jtype = s->type[j];
@@ -860,7 +1205,10 @@ static void pair_compute(orc_sys *s, int shearupdate) {
         surfaces_intersect(s, &sd, &fi, &fj, s->cfg.rolling_model);
         has_force = 1;
       } else if (rsq < cdm * radsum * radsum) {
+        /* ContactModel::surfacesClose: normal (no-op), cohesion, tangential */
+        if (sd.bondhist) bond_nonlinear(s, &sd, &fi, &fj);
         surfaces_close(&sd);
+        has_force = sd.has_force_update;
       }
       if (has_force) {
         for (int d = 0; d < 3; d++) {
@@ -1230,6 +1578,7 @@ static void compute_forces(orc_sys *s, int shearupdate) {
 
 int orc_setup(orc_sys *s) {
   if (!s->Yeff) { snprintf(s->err, sizeof s->err, "pair parameters not set"); return -1; }
+  if (bond_contact_distance_factor(s)) return -1;
   if (rebuild(s)) return -1;
   compute_forces(s, 0);
   return 0;

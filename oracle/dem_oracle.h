@@ -52,6 +52,31 @@ int orc_set_pair_params(orc_sys *s, int ntypes, const double *Yeff, const double
                         const double *coeffRollFrict, const double *coeffRestLog,
                         double charVel);
 
+/* cohesion bond/nonlinear (src/cohesion_model_bond_nonlinear.h): the 23
+ * per-type-pair property/global tables, each (ntypes+1)^2, stacked in this
+ * order into one array; unused tables (e.g. maxSigma without stressBreak)
+ * may hold zeros. */
+enum {
+  ORC_BOND_RADIUS_MULTIPLIER, ORC_BOND_K_FN1, ORC_BOND_KU_FN1, ORC_BOND_KC_FN1, ORC_BOND_K_FN2,
+  ORC_BOND_KU_FN2, ORC_BOND_KC_FN2, ORC_BOND_K_FT, ORC_BOND_K_TN, ORC_BOND_KU_TN, ORC_BOND_KC_TN,
+  ORC_BOND_K_TT, ORC_BOND_KU_TT, ORC_BOND_KC_TT, ORC_BOND_DAMP_FN, ORC_BOND_DAMP_FT,
+  ORC_BOND_DAMP_TN, ORC_BOND_DAMP_TT, ORC_BOND_MAX_DIST, ORC_BOND_MAX_SIGMA, ORC_BOND_MAX_TAU,
+  ORC_BOND_RATIO_TC, ORC_BOND_CREATE_DIST, ORC_BOND_NTABLES
+};
+/* The model's on/off settings (registerSettings, :231-243) and the scalar
+ * tsCreateBondnonlinear. */
+typedef struct orc_bond_settings {
+  double tsCreate;
+  int stressBreak, tensionStress, compressionStress, shearStress, normalTorqueStress,
+      shearTorqueStress, createBondAlways, dampingBond, dampingBondSmooth, ratioTCBond;
+} orc_bond_settings;
+/* After orc_set_pair_params; cfg.cohesion_model must be ORC_COHESION_BOND_NONLINEAR.
+ * The granular list then carries dnum = 31 history doubles per pair in the
+ * reference's order: 28 bond values (bondFlag, initial_dist, contactPos[3],
+ * ft[3], thetan[3], thetat[3], deltan_max, thetan_max[3], thetat_max[3],
+ * thetan_min[3], thetat_min[3], deltan_min), then shear[3]. */
+int orc_set_bond_params(orc_sys *s, const double *tables, const orc_bond_settings *st);
+
 /* fix wall/gran ... primitive type WTYPE {x,y,z}plane POS (axis 0/1/2). */
 int orc_add_plane(orc_sys *s, int axis, double pos, int wall_type, int rolling_model);
 

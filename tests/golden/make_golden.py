@@ -54,6 +54,19 @@ def cases():
         fill_height=12e-3, rollfrict=((0.3,),), rolling_model=1, density=1500.0, E=(1e7,),
         nu=(0.3,), rest=((0.5,),), frict=((0.6,),), clearance=-0.6e-3),
         400, [0, 1, 10, 100, 200, 400])
+    # fibres of bonded spheres (cohesion bond/nonlinear), floor of wall type 2
+    for name, seed, stress in (("fibre_bond", 41, 0), ("fibre_bond_stress", 43, 1)):
+        r = 0.5e-3
+        bp = workloads.bond_params(
+            2, [1], tsCreate=1.0, radiusMultiplier=0.5, K_fn1=200.0, Ku_fn1=400.0, Kc_fn1=100.0,
+            K_fn2=1e12, Ku_fn2=2e12, Kc_fn2=5e11, K_ft=5e11, K_tn=5e11, Ku_tn=1e12, Kc_tn=2.5e11,
+            K_tt=5e11, Ku_tt=1e12, Kc_tt=2.5e11, damp_fn=0.05, damp_ft=0.05, damp_tn=0.05,
+            damp_tt=0.05, maxDistance=2 * r * 1.0035, maxSigma=6e6, maxTau=6e6, ratioTC=0.5,
+            createDistance=2 * r * 1.002, stressBreak=stress, dampingBondSmooth=stress,
+            ratioTCBond=stress)
+        c[name] = (workloads.fibre_case(seed, nfib=60, nper=5, radius=r, box=(8e-3, 8e-3, 10e-3),
+                                        gap=1.01, vmax=3.0, wmax=4000.0, bond=bp),
+                   300, [0, 1, 2, 3, 10, 50, 100, 200, 300])
     return c
 
 
@@ -84,6 +97,12 @@ def write_inputs(case, d, nsteps, snaps):
     model = "model %s tangential history" % ("hooke" if case["normal_model"] == 1 else "hertz")
     if case["rolling_model"] == 1:
         model += " rolling_friction cdt"
+    bond = case.get("bond") if case.get("cohesion_model", 0) == 1 else None
+    if bond is not None:
+        model += " cohesion bond/nonlinear"
+        for f in workloads.BOND_FLAGS:
+            if bond["settings"][f] != workloads.BOND_DEFAULTS[f]:
+                model += " %s %s" % (workloads.BOND_KEYWORDS[f], "on" if bond["settings"][f] else "off")
     tpl = lambda m: " ".join(fmt(m[i][j]) for i in range(nt) for j in range(nt))  # noqa: E731
     s = ["atom_style granular", "atom_modify map array sort 0 0", "boundary %s" % bnd,
          "newton off", "communicate single vel yes", "units si",
@@ -97,6 +116,12 @@ def write_inputs(case, d, nsteps, snaps):
                  % (nt, tpl(mat["rollfrict"])))
     if case["normal_model"] == 1:
         s.append("fix m6 all property/global characteristicVelocity scalar %s" % fmt(case["charVel"]))
+    if bond is not None:
+        for k, name in enumerate(workloads.BOND_TABLES):
+            s.append("fix b%d all property/global %s peratomtypepair %d %s"
+                     % (k, name, nt, tpl(bond["tables"][k][1:, 1:])))
+        s.append("fix bts all property/global tsCreateBondnonlinear scalar %s"
+                 % fmt(bond["settings"]["tsCreate"]))
     s += ["pair_style gran %s" % model, "pair_coeff * *", "timestep %s" % fmt(case["dt"])]
     g = case["gravity"]
     s.append("fix gravi all gravity 9.81 vector 0.0 0.0 -1.0")
@@ -220,7 +245,11 @@ def run_case(name, case, nsteps, snaps):
                 if k != "step":
                     out["s%d_%s" % (st, k)] = v
         loop = [l for l in open(os.path.join(d, "log.case")) if l.startswith("Loop time")]
-    meta = {k: v for k, v in case.items() if k not in ("atoms", "meshes") and not isinstance(v, np.ndarray)}
+    meta = {k: v for k, v in case.items()
+            if k not in ("atoms", "meshes", "bond") and not isinstance(v, np.ndarray)}
+    if "bond" in case:
+        meta["bond_settings"] = case["bond"]["settings"]
+        out["bond_tables"] = case["bond"]["tables"]
     meta.update(nsteps=nsteps, snaps=snaps, loop=loop)
     meta["meshes"] = [dict(wall_type=m["wall_type"], rolling=m.get("rolling", 0))
                       for m in case.get("meshes", [])]

@@ -37,6 +37,8 @@ def load_golden(name):
         case[k] = z[k]
     case["atoms"] = dict(tag=z["init_tag"], type=z["init_type"], x=z["init_x"], v=z["init_v"],
                          omega=z["init_omega"], radius=z["init_radius"], rmass=z["init_rmass"])
+    if "bond_settings" in meta:
+        case["bond"] = dict(tables=z["bond_tables"], settings=meta["bond_settings"])
     snaps = {}
     for st in meta["snaps"]:
         pre = "s%d_" % st
@@ -45,6 +47,19 @@ def load_golden(name):
 
 
 DIVERGED_RTOL = 1e-7    # forces after >10 steps of independently rounded trajectories
+
+
+def newton_sign(dnum):
+    """Sign of each history value in the partner's copy (newtonflag of
+    add_history_value): shear[3] of tangential history flips; of the 28
+    values of cohesion bond/nonlinear that precede it, ft[3], thetan[3] and
+    thetat[3] (indices 5..13) flip, the rest keep their sign."""
+    if dnum == 3:
+        return -np.ones(3)
+    sgn = np.ones(dnum)
+    sgn[5:14] = -1.0
+    sgn[28:31] = -1.0
+    return sgn
 
 
 def restart_from_snapshot(case, snap):
@@ -66,9 +81,10 @@ def restart_from_snapshot(case, snap):
         ti, tj, h = int(snap["pair_tag_i"][p]), int(snap["pair_tag_j"][p]), snap["pair_hist"][p]
         to.append(ti); tp.append(tj); hs.append(h)
         if not np.any(snap["pair_shift"][p]):
-            to.append(tj); tp.append(ti); hs.append(-h)
+            to.append(tj); tp.append(ti); hs.append(newton_sign(len(h)) * h)
     walls = [snap[k] for k in sorted(k for k in snap if k.startswith("wall") and k.endswith("_hist"))]
-    return ck, np.array(to, np.int32), np.array(tp, np.int32), np.array(hs).reshape(-1, 3), walls
+    dnum = snap["pair_hist"].shape[1]
+    return ck, np.array(to, np.int32), np.array(tp, np.int32), np.array(hs).reshape(-1, dnum), walls
 
 
 def canonical_pairs(tag_i, tag_j, shift, flag, hist):
@@ -79,7 +95,7 @@ def canonical_pairs(tag_i, tag_j, shift, flag, hist):
         sh = tuple(int(t) for t in shift[p])
         h = np.asarray(hist[p], dtype=np.float64)
         if sh == (0, 0, 0) and ti > tj:
-            ti, tj, h = tj, ti, -h
+            ti, tj, h = tj, ti, newton_sign(len(h)) * h
         key = (ti, tj, sh)
         assert key not in out, "duplicate pair %r" % (key,)
         out[key] = (int(flag[p]), h)
@@ -108,9 +124,13 @@ def compare_pairs(got, ref, hist_rtol=HIST_RTOL):
     extra = ks_g - ks_r
     common = ks_g & ks_r
     flagmis = [k for k in common if (got[k][0] != 0) != (ref[k][0] != 0)]
-    hs = max([np.max(np.abs(ref[k][1])) for k in common] + [0.0])
-    hm = 0.0
-    for k in common:
-        d = np.max(np.abs(got[k][1] - ref[k][1]))
-        hm = max(hm, d / hs if hs > 0 else d)
-    return missing, extra, flagmis, hm
+    if not common:
+        return missing, extra, flagmis, 0.0
+    # each history value (column) relative to its own largest magnitude
+    ks = sorted(common)
+    G = np.array([got[k][1] for k in ks])
+    R = np.array([ref[k][1] for k in ks])
+    scale = np.max(np.abs(R), axis=0)
+    d = np.max(np.abs(G - R), axis=0)
+    rel = np.where(scale > 0, d / np.where(scale > 0, scale, 1.0), d)
+    return missing, extra, flagmis, float(np.max(rel))

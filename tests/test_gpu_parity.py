@@ -21,7 +21,7 @@ from golden_io import (DIVERGED_RTOL, FORCE_RTOL, HIST_RTOL, TRAJ_RTOL, canonica
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["dense_hertz", "poly_cdt", "hooke"]
+CASES = ["dense_hertz", "poly_cdt", "hooke", "fibre_bond", "fibre_bond_stress"]
 
 
 def _gpu(case):
@@ -162,6 +162,52 @@ def test_gpu_matches_oracle_6912_atoms(rolling):
         missing, extra, flagmis, hm = compare_pairs(_pairs(g), op)
         assert not missing and not extra and not flagmis
         assert hm < (HIST_RTOL if done <= 10 else 1e-6)
+    assert g.nrebuilds == o.nrebuilds
+
+
+def _fibre_case(seed, stress):
+    from gb300dem import workloads
+    r = 0.5e-3
+    bp = workloads.bond_params(
+        2, [1], tsCreate=1.0, radiusMultiplier=0.5, K_fn1=200.0, Ku_fn1=400.0, Kc_fn1=100.0,
+        K_fn2=1e12, Ku_fn2=2e12, Kc_fn2=5e11, K_ft=5e11, K_tn=5e11, Ku_tn=1e12, Kc_tn=2.5e11,
+        K_tt=5e11, Ku_tt=1e12, Kc_tt=2.5e11, damp_fn=0.05, damp_ft=0.05, damp_tn=0.05,
+        damp_tt=0.05, maxDistance=2 * r * 1.0035, maxSigma=6e6, maxTau=6e6, ratioTC=0.5,
+        createDistance=2 * r * 1.002, stressBreak=stress, dampingBondSmooth=stress,
+        ratioTCBond=stress)
+    return workloads.fibre_case(seed, nfib=400, nper=6, radius=r, box=(20e-3, 20e-3, 16e-3),
+                                gap=1.01, vmax=3.0, wmax=4000.0, bond=bp, skin=1e-4, max_fail=2000)
+
+
+@pytest.mark.parametrize("stress", [0, 1])
+def test_gpu_bonded_fibres_match_oracle(stress):
+    """cohesion bond/nonlinear on ~1800 atoms: bond topology (bondFlag, the
+    cohesion contact bit) bit-exact, all 31 history values, forces."""
+    from oracle.binding import Oracle
+    case = _fibre_case(57 + stress, stress)
+    g = _gpu(case)
+    o = Oracle(case)
+    g.setup()
+    o.setup()
+    done = 0
+    for chunk in (1, 1, 8, 90, 100):
+        g.step(chunk)
+        o.run(chunk)
+        done += chunk
+        a, b = sort_by_tag(g.atoms()), sort_by_tag(o.atoms())
+        ftol = FORCE_RTOL if done <= 10 else DIVERGED_RTOL
+        assert max_rel(a["f"], b["f"]) < ftol, (done, max_rel(a["f"], b["f"]))
+        assert max_rel(a["torque"], b["torque"]) < ftol, (done, max_rel(a["torque"], b["torque"]))
+        assert max_rel(a["x"], b["x"], scale=_box(case)) < TRAJ_RTOL
+        po = o.pairs()
+        op = canonical_pairs(po["tag_i"], po["tag_j"], po["shift"], po["flag"], po["hist"])
+        gp = _pairs(g)
+        missing, extra, flagmis, hm = compare_pairs(gp, op)
+        assert not missing and not extra and not flagmis, (done, len(missing), len(extra))
+        assert all(gp[k][0] == op[k][0] for k in op), "contact flag bits differ"
+        nb = sum(1 for k in op if op[k][1][0] > 0.5)
+        assert nb > 300 and sum(1 for k in gp if gp[k][1][0] > 0.5) == nb
+        assert hm < (HIST_RTOL if done <= 10 else 1e-6), (done, hm)
     assert g.nrebuilds == o.nrebuilds
 
 

@@ -11,7 +11,7 @@ from golden_io import (FORCE_RTOL, HIST_RTOL, canonical_pairs, compare_pairs, lo
                        max_rel, sort_by_tag)
 from oracle.binding import Oracle
 
-CASES = ["dense_hertz", "poly_cdt", "hooke"]
+CASES = ["dense_hertz", "poly_cdt", "hooke", "fibre_bond", "fibre_bond_stress"]
 
 
 @pytest.mark.parametrize("name", CASES)
