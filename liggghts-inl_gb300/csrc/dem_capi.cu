@@ -139,6 +139,7 @@ static int alloc_atoms(dem_handle *h, int nmax) {
     for (double **pp : d) CUDA_TRY(h, dalloc(L, pp, nmax));
     CUDA_TRY(h, dalloc(L, &A.type, nmax));
     CUDA_TRY(h, dalloc(L, &A.tag, nmax));
+    CUDA_TRY(h, dalloc(L, &A.lidx, nmax));
     CUDA_TRY(h, dalloc(L, &A.whist, (size_t)3 * kMaxPlanes * nmax));
     CUDA_TRY(h, dalloc(L, &A.wbits, nmax));
   }
@@ -660,6 +661,11 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
   CUDA_TRY(h, cudaMemcpy(A.m, rmass, n * sizeof(double), cudaMemcpyHostToDevice));
   CUDA_TRY(h, cudaMemcpy(A.type, type, n * sizeof(int), cudaMemcpyHostToDevice));
   CUDA_TRY(h, cudaMemcpy(A.tag, tag, n * sizeof(int), cudaMemcpyHostToDevice));
+  {  // the upload order is the caller's local order
+    std::vector<int> li(n);
+    for (int i = 0; i < n; i++) li[i] = i;
+    CUDA_TRY(h, cudaMemcpy(A.lidx, li.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  }
   for (int i = 0; i < n; i++) buf[i] = dtf / (rmass[i] * (1. + 0.0));
   CUDA_TRY(h, cudaMemcpy(A.dtfm, buf.data(), n * sizeof(double), cudaMemcpyHostToDevice));
   for (int i = 0; i < n; i++) buf[i] = dtfrotate / (radius[i] * radius[i] * rmass[i]);
@@ -893,7 +899,7 @@ int dem_download_contacts(dem_handle *h, int *tag_i, int *tag_j, int *shift, int
   if (rc) return rc;
   const int n = h->host_ctrl.n, np = h->host_ctrl.np;
   const PairArrays &L = h->s.pairs[0];
-  std::vector<int> pi(np), pj(np), tags(n), fl(np);
+  std::vector<int> pi(np), pj(np), tags(n), fl(np), li(n);
   std::vector<uint8_t> sh(np);
   if (np) {
     CUDA_TRY(h, cudaMemcpy(pi.data(), L.i, np * sizeof(int), cudaMemcpyDeviceToHost));
@@ -902,6 +908,18 @@ int dem_download_contacts(dem_handle *h, int *tag_i, int *tag_j, int *shift, int
     CUDA_TRY(h, cudaMemcpy(fl.data(), L.flag, np * sizeof(int), cudaMemcpyDeviceToHost));
   }
   CUDA_TRY(h, cudaMemcpy(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost));
+  CUDA_TRY(h, cudaMemcpy(li.data(), h->s.atoms[0].lidx, n * sizeof(int), cudaMemcpyDeviceToHost));
+  // pairs of two owned atoms are returned as the reference holds them: owned
+  // by the atom that comes first in the caller's local order (shear negated
+  // when the list holds the other orientation; bond values are kept in that
+  // orientation already)
+  std::vector<char> swap(np, 0);
+  for (int p = 0; p < np; p++) {
+    if (sh[p] == kNoShift && li[pi[p]] > li[pj[p]]) {
+      swap[p] = 1;
+      std::swap(pi[p], pj[p]);
+    }
+  }
   for (int p = 0; p < np; p++) {
     if (tag_i) tag_i[p] = tags[pi[p]];
     if (tag_j) tag_j[p] = tags[pj[p]];
@@ -920,7 +938,7 @@ int dem_download_contacts(dem_handle *h, int *tag_i, int *tag_j, int *shift, int
       const int d = dev_hist_index(h->s, r);
       CUDA_TRY(h, cudaMemcpy(hb.data(), L.hist + (size_t)d * h->s.pcap, np * sizeof(double),
                              cudaMemcpyDeviceToHost));
-      for (int p = 0; p < np; p++) hist[(size_t)p * dnum + r] = hb[p];
+      for (int p = 0; p < np; p++) hist[(size_t)p * dnum + r] = (swap[p] && d < kDnumShear) ? -hb[p] : hb[p];
     }
   }
   return DEM_OK;

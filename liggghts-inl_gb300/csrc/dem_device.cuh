@@ -45,10 +45,12 @@ enum {
   kBondNormalTorque = 1 << 4, kBondShearTorque = 1 << 5, kBondCreateAlways = 1 << 6,
   kBondDamping = 1 << 7, kBondDampingSmooth = 1 << 8, kBondUseRatioTC = 1 << 9
 };
-// newtonflag of device history value d (sign flips in the partner's copy)
-__host__ __device__ __forceinline__ bool hist_newton(int d) {
-  return d < kDnumShear || (d >= kDnumShear + 5 && d <= kDnumShear + 13);
-}
+// The shear history is kept in the list's own orientation (owner = lower
+// cell-sorted index; it changes sign when that orientation flips).  The bond
+// values are kept in the reference's orientation, owner = lower lidx (the
+// reference's local index order), because its twisting/bending extremes and
+// smooth damping are not symmetric under a flip; the bond law is evaluated
+// in that orientation.
 
 // status words in Ctrl::status
 constexpr int kStatOk = 0;
@@ -64,6 +66,7 @@ struct AtomArrays {
   double *r, *m, *dtfm, *dtir;
   double *xh, *yh, *zh;     // xhold
   int *type, *tag;
+  int *lidx;                // the atom's index in the caller's (reference's) local order
   double *whist;            // [(w*3+d)*nmax + i]
   uint8_t *wbits;           // bit w: atom in primitive wall w's neighbour list
 };

@@ -259,7 +259,7 @@ __global__ void k_permute(Sys s) {
     B.tx[i] = A.tx[o]; B.ty[i] = A.ty[o]; B.tz[i] = A.tz[o];
     const double r = A.r[o];
     B.r[i] = r; B.m[i] = A.m[o]; B.dtfm[i] = A.dtfm[o]; B.dtir[i] = A.dtir[o];
-    B.type[i] = A.type[o]; B.tag[i] = A.tag[o];
+    B.type[i] = A.type[o]; B.tag[i] = A.tag[o]; B.lidx[i] = A.lidx[o];
     uint8_t bits = 0;
     for (int w = 0; w < s.nplanes; w++) {
       for (int d = 0; d < 3; d++)
@@ -299,7 +299,7 @@ __global__ void k_copy_atoms(Sys s) {
     A.fx[i] = B.fx[i]; A.fy[i] = B.fy[i]; A.fz[i] = B.fz[i];
     A.tx[i] = B.tx[i]; A.ty[i] = B.ty[i]; A.tz[i] = B.tz[i];
     A.r[i] = B.r[i]; A.m[i] = B.m[i]; A.dtfm[i] = B.dtfm[i]; A.dtir[i] = B.dtir[i];
-    A.type[i] = B.type[i]; A.tag[i] = B.tag[i];
+    A.type[i] = B.type[i]; A.tag[i] = B.tag[i]; A.lidx[i] = B.lidx[i];
     for (int w = 0; w < s.nplanes; w++)
       for (int d = 0; d < 3; d++)
         A.whist[(size_t)(w * 3 + d) * s.nmax + i] = B.whist[(size_t)(w * 3 + d) * s.nmax + i];
@@ -459,6 +459,24 @@ __global__ void k_mesh_cand(Sys s, int k) {
   }
 }
 
+// Entry of the old list for the atom pair (owner o, partner q) in old
+// indices: o's own row first, then the entries where o was the partner
+// (flip = true).  Only flagged entries carry history (pre_exchange keeps
+// those).  Returns -1 when none.
+__device__ __forceinline__ int find_old(const PairArrays &L, int o, int q, bool &flip) {
+  flip = false;
+  for (int k = L.row[o]; k < L.row[o + 1]; k++)
+    if (L.j[k] == q && L.flag[k] != 0) return k;
+  for (int k = L.rev_start[o]; k < L.rev_start[o + 1]; k++) {
+    const int e = L.rev[k];
+    if (L.i[e] == q && L.flag[e] != 0) {
+      flip = true;
+      return e;
+    }
+  }
+  return -1;
+}
+
 // ----------------------------------------------------------------------------
 // rebuild: granular half list (Neighbor::granular_bin_no_newton,
 // src/neigh_gran.cpp:485-644), 27-cell stencil with periodic images.
@@ -529,27 +547,19 @@ __global__ void k_pairs(Sys s) {
             if (out >= out_end) continue;  // count and fill passes agree; guard only
             // history carry-over: partner lookup by identity in the old list
             // (FixContactHistory::pre_exchange + the partner search of
-            // src/neigh_gran.cpp:590-620); in the j-side copy the values
-            // registered with newtonflag 1 change sign.
-            int src = -1;
+            // src/neigh_gran.cpp:590-620).  The shear comes from the entry
+            // owned by i (negated when the old entry was owned by j); the
+            // bond values come from the entry of the reference's owner and
+            // are copied as they are.
+            int src = -1, bsrc = -1;
             bool flip = false;
             if (rsq < __dmul_rn(radsum, radsum)) {
               const int oi = s.perm[i], oj = s.perm[j];
-              for (int q = L.row[oi]; q < L.row[oi + 1]; q++) {
-                if (L.j[q] == oj && L.flag[q] != 0) {
-                  src = q;
-                  break;
-                }
-              }
-              if (src < 0) {
-                for (int k = L.rev_start[oi]; k < L.rev_start[oi + 1]; k++) {
-                  const int q = L.rev[k];
-                  if (L.i[q] == oj && L.flag[q] != 0) {
-                    src = q;
-                    flip = true;
-                    break;
-                  }
-                }
+              src = find_old(L, oi, oj, flip);
+              bsrc = src;
+              if (s.bond && src >= 0 && code == kNoShift && A.lidx[i] > A.lidx[j]) {
+                bool f2;
+                bsrc = find_old(L, oj, oi, f2);
               }
             }
             const int p = out++;
@@ -557,14 +567,10 @@ __global__ void k_pairs(Sys s) {
             M.j[p] = j;
             M.sh[p] = (uint8_t)code;
             M.flag[p] = src >= 0 ? 1 : 0;
-            for (int d = 0; d < s.dnum; d++) {
-              double hv = 0.0;
-              if (src >= 0) {
-                hv = L.hist[(size_t)d * s.pcap + src];
-                if (flip && hist_newton(d)) hv = -hv;
-              }
-              M.hist[(size_t)d * s.pcap + p] = hv;
-            }
+            for (int d = 0; d < kDnumShear; d++)
+              M.hist[(size_t)d * s.pcap + p] = src >= 0 ? (flip ? -1.0 : 1.0) * L.hist[(size_t)d * s.pcap + src] : 0.0;
+            for (int d = kDnumShear; d < s.dnum; d++)
+              M.hist[(size_t)d * s.pcap + p] = bsrc >= 0 ? L.hist[(size_t)d * s.pcap + bsrc] : 0.0;
             const double mj = A.m[j];
             const double meff = mi * mj / (mi + mj);
             const double reff = radi * radj / (radi + radj);
@@ -764,17 +770,31 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
       ContactOut bo;
       bool bonded = false;
       if (BOND) {
+        // evaluated in the reference's orientation: owner = lower lidx
+        // (periodic entries are directed and always owned by i)
+        const bool rev = L.sh[q] == kNoShift && A.lidx[i] > A.lidx[j];
+        const int a = rev ? j : i, b = rev ? i : j;
+        const double sg = rev ? -1.0 : 1.0;
         BondIn bi;
-        bi.d[0] = ci.d[0]; bi.d[1] = ci.d[1]; bi.d[2] = ci.d[2];
+        bi.d[0] = sg * ci.d[0]; bi.d[1] = sg * ci.d[1]; bi.d[2] = sg * ci.d[2];
         bi.rsq = rsq_q;
-        bi.radi = ci.radi;
-        bi.radj = ci.radj;
-        bi.vi[0] = A.vx[i]; bi.vi[1] = A.vy[i]; bi.vi[2] = A.vz[i];
-        bi.vj[0] = A.vx[j]; bi.vj[1] = A.vy[j]; bi.vj[2] = A.vz[j];
-        for (int k = 0; k < 3; k++) { bi.wi[k] = ci.wi[k]; bi.wj[k] = ci.wj[k]; }
-        bi.xi[0] = A.x[i]; bi.xi[1] = A.y[i]; bi.xi[2] = A.z[i];
-        bi.tp = A.type[i] * (s.ntypes + 1) + A.type[j];
-        bonded = bond_nonlinear(s, bi, L.hist + 3 * P + q, P, L.flag + q, shearupdate != 0, ntimestep, bo);
+        bi.radi = A.r[a];
+        bi.radj = A.r[b];
+        bi.vi[0] = A.vx[a]; bi.vi[1] = A.vy[a]; bi.vi[2] = A.vz[a];
+        bi.vj[0] = A.vx[b]; bi.vj[1] = A.vy[b]; bi.vj[2] = A.vz[b];
+        bi.wi[0] = A.wx[a]; bi.wi[1] = A.wy[a]; bi.wi[2] = A.wz[a];
+        bi.wj[0] = A.wx[b]; bi.wj[1] = A.wy[b]; bi.wj[2] = A.wz[b];
+        bi.xi[0] = A.x[a]; bi.xi[1] = A.y[a]; bi.xi[2] = A.z[a];
+        bi.tp = A.type[a] * (s.ntypes + 1) + A.type[b];
+        ContactOut bc;
+        bonded = bond_nonlinear(s, bi, L.hist + 3 * P + q, P, L.flag + q, shearupdate != 0, ntimestep, bc);
+        if (bonded) {  // back to the list's orientation (i owns the entry)
+          for (int k = 0; k < 3; k++) {
+            bo.F[k] = sg * bc.F[k];
+            bo.Ti[k] = rev ? bc.Tj[k] : bc.Ti[k];
+            bo.Tj[k] = rev ? bc.Ti[k] : bc.Tj[k];
+          }
+        }
       }
       ContactOut o;
       if (touch) {
