@@ -722,8 +722,12 @@ int dem_upload_contact_history(dem_handle *h, int ne, const int *towner, const i
   }
   const PairArrays &L = h->s.pairs[0];
   if (ne) {
+    // each entry is its owner's own partner-list copy: marked as a directed
+    // (image) entry so that the first build takes it as it is
+    std::vector<uint8_t> dsh(ne, 0);
     CUDA_TRY(h, cudaMemcpy(L.i, pi.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemcpy(L.j, pj.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(L.sh, dsh.data(), ne, cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemcpy(L.flag, fl.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemcpy(L.hist, hh.data(), hh.size() * sizeof(double), cudaMemcpyHostToDevice));
   }

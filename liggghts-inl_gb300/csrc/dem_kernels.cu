@@ -545,32 +545,36 @@ __global__ void k_pairs(Sys s) {
               continue;
             }
             if (out >= out_end) continue;  // count and fill passes agree; guard only
-            // history carry-over: partner lookup by identity in the old list
-            // (FixContactHistory::pre_exchange + the partner search of
-            // src/neigh_gran.cpp:590-620).  The shear comes from the entry
-            // owned by i (negated when the old entry was owned by j); the
-            // bond values come from the entry of the reference's owner and
-            // are copied as they are.
-            int src = -1, bsrc = -1;
-            bool flip = false;
+            // history carry-over as the reference does it (pre_exchange
+            // partner lists + the lookup of src/neigh_gran.cpp:590-620): the
+            // new entry's reference owner R (lower lidx of an owned pair,
+            // else i) takes its partner-list entry for the other atom: its
+            // own old entry, or the partner copy of an old owned pair, in
+            // which the values registered with newtonflag 1 change sign.
+            // The shear is then expressed in the list's own orientation.
+            int e = -1;
+            double ssign = 1.0;
+            bool quirk = false;
             if (rsq < __dmul_rn(radsum, radsum)) {
-              const int oi = s.perm[i], oj = s.perm[j];
-              src = find_old(L, oi, oj, flip);
-              bsrc = src;
-              if (s.bond && src >= 0 && code == kNoShift && A.lidx[i] > A.lidx[j]) {
-                bool f2;
-                bsrc = find_old(L, oj, oi, f2);
-              }
+              const bool rj = s.bond && code == kNoShift && A.lidx[i] > A.lidx[j];
+              bool fl;
+              e = rj ? find_old(L, s.perm[j], s.perm[i], fl) : find_old(L, s.perm[i], s.perm[j], fl);
+              ssign = (fl ? -1.0 : 1.0) * (rj ? -1.0 : 1.0);
+              quirk = s.bond && e >= 0 && !rj && code != kNoShift && L.sh[e] == kNoShift &&
+                      A.lidx[i] > A.lidx[j];
             }
             const int p = out++;
             M.i[p] = i;
             M.j[p] = j;
             M.sh[p] = (uint8_t)code;
-            M.flag[p] = src >= 0 ? 1 : 0;
+            M.flag[p] = e >= 0 ? 1 : 0;
             for (int d = 0; d < kDnumShear; d++)
-              M.hist[(size_t)d * s.pcap + p] = src >= 0 ? (flip ? -1.0 : 1.0) * L.hist[(size_t)d * s.pcap + src] : 0.0;
-            for (int d = kDnumShear; d < s.dnum; d++)
-              M.hist[(size_t)d * s.pcap + p] = bsrc >= 0 ? L.hist[(size_t)d * s.pcap + bsrc] : 0.0;
+              M.hist[(size_t)d * s.pcap + p] = e >= 0 ? ssign * L.hist[(size_t)d * s.pcap + e] : 0.0;
+            for (int d = kDnumShear; d < s.dnum; d++) {
+              double hv = e >= 0 ? L.hist[(size_t)d * s.pcap + e] : 0.0;
+              if (quirk && d >= kDnumShear + 5 && d <= kDnumShear + 13) hv = -hv;
+              M.hist[(size_t)d * s.pcap + p] = hv;
+            }
             const double mj = A.m[j];
             const double meff = mi * mj / (mi + mj);
             const double reff = radi * radj / (radi + radj);
