@@ -151,6 +151,16 @@ int dem_add_mesh(dem_handle *h, int ntri, const double *nodes, int wall_type, in
                  const unsigned char *edge_active, const unsigned char *corner_active,
                  int *mesh_id);
 
+/* fix move/mesh mesh ID linear vx vy vz (FixMoveMesh + MeshMoverLinear,
+ * src/fix_move_mesh.cpp:194-240, src/mesh_mover_linear.cpp:95-112): every
+ * step the mesh moves by dt*vel after the particles' drift; node velocities
+ * are vel (0 in the dem_setup force pass); a node that travelled more than
+ * skin/2 since the last neighbour build forces a build at the next step
+ * (FixMesh::pre_force, MultiNodeMesh::decideRebuild).  Before dem_upload_atoms. */
+int dem_set_mesh_motion(dem_handle *h, int mesh_id, const double *vel);
+/* Current node positions of a mesh, ntri*9 in element order. */
+int dem_download_mesh_nodes(dem_handle *h, int mesh_id, double *nodes);
+
 /* Host-only: edge/corner activity of a triangle mesh as SurfaceMesh::buildNeighbours
  * computes it (src/surface_mesh_I.h:473-1236), ntri*3 flags each. */
 int dem_mesh_topology(int ntri, const double *nodes, unsigned char *edge_active,

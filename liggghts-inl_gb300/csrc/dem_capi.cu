@@ -513,6 +513,50 @@ int dem_add_mesh(dem_handle *h, int ntri, const double *nodes, int wall_type, in
   return DEM_OK;
 }
 
+int dem_set_mesh_motion(dem_handle *h, int mesh_id, const double *vel) {
+  if (!h || !vel || mesh_id < 0 || mesh_id >= h->s.nmeshes) return DEM_ERR_BAD_ARG;
+  if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "set mesh motion before uploading atoms");
+  MeshDev &M = h->s.meshes[mesh_id];
+  for (int d = 0; d < 3; d++) {
+    if (!std::isfinite(vel[d])) return fail(h, DEM_ERR_BAD_ARG, "non-finite mesh velocity");
+    M.vel[d] = vel[d];
+    M.dx[d] = h->s.dt * vel[d];  // vectorScalarMult3D(vel_, dt, dx)
+  }
+  if (!M.node_last) {
+    CUDA_TRY(h, dalloc(h->allocs_misc, &M.node_last, (size_t)9 * M.ntri));
+    std::vector<double> nl((size_t)9 * M.ntri);
+    const MeshHost &mh = h->mesh_host[mesh_id];
+    for (int t = 0; t < M.ntri; t++)
+      for (int q = 0; q < 9; q++) nl[(size_t)t * 9 + q] = mh.tri[(size_t)t * kTriStride + q];
+    CUDA_TRY(h, cudaMemcpy(M.node_last, nl.data(), nl.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  M.moving = 1;
+  M.vel_on = 0;
+  h->sys_gen++;
+  return DEM_OK;
+}
+
+int dem_download_mesh_nodes(dem_handle *h, int mesh_id, double *nodes) {
+  if (!h || !nodes || mesh_id < 0 || mesh_id >= h->s.nmeshes) return DEM_ERR_BAD_ARG;
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  const MeshDev &M = h->s.meshes[mesh_id];
+  std::vector<double> g((size_t)kTriStride * M.ntri);
+  CUDA_TRY(h, cudaMemcpy(g.data(), M.tri, g.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  for (int t = 0; t < M.ntri; t++)
+    for (int q = 0; q < 9; q++) nodes[(size_t)t * 9 + q] = g[(size_t)t * kTriStride + q];
+  return DEM_OK;
+}
+
+static void set_mesh_velocity_on(dem_handle *h, int on) {
+  for (int k = 0; k < h->s.nmeshes; k++) {
+    MeshDev &M = h->s.meshes[k];
+    if (M.moving && M.vel_on != on) {
+      M.vel_on = on;
+      h->sys_gen++;  // kernels of an existing graph hold the old value
+    }
+  }
+}
+
 int dem_mesh_ncontacts(dem_handle *h, int mesh_id, int *nc) {
   if (!h || !h->have_atoms || !nc || mesh_id < 0 || mesh_id >= h->s.nmeshes) return DEM_ERR_BAD_ARG;
   int rc = read_ctrl(h);
@@ -752,6 +796,7 @@ int dem_upload_wall_history(dem_handle *h, int wall_id, const double *hist) {
 int dem_setup(dem_handle *h) {
   if (!h || !h->have_atoms) return DEM_ERR_BAD_ARG;
   cudaGetLastError();
+  set_mesh_velocity_on(h, 0);  // FixMoveMesh::setup: node velocities 0
   h->kt.kernel_launches += launch_set_rebuild(h->s, 1, h->st);
   h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);
   bool resumed = true;
@@ -773,6 +818,7 @@ int dem_step(dem_handle *h, int nsteps) {
   if (!h || nsteps < 0) return DEM_ERR_BAD_ARG;
   if (!h->setup_done) return fail(h, DEM_ERR_BAD_ARG, "dem_setup must precede dem_step");
   if (nsteps == 0) return DEM_OK;
+  set_mesh_velocity_on(h, 1);
   int rc = read_ctrl(h);
   if (rc) return rc;
   const long long ts0 = h->host_ctrl.ntimestep;
@@ -786,6 +832,7 @@ int dem_step(dem_handle *h, int nsteps) {
     mark_start(h);
     if (first) {  // step 1 starts from stored forces: initial_integrate only
       h->kt.kernel_launches += launch_particle(h->s, h->lc, kModeInitial, 1, h->st);
+      h->kt.kernel_launches += launch_mesh_move(h->s, h->lc, h->st);
       mark(h, 0);
       h->kt.kernel_launches += launch_decide(h->s, h->st);
       h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);
@@ -810,6 +857,7 @@ int dem_step(dem_handle *h, int nsteps) {
     } else {
       for (long long k = k0; k < chunk; k++) {
         h->kt.kernel_launches += launch_particle(h->s, h->lc, kModeGatherFinalInitial, 1, h->st);
+        h->kt.kernel_launches += launch_mesh_move(h->s, h->lc, h->st);
         mark(h, 0);
         h->kt.kernel_launches += launch_decide(h->s, h->st);
         h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);

@@ -124,8 +124,11 @@ struct MeshDev {
   double distmax, tskin;  // FixNeighlistMesh: bounding-box growth and neighbuild threshold
   double *tri;        // [t*kTriStride]
   int *meta;          // [t]
-  double *nodev;      // node velocities [t*9] (moving mesh) or nullptr
-  double vel[3];      // move/mesh linear velocity
+  // fix move/mesh ... linear: every step nodes and centres move by dx =
+  // dt*vel; node velocities are vel (0 during the setup force pass)
+  double vel[3], dx[3];
+  int vel_on;
+  double *node_last;  // node positions at the last neighbour build [t*9]
   int *cn_start, *cn_list;          // coplanar node-neighbours (areCoplanarNodeNeighs)
   int *tc_count, *tc_start, *tc_fill, *tc_list;  // triangles registered per atom cell
   int tc_cap;

@@ -75,15 +75,30 @@ __device__ __forceinline__ int cell_coord(const Sys &s, double x, int d) {
 // step control
 // ----------------------------------------------------------------------------
 
+// Neighbor::decide (src/neighbor.cpp:1362-1376): a fix that forces a
+// rebuild at this step (FixMesh::next_reneighbor) comes before the
+// ago/every/delay/check logic.  A moving mesh that travelled more than skin/2
+// on a step without rebuild forces one at the next step.
+__device__ __forceinline__ int decide_rebuild(const Sys &s, Ctrl *c) {
+  int reb = 0;
+  if (c->force_rebuild) {
+    reb = 1;
+  } else {
+    c->ago++;
+    if (c->ago >= s.neigh_delay && c->ago % s.neigh_every == 0) reb = s.neigh_check ? c->moved : 1;
+  }
+  c->force_rebuild = reb ? 0 : c->mesh_moved;
+  c->mesh_moved = 0;
+  c->rebuild = reb;
+  c->moved = 0;
+  return reb;
+}
+
 __global__ void k_decide(Sys s) {
   Ctrl *c = s.ctrl;
   if (c->halt) return;
   c->ntimestep++;
-  c->ago++;
-  int reb = 0;
-  if (c->ago >= s.neigh_delay && c->ago % s.neigh_every == 0) reb = s.neigh_check ? c->moved : 1;
-  c->rebuild = reb;
-  c->moved = 0;
+  decide_rebuild(s, c);
 }
 
 // k_decide for the graph-resident step loop: also drives the IF node around
@@ -96,11 +111,7 @@ __global__ void k_decide_loop(Sys s, cudaGraphConditionalHandle hreb, cudaGraphC
     return;
   }
   c->ntimestep++;
-  c->ago++;
-  int reb = 0;
-  if (c->ago >= s.neigh_delay && c->ago % s.neigh_every == 0) reb = s.neigh_check ? c->moved : 1;
-  c->rebuild = reb;
-  c->moved = 0;
+  const int reb = decide_rebuild(s, c);
   c->loop_left--;
   cudaGraphSetConditional(hreb, reb ? 1u : 0u);
   cudaGraphSetConditional(hloop, c->loop_left > 0 ? 1u : 0u);
@@ -334,6 +345,34 @@ __device__ __forceinline__ void mslot_swap(const MeshDev &M, size_t nmax, int i,
   }
 }
 
+// MeshMoverLinear::initial_integrate + MultiNodeMesh::move (nodes and
+// centres += dx, src/multi_node_mesh_I.h:502-520), then
+// MultiNodeMesh::decideRebuild (any node > skin/2 from its position at the
+// last build, src/multi_node_mesh_I.h:792-823); the decision is used by
+// k_decide only on steps that do not rebuild anyway (FixMesh::pre_force).
+__global__ void k_mesh_move(Sys s, int k) {
+  Ctrl *c = s.ctrl;
+  if (c->halt) return;
+  const MeshDev &M = s.meshes[k];
+  const double trigger = __dmul_rn(__dmul_rn(0.25, s.skin), s.skin);
+  bool moved = false;
+  GRID_STRIDE(t, M.ntri) {
+    double *g = M.tri + (size_t)t * kTriStride;
+    for (int q = 0; q < 3; q++) {
+      double dsq = 0.0;
+      for (int d = 0; d < 3; d++) {
+        const double x = __dadd_rn(g[3 * q + d], M.dx[d]);
+        g[3 * q + d] = x;
+        const double e = __dadd_rn(x, -M.node_last[(size_t)t * 9 + 3 * q + d]);
+        dsq = d == 0 ? __dmul_rn(e, e) : __dadd_rn(dsq, __dmul_rn(e, e));
+      }
+      moved |= dsq > trigger;
+    }
+    for (int d = 0; d < 3; d++) g[33 + d] = __dadd_rn(g[33 + d], M.dx[d]);
+  }
+  if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(&c->mesh_moved, 1);
+}
+
 // sort_contacts: move filled slots forward (swap first empty <-> last filled)
 __global__ void k_mesh_sort(Sys s, int k) {
   Ctrl *c = s.ctrl;
@@ -373,6 +412,8 @@ __global__ void k_tri_count(Sys s, int k) {
   if (gated(s.ctrl)) return;
   const MeshDev &M = s.meshes[k];
   GRID_STRIDE(t, M.ntri) {
+    if (M.moving)  // FixMesh::pre_force on a rebuild step: storeNodePosRebuild
+      for (int q = 0; q < 9; q++) M.node_last[(size_t)t * 9 + q] = M.tri[(size_t)t * kTriStride + q];
     int lo[3], hi[3];
     tri_cell_range(s, M, t, lo, hi);
     for (int z = lo[2]; z <= hi[2]; z++)
@@ -986,10 +1027,8 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
         }
     }
     double vwall[3] = {0., 0., 0.};
-    if (M.nodev) {
-      const double *vn = M.nodev + 9 * (size_t)t;
-      for (int d = 0; d < 3; d++) vwall[d] = (bary[0] * vn[d] + bary[1] * vn[3 + d] + bary[2] * vn[6 + d]);
-    }
+    if (M.moving && M.vel_on)  // barycentric node velocity, src/fix_wall_gran.cpp:929-934
+      for (int d = 0; d < 3; d++) vwall[d] = (bary[0] * M.vel[d] + bary[1] * M.vel[d] + bary[2] * M.vel[d]);
     wall_force<NORMAL>(s, A, i, deltan, delta, vwall, M.wall_type, M.rolling != 0,
                        sh + (size_t)(3 * slot) * nmax + i, nmax, shearupdate, v, om, fx, fy, fz, tx, ty, tz);
   }
@@ -1186,6 +1225,7 @@ cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st,
   if ((e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
     return e;
   int k = launch_particle(s, lc, kModeGatherFinalInitial, 1, st);
+  k += launch_mesh_move(s, lc, st);
   k_decide_loop<<<1, 1, 0, st>>>(s, hreb, hloop);
   k++;
   cudaStreamCaptureStatus cs;
@@ -1215,6 +1255,16 @@ cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st,
   *kernels_per_step = k;
   *kernels_per_rebuild = kr;
   return e;
+}
+
+int launch_mesh_move(const Sys &s, const LaunchCfg &lc, cudaStream_t st) {
+  int nl = 0;
+  for (int k = 0; k < s.nmeshes; k++) {
+    if (!s.meshes[k].moving) continue;
+    k_mesh_move<<<grid_for(s.meshes[k].ntri, 256, lc.max_grid), 256, 0, st>>>(s, k);
+    nl++;
+  }
+  return nl;
 }
 
 int launch_set_loop(const Sys &s, int n, cudaStream_t st) {

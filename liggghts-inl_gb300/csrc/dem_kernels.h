@@ -24,6 +24,8 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
 int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t st);
 int launch_particle(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, cudaStream_t st);
 int launch_set_loop(const Sys &s, int n, cudaStream_t st);
+// fix move/mesh: moves the moving meshes by one step (after the drift)
+int launch_mesh_move(const Sys &s, const LaunchCfg &lc, cudaStream_t st);
 // Executable graph of the steady-state step loop (WHILE node over steps, IF
 // node around the rebuild); see dem_kernels.cu.
 cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st, cudaStream_t st2,

@@ -87,6 +87,8 @@ def load(build=True):
     L.dem_add_mesh.argtypes = [P, I, P, I, I, P, P, P]
     L.dem_mesh_topology.argtypes = [I, P, P, P]
     L.dem_mesh_ncontacts.argtypes = [P, I, P]
+    L.dem_set_mesh_motion.argtypes = [P, I, P]
+    L.dem_download_mesh_nodes.argtypes = [P, I, P]
     L.dem_download_mesh_contacts.argtypes = [P, I, P, P, P, P]
     L.dem_upload_contact_history.argtypes = [P, I, P, P, P]
     L.dem_upload_wall_history.argtypes = [P, I, P]
@@ -168,6 +170,7 @@ class DemSystem:
         for (axis, pos, wtype, roll) in case.get("planes", []):
             self._check(L.dem_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll), None))
         self._meshkeep = []
+        self._nodes_shape = []
         for m in case.get("meshes", []):
             nodes = np.ascontiguousarray(m["nodes"], dtype=np.float64)
             ea, ca = m.get("edge_active"), m.get("corner_active")
@@ -176,6 +179,10 @@ class DemSystem:
             self._meshkeep += [nodes, ea, ca]
             self._check(L.dem_add_mesh(self.h, len(nodes), _p(nodes), int(m["wall_type"]),
                                        int(m.get("rolling", 0)), _p(ea), _p(ca), None))
+            if m.get("vel") is not None:
+                vel = np.ascontiguousarray(m["vel"], dtype=np.float64)
+                self._check(L.dem_set_mesh_motion(self.h, len(self._meshkeep) // 3 - 1, _p(vel)))
+            self._nodes_shape.append(nodes.shape)
         if "atoms" in case:
             self.upload(case["atoms"])
 
@@ -235,6 +242,11 @@ class DemSystem:
         self._check(L.dem_download_contacts(self.h, *[_p(out[k]) for k in
                                                       ("tag_i", "tag_j", "shift", "flag", "hist")]))
         return out
+
+    def mesh_nodes(self, k):
+        nodes = np.zeros(self._nodes_shape[k])
+        self._check(load().dem_download_mesh_nodes(self.h, int(k), _p(nodes)))
+        return nodes
 
     def mesh_contacts(self, k):
         L = load()

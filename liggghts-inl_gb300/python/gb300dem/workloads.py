@@ -204,7 +204,7 @@ def fibre_case(seed, nfib, nper, radius, box, spacing=(0.999, 1.001), density=10
                E=(5e7, 5e7), nu=(0.3, 0.3), rest=((0.5, 0.5), (0.5, 0.5)),
                frict=((0.3, 0.3), (0.3, 0.3)), vmax=0.0, wmax=0.0, dt=1e-7, skin=2e-4,
                gravity=(0.0, 0.0, -9.81), bond=None, gap=1.3, max_tries=200000, z0=None,
-               max_fail=None):
+               max_fail=None, periodic_xy=True):
     """Straight fibres of nper touching spheres (type 1) with directions
     uniform on the sphere, centres uniform in the box; a floor plane of wall
     type 2 at z = 0, periodic in x and y.  Sphere spacing along a fibre is
@@ -234,9 +234,10 @@ def fibre_case(seed, nfib, nper, radius, box, spacing=(0.999, 1.001), density=10
                     for oz in (-1, 0, 1):
                         for q in grid.get(((kx + ox) % ncx, (ky + oy) % ncy, kz + oz), ()):
                             dx = p[0] - q[0]
-                            dx -= Lx * round(dx / Lx)
                             dy = p[1] - q[1]
-                            dy -= Ly * round(dy / Ly)
+                            if periodic_xy:
+                                dx -= Lx * round(dx / Lx)
+                                dy -= Ly * round(dy / Ly)
                             dz = p[2] - q[2]
                             if dx * dx + dy * dy + dz * dz < (gap * d) ** 2:
                                 return False
@@ -252,12 +253,17 @@ def fibre_case(seed, nfib, nper, radius, box, spacing=(0.999, 1.001), density=10
         half = 0.5 * (nper - 1) * sp
         lo = np.array([0.0, 0.0, (z0 if z0 is not None else radius) + half * abs(u[2]) + radius])
         hi = np.array([Lx, Ly, Lz - half * abs(u[2]) - radius])
+        if not periodic_xy:  # whole fibre inside the side walls
+            for ax in (0, 1):
+                lo[ax] = half * abs(u[ax]) + radius
+                hi[ax] = box[ax] - half * abs(u[ax]) - radius
         if np.any(hi <= lo):
             continue
         c = rng.uniform(lo, hi)
         chain = c + (np.arange(nper) - 0.5 * (nper - 1))[:, None] * sp * u
-        chain[:, 0] %= Lx
-        chain[:, 1] %= Ly
+        if periodic_xy:
+            chain[:, 0] %= Lx
+            chain[:, 1] %= Ly
         if not clear(chain):
             continue
         for p in chain:
@@ -270,7 +276,8 @@ def fibre_case(seed, nfib, nper, radius, box, spacing=(0.999, 1.001), density=10
     v = rng.uniform(-vmax, vmax, size=(n, 3)) if vmax > 0 else np.zeros((n, 3))
     w = rng.uniform(-wmax, wmax, size=(n, 3)) if wmax > 0 else np.zeros((n, 3))
     case = dict(
-        boxlo=(0.0, 0.0, 0.0), boxhi=(Lx, Ly, Lz), periodic=(1, 1, 0), dt=dt, skin=skin, cdf=1.0,
+        boxlo=(0.0, 0.0, 0.0), boxhi=(Lx, Ly, Lz), periodic=(1, 1, 0) if periodic_xy else (0, 0, 0),
+        dt=dt, skin=skin, cdf=1.0,
         neigh=(1, 0, 1), normal_model=0, rolling_model=0, gravity=gravity, ntypes=2, charVel=0.0,
         planes=[(2, 0.0, 2, 0)], cohesion_model=1 if bond is not None else 0,
         material=dict(E=list(E), nu=list(nu), rest=[list(q) for q in rest],
@@ -283,6 +290,34 @@ def fibre_case(seed, nfib, nper, radius, box, spacing=(0.999, 1.001), density=10
         case["bond"] = bond
     case.update(derive_tables(E, nu, rest, frict, None))
     return case
+
+
+def plate_mesh(x0, x1, y0, y1, z):
+    """Two triangles of a horizontal plate [x0,x1] x [y0,y1] at height z,
+    normal +z; nodes[2, 3, 3]."""
+    a, b, c, d = (x0, y0, z), (x1, y0, z), (x1, y1, z), (x0, y1, z)
+    return np.array([(a, b, c), (a, c, d)], dtype=np.float64)
+
+
+def press_case(seed, nfib, nper, radius, box, plate_gap, plate_vel, inset=None, fill_height=None,
+               **kw):
+    """Fibres of bonded spheres in a closed box: floor and four side walls are
+    primitive planes of wall type 2, the lid is a two-triangle mesh plate of
+    wall type 2 that starts plate_gap above the highest sphere surface and
+    moves with velocity plate_vel (fix move/mesh ... linear).  Fibres fill
+    the box up to fill_height (default 80 % of its height)."""
+    Lx, Ly, Lz = box
+    zf = 0.8 * Lz if fill_height is None else fill_height
+    c = fibre_case(seed, nfib, nper, radius, (Lx, Ly, zf), periodic_xy=False, **kw)
+    c["boxhi"] = (Lx, Ly, Lz)
+    x = c["atoms"]["x"]
+    ztop = float(np.max(x[:, 2])) + radius + plate_gap
+    if inset is None:
+        inset = 0.1 * radius
+    c["planes"] = [(2, 0.0, 2, 0), (0, 0.0, 2, 0), (0, Lx, 2, 0), (1, 0.0, 2, 0), (1, Ly, 2, 0)]
+    c["meshes"] = [dict(nodes=plate_mesh(inset, Lx - inset, inset, Ly - inset, ztop), wall_type=2,
+                        rolling=0, vel=tuple(float(v) for v in plate_vel))]
+    return c
 
 
 def lattice_case(seed, nx, ny, nz, spacing, radius=(1e-3, 1e-3), density=2500.0,

@@ -84,6 +84,8 @@ def lib():
         L.orc_set_wall_history.argtypes = [P, ctypes.c_int, P]
         L.orc_add_mesh.argtypes = [P, ctypes.c_int, P, ctypes.c_int, ctypes.c_int, P, P]
         L.orc_get_mesh_flags.argtypes = [P, ctypes.c_int, P, P]
+        L.orc_set_mesh_motion.argtypes = [P, ctypes.c_int] + [ctypes.c_double] * 3
+        L.orc_get_mesh_nodes.argtypes = [P, ctypes.c_int, P]
         L.orc_get_mesh_contacts.argtypes = [P, ctypes.c_int, P, P, P, P]
         _lib = L
     return _lib
@@ -136,6 +138,7 @@ class Oracle:
         for (axis, pos, wtype, roll) in case.get("planes", []):
             L.orc_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll))
         self.nmesh = 0
+        self._mesh_nodes = []
         for m in case.get("meshes", []):
             nodes = np.ascontiguousarray(m["nodes"], dtype=np.float64)
             ea = m.get("edge_active")
@@ -143,8 +146,11 @@ class Oracle:
             ea = np.ascontiguousarray(ea, dtype=np.uint8) if ea is not None else None
             ca = np.ascontiguousarray(ca, dtype=np.uint8) if ca is not None else None
             self._keep += [nodes, ea, ca]
+            self._mesh_nodes.append(nodes)
             self._check(L.orc_add_mesh(self.h, len(nodes), _p(nodes), int(m["wall_type"]),
                                        int(m.get("rolling", 0)), _p(ea), _p(ca)))
+            if m.get("vel") is not None:
+                self._check(L.orc_set_mesh_motion(self.h, self.nmesh, *[float(v) for v in m["vel"]]))
             self.nmesh += 1
         a = case["atoms"]
         n = len(a["tag"])
@@ -206,7 +212,12 @@ class Oracle:
         return ea, ca
 
     def _keep_mesh_nodes(self, k):
-        return [a for a in self._keep if isinstance(a, np.ndarray) and a.ndim == 3][k]
+        return self._mesh_nodes[k]
+
+    def mesh_nodes(self, k):
+        nodes = np.zeros_like(self._keep_mesh_nodes(k))
+        lib().orc_get_mesh_nodes(self.h, int(k), _p(nodes))
+        return nodes
 
     def mesh_contacts(self, k):
         L = lib()

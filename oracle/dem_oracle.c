@@ -86,6 +86,7 @@ struct orc_sys {
 
   double cutneighmax;
   long ntimestep, nrebuilds;
+  long next_reneighbor;  /* FixMesh::next_reneighbor (mesh moved > skin/2) */
   int ago;
   int computeflag;   /* FixContactHistory computeflag_: a pair compute ran */
 };
@@ -106,6 +107,7 @@ orc_sys *orc_create(const orc_config *cfg) {
   s->bond_on = cfg->cohesion_model == ORC_COHESION_BOND_NONLINEAR;
   s->dnum = s->bond_on ? 31 : 3;
   s->shear_off = s->bond_on ? 28 : 0;
+  s->next_reneighbor = -1;
   return s;
 }
 
@@ -122,7 +124,7 @@ void orc_destroy(orc_sys *s) {
     orc_mesh *m = &s->meshes[k];
     free(m->node); free(m->nodev); free(m->edgeVec); free(m->edgeLen); free(m->edgeNorm);
     free(m->surfNorm); free(m->center); free(m->rBound); free(m->obtuse); free(m->edgeActive);
-    free(m->cornerActive); free(m->nNeighs); free(m->neighFaces); free(m->cstart); free(m->cand);
+    free(m->cornerActive); free(m->nNeighs); free(m->nodeLast); free(m->neighFaces); free(m->cstart); free(m->cand);
     free(m->nslot); free(m->npartner); free(m->partner); free(m->keep); free(m->inter); free(m->hist);
   }
   free(s);
@@ -228,6 +230,51 @@ int orc_add_mesh(orc_sys *s, int ntri, const double *nodes, int wall_type, int r
   mesh_topology(m);
   if (edge_active) memcpy(m->edgeActive, edge_active, t3);
   if (corner_active) memcpy(m->cornerActive, corner_active, t3);
+  return 0;
+}
+
+int orc_set_mesh_motion(orc_sys *s, int k, double vx, double vy, double vz) {
+  if (k < 0 || k >= s->nmeshes || s->n > 0) { snprintf(s->err, sizeof s->err, "set mesh motion before atoms"); return -1; }
+  orc_mesh *m = &s->meshes[k];
+  m->moving = 1;
+  m->vel[0] = vx; m->vel[1] = vy; m->vel[2] = vz;
+  const size_t t9 = 9 * (size_t)m->ntri;
+  m->nodev = (double *)xrealloc(m->nodev, t9 * sizeof(double));
+  memset(m->nodev, 0, t9 * sizeof(double));
+  m->nodeLast = (double *)xrealloc(m->nodeLast, t9 * sizeof(double));
+  memcpy(m->nodeLast, m->node, t9 * sizeof(double));
+  return 0;
+}
+
+int orc_get_mesh_nodes(const orc_sys *s, int k, double *nodes) {
+  if (k < 0 || k >= s->nmeshes) return -1;
+  memcpy(nodes, s->meshes[k].node, 9 * (size_t)s->meshes[k].ntri * sizeof(double));
+  return s->meshes[k].ntri;
+}
+
+/* MeshMoverLinear::initial_integrate: v := 0 then += vel; nodes and centres
+ * move by dx = dt*vel (MultiNodeMesh::move, src/multi_node_mesh_I.h:502-520) */
+static void mesh_move(orc_sys *s, orc_mesh *m) {
+  double dx[3];
+  for (int d = 0; d < 3; d++) dx[d] = s->cfg.dt * m->vel[d];
+  for (int t = 0; t < m->ntri; t++) {
+    for (int q = 0; q < 3; q++)
+      for (int d = 0; d < 3; d++) {
+        m->node[9 * (size_t)t + 3 * q + d] = m->node[9 * (size_t)t + 3 * q + d] + dx[d];
+        m->nodev[9 * (size_t)t + 3 * q + d] = 0.0 + m->vel[d];
+      }
+    for (int d = 0; d < 3; d++) m->center[3 * (size_t)t + d] = m->center[3 * (size_t)t + d] + dx[d];
+  }
+}
+
+/* MultiNodeMesh::decideRebuild, src/multi_node_mesh_I.h:792-823 */
+static int mesh_moved(const orc_sys *s, const orc_mesh *m) {
+  const double triggersq = 0.25 * s->cfg.skin * s->cfg.skin;
+  for (size_t k = 0; k < (size_t)m->ntri * 3; k++) {
+    const double *a = &m->node[3 * k], *b = &m->nodeLast[3 * k];
+    const double dx = a[0] - b[0], dy = a[1] - b[1], dz = a[2] - b[2];
+    if (dx * dx + dy * dy + dz * dz > triggersq) return 1;
+  }
   return 0;
 }
 
@@ -1549,6 +1596,8 @@ static int check_distance(orc_sys *s) {
 }
 
 static int decide(orc_sys *s) {
+  /* fixes that force a rebuild (FixMesh::next_reneighbor) come first */
+  if (s->ntimestep == s->next_reneighbor) return 1;
   s->ago++;
   if (s->ago >= s->cfg.neigh_delay && s->ago % s->cfg.neigh_every == 0) {
     if (s->cfg.neigh_check == 0) return 1;
@@ -1558,6 +1607,11 @@ static int decide(orc_sys *s) {
 }
 
 static int rebuild(orc_sys *s) {
+  /* FixMesh::pre_force on a rebuild step: node positions of this build
+   * (refreshOwned -> storeNodePosRebuild) */
+  for (int k = 0; k < s->nmeshes; k++)
+    if (s->meshes[k].moving)
+      memcpy(s->meshes[k].nodeLast, s->meshes[k].node, 9 * (size_t)s->meshes[k].ntri * sizeof(double));
   if (s->computeflag) pre_exchange(s);
   for (int k = 0; k < s->nmeshes; k++) mesh_sort_contacts(s, &s->meshes[k]);
   pbc_and_exchange(s);
@@ -1588,8 +1642,14 @@ int orc_run(orc_sys *s, int nsteps) {
   for (int k = 0; k < nsteps; k++) {
     s->ntimestep++;
     initial_integrate(s);
+    for (int k = 0; k < s->nmeshes; k++)
+      if (s->meshes[k].moving) mesh_move(s, &s->meshes[k]);
     if (decide(s)) {
       if (rebuild(s)) return -1;
+    } else {
+      /* FixMesh::pre_force on a regular step */
+      for (int k = 0; k < s->nmeshes; k++)
+        if (s->meshes[k].moving && mesh_moved(s, &s->meshes[k])) s->next_reneighbor = s->ntimestep + 1;
     }
     compute_forces(s, 1);
     final_integrate(s);

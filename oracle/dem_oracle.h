@@ -85,6 +85,11 @@ int orc_add_plane(orc_sys *s, int axis, double pos, int wall_type, int rolling_m
  * them as SurfaceMesh::buildNeighbours does.  Add meshes before atoms. */
 int orc_add_mesh(orc_sys *s, int ntri, const double *nodes, int wall_type, int rolling_model,
                  const unsigned char *edge_active, const unsigned char *corner_active);
+/* fix move/mesh mesh ID linear vx vy vz (FixMoveMesh + MeshMoverLinear,
+ * src/fix_move_mesh.cpp:194-240, src/mesh_mover_linear.cpp:95-112); add
+ * before atoms. */
+int orc_set_mesh_motion(orc_sys *s, int mesh, double vx, double vy, double vz);
+int orc_get_mesh_nodes(const orc_sys *s, int mesh, double *nodes);
 int orc_get_mesh_flags(const orc_sys *s, int mesh, unsigned char *edge_active,
                        unsigned char *corner_active);
 int orc_get_mesh_contacts(const orc_sys *s, int mesh, int *tag, int *tri, int *slot, double *hist);

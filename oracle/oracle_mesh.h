@@ -40,6 +40,10 @@ typedef struct {
   unsigned char *edgeActive, *cornerActive; /* [t][3] */
   int *nNeighs, *neighFaces;                /* [t][5] edge neighbours (ids = index) */
   int wall_type, rolling;
+  /* fix move/mesh ... linear vx vy vz */
+  int moving;
+  double vel[3];
+  double *nodeLast;    /* node positions at the last neighbour build [t][3][3] */
   /* per-triangle candidate lists (rebuild) */
   int *cstart, *cand;
   /* per-atom slots (FixContactHistoryMesh), capacity MESH_MAXSLOT */

@@ -54,6 +54,18 @@ def cases():
         fill_height=12e-3, rollfrict=((0.3,),), rolling_model=1, density=1500.0, E=(1e7,),
         nu=(0.3,), rest=((0.5,),), frict=((0.6,),), clearance=-0.6e-3),
         400, [0, 1, 10, 100, 200, 400])
+    # bonded fibres pressed by a moving two-triangle plate (fix move/mesh
+    # linear) in a box of primitive walls; the plate's travel triggers rebuilds
+    r = 0.5e-3
+    bp = workloads.bond_params(
+        2, [1], tsCreate=1.0, radiusMultiplier=0.5, K_fn1=200.0, Ku_fn1=400.0, Kc_fn1=100.0,
+        K_fn2=1e12, Ku_fn2=2e12, Kc_fn2=5e11, K_ft=5e11, K_tn=5e11, Ku_tn=1e12, Kc_tn=2.5e11,
+        K_tt=5e11, Ku_tt=1e12, Kc_tt=2.5e11, damp_fn=0.05, damp_ft=0.05, damp_tn=0.05,
+        damp_tt=0.05, maxDistance=2 * r * 1.0035, createDistance=2 * r * 1.002)
+    c["fibre_press"] = (workloads.press_case(
+        47, nfib=60, nper=4, radius=r, box=(9e-3, 9e-3, 7e-3), plate_gap=0.1e-3,
+        plate_vel=(0.0, 0.0, -6.0), gap=1.01, vmax=1.0, wmax=2000.0, bond=bp, skin=1e-4,
+        max_fail=5000), 600, [0, 1, 2, 10, 50, 100, 200, 300, 400, 500, 600])
     # fibres of bonded spheres (cohesion bond/nonlinear), floor of wall type 2
     for name, seed, stress in (("fibre_bond", 41, 0), ("fibre_bond_stress", 43, 1)):
         r = 0.5e-3
@@ -139,6 +151,8 @@ def write_inputs(case, d, nsteps, snaps):
         if m.get("rolling", 0) == 1:
             wm += " rolling_friction cdt"
         s.append("fix mwall%d all wall/gran %s mesh n_meshes 1 meshes cad%d" % (k, wm, k))
+        if m.get("vel") is not None:
+            s.append("fix mv%d all move/mesh mesh cad%d linear %s" % (k, k, " ".join(fmt(v) for v in m["vel"])))
     if not all(case["periodic"]):
         s.append("thermo_modify lost ignore")
     s += ["fix integr all nve/sphere",
@@ -231,6 +245,7 @@ def read_snapshot(path):
         snap["mesh%d_ids" % k] = m["ids"]
         snap["mesh%d_edge_active" % k] = m["edge_active"]
         snap["mesh%d_corner_active" % k] = m["corner_active"]
+        snap["mesh%d_node" % k] = m["nodes"]
     return snap
 
 
@@ -251,7 +266,7 @@ def run_case(name, case, nsteps, snaps):
         meta["bond_settings"] = case["bond"]["settings"]
         out["bond_tables"] = case["bond"]["tables"]
     meta.update(nsteps=nsteps, snaps=snaps, loop=loop)
-    meta["meshes"] = [dict(wall_type=m["wall_type"], rolling=m.get("rolling", 0))
+    meta["meshes"] = [dict(wall_type=m["wall_type"], rolling=m.get("rolling", 0), vel=m.get("vel"))
                       for m in case.get("meshes", [])]
     for k, m in enumerate(case.get("meshes", [])):
         out["mesh%d_nodes" % k] = m["nodes"]

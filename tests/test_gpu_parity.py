@@ -130,6 +130,43 @@ def test_gpu_mesh_walls_match_reference(name):
         assert hm < (HIST_RTOL if st <= 100 else 1e-6), (name, st, hm)
 
 
+def test_gpu_moving_mesh_press_matches_reference():
+    """fix move/mesh linear plate pressing bonded fibres: plate node
+    positions bit-exact, rebuilds forced by the plate's travel, forces, pair
+    and bond sets, plate contact slots and wall histories."""
+    case, snaps = load_golden("fibre_press")
+    g = _gpu(case)
+    g.setup()
+    prev = 0
+    for st in sorted(snaps):
+        if st > prev:
+            g.step(st - prev)
+            prev = st
+        r = snaps[st]
+        assert np.array_equal(g.mesh_nodes(0), r["mesh0_node"]), st
+        a = sort_by_tag(g.atoms())
+        assert np.array_equal(a["tag"], r["tag"])
+        ftol = FORCE_RTOL if st <= 10 else DIVERGED_RTOL
+        assert max_rel(a["f"], r["f"]) < ftol, (st, max_rel(a["f"], r["f"]))
+        assert max_rel(a["torque"], r["torque"]) < ftol, st
+        rp = canonical_pairs(r["pair_tag_i"], r["pair_tag_j"], r["pair_shift"], r["pair_flag"],
+                             r["pair_hist"])
+        gp = _pairs(g)
+        missing, extra, flagmis, hm = compare_pairs(gp, rp)
+        assert not missing and not extra and not flagmis, st
+        assert all(gp[k][0] == rp[k][0] for k in rp), "contact flags differ"
+        assert hm < (HIST_RTOL if st <= 100 else 1e-6), (st, hm)
+        mc = g.mesh_contacts(0)
+        gm = {(int(t), int(tr)): int(sl) for t, tr, sl in zip(mc["tag"], mc["tri"], mc["slot"])}
+        rm = {(int(t), int(tr)): int(sl) for t, tr, sl in
+              zip(r["mesh0_contact_tag"], r["mesh0_contact_tri"], r["mesh0_contact_slot"])}
+        assert gm == rm, st
+        order = np.argsort(g.atoms()["tag"], kind="stable")
+        for w in range(5):
+            assert max_rel(g.wall_history(w)[order], r["wall%d_hist" % w]) < (HIST_RTOL if st <= 100 else 1e-6)
+    assert g.nrebuilds >= 4
+
+
 def _bigger_case(seed=3, rolling=0):
     from gb300dem import workloads
     return workloads.lattice_case(seed=seed, nx=24, ny=24, nz=12, spacing=1.97e-3,
