@@ -142,6 +142,8 @@ static int alloc_atoms(dem_handle *h, int nmax) {
     CUDA_TRY(h, dalloc(L, &A.lidx, nmax));
     CUDA_TRY(h, dalloc(L, &A.whist, (size_t)3 * kMaxPlanes * nmax));
     CUDA_TRY(h, dalloc(L, &A.wbits, nmax));
+    double **fm[] = {&A.fmx, &A.fmy, &A.fmz, &A.tmx, &A.tmy, &A.tmz};
+    for (double **pp : fm) CUDA_TRY(h, dalloc(L, pp, nmax));
   }
   for (int b = 0; b < 2; b++) {
     PairArrays &P = s.pairs[b];
@@ -151,6 +153,8 @@ static int alloc_atoms(dem_handle *h, int nmax) {
     CUDA_TRY(h, cudaMemset(P.rev_start, 0, (nmax + 1) * sizeof(int)));
   }
   CUDA_TRY(h, dalloc(L, &s.perm, nmax));
+  CUDA_TRY(h, dalloc(L, &s.xf, nmax));
+  CUDA_TRY(h, dalloc(L, &s.mlist, nmax));
   CUDA_TRY(h, dalloc(L, &s.order, nmax));
   CUDA_TRY(h, dalloc(L, &s.pcount, nmax + 1));
   CUDA_TRY(h, dalloc(L, &s.rev_count, nmax + 1));
@@ -631,6 +635,18 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
   const double cutoff = (maxrad + maxrad) * s.cdf;
   s.cutneighmax = std::sqrt(cutoff * cutoff) + s.skin;
   s.ghost_slab = s.cutneighmax / 2. + s.skin / 2.;
+  {  // FP32 neighbour prefilter margin: bound of the FP32 error of rsq
+     // relative to the smallest cutoff^2, times 4, at least 1e-4
+    double cmax = 0.0, pmax = 0.0;
+    for (int d = 0; d < 3; d++) {
+      cmax = std::max(cmax, std::max(std::fabs(s.boxlo[d]), std::fabs(s.boxhi[d])));
+      pmax = std::max(pmax, s.prd[d]);
+    }
+    const double e = 3.0 * std::ldexp(cmax + pmax, -24);  // per component of delta
+    const double cmin = 2.0 * minrad * s.cdf + s.skin;
+    const double rel = 2.0 * std::sqrt(3.0) * e / cmin + 3.0 * e * e / (cmin * cmin) + 1e-6;
+    s.pf_margin = (float)std::min(0.5, std::max(1e-4, 4.0 * rel));
+  }
   long ncell = 1;
   for (int d = 0; d < 3; d++) {
     long nc = (long)std::floor(s.prd[d] / (s.cutneighmax * (1.0 + 1e-9)));
@@ -805,6 +821,7 @@ int dem_setup(dem_handle *h) {
     if (rc) return rc;
   }
   h->kt.kernel_launches += launch_pair(h->s, h->lc, 0, h->st);
+  h->kt.kernel_launches += launch_wall_force(h->s, h->lc, 0, h->st);
   h->kt.kernel_launches += launch_particle(h->s, h->lc, kModeGather, 0, h->st);
   CUDA_TRY(h, cudaGetLastError());
   bool dummy;
@@ -838,6 +855,7 @@ int dem_step(dem_handle *h, int nsteps) {
       h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);
       mark(h, 1);
       h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
+      h->kt.kernel_launches += launch_wall_force(h->s, h->lc, 1, h->st);
       mark(h, 2);
       first = false;
       k0 = 1;
@@ -863,6 +881,7 @@ int dem_step(dem_handle *h, int nsteps) {
         h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);
         mark(h, 1);
         h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
+        h->kt.kernel_launches += launch_wall_force(h->s, h->lc, 1, h->st);
         mark(h, 2);
       }
     }
@@ -874,11 +893,15 @@ int dem_step(dem_handle *h, int nsteps) {
       // the halted step's rebuild is now finished; compute its forces and
       // continue after it (later queued kernels were no-ops)
       h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
+      h->kt.kernel_launches += launch_wall_force(h->s, h->lc, 1, h->st);
       bool again = true;
       while (again) {
         rc = recover(h, &again);
         if (rc) return rc;
-        if (again) h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
+        if (again) {
+          h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
+          h->kt.kernel_launches += launch_wall_force(h->s, h->lc, 1, h->st);
+        }
       }
       rc = read_ctrl(h);
       if (rc) return rc;

@@ -15,6 +15,7 @@
 //              needed to decide a rebuild.
 #pragma once
 #include <stdint.h>
+#include <vector_types.h>
 
 namespace gb300 {
 
@@ -68,7 +69,9 @@ struct AtomArrays {
   int *type, *tag;
   int *lidx;                // the atom's index in the caller's (reference's) local order
   double *whist;            // [(w*3+d)*nmax + i]
-  uint8_t *wbits;           // bit w: atom in primitive wall w's neighbour list
+  uint8_t *wbits;           // bit w: atom in primitive wall w's neighbour list;
+                            // bit 7: atom has candidate mesh triangles
+  double *fmx, *fmy, *fmz, *tmx, *tmy, *tmz;  // mesh wall force/torque of the step (bit 7 atoms)
 };
 
 struct PairArrays {
@@ -100,6 +103,7 @@ struct Ctrl {
   int loop_left;    // steps left for the device-side step loop (graph WHILE node)
   int mesh_moved;   // a moving mesh node travelled > skin/2 since the last build
   int force_rebuild;  // rebuild at the next decide (FixMesh next_reneighbor)
+  int nmlist;         // atoms with candidate mesh triangles (Sys::mlist)
 };
 
 struct Plane {
@@ -151,6 +155,8 @@ struct Sys {
   double *resF, *resTi, *resTj;  // [3*pcap]
   uint8_t *active;  // [pcap]
   int *scan_tmp;
+  float4 *xf;       // FP32 copy (x, y, z, r) of the cell-sorted atoms, rebuild only
+  int *mlist;       // atoms with candidate mesh triangles [nmax]
   // parameters
   double *params;   // 6 matrices of (nt+1)^2: Y, G, beta, mu, mur, restlog
   int ntypes;
@@ -161,6 +167,7 @@ struct Sys {
   int periodic[3];
   double dt, skin, cdf, cutneighmax;
   double ghost_slab;  // cutneighmax/2 + skin/2: CommBrick slab_offset of the ghost band
+  float pf_margin;    // relative margin of the FP32 neighbour prefilter (see k_pairs)
   // cohesion bond/nonlinear (bond = 0: off, dnum = 3)
   int bond, dnum;
   double *bondp;      // kBondTables matrices of (nt+1)^2

@@ -246,6 +246,7 @@ __global__ void k_cell_sort(Sys s) {
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     c->n_new = s.cell_start[s.ncell];
+    c->nmlist = 0;
     c->lost_step = c->n - c->n_new;
   }
 }
@@ -311,6 +312,7 @@ __global__ void k_copy_atoms(Sys s) {
     A.tx[i] = B.tx[i]; A.ty[i] = B.ty[i]; A.tz[i] = B.tz[i];
     A.r[i] = B.r[i]; A.m[i] = B.m[i]; A.dtfm[i] = B.dtfm[i]; A.dtir[i] = B.dtir[i];
     A.type[i] = B.type[i]; A.tag[i] = B.tag[i]; A.lidx[i] = B.lidx[i];
+    s.xf[i] = make_float4((float)B.x[i], (float)B.y[i], (float)B.z[i], (float)B.r[i]);
     for (int w = 0; w < s.nplanes; w++)
       for (int d = 0; d < 3; d++)
         A.whist[(size_t)(w * 3 + d) * s.nmax + i] = B.whist[(size_t)(w * 3 + d) * s.nmax + i];
@@ -518,6 +520,31 @@ __device__ __forceinline__ int find_old(const PairArrays &L, int o, int q, bool 
   return -1;
 }
 
+// atoms in a primitive wall's neighbour list or with candidate triangles on
+// any mesh: bit 7 of wbits and the compact list the wall kernel walks (its
+// order does not matter: one thread computes all of an atom's wall forces)
+__global__ void k_wall_list(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const AtomArrays &A = s.atoms[0];
+  const int n = c->n_new;
+  const int lane = threadIdx.x & 31;
+  for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const int i = base + threadIdx.x;
+    bool has = false;
+    if (i < n) {
+      has = (A.wbits[i] & 0x7fu) != 0;
+      for (int k = 0; k < s.nmeshes; k++) has |= s.meshes[k].cand_n[i] > 0;
+      A.wbits[i] = has ? (uint8_t)(A.wbits[i] | 0x80u) : (uint8_t)(A.wbits[i] & 0x7fu);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, has);
+    int first = 0;
+    if (lane == 0 && m) first = atomicAdd(&c->nmlist, __popc(m));
+    first = __shfl_sync(0xffffffffu, first, 0);
+    if (has) s.mlist[first + __popc(m & ((1u << lane) - 1u))] = i;
+  }
+}
+
 // ----------------------------------------------------------------------------
 // rebuild: granular half list (Neighbor::granular_bin_no_newton,
 // src/neigh_gran.cpp:485-644), 27-cell stencil with periodic images.
@@ -541,6 +568,9 @@ __global__ void k_pairs(Sys s) {
     const double radi = A.r[i];
     const double mi = A.m[i];
     const int ci[3] = {cell_coord(s, xi, 0), cell_coord(s, yi, 1), cell_coord(s, zi, 2)};
+    const float4 pi = s.xf[i];
+    const float cdff = (float)s.cdf, skinf = (float)s.skin;
+    const float hi_f = 1.0f + s.pf_margin, lo_f = 1.0f - s.pf_margin;
     int cnt = 0;
     int out = FILL ? M.row[i] : 0;
     const int out_end = FILL ? M.row[i + 1] : 0;
@@ -568,9 +598,25 @@ __global__ void k_pairs(Sys s) {
           const int code = (sv[0] + 1) + 3 * (sv[1] + 1) + 9 * (sv[2] + 1);
           const int cell = cc[0] + s.nc[0] * (cc[1] + s.nc[1] * cc[2]);
           const int jb = s.cell_start[cell], je = s.cell_start[cell + 1];
+          const float sxf = sv[0] * (float)s.prd[0], syf = sv[1] * (float)s.prd[1], szf = sv[2] * (float)s.prd[2];
           for (int j = jb; j < je; j++) {
             if (code == kNoShift && j <= i) continue;
+            // FP32 prefilter of rsq <= (radsum*cdf + skin)^2: candidates
+            // clearly outside (or clearly inside) by more than the bound of
+            // the FP32 rounding are decided without FP64; the rest, and
+            // every entry the fill pass writes, use the exact FP64 test.
+            const float4 pj = s.xf[j];
+            const float fx = pi.x - (pj.x + sxf), fy = pi.y - (pj.y + syf), fz = pi.z - (pj.z + szf);
+            const float rsqf = fx * fx + fy * fy + fz * fz;
+            const float csf = (pi.w + pj.w) * cdff + skinf;
+            const float cs2f = csf * csf;
+            if (rsqf > cs2f * hi_f) continue;
             if (code != kNoShift && !ghost_exists(s, A, j, sv)) continue;
+            const bool clear_in = rsqf < cs2f * lo_f;
+            if (!FILL && clear_in) {
+              cnt++;
+              continue;
+            }
             double xj = A.x[j], yj = A.y[j], zj = A.z[j];
             image(s, code, xj, yj, zj);
             const double delx = __dadd_rn(xi, -xj);
@@ -1041,6 +1087,36 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
   M.npart[0][i] = np;
 }
 
+// FixWallGran::post_force_primitive / post_force_mesh for the atoms near a
+// wall (the compact list of k_wall_list): wall forces and torques of the
+// current state, planes then meshes in order, into fm/tm.  Independent of
+// the pair kernel of the same step (it reads positions and velocities and
+// writes only the wall histories, mesh slots and fm/tm), so the two run side
+// by side; the per-atom kernel adds fm/tm.
+template <int NORMAL>
+__global__ void __launch_bounds__(128) k_wall_force(Sys s, int shearupdate) {
+  Ctrl *c = s.ctrl;
+  if (c->halt) return;
+  const AtomArrays &A = s.atoms[0];
+  const int nl = c->nmlist;
+  bool meshbad = false;
+  GRID_STRIDE(q, nl) {
+    const int i = s.mlist[q];
+    double v[3] = {A.vx[i], A.vy[i], A.vz[i]};
+    double om[3] = {A.wx[i], A.wy[i], A.wz[i]};
+    double xv[3] = {A.x[i], A.y[i], A.z[i]};
+    double fx = 0., fy = 0., fz = 0., tx = 0., ty = 0., tz = 0.;
+    const uint8_t bits = A.wbits[i];
+    for (int w = 0; w < s.nplanes; w++)
+      if (bits & (1u << w)) plane_contact<NORMAL>(s, A, i, w, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz);
+    for (int k = 0; k < s.nmeshes; k++)
+      mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad);
+    A.fmx[i] = fx; A.fmy[i] = fy; A.fmz[i] = fz;
+    A.tmx[i] = tx; A.tmy[i] = ty; A.tmz[i] = tz;
+  }
+  if (__any_sync(0xffffffffu, meshbad) && (threadIdx.x & 31) == 0) atomicExch(&c->status, kStatMeshSlots);
+}
+
 template <int NORMAL, bool GATHER, bool FINAL, bool INITIAL>
 __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
   Ctrl *c = s.ctrl;
@@ -1051,7 +1127,7 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
   const size_t P = s.pcap;
   const double dtv = s.dt;
   const double trigger = 0.25 * s.skin * s.skin;
-  bool moved = false, bad = false, meshbad = false;
+  bool moved = false, bad = false;
   GRID_STRIDE(i, n) {
     double fx, fy, fz, tx, ty, tz;
     double v[3] = {A.vx[i], A.vy[i], A.vz[i]};
@@ -1078,14 +1154,10 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
         fy = __dadd_rn(fy, __dmul_rn(massone, s.g[1]));
         fz = __dadd_rn(fz, __dmul_rn(massone, s.g[2]));
       }
-      const uint8_t bits = A.wbits[i];
-      if (bits) {
-        for (int w = 0; w < s.nplanes; w++)
-          if (bits & (1u << w))
-            plane_contact<NORMAL>(s, A, i, w, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz);
+      if (A.wbits[i] & 0x80u) {  // walls, computed by k_wall_force for this step
+        fx += A.fmx[i]; fy += A.fmy[i]; fz += A.fmz[i];
+        tx += A.tmx[i]; ty += A.tmy[i]; tz += A.tmz[i];
       }
-      for (int k = 0; k < s.nmeshes; k++)
-        mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad);
       A.fx[i] = fx; A.fy[i] = fy; A.fz[i] = fz;
       A.tx[i] = tx; A.ty[i] = ty; A.tz[i] = tz;
     } else {
@@ -1129,9 +1201,6 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
   if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(&c->moved, 1);
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) {
     atomicExch(&c->status, kStatNan);
-  }
-  if (__any_sync(0xffffffffu, meshbad) && (threadIdx.x & 31) == 0) {
-    atomicExch(&c->status, kStatMeshSlots);
   }
 }
 
@@ -1198,6 +1267,10 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
     k_tri_fill<<<gT, B, 0, st>>>(s, k);
     k_mesh_cand<<<gN, B, 0, st>>>(s, k);
   }
+  if (s.nmeshes > 0 || s.nplanes > 0) {
+    k_wall_list<<<gN, B, 0, st>>>(s);
+    nl++;
+  }
   k_finish_rebuild<<<1, 1, 0, st>>>(s);
   return nl + 4;
 }
@@ -1243,9 +1316,23 @@ cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st,
   cudaGraph_t rbody = ip.conditional.phGraph_out[0];
   if ((e = cudaStreamUpdateCaptureDependencies(st, &inode, nullptr, 1, cudaStreamSetCaptureDependencies)) != cudaSuccess)
     return e;
+  // the pair kernel and the wall kernel of the step run side by side
+  cudaEvent_t fork = nullptr, join = nullptr;
+  const bool walls = s.nmeshes > 0 || s.nplanes > 0;
+  if (walls) {
+    if ((e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming)) != cudaSuccess) return e;
+    if ((e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st2, fork, 0)) != cudaSuccess) return e;
+    k += launch_wall_force(s, lc, 1, st2);
+    if ((e = cudaEventRecord(join, st2)) != cudaSuccess) return e;
+  }
   k += launch_pair(s, lc, 1, st);
+  if (walls && (e = cudaStreamWaitEvent(st, join, 0)) != cudaSuccess) return e;
   cudaGraph_t out = nullptr;
   if ((e = cudaStreamEndCapture(st, &out)) != cudaSuccess) return e;
+  if (fork) cudaEventDestroy(fork);
+  if (join) cudaEventDestroy(join);
   if ((e = cudaStreamBeginCaptureToGraph(st2, rbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
     return e;
   const int kr = launch_rebuild(s, lc, st2, 0);
@@ -1255,6 +1342,14 @@ cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st,
   *kernels_per_step = k;
   *kernels_per_rebuild = kr;
   return e;
+}
+
+int launch_wall_force(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t st) {
+  if (s.nmeshes == 0 && s.nplanes == 0) return 0;
+  const int g = grid_for(s.nmax, 128, lc.max_grid);
+  if (s.normal == kHertz) k_wall_force<kHertz><<<g, 128, 0, st>>>(s, shearupdate);
+  else k_wall_force<kHooke><<<g, 128, 0, st>>>(s, shearupdate);
+  return 1;
 }
 
 int launch_mesh_move(const Sys &s, const LaunchCfg &lc, cudaStream_t st) {

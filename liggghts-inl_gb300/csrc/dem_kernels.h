@@ -24,6 +24,9 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
 int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t st);
 int launch_particle(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, cudaStream_t st);
 int launch_set_loop(const Sys &s, int n, cudaStream_t st);
+// wall (plane and mesh) forces of the current state, before the particle
+// kernel that gathers the step's forces; none without walls
+int launch_wall_force(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t st);
 // fix move/mesh: moves the moving meshes by one step (after the drift)
 int launch_mesh_move(const Sys &s, const LaunchCfg &lc, cudaStream_t st);
 // Executable graph of the steady-state step loop (WHILE node over steps, IF
