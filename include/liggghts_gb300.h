@@ -220,6 +220,8 @@ typedef struct dem_kernel_times {
   double neigh_ms;             /* decide + rebuild stage (Neighbor::decide/build) */
   long long neigh_stages;
   long long kernel_launches;
+  double wall_ms;              /* wall kernel: primitive planes and meshes (FixWallGran::post_force) */
+  long long wall_launches;
 } dem_kernel_times;
 int dem_profile(dem_handle *h, int enable);
 int dem_get_kernel_times(dem_handle *h, dem_kernel_times *out);

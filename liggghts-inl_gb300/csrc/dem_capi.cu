@@ -43,7 +43,7 @@ struct dem_handle {
   bool profile = false;
   std::vector<cudaEvent_t> evpool;
   int evused = 0;
-  std::vector<int> evkind;  // 0 particle, 1 neigh, 2 pair: kind of interval ending at event k
+  std::vector<int> evkind;  // 0 particle, 1 neigh, 2 pair, 3 wall: kind of interval ending at event k
   dem_kernel_times kt{};
   // graph-resident step loop
   bool use_graph = true;
@@ -92,6 +92,7 @@ static void harvest(dem_handle *h) {
     if (h->evkind[k] == 0) { h->kt.particle_ms += ms; h->kt.particle_launches++; }
     if (h->evkind[k] == 1) { h->kt.neigh_ms += ms; h->kt.neigh_stages++; }
     if (h->evkind[k] == 2) { h->kt.pair_ms += ms; h->kt.pair_launches++; }
+    if (h->evkind[k] == 3) { h->kt.wall_ms += ms; h->kt.wall_launches++; }
   }
   h->evused = 0;
 }
@@ -646,6 +647,9 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
     const double cmin = 2.0 * minrad * s.cdf + s.skin;
     const double rel = 2.0 * std::sqrt(3.0) * e / cmin + 3.0 * e * e / (cmin * cmin) + 1e-6;
     s.pf_margin = (float)std::min(0.5, std::max(1e-4, 4.0 * rel));
+    const double tmin = 2.0 * minrad;
+    const double relt = 2.0 * std::sqrt(3.0) * e / tmin + 3.0 * e * e / (tmin * tmin) + 1e-6;
+    s.pf_margin_touch = (float)std::min(0.5, std::max(1e-4, 4.0 * relt));
   }
   long ncell = 1;
   for (int d = 0; d < 3; d++) {
@@ -855,8 +859,9 @@ int dem_step(dem_handle *h, int nsteps) {
       h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);
       mark(h, 1);
       h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
-      h->kt.kernel_launches += launch_wall_force(h->s, h->lc, 1, h->st);
       mark(h, 2);
+      h->kt.kernel_launches += launch_wall_force(h->s, h->lc, 1, h->st);
+      mark(h, 3);
       first = false;
       k0 = 1;
     }
@@ -881,8 +886,9 @@ int dem_step(dem_handle *h, int nsteps) {
         h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);
         mark(h, 1);
         h->kt.kernel_launches += launch_pair(h->s, h->lc, 1, h->st);
-        h->kt.kernel_launches += launch_wall_force(h->s, h->lc, 1, h->st);
         mark(h, 2);
+        h->kt.kernel_launches += launch_wall_force(h->s, h->lc, 1, h->st);
+        mark(h, 3);
       }
     }
     CUDA_TRY(h, cudaGetLastError());
@@ -1056,7 +1062,7 @@ int dem_profile(dem_handle *h, int enable) {
   h->kt = dem_kernel_times{};
   h->profile = enable != 0;
   if (h->profile && h->evpool.empty()) {
-    const int nev = 3 * kCheckEvery + 8;
+    const int nev = 4 * kCheckEvery + 8;
     h->evpool.resize(nev);
     h->evkind.resize(nev);
     for (auto &e : h->evpool) CUDA_TRY(h, cudaEventCreate(&e));

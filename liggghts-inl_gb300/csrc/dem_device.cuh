@@ -155,7 +155,7 @@ struct Sys {
   double *resF, *resTi, *resTj;  // [3*pcap]
   uint8_t *active;  // [pcap]
   int *scan_tmp;
-  float4 *xf;       // FP32 copy (x, y, z, r) of the cell-sorted atoms, rebuild only
+  float4 *xf;       // FP32 copy (x, y, z, r) of the atoms, refreshed by every drift
   int *mlist;       // atoms with candidate mesh triangles [nmax]
   // parameters
   double *params;   // 6 matrices of (nt+1)^2: Y, G, beta, mu, mur, restlog
@@ -168,6 +168,7 @@ struct Sys {
   double dt, skin, cdf, cutneighmax;
   double ghost_slab;  // cutneighmax/2 + skin/2: CommBrick slab_offset of the ghost band
   float pf_margin;    // relative margin of the FP32 neighbour prefilter (see k_pairs)
+  float pf_margin_touch;  // the same for the touching test of k_pair (radsum^2)
   // cohesion bond/nonlinear (bond = 0: off, dnum = 3)
   int bond, dnum;
   double *bondp;      // kBondTables matrices of (nt+1)^2

@@ -523,12 +523,15 @@ __device__ __forceinline__ int find_old(const PairArrays &L, int o, int q, bool 
 // atoms in a primitive wall's neighbour list or with candidate triangles on
 // any mesh: bit 7 of wbits and the compact list the wall kernel walks (its
 // order does not matter: one thread computes all of an atom's wall forces)
-__global__ void k_wall_list(Sys s) {
+__global__ void __launch_bounds__(256) k_wall_list(Sys s) {
+  __shared__ int wc[8], wbase;
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
   const AtomArrays &A = s.atoms[0];
   const int n = c->n_new;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // one reservation per block keeps each block's atoms ascending and
+  // contiguous in the list (coalesced per-atom loads in the wall kernel)
   for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const int i = base + threadIdx.x;
     bool has = false;
@@ -538,10 +541,18 @@ __global__ void k_wall_list(Sys s) {
       A.wbits[i] = has ? (uint8_t)(A.wbits[i] | 0x80u) : (uint8_t)(A.wbits[i] & 0x7fu);
     }
     const unsigned m = __ballot_sync(0xffffffffu, has);
-    int first = 0;
-    if (lane == 0 && m) first = atomicAdd(&c->nmlist, __popc(m));
-    first = __shfl_sync(0xffffffffu, first, 0);
-    if (has) s.mlist[first + __popc(m & ((1u << lane) - 1u))] = i;
+    if (lane == 0) wc[warp] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w = 0; w < 8; w++) tot += wc[w];
+      wbase = tot ? atomicAdd(&c->nmlist, tot) : 0;
+    }
+    __syncthreads();
+    int off = wbase;
+    for (int w = 0; w < warp; w++) off += wc[w];
+    if (has) s.mlist[off + __popc(m & ((1u << lane) - 1u))] = i;
+    __syncthreads();
   }
 }
 
@@ -790,11 +801,32 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
   const long long ntimestep = BOND ? c->ntimestep : 0;
   const bool may_create = BOND && shearupdate &&
                           ((s.bond_flags & kBondCreateAlways) || ntimestep == s.bond_ts_create);
+  // FP32 prefilter (contact distance factor 1, no bonds: an entry that is
+  // not touching has no further work): entries clearly apart by more than
+  // the FP32 rounding bound skip the exact FP64 test
+  const bool prefilter = !BOND && s.cdf == 1.0;
+  const float hi_f = 1.0f + s.pf_margin_touch;
   for (int base = blockIdx.x * kPairTile; base < np; base += gridDim.x * kPairTile) {
     const int p = base + threadIdx.x;
     bool queue = false;
     double delx = 0., dely = 0., delz = 0., rsq = 0.;
-    if (p < np) {
+    bool apart = false;
+    if (p < np && prefilter) {
+      const int i = L.i[p], j = L.j[p];
+      const int code = L.sh[p];
+      const float4 pi = s.xf[i], pj = s.xf[j];
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      if (code != kNoShift) {
+        sx = (code % 3 - 1) * (float)s.prd[0];
+        sy = ((code / 3) % 3 - 1) * (float)s.prd[1];
+        sz = (code / 9 - 1) * (float)s.prd[2];
+      }
+      const float fx = pi.x - (pj.x + sx), fy = pi.y - (pj.y + sy), fz = pi.z - (pj.z + sz);
+      const float rs = pi.w + pj.w;
+      apart = fx * fx + fy * fy + fz * fz > rs * rs * hi_f;
+      if (apart) s.active[p] = 0;
+    }
+    if (p < np && !apart) {
       const int i = L.i[p], j = L.j[p];
       const int code = L.sh[p];
       double xj = A.x[j], yj = A.y[j], zj = A.z[j];
@@ -889,8 +921,10 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
       }
       ContactOut o;
       if (touch) {
-        ci.r = sqrt(rsq_q);
+        // r from 1/r: within an ulp of sqrt(rsq), which moves the overlap
+        // radsum - r by ~1e-13 of itself
         ci.rinv = rsqrt(rsq_q);
+        ci.r = rsq_q * ci.rinv;
         ci.reff = L.reff[q];
         ci.c0 = L.c0[q];
         ci.c1 = L.c1[q];
@@ -1035,9 +1069,19 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
   int np = M.npart[0][i];
   const double radi = A.r[i];
   const double cdm1 = s.cdf - 1.0;
+  // a triangle is at least as far as its plane: candidates whose plane is
+  // clearly beyond the contact range (relative margin 1e-9, far above the
+  // rounding of either side) skip the closest-feature resolution; the
+  // resolution would return deltan > 0 and skip them as well
+  const double reach = __dmul_rn(__dadd_rn(radi, fmax(0.0, __dmul_rn(cdm1, radi))), 1.0 + 1e-9);
   for (int q = 0; q < nc; q++) {
     const int t = M.cand[(size_t)q * nmax + i];
     const double *g = M.tri + (size_t)t * kTriStride;
+    {
+      const double *sn = tri_sn(g), *n0 = tri_node(g, 0);
+      const double dn = sn[0] * (xv[0] - n0[0]) + sn[1] * (xv[1] - n0[1]) + sn[2] * (xv[2] - n0[2]);
+      if (fabs(dn) > reach) continue;
+    }
     double delta[3], bary[3];
     int bs;
     const double deltan = resolve_tri_sphere(g, M.meta[t], radi, xv, delta, bary, bs);
@@ -1188,6 +1232,7 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
         om[1] = fma(dtir, ty, om[1]);
         om[2] = fma(dtir, tz, om[2]);
         A.x[i] = xv[0]; A.y[i] = xv[1]; A.z[i] = xv[2];
+        s.xf[i] = make_float4((float)xv[0], (float)xv[1], (float)xv[2], (float)A.r[i]);
         const double dx = __dadd_rn(xv[0], -A.xh[i]);
         const double dy = __dadd_rn(xv[1], -A.yh[i]);
         const double dz = __dadd_rn(xv[2], -A.zh[i]);

@@ -62,7 +62,8 @@ class DemKernelTimes(ctypes.Structure):
     _fields_ = [("pair_ms", ctypes.c_double), ("pair_launches", ctypes.c_longlong),
                 ("particle_ms", ctypes.c_double), ("particle_launches", ctypes.c_longlong),
                 ("neigh_ms", ctypes.c_double), ("neigh_stages", ctypes.c_longlong),
-                ("kernel_launches", ctypes.c_longlong)]
+                ("kernel_launches", ctypes.c_longlong), ("wall_ms", ctypes.c_double),
+                ("wall_launches", ctypes.c_longlong)]
 
 
 _lib = None
