@@ -10,6 +10,8 @@
 // atomics anywhere.  Integer atomics are only used for counting; each
 // resulting order is made canonical by a per-cell / per-atom sort.
 #include <cuda_runtime.h>
+
+#include <algorithm>
 #include <stdint.h>
 
 #include "bond_law.cuh"
@@ -577,7 +579,6 @@ __global__ void k_pairs(Sys s) {
     }
     const double xi = A.x[i], yi = A.y[i], zi = A.z[i];
     const double radi = A.r[i];
-    const double mi = A.m[i];
     const int ci[3] = {cell_coord(s, xi, 0), cell_coord(s, yi, 1), cell_coord(s, zi, 2)};
     const float4 pi = s.xf[i];
     const float cdff = (float)s.cdf, skinf = (float)s.skin;
@@ -643,52 +644,70 @@ __global__ void k_pairs(Sys s) {
               continue;
             }
             if (out >= out_end) continue;  // count and fill passes agree; guard only
-            // history carry-over as the reference does it (pre_exchange
-            // partner lists + the lookup of src/neigh_gran.cpp:590-620): the
-            // new entry's reference owner R (lower lidx of an owned pair,
-            // else i) takes its partner-list entry for the other atom: its
-            // own old entry, or the partner copy of an old owned pair, in
-            // which the values registered with newtonflag 1 change sign.
-            // The shear is then expressed in the list's own orientation.
-            int e = -1;
-            double ssign = 1.0;
-            bool quirk = false;
-            if (rsq < __dmul_rn(radsum, radsum)) {
-              const bool rj = s.bond && code == kNoShift && A.lidx[i] > A.lidx[j];
-              bool fl;
-              e = rj ? find_old(L, s.perm[j], s.perm[i], fl) : find_old(L, s.perm[i], s.perm[j], fl);
-              ssign = (fl ? -1.0 : 1.0) * (rj ? -1.0 : 1.0);
-              quirk = s.bond && e >= 0 && !rj && code != kNoShift && L.sh[e] == kNoShift &&
-                      A.lidx[i] > A.lidx[j];
-            }
             const int p = out++;
             M.i[p] = i;
             M.j[p] = j;
             M.sh[p] = (uint8_t)code;
-            M.flag[p] = e >= 0 ? 1 : 0;
-            for (int d = 0; d < kDnumShear; d++)
-              M.hist[(size_t)d * s.pcap + p] = e >= 0 ? ssign * L.hist[(size_t)d * s.pcap + e] : 0.0;
-            for (int d = kDnumShear; d < s.dnum; d++) {
-              double hv = e >= 0 ? L.hist[(size_t)d * s.pcap + e] : 0.0;
-              if (quirk && d >= kDnumShear + 5 && d <= kDnumShear + 13) hv = -hv;
-              M.hist[(size_t)d * s.pcap + p] = hv;
-            }
-            const double mj = A.m[j];
-            const double meff = mi * mj / (mi + mj);
-            const double reff = radi * radj / (radi + radj);
-            const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], A.type[j]);
-            double c0, c1;
-            if (s.normal == kHertz) contact_consts<kHertz>(tp, meff, reff, s.charVel, s.tdamp, c0, c1);
-            else contact_consts<kHooke>(tp, meff, reff, s.charVel, s.tdamp, c0, c1);
-            M.reff[p] = reff;
-            M.c0[p] = c0;
-            M.c1[p] = c1;
-            if (code == kNoShift) atomicAdd(&s.rev_count[j], 1);
           }
         }
       }
     }
     if (!FILL) s.pcount[i] = cnt;
+  }
+}
+
+// Per new list entry (one thread each, dense): exact distance, history
+// carry-over, per-pair contact constants, reverse-list count.  The carry-over
+// is the reference's (pre_exchange partner lists + the lookup of
+// src/neigh_gran.cpp:590-620): the new entry's reference owner R (lower lidx
+// of an owned pair, else i) takes its partner-list entry for the other atom:
+// its own old entry, or the partner copy of an old owned pair, in which the
+// values registered with newtonflag 1 change sign.  The shear is then
+// expressed in the list's own orientation; history is carried only when the
+// pair is within radsum*cdf at the build.
+__global__ void k_pair_init(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const AtomArrays &A = s.atoms[0];
+  const PairArrays &L = s.pairs[0];  // old list (old atom order)
+  const PairArrays &M = s.pairs[1];  // new list
+  const int np = c->np_new;
+  GRID_STRIDE(p, np) {
+    const int i = M.i[p], j = M.j[p], code = M.sh[p];
+    double xj = A.x[j], yj = A.y[j], zj = A.z[j];
+    image(s, code, xj, yj, zj);
+    const double rsq = rsq_rn(__dadd_rn(A.x[i], -xj), __dadd_rn(A.y[i], -yj), __dadd_rn(A.z[i], -zj));
+    const double radi = A.r[i], radj = A.r[j];
+    const double radsum = __dmul_rn(__dadd_rn(radi, radj), s.cdf);
+    int e = -1;
+    double ssign = 1.0;
+    bool quirk = false;
+    if (rsq < __dmul_rn(radsum, radsum)) {
+      const bool rj = s.bond && code == kNoShift && A.lidx[i] > A.lidx[j];
+      bool fl;
+      e = rj ? find_old(L, s.perm[j], s.perm[i], fl) : find_old(L, s.perm[i], s.perm[j], fl);
+      ssign = (fl ? -1.0 : 1.0) * (rj ? -1.0 : 1.0);
+      quirk = s.bond && e >= 0 && !rj && code != kNoShift && L.sh[e] == kNoShift && A.lidx[i] > A.lidx[j];
+    }
+    M.flag[p] = e >= 0 ? 1 : 0;
+    for (int d = 0; d < kDnumShear; d++)
+      M.hist[(size_t)d * s.pcap + p] = e >= 0 ? ssign * L.hist[(size_t)d * s.pcap + e] : 0.0;
+    for (int d = kDnumShear; d < s.dnum; d++) {
+      double hv = e >= 0 ? L.hist[(size_t)d * s.pcap + e] : 0.0;
+      if (quirk && d >= kDnumShear + 5 && d <= kDnumShear + 13) hv = -hv;
+      M.hist[(size_t)d * s.pcap + p] = hv;
+    }
+    const double mi = A.m[i], mj = A.m[j];
+    const double meff = mi * mj / (mi + mj);
+    const double reff = radi * radj / (radi + radj);
+    const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], A.type[j]);
+    double c0, c1;
+    if (s.normal == kHertz) contact_consts<kHertz>(tp, meff, reff, s.charVel, s.tdamp, c0, c1);
+    else contact_consts<kHooke>(tp, meff, reff, s.charVel, s.tdamp, c0, c1);
+    M.reff[p] = reff;
+    M.c0[p] = c0;
+    M.c1[p] = c1;
+    if (code == kNoShift) atomicAdd(&s.rev_count[j], 1);
   }
 }
 
@@ -801,32 +820,11 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
   const long long ntimestep = BOND ? c->ntimestep : 0;
   const bool may_create = BOND && shearupdate &&
                           ((s.bond_flags & kBondCreateAlways) || ntimestep == s.bond_ts_create);
-  // FP32 prefilter (contact distance factor 1, no bonds: an entry that is
-  // not touching has no further work): entries clearly apart by more than
-  // the FP32 rounding bound skip the exact FP64 test
-  const bool prefilter = !BOND && s.cdf == 1.0;
-  const float hi_f = 1.0f + s.pf_margin_touch;
   for (int base = blockIdx.x * kPairTile; base < np; base += gridDim.x * kPairTile) {
     const int p = base + threadIdx.x;
     bool queue = false;
     double delx = 0., dely = 0., delz = 0., rsq = 0.;
-    bool apart = false;
-    if (p < np && prefilter) {
-      const int i = L.i[p], j = L.j[p];
-      const int code = L.sh[p];
-      const float4 pi = s.xf[i], pj = s.xf[j];
-      float sx = 0.f, sy = 0.f, sz = 0.f;
-      if (code != kNoShift) {
-        sx = (code % 3 - 1) * (float)s.prd[0];
-        sy = ((code / 3) % 3 - 1) * (float)s.prd[1];
-        sz = (code / 9 - 1) * (float)s.prd[2];
-      }
-      const float fx = pi.x - (pj.x + sx), fy = pi.y - (pj.y + sy), fz = pi.z - (pj.z + sz);
-      const float rs = pi.w + pj.w;
-      apart = fx * fx + fy * fy + fz * fz > rs * rs * hi_f;
-      if (apart) s.active[p] = 0;
-    }
-    if (p < np && !apart) {
+    if (p < np) {
       const int i = L.i[p], j = L.j[p];
       const int code = L.sh[p];
       double xj = A.x[j], yj = A.y[j], zj = A.z[j];
@@ -958,6 +956,125 @@ __global__ void __launch_bounds__(kPairTile) k_pair(Sys s, int shearupdate) {
     }
     __syncthreads();
   }
+}
+
+// Pair forces without cohesion and with contact distance factor 1 (an entry
+// that is not touching needs no work).  Each tile first tests its entries in
+// FP32 (x, y, z, r refreshed by every drift): entries apart by more than the
+// bound of the FP32 rounding (pf_margin_touch) only clear their active flag.
+// The rest are queued in shared memory until a full tile of 256 has
+// gathered, which then runs the exact test and the FP64 contact law on dense
+// warps (the FP64 pipe issues per warp, so idle lanes would waste it).
+template <int NORMAL, bool ROLL>
+__device__ __forceinline__ void pair_entry(const Sys &s, int q, int shearupdate) {
+  const AtomArrays &A = s.atoms[0];
+  const PairArrays &L = s.pairs[0];
+  const size_t P = s.pcap;
+  const int i = L.i[q], j = L.j[q];
+  double xj = A.x[j], yj = A.y[j], zj = A.z[j];
+  image(s, L.sh[q], xj, yj, zj);
+  ContactIn ci;
+  ci.d[0] = __dadd_rn(A.x[i], -xj);
+  ci.d[1] = __dadd_rn(A.y[i], -yj);
+  ci.d[2] = __dadd_rn(A.z[i], -zj);
+  const double rsq = rsq_rn(ci.d[0], ci.d[1], ci.d[2]);
+  ci.radi = A.r[i];
+  ci.radj = A.r[j];
+  ci.radsum = __dadd_rn(ci.radi, ci.radj);
+  if (!(rsq < __dmul_rn(ci.radsum, ci.radsum))) {
+    s.active[q] = 0;
+    return;
+  }
+  ci.vr[0] = A.vx[i] - A.vx[j];
+  ci.vr[1] = A.vy[i] - A.vy[j];
+  ci.vr[2] = A.vz[i] - A.vz[j];
+  ci.wi[0] = A.wx[i]; ci.wi[1] = A.wy[i]; ci.wi[2] = A.wz[i];
+  ci.wj[0] = A.wx[j]; ci.wj[1] = A.wy[j]; ci.wj[2] = A.wz[j];
+  // r from 1/r: within an ulp of sqrt(rsq), which moves the overlap
+  // radsum - r by ~1e-13 of itself
+  ci.rinv = rsqrt(rsq);
+  ci.r = rsq * ci.rinv;
+  ci.reff = L.reff[q];
+  ci.c0 = L.c0[q];
+  ci.c1 = L.c1[q];
+  ci.en[0] = ci.d[0] * ci.rinv;
+  ci.en[1] = ci.d[1] * ci.rinv;
+  ci.en[2] = ci.d[2] * ci.rinv;
+  ci.deltan_wall = 0.0;
+  const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], A.type[j]);
+  double sh3[3] = {L.hist[q], L.hist[P + q], L.hist[2 * P + q]};
+  ContactOut o;
+  contact_law<NORMAL, false>(ci, tp, s.dt, s.tdamp, s.limitf, ROLL, shearupdate != 0, sh3, o);
+  if (shearupdate) {
+    L.hist[q] = sh3[0];
+    L.hist[P + q] = sh3[1];
+    L.hist[2 * P + q] = sh3[2];
+  }
+  L.flag[q] |= (kContactNormal | kContactTangential);
+  s.resF[q] = o.F[0]; s.resF[P + q] = o.F[1]; s.resF[2 * P + q] = o.F[2];
+  s.resTi[q] = o.Ti[0]; s.resTi[P + q] = o.Ti[1]; s.resTi[2 * P + q] = o.Ti[2];
+  s.resTj[q] = o.Tj[0]; s.resTj[P + q] = o.Tj[1]; s.resTj[2 * P + q] = o.Tj[2];
+  s.active[q] = 1;
+}
+
+template <int NORMAL, bool ROLL>
+__global__ void __launch_bounds__(kPairTile, 3) k_pair_pf(Sys s, int shearupdate) {
+  __shared__ int q[2 * kPairTile];
+  __shared__ int wcnt[kPairTile / 32];
+  __shared__ int qn_s;
+  Ctrl *c = s.ctrl;
+  if (c->halt) return;
+  const PairArrays &L = s.pairs[0];
+  const int np = c->np;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const float hi_f = 1.0f + s.pf_margin_touch;
+  const float px = (float)s.prd[0], py = (float)s.prd[1], pz = (float)s.prd[2];
+  if (threadIdx.x == 0) qn_s = 0;
+  __syncthreads();
+  for (int base = blockIdx.x * kPairTile; base < np; base += gridDim.x * kPairTile) {
+    const int p = base + threadIdx.x;
+    bool maybe = false;
+    if (p < np) {
+      const int code = L.sh[p];
+      const float4 a = s.xf[L.i[p]], b = s.xf[L.j[p]];
+      float sx = 0.f, sy = 0.f, sz = 0.f;
+      if (code != kNoShift) {
+        sx = (code % 3 - 1) * px;
+        sy = ((code / 3) % 3 - 1) * py;
+        sz = (code / 9 - 1) * pz;
+      }
+      const float fx = a.x - (b.x + sx), fy = a.y - (b.y + sy), fz = a.z - (b.z + sz);
+      const float rs = a.w + b.w;
+      maybe = !(fx * fx + fy * fy + fz * fz > rs * rs * hi_f);
+      if (!maybe) s.active[p] = 0;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, maybe);
+    if (lane == 0) wcnt[warp] = __popc(m);
+    __syncthreads();
+    int off = 0, tot = 0;
+#pragma unroll
+    for (int k = 0; k < kPairTile / 32; k++) {
+      const int v = wcnt[k];
+      off += (k < warp) ? v : 0;
+      tot += v;
+    }
+    const int qn = qn_s;
+    if (maybe) q[qn + off + __popc(m & ((1u << lane) - 1u))] = p;
+    __syncthreads();
+    if (threadIdx.x == 0) qn_s = qn + tot;
+    __syncthreads();
+    if (qn_s >= kPairTile) {
+      pair_entry<NORMAL, ROLL>(s, q[threadIdx.x], shearupdate);
+      const int rem = qn_s - kPairTile;
+      __syncthreads();
+      const int v = threadIdx.x < rem ? q[kPairTile + threadIdx.x] : 0;
+      __syncthreads();
+      if (threadIdx.x < rem) q[threadIdx.x] = v;
+      if (threadIdx.x == 0) qn_s = rem;
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x < qn_s) pair_entry<NORMAL, ROLL>(s, q[threadIdx.x], shearupdate);
 }
 
 // ----------------------------------------------------------------------------
@@ -1297,7 +1414,8 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
   k_zero_gated<<<gN, B, 0, st>>>(s, s.rev_count, s.nmax + 1);
   k_zero_gated<<<gN, B, 0, st>>>(s, s.rev_fill, s.nmax + 1);
   k_pairs<true><<<gN, B, 0, st>>>(s);
-  nl += 3 + scan_exclusive(s, s.rev_count, s.pairs[1].rev_start, s.nmax + 1, s.scan_tmp, true, st);
+  k_pair_init<<<gP, B, 0, st>>>(s);
+  nl += 4 + scan_exclusive(s, s.rev_count, s.pairs[1].rev_start, s.nmax + 1, s.scan_tmp, true, st);
   k_rev_fill<<<gP, B, 0, st>>>(s);
   k_rev_sort<<<gN, B, 0, st>>>(s);
   k_copy_pairs<<<grid_for((long)s.pcap > s.nmax + 1 ? s.pcap : s.nmax + 1, B, lc.max_grid), B, 0, st>>>(s);
@@ -1389,11 +1507,25 @@ cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st,
   return e;
 }
 
+// The wall kernel walks a short list (atoms near walls) with long per-atom
+// dependency chains; it is launched with the device's highest priority so
+// that its blocks start before those of the pair kernel beside it.
 int launch_wall_force(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t st) {
   if (s.nmeshes == 0 && s.nplanes == 0) return 0;
-  const int g = grid_for(s.nmax, 128, lc.max_grid);
-  if (s.normal == kHertz) k_wall_force<kHertz><<<g, 128, 0, st>>>(s, shearupdate);
-  else k_wall_force<kHooke><<<g, 128, 0, st>>>(s, shearupdate);
+  int lo = 0, hi = 0;
+  cudaDeviceGetStreamPriorityRange(&lo, &hi);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid_for(s.nmax, 128, std::min(lc.max_grid, 304)));
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributePriority;
+  attr[0].val.priority = hi;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (s.normal == kHertz) cudaLaunchKernelEx(&cfg, k_wall_force<kHertz>, s, shearupdate);
+  else cudaLaunchKernelEx(&cfg, k_wall_force<kHooke>, s, shearupdate);
   return 1;
 }
 
@@ -1431,6 +1563,16 @@ int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t
     } else {
       if (s.rolling) k_pair<kHooke, true, true><<<g, B, 0, st>>>(s, shearupdate);
       else k_pair<kHooke, false, true><<<g, B, 0, st>>>(s, shearupdate);
+    }
+    return 1;
+  }
+  if (s.cdf == 1.0) {
+    if (s.normal == kHertz) {
+      if (s.rolling) k_pair_pf<kHertz, true><<<g, B, 0, st>>>(s, shearupdate);
+      else k_pair_pf<kHertz, false><<<g, B, 0, st>>>(s, shearupdate);
+    } else {
+      if (s.rolling) k_pair_pf<kHooke, true><<<g, B, 0, st>>>(s, shearupdate);
+      else k_pair_pf<kHooke, false><<<g, B, 0, st>>>(s, shearupdate);
     }
     return 1;
   }
