@@ -140,6 +140,32 @@ int dem_set_bond_params(dem_handle *h, const double *tables, const dem_bond_sett
 int dem_add_plane(dem_handle *h, int axis, double pos, int wall_type, int rolling_model,
                   int *wall_id);
 
+/* A primitive plane whose position depends on the atom's type (pos_by_type,
+ * ntypes+1 entries, entry 0 unused) and whose wall type is the atom's own
+ * type: the floors of independent systems stacked into one handle (the
+ * batched ensemble), each system with its own atom type and material.  No
+ * reference counterpart (the reference runs one process per system). */
+int dem_add_plane_per_type(dem_handle *h, int axis, const double *pos_by_type, int rolling_model,
+                           int *wall_id);
+
+/* Batched ensemble: the handle holds nsys independent systems that share the
+ * box (boundaries, size) and the model; system k is made of the atoms of
+ * type k+1 (each system one material, the type-pair tables' diagonal), its
+ * walls are per-type planes (dem_add_plane_per_type).  Every system keeps
+ * its own coordinates; its neighbour cells form their own block, so no pair
+ * crosses systems.  All systems advance together in one step loop; a
+ * neighbour rebuild, decided over all atoms, rebuilds every system.  After
+ * dem_set_pair_params (ntypes == nsys), before dem_upload_atoms; no meshes. */
+int dem_set_ensemble(dem_handle *h, int nsys);
+
+/* Launch shape and neighbour-cell size, set before dem_upload_atoms:
+ * grid-stride kernels use at most blocks_per_sm blocks per SM (default 8);
+ * cell edges are cell_scale x the neighbour cutoff (default 1, range 1..4).
+ * Neither changes the pair set; the cell size changes the order in which a
+ * list is built, hence summation order (rounding only).  Used by the
+ * ensemble autotuner. */
+int dem_set_tuning(dem_handle *h, int blocks_per_sm, double cell_scale);
+
 /* fix mesh/surface FILE type WALL_TYPE + fix wall/gran ... mesh n_meshes 1
  * meshes ID (src/fix_mesh_surface.cpp, src/fix_wall_gran.cpp:803-982):
  * nodes is ntri*9 (triangle t, node q, coordinate d at 9*t+3*q+d) in element

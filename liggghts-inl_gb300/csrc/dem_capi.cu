@@ -53,6 +53,8 @@ struct dem_handle {
   int graph_kps = 0, graph_kpr = 0;
   std::vector<MeshHost> mesh_host;
   std::vector<double> bond_tables;  // host copy for the cutoff derivation
+  double cell_scale = 1.0;          // neighbour cell edge / cutneighmax (dem_set_tuning)
+  int ens_nsys = 0;                 // batched ensemble: number of systems (dem_set_ensemble)
   dem_bond_settings bond_settings{};
 };
 
@@ -480,10 +482,56 @@ int dem_add_plane(dem_handle *h, int axis, double pos, int wall_type, int rollin
   Plane &p = h->s.planes[h->s.nplanes];
   p.axis = axis;
   p.pos = pos;
+  p.pos_t = nullptr;
   p.wall_type = wall_type;
   p.rolling = rolling_model == DEM_ROLLING_CDT ? 1 : 0;
   if (wall_id) *wall_id = h->s.nplanes;
   h->s.nplanes++;
+  h->sys_gen++;
+  return DEM_OK;
+}
+
+int dem_add_plane_per_type(dem_handle *h, int axis, const double *pos_by_type, int rolling_model,
+                           int *wall_id) {
+  if (!h || axis < 0 || axis > 2 || !pos_by_type) return DEM_ERR_BAD_ARG;
+  if (!h->have_params) return fail(h, DEM_ERR_BAD_ARG, "set pair parameters first");
+  if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "add walls before uploading atoms");
+  if (h->s.nplanes >= kMaxPlanes) return fail(h, DEM_ERR_BAD_ARG, "too many primitive walls");
+  double *dpos = nullptr;
+  CUDA_TRY(h, dalloc(h->allocs_misc, &dpos, (size_t)h->s.ntypes + 1));
+  CUDA_TRY(h, cudaMemcpy(dpos, pos_by_type, ((size_t)h->s.ntypes + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  Plane &p = h->s.planes[h->s.nplanes];
+  p.axis = axis;
+  p.pos = pos_by_type[1];
+  p.pos_t = dpos;
+  p.wall_type = 0;
+  p.rolling = rolling_model == DEM_ROLLING_CDT ? 1 : 0;
+  if (wall_id) *wall_id = h->s.nplanes;
+  h->s.nplanes++;
+  h->sys_gen++;
+  return DEM_OK;
+}
+
+int dem_set_ensemble(dem_handle *h, int nsys) {
+  if (!h || nsys < 1) return DEM_ERR_BAD_ARG;
+  if (!h->have_params || h->s.ntypes != nsys)
+    return fail(h, DEM_ERR_BAD_ARG, "an ensemble of nsys systems needs ntypes == nsys (system k = type k+1)");
+  if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "declare the ensemble before uploading atoms");
+  if (h->s.nmeshes > 0) return fail(h, DEM_ERR_UNSUPPORTED, "mesh walls are not supported in ensembles");
+  h->ens_nsys = nsys;
+  h->sys_gen++;
+  return DEM_OK;
+}
+
+int dem_set_tuning(dem_handle *h, int blocks_per_sm, double cell_scale) {
+  if (!h || blocks_per_sm < 1 || blocks_per_sm > 64 || !(cell_scale >= 1.0) || cell_scale > 4.0)
+    return DEM_ERR_BAD_ARG;
+  if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "set the tuning before uploading atoms");
+  cudaDeviceProp prop;
+  int sms = 152;
+  if (cudaGetDeviceProperties(&prop, h->device) == cudaSuccess) sms = prop.multiProcessorCount;
+  h->lc.max_grid = sms * blocks_per_sm;
+  h->cell_scale = cell_scale;
   h->sys_gen++;
   return DEM_OK;
 }
@@ -653,21 +701,23 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
   }
   long ncell = 1;
   for (int d = 0; d < 3; d++) {
-    long nc = (long)std::floor(s.prd[d] / (s.cutneighmax * (1.0 + 1e-9)));
+    long nc = (long)std::floor(s.prd[d] / (s.cutneighmax * h->cell_scale * (1.0 + 1e-9)));
     if (nc < 1) nc = 1;
     if (s.periodic[d] && nc < 3)
       return fail(h, DEM_ERR_BOX, "periodic box dimension shorter than 3 neighbour cutoffs");
     s.nc[d] = (int)std::min<long>(nc, 4096);
     ncell *= s.nc[d];
   }
-  while (ncell > kMaxCells) {  // very sparse boxes: coarser cells stay conservative
+  const long nsys = std::max(1, h->ens_nsys);
+  while (ncell * nsys > kMaxCells) {  // very sparse boxes: coarser cells stay conservative
     int d = (s.nc[0] >= s.nc[1] && s.nc[0] >= s.nc[2]) ? 0 : (s.nc[1] >= s.nc[2] ? 1 : 2);
     if (s.periodic[d] && s.nc[d] <= 3) break;
     s.nc[d] = std::max(s.periodic[d] ? 3 : 1, s.nc[d] / 2);
     ncell = (long)s.nc[0] * s.nc[1] * s.nc[2];
   }
   for (int d = 0; d < 3; d++) s.csz[d] = s.prd[d] / s.nc[d];
-  s.ncell = (int)ncell;
+  s.ens_ncell = h->ens_nsys > 0 ? (int)ncell : 0;
+  s.ncell = (int)(ncell * nsys);
   // FixNeighlistMesh::pre_force distmax/skin (static meshes), src/fix_neighlist_mesh.cpp:249-264
   for (int k = 0; k < s.nmeshes; k++) {
     MeshDev &M = s.meshes[k];

@@ -109,9 +109,14 @@ struct Ctrl {
 struct Plane {
   int axis;
   double pos;
-  int wall_type;
+  int wall_type;      // 0: the wall takes each atom's own type (per-type planes)
   int rolling;
+  const double *pos_t;  // per-atom-type position [ntypes+1] (stacked ensembles) or nullptr
 };
+
+__device__ __forceinline__ double plane_pos(const Plane &pl, int type) {
+  return pl.pos_t ? pl.pos_t[type] : pl.pos;
+}
 
 // Triangle-mesh wall (fix mesh/surface + fix wall/gran mesh).
 constexpr int kMaxMeshes = 4;
@@ -162,6 +167,9 @@ struct Sys {
   int ntypes;
   int nmax, pcap;
   int ncell, nc[3];
+  // batched ensemble: independent systems, system k = atom type k+1, each
+  // with its own block of ens_ncell neighbour cells (0: one system)
+  int ens_ncell;
   double csz[3];
   double boxlo[3], boxhi[3], prd[3];
   int periodic[3];

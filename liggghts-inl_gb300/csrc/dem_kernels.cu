@@ -212,7 +212,7 @@ __global__ void k_cell_count(Sys s) {
     int cell = s.ncell;
     if (!lost) {
       const int cx = cell_coord(s, xv[0], 0), cy = cell_coord(s, xv[1], 1), cz = cell_coord(s, xv[2], 2);
-      cell = cx + s.nc[0] * (cy + s.nc[1] * cz);
+      cell = cx + s.nc[0] * (cy + s.nc[1] * cz) + (s.ens_ncell ? (A.type[i] - 1) * s.ens_ncell : 0);
     }
     s.pcount[i] = cell;  // reused as per-atom cell id until the pair count
     atomicAdd(&s.cell_count[cell], 1);
@@ -280,7 +280,7 @@ __global__ void k_permute(Sys s) {
         B.whist[(size_t)(w * 3 + d) * s.nmax + i] = A.whist[(size_t)(w * 3 + d) * s.nmax + o];
       const double pos = s.planes[w].axis == 0 ? x : (s.planes[w].axis == 1 ? y : z);
       const double dMax = r + s.skin;
-      const double dist = pos - s.planes[w].pos;
+      const double dist = pos - plane_pos(s.planes[w], A.type[o]);
       const double absdist = (dist > 0.0) ? dist : -dist;
       if (absdist <= dMax) bits |= (uint8_t)(1u << w);
     }
@@ -581,6 +581,7 @@ __global__ void k_pairs(Sys s) {
     const double radi = A.r[i];
     const int ci[3] = {cell_coord(s, xi, 0), cell_coord(s, yi, 1), cell_coord(s, zi, 2)};
     const float4 pi = s.xf[i];
+    const int cell_base = s.ens_ncell ? (A.type[i] - 1) * s.ens_ncell : 0;
     const float cdff = (float)s.cdf, skinf = (float)s.skin;
     const float hi_f = 1.0f + s.pf_margin, lo_f = 1.0f - s.pf_margin;
     int cnt = 0;
@@ -608,7 +609,7 @@ __global__ void k_pairs(Sys s) {
           }
           if (skip) continue;
           const int code = (sv[0] + 1) + 3 * (sv[1] + 1) + 9 * (sv[2] + 1);
-          const int cell = cc[0] + s.nc[0] * (cc[1] + s.nc[1] * cc[2]);
+          const int cell = cc[0] + s.nc[0] * (cc[1] + s.nc[1] * cc[2]) + cell_base;
           const int jb = s.cell_start[cell], je = s.cell_start[cell + 1];
           const float sxf = sv[0] * (float)s.prd[0], syf = sv[1] * (float)s.prd[1], szf = sv[2] * (float)s.prd[2];
           for (int j = jb; j < je; j++) {
@@ -1137,15 +1138,16 @@ __device__ __forceinline__ void plane_contact(const Sys &s, const AtomArrays &A,
   const Plane &pl = s.planes[w];
   const int ax = pl.axis, ay = (ax + 1) % 3, az = (ax + 2) % 3;
   const double radi = A.r[i];
+  const double ppos = plane_pos(pl, A.type[i]);
   double delta[3];
   double deltan;
   // Plane<dim>::resolveContact, src/primitive_wall_definitions.h:123-140
-  if (xv[ax] > pl.pos) {
-    delta[ax] = pl.pos - xv[ax];
-    deltan = xv[ax] - pl.pos - radi;
+  if (xv[ax] > ppos) {
+    delta[ax] = ppos - xv[ax];
+    deltan = xv[ax] - ppos - radi;
   } else {
-    delta[ax] = pl.pos - xv[ax];
-    deltan = pl.pos - xv[ax] - radi;
+    delta[ax] = ppos - xv[ax];
+    deltan = ppos - xv[ax] - radi;
   }
   delta[ay] = 0.;
   delta[az] = 0.;
@@ -1155,8 +1157,8 @@ __device__ __forceinline__ void plane_contact(const Sys &s, const AtomArrays &A,
   const double cdm1 = s.cdf - 1.0;
   if (deltan <= 0 || deltan < cdm1 * radi) {
     const double vwall[3] = {0., 0., 0.};
-    wall_force<NORMAL>(s, A, i, deltan, delta, vwall, pl.wall_type, pl.rolling != 0, h, hs,
-                       shearupdate, v, om, fx, fy, fz, tx, ty, tz);
+    wall_force<NORMAL>(s, A, i, deltan, delta, vwall, pl.wall_type ? pl.wall_type : A.type[i],
+                       pl.rolling != 0, h, hs, shearupdate, v, om, fx, fy, fz, tx, ty, tz);
   } else {
     h[0] = 0.0; h[hs] = 0.0; h[2 * hs] = 0.0;
   }

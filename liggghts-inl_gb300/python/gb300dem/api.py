@@ -84,6 +84,9 @@ def load(build=True):
     L.dem_set_bond_params.argtypes = [P, P, ctypes.POINTER(DemBondSettings)]
     L.dem_derive_hertz_tables.argtypes = [I] + [P] * 7
     L.dem_add_plane.argtypes = [P, I, ctypes.c_double, I, I, P]
+    L.dem_add_plane_per_type.argtypes = [P, I, P, I, P]
+    L.dem_set_tuning.argtypes = [P, I, ctypes.c_double]
+    L.dem_set_ensemble.argtypes = [P, I]
     L.dem_upload_atoms.argtypes = [P, I] + [P] * 7
     L.dem_add_mesh.argtypes = [P, I, P, I, I, P, P, P]
     L.dem_mesh_topology.argtypes = [I, P, P, P]
@@ -170,6 +173,14 @@ class DemSystem:
             self._check(L.dem_set_bond_params(self.h, _p(bt), ctypes.byref(st)))
         for (axis, pos, wtype, roll) in case.get("planes", []):
             self._check(L.dem_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll), None))
+        for (axis, pos_t, roll) in case.get("planes_per_type", []):
+            pt = np.ascontiguousarray(pos_t, dtype=np.float64)
+            self._check(L.dem_add_plane_per_type(self.h, int(axis), _p(pt), int(roll), None))
+        if case.get("tuning") is not None:
+            bps, cs = case["tuning"]
+            self._check(L.dem_set_tuning(self.h, int(bps), float(cs)))
+        if case.get("ensemble"):
+            self._check(L.dem_set_ensemble(self.h, int(case["ensemble"])))
         self._meshkeep = []
         self._nodes_shape = []
         for m in case.get("meshes", []):

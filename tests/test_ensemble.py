@@ -1,0 +1,79 @@
+"""Batched ensemble runner (gb300dem.ensemble): packing on the CPU, and on
+the GPU each packed system against the oracle running that system alone.
+
+The ensemble decides neighbour rebuilds for all systems together; with
+`neigh_modify every 1 check no` (a rebuild every step) the schedule is the
+same as each system's own, so every system must match its standalone run:
+forces within FORCE_RTOL per step while the trajectories agree to rounding,
+pair sets bit-exact."""
+import numpy as np
+import pytest
+
+from golden_io import FORCE_RTOL, TRAJ_RTOL, canonical_pairs, compare_pairs, max_rel, sort_by_tag
+
+
+def _systems(n=5, neigh=(1, 0, 0)):
+    from gb300dem import ensemble
+    sy = ensemble.settling_systems(11, n, nmin=150, nmax=500)
+    for k, s in enumerate(sy):
+        s["neigh"] = neigh
+        rng = np.random.default_rng(100 + k)
+        s["atoms"]["v"] = rng.uniform(-0.5, 0.5, size=s["atoms"]["x"].shape)
+    return sy
+
+
+def test_pack_layout():
+    from gb300dem import ensemble
+    sy = _systems()
+    case, lay = ensemble.pack(sy)
+    a = case["atoms"]
+    assert len(np.unique(a["tag"])) == len(a["tag"])
+    assert case["ntypes"] == len(sy) == case["ensemble"]
+    for k, s in enumerate(sy):
+        t = k + 1
+        sel = a["type"] == t
+        assert sel.sum() == len(s["atoms"]["tag"])
+        for name in ("Yeff", "Geff", "betaeff", "coeffFrict"):
+            assert case[name][t, t] == s[name][1, 1]
+        # every system keeps its own coordinates, bit for bit
+        assert np.array_equal(a["x"][sel], s["atoms"]["x"])
+        assert np.array_equal(a["tag"][sel] - lay["offsets"][k], s["atoms"]["tag"])
+        assert case["planes_per_type"][0][1][t] == s["planes"][0][1]
+
+
+@pytest.mark.gpu
+def test_ensemble_systems_match_standalone_oracle():
+    from gb300dem import ensemble
+    from oracle.binding import Oracle
+    sy = _systems()
+    e = ensemble.Ensemble(sy)
+    e.setup()
+    orcs = [Oracle(s) for s in sy]
+    for o in orcs:
+        o.setup()
+    done = 0
+    for chunk in (1, 4, 5, 20):
+        e.step(chunk)
+        for o in orcs:
+            o.run(chunk)
+        done += chunk
+        allp = e.sys.pairs()
+        for k, (s, o) in enumerate(zip(sy, orcs)):
+            a, b = e.system_atoms(k), sort_by_tag(o.atoms())
+            assert np.array_equal(a["tag"], b["tag"])
+            ftol = FORCE_RTOL if done <= 10 else 1e-7
+            assert max_rel(a["f"], b["f"]) < ftol, (k, done, max_rel(a["f"], b["f"]))
+            assert max_rel(a["torque"], b["torque"]) < ftol, (k, done)
+            assert max_rel(a["x"], b["x"], scale=0.05) < TRAJ_RTOL
+            tag0 = e.layout["offsets"][k]
+            ntag = len(s["atoms"]["tag"])
+            sel = (allp["tag_i"] > tag0) & (allp["tag_i"] <= tag0 + ntag)
+            gp = canonical_pairs(allp["tag_i"][sel] - tag0, allp["tag_j"][sel] - tag0, allp["shift"][sel],
+                                 allp["flag"][sel], allp["hist"][sel])
+            po = o.pairs()
+            op = canonical_pairs(po["tag_i"], po["tag_j"], po["shift"], po["flag"], po["hist"])
+            missing, extra, flagmis, hm = compare_pairs(gp, op)
+            assert not missing and not extra and not flagmis, (k, done)
+            assert hm < 1e-9, (k, done, hm)
+    assert e.stats()["nrebuilds"] == done + 1
+    e.close()
