@@ -332,13 +332,63 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def run_ensemble(args):
+    """Batched ensemble (256 settling columns, N_k ~ U[2000, 20000]): the
+    packed ensemble against the same systems run one at a time through the
+    plain path (one handle per system, same library, same step count)."""
+    from gb300dem import api, ensemble
+    nsys = max(2, int(round(256 * args.scale)))
+    systems = ensemble.settling_systems(2024, nsys)
+    ntot = sum(len(s["atoms"]["tag"]) for s in systems)
+    best, table = ensemble.autotune(systems[: max(2, nsys // 4)], steps=20, warm=3)
+    e = ensemble.Ensemble(systems, tuning=best)
+    e.setup()
+    e.step(args.warmup)
+    clocks = Clocks()
+    clocks.start()
+    e.step(args.steps)
+    cl = clocks.stop()
+    st = e.stats()
+    ens_ms = st["last_step_ms"]
+    value = ntot * args.steps / (ens_ms * 1e-3)
+    e.close()
+    # plain path: each system alone, the same number of steps
+    plain_ms, plain_ps = 0.0, 0
+    for s in systems:
+        g = api.DemSystem(s)
+        g.setup()
+        g.step(args.warmup)
+        g.step(args.steps)
+        plain_ms += g.stats()["last_step_ms"]
+        plain_ps += len(s["atoms"]["tag"]) * args.steps
+        g.close()
+    plain = plain_ps / (plain_ms * 1e-3)
+    line = {"metric": "particle-steps/s (batched ensemble, %d settling columns)" % nsys, "value": value,
+            "unit": "particle-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ens_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)", "impl": "gb300",
+            "config": {"workload": "ensemble%d" % nsys, "systems": nsys, "atoms": ntot,
+                       "description": "settling columns, N_k ~ U[2000, 20000], r U[0.9, 1.1] mm, "
+                                      "E log-U[1e6, 1e8] Pa, e U[0.3, 0.95], mu U[0.1, 0.9], box "
+                                      "0.05 x 0.05 x 0.3 m periodic x/y, floor, Hertz + history, dt 1e-6",
+                       "tuning": {"blocks_per_sm": best[0], "cell_scale": best[1]},
+                       "rebuilds_total": st["nrebuilds"]},
+            "plain_one_at_a_time": {"value": plain, "unit": "particle-steps/s",
+                                    "note": "the same systems, one handle each, run in turn"},
+            "ensemble_over_plain": value / plain,
+            "autotune": [{"blocks_per_sm": t[0][0], "cell_scale": t[0][1], "ms_per_step": t[1]}
+                         for t in table],
+            "clocks": cl}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hopper1m", choices=["hopper1m", "column1m"])
+    ap.add_argument("--workload", default="hopper1m", choices=["hopper1m", "column1m", "ensemble256"])
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0,
@@ -348,6 +398,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "ensemble256":
+        run_ensemble(args)
     else:
         run_gb300(args)
 
