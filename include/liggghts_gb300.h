@@ -286,6 +286,70 @@ int dem_measure_fp64_peak(double *tflops);
 const char *dem_last_error(dem_handle *h);
 const char *dem_version(void);
 
+/* ------------------------------------------------------------------------
+ * Discrete adjoint (no counterpart in the reference, which has no
+ * derivatives).  Gradients of a scalar loss of the final state of an
+ * N-step run with respect to Young's modulus, restitution, friction and
+ * every particle radius, by reverse-mode differentiation of the exact
+ * discrete timestep: Verlet::setup + N Verlet steps (src/verlet.cpp:281-389)
+ * of FixNVESphere, PairGran Hertz + tangential history (cdf 1, no rolling,
+ * no cohesion), FixGravity and FixWallGran primitive planes, one atom type
+ * and one material (Yeff/Geff/betaeff of the material against itself,
+ * src/global_properties.cpp).  Masses follow the radii: m = 4/3 pi r^3 rho.
+ * The neighbour list is rebuilt every `segment` steps, after the drift of
+ * steps segment, 2*segment, ... (neigh_modify every segment delay 0 check
+ * no); each rebuild is a checkpoint, so memory grows as N/segment states
+ * plus one segment of tape (segment ~ sqrt(N) minimises it).  Within a
+ * segment no atom may move more than skin/2 from its position at the build
+ * (DEM_ERR_BAD_ARG otherwise, with a message).  The loss:
+ *   w_ke * (translational + rotational kinetic energy)
+ * + w_height * (mean z - height_target)^2
+ * + w_wallforce * (normal force of plane wall_id on the atoms, summed over
+ *                  atoms at the last step - wallforce_target)^2
+ * Gradients are exact for this piecewise-smooth map away from switch
+ * points (contacts opening or closing, stick/slip transitions).
+ * ------------------------------------------------------------------------ */
+typedef struct dem_adjoint_config {
+  double boxlo[3], boxhi[3];
+  int periodic[3];
+  double dt, skin;
+  double density;       /* FixDensity / set density: rmass = 4/3 pi r^3 rho */
+  double poisson;       /* property/global poissonsRatio */
+  int gravity_on;
+  double gravity[3];    /* acceleration vector (fix gravity magnitude * direction) */
+  int nplanes;          /* <= 8 primitive planes (wall/gran ... primitive type 1 [xyz]plane) */
+  int plane_axis[8];
+  double plane_pos[8];
+} dem_adjoint_config;
+
+typedef struct dem_adjoint_loss {
+  double w_ke;
+  double w_height, height_target;
+  double w_wallforce, wallforce_target;
+  int wall_id;          /* plane index for the wall-force term, -1 none */
+} dem_adjoint_loss;
+
+typedef struct dem_adjoint dem_adjoint;
+int dem_adjoint_create(const dem_adjoint_config *cfg, dem_adjoint **out);
+int dem_adjoint_destroy(dem_adjoint *h);
+/* initial state (host arrays): x, v, omega n*3, radius n (the radii define the
+ * neighbour cells; runs may use radii up to 1 % larger) */
+int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *v, const double *omega,
+                          const double *radius);
+/* forward only: loss of the final state; radius NULL = the initial radii */
+int dem_adjoint_forward(dem_adjoint *h, double E, double restitution, double friction, const double *radius,
+                        int nsteps, int segment, const dem_adjoint_loss *loss, double *loss_out);
+/* forward + backward: loss and its gradients (grad_radius n entries) */
+int dem_adjoint_gradient(dem_adjoint *h, double E, double restitution, double friction, const double *radius,
+                         int nsteps, int segment, const dem_adjoint_loss *loss, double *loss_out,
+                         double *grad_E, double *grad_restitution, double *grad_friction, double *grad_radius);
+/* final state of the last run (host arrays, n*3 each, NULL to skip) */
+int dem_adjoint_download(dem_adjoint *h, double *x, double *v, double *omega);
+/* device time of the last run's forward and backward passes, its segment
+ * count and largest list */
+int dem_adjoint_times(dem_adjoint *h, double *forward_ms, double *backward_ms, int *segments, int *max_pairs);
+const char *dem_adjoint_last_error(dem_adjoint *h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,1243 @@
+// Discrete adjoint of the sphere-DEM timestep (Hertz + tangential history,
+// primitive planes, gravity, nve/sphere) with sqrt(N) checkpointing.
+//
+// Forward model: the reference's Verlet step (src/verlet.cpp:281-389) with
+// FixNVESphere (src/fix_nve_sphere.cpp:120-215), PairGran with the Hertz +
+// tangential-history contact model, FixWallGran primitive planes and
+// FixGravity:
+//   vh = v + a F, wh = w + b T, x' = x + dt vh        initial_integrate
+//   [rebuild: pbc wrap, neighbour list, history carried to the new list]
+//   F', T', shear' = forces(x', vh, wh, shear)        pair + gravity + walls
+//   v' = vh + a F', w' = wh + b T'                    final_integrate
+// with a = dt/2/m, b = dt/2/(0.4 r^2 m), m = 4/3 pi r^3 rho; Verlet::setup
+// evaluates the forces of the initial state without history update.  The
+// neighbour list is rebuilt every L steps, at steps L, 2L, ... after the
+// drift (neigh_modify every L delay 0 check no): the same schedule the
+// reference runs with those settings.  Atoms keep their input order (no
+// spatial sort), so the adjoint state indexes the same atoms over the whole
+// horizon.
+//
+// The steps that share one list form a segment.  The forward pass stores one
+// checkpoint per segment: the state before the segment's first drift, the
+// segment's neighbour list and its history as carried at the build.  The
+// backward pass replays each segment from its checkpoint, recording the
+// per-step tape (positions and half-step velocities the forces saw, the
+// history before each force evaluation, the forces), then runs the reverse
+// kernels over the tape.  Memory: one checkpoint per segment plus one
+// segment of tape, O(sqrt(N)) states for L ~ sqrt(N).  The forward pass
+// checks that no atom moves more than skin/2 away from its position at the
+// build within a segment (the list then holds every touching pair).
+//
+// History carry-over follows FixContactHistory (src/fix_contact_history.cpp
+// pre_exchange/post_neighbor): a new entry (owner i, partner j) takes the
+// history of i's old entry with partner j, else (negated) that of j's old
+// local entry with partner i, when the pair touches at the build and that
+// old entry carries history.  The backward pass maps the history adjoints
+// back through the same map.
+//
+// Reverse-mode arithmetic is deterministic: pair results are gathered per
+// atom in list order (own row, then reverse list), parameter gradients are
+// reduced per block and then summed in block order.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "../../include/liggghts_gb300.h"
+#include "adjoint_law.cuh"
+#include "dem_device.cuh"
+#include "dem_kernels.h"
+
+using namespace gb300;
+
+namespace {
+
+constexpr int kAB = 256;
+constexpr int kMaxGrid = 152 * 16;
+
+struct AList {
+  int np = 0;
+  int *pi = nullptr, *pj = nullptr, *row = nullptr, *rev_start = nullptr, *rev = nullptr;
+  int *carry = nullptr;     // old entry e (>= 0), -(e + 2) for a flipped copy, -1 none
+  uint8_t *sh = nullptr;    // image code of the partner
+  uint8_t *flag = nullptr;  // entry carries history (carried or touched)
+  double *shear = nullptr;  // [3*p+k], evolving
+};
+
+struct ADev {
+  int n;
+  double dt, skin, lo[3], hi[3], prd[3];
+  int per[3];
+  double g[3];
+  int gravity_on;
+  int nplanes;
+  int pax[8];
+  double ppos[8];
+  double Y, G, beta, mu;
+  double dtf, dtfrot;
+  double *x, *v, *w, *F, *T, *r, *m, *ws;  // ws [(w*n + i)*3 + k]
+  // list in use
+  int np;
+  const int *pi, *pj, *row, *rev_start, *rev;
+  const uint8_t *sh;
+  uint8_t *flag;
+  double *shear;
+  // pair outputs of the current force evaluation
+  double *pF, *pTi, *pTj;
+  uint8_t *touch;
+  // cells
+  int nc[3];
+  double csz[3];
+  int ncell;
+  int *cell_of, *cell_count, *cell_start, *cell_fill, *order, *pcount;
+  int *err;  // [0]: an atom moved more than skin/2 from its build position
+};
+
+__device__ __forceinline__ int a_cell_coord(const ADev &s, double x, int d) {
+  int c = (int)((x - s.lo[d]) / s.csz[d]);
+  c = c < 0 ? 0 : c;
+  c = c >= s.nc[d] ? s.nc[d] - 1 : c;
+  return c;
+}
+
+__device__ __forceinline__ void a_image(const ADev &s, int code, double xj[3]) {
+  if (code == kNoShift) return;
+  const int sv[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
+  for (int d = 0; d < 3; d++)
+    if (sv[d]) xj[d] = __dadd_rn(xj[d], sv[d] * s.prd[d]);
+}
+
+#define AGRID(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
+
+// ---------------------------------------------------------------- list build
+// Domain::pbc (src/domain.cpp:550-650) for periodic dimensions
+__global__ void ka_wrap(ADev s) {
+  AGRID(i, s.n) {
+    for (int d = 0; d < 3; d++) {
+      if (!s.per[d]) continue;
+      double x = s.x[3 * i + d];
+      if (x < s.lo[d]) x += s.prd[d];
+      if (x >= s.hi[d]) {
+        x -= s.prd[d];
+        if (x < s.lo[d]) x = s.lo[d];
+      }
+      s.x[3 * i + d] = x;
+    }
+  }
+}
+__global__ void ka_cell(ADev s) {
+  AGRID(i, s.n) {
+    int c[3];
+    for (int d = 0; d < 3; d++) c[d] = a_cell_coord(s, s.x[3 * i + d], d);
+    const int cell = c[0] + s.nc[0] * (c[1] + s.nc[1] * c[2]);
+    s.cell_of[i] = cell;
+    atomicAdd(&s.cell_count[cell], 1);
+  }
+}
+__global__ void ka_scatter(ADev s) {
+  AGRID(i, s.n) {
+    const int c = s.cell_of[i];
+    s.order[s.cell_start[c] + atomicAdd(&s.cell_fill[c], 1)] = i;
+  }
+}
+// ascending atom index within a cell: the list order does not depend on
+// the order of the atomics above
+__global__ void ka_cellsort(ADev s) {
+  AGRID(c, s.ncell) {
+    const int b = s.cell_start[c], e = s.cell_start[c + 1];
+    for (int k = b + 1; k < e; k++) {
+      const int v = s.order[k];
+      int m = k - 1;
+      while (m >= b && s.order[m] > v) {
+        s.order[m + 1] = s.order[m];
+        m--;
+      }
+      s.order[m + 1] = v;
+    }
+  }
+}
+
+// granular half list in input order: local pairs once (owner = lower index),
+// periodic images as directed entries of each owner; cutoff ri + rj + skin
+template <bool FILL>
+__global__ void ka_pairs(ADev s, int *pi, int *pj, uint8_t *shc, const int *row) {
+  AGRID(i, s.n) {
+    const double xi[3] = {s.x[3 * i], s.x[3 * i + 1], s.x[3 * i + 2]};
+    const double ri = s.r[i];
+    int ci[3];
+    for (int d = 0; d < 3; d++) ci[d] = a_cell_coord(s, xi[d], d);
+    int cnt = 0, out = FILL ? row[i] : 0;
+    const int out_end = FILL ? row[i + 1] : 0;
+    for (int oz = -1; oz <= 1; oz++)
+      for (int oy = -1; oy <= 1; oy++)
+        for (int ox = -1; ox <= 1; ox++) {
+          const int o[3] = {ox, oy, oz};
+          int cc[3], sv[3] = {0, 0, 0};
+          bool skip = false;
+          for (int d = 0; d < 3; d++) {
+            cc[d] = ci[d] + o[d];
+            if (cc[d] < 0) {
+              if (!s.per[d]) skip = true;
+              cc[d] += s.nc[d];
+              sv[d] = -1;
+            } else if (cc[d] >= s.nc[d]) {
+              if (!s.per[d]) skip = true;
+              cc[d] -= s.nc[d];
+              sv[d] = 1;
+            }
+          }
+          if (skip) continue;
+          const int code = (sv[0] + 1) + 3 * (sv[1] + 1) + 9 * (sv[2] + 1);
+          const int cell = cc[0] + s.nc[0] * (cc[1] + s.nc[1] * cc[2]);
+          for (int q = s.cell_start[cell]; q < s.cell_start[cell + 1]; q++) {
+            const int j = s.order[q];
+            if (code == kNoShift && j <= i) continue;
+            double xj[3] = {s.x[3 * j], s.x[3 * j + 1], s.x[3 * j + 2]};
+            a_image(s, code, xj);
+            const double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+            const double cs = ri + s.r[j] + s.skin;
+            if (dx * dx + dy * dy + dz * dz > cs * cs) continue;
+            if (!FILL) {
+              cnt++;
+              continue;
+            }
+            if (out >= out_end) continue;
+            pi[out] = i;
+            pj[out] = j;
+            shc[out] = (uint8_t)code;
+            out++;
+          }
+        }
+    if (!FILL) s.pcount[i] = cnt;
+  }
+}
+
+// reverse lists over all entries (periodic included), ascending per partner
+__global__ void ka_rev_count(int np, const int *pj, int *cnt) {
+  AGRID(p, np) atomicAdd(&cnt[pj[p]], 1);
+}
+__global__ void ka_rev_fill(int np, const int *pj, const int *start, int *fill, int *rev) {
+  AGRID(p, np) rev[start[pj[p]] + atomicAdd(&fill[pj[p]], 1)] = p;
+}
+__global__ void ka_rev_sort(int n, const int *start, int *rev) {
+  AGRID(i, n) {
+    const int b = start[i], e = start[i + 1];
+    for (int k = b + 1; k < e; k++) {
+      const int v = rev[k];
+      int m = k - 1;
+      while (m >= b && rev[m] > v) {
+        rev[m + 1] = rev[m];
+        m--;
+      }
+      rev[m + 1] = v;
+    }
+  }
+}
+
+// history carried from the previous list (see the file comment); also sets
+// the new entries' flags
+__global__ void ka_carry(ADev s, AList nw, AList old) {
+  AGRID(p, nw.np) {
+    const int i = nw.pi[p], j = nw.pj[p], code = nw.sh[p];
+    int e = -1;
+    double sgn = 1.0;
+    double xj[3] = {s.x[3 * j], s.x[3 * j + 1], s.x[3 * j + 2]};
+    a_image(s, code, xj);
+    const double dx = s.x[3 * i] - xj[0], dy = s.x[3 * i + 1] - xj[1], dz = s.x[3 * i + 2] - xj[2];
+    const double rs = s.r[i] + s.r[j];
+    if (old.np > 0 && dx * dx + dy * dy + dz * dz < rs * rs) {
+      for (int q = old.row[i]; q < old.row[i + 1]; q++)
+        if (old.pj[q] == j && old.flag[q]) {
+          e = q;
+          break;
+        }
+      if (e < 0)
+        for (int q = old.rev_start[i]; q < old.rev_start[i + 1]; q++) {
+          const int o = old.rev[q];
+          if (old.pi[o] == j && old.sh[o] == kNoShift && old.flag[o]) {
+            e = o;
+            sgn = -1.0;
+            break;
+          }
+        }
+    }
+    nw.carry[p] = e < 0 ? -1 : (sgn > 0 ? e : -(e + 2));
+    nw.flag[p] = e >= 0 ? 1 : 0;
+    for (int k = 0; k < 3; k++) nw.shear[3 * p + k] = e >= 0 ? sgn * old.shear[3 * e + k] : 0.0;
+  }
+}
+
+// ------------------------------------------------------------------- forward
+__device__ __forceinline__ VjpIn pair_in(const ADev &s, const double *x, int p, const double *vh,
+                                         const double *wh, const double *shear) {
+  VjpIn a;
+  const int i = s.pi[p], j = s.pj[p];
+  double xj[3] = {x[3 * j], x[3 * j + 1], x[3 * j + 2]};
+  a_image(s, s.sh[p], xj);
+  for (int k = 0; k < 3; k++) {
+    a.d[k] = x[3 * i + k] - xj[k];
+    a.vr[k] = vh[3 * i + k] - vh[3 * j + k];
+    a.wi[k] = wh[3 * i + k];
+    a.wj[k] = wh[3 * j + k];
+    a.sh[k] = shear[3 * p + k];
+  }
+  a.ri = s.r[i];
+  a.rj = s.r[j];
+  a.mi = s.m[i];
+  a.mj = s.m[j];
+  a.Y = s.Y;
+  a.G = s.G;
+  a.beta = s.beta;
+  a.mu = s.mu;
+  a.dt = s.dt;
+  a.wall = false;
+  return a;
+}
+
+__device__ __forceinline__ bool pair_touch(const VjpIn &a) {
+  const double rs = a.ri + a.rj;
+  return dot3(a.d, a.d) < rs * rs;
+}
+
+// plane w against atom i (FixWallGran primitive: overlap when the distance
+// to the plane is at most the radius); false when not touching
+__device__ __forceinline__ bool wall_in(const ADev &s, const double *x, int w, int i, const double *vh,
+                                        const double *wh, const double *ws, VjpIn &a) {
+  const int ax = s.pax[w];
+  const double pos = s.ppos[w];
+  const double xa = x[3 * i + ax];
+  const double dist = xa > pos ? xa - pos : pos - xa;
+  if (!(dist - s.r[i] <= 0)) return false;
+  for (int k = 0; k < 3; k++) {
+    a.d[k] = k == ax ? xa - pos : 0.0;
+    a.vr[k] = vh[3 * i + k];
+    a.wi[k] = wh[3 * i + k];
+    a.wj[k] = 0.0;
+    a.sh[k] = ws[((size_t)w * s.n + i) * 3 + k];
+  }
+  a.ri = s.r[i];
+  a.rj = 0.0;
+  a.mi = s.m[i];
+  a.mj = 0.0;
+  a.Y = s.Y;
+  a.G = s.G;
+  a.beta = s.beta;
+  a.mu = s.mu;
+  a.dt = s.dt;
+  a.wall = true;
+  return true;
+}
+
+// pair forces of the current state (vh, wh: the velocities the forces see);
+// tape_sh receives the history before the update
+__global__ void ka_pair_force(ADev s, const double *vh, const double *wh, int upd, double *tape_sh) {
+  AGRID(p, s.np) {
+    VjpIn a = pair_in(s, s.x, p, vh, wh, s.shear);
+    a.upd = upd != 0;
+    if (tape_sh)
+      for (int k = 0; k < 3; k++) tape_sh[3 * p + k] = a.sh[k];
+    if (!pair_touch(a)) {
+      s.touch[p] = 0;  // history kept (no surfacesClose band with cdf 1)
+      continue;
+    }
+    LawState S;
+    double F[3], Ti[3], Tj[3], s3[3];
+    law_forward(a, S, F, Ti, Tj, s3);
+    for (int k = 0; k < 3; k++) {
+      s.pF[3 * p + k] = F[k];
+      s.pTi[3 * p + k] = Ti[k];
+      s.pTj[3 * p + k] = Tj[k];
+      if (upd) s.shear[3 * p + k] = s3[k];
+    }
+    if (upd) s.flag[p] = 1;
+    s.touch[p] = 1;
+  }
+}
+
+// total force/torque per atom: own row, reverse list (local entries), gravity,
+// planes; with final_kick the second half-kick v = vh + a F, w = wh + b T.
+// tape_ws receives the wall history before the update, wallF the wall forces.
+__global__ void ka_gather(ADev s, const double *vh, const double *wh, int upd, int final_kick,
+                          double *tape_ws, double *wallF) {
+  AGRID(i, s.n) {
+    double f[3] = {0., 0., 0.}, t[3] = {0., 0., 0.};
+    for (int p = s.row[i]; p < s.row[i + 1]; p++)
+      if (s.touch[p])
+        for (int k = 0; k < 3; k++) {
+          f[k] += s.pF[3 * p + k];
+          t[k] += s.pTi[3 * p + k];
+        }
+    for (int q = s.rev_start[i]; q < s.rev_start[i + 1]; q++) {
+      const int p = s.rev[q];
+      if (!s.touch[p] || s.sh[p] != kNoShift) continue;
+      for (int k = 0; k < 3; k++) {
+        f[k] -= s.pF[3 * p + k];
+        t[k] += s.pTj[3 * p + k];
+      }
+    }
+    if (s.gravity_on)
+      for (int k = 0; k < 3; k++) f[k] += s.m[i] * s.g[k];
+    for (int w = 0; w < s.nplanes; w++) {
+      double *hw = s.ws + ((size_t)w * s.n + i) * 3;
+      if (tape_ws)
+        for (int k = 0; k < 3; k++) tape_ws[((size_t)w * s.n + i) * 3 + k] = hw[k];
+      VjpIn a;
+      if (!wall_in(s, s.x, w, i, vh, wh, s.ws, a)) {
+        for (int k = 0; k < 3; k++) hw[k] = 0.0;  // surfacesClose
+        if (wallF)
+          for (int k = 0; k < 3; k++) wallF[((size_t)w * s.n + i) * 3 + k] = 0.0;
+        continue;
+      }
+      a.upd = upd != 0;
+      LawState S;
+      double F[3], Ti[3], Tj[3], s3[3];
+      law_forward(a, S, F, Ti, Tj, s3);
+      for (int k = 0; k < 3; k++) {
+        f[k] += F[k];
+        t[k] += Ti[k];
+        if (upd) hw[k] = s3[k];
+        if (wallF) wallF[((size_t)w * s.n + i) * 3 + k] = F[k];
+      }
+    }
+    const double a = s.dtf / s.m[i];
+    const double b = s.dtfrot / (s.r[i] * s.r[i] * s.m[i]);
+    for (int k = 0; k < 3; k++) {
+      s.F[3 * i + k] = f[k];
+      s.T[3 * i + k] = t[k];
+      if (final_kick) {
+        s.v[3 * i + k] = vh[3 * i + k] + a * f[k];
+        s.w[3 * i + k] = wh[3 * i + k] + b * t[k];
+      }
+    }
+  }
+}
+
+// first half-kick and drift (v, w then hold vh, wh); xref: positions at the
+// list build to check the displacement against, or null
+__global__ void ka_kick_drift(ADev s, const double *xref) {
+  AGRID(i, s.n) {
+    const double a = s.dtf / s.m[i];
+    const double b = s.dtfrot / (s.r[i] * s.r[i] * s.m[i]);
+    double dsq = 0.0;
+    for (int k = 0; k < 3; k++) {
+      s.v[3 * i + k] += a * s.F[3 * i + k];
+      s.w[3 * i + k] += b * s.T[3 * i + k];
+      s.x[3 * i + k] += s.dt * s.v[3 * i + k];
+      if (xref) {
+        const double e = s.x[3 * i + k] - xref[3 * i + k];
+        dsq += e * e;
+      }
+    }
+    if (dsq > 0.25 * s.skin * s.skin) s.err[0] = 1;
+  }
+}
+
+// ------------------------------------------------------------------ backward
+struct ABar {
+  double *xb, *vb, *wb, *Fb, *Tb, *rb, *mb, *sb, *wsb;
+  // per-entry VJP outputs of the pair law
+  double *pd, *pv, *pwi, *pwj, *pri, *prj, *pmi, *pmj, *pth;  // pth [4*p]: Y, G, beta, mu
+  double *wth;  // [4*i] wall parameter adjoints per atom
+  double *th;   // [4] accumulated parameter adjoints
+};
+
+// second half-kick: v' = vh + a F', w' = wh + b T'
+__global__ void kb_final(ADev s, ABar B, const double *Fn1, const double *Tn1) {
+  AGRID(i, s.n) {
+    const double m = s.m[i], r = s.r[i];
+    const double a = s.dtf / m, b = s.dtfrot / (r * r * m);
+    double fv = 0.0, tw = 0.0;
+    for (int k = 0; k < 3; k++) {
+      B.Fb[3 * i + k] += a * B.vb[3 * i + k];
+      B.Tb[3 * i + k] += b * B.wb[3 * i + k];
+      fv += Fn1[3 * i + k] * B.vb[3 * i + k];
+      tw += Tn1[3 * i + k] * B.wb[3 * i + k];
+    }
+    B.mb[i] += -a / m * fv - b / m * tw;
+    B.rb[i] += -2.0 * b / r * tw;
+  }
+}
+
+// gravity and walls of one force evaluation at positions x; vh/wh the
+// velocities the forces saw, ws_before the wall history before it; seed adds
+// d(loss)/d(normal wall force) on plane seed_w
+__global__ void kb_walls(ADev s, ABar B, const double *x, const double *vh, const double *wh,
+                         const double *ws_before, int upd, int seed_w, double seed) {
+  AGRID(i, s.n) {
+    double th[4] = {0., 0., 0., 0.};
+    if (s.gravity_on)
+      B.mb[i] += s.g[0] * B.Fb[3 * i] + s.g[1] * B.Fb[3 * i + 1] + s.g[2] * B.Fb[3 * i + 2];
+    for (int w = 0; w < s.nplanes; w++) {
+      double *wsb = B.wsb + ((size_t)w * s.n + i) * 3;
+      VjpIn a;
+      if (!wall_in(s, x, w, i, vh, wh, ws_before, a)) {
+        if (upd)
+          for (int k = 0; k < 3; k++) wsb[k] = 0.0;  // history zeroed: no dependence
+        continue;
+      }
+      a.upd = upd != 0;
+      VjpBar bb;
+      for (int k = 0; k < 3; k++) {
+        bb.F[k] = B.Fb[3 * i + k] + (w == seed_w && k == s.pax[w] ? seed : 0.0);
+        bb.Ti[k] = B.Tb[3 * i + k];
+        bb.Tj[k] = 0.0;
+        bb.s3[k] = upd ? wsb[k] : 0.0;
+      }
+      law_vjp(a, bb);
+      for (int k = 0; k < 3; k++) {
+        if (k == s.pax[w]) B.xb[3 * i + k] += bb.d[k];  // off-axis components of d are constants
+        B.vb[3 * i + k] += bb.vr[k];
+        B.wb[3 * i + k] += bb.wi[k];
+        wsb[k] = bb.sh[k] + (upd ? 0.0 : wsb[k]);
+      }
+      B.rb[i] += bb.ri;
+      B.mb[i] += bb.mi;
+      th[0] += bb.Y;
+      th[1] += bb.G;
+      th[2] += bb.beta;
+      th[3] += bb.mu;
+    }
+    for (int k = 0; k < 4; k++) B.wth[4 * i + k] = th[k];
+  }
+}
+
+__global__ void kb_pairs(ADev s, ABar B, const double *x, const double *vh, const double *wh,
+                         const double *sh_before, int upd) {
+  AGRID(p, s.np) {
+    VjpIn a = pair_in(s, x, p, vh, wh, sh_before);
+    a.upd = upd != 0;
+    const int i = s.pi[p], j = s.pj[p];
+    const bool local = s.sh[p] == kNoShift;
+    if (!pair_touch(a)) {
+      for (int k = 0; k < 3; k++) B.pd[3 * p + k] = B.pv[3 * p + k] = B.pwi[3 * p + k] = B.pwj[3 * p + k] = 0.0;
+      B.pri[p] = B.prj[p] = B.pmi[p] = B.pmj[p] = 0.0;
+      for (int k = 0; k < 4; k++) B.pth[4 * p + k] = 0.0;
+      continue;  // history unchanged: its adjoint passes through
+    }
+    VjpBar bb;
+    for (int k = 0; k < 3; k++) {
+      bb.F[k] = B.Fb[3 * i + k] - (local ? B.Fb[3 * j + k] : 0.0);
+      bb.Ti[k] = B.Tb[3 * i + k];
+      bb.Tj[k] = local ? B.Tb[3 * j + k] : 0.0;
+      bb.s3[k] = upd ? B.sb[3 * p + k] : 0.0;
+    }
+    law_vjp(a, bb);
+    for (int k = 0; k < 3; k++) {
+      B.pd[3 * p + k] = bb.d[k];
+      B.pv[3 * p + k] = bb.vr[k];
+      B.pwi[3 * p + k] = bb.wi[k];
+      B.pwj[3 * p + k] = bb.wj[k];  // F_i and T_i depend on w_j for periodic images too
+      B.sb[3 * p + k] = bb.sh[k] + (upd ? 0.0 : B.sb[3 * p + k]);
+    }
+    B.pri[p] = bb.ri;
+    B.prj[p] = bb.rj;
+    B.pmi[p] = bb.mi;
+    B.pmj[p] = bb.mj;
+    B.pth[4 * p + 0] = bb.Y;
+    B.pth[4 * p + 1] = bb.G;
+    B.pth[4 * p + 2] = bb.beta;
+    B.pth[4 * p + 3] = bb.mu;
+  }
+}
+
+// per atom: pair adjoints in list order (own row, then reverse list), then
+// the drift x' = x + dt vh and the first half-kick vh = v + a F, wh = w + b T
+// with Fn/Tn the forces at the step's start; drift = 0 for the setup pass
+__global__ void kb_gather_kick(ADev s, ABar B, const double *Fn, const double *Tn, int drift) {
+  AGRID(i, s.n) {
+    double xb[3], vb[3], wb[3], rb = 0.0, mb = 0.0;
+    for (int k = 0; k < 3; k++) {
+      xb[k] = B.xb[3 * i + k];
+      vb[k] = B.vb[3 * i + k];
+      wb[k] = B.wb[3 * i + k];
+    }
+    for (int p = s.row[i]; p < s.row[i + 1]; p++) {
+      for (int k = 0; k < 3; k++) {
+        xb[k] += B.pd[3 * p + k];
+        vb[k] += B.pv[3 * p + k];
+        wb[k] += B.pwi[3 * p + k];
+      }
+      rb += B.pri[p];
+      mb += B.pmi[p];
+    }
+    for (int q = s.rev_start[i]; q < s.rev_start[i + 1]; q++) {
+      const int p = s.rev[q];
+      for (int k = 0; k < 3; k++) {
+        xb[k] -= B.pd[3 * p + k];
+        vb[k] -= B.pv[3 * p + k];
+        wb[k] += B.pwj[3 * p + k];
+      }
+      rb += B.prj[p];
+      mb += B.pmj[p];
+    }
+    if (!drift) {  // setup force pass: adjoints of the initial state
+      for (int k = 0; k < 3; k++) {
+        B.xb[3 * i + k] = xb[k];
+        B.vb[3 * i + k] = vb[k];
+        B.wb[3 * i + k] = wb[k];
+      }
+      B.rb[i] += rb;
+      B.mb[i] += mb;
+      continue;
+    }
+    const double m = s.m[i], r = s.r[i];
+    const double a = s.dtf / m, b = s.dtfrot / (r * r * m);
+    double fv = 0.0, tw = 0.0;
+    for (int k = 0; k < 3; k++) {
+      vb[k] += s.dt * xb[k];
+      B.xb[3 * i + k] = xb[k];
+      B.vb[3 * i + k] = vb[k];
+      B.wb[3 * i + k] = wb[k];
+      B.Fb[3 * i + k] = a * vb[k];
+      B.Tb[3 * i + k] = b * wb[k];
+      fv += Fn[3 * i + k] * vb[k];
+      tw += Tn[3 * i + k] * wb[k];
+    }
+    B.rb[i] += rb - 2.0 * b / r * tw;
+    B.mb[i] += mb - a / m * fv - b / m * tw;
+  }
+}
+
+// deterministic sum of cnt rows of 4 doubles: per-block partials, then one
+// thread per component adds them in block order into acc
+__global__ void kb_reduce4(const double *in, int cnt, double *part) {
+  __shared__ double sm[4][kAB];
+  double acc[4] = {0., 0., 0., 0.};
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x)
+    for (int k = 0; k < 4; k++) acc[k] += in[4 * q + k];
+  for (int k = 0; k < 4; k++) sm[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int st = kAB / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st)
+      for (int k = 0; k < 4; k++) sm[k][threadIdx.x] += sm[k][threadIdx.x + st];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 4; k++) part[4 * blockIdx.x + k] = sm[k][0];
+}
+__global__ void kb_accum4(const double *part, int nb, double *acc) {
+  if (threadIdx.x >= 4) return;
+  double v = acc[threadIdx.x];
+  for (int b = 0; b < nb; b++) v += part[4 * b + threadIdx.x];
+  acc[threadIdx.x] = v;
+}
+
+// history adjoints at a build back to the previous list's entries: direct
+// copies first, then the flipped copies of old local entries (each old entry
+// has at most one source of each kind, so both passes are race-free)
+__global__ void kb_uncarry(int np_new, const int *carry, const double *sb_new, double *sb_old, int flipped) {
+  AGRID(p, np_new) {
+    const int c = carry[p];
+    if (!flipped && c >= 0)
+      for (int k = 0; k < 3; k++) sb_old[3 * c + k] += sb_new[3 * p + k];
+    if (flipped && c <= -2)
+      for (int k = 0; k < 3; k++) sb_old[3 * (-c - 2) + k] -= sb_new[3 * p + k];
+  }
+}
+
+int grid_of(long n) { return (int)std::max<long>(1, std::min<long>((n + kAB - 1) / kAB, kMaxGrid)); }
+
+// device memory of one run: a bump arena sized by the previous run's demand
+// (repeated runs of the same problem allocate nothing), spilling to
+// cudaMalloc when a run needs more
+struct Arena {
+  char *base = nullptr;
+  size_t cap = 0, used = 0, want = 0;
+  std::vector<void *> spill;
+  void *get(size_t bytes) {
+    bytes = (std::max<size_t>(bytes, 1) + 255) & ~size_t(255);
+    want += bytes;
+    if (used + bytes <= cap) {
+      void *p = base + used;
+      used += bytes;
+      return p;
+    }
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes) != cudaSuccess) return nullptr;
+    spill.push_back(p);
+    return p;
+  }
+  cudaError_t reset() {
+    for (void *p : spill) cudaFree(p);
+    spill.clear();
+    if (want > cap) {
+      if (base) cudaFree(base);
+      base = nullptr;
+      cap = 0;
+      const size_t c = want + want / 4;
+      cudaError_t e = cudaMalloc(&base, c);
+      if (e != cudaSuccess) return e;
+      cap = c;
+    }
+    used = 0;
+    want = 0;
+    return cudaSuccess;
+  }
+  void release() {
+    for (void *p : spill) cudaFree(p);
+    spill.clear();
+    if (base) cudaFree(base);
+    base = nullptr;
+    cap = used = want = 0;
+  }
+};
+
+}  // namespace
+
+struct dem_adjoint {
+  dem_adjoint_config cfg{};
+  ADev s{};
+  int n = 0;
+  std::vector<void *> owned;  // freed with the handle
+  Arena arena;                // per-run checkpoints, lists and tape
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  std::string err;
+  double *x0 = nullptr, *v0 = nullptr, *w0 = nullptr, *r0 = nullptr;  // initial state
+  double rmax0 = 0.0;
+  double *xref = nullptr;  // positions at the last build
+  double *wallF = nullptr;
+  int *scan_tmp = nullptr, *rcnt = nullptr, *rfill = nullptr;
+  Sys nosys{};  // the scan helper's gate argument (ungated here)
+  int pcap = 0;
+  ABar B{};
+  double *part = nullptr;
+  double last_fwd_ms = 0.0, last_bwd_ms = 0.0;
+  int last_nseg = 0, last_maxnp = 0;
+};
+
+#define ATRY(h, call)                                                \
+  do {                                                               \
+    cudaError_t e_ = (call);                                         \
+    if (e_ != cudaSuccess) {                                         \
+      (h)->err = std::string(#call) + ": " + cudaGetErrorString(e_); \
+      return DEM_ERR_CUDA;                                           \
+    }                                                                \
+  } while (0)
+
+#define AGET(h, ptr, type, count)                                                \
+  do {                                                                           \
+    (ptr) = static_cast<type *>((h)->arena.get((size_t)(count) * sizeof(type))); \
+    if (!(ptr)) {                                                                \
+      (h)->err = "device memory exhausted";                                      \
+      return DEM_ERR_CUDA;                                                       \
+    }                                                                            \
+  } while (0)
+
+namespace {
+
+template <typename T>
+cudaError_t dmalloc(std::vector<void *> &owned, T **p, size_t n) {
+  void *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, std::max<size_t>(n, 1) * sizeof(T));
+  if (e == cudaSuccess) {
+    owned.push_back(q);
+    *p = static_cast<T *>(q);
+  }
+  return e;
+}
+
+struct Checkpoint {
+  double *x, *v, *w, *F, *T, *ws;  // state before the segment's first drift
+  double *sh0;                     // the list's history as carried at the build
+  AList L;
+};
+
+// neighbour list of the current positions; old: the previous list (with its
+// current history and flags) or np = 0
+int build_list(dem_adjoint *h, AList &L, const AList &old) {
+  ADev &s = h->s;
+  const int n = h->n;
+  const cudaStream_t st = h->st;
+  ATRY(h, cudaMemsetAsync(s.cell_count, 0, (s.ncell + 2) * sizeof(int), st));
+  ATRY(h, cudaMemsetAsync(s.cell_fill, 0, (s.ncell + 2) * sizeof(int), st));
+  ka_cell<<<grid_of(n), kAB, 0, st>>>(s);
+  scan_exclusive(h->nosys, s.cell_count, s.cell_start, s.ncell + 1, h->scan_tmp, false, st);
+  ka_scatter<<<grid_of(n), kAB, 0, st>>>(s);
+  ka_cellsort<<<grid_of(s.ncell), kAB, 0, st>>>(s);
+  ka_pairs<false><<<grid_of(n), kAB, 0, st>>>(s, nullptr, nullptr, nullptr, nullptr);
+  ATRY(h, cudaMemsetAsync(s.pcount + n, 0, sizeof(int), st));
+  AGET(h, L.row, int, n + 1);
+  scan_exclusive(h->nosys, s.pcount, L.row, n + 1, h->scan_tmp, false, st);
+  int np = 0;
+  ATRY(h, cudaMemcpyAsync(&np, L.row + n, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ATRY(h, cudaStreamSynchronize(st));
+  L.np = np;
+  AGET(h, L.pi, int, np);
+  AGET(h, L.pj, int, np);
+  AGET(h, L.sh, uint8_t, np);
+  AGET(h, L.flag, uint8_t, np);
+  AGET(h, L.rev_start, int, n + 1);
+  AGET(h, L.rev, int, np);
+  AGET(h, L.carry, int, np);
+  AGET(h, L.shear, double, 3 * (size_t)np);
+  ka_pairs<true><<<grid_of(n), kAB, 0, st>>>(s, L.pi, L.pj, L.sh, L.row);
+  ATRY(h, cudaMemsetAsync(h->rcnt, 0, (n + 1) * sizeof(int), st));
+  ATRY(h, cudaMemsetAsync(h->rfill, 0, (n + 1) * sizeof(int), st));
+  if (np > 0) ka_rev_count<<<grid_of(np), kAB, 0, st>>>(np, L.pj, h->rcnt);
+  scan_exclusive(h->nosys, h->rcnt, L.rev_start, n + 1, h->scan_tmp, false, st);
+  if (np > 0) {
+    ka_rev_fill<<<grid_of(np), kAB, 0, st>>>(np, L.pj, L.rev_start, h->rfill, L.rev);
+    ka_carry<<<grid_of(np), kAB, 0, st>>>(s, L, old);
+  }
+  ka_rev_sort<<<grid_of(n), kAB, 0, st>>>(n, L.rev_start, L.rev);
+  ATRY(h, cudaGetLastError());
+  return DEM_OK;
+}
+
+void use_list(dem_adjoint *h, const AList &L, double *shear) {
+  ADev &s = h->s;
+  s.np = L.np;
+  s.pi = L.pi;
+  s.pj = L.pj;
+  s.sh = L.sh;
+  s.flag = L.flag;
+  s.row = L.row;
+  s.rev_start = L.rev_start;
+  s.rev = L.rev;
+  s.shear = shear;
+}
+
+int ensure_pairs(dem_adjoint *h, int np) {
+  if (np <= h->pcap) return DEM_OK;
+  const int cap = std::max(np, 1024) + std::max(np, 1024) / 4;
+  double **d3[] = {&h->s.pF, &h->s.pTi, &h->s.pTj, &h->B.pd, &h->B.pv, &h->B.pwi, &h->B.pwj, &h->B.sb};
+  for (double **q : d3) ATRY(h, dmalloc(h->owned, q, 3 * (size_t)cap));
+  double **d1[] = {&h->B.pri, &h->B.prj, &h->B.pmi, &h->B.pmj};
+  for (double **q : d1) ATRY(h, dmalloc(h->owned, q, (size_t)cap));
+  ATRY(h, dmalloc(h->owned, &h->B.pth, 4 * (size_t)cap));
+  ATRY(h, dmalloc(h->owned, &h->s.touch, (size_t)cap));
+  h->pcap = cap;
+  return DEM_OK;
+}
+
+// Yeff, Geff, betaeff of one material against itself
+// (src/global_properties.cpp: Yeff, Geff, betaeff) and their derivatives
+void derive(double E, double nu, double e, double &Y, double &G, double &beta, double &dYdE,
+            double &dGdE, double &dbde) {
+  Y = 1. / ((1. - nu * nu) / E + (1. - nu * nu) / E);
+  G = 1. / (2. * (2. - nu) * (1. + nu) / E + 2. * (2. - nu) * (1. + nu) / E);
+  const double lg = std::log(e);
+  beta = lg / std::sqrt(lg * lg + M_PI * M_PI);
+  dYdE = Y / E;
+  dGdE = G / E;
+  dbde = (1.0 / e) * (M_PI * M_PI) / std::pow(lg * lg + M_PI * M_PI, 1.5);
+}
+
+void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, double *tape_sh,
+                double *tape_ws, int final_kick, double *wallF) {
+  ADev &s = h->s;
+  if (s.np > 0) ka_pair_force<<<grid_of(s.np), kAB, 0, h->st>>>(s, vh, wh, upd, tape_sh);
+  ka_gather<<<grid_of(h->n), kAB, 0, h->st>>>(s, vh, wh, upd, final_kick, tape_ws, wallF);
+}
+
+void accumulate(dem_adjoint *h, const double *in, int cnt) {
+  if (cnt <= 0) return;
+  const int g = std::min(grid_of(cnt), 304);
+  kb_reduce4<<<g, kAB, 0, h->st>>>(in, cnt, h->part);
+  kb_accum4<<<1, 32, 0, h->st>>>(h->part, g, h->B.th);
+}
+
+void copyd(dem_adjoint *h, double *dst, const double *src, size_t count) {
+  if (count) cudaMemcpyAsync(dst, src, count * sizeof(double), cudaMemcpyDeviceToDevice, h->st);
+}
+
+}  // namespace
+
+extern "C" {
+
+int dem_adjoint_create(const dem_adjoint_config *cfg, dem_adjoint **out) {
+  if (!cfg || !out) return DEM_ERR_BAD_ARG;
+  *out = nullptr;
+  if (!(cfg->dt > 0) || !(cfg->skin > 0) || !(cfg->density > 0) || cfg->nplanes < 0 || cfg->nplanes > 8 ||
+      !(cfg->poisson > -1.0 && cfg->poisson < 0.5))
+    return DEM_ERR_BAD_ARG;
+  for (int d = 0; d < 3; d++)
+    if (!(cfg->boxhi[d] > cfg->boxlo[d])) return DEM_ERR_BAD_ARG;
+  for (int w = 0; w < cfg->nplanes; w++)
+    if (cfg->plane_axis[w] < 0 || cfg->plane_axis[w] > 2) return DEM_ERR_BAD_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DEM_ERR_NO_DEVICE;
+  dem_adjoint *h = new dem_adjoint();
+  h->cfg = *cfg;
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&h->ev[0]) != cudaSuccess || cudaEventCreate(&h->ev[1]) != cudaSuccess) {
+    dem_adjoint_destroy(h);
+    return DEM_ERR_CUDA;
+  }
+  ADev &s = h->s;
+  for (int d = 0; d < 3; d++) {
+    s.lo[d] = cfg->boxlo[d];
+    s.hi[d] = cfg->boxhi[d];
+    s.prd[d] = cfg->boxhi[d] - cfg->boxlo[d];
+    s.per[d] = cfg->periodic[d] ? 1 : 0;
+    s.g[d] = cfg->gravity[d];
+  }
+  s.gravity_on = cfg->gravity_on ? 1 : 0;
+  s.dt = cfg->dt;
+  s.skin = cfg->skin;
+  s.nplanes = cfg->nplanes;
+  for (int w = 0; w < cfg->nplanes; w++) {
+    s.pax[w] = cfg->plane_axis[w];
+    s.ppos[w] = cfg->plane_pos[w];
+  }
+  // FixNVESphere: dtf = dt/2 (force units 1), dtfrot = dtf / INERTIA (0.4)
+  s.dtf = 0.5 * cfg->dt;
+  s.dtfrot = s.dtf / 0.4;
+  *out = h;
+  return DEM_OK;
+}
+
+int dem_adjoint_destroy(dem_adjoint *h) {
+  if (!h) return DEM_ERR_BAD_ARG;
+  if (h->st) cudaStreamSynchronize(h->st);
+  h->arena.release();
+  for (void *p : h->owned) cudaFree(p);
+  for (cudaEvent_t e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return DEM_OK;
+}
+
+int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *v, const double *omega,
+                          const double *radius) {
+  if (!h || n < 1 || !x || !v || !omega || !radius || h->n) return DEM_ERR_BAD_ARG;
+  ADev &s = h->s;
+  double rmax = 0.0;
+  for (int i = 0; i < n; i++) {
+    if (!(radius[i] > 0.0)) return DEM_ERR_BAD_ARG;
+    rmax = std::max(rmax, radius[i]);
+  }
+  // cells at least one neighbour cutoff wide for radii up to 1 % larger
+  // than the initial ones
+  const double cut = 2.0 * rmax * 1.01 + s.skin;
+  long ncell = 1;
+  int nc[3];
+  for (int d = 0; d < 3; d++) {
+    long c = (long)std::floor(s.prd[d] / (cut * (1.0 + 1e-9)));
+    c = std::max(1L, std::min(c, 1024L));
+    if (s.per[d] && c < 3) return DEM_ERR_BOX;
+    nc[d] = (int)c;
+    ncell *= c;
+  }
+  if (ncell > 16000000L) return DEM_ERR_BAD_ARG;
+  h->n = n;
+  h->rmax0 = rmax;
+  s.n = n;
+  for (int d = 0; d < 3; d++) {
+    s.nc[d] = nc[d];
+    s.csz[d] = s.prd[d] / nc[d];
+  }
+  s.ncell = (int)ncell;
+  double **d3[] = {&s.x, &s.v, &s.w, &s.F, &s.T, &h->x0, &h->v0, &h->w0, &h->xref,
+                   &h->B.xb, &h->B.vb, &h->B.wb, &h->B.Fb, &h->B.Tb};
+  for (double **q : d3) ATRY(h, dmalloc(h->owned, q, 3 * (size_t)n));
+  double **d1[] = {&s.r, &s.m, &h->r0, &h->B.rb, &h->B.mb};
+  for (double **q : d1) ATRY(h, dmalloc(h->owned, q, (size_t)n));
+  const size_t W3 = 3 * (size_t)std::max(1, s.nplanes) * n;
+  ATRY(h, dmalloc(h->owned, &s.ws, W3));
+  ATRY(h, dmalloc(h->owned, &h->B.wsb, W3));
+  ATRY(h, dmalloc(h->owned, &h->wallF, W3));
+  ATRY(h, dmalloc(h->owned, &h->B.wth, 4 * (size_t)n));
+  ATRY(h, dmalloc(h->owned, &h->B.th, 4));
+  ATRY(h, dmalloc(h->owned, &h->part, 4 * (size_t)kMaxGrid));
+  ATRY(h, dmalloc(h->owned, &s.cell_of, (size_t)n));
+  ATRY(h, dmalloc(h->owned, &s.cell_count, (size_t)ncell + 2));
+  ATRY(h, dmalloc(h->owned, &s.cell_start, (size_t)ncell + 2));
+  ATRY(h, dmalloc(h->owned, &s.cell_fill, (size_t)ncell + 2));
+  ATRY(h, dmalloc(h->owned, &s.order, (size_t)n));
+  ATRY(h, dmalloc(h->owned, &s.pcount, (size_t)n + 1));
+  ATRY(h, dmalloc(h->owned, &h->rcnt, (size_t)n + 1));
+  ATRY(h, dmalloc(h->owned, &h->rfill, (size_t)n + 1));
+  ATRY(h, dmalloc(h->owned, &s.err, 4));
+  const long maxlen = std::max<long>(n + 1, ncell + 2);
+  ATRY(h, dmalloc(h->owned, &h->scan_tmp, (size_t)((maxlen + 4095) / 4096 + 2)));
+  ATRY(h, cudaMemcpy(h->x0, x, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+  ATRY(h, cudaMemcpy(h->v0, v, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+  ATRY(h, cudaMemcpy(h->w0, omega, 3 * (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+  ATRY(h, cudaMemcpy(h->r0, radius, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+  return DEM_OK;
+}
+
+static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *radius, int nsteps,
+                   int seg, const dem_adjoint_loss *loss, double *loss_out, double *gE, double *ge,
+                   double *gmu, double *gr, bool backward) {
+  if (!h || !h->n || nsteps < 1 || seg < 1 || !loss || !loss_out || !(E > 0) || !(e > 0 && e < 1) ||
+      !(mu >= 0))
+    return DEM_ERR_BAD_ARG;
+  if (backward && (!gE || !ge || !gmu || !gr)) return DEM_ERR_BAD_ARG;
+  ADev &s = h->s;
+  const int n = h->n;
+  const cudaStream_t st = h->st;
+  std::vector<double> rr(n), mm(n);
+  if (radius) {
+    for (int i = 0; i < n; i++) rr[i] = radius[i];
+  } else {
+    ATRY(h, cudaMemcpy(rr.data(), h->r0, n * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  for (int i = 0; i < n; i++) {
+    if (!(rr[i] > 0) || rr[i] > 1.01 * h->rmax0) return DEM_ERR_BAD_ARG;
+    mm[i] = 4.0 * M_PI / 3.0 * rr[i] * rr[i] * rr[i] * h->cfg.density;  // FixDensity: rmass = 4/3 pi r^3 rho
+  }
+  ATRY(h, cudaStreamSynchronize(st));
+  ATRY(h, h->arena.reset());
+  double Y, G, beta, dYdE, dGdE, dbde;
+  derive(E, h->cfg.poisson, e, Y, G, beta, dYdE, dGdE, dbde);
+  s.Y = Y;
+  s.G = G;
+  s.beta = beta;
+  s.mu = mu;
+  const size_t S3 = 3 * (size_t)n, W3 = 3 * (size_t)std::max(1, s.nplanes) * n;
+  ATRY(h, cudaMemcpyAsync(s.r, rr.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+  ATRY(h, cudaMemcpyAsync(s.m, mm.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+  copyd(h, s.x, h->x0, S3);
+  copyd(h, s.v, h->v0, S3);
+  copyd(h, s.w, h->w0, S3);
+  ATRY(h, cudaMemsetAsync(s.ws, 0, W3 * sizeof(double), st));
+  ATRY(h, cudaMemsetAsync(s.err, 0, 4 * sizeof(int), st));
+  ATRY(h, cudaEventRecord(h->ev[0], st));
+  // ------------------------------------------------------------ forward
+  // segment k covers steps max(1, kL) .. min(N, (k+1)L - 1); its list is
+  // built after the drift of step kL (k >= 1) or at setup (k = 0)
+  const int nseg = nsteps / seg + 1;
+  std::vector<Checkpoint> cps(nseg);
+  int rc;
+  AList none;
+  int maxnp = 1;
+  for (int k = 0; k < nseg; k++) {
+    Checkpoint &c = cps[k];
+    const int first = std::max(1, k * seg), last = std::min(nsteps, (k + 1) * seg - 1);
+    AGET(h, c.x, double, S3);
+    AGET(h, c.v, double, S3);
+    AGET(h, c.w, double, S3);
+    AGET(h, c.F, double, S3);
+    AGET(h, c.T, double, S3);
+    AGET(h, c.ws, double, W3);
+    if (k == 0) {
+      ka_wrap<<<grid_of(n), kAB, 0, st>>>(s);
+      rc = build_list(h, c.L, none);
+      if (rc) return rc;
+      rc = ensure_pairs(h, c.L.np);
+      if (rc) return rc;
+      use_list(h, c.L, c.L.shear);
+      force_pass(h, s.v, s.w, 0, nullptr, nullptr, 0, nullptr);  // Verlet::setup
+      copyd(h, h->xref, s.x, S3);
+      AGET(h, c.sh0, double, 3 * (size_t)c.L.np);
+      copyd(h, c.sh0, c.L.shear, 3 * (size_t)c.L.np);
+    }
+    copyd(h, c.x, s.x, S3);
+    copyd(h, c.v, s.v, S3);
+    copyd(h, c.w, s.w, S3);
+    copyd(h, c.F, s.F, S3);
+    copyd(h, c.T, s.T, S3);
+    copyd(h, c.ws, s.ws, W3);
+    for (int t = first; t <= last; t++) {
+      const bool build = (k > 0 && t == first);
+      ka_kick_drift<<<grid_of(n), kAB, 0, st>>>(s, build ? nullptr : h->xref);
+      if (build) {
+        ka_wrap<<<grid_of(n), kAB, 0, st>>>(s);
+        rc = build_list(h, c.L, cps[k - 1].L);
+        if (rc) return rc;
+        rc = ensure_pairs(h, c.L.np);
+        if (rc) return rc;
+        use_list(h, c.L, c.L.shear);
+        copyd(h, h->xref, s.x, S3);
+        AGET(h, c.sh0, double, 3 * (size_t)c.L.np);
+        copyd(h, c.sh0, c.L.shear, 3 * (size_t)c.L.np);
+      }
+      force_pass(h, s.v, s.w, 1, nullptr, nullptr, 1, t == nsteps ? h->wallF : nullptr);
+    }
+    maxnp = std::max(maxnp, c.L.np);
+  }
+  ATRY(h, cudaGetLastError());
+  int flag = 0;
+  ATRY(h, cudaMemcpyAsync(&flag, s.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  std::vector<double> xf(S3), vf(S3), wf(S3), wallf(W3);
+  ATRY(h, cudaMemcpyAsync(xf.data(), s.x, S3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ATRY(h, cudaMemcpyAsync(vf.data(), s.v, S3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ATRY(h, cudaMemcpyAsync(wf.data(), s.w, S3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (s.nplanes > 0)
+    ATRY(h, cudaMemcpyAsync(wallf.data(), h->wallF, W3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ATRY(h, cudaEventRecord(h->ev[1], st));
+  ATRY(h, cudaStreamSynchronize(st));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+  h->last_fwd_ms = ms;
+  h->last_nseg = nseg;
+  h->last_maxnp = maxnp;
+  if (flag) {
+    h->err = "an atom moved more than skin/2 from its position at the list build: use shorter segments or a larger skin";
+    return DEM_ERR_BAD_ARG;
+  }
+  // loss of the final state
+  double ke = 0.0, hz = 0.0, fw = 0.0;
+  for (int i = 0; i < n; i++) {
+    const double I = 0.4 * mm[i] * rr[i] * rr[i];
+    for (int k = 0; k < 3; k++)
+      ke += 0.5 * mm[i] * vf[3 * i + k] * vf[3 * i + k] + 0.5 * I * wf[3 * i + k] * wf[3 * i + k];
+    hz += xf[3 * i + 2];
+  }
+  hz /= n;
+  const int lw = loss->wall_id;
+  const bool use_wall = lw >= 0 && lw < s.nplanes;
+  if (use_wall)
+    for (int i = 0; i < n; i++) fw += wallf[((size_t)lw * n + i) * 3 + s.pax[lw]];
+  *loss_out = loss->w_ke * ke + loss->w_height * (hz - loss->height_target) * (hz - loss->height_target) +
+              (use_wall ? loss->w_wallforce * (fw - loss->wallforce_target) * (fw - loss->wallforce_target) : 0.0);
+  if (!backward) return DEM_OK;
+  // ----------------------------------------------------------- backward
+  ATRY(h, cudaEventRecord(h->ev[0], st));
+  ABar &B = h->B;
+  {  // adjoints of the final state
+    std::vector<double> xb(S3, 0.0), vb(S3), wb(S3), mb(n), rb(n);
+    for (int i = 0; i < n; i++) {
+      const double I = 0.4 * mm[i] * rr[i] * rr[i];
+      double v2 = 0.0, w2 = 0.0;
+      for (int k = 0; k < 3; k++) {
+        vb[3 * i + k] = loss->w_ke * mm[i] * vf[3 * i + k];
+        wb[3 * i + k] = loss->w_ke * I * wf[3 * i + k];
+        v2 += vf[3 * i + k] * vf[3 * i + k];
+        w2 += wf[3 * i + k] * wf[3 * i + k];
+      }
+      xb[3 * i + 2] = loss->w_height * 2.0 * (hz - loss->height_target) / n;
+      mb[i] = loss->w_ke * (0.5 * v2 + 0.2 * rr[i] * rr[i] * w2);
+      rb[i] = loss->w_ke * 0.4 * mm[i] * rr[i] * w2;
+    }
+    ATRY(h, cudaMemcpyAsync(B.xb, xb.data(), S3 * sizeof(double), cudaMemcpyHostToDevice, st));
+    ATRY(h, cudaMemcpyAsync(B.vb, vb.data(), S3 * sizeof(double), cudaMemcpyHostToDevice, st));
+    ATRY(h, cudaMemcpyAsync(B.wb, wb.data(), S3 * sizeof(double), cudaMemcpyHostToDevice, st));
+    ATRY(h, cudaMemcpyAsync(B.mb, mb.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+    ATRY(h, cudaMemcpyAsync(B.rb, rb.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+    ATRY(h, cudaStreamSynchronize(st));  // the host vectors go out of scope
+  }
+  ATRY(h, cudaMemsetAsync(B.Fb, 0, S3 * sizeof(double), st));
+  ATRY(h, cudaMemsetAsync(B.Tb, 0, S3 * sizeof(double), st));
+  ATRY(h, cudaMemsetAsync(B.wsb, 0, W3 * sizeof(double), st));
+  ATRY(h, cudaMemsetAsync(B.sb, 0, 3 * (size_t)h->pcap * sizeof(double), st));
+  ATRY(h, cudaMemsetAsync(B.th, 0, 4 * sizeof(double), st));
+  const double fw_seed = use_wall ? loss->w_wallforce * 2.0 * (fw - loss->wallforce_target) : 0.0;
+  // tape of one segment
+  double *tx, *tvh, *twh, *tF, *tT, *tws, *tsh, *shr, *sb_prev;
+  AGET(h, tx, double, S3 * seg);
+  AGET(h, tvh, double, S3 * seg);
+  AGET(h, twh, double, S3 * seg);
+  AGET(h, tF, double, S3 * seg);
+  AGET(h, tT, double, S3 * seg);
+  AGET(h, tws, double, W3 * seg);
+  AGET(h, tsh, double, 3 * (size_t)maxnp * seg);
+  AGET(h, shr, double, 3 * (size_t)maxnp);
+  AGET(h, sb_prev, double, 3 * (size_t)maxnp);
+  for (int k = nseg - 1; k >= 0; k--) {
+    Checkpoint &c = cps[k];
+    const int first = std::max(1, k * seg), last = std::min(nsteps, (k + 1) * seg - 1);
+    // replay from the checkpoint, recording the tape
+    copyd(h, s.x, c.x, S3);
+    copyd(h, s.v, c.v, S3);
+    copyd(h, s.w, c.w, S3);
+    copyd(h, s.F, c.F, S3);
+    copyd(h, s.T, c.T, S3);
+    copyd(h, s.ws, c.ws, W3);
+    copyd(h, shr, c.sh0, 3 * (size_t)c.L.np);
+    use_list(h, c.L, shr);
+    for (int t = first; t <= last; t++) {
+      const int q = t - first;
+      ka_kick_drift<<<grid_of(n), kAB, 0, st>>>(s, nullptr);
+      if (k > 0 && t == first) ka_wrap<<<grid_of(n), kAB, 0, st>>>(s);
+      copyd(h, tx + S3 * q, s.x, S3);
+      copyd(h, tvh + S3 * q, s.v, S3);
+      copyd(h, twh + S3 * q, s.w, S3);
+      force_pass(h, tvh + S3 * q, twh + S3 * q, 1, tsh + 3 * (size_t)maxnp * q, tws + W3 * q, 1, nullptr);
+      copyd(h, tF + S3 * q, s.F, S3);
+      copyd(h, tT + S3 * q, s.T, S3);
+    }
+    // reverse over the segment's steps
+    for (int t = last; t >= first; t--) {
+      const int q = t - first;
+      const double *xs = tx + S3 * q, *vh = tvh + S3 * q, *wh = twh + S3 * q;
+      kb_final<<<grid_of(n), kAB, 0, st>>>(s, B, tF + S3 * q, tT + S3 * q);
+      kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, xs, vh, wh, tws + W3 * q, 1, t == nsteps ? lw : -1,
+                                           t == nsteps ? fw_seed : 0.0);
+      if (s.np > 0)
+        kb_pairs<<<grid_of(s.np), kAB, 0, st>>>(s, B, xs, vh, wh, tsh + 3 * (size_t)maxnp * q, 1);
+      const double *Fn = q > 0 ? tF + S3 * (q - 1) : c.F;
+      const double *Tn = q > 0 ? tT + S3 * (q - 1) : c.T;
+      kb_gather_kick<<<grid_of(n), kAB, 0, st>>>(s, B, Fn, Tn, 1);
+      accumulate(h, B.pth, s.np);
+      accumulate(h, B.wth, n);
+    }
+    if (k > 0) {  // history adjoints back through the carry at this build
+      const AList &po = cps[k - 1].L;
+      ATRY(h, cudaMemsetAsync(sb_prev, 0, 3 * (size_t)std::max(1, po.np) * sizeof(double), st));
+      if (c.L.np > 0) {
+        kb_uncarry<<<grid_of(c.L.np), kAB, 0, st>>>(c.L.np, c.L.carry, B.sb, sb_prev, 0);
+        kb_uncarry<<<grid_of(c.L.np), kAB, 0, st>>>(c.L.np, c.L.carry, B.sb, sb_prev, 1);
+      }
+      copyd(h, B.sb, sb_prev, 3 * (size_t)po.np);
+    }
+  }
+  {  // Verlet::setup force pass: initial state, zero history, no update
+    Checkpoint &c = cps[0];
+    ATRY(h, cudaMemsetAsync(tws, 0, W3 * sizeof(double), st));
+    ATRY(h, cudaMemsetAsync(shr, 0, 3 * (size_t)maxnp * sizeof(double), st));
+    use_list(h, c.L, shr);
+    kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, c.x, c.v, c.w, tws, 0, -1, 0.0);
+    if (s.np > 0) kb_pairs<<<grid_of(s.np), kAB, 0, st>>>(s, B, c.x, c.v, c.w, shr, 0);
+    kb_gather_kick<<<grid_of(n), kAB, 0, st>>>(s, B, nullptr, nullptr, 0);
+    accumulate(h, B.pth, s.np);
+    accumulate(h, B.wth, n);
+  }
+  ATRY(h, cudaGetLastError());
+  std::vector<double> rb(n), mb(n), th(4);
+  ATRY(h, cudaMemcpyAsync(rb.data(), B.rb, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ATRY(h, cudaMemcpyAsync(mb.data(), B.mb, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ATRY(h, cudaMemcpyAsync(th.data(), B.th, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ATRY(h, cudaEventRecord(h->ev[1], st));
+  ATRY(h, cudaStreamSynchronize(st));
+  cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+  h->last_bwd_ms = ms;
+  for (int i = 0; i < n; i++) gr[i] = rb[i] + mb[i] * 3.0 * mm[i] / rr[i];  // dm/dr = 3 m / r
+  *gE = th[0] * dYdE + th[1] * dGdE;
+  *ge = th[2] * dbde;
+  *gmu = th[3];
+  return DEM_OK;
+}
+
+int dem_adjoint_forward(dem_adjoint *h, double E, double restitution, double friction, const double *radius,
+                        int nsteps, int segment, const dem_adjoint_loss *loss, double *loss_out) {
+  return adj_run(h, E, restitution, friction, radius, nsteps, segment, loss, loss_out, nullptr, nullptr,
+                 nullptr, nullptr, false);
+}
+
+int dem_adjoint_gradient(dem_adjoint *h, double E, double restitution, double friction, const double *radius,
+                         int nsteps, int segment, const dem_adjoint_loss *loss, double *loss_out,
+                         double *grad_E, double *grad_restitution, double *grad_friction, double *grad_radius) {
+  return adj_run(h, E, restitution, friction, radius, nsteps, segment, loss, loss_out, grad_E, grad_restitution,
+                 grad_friction, grad_radius, true);
+}
+
+int dem_adjoint_download(dem_adjoint *h, double *x, double *v, double *omega) {
+  if (!h || !h->n) return DEM_ERR_BAD_ARG;
+  const size_t b = 3 * (size_t)h->n * sizeof(double);
+  ATRY(h, cudaStreamSynchronize(h->st));
+  if (x) ATRY(h, cudaMemcpy(x, h->s.x, b, cudaMemcpyDeviceToHost));
+  if (v) ATRY(h, cudaMemcpy(v, h->s.v, b, cudaMemcpyDeviceToHost));
+  if (omega) ATRY(h, cudaMemcpy(omega, h->s.w, b, cudaMemcpyDeviceToHost));
+  return DEM_OK;
+}
+
+int dem_adjoint_times(dem_adjoint *h, double *forward_ms, double *backward_ms, int *segments, int *max_pairs) {
+  if (!h) return DEM_ERR_BAD_ARG;
+  if (forward_ms) *forward_ms = h->last_fwd_ms;
+  if (backward_ms) *backward_ms = h->last_bwd_ms;
+  if (segments) *segments = h->last_nseg;
+  if (max_pairs) *max_pairs = h->last_maxnp;
+  return DEM_OK;
+}
+
+const char *dem_adjoint_last_error(dem_adjoint *h) { return h ? h->err.c_str() : "null handle"; }
+
+}  // extern "C"

@@ -17,6 +17,10 @@ enum {
   kModeGatherFinalInitial = 3,  // sum forces + final(n) + initial(n+1) (steady state)
 };
 
+// exclusive prefix sum of len ints (len <= 4096*4096 - 1); tmp holds
+// (len+4095)/4096 + 1 ints; gate: skip unless the system rebuilds
+int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, bool gate,
+                   cudaStream_t st);
 int launch_decide(const Sys &s, cudaStream_t st);
 int launch_set_rebuild(const Sys &s, int v, cudaStream_t st);
 // stage 0: full rebuild; stage 1: resume after a pair-capacity overflow

@@ -17,7 +17,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
            "-Xcompiler", "-ffp-contract=off",
                   "-Xptxas", "-warn-spills"]
-SOURCES = ["dem_kernels.cu", "dem_capi.cu", "dem_probe.cu", "dem_noalloc.cu", "dem_mesh_host.cu"]
+SOURCES = ["dem_kernels.cu", "dem_capi.cu", "dem_probe.cu", "dem_noalloc.cu", "dem_mesh_host.cu",
+           "dem_adjoint.cu"]
 
 
 def nvcc():
