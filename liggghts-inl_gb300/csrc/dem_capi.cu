@@ -157,6 +157,7 @@ static int alloc_atoms(dem_handle *h, int nmax) {
   }
   CUDA_TRY(h, dalloc(L, &s.perm, nmax));
   CUDA_TRY(h, dalloc(L, &s.xf, nmax));
+  CUDA_TRY(h, dalloc(L, &s.xhf, nmax));
   CUDA_TRY(h, dalloc(L, &s.mlist, nmax));
   CUDA_TRY(h, dalloc(L, &s.order, nmax));
   CUDA_TRY(h, dalloc(L, &s.pcount, nmax + 1));
@@ -554,6 +555,16 @@ int dem_add_mesh(dem_handle *h, int ntri, const double *nodes, int wall_type, in
   CUDA_TRY(h, cudaMemcpy(M.tri, mh.tri.data(), mh.tri.size() * sizeof(double), cudaMemcpyHostToDevice));
   CUDA_TRY(h, dalloc(L, &M.meta, mh.meta.size()));
   CUDA_TRY(h, cudaMemcpy(M.meta, mh.meta.data(), mh.meta.size() * sizeof(int), cudaMemcpyHostToDevice));
+  {
+    std::vector<float4> tf(2 * (size_t)ntri);
+    for (int t = 0; t < ntri; t++) {
+      const double *g = &mh.tri[(size_t)t * kTriStride];
+      tf[2 * (size_t)t] = make_float4((float)g[0], (float)g[1], (float)g[2], 0.f);
+      tf[2 * (size_t)t + 1] = make_float4((float)g[30], (float)g[31], (float)g[32], 0.f);
+    }
+    CUDA_TRY(h, dalloc(L, &M.trif, tf.size()));
+    CUDA_TRY(h, cudaMemcpy(M.trif, tf.data(), tf.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  }
   CUDA_TRY(h, dalloc(L, &M.cn_start, mh.cn_start.size()));
   CUDA_TRY(h, cudaMemcpy(M.cn_start, mh.cn_start.data(), mh.cn_start.size() * sizeof(int), cudaMemcpyHostToDevice));
   CUDA_TRY(h, dalloc(L, &M.cn_list, std::max<size_t>(1, mh.cn_list.size())));
@@ -698,6 +709,13 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
     const double tmin = 2.0 * minrad;
     const double relt = 2.0 * std::sqrt(3.0) * e / tmin + 3.0 * e * e / (tmin * tmin) + 1e-6;
     s.pf_margin_touch = (float)std::min(0.5, std::max(1e-4, 4.0 * relt));
+    // displacement prefilter: |(float)x - (float)xhold| is within
+    // sqrt(3)*2^-23*C + 4*2^-24*|d| of |x - xhold| (C bounds coordinates);
+    // four times that is the band the exact test decides
+    const double hs = 0.5 * s.skin;
+    const double band = 4.0 * (std::sqrt(3.0) * std::ldexp(cmax + pmax, -23) + 4.0 * std::ldexp(hs, -24));
+    s.skin_lo2 = hs > band ? (float)((hs - band) * (hs - band) * (1.0 - 1e-6)) : -1.0f;
+    s.skin_hi2 = (float)((hs + band) * (hs + band) * (1.0 + 1e-6));
   }
   long ncell = 1;
   for (int d = 0; d < 3; d++) {

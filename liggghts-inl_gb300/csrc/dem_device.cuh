@@ -132,6 +132,7 @@ struct MeshDev {
   int ntri, wall_type, rolling, moving;
   double distmax, tskin;  // FixNeighlistMesh: bounding-box growth and neighbuild threshold
   double *tri;        // [t*kTriStride]
+  float4 *trif;       // [2t]: node 0, [2t+1]: unit normal, FP32 copies (plane-distance prefilter)
   int *meta;          // [t]
   // fix move/mesh ... linear: every step nodes and centres move by dx =
   // dt*vel; node velocities are vel (0 during the setup force pass)
@@ -161,6 +162,7 @@ struct Sys {
   uint8_t *active;  // [pcap]
   int *scan_tmp;
   float4 *xf;       // FP32 copy (x, y, z, r) of the atoms, refreshed by every drift
+  float4 *xhf;      // FP32 copy of x at the last neighbour build (displacement prefilter)
   int *mlist;       // atoms with candidate mesh triangles [nmax]
   // parameters
   double *params;   // 6 matrices of (nt+1)^2: Y, G, beta, mu, mur, restlog
@@ -177,6 +179,10 @@ struct Sys {
   double ghost_slab;  // cutneighmax/2 + skin/2: CommBrick slab_offset of the ghost band
   float pf_margin;    // relative margin of the FP32 neighbour prefilter (see k_pairs)
   float pf_margin_touch;  // the same for the touching test of k_pair (radsum^2)
+  // FP32 prefilter of the displacement test |x - xhold|^2 > skin^2/4: below
+  // skin_lo2 no atom can have moved, above skin_hi2 it has; in between the
+  // exact FP64 test decides
+  float skin_lo2, skin_hi2;
   // cohesion bond/nonlinear (bond = 0: off, dnum = 3)
   int bond, dnum;
   double *bondp;      // kBondTables matrices of (nt+1)^2

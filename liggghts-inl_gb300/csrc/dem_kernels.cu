@@ -314,7 +314,9 @@ __global__ void k_copy_atoms(Sys s) {
     A.tx[i] = B.tx[i]; A.ty[i] = B.ty[i]; A.tz[i] = B.tz[i];
     A.r[i] = B.r[i]; A.m[i] = B.m[i]; A.dtfm[i] = B.dtfm[i]; A.dtir[i] = B.dtir[i];
     A.type[i] = B.type[i]; A.tag[i] = B.tag[i]; A.lidx[i] = B.lidx[i];
-    s.xf[i] = make_float4((float)B.x[i], (float)B.y[i], (float)B.z[i], (float)B.r[i]);
+    const float4 xf = make_float4((float)B.x[i], (float)B.y[i], (float)B.z[i], (float)B.r[i]);
+    s.xf[i] = xf;
+    s.xhf[i] = xf;  // xhold = x at this build (k_permute)
     for (int w = 0; w < s.nplanes; w++)
       for (int d = 0; d < 3; d++)
         A.whist[(size_t)(w * 3 + d) * s.nmax + i] = B.whist[(size_t)(w * 3 + d) * s.nmax + i];
@@ -373,6 +375,7 @@ __global__ void k_mesh_move(Sys s, int k) {
       moved |= dsq > trigger;
     }
     for (int d = 0; d < 3; d++) g[33 + d] = __dadd_rn(g[33 + d], M.dx[d]);
+    M.trif[2 * (size_t)t] = make_float4((float)g[0], (float)g[1], (float)g[2], 0.f);
   }
   if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(&c->mesh_moved, 1);
 }
@@ -1193,7 +1196,26 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
   // rounding of either side) skip the closest-feature resolution; the
   // resolution would return deltan > 0 and skip them as well
   const double reach = __dmul_rn(__dadd_rn(radi, fmax(0.0, __dmul_rn(cdm1, radi))), 1.0 + 1e-9);
-  for (int q = 0; q < nc; q++) {
+  // FP32 pass over the candidates: the plane distance in FP32 is within
+  // 5*2^-24*S of the FP64 one (S: sum of the magnitudes of the atom's and
+  // node 0's coordinates), so a candidate farther than reach plus 2^-21*S
+  // is beyond reach in FP64 too; the rest take the FP64 path below in
+  // ascending order (the FP64 pipe then issues only for those)
+  unsigned todo = 0u;
+  {
+    const float4 xa = s.xf[i];
+    const float reach_f = (float)reach * (1.0f + 0x1p-20f);
+    for (int q = 0; q < nc; q++) {
+      const int t = M.cand[(size_t)q * nmax + i];
+      const float4 n0 = M.trif[2 * (size_t)t], sn = M.trif[2 * (size_t)t + 1];
+      const float dn = sn.x * (xa.x - n0.x) + sn.y * (xa.y - n0.y) + sn.z * (xa.z - n0.z);
+      const float mag = fabsf(xa.x) + fabsf(xa.y) + fabsf(xa.z) + fabsf(n0.x) + fabsf(n0.y) + fabsf(n0.z);
+      if (!(fabsf(dn) > reach_f + mag * 0x1p-21f)) todo |= 1u << q;
+    }
+  }
+  while (todo) {
+    const int q = __ffs(todo) - 1;
+    todo &= todo - 1u;
     const int t = M.cand[(size_t)q * nmax + i];
     const double *g = M.tri + (size_t)t * kTriStride;
     {
@@ -1257,7 +1279,7 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
 // writes only the wall histories, mesh slots and fm/tm), so the two run side
 // by side; the per-atom kernel adds fm/tm.
 template <int NORMAL>
-__global__ void __launch_bounds__(128) k_wall_force(Sys s, int shearupdate) {
+__global__ void __launch_bounds__(64) k_wall_force(Sys s, int shearupdate) {
   Ctrl *c = s.ctrl;
   if (c->halt) return;
   const AtomArrays &A = s.atoms[0];
@@ -1280,6 +1302,61 @@ __global__ void __launch_bounds__(128) k_wall_force(Sys s, int shearupdate) {
   if (__any_sync(0xffffffffu, meshbad) && (threadIdx.x & 31) == 0) atomicExch(&c->status, kStatMeshSlots);
 }
 
+// Force gather of one atom: its own row (ascending), then its reverse list
+// (ascending), the reference's per-atom order.  The FP64 pipe issues per warp
+// instruction, so additions inside a loop over all list entries cost one
+// issue per entry of the warp's longest row, active or not.  Here a first,
+// integer-only pass collects the active entries of up to 32 entries per list
+// as bit masks; one loop over the set bits then does the FP64 additions, so a
+// warp issues them only as often as its busiest atom has contacts.  A reverse
+// contribution adds the negated force (sign bit flipped on the integer pipe:
+// a + (-b) is exactly a - b) and Tj instead of Ti.
+__device__ __forceinline__ void gather_contacts(const Sys &s, const PairArrays &L, size_t P, int i, double &fx,
+                                                double &fy, double &fz, double &tx, double &ty, double &tz) {
+  const int pb = L.row[i], pe = L.row[i + 1];
+  const int rb = L.rev_start[i], re = L.rev_start[i + 1];
+  if (pe - pb <= 32 && re - rb <= 32) {
+    unsigned om = 0u, rm = 0u;
+    for (int k = 0; k < pe - pb; k++) om |= (s.active[pb + k] ? 1u : 0u) << k;
+    for (int k = 0; k < re - rb; k++) rm |= (s.active[L.rev[rb + k]] ? 1u : 0u) << k;
+    const int cnt = __popc(om) + __popc(rm);
+    for (int t = 0; t < cnt; t++) {
+      int p;
+      unsigned long long sg;
+      const double *T;
+      if (om) {
+        p = pb + __ffs(om) - 1;
+        om &= om - 1u;
+        sg = 0ull;
+        T = s.resTi;
+      } else {
+        p = L.rev[rb + __ffs(rm) - 1];
+        rm &= rm - 1u;
+        sg = 0x8000000000000000ull;
+        T = s.resTj;
+      }
+      fx += __longlong_as_double(__double_as_longlong(s.resF[p]) ^ sg);
+      fy += __longlong_as_double(__double_as_longlong(s.resF[P + p]) ^ sg);
+      fz += __longlong_as_double(__double_as_longlong(s.resF[2 * P + p]) ^ sg);
+      tx += T[p];
+      ty += T[P + p];
+      tz += T[2 * P + p];
+    }
+    return;
+  }
+  for (int p = pb; p < pe; p++) {  // lists longer than 32 entries
+    if (!s.active[p]) continue;
+    fx += s.resF[p]; fy += s.resF[P + p]; fz += s.resF[2 * P + p];
+    tx += s.resTi[p]; ty += s.resTi[P + p]; tz += s.resTi[2 * P + p];
+  }
+  for (int k = rb; k < re; k++) {
+    const int p = L.rev[k];
+    if (!s.active[p]) continue;
+    fx -= s.resF[p]; fy -= s.resF[P + p]; fz -= s.resF[2 * P + p];
+    tx += s.resTj[p]; ty += s.resTj[P + p]; tz += s.resTj[2 * P + p];
+  }
+}
+
 template <int NORMAL, bool GATHER, bool FINAL, bool INITIAL>
 __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
   Ctrl *c = s.ctrl;
@@ -1297,26 +1374,19 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
     double om[3] = {A.wx[i], A.wy[i], A.wz[i]};
     double xv[3] = {A.x[i], A.y[i], A.z[i]};
     if (GATHER) {
-      fx = fy = fz = tx = ty = tz = 0.0;
-      const int pb = L.row[i], pe = L.row[i + 1];
-      for (int p = pb; p < pe; p++) {
-        if (!s.active[p]) continue;
-        fx += s.resF[p]; fy += s.resF[P + p]; fz += s.resF[2 * P + p];
-        tx += s.resTi[p]; ty += s.resTi[P + p]; tz += s.resTi[2 * P + p];
+      // FixGravity::post_force (src/fix_gravity.cpp:329-337) adds m*g after
+      // the pair forces; starting the sum from it instead changes only the
+      // rounding order and saves three FP64 additions
+      if (s.gravity_on) {
+        const double massone = A.m[i];
+        fx = __dmul_rn(massone, s.g[0]);
+        fy = __dmul_rn(massone, s.g[1]);
+        fz = __dmul_rn(massone, s.g[2]);
+      } else {
+        fx = fy = fz = 0.0;
       }
-      const int rb = L.rev_start[i], re = L.rev_start[i + 1];
-      for (int k = rb; k < re; k++) {
-        const int p = L.rev[k];
-        if (!s.active[p]) continue;
-        fx -= s.resF[p]; fy -= s.resF[P + p]; fz -= s.resF[2 * P + p];
-        tx += s.resTj[p]; ty += s.resTj[P + p]; tz += s.resTj[2 * P + p];
-      }
-      if (s.gravity_on) {  // FixGravity::post_force, src/fix_gravity.cpp:329-337
-        const double massone = A.m[i] * 1.;
-        fx = __dadd_rn(fx, __dmul_rn(massone, s.g[0]));
-        fy = __dadd_rn(fy, __dmul_rn(massone, s.g[1]));
-        fz = __dadd_rn(fz, __dmul_rn(massone, s.g[2]));
-      }
+      tx = ty = tz = 0.0;
+      gather_contacts(s, L, P, i, fx, fy, fz, tx, ty, tz);
       if (A.wbits[i] & 0x80u) {  // walls, computed by k_wall_force for this step
         fx += A.fmx[i]; fy += A.fmy[i]; fz += A.fmz[i];
         tx += A.tmx[i]; ty += A.tmy[i]; tz += A.tmz[i];
@@ -1351,17 +1421,31 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
         om[1] = fma(dtir, ty, om[1]);
         om[2] = fma(dtir, tz, om[2]);
         A.x[i] = xv[0]; A.y[i] = xv[1]; A.z[i] = xv[2];
-        s.xf[i] = make_float4((float)xv[0], (float)xv[1], (float)xv[2], (float)A.r[i]);
-        const double dx = __dadd_rn(xv[0], -A.xh[i]);
-        const double dy = __dadd_rn(xv[1], -A.yh[i]);
-        const double dz = __dadd_rn(xv[2], -A.zh[i]);
-        if (rsq_rn(dx, dy, dz) > trigger) moved = true;
-        if (!isfinite(xv[0] + xv[1] + xv[2])) bad = true;
+        const float4 nf = make_float4((float)xv[0], (float)xv[1], (float)xv[2], (float)A.r[i]);
+        s.xf[i] = nf;
+        // Neighbor::check_distance (src/neighbor.cpp:1426-1466) with an FP32
+        // prefilter: only displacements within the rounding band of skin/2
+        // take the exact FP64 test, so the decision is the reference's
+        const float4 hf = s.xhf[i];
+        const float ex = nf.x - hf.x, ey = nf.y - hf.y, ez = nf.z - hf.z;
+        const float rf2 = ex * ex + ey * ey + ez * ez;
+        if (rf2 > s.skin_hi2) {
+          moved = true;
+        } else if (rf2 > s.skin_lo2) {
+          const double dx = __dadd_rn(xv[0], -A.xh[i]);
+          const double dy = __dadd_rn(xv[1], -A.yh[i]);
+          const double dz = __dadd_rn(xv[2], -A.zh[i]);
+          if (rsq_rn(dx, dy, dz) > trigger) moved = true;
+        }
+        // a non-finite coordinate converts to a non-finite float (so does one
+        // beyond the FP32 range, which no granular box reaches)
+        if (!(isfinite(nf.x) && isfinite(nf.y) && isfinite(nf.z))) bad = true;
       }
       A.vx[i] = v[0]; A.vy[i] = v[1]; A.vz[i] = v[2];
       A.wx[i] = om[0]; A.wy[i] = om[1]; A.wz[i] = om[2];
     }
   }
+  (void)shearupdate;
   if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(&c->moved, 1);
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) {
     atomicExch(&c->status, kStatNan);
@@ -1517,8 +1601,11 @@ int launch_wall_force(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaSt
   int lo = 0, hi = 0;
   cudaDeviceGetStreamPriorityRange(&lo, &hi);
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid_for(s.nmax, 128, std::min(lc.max_grid, 304)));
-  cfg.blockDim = dim3(128);
+  // one wall atom per thread in blocks of 64 (a sweep of 32..128 threads and
+  // 304..4864 blocks on the 1M-atom hopper moved the step time by < 3 %:
+  // the kernel is bound by its per-atom chains, not by its launch shape)
+  cfg.gridDim = dim3(grid_for(s.nmax, 64, 2 * lc.max_grid));
+  cfg.blockDim = dim3(64);
   cfg.dynamicSmemBytes = 0;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
