@@ -1278,26 +1278,235 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
 // the pair kernel of the same step (it reads positions and velocities and
 // writes only the wall histories, mesh slots and fm/tm), so the two run side
 // by side; the per-atom kernel adds fm/tm.
+//
+// A block takes a tile of kWallTile listed atoms (one thread each) and, per
+// mesh, runs the FP64-heavy parts densely over the tile's work instead of
+// per atom (the FP64 pipe issues per warp instruction, and atoms differ in
+// their number of candidates and contacts):
+//   A  per atom, FP32: the candidates whose plane is within reach (see
+//      mesh_contacts), queued in ascending order;
+//   B  per queued candidate: exact plane test and closest feature
+//      (TriMesh::resolveTriSphereContactBary), kept when touching;
+//   C  per atom, integer work in candidate order: FixContactHistoryMesh's
+//      slot semantics (handleContact, coplanarContactAlready); an atom whose
+//      new face contact would copy a coplanar neighbour's history
+//      (checkCoplanarContactHistory) takes the sequential path instead,
+//      since that copy depends on the order of the contact updates;
+//   D  per contact: the contact law with the slot's history;
+//   E  per atom: contact forces summed in candidate order, slot clean-up.
+// A tile whose queue would exceed kWallCap entries runs the sequential path
+// for all its atoms.  Both paths give the same result.
+constexpr int kWallTile = 64;
+constexpr int kWallCap = 16 * kWallTile;
+constexpr int kWallRes = 7;  // doubles per queued candidate: deltan, delta[3], vwall[3]; then F[3], T[3]
+
+__device__ __forceinline__ int wall_tile_scan(int v, int &total, int *wsum) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  int base = 0;
+  total = 0;
+  for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+    if (w < warp) base += wsum[w];
+    total += wsum[w];
+  }
+  __syncthreads();
+  return base + inc - v;
+}
+
 template <int NORMAL>
-__global__ void __launch_bounds__(64) k_wall_force(Sys s, int shearupdate) {
+__global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate) {
+  extern __shared__ double wres[];             // [kWallCap * kWallRes]
+  __shared__ unsigned char qa[kWallCap], qq[kWallCap];
+  __shared__ int qst[kWallCap];                // bit 0 touching, bit 1 face, bits 8+: contact slot + 1
+  __shared__ int wsum[kWallTile / 32];
   Ctrl *c = s.ctrl;
   if (c->halt) return;
   const AtomArrays &A = s.atoms[0];
   const int nl = c->nmlist;
+  const size_t nmax = s.nmax;
+  const double cdm1 = s.cdf - 1.0;
   bool meshbad = false;
-  GRID_STRIDE(q, nl) {
-    const int i = s.mlist[q];
-    double v[3] = {A.vx[i], A.vy[i], A.vz[i]};
-    double om[3] = {A.wx[i], A.wy[i], A.wz[i]};
-    double xv[3] = {A.x[i], A.y[i], A.z[i]};
+  for (int base = blockIdx.x * kWallTile; base < nl; base += gridDim.x * kWallTile) {
+    const int a = threadIdx.x;
+    const bool valid = base + a < nl;
+    const int i = valid ? s.mlist[base + a] : 0;
+    double v[3] = {0., 0., 0.}, om[3] = {0., 0., 0.}, xv[3] = {0., 0., 0.};
     double fx = 0., fy = 0., fz = 0., tx = 0., ty = 0., tz = 0.;
-    const uint8_t bits = A.wbits[i];
-    for (int w = 0; w < s.nplanes; w++)
-      if (bits & (1u << w)) plane_contact<NORMAL>(s, A, i, w, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz);
-    for (int k = 0; k < s.nmeshes; k++)
-      mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad);
-    A.fmx[i] = fx; A.fmy[i] = fy; A.fmz[i] = fz;
-    A.tmx[i] = tx; A.tmy[i] = ty; A.tmz[i] = tz;
+    if (valid) {
+      v[0] = A.vx[i]; v[1] = A.vy[i]; v[2] = A.vz[i];
+      om[0] = A.wx[i]; om[1] = A.wy[i]; om[2] = A.wz[i];
+      xv[0] = A.x[i]; xv[1] = A.y[i]; xv[2] = A.z[i];
+      const uint8_t bits = A.wbits[i];
+      for (int w = 0; w < s.nplanes; w++)
+        if (bits & (1u << w)) plane_contact<NORMAL>(s, A, i, w, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz);
+    }
+    for (int k = 0; k < s.nmeshes; k++) {
+      const MeshDev &M = s.meshes[k];
+      int *st = M.slot_tri[0];
+      double *sh = M.slot_hist[0];
+      // ---- A: FP32 candidate pass
+      const int nc = valid ? M.cand_n[i] : 0;
+      const double radi = valid ? A.r[i] : 0.0;
+      const double reach = __dmul_rn(__dadd_rn(radi, fmax(0.0, __dmul_rn(cdm1, radi))), 1.0 + 1e-9);
+      unsigned todo = 0u;
+      if (nc > 0) {
+        const float4 xa = s.xf[i];
+        const float reach_f = (float)reach * (1.0f + 0x1p-20f);
+        for (int q = 0; q < nc; q++) {
+          const int t = M.cand[(size_t)q * nmax + i];
+          const float4 n0 = M.trif[2 * (size_t)t], sn = M.trif[2 * (size_t)t + 1];
+          const float dn = sn.x * (xa.x - n0.x) + sn.y * (xa.y - n0.y) + sn.z * (xa.z - n0.z);
+          const float mag = fabsf(xa.x) + fabsf(xa.y) + fabsf(xa.z) + fabsf(n0.x) + fabsf(n0.y) + fabsf(n0.z);
+          if (!(fabsf(dn) > reach_f + mag * 0x1p-21f)) todo |= 1u << q;
+        }
+      }
+      const int cnt = __popc(todo);
+      int total;
+      const int off = wall_tile_scan(cnt, total, wsum);
+      if (total > kWallCap) {  // sequential path for this tile
+        if (nc > 0) mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad);
+        __syncthreads();
+        continue;
+      }
+      {
+        unsigned m = todo;
+        for (int e = off; m; e++) {
+          qa[e] = (unsigned char)a;
+          qq[e] = (unsigned char)(__ffs(m) - 1);
+          m &= m - 1u;
+        }
+      }
+      __syncthreads();
+      // ---- B: exact plane test and closest feature per queued candidate
+      for (int e = threadIdx.x; e < total; e += kWallTile) {
+        const int ie = s.mlist[base + qa[e]];
+        const int t = M.cand[(size_t)qq[e] * nmax + ie];
+        const double *g = M.tri + (size_t)t * kTriStride;
+        const double xe[3] = {A.x[ie], A.y[ie], A.z[ie]};
+        const double re = A.r[ie];
+        const double reach_e = __dmul_rn(__dadd_rn(re, fmax(0.0, __dmul_rn(cdm1, re))), 1.0 + 1e-9);
+        int state = 0;
+        const double *snv = tri_sn(g), *n0 = tri_node(g, 0);
+        const double dn = snv[0] * (xe[0] - n0[0]) + snv[1] * (xe[1] - n0[1]) + snv[2] * (xe[2] - n0[2]);
+        if (!(fabs(dn) > reach_e)) {
+          double delta[3], bary[3];
+          int bs;
+          const double deltan = resolve_tri_sphere(g, M.meta[t], re, xe, delta, bary, bs);
+          if (!(deltan > s.cutneighmax) && (deltan <= 0 || deltan < cdm1 * re)) {
+            state = 1 | (bs == 7 ? 2 : 0);
+            double *r = wres + (size_t)e * kWallRes;
+            r[0] = deltan;
+            r[1] = delta[0]; r[2] = delta[1]; r[3] = delta[2];
+            double vwall[3] = {0., 0., 0.};
+            if (M.moving && M.vel_on)  // barycentric node velocity, src/fix_wall_gran.cpp:929-934
+              for (int d = 0; d < 3; d++) vwall[d] = (bary[0] * M.vel[d] + bary[1] * M.vel[d] + bary[2] * M.vel[d]);
+            r[4] = vwall[0]; r[5] = vwall[1]; r[6] = vwall[2];
+          }
+        }
+        qst[e] = state;
+      }
+      __syncthreads();
+      // ---- C: slot semantics per atom, in candidate order
+      bool fallback = false;
+      unsigned keep = 0u;
+      int np = 0;
+      if (nc > 0) {
+        np = M.npart[0][i];
+        int stl[kMeshMaxCand];
+        for (int u = 0; u < nc; u++) stl[u] = st[u * nmax + i];
+        unsigned fresh = 0u;
+        for (int e = off; e < off + cnt && !fallback; e++) {
+          if (!(qst[e] & 1)) continue;
+          const int t = M.cand[(size_t)qq[e] * nmax + i];
+          int slot = -1;
+          for (int u = 0; u < nc; u++)
+            if (stl[u] == t) { slot = u; break; }
+          if (slot >= 0) {
+            keep |= 1u << slot;
+          } else {
+            const bool face = (qst[e] & 2) != 0;
+            if (face) {  // coplanarContactAlready
+              bool already = false;
+              for (int u = 0; u < nc; u++)
+                if (stl[u] >= 0 && stl[u] != t && ((keep >> u) & 1u) && mesh_coplanar(M, stl[u], t)) already = true;
+              if (already) continue;
+            }
+            if (np >= nc) { meshbad = true; continue; }
+            for (int u = 0; u < nc; u++)
+              if (stl[u] == -1) { slot = u; break; }
+            if (face)  // checkCoplanarContactHistory would copy: order-dependent
+              for (int u = 0; u < nc; u++)
+                if (stl[u] >= 0 && stl[u] != t && mesh_coplanar(M, stl[u], t)) fallback = true;
+            if (fallback) break;
+            stl[slot] = t;
+            keep |= 1u << slot;
+            fresh |= 1u << slot;
+            np++;
+          }
+          qst[e] |= (slot + 1) << 8;
+        }
+        if (fallback) {
+          for (int e = off; e < off + cnt; e++) qst[e] &= 0xff;
+        } else {
+          for (int u = 0; u < nc; u++)
+            if ((fresh >> u) & 1u) {
+              st[u * nmax + i] = stl[u];
+              for (int d = 0; d < 3; d++) sh[(3 * u + d) * nmax + i] = 0.0;
+            }
+        }
+      }
+      __syncthreads();
+      // ---- D: contact law per contact
+      for (int e = threadIdx.x; e < total; e += kWallTile) {
+        const int slot = (qst[e] >> 8) - 1;
+        if (slot < 0) continue;
+        const int ie = s.mlist[base + qa[e]];
+        double *r = wres + (size_t)e * kWallRes;
+        const double delta[3] = {r[1], r[2], r[3]};
+        const double vwall[3] = {r[4], r[5], r[6]};
+        double ve[3] = {A.vx[ie], A.vy[ie], A.vz[ie]};
+        double oe[3] = {A.wx[ie], A.wy[ie], A.wz[ie]};
+        double cfx = 0., cfy = 0., cfz = 0., ctx = 0., cty = 0., ctz = 0.;
+        wall_force<NORMAL>(s, A, ie, r[0], delta, vwall, M.wall_type, M.rolling != 0,
+                           sh + (size_t)(3 * slot) * nmax + ie, nmax, shearupdate, ve, oe, cfx, cfy, cfz, ctx,
+                           cty, ctz);
+        r[0] = cfx; r[1] = cfy; r[2] = cfz;
+        r[3] = ctx; r[4] = cty; r[5] = ctz;
+      }
+      __syncthreads();
+      // ---- E: sums in candidate order, clean-up (or the sequential path)
+      if (nc > 0) {
+        if (fallback) {
+          mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad);
+        } else {
+          for (int e = off; e < off + cnt; e++) {
+            if ((qst[e] >> 8) == 0) continue;
+            const double *r = wres + (size_t)e * kWallRes;
+            fx += r[0]; fy += r[1]; fz += r[2];
+            tx += r[3]; ty += r[4]; tz += r[5];
+          }
+          for (int u = 0; u < nc; u++)  // cleanUpContacts
+            if (!((keep >> u) & 1u)) {
+              if (st[u * nmax + i] > -1) np--;
+              st[u * nmax + i] = -1;
+              for (int d = 0; d < 3; d++) sh[(3 * u + d) * nmax + i] = 0.0;
+            }
+          M.npart[0][i] = np;
+        }
+      }
+      __syncthreads();
+    }
+    if (valid) {
+      A.fmx[i] = fx; A.fmy[i] = fy; A.fmz[i] = fz;
+      A.tmx[i] = tx; A.tmy[i] = ty; A.tmz[i] = tz;
+    }
   }
   if (__any_sync(0xffffffffu, meshbad) && (threadIdx.x & 31) == 0) atomicExch(&c->status, kStatMeshSlots);
 }
@@ -1601,12 +1810,15 @@ int launch_wall_force(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaSt
   int lo = 0, hi = 0;
   cudaDeviceGetStreamPriorityRange(&lo, &hi);
   cudaLaunchConfig_t cfg = {};
-  // one wall atom per thread in blocks of 64 (a sweep of 32..128 threads and
-  // 304..4864 blocks on the 1M-atom hopper moved the step time by < 3 %:
-  // the kernel is bound by its per-atom chains, not by its launch shape)
-  cfg.gridDim = dim3(grid_for(s.nmax, 64, 2 * lc.max_grid));
-  cfg.blockDim = dim3(64);
-  cfg.dynamicSmemBytes = 0;
+  cfg.gridDim = dim3(grid_for(s.nmax, kWallTile, 2 * lc.max_grid));
+  cfg.blockDim = dim3(kWallTile);
+  cfg.dynamicSmemBytes = (size_t)kWallCap * kWallRes * sizeof(double);
+  static bool smem_set = false;  // more than the 48 KB default of dynamic shared memory
+  if (!smem_set) {
+    cudaFuncSetAttribute(k_wall_force<kHertz>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.dynamicSmemBytes);
+    cudaFuncSetAttribute(k_wall_force<kHooke>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.dynamicSmemBytes);
+    smem_set = true;
+  }
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributePriority;
