@@ -30,11 +30,16 @@ import numpy as np  # noqa: E402
 METRIC = "particle-steps/s (1M Hertz/history spheres)"
 
 # Per-atom FP64 arithmetic (flop, DFMA = 2) and DRAM bytes (read + write) of
-# one launch, from ncu captures of the workload at 500k atoms
-# (profiles/k_pair_hopper1m_500k.md, profiles/k_particle_hopper1m_500k.md).
+# one launch, and the FP64 pipe's active fraction, from ncu captures of the
+# workload at 500k atoms (profiles/k_pair_pf_hopper1m_500k.md,
+# profiles/k_particle_hopper1m_500k.md, profiles/k_wall_force_hopper1m_500k.md).
 PROFILED_PER_ATOM = {
-    "hopper1m": {"pair": {"fp64_flop": 119.2, "dram_bytes": 410.6},
-                 "particle": {"fp64_flop": 54.6, "dram_bytes": 404.5}},
+    "hopper1m": {"pair": {"fp64_flop": 81.6, "dram_bytes": 422.2, "fp64_pipe_active": 0.714},
+                 "particle": {"fp64_flop": 38.7, "dram_bytes": 395.5, "fp64_pipe_active": 0.745},
+                 "wall": {"fp64_flop": 0.256, "dram_bytes": 10.0, "fp64_pipe_active": 0.072},
+                 # touching fraction of the list entries: contact-side additions in
+                 # k_particle (6 per side) over the list length, same capture
+                 "touch_frac": 0.14},
 }
 
 
@@ -269,7 +274,7 @@ def run_gb300(args):
         fp64_peak = api.fp64_peak_tflops()
     except Exception:
         fp64_peak = None
-    frac_touch = 0.5
+    frac_touch = PROFILED_PER_ATOM.get(args.workload, {}).get("touch_frac", 0.5)
     pair_bytes = n * 92 + npairs * 10 + frac_touch * npairs * 144
     part_bytes = n * (15 * 8 * 2 + 8 * 4 + 1) + npairs * (4 + 1 + 72) + frac_touch * npairs * 4
     dom = "pair" if pair_ms >= part_ms else "particle"
@@ -288,14 +293,18 @@ def run_gb300(args):
     if per_atom and fp64_peak:
         flops = per_atom["fp64_flop"] * n
         ach_tf = flops / (dom_ms * 1e-3) / 1e12
-        roof = {"kernel": "k_pair" if dom == "pair" else "k_particle", "bound": "fp64",
+        roof = {"kernel": "k_pair_pf" if dom == "pair" else "k_particle", "bound": "fp64",
                 "achieved": ach_tf, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach_tf / fp64_peak,
                 "traffic": hbm_roof["traffic"],
                 "peak_source": "FP64 FMA peak measured live on this GPU (dem_measure_fp64_peak), "
                                "of measured",
-                "fp64_flop_per_launch": flops, "hbm": hbm_roof}
+                "fp64_flop_per_launch": flops, "hbm": hbm_roof,
+                "fp64_pipe_active_ncu": per_atom.get("fp64_pipe_active"),
+                "note": "flop counts DADD/DMUL + 2*DFMA; the FP64 pipe also issues compares, "
+                        "conversions and the idle lanes of partly active warps, so pipe-active "
+                        "(ncu) exceeds achieved/peak"}
     else:
-        roof = dict(hbm_roof, kernel="k_pair" if dom == "pair" else "k_particle", bound="hbm")
+        roof = dict(hbm_roof, kernel="k_pair_pf" if dom == "pair" else "k_particle", bound="hbm")
     roof.update({"avg_launch_ms": dom_ms,
                  "shares": {"pair": pair_ms / tot_ms, "particle": part_ms / tot_ms,
                             "wall": wall_ms / tot_ms, "neigh": neigh_ms / tot_ms},
