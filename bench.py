@@ -171,6 +171,24 @@ def cpu_sample(name, cores, steps, warm=2, scale=0.01):
 
 
 # ----------------------------------------------------------------------------
+# replicas (N > 1): independent systems, one per rank, no data-path exchange
+# ----------------------------------------------------------------------------
+
+def replica_throughput(dev_ms, atoms, steps, dist=None, device=None):
+    """Whole-job particle-steps/s of N replicas: every rank ran `atoms`
+    atoms for `steps` steps in `dev_ms` ms (its device time); the job's time
+    is the slowest rank's (max over ranks).  Returns (value, max_ms)."""
+    world = 1
+    if dist is not None and dist.is_initialized():
+        import torch
+        world = dist.get_world_size()
+        t = torch.tensor([float(dev_ms)], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    return world * atoms * steps / (dev_ms * 1e-3), dev_ms
+
+
+# ----------------------------------------------------------------------------
 # arms
 # ----------------------------------------------------------------------------
 
@@ -228,13 +246,7 @@ def run_gb300(args):
     cl = clocks.stop()
     st = g.stats()
     kt = g.kernel_times()
-    dev_ms = st["last_step_ms"]
-    if dist:
-        import torch
-        tt = torch.tensor([dev_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        dev_ms = float(tt.item())
-    value = world * n * args.steps / (dev_ms * 1e-3)
+    value, dev_ms = replica_throughput(st["last_step_ms"], n, args.steps, dist, device="cuda")
     # ---- per-kernel times (separate profiled run of the same length)
     g.profile(True)
     g.step(args.steps)
@@ -253,7 +265,7 @@ def run_gb300(args):
     h2d = n * (3 * 3 * 8 + 2 * 8 + 2 * 4)
     d2h = n * (5 * 3 * 8 + 2 * 8 + 2 * 4)
     assert out["x"].shape == (n, 3)
-    e2e = world * n * args.steps / e2e_s
+    e2e, _ = replica_throughput(e2e_s * 1e3, n, args.steps, dist, device="cuda")  # slowest rank
     g2.close()
     # ---- roofline of the dominant kernel
     peaks = measured_peaks()
