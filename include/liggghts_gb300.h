@@ -249,6 +249,30 @@ typedef struct dem_kernel_times {
   double wall_ms;              /* wall kernel: primitive planes and meshes (FixWallGran::post_force) */
   long long wall_launches;
 } dem_kernel_times;
+/* On-device diagnostics of the current state, without downloading the atoms
+ * (long-run acceptance metrics; the reference's ComputeKE and
+ * ComputeERotateSphere, src/compute_ke.cpp, src/compute_erotate_sphere.cpp,
+ * and the total force of each wall as fix mesh/surface/stress and
+ * wall/gran store_force report it).  After dem_setup or dem_step:
+ *   ke_translational = 1/2 sum m v^2, ke_rotational = 1/2 sum 0.4 m r^2 w^2;
+ *   ncontacts = list entries with a contact force in the last force pass;
+ *   solid_volume = sum 4/3 pi r^3 over the atoms whose centre lies in the
+ *   region [lo, hi) (NULL: the box), packing_fraction = solid_volume over
+ *   the region's volume;
+ *   wall_force[w] = total force of wall w on the atoms in the last force
+ *   pass, walls numbered in the order they were added, planes first, then
+ *   meshes (nwalls of them, at most DEM_DIAG_MAX_WALLS).
+ * Sums are deterministic (fixed block order). */
+#define DEM_DIAG_MAX_WALLS 16
+typedef struct dem_diagnostics {
+  double ke_translational, ke_rotational;
+  long long ncontacts;
+  double solid_volume, packing_fraction;
+  int nwalls;
+  double wall_force[DEM_DIAG_MAX_WALLS][3];
+} dem_diagnostics;
+int dem_get_diagnostics(dem_handle *h, const double *region_lo, const double *region_hi, dem_diagnostics *out);
+
 int dem_profile(dem_handle *h, int enable);
 int dem_get_kernel_times(dem_handle *h, dem_kernel_times *out);
 

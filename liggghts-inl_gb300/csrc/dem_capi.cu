@@ -36,6 +36,7 @@ struct dem_handle {
   std::string err;
   bool have_params = false, have_atoms = false, setup_done = false;
   std::vector<void *> allocs_atoms, allocs_pairs, allocs_misc;
+  double *diag_buf = nullptr;  // dem_get_diagnostics partial sums
   LaunchCfg lc{152 * 8};
   float last_ms = 0.f;
   Ctrl host_ctrl{};
@@ -159,6 +160,8 @@ static int alloc_atoms(dem_handle *h, int nmax) {
   CUDA_TRY(h, dalloc(L, &s.xf, nmax));
   CUDA_TRY(h, dalloc(L, &s.xhf, nmax));
   CUDA_TRY(h, dalloc(L, &s.mlist, nmax));
+  CUDA_TRY(h, dalloc(L, &s.wforce, (size_t)3 * std::max(1, s.nplanes + s.nmeshes) * nmax));
+  CUDA_TRY(h, cudaMemset(s.wforce, 0, (size_t)3 * std::max(1, s.nplanes + s.nmeshes) * nmax * sizeof(double)));
   CUDA_TRY(h, dalloc(L, &s.order, nmax));
   CUDA_TRY(h, dalloc(L, &s.pcount, nmax + 1));
   CUDA_TRY(h, dalloc(L, &s.rev_count, nmax + 1));
@@ -350,6 +353,7 @@ int dem_destroy(dem_handle *h) {
   free_list(h->allocs_pairs);
   free_list(h->allocs_atoms);
   free_list(h->allocs_misc);
+  if (h->diag_buf) cudaFree(h->diag_buf);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
   for (auto &e : h->evpool) cudaEventDestroy(e);
@@ -993,6 +997,54 @@ int dem_step(dem_handle *h, int nsteps) {
   rc = recover(h, &dummy);
   if (rc) return rc;
   cudaEventElapsedTime(&h->last_ms, h->ev0, h->ev1);
+  return DEM_OK;
+}
+
+int dem_get_diagnostics(dem_handle *h, const double *region_lo, const double *region_hi, dem_diagnostics *out) {
+  if (!h || !out || !h->have_atoms || !h->setup_done) return DEM_ERR_BAD_ARG;
+  const Sys &s = h->s;
+  const int nw = s.nplanes + s.nmeshes;
+  if (nw > DEM_DIAG_MAX_WALLS) return fail(h, DEM_ERR_BAD_ARG, "more walls than DEM_DIAG_MAX_WALLS");
+  double lo[3], hi[3];
+  for (int d = 0; d < 3; d++) {
+    lo[d] = region_lo ? region_lo[d] : s.boxlo[d];
+    hi[d] = region_hi ? region_hi[d] : s.boxhi[d];
+    if (!(hi[d] > lo[d])) return fail(h, DEM_ERR_BAD_ARG, "empty diagnostics region");
+  }
+  const int nb = 2 * 152;
+  if (!h->diag_buf) {
+    CUDA_TRY(h, cudaMalloc(&h->diag_buf, (size_t)(nb * 3 + nb * 3 * DEM_DIAG_MAX_WALLS + 1) * sizeof(double)));
+  }
+  double *pa = h->diag_buf, *pw = pa + nb * 3;
+  unsigned long long *cnt = reinterpret_cast<unsigned long long *>(pw + nb * 3 * DEM_DIAG_MAX_WALLS);
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  h->kt.kernel_launches += launch_diagnostics(s, h->lc, lo, hi, pa, pw, cnt, nb, h->st);
+  CUDA_TRY(h, cudaGetLastError());
+  std::vector<double> host((size_t)nb * 3 + (size_t)nb * 3 * DEM_DIAG_MAX_WALLS + 1);
+  CUDA_TRY(h, cudaMemcpyAsync(host.data(), h->diag_buf, host.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  double ke = 0.0, er = 0.0, vol = 0.0;
+  for (int b = 0; b < nb; b++) {
+    ke += host[3 * b];
+    er += host[3 * b + 1];
+    vol += host[3 * b + 2];
+  }
+  std::memset(out, 0, sizeof(*out));
+  out->ke_translational = 0.5 * ke;          // ComputeKE: scalar *= 0.5 * mvv2e
+  out->ke_rotational = 0.5 * 0.4 * er;       // ComputeERotateSphere: scalar *= 0.5 * INERTIA * mvv2e
+  out->solid_volume = 4.0 * M_PI / 3.0 * vol;
+  out->packing_fraction = out->solid_volume / ((hi[0] - lo[0]) * (hi[1] - lo[1]) * (hi[2] - lo[2]));
+  out->nwalls = nw;
+  for (int w = 0; w < nw; w++)
+    for (int d = 0; d < 3; d++) {
+      double acc = 0.0;
+      for (int b = 0; b < nb; b++) acc += host[(size_t)nb * 3 + ((size_t)b * nw + w) * 3 + d];
+      out->wall_force[w][d] = acc;
+    }
+  unsigned long long nc = 0;
+  std::memcpy(&nc, &host[host.size() - 1], sizeof(nc));
+  out->ncontacts = (long long)nc;
   return DEM_OK;
 }
 

@@ -164,6 +164,8 @@ struct Sys {
   float4 *xf;       // FP32 copy (x, y, z, r) of the atoms, refreshed by every drift
   float4 *xhf;      // FP32 copy of x at the last neighbour build (displacement prefilter)
   int *mlist;       // atoms with candidate mesh triangles [nmax]
+  double *wforce;   // [(w*3+d)*nmax + i]: force of wall w (planes, then meshes) on listed
+                    // atom i at the last force evaluation (diagnostics)
   // parameters
   double *params;   // 6 matrices of (nt+1)^2: Y, G, beta, mu, mur, restlog
   int ntypes;

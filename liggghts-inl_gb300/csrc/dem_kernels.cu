@@ -1180,7 +1180,7 @@ __device__ __forceinline__ bool mesh_coplanar(const MeshDev &M, int a, int b) {
 template <int NORMAL>
 __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, int shearupdate,
                               double v[3], double om[3], double xv[3], double &fx, double &fy,
-                              double &fz, double &tx, double &ty, double &tz, bool &bad) {
+                              double &fz, double &tx, double &ty, double &tz, bool &bad, double msum[3]) {
   const MeshDev &M = s.meshes[k];
   const int nc = M.cand_n[i];
   if (nc == 0) return;
@@ -1260,8 +1260,12 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
     double vwall[3] = {0., 0., 0.};
     if (M.moving && M.vel_on)  // barycentric node velocity, src/fix_wall_gran.cpp:929-934
       for (int d = 0; d < 3; d++) vwall[d] = (bary[0] * M.vel[d] + bary[1] * M.vel[d] + bary[2] * M.vel[d]);
+    double cfx = 0., cfy = 0., cfz = 0., ctx = 0., cty = 0., ctz = 0.;
     wall_force<NORMAL>(s, A, i, deltan, delta, vwall, M.wall_type, M.rolling != 0,
-                       sh + (size_t)(3 * slot) * nmax + i, nmax, shearupdate, v, om, fx, fy, fz, tx, ty, tz);
+                       sh + (size_t)(3 * slot) * nmax + i, nmax, shearupdate, v, om, cfx, cfy, cfz, ctx, cty, ctz);
+    fx += cfx; fy += cfy; fz += cfz;
+    tx += ctx; ty += cty; tz += ctz;
+    msum[0] += cfx; msum[1] += cfy; msum[2] += cfz;
   }
   for (int u = 0; u < nc; u++)  // cleanUpContacts
     if (!((keep >> u) & 1u)) {
@@ -1344,8 +1348,15 @@ __global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate
       om[0] = A.wx[i]; om[1] = A.wy[i]; om[2] = A.wz[i];
       xv[0] = A.x[i]; xv[1] = A.y[i]; xv[2] = A.z[i];
       const uint8_t bits = A.wbits[i];
-      for (int w = 0; w < s.nplanes; w++)
-        if (bits & (1u << w)) plane_contact<NORMAL>(s, A, i, w, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz);
+      for (int w = 0; w < s.nplanes; w++) {
+        double pfx = 0., pfy = 0., pfz = 0., ptx = 0., pty = 0., ptz = 0.;
+        if (bits & (1u << w)) plane_contact<NORMAL>(s, A, i, w, shearupdate, v, om, xv, pfx, pfy, pfz, ptx, pty, ptz);
+        fx += pfx; fy += pfy; fz += pfz;
+        tx += ptx; ty += pty; tz += ptz;
+        s.wforce[(size_t)(3 * w) * nmax + i] = pfx;
+        s.wforce[(size_t)(3 * w + 1) * nmax + i] = pfy;
+        s.wforce[(size_t)(3 * w + 2) * nmax + i] = pfz;
+      }
     }
     for (int k = 0; k < s.nmeshes; k++) {
       const MeshDev &M = s.meshes[k];
@@ -1370,8 +1381,12 @@ __global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate
       const int cnt = __popc(todo);
       int total;
       const int off = wall_tile_scan(cnt, total, wsum);
+      double msum[3] = {0., 0., 0.};
+      double *const wf = s.wforce + (size_t)(3 * (s.nplanes + k)) * nmax;
       if (total > kWallCap) {  // sequential path for this tile
-        if (nc > 0) mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad);
+        if (nc > 0) mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad, msum);
+        if (valid)
+          for (int d = 0; d < 3; d++) wf[(size_t)d * nmax + i] = msum[d];
         __syncthreads();
         continue;
       }
@@ -1484,13 +1499,14 @@ __global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate
       // ---- E: sums in candidate order, clean-up (or the sequential path)
       if (nc > 0) {
         if (fallback) {
-          mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad);
+          mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad, msum);
         } else {
           for (int e = off; e < off + cnt; e++) {
             if ((qst[e] >> 8) == 0) continue;
             const double *r = wres + (size_t)e * kWallRes;
             fx += r[0]; fy += r[1]; fz += r[2];
             tx += r[3]; ty += r[4]; tz += r[5];
+            msum[0] += r[0]; msum[1] += r[1]; msum[2] += r[2];
           }
           for (int u = 0; u < nc; u++)  // cleanUpContacts
             if (!((keep >> u) & 1u)) {
@@ -1501,6 +1517,8 @@ __global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate
           M.npart[0][i] = np;
         }
       }
+      if (valid)
+        for (int d = 0; d < 3; d++) wf[(size_t)d * nmax + i] = msum[d];
       __syncthreads();
     }
     if (valid) {
@@ -1659,6 +1677,84 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) {
     atomicExch(&c->status, kStatNan);
   }
+}
+
+// ----------------------------------------------------------------------------
+// diagnostics (dem_get_diagnostics): deterministic per-block partial sums,
+// added in block order by the host
+// ----------------------------------------------------------------------------
+
+constexpr int kDiagBlock = 256;
+
+__device__ __forceinline__ double block_sum(double v, double *sm) {
+  sm[threadIdx.x] = v;
+  __syncthreads();
+  for (int st = kDiagBlock / 2; st > 0; st >>= 1) {
+    if (threadIdx.x < st) sm[threadIdx.x] += sm[threadIdx.x + st];
+    __syncthreads();
+  }
+  const double r = sm[0];
+  __syncthreads();
+  return r;
+}
+
+// ComputeKE (sum m v^2), ComputeERotateSphere (sum w^2 r^2 m) and the solid
+// volume (sum r^3) of the atoms whose centre lies in [lo, hi)
+__global__ void __launch_bounds__(kDiagBlock) k_diag_atoms(Sys s, double3 lo, double3 hi, double *part) {
+  __shared__ double sm[kDiagBlock];
+  const AtomArrays &A = s.atoms[0];
+  const int n = s.ctrl->n;
+  double ke = 0.0, er = 0.0, vol = 0.0;
+  GRID_STRIDE(i, n) {
+    const double m = A.m[i], r = A.r[i];
+    ke += m * (A.vx[i] * A.vx[i] + A.vy[i] * A.vy[i] + A.vz[i] * A.vz[i]);
+    er += (A.wx[i] * A.wx[i] + A.wy[i] * A.wy[i] + A.wz[i] * A.wz[i]) * r * r * m;
+    const double x = A.x[i], y = A.y[i], z = A.z[i];
+    if (x >= lo.x && x < hi.x && y >= lo.y && y < hi.y && z >= lo.z && z < hi.z) vol += r * r * r;
+  }
+  ke = block_sum(ke, sm);
+  er = block_sum(er, sm);
+  vol = block_sum(vol, sm);
+  if (threadIdx.x == 0) {
+    part[3 * blockIdx.x] = ke;
+    part[3 * blockIdx.x + 1] = er;
+    part[3 * blockIdx.x + 2] = vol;
+  }
+}
+
+// per-wall force sums over the listed wall atoms: part[(blk*nw + w)*3 + d]
+__global__ void __launch_bounds__(kDiagBlock) k_diag_walls(Sys s, int nw, double *part) {
+  __shared__ double sm[kDiagBlock];
+  const int nl = s.ctrl->nmlist;
+  for (int w = 0; w < nw; w++)
+    for (int d = 0; d < 3; d++) {
+      const double *wf = s.wforce + (size_t)(3 * w + d) * s.nmax;
+      double acc = 0.0;
+      GRID_STRIDE(q, nl) acc += wf[s.mlist[q]];
+      acc = block_sum(acc, sm);
+      if (threadIdx.x == 0) part[((size_t)blockIdx.x * nw + w) * 3 + d] = acc;
+    }
+}
+
+// list entries with a contact force in the last force evaluation
+__global__ void k_diag_contacts(Sys s, unsigned long long *cnt) {
+  const int np = s.ctrl->np;
+  unsigned long long c = 0;
+  GRID_STRIDE(p, np) c += s.active[p] ? 1ull : 0ull;
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(cnt, c);
+}
+
+int launch_diagnostics(const Sys &s, const LaunchCfg &lc, const double lo[3], const double hi[3], double *part_atoms,
+                       double *part_walls, unsigned long long *contacts, int nblocks, cudaStream_t st) {
+  const int nw = s.nplanes + s.nmeshes;
+  k_diag_atoms<<<nblocks, kDiagBlock, 0, st>>>(s, make_double3(lo[0], lo[1], lo[2]),
+                                               make_double3(hi[0], hi[1], hi[2]), part_atoms);
+  if (nw > 0) k_diag_walls<<<nblocks, kDiagBlock, 0, st>>>(s, nw, part_walls);
+  cudaMemsetAsync(contacts, 0, sizeof(unsigned long long), st);
+  const int gc = (int)std::max<long>(1, std::min<long>(((long)s.pcap + 255) / 256, lc.max_grid));
+  k_diag_contacts<<<gc, 256, 0, st>>>(s, contacts);
+  return nw > 0 ? 3 : 2;
 }
 
 // ----------------------------------------------------------------------------

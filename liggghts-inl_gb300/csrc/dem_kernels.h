@@ -19,6 +19,8 @@ enum {
 
 // exclusive prefix sum of len ints (len <= 4096*4096 - 1); tmp holds
 // (len+4095)/4096 + 1 ints; gate: skip unless the system rebuilds
+int launch_diagnostics(const Sys &s, const LaunchCfg &lc, const double lo[3], const double hi[3], double *part_atoms,
+                       double *part_walls, unsigned long long *contacts, int nblocks, cudaStream_t st);
 int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, bool gate,
                    cudaStream_t st);
 int launch_decide(const Sys &s, cudaStream_t st);

@@ -66,6 +66,13 @@ class DemKernelTimes(ctypes.Structure):
                 ("wall_launches", ctypes.c_longlong)]
 
 
+class DemDiagnostics(ctypes.Structure):
+    _fields_ = [("ke_translational", ctypes.c_double), ("ke_rotational", ctypes.c_double),
+                ("ncontacts", ctypes.c_longlong), ("solid_volume", ctypes.c_double),
+                ("packing_fraction", ctypes.c_double), ("nwalls", ctypes.c_int),
+                ("wall_force", (ctypes.c_double * 3) * 16)]
+
+
 _lib = None
 P = ctypes.c_void_p
 
@@ -110,6 +117,7 @@ def load(build=True):
     L.dem_profile.argtypes = [P, I]
     L.dem_get_kernel_times.argtypes = [P, ctypes.POINTER(DemKernelTimes)]
     L.dem_measure_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
+    L.dem_get_diagnostics.argtypes = [P, P, P, ctypes.POINTER(DemDiagnostics)]
     _lib = L
     return L
 
@@ -275,6 +283,21 @@ class DemSystem:
         h = np.zeros((self.natoms(), 3))
         self._check(load().dem_download_wall_history(self.h, int(w), _p(h)))
         return h
+
+    def diagnostics(self, region=None):
+        """dem_get_diagnostics: kinetic energies, contact count, solid volume
+        and packing fraction of the atoms centred in region=(lo, hi) (None:
+        the box), per-wall total forces of the last force pass."""
+        d = DemDiagnostics()
+        lo = hi = None
+        if region is not None:
+            lo = np.ascontiguousarray(region[0], dtype=np.float64)
+            hi = np.ascontiguousarray(region[1], dtype=np.float64)
+        self._check(load().dem_get_diagnostics(self.h, _p(lo), _p(hi), ctypes.byref(d)))
+        wf = np.array([[d.wall_force[w][k] for k in range(3)] for w in range(d.nwalls)]).reshape(-1, 3)
+        return dict(ke_translational=d.ke_translational, ke_rotational=d.ke_rotational,
+                    ncontacts=int(d.ncontacts), solid_volume=d.solid_volume,
+                    packing_fraction=d.packing_fraction, wall_force=wf)
 
     def stats(self):
         s = DemStats()

@@ -87,6 +87,9 @@ def lib():
         L.orc_set_mesh_motion.argtypes = [P, ctypes.c_int] + [ctypes.c_double] * 3
         L.orc_get_mesh_nodes.argtypes = [P, ctypes.c_int, P]
         L.orc_get_mesh_contacts.argtypes = [P, ctypes.c_int, P, P, P, P]
+        L.orc_ncontacts.restype = ctypes.c_longlong
+        L.orc_ncontacts.argtypes = [P]
+        L.orc_get_wall_forces.argtypes = [P, P]
         _lib = L
     return _lib
 
@@ -226,6 +229,14 @@ class Oracle:
                    hist=np.zeros((n, 3)))
         L.orc_get_mesh_contacts(self.h, int(k), *[_p(out[q]) for q in ("tag", "tri", "slot", "hist")])
         return out
+
+    def diagnostics(self):
+        """Entries with a contact force and the per-wall total forces of the
+        last force pass (planes, then meshes)."""
+        L = lib()
+        out = np.zeros((16, 3))
+        nw = L.orc_get_wall_forces(self.h, _p(out))
+        return dict(ncontacts=int(L.orc_ncontacts(self.h)), wall_force=out[:nw].copy())
 
     def wall_history(self, w):
         L = lib()

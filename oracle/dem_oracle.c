@@ -51,6 +51,11 @@ typedef struct {
 
 struct orc_sys {
   orc_config cfg;
+  /* diagnostics of the last force pass: entries with a contact force, and
+   * the total force of each wall (planes, then meshes) on the atoms */
+  long long ncontacts;
+  double wall_f[3 * ORC_DIAG_MAX_WALLS];
+  double *cur_wall_f;
   char err[256];
   int ntypes;
   double *Yeff, *Geff, *betaeff, *frict, *rollfrict, *restlog;
@@ -1258,6 +1263,7 @@ static void pair_compute(orc_sys *s, int shearupdate) {
         has_force = sd.has_force_update;
       }
       if (has_force) {
+        s->ncontacts++;
         for (int d = 0; d < 3; d++) {
           s->f[3 * i + d] += 1.0 * fi.dF[d];
           s->torque[3 * i + d] += 1.0 * fi.dT[d];
@@ -1315,6 +1321,7 @@ static void wall_contact(orc_sys *s, int ip, double deltan, const double *delta,
     for (int d = 0; d < 3; d++) {
       s->f[3 * ip + d] += fi.dF[d];
       s->torque[3 * ip + d] += fi.dT[d];
+      if (s->cur_wall_f) s->cur_wall_f[d] += fi.dF[d];
     }
   } else {
     surfaces_close(&sd);
@@ -1551,6 +1558,8 @@ static void mesh_post_force(orc_sys *s, orc_mesh *m, int shearupdate) {
 static void force_clear(orc_sys *s) {
   memset(s->f, 0, 3 * (size_t)s->n * sizeof(double));
   memset(s->torque, 0, 3 * (size_t)s->n * sizeof(double));
+  s->ncontacts = 0;
+  memset(s->wall_f, 0, sizeof s->wall_f);
 }
 
 static void initial_integrate(orc_sys *s) {
@@ -1626,8 +1635,16 @@ static void compute_forces(orc_sys *s, int shearupdate) {
   force_clear(s);
   pair_compute(s, shearupdate);
   gravity_post_force(s);
-  for (int w = 0; w < s->nplanes; w++) plane_post_force(s, &s->planes[w], shearupdate);
-  for (int k = 0; k < s->nmeshes; k++) mesh_post_force(s, &s->meshes[k], shearupdate);
+  for (int w = 0; w < s->nplanes; w++) {
+    s->cur_wall_f = w < ORC_DIAG_MAX_WALLS ? &s->wall_f[3 * w] : NULL;
+    plane_post_force(s, &s->planes[w], shearupdate);
+  }
+  for (int k = 0; k < s->nmeshes; k++) {
+    const int w = s->nplanes + k;
+    s->cur_wall_f = w < ORC_DIAG_MAX_WALLS ? &s->wall_f[3 * w] : NULL;
+    mesh_post_force(s, &s->meshes[k], shearupdate);
+  }
+  s->cur_wall_f = NULL;
 }
 
 int orc_setup(orc_sys *s) {
@@ -1655,6 +1672,15 @@ int orc_run(orc_sys *s, int nsteps) {
     final_integrate(s);
   }
   return 0;
+}
+
+/* diagnostics of the last force pass (see dem_get_diagnostics) */
+long long orc_ncontacts(const orc_sys *s) { return s->ncontacts; }
+int orc_get_wall_forces(const orc_sys *s, double *out) {
+  const int nw = s->nplanes + s->nmeshes;
+  for (int w = 0; w < nw && w < ORC_DIAG_MAX_WALLS; w++)
+    for (int d = 0; d < 3; d++) out[3 * w + d] = s->wall_f[3 * w + d];
+  return nw;
 }
 
 int orc_natoms(const orc_sys *s) { return s->n; }

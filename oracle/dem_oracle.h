@@ -107,6 +107,11 @@ int orc_set_wall_history(orc_sys *s, int wall, const double *hist);
 int orc_setup(orc_sys *s);            /* Verlet::setup */
 int orc_run(orc_sys *s, int nsteps);  /* nsteps iterations of Verlet::run */
 
+#define ORC_DIAG_MAX_WALLS 16
+/* entries with a contact force, and the total force of each wall (planes,
+ * then meshes; 3 doubles each) in the last force pass */
+long long orc_ncontacts(const orc_sys *s);
+int orc_get_wall_forces(const orc_sys *s, double *out);
 int orc_natoms(const orc_sys *s);
 int orc_get_atoms(const orc_sys *s, int *tag, int *type, double *x, double *v, double *omega,
                   double *f, double *torque, double *radius, double *rmass);

@@ -316,3 +316,46 @@ def test_gpu_deterministic_bitwise():
         g.close()
     for k in ("x", "v", "omega", "f", "torque"):
         assert np.array_equal(runs[0][k], runs[1][k]), k
+
+
+@pytest.mark.parametrize("name", ["hopper_mesh", "fibre_press"])
+def test_gpu_diagnostics_match_oracle(name):
+    """dem_get_diagnostics against the oracle through the non-chaotic window:
+    kinetic energies from the oracle's atoms, contact count and per-wall
+    total forces from the oracle's last force pass, solid volume in a
+    sub-region."""
+    from oracle.binding import Oracle
+    case, _ = load_golden(name)
+    g = _gpu(case)
+    o = Oracle(case)
+    g.setup()
+    o.setup()
+    lo = np.asarray(case["boxlo"], dtype=float)
+    hi = np.asarray(case["boxhi"], dtype=float)
+    region = (lo, lo + 0.5 * (hi - lo))
+    done = 0
+    for chunk in (0, 1, 9, 40):
+        if chunk:
+            g.step(chunk)
+            o.run(chunk)
+            done += chunk
+        d = g.diagnostics()
+        r = o.diagnostics()
+        a = sort_by_tag(o.atoms())
+        m, rad = a["rmass"], a["radius"]
+        ke = 0.5 * np.sum(m * np.sum(a["v"] ** 2, axis=1))
+        er = 0.5 * 0.4 * np.sum(m * rad ** 2 * np.sum(a["omega"] ** 2, axis=1))
+        tol = 1e-11 if done <= 10 else 1e-7
+        assert abs(d["ke_translational"] - ke) <= tol * ke, (name, done)
+        assert abs(d["ke_rotational"] - er) <= tol * max(er, 1e-300), (name, done)
+        assert d["ncontacts"] == r["ncontacts"], (name, done, d["ncontacts"], r["ncontacts"])
+        wf = d["wall_force"]
+        assert wf.shape == r["wall_force"].shape
+        scale = max(np.abs(a["f"]).max(), np.abs(r["wall_force"]).max())
+        assert np.abs(wf - r["wall_force"]).max() <= tol * scale, (name, done, wf, r["wall_force"])
+        inside = np.all((a["x"] >= region[0]) & (a["x"] < region[1]), axis=1)
+        vol = 4.0 * np.pi / 3.0 * np.sum(rad[inside] ** 3)
+        dr = g.diagnostics(region)
+        assert abs(dr["solid_volume"] - vol) <= 1e-12 * max(vol, 1e-300), (name, done)
+        assert abs(dr["packing_fraction"] - vol / np.prod(region[1] - region[0])) <= 1e-12
+    g.close()
