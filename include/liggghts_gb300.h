@@ -184,6 +184,14 @@ int dem_add_mesh(dem_handle *h, int ntri, const double *nodes, int wall_type, in
  * skin/2 since the last neighbour build forces a build at the next step
  * (FixMesh::pre_force, MultiNodeMesh::decideRebuild).  Before dem_upload_atoms. */
 int dem_set_mesh_motion(dem_handle *h, int mesh_id, const double *vel);
+/* fix move/mesh mesh ID rotate origin O axis A period T (MeshMoverRotate,
+ * src/mesh_mover_rotation.cpp:66-131): every step after the particles' drift
+ * the mesh turns by 2 pi dt / T about the axis through O (nodes, centres and
+ * the element vectors, in the reference's quaternion arithmetic, so nodes
+ * match bit for bit); node velocities are w x (node - O) (0 in the dem_setup
+ * force pass); node travel beyond skin/2 forces a rebuild as with linear
+ * motion.  One mover per mesh; before dem_upload_atoms. */
+int dem_set_mesh_rotation(dem_handle *h, int mesh_id, const double *origin, const double *axis, double period);
 /* Current node positions of a mesh, ntri*9 in element order. */
 int dem_download_mesh_nodes(dem_handle *h, int mesh_id, double *nodes);
 

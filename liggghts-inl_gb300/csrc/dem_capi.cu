@@ -604,6 +604,50 @@ int dem_set_mesh_motion(dem_handle *h, int mesh_id, const double *vel) {
   return DEM_OK;
 }
 
+int dem_set_mesh_rotation(dem_handle *h, int mesh_id, const double *origin, const double *axis, double period) {
+  if (!h || !origin || !axis || mesh_id < 0 || mesh_id >= h->s.nmeshes) return DEM_ERR_BAD_ARG;
+  if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "set mesh motion before uploading atoms");
+  if (!(period != 0.0) || !std::isfinite(period)) return fail(h, DEM_ERR_BAD_ARG, "bad rotation period");
+  MeshDev &M = h->s.meshes[mesh_id];
+  if (M.moving) return fail(h, DEM_ERR_BAD_ARG, "one mover per mesh");
+  // MeshMoverRotate: axis_ normalised by vectorNormalize3D, omega_ = 2 pi / T
+  double ax[3] = {axis[0], axis[1], axis[2]};
+  const double norm = std::sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+  if (!(norm > 0.0)) return fail(h, DEM_ERR_BAD_ARG, "zero rotation axis");
+  const double invnorm = 1. / norm;
+  for (int d = 0; d < 3; d++) ax[d] *= invnorm;
+  const double omega = 2. * M_PI / period;
+  const double dangle = omega * h->s.dt;  // incrementalPhi = omega_ * dt
+  // MultiNodeMesh::rotate(dAngle, axis, p): axisNorm = axis / |axis|, dQ
+  double an[3] = {ax[0], ax[1], ax[2]};
+  const double mag = std::sqrt(an[0] * an[0] + an[1] * an[1] + an[2] * an[2]);
+  const double sinv = 1. / mag;
+  for (int d = 0; d < 3; d++) an[d] = sinv * an[d];
+  M.rq[0] = std::cos(dangle * 0.5);
+  for (int d = 0; d < 3; d++) M.rq[d + 1] = an[d] * std::sin(dangle * 0.5);
+  for (int d = 0; d < 3; d++) {
+    M.rorig[d] = origin[d];
+    M.romega[d] = ax[d] * omega;  // vectorScalarMult3D(axis_, omega_, omegaVec)
+    M.vel[d] = 0.0;
+    M.dx[d] = 0.0;
+  }
+  CUDA_TRY(h, dalloc(h->allocs_misc, &M.nodev, (size_t)9 * M.ntri));
+  CUDA_TRY(h, cudaMemset(M.nodev, 0, (size_t)9 * M.ntri * sizeof(double)));
+  if (!M.node_last) {
+    CUDA_TRY(h, dalloc(h->allocs_misc, &M.node_last, (size_t)9 * M.ntri));
+    std::vector<double> nl((size_t)9 * M.ntri);
+    const MeshHost &mh = h->mesh_host[mesh_id];
+    for (int t = 0; t < M.ntri; t++)
+      for (int q = 0; q < 9; q++) nl[(size_t)t * 9 + q] = mh.tri[(size_t)t * kTriStride + q];
+    CUDA_TRY(h, cudaMemcpy(M.node_last, nl.data(), nl.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  M.rotating = 1;
+  M.moving = 1;
+  M.vel_on = 0;
+  h->sys_gen++;
+  return DEM_OK;
+}
+
 int dem_download_mesh_nodes(dem_handle *h, int mesh_id, double *nodes) {
   if (!h || !nodes || mesh_id < 0 || mesh_id >= h->s.nmeshes) return DEM_ERR_BAD_ARG;
   CUDA_TRY(h, cudaStreamSynchronize(h->st));

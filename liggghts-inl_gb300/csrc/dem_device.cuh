@@ -138,6 +138,12 @@ struct MeshDev {
   // dt*vel; node velocities are vel (0 during the setup force pass)
   double vel[3], dx[3];
   int vel_on;
+  // fix move/mesh ... rotate origin O axis A period T: per-step quaternion
+  // (MultiNodeMesh::rotate), origin, angular velocity vector, node
+  // velocities w x (node - O) [t*9]
+  int rotating;
+  double rq[4], rorig[3], romega[3];
+  double *nodev;
   double *node_last;  // node positions at the last neighbour build [t*9]
   int *cn_start, *cn_list;          // coplanar node-neighbours (areCoplanarNodeNeighs)
   int *tc_count, *tc_start, *tc_fill, *tc_list;  // triangles registered per atom cell

@@ -356,6 +356,79 @@ __device__ __forceinline__ void mslot_swap(const MeshDev &M, size_t nmax, int i,
 // MultiNodeMesh::decideRebuild (any node > skin/2 from its position at the
 // last build, src/multi_node_mesh_I.h:792-823); the decision is used by
 // k_decide only on steps that do not rebuild anyway (FixMesh::pre_force).
+// MathExtra::quatquat (src/math_extra.h:596-602) and
+// MathExtraLiggghts::vec_quat_rotate (src/math_extra_liggghts.h:455-471) in
+// the reference's operation order, exactly rounded: rotated nodes are
+// bit-identical to the reference's
+__device__ __forceinline__ void quatquat_rn(const double *a, const double *b, double *c) {
+  c[0] = __dsub_rn(__dsub_rn(__dsub_rn(__dmul_rn(a[0], b[0]), __dmul_rn(a[1], b[1])), __dmul_rn(a[2], b[2])),
+                   __dmul_rn(a[3], b[3]));
+  c[1] = __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(a[0], b[1]), __dmul_rn(b[0], a[1])), __dmul_rn(a[2], b[3])),
+                   __dmul_rn(a[3], b[2]));
+  c[2] = __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(a[0], b[2]), __dmul_rn(b[0], a[2])), __dmul_rn(a[3], b[1])),
+                   __dmul_rn(a[1], b[3]));
+  c[3] = __dsub_rn(__dadd_rn(__dadd_rn(__dmul_rn(a[0], b[3]), __dmul_rn(b[0], a[3])), __dmul_rn(a[1], b[2])),
+                   __dmul_rn(a[2], b[1]));
+}
+__device__ __forceinline__ void vec_quat_rotate_rn(double *v, const double *q) {
+  const double vq[4] = {0., v[0], v[1], v[2]};
+  const double qc[4] = {q[0], -q[1], -q[2], -q[3]};
+  double t[4], r[4];
+  quatquat_rn(q, vq, t);
+  quatquat_rn(t, qc, r);
+  v[0] = r[1];
+  v[1] = r[2];
+  v[2] = r[3];
+}
+
+// MeshMoverRotate::initial_integrate (src/mesh_mover_rotation.cpp:105-131):
+// nodes and centres (MultiNodeMesh::rotate(dQ, origin),
+// src/multi_node_mesh_I.h:643-668), the rotating element vectors edgeVec,
+// edgeNorm, surfaceNorm (CustomValueTracker::rotate), node velocities
+// 0 + w x (node - O); then the node-travel test of decideRebuild
+__global__ void k_mesh_rotate(Sys s, int k) {
+  Ctrl *c = s.ctrl;
+  if (c->halt) return;
+  const MeshDev &M = s.meshes[k];
+  const double trigger = __dmul_rn(__dmul_rn(0.25, s.skin), s.skin);
+  const double *o = M.rorig, *q = M.rq, *w = M.romega;
+  const bool trans = __dadd_rn(__dadd_rn(__dmul_rn(o[0], o[0]), __dmul_rn(o[1], o[1])), __dmul_rn(o[2], o[2])) > 0.;
+  const double third = 1. / 3.;
+  bool moved = false;
+  GRID_STRIDE(t, M.ntri) {
+    double *g = M.tri + (size_t)t * kTriStride;
+    double cen[3] = {0., 0., 0.};
+    for (int j = 0; j < 3; j++) {
+      double nd[3] = {g[3 * j], g[3 * j + 1], g[3 * j + 2]};
+      if (trans)
+        for (int d = 0; d < 3; d++) nd[d] = __dsub_rn(nd[d], o[d]);
+      vec_quat_rotate_rn(nd, q);
+      if (trans)
+        for (int d = 0; d < 3; d++) nd[d] = __dadd_rn(nd[d], o[d]);
+      double dsq = 0.0;
+      for (int d = 0; d < 3; d++) {
+        g[3 * j + d] = nd[d];
+        cen[d] = __dadd_rn(nd[d], cen[d]);
+        const double e = __dadd_rn(nd[d], -M.node_last[(size_t)t * 9 + 3 * j + d]);
+        dsq = d == 0 ? __dmul_rn(e, e) : __dadd_rn(dsq, __dmul_rn(e, e));
+      }
+      moved |= dsq > trigger;
+      const double r[3] = {__dsub_rn(nd[0], o[0]), __dsub_rn(nd[1], o[1]), __dsub_rn(nd[2], o[2])};
+      double *v = M.nodev + (size_t)t * 9 + 3 * j;
+      v[0] = __dadd_rn(0.0, __dsub_rn(__dmul_rn(w[1], r[2]), __dmul_rn(w[2], r[1])));
+      v[1] = __dadd_rn(0.0, __dsub_rn(__dmul_rn(w[2], r[0]), __dmul_rn(w[0], r[2])));
+      v[2] = __dadd_rn(0.0, __dsub_rn(__dmul_rn(w[0], r[1]), __dmul_rn(w[1], r[0])));
+    }
+    for (int d = 0; d < 3; d++) g[33 + d] = __dmul_rn(third, cen[d]);
+    for (int j = 0; j < 3; j++) vec_quat_rotate_rn(g + 9 + 3 * j, q);   // edgeVec
+    for (int j = 0; j < 3; j++) vec_quat_rotate_rn(g + 18 + 3 * j, q);  // edgeNorm
+    vec_quat_rotate_rn(g + 30, q);                                      // surfaceNorm
+    M.trif[2 * (size_t)t] = make_float4((float)g[0], (float)g[1], (float)g[2], 0.f);
+    M.trif[2 * (size_t)t + 1] = make_float4((float)g[30], (float)g[31], (float)g[32], 0.f);
+  }
+  if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(&c->mesh_moved, 1);
+}
+
 __global__ void k_mesh_move(Sys s, int k) {
   Ctrl *c = s.ctrl;
   if (c->halt) return;
@@ -1167,6 +1240,17 @@ __device__ __forceinline__ void plane_contact(const Sys &s, const AtomArrays &A,
   }
 }
 
+// barycentric node velocity at the contact point (src/fix_wall_gran.cpp:929-934):
+// the linear mover's node velocities are all vel, the rotating mover's nodev
+__device__ __forceinline__ void mesh_vwall(const MeshDev &M, int t, const double bary[3], double vwall[3]) {
+  if (M.rotating) {
+    const double *vn = M.nodev + (size_t)t * 9;
+    for (int d = 0; d < 3; d++) vwall[d] = (bary[0] * vn[d] + bary[1] * vn[3 + d] + bary[2] * vn[6 + d]);
+  } else {
+    for (int d = 0; d < 3; d++) vwall[d] = (bary[0] * M.vel[d] + bary[1] * M.vel[d] + bary[2] * M.vel[d]);
+  }
+}
+
 // SurfaceMesh::areCoplanarNodeNeighs from the precomputed lists
 __device__ __forceinline__ bool mesh_coplanar(const MeshDev &M, int a, int b) {
   for (int q = M.cn_start[a]; q < M.cn_start[a + 1]; q++)
@@ -1258,8 +1342,7 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
         }
     }
     double vwall[3] = {0., 0., 0.};
-    if (M.moving && M.vel_on)  // barycentric node velocity, src/fix_wall_gran.cpp:929-934
-      for (int d = 0; d < 3; d++) vwall[d] = (bary[0] * M.vel[d] + bary[1] * M.vel[d] + bary[2] * M.vel[d]);
+    if (M.moving && M.vel_on) mesh_vwall(M, t, bary, vwall);
     double cfx = 0., cfy = 0., cfz = 0., ctx = 0., cty = 0., ctz = 0.;
     wall_force<NORMAL>(s, A, i, deltan, delta, vwall, M.wall_type, M.rolling != 0,
                        sh + (size_t)(3 * slot) * nmax + i, nmax, shearupdate, v, om, cfx, cfy, cfz, ctx, cty, ctz);
@@ -1420,8 +1503,7 @@ __global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate
             r[0] = deltan;
             r[1] = delta[0]; r[2] = delta[1]; r[3] = delta[2];
             double vwall[3] = {0., 0., 0.};
-            if (M.moving && M.vel_on)  // barycentric node velocity, src/fix_wall_gran.cpp:929-934
-              for (int d = 0; d < 3; d++) vwall[d] = (bary[0] * M.vel[d] + bary[1] * M.vel[d] + bary[2] * M.vel[d]);
+            if (M.moving && M.vel_on) mesh_vwall(M, t, bary, vwall);
             r[4] = vwall[0]; r[5] = vwall[1]; r[6] = vwall[2];
           }
         }
@@ -1930,7 +2012,10 @@ int launch_mesh_move(const Sys &s, const LaunchCfg &lc, cudaStream_t st) {
   int nl = 0;
   for (int k = 0; k < s.nmeshes; k++) {
     if (!s.meshes[k].moving) continue;
-    k_mesh_move<<<grid_for(s.meshes[k].ntri, 256, lc.max_grid), 256, 0, st>>>(s, k);
+    if (s.meshes[k].rotating)
+      k_mesh_rotate<<<grid_for(s.meshes[k].ntri, 256, lc.max_grid), 256, 0, st>>>(s, k);
+    else
+      k_mesh_move<<<grid_for(s.meshes[k].ntri, 256, lc.max_grid), 256, 0, st>>>(s, k);
     nl++;
   }
   return nl;

@@ -99,6 +99,7 @@ def load(build=True):
     L.dem_mesh_topology.argtypes = [I, P, P, P]
     L.dem_mesh_ncontacts.argtypes = [P, I, P]
     L.dem_set_mesh_motion.argtypes = [P, I, P]
+    L.dem_set_mesh_rotation.argtypes = [P, I, P, P, ctypes.c_double]
     L.dem_download_mesh_nodes.argtypes = [P, I, P]
     L.dem_download_mesh_contacts.argtypes = [P, I, P, P, P, P]
     L.dem_upload_contact_history.argtypes = [P, I, P, P, P]
@@ -202,6 +203,12 @@ class DemSystem:
             if m.get("vel") is not None:
                 vel = np.ascontiguousarray(m["vel"], dtype=np.float64)
                 self._check(L.dem_set_mesh_motion(self.h, len(self._meshkeep) // 3 - 1, _p(vel)))
+            if m.get("rotate") is not None:
+                ro = m["rotate"]
+                org = np.ascontiguousarray(ro["origin"], dtype=np.float64)
+                axv = np.ascontiguousarray(ro["axis"], dtype=np.float64)
+                self._check(L.dem_set_mesh_rotation(self.h, len(self._meshkeep) // 3 - 1, _p(org), _p(axv),
+                                                    float(ro["period"])))
             self._nodes_shape.append(nodes.shape)
         if "atoms" in case:
             self.upload(case["atoms"])

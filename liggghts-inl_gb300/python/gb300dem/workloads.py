@@ -320,6 +320,27 @@ def press_case(seed, nfib, nper, radius, box, plate_gap, plate_vel, inset=None, 
     return c
 
 
+def paddle_mesh(cx, cy, half_len, z0, z1):
+    """A vertical two-triangle paddle through (cx, cy) spanning x in
+    [cx - half_len, cx + half_len], z in [z0, z1] at y = cy; nodes[2, 3, 3]."""
+    a, b, c, d = (cx - half_len, cy, z0), (cx + half_len, cy, z0), (cx + half_len, cy, z1), (cx - half_len, cy, z1)
+    return np.array([(a, b, c), (a, c, d)], dtype=np.float64)
+
+
+def mixer_case(seed, nx, ny, nz, spacing, radius, blade_half_len, blade_height, period, **kw):
+    """A jittered lattice on a floor (periodic x/y) stirred by a vertical
+    paddle mesh turning about the vertical axis through the box centre (fix
+    move/mesh ... rotate origin O axis 0 0 1 period T).  The paddle lies in
+    the gap between two lattice rows."""
+    c = lattice_case(seed, nx, ny, nz, spacing, radius=radius, **kw)
+    cx = 0.5 * nx * spacing
+    cy = (ny // 2) * spacing
+    c["meshes"] = [dict(nodes=paddle_mesh(cx, cy, blade_half_len, 0.0, blade_height), wall_type=1,
+                        rolling=c.get("rolling_model", 0),
+                        rotate=dict(origin=(cx, cy, 0.0), axis=(0.0, 0.0, 1.0), period=float(period)))]
+    return c
+
+
 def lattice_case(seed, nx, ny, nz, spacing, radius=(1e-3, 1e-3), density=2500.0,
                  z0=None, jitter=0.0, vmax=0.0, wmax=0.0, ntypes=1, E=(5e6,), nu=(0.45,),
                  rest=((0.9,),), frict=((0.5,),), rollfrict=None, periodic=(1, 1, 0),

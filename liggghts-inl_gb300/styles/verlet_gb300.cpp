@@ -148,8 +148,13 @@ void VerletGB300::create_device() {
     for (size_t w = 0; w < walls_.size(); w++)
       for (size_t m = 0; m < walls_[w]->mesh_ids().size(); m++)
         if (walls_[w]->mesh_ids()[m] == movers_[k]->mesh_id()) {
-          check(dem_set_mesh_motion(h_, walls_[w]->device_mesh_ids()[m], movers_[k]->velocity()),
-                "dem_set_mesh_motion");
+          if (movers_[k]->rotating())
+            check(dem_set_mesh_rotation(h_, walls_[w]->device_mesh_ids()[m], movers_[k]->origin(),
+                                        movers_[k]->axis(), movers_[k]->period()),
+                  "dem_set_mesh_rotation");
+          else
+            check(dem_set_mesh_motion(h_, walls_[w]->device_mesh_ids()[m], movers_[k]->velocity()),
+                  "dem_set_mesh_motion");
           found = true;
         }
     if (!found) error->all(FLERR, "verlet/gb300: move/mesh/gb300 names a mesh no wall/gran/gb300 uses");
@@ -256,9 +261,20 @@ void VerletGB300::download() {
 /* moving meshes: the host copy follows the device at output.  Linear motion
    moves every node by the same vector, so the host mesh is translated by the
    difference of one node through the mesh's own move() (which also updates
-   its centres and bounding data) */
-void VerletGB300::sync_meshes() {
+   its centres and bounding data).  A rotating mesh is turned by the host's
+   own mover (FixMoveMesh::initial_integrate, once per step of the
+   stretch), which runs the reference's arithmetic on the host copy. */
+void VerletGB300::sync_meshes(int nsteps) {
   if (movers_.empty()) return;
+  bool linear = false;
+  for (size_t k = 0; k < movers_.size(); k++) {
+    if (movers_[k]->rotating()) {
+      for (int n = 0; n < nsteps; n++) movers_[k]->initial_integrate(0);
+    } else {
+      linear = true;
+    }
+  }
+  if (!linear) return;
   for (size_t w = 0; w < walls_.size(); w++)
     for (size_t m = 0; m < walls_[w]->mesh_ids().size(); m++) {
       FixMeshSurface *fm =
@@ -295,7 +311,7 @@ void VerletGB300::setup() {
   // carry-over + forces without history update
   check(dem_setup(h_), "dem_setup");
   download();
-  sync_meshes();
+  sync_meshes(0);
   // the reference's own setup for the host side (ghosts, host lists, output
   // at the setup step); pair gran/gb300 copies the device forces in
   Verlet::setup();
@@ -317,7 +333,7 @@ void VerletGB300::run(int n) {
     timer->stamp(TIME_PAIR);
     update->ntimestep = next;
     download();
-    sync_meshes();
+    sync_meshes(k);
     stamp_ = host_stamp();
     if (next == output->next) {
       ev_set(next);

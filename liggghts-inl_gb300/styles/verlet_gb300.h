@@ -74,7 +74,7 @@ class VerletGB300 : public Verlet {
   void collect_styles();
   void create_device();
   void download();
-  void sync_meshes();
+  void sync_meshes(int nsteps);
   uint64_t host_stamp() const;
 };
 

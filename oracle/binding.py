@@ -86,6 +86,7 @@ def lib():
         L.orc_get_mesh_flags.argtypes = [P, ctypes.c_int, P, P]
         L.orc_set_mesh_motion.argtypes = [P, ctypes.c_int] + [ctypes.c_double] * 3
         L.orc_get_mesh_nodes.argtypes = [P, ctypes.c_int, P]
+        L.orc_set_mesh_rotation.argtypes = [P, ctypes.c_int, P, P, ctypes.c_double]
         L.orc_get_mesh_contacts.argtypes = [P, ctypes.c_int, P, P, P, P]
         L.orc_ncontacts.restype = ctypes.c_longlong
         L.orc_ncontacts.argtypes = [P]
@@ -154,6 +155,12 @@ class Oracle:
                                        int(m.get("rolling", 0)), _p(ea), _p(ca)))
             if m.get("vel") is not None:
                 self._check(L.orc_set_mesh_motion(self.h, self.nmesh, *[float(v) for v in m["vel"]]))
+            if m.get("rotate") is not None:
+                ro = m["rotate"]
+                org = np.ascontiguousarray(ro["origin"], dtype=np.float64)
+                axv = np.ascontiguousarray(ro["axis"], dtype=np.float64)
+                self._keep += [org, axv]
+                self._check(L.orc_set_mesh_rotation(self.h, self.nmesh, _p(org), _p(axv), float(ro["period"])))
             self.nmesh += 1
         a = case["atoms"]
         n = len(a["tag"])

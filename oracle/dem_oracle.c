@@ -251,6 +251,41 @@ int orc_set_mesh_motion(orc_sys *s, int k, double vx, double vy, double vz) {
   return 0;
 }
 
+/* fix move/mesh mesh ID rotate origin O axis A period T (MeshMoverRotate,
+ * src/mesh_mover_rotation.cpp:66-131): axis normalised
+ * (vectorNormalize3D), omega = 2 pi / T; every step the mesh turns by
+ * omega*dt through the quaternion of MultiNodeMesh::rotate(dAngle, axis, p)
+ * (src/multi_node_mesh_I.h:620-640) */
+int orc_set_mesh_rotation(orc_sys *s, int k, const double *origin, const double *axis, double period) {
+  if (k < 0 || k >= s->nmeshes || s->n > 0) { snprintf(s->err, sizeof s->err, "set mesh motion before atoms"); return -1; }
+  if (!(period != 0.0)) { snprintf(s->err, sizeof s->err, "rotation period is zero"); return -1; }
+  orc_mesh *m = &s->meshes[k];
+  double ax[3] = {axis[0], axis[1], axis[2]};
+  const double norm = sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+  const double invnorm = (norm == 0.) ? 0. : 1. / norm;
+  for (int d = 0; d < 3; d++) ax[d] *= invnorm;
+  const double omega = 2. * M_PI / period;
+  const double dangle = omega * s->cfg.dt;
+  /* MultiNodeMesh::rotate(dAngle, axis, p): axisNorm = axis / |axis| */
+  double an[3] = {ax[0], ax[1], ax[2]};
+  const double mag = sqrt(an[0] * an[0] + an[1] * an[1] + an[2] * an[2]);
+  const double sinv = 1. / mag;
+  for (int d = 0; d < 3; d++) an[d] = sinv * an[d];
+  m->rot_dq[0] = cos(dangle * 0.5);
+  for (int d = 0; d < 3; d++) m->rot_dq[d + 1] = an[d] * sin(dangle * 0.5);
+  for (int d = 0; d < 3; d++) {
+    m->rot_origin[d] = origin[d];
+    m->rot_omega[d] = ax[d] * omega; /* vectorScalarMult3D(axis_, omega_, omegaVec) */
+  }
+  m->moving = 2;
+  const size_t t9 = 9 * (size_t)m->ntri;
+  m->nodev = (double *)xrealloc(m->nodev, t9 * sizeof(double));
+  memset(m->nodev, 0, t9 * sizeof(double));
+  m->nodeLast = (double *)xrealloc(m->nodeLast, t9 * sizeof(double));
+  memcpy(m->nodeLast, m->node, t9 * sizeof(double));
+  return 0;
+}
+
 int orc_get_mesh_nodes(const orc_sys *s, int k, double *nodes) {
   if (k < 0 || k >= s->nmeshes) return -1;
   memcpy(nodes, s->meshes[k].node, 9 * (size_t)s->meshes[k].ntri * sizeof(double));
@@ -270,6 +305,63 @@ static void mesh_move(orc_sys *s, orc_mesh *m) {
       }
     for (int d = 0; d < 3; d++) m->center[3 * (size_t)t + d] = m->center[3 * (size_t)t + d] + dx[d];
   }
+}
+
+/* MathExtra::quatquat (src/math_extra.h:596-602) */
+static void quatquat(const double *a, const double *b, double *c) {
+  c[0] = a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3];
+  c[1] = a[0] * b[1] + b[0] * a[1] + a[2] * b[3] - a[3] * b[2];
+  c[2] = a[0] * b[2] + b[0] * a[2] + a[3] * b[1] - a[1] * b[3];
+  c[3] = a[0] * b[3] + b[0] * a[3] + a[1] * b[2] - a[2] * b[1];
+}
+
+/* MathExtraLiggghts::vec_quat_rotate, in place (src/math_extra_liggghts.h:455-471):
+ * (0, v) -> q (0, v) q* */
+static void vec_quat_rotate(double *v, const double *q) {
+  const double vq[4] = {0., v[0], v[1], v[2]};
+  const double qc[4] = {q[0], -q[1], -q[2], -q[3]};
+  double t[4], r[4];
+  quatquat(q, vq, t);
+  quatquat(t, qc, r);
+  v[0] = r[1]; v[1] = r[2]; v[2] = r[3];
+}
+
+/* MeshMoverRotate::initial_integrate (src/mesh_mover_rotation.cpp:105-131):
+ * MultiNodeMesh::rotate(dQ, origin) on nodes and centres
+ * (src/multi_node_mesh_I.h:643-668), the rotating element vectors (edgeVec,
+ * edgeNorm, surfaceNorm; TrackingMesh::rotate -> CustomValueTracker), then
+ * node velocities v = 0 + omega x (node - origin) */
+static void mesh_rotate(orc_sys *s, orc_mesh *m) {
+  (void)s;
+  const double *o = m->rot_origin, *q = m->rot_dq, *w = m->rot_omega;
+  const int trans = (o[0] * o[0] + o[1] * o[1] + o[2] * o[2]) > 0.;
+  for (int t = 0; t < m->ntri; t++) {
+    double *c = &m->center[3 * (size_t)t];
+    c[0] = c[1] = c[2] = 0.0;
+    for (int j = 0; j < 3; j++) {
+      double *nd = &m->node[9 * (size_t)t + 3 * j];
+      if (trans) for (int d = 0; d < 3; d++) nd[d] = nd[d] - o[d];
+      vec_quat_rotate(nd, q);
+      if (trans) for (int d = 0; d < 3; d++) nd[d] = nd[d] + o[d];
+      for (int d = 0; d < 3; d++) c[d] = nd[d] + c[d];
+    }
+    const double sinv = 1. / 3.;
+    for (int d = 0; d < 3; d++) c[d] = sinv * c[d];
+  }
+  for (int t = 0; t < m->ntri; t++) {
+    for (int j = 0; j < 3; j++) vec_quat_rotate(&m->edgeVec[9 * (size_t)t + 3 * j], q);
+    for (int j = 0; j < 3; j++) vec_quat_rotate(&m->edgeNorm[9 * (size_t)t + 3 * j], q);
+    vec_quat_rotate(&m->surfNorm[3 * (size_t)t], q);
+  }
+  for (int t = 0; t < m->ntri; t++)
+    for (int j = 0; j < 3; j++) {
+      const double *nd = &m->node[9 * (size_t)t + 3 * j];
+      const double r[3] = {nd[0] - o[0], nd[1] - o[1], nd[2] - o[2]};
+      double *v = &m->nodev[9 * (size_t)t + 3 * j];
+      v[0] = 0.0 + (w[1] * r[2] - w[2] * r[1]);
+      v[1] = 0.0 + (w[2] * r[0] - w[0] * r[2]);
+      v[2] = 0.0 + (w[0] * r[1] - w[1] * r[0]);
+    }
 }
 
 /* MultiNodeMesh::decideRebuild, src/multi_node_mesh_I.h:792-823 */
@@ -1660,7 +1752,8 @@ int orc_run(orc_sys *s, int nsteps) {
     s->ntimestep++;
     initial_integrate(s);
     for (int k = 0; k < s->nmeshes; k++)
-      if (s->meshes[k].moving) mesh_move(s, &s->meshes[k]);
+      if (s->meshes[k].moving == 1) mesh_move(s, &s->meshes[k]);
+      else if (s->meshes[k].moving == 2) mesh_rotate(s, &s->meshes[k]);
     if (decide(s)) {
       if (rebuild(s)) return -1;
     } else {

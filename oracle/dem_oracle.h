@@ -89,6 +89,7 @@ int orc_add_mesh(orc_sys *s, int ntri, const double *nodes, int wall_type, int r
  * src/fix_move_mesh.cpp:194-240, src/mesh_mover_linear.cpp:95-112); add
  * before atoms. */
 int orc_set_mesh_motion(orc_sys *s, int mesh, double vx, double vy, double vz);
+int orc_set_mesh_rotation(orc_sys *s, int mesh, const double *origin, const double *axis, double period);
 int orc_get_mesh_nodes(const orc_sys *s, int mesh, double *nodes);
 int orc_get_mesh_flags(const orc_sys *s, int mesh, unsigned char *edge_active,
                        unsigned char *corner_active);

@@ -40,9 +40,11 @@ typedef struct {
   unsigned char *edgeActive, *cornerActive; /* [t][3] */
   int *nNeighs, *neighFaces;                /* [t][5] edge neighbours (ids = index) */
   int wall_type, rolling;
-  /* fix move/mesh ... linear vx vy vz */
+  /* fix move/mesh ... linear vx vy vz (moving = 1) or
+   * rotate origin ox oy oz axis ax ay az period T (moving = 2) */
   int moving;
   double vel[3];
+  double rot_origin[3], rot_omega[3], rot_dq[4];
   double *nodeLast;    /* node positions at the last neighbour build [t][3][3] */
   /* per-triangle candidate lists (rebuild) */
   int *cstart, *cand;

@@ -66,6 +66,11 @@ def cases():
         47, nfib=60, nper=4, radius=r, box=(9e-3, 9e-3, 7e-3), plate_gap=0.1e-3,
         plate_vel=(0.0, 0.0, -6.0), gap=1.01, vmax=1.0, wmax=2000.0, bond=bp, skin=1e-4,
         max_fail=5000), 600, [0, 1, 2, 10, 50, 100, 200, 300, 400, 500, 600])
+    # a lattice stirred by a rotating paddle mesh (fix move/mesh rotate)
+    c["mixer_rotate"] = (workloads.mixer_case(
+        53, nx=8, ny=8, nz=3, spacing=2.2e-3, radius=(0.95e-3, 1.0e-3), blade_half_len=6e-3,
+        blade_height=7e-3, period=0.02, z0=1.0e-3, jitter=2e-5, vmax=0.5, wmax=50.0),
+        600, [0, 1, 2, 10, 50, 100, 200, 300, 400, 500, 600])
     # fibres of bonded spheres (cohesion bond/nonlinear), floor of wall type 2
     for name, seed, stress in (("fibre_bond", 41, 0), ("fibre_bond_stress", 43, 1)):
         r = 0.5e-3
@@ -153,6 +158,11 @@ def write_inputs(case, d, nsteps, snaps):
         s.append("fix mwall%d all wall/gran %s mesh n_meshes 1 meshes cad%d" % (k, wm, k))
         if m.get("vel") is not None:
             s.append("fix mv%d all move/mesh mesh cad%d linear %s" % (k, k, " ".join(fmt(v) for v in m["vel"])))
+        if m.get("rotate") is not None:
+            ro = m["rotate"]
+            s.append("fix mv%d all move/mesh mesh cad%d rotate origin %s axis %s period %s"
+                     % (k, k, " ".join(fmt(v) for v in ro["origin"]), " ".join(fmt(v) for v in ro["axis"]),
+                        fmt(ro["period"])))
     if not all(case["periodic"]):
         s.append("thermo_modify lost ignore")
     s += ["fix integr all nve/sphere",
@@ -266,8 +276,8 @@ def run_case(name, case, nsteps, snaps):
         meta["bond_settings"] = case["bond"]["settings"]
         out["bond_tables"] = case["bond"]["tables"]
     meta.update(nsteps=nsteps, snaps=snaps, loop=loop)
-    meta["meshes"] = [dict(wall_type=m["wall_type"], rolling=m.get("rolling", 0), vel=m.get("vel"))
-                      for m in case.get("meshes", [])]
+    meta["meshes"] = [dict(wall_type=m["wall_type"], rolling=m.get("rolling", 0), vel=m.get("vel"),
+                           rotate=m.get("rotate")) for m in case.get("meshes", [])]
     for k, m in enumerate(case.get("meshes", [])):
         out["mesh%d_nodes" % k] = m["nodes"]
     a = case["atoms"]

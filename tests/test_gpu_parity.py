@@ -359,3 +359,44 @@ def test_gpu_diagnostics_match_oracle(name):
         assert abs(dr["solid_volume"] - vol) <= 1e-12 * max(vol, 1e-300), (name, done)
         assert abs(dr["packing_fraction"] - vol / np.prod(region[1] - region[0])) <= 1e-12
     g.close()
+
+
+def test_gpu_rotating_mesh_matches_reference():
+    """fix move/mesh rotate: a paddle stirring a lattice.  Paddle nodes bit-exact
+    against the oracle run on the same machine (both take the per-step
+    quaternion from this machine's libm cos/sin) and within 1e-15 of the
+    reference's snapshots (whose libm may round those differently); the same
+    rebuild steps; forces, pair sets and paddle contact slots as the
+    reference's."""
+    from oracle.binding import Oracle
+    case, snaps = load_golden("mixer_rotate")
+    g = _gpu(case)
+    o = Oracle(case)
+    g.setup()
+    o.setup()
+    prev = 0
+    for st in sorted(snaps):
+        if st > prev:
+            g.step(st - prev)
+            o.run(st - prev)
+            prev = st
+        r = snaps[st]
+        assert np.array_equal(g.mesh_nodes(0), o.mesh_nodes(0)), st
+        assert np.abs(g.mesh_nodes(0) - r["mesh0_node"]).max() <= 1e-15 * np.abs(r["mesh0_node"]).max(), st
+        assert g.nrebuilds == o.nrebuilds, st
+        a = sort_by_tag(g.atoms())
+        assert np.array_equal(a["tag"], r["tag"])
+        ftol = FORCE_RTOL if st <= 10 else DIVERGED_RTOL
+        assert max_rel(a["f"], r["f"]) < ftol, (st, max_rel(a["f"], r["f"]))
+        assert max_rel(a["torque"], r["torque"]) < ftol, st
+        rp = canonical_pairs(r["pair_tag_i"], r["pair_tag_j"], r["pair_shift"], r["pair_flag"],
+                             r["pair_hist"])
+        missing, extra, flagmis, hm = compare_pairs(_pairs(g), rp)
+        assert not missing and not extra and not flagmis, st
+        mc = g.mesh_contacts(0)
+        gm = {(int(t), int(tr)): int(sl) for t, tr, sl in zip(mc["tag"], mc["tri"], mc["slot"])}
+        rm = {(int(t), int(tr)): int(sl) for t, tr, sl in
+              zip(r["mesh0_contact_tag"], r["mesh0_contact_tri"], r["mesh0_contact_slot"])}
+        assert gm == rm, st
+    assert g.nrebuilds >= 4
+    g.close()
