@@ -211,6 +211,22 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
                      const double *v, const double *omega, const double *radius,
                      const double *rmass);
 
+/* Insertion (fix insert/pack, insert/stream, insert/rate/region: the
+ * reference's FixInsert::pre_exchange, src/fix_insert.cpp).  Before
+ * dem_upload_atoms, dem_set_capacity reserves room for natoms_max atoms and
+ * declares the radius range [rmin, rmax] inserted atoms may take (0: the
+ * uploaded atoms' range); the neighbour cutoff is sized for it, as
+ * PairGran::init_one sizes it for the insertion templates.  Between
+ * dem_step calls, dem_insert_atoms stages k new atoms (host arrays as in
+ * dem_upload_atoms); they join at the next step after its initial
+ * integration, and that step rebuilds the neighbour list, which is when and
+ * how FixInsert adds atoms in the reference (pre_exchange of the insertion
+ * step, next_reneighbor = that step).  DEM_ERR_CAPACITY when the capacity
+ * would be exceeded.  Not with an ensemble. */
+int dem_set_capacity(dem_handle *h, int natoms_max, double rmin, double rmax);
+int dem_insert_atoms(dem_handle *h, int k, const int *tag, const int *type, const double *x, const double *v,
+                     const double *omega, const double *radius, const double *rmass);
+
 /* Restart data, valid between dem_upload_atoms and dem_setup (atoms indexed in
  * upload order).  Contact history as the reference keeps it per atom
  * (FixContactHistory npartner/partner/contacthistory, restored by

@@ -56,6 +56,12 @@ struct dem_handle {
   std::vector<double> bond_tables;  // host copy for the cutoff derivation
   double cell_scale = 1.0;          // neighbour cell edge / cutneighmax (dem_set_tuning)
   int ens_nsys = 0;                 // batched ensemble: number of systems (dem_set_ensemble)
+  // insertion (dem_set_capacity / dem_insert_atoms)
+  int cap_n = 0;                    // atom capacity (0: the uploaded count)
+  double cap_rmin = 0.0, cap_rmax = 0.0;  // radius range inserted atoms may take
+  double eff_rmin = 0.0, eff_rmax = 0.0;  // radii the neighbour cutoff was sized for
+  int pending_insert = 0;           // staged atoms that join at the next step
+  int next_lidx = 0;                // caller-order index of the next inserted atom
   dem_bond_settings bond_settings{};
 };
 
@@ -732,6 +738,12 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
     maxrad = std::max(maxrad, radius[i]);
     minrad = std::min(minrad, radius[i]);
   }
+  // radii that later insertions may bring (PairGran::init_one takes the
+  // insertion templates' radii into maxrad/minrad the same way)
+  if (h->cap_rmax > 0.0) maxrad = std::max(maxrad, h->cap_rmax);
+  if (h->cap_rmin > 0.0) minrad = std::min(minrad, h->cap_rmin);
+  h->eff_rmin = minrad;
+  h->eff_rmax = maxrad;
   s.cdf = h->cfg.contact_distance_factor;
   if (s.bond) {
     if (!s.bondp) return fail(h, DEM_ERR_BAD_ARG, "cohesion bond/nonlinear needs dem_set_bond_params");
@@ -812,8 +824,11 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
     }
     M.tc_cap = (int)std::min<long>(2147000000L, 2 * tot + 4096);
   }
-  int rc = alloc_atoms(h, n);
+  if (h->cap_n > 0 && h->cap_n < n) return fail(h, DEM_ERR_CAPACITY, "more atoms than the capacity set");
+  int rc = alloc_atoms(h, std::max(n, h->cap_n));
   if (rc) return rc;
+  h->pending_insert = 0;
+  h->next_lidx = n;
   // Initial pair capacity: 16 entries per atom.  LIGGGHTS_GB300_PAIRS_PER_ATOM
   // overrides it; a deliberately small value exercises the overflow path
   // (device halt, host growth, resumed rebuild) in tests.
@@ -860,6 +875,80 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
   CUDA_TRY(h, cudaMemcpy(s.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice));
   h->have_atoms = true;
   h->setup_done = false;
+  return DEM_OK;
+}
+
+int dem_set_capacity(dem_handle *h, int natoms_max, double rmin, double rmax) {
+  if (!h || natoms_max < 0 || rmin < 0.0 || rmax < 0.0 || (rmin > 0.0 && rmax > 0.0 && rmin > rmax))
+    return DEM_ERR_BAD_ARG;
+  if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "set the capacity before uploading atoms");
+  if ((long)natoms_max > kMaxScan) return fail(h, DEM_ERR_BAD_ARG, "capacity too large for one handle");
+  h->cap_n = natoms_max;
+  h->cap_rmin = rmin;
+  h->cap_rmax = rmax;
+  return DEM_OK;
+}
+
+int dem_insert_atoms(dem_handle *h, int k, const int *tag, const int *type, const double *x, const double *v,
+                     const double *omega, const double *radius, const double *rmass) {
+  if (!h || k < 0 || (k > 0 && (!tag || !type || !x || !v || !omega || !radius || !rmass))) return DEM_ERR_BAD_ARG;
+  if (!h->have_atoms || !h->setup_done) return fail(h, DEM_ERR_BAD_ARG, "insert after dem_setup");
+  if (h->ens_nsys > 0) return fail(h, DEM_ERR_UNSUPPORTED, "insertion into an ensemble");
+  if (k == 0) return DEM_OK;
+  Sys &s = h->s;
+  for (int q = 0; q < k; q++) {
+    if (type[q] < 1 || type[q] > s.ntypes) return fail(h, DEM_ERR_BAD_ARG, "atom type out of range");
+    if (!(rmass[q] > 0.0)) return fail(h, DEM_ERR_BAD_ARG, "rmass must be > 0");
+    if (!(radius[q] >= h->eff_rmin && radius[q] <= h->eff_rmax))
+      return fail(h, DEM_ERR_BAD_ARG, "inserted radius outside the range the neighbour cutoff was sized for "
+                                      "(dem_set_capacity)");
+    for (int d = 0; d < 3; d++)
+      if (!std::isfinite(x[3 * q + d]) || !std::isfinite(v[3 * q + d]) || !std::isfinite(omega[3 * q + d]))
+        return fail(h, DEM_ERR_BAD_ARG, "non-finite inserted state");
+  }
+  int rc = read_ctrl(h);
+  if (rc) return rc;
+  const int first = h->host_ctrl.n + h->pending_insert;
+  if ((long)first + k > (long)s.nmax) return fail(h, DEM_ERR_CAPACITY, "atom capacity exceeded (dem_set_capacity)");
+  // FixNVESphere per-atom constants as at upload
+  const double dtf = 0.5 * s.dt * 1.0;
+  const double dtfrotate = dtf / 0.4;
+  std::vector<double> dtfm(k), dtir(k);
+  for (int q = 0; q < k; q++) {
+    dtfm[q] = dtf / (rmass[q] * (1. + 0.0));
+    dtir[q] = dtfrotate / (radius[q] * radius[q] * rmass[q]);
+  }
+  double *buf = nullptr;
+  int *ibuf = nullptr;
+  const size_t nd = (size_t)k * (9 + 4);
+  CUDA_TRY(h, cudaMalloc(&buf, nd * sizeof(double)));
+  CUDA_TRY(h, cudaMalloc(&ibuf, (size_t)2 * k * sizeof(int)));
+  const double *src[] = {x, v, omega};
+  for (int a = 0; a < 3; a++)
+    CUDA_TRY(h, cudaMemcpy(buf + (size_t)3 * k * a, src[a], (size_t)3 * k * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpy(buf + (size_t)9 * k, radius, (size_t)k * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpy(buf + (size_t)10 * k, rmass, (size_t)k * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpy(buf + (size_t)11 * k, dtfm.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpy(buf + (size_t)12 * k, dtir.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpy(ibuf, type, (size_t)k * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpy(ibuf + k, tag, (size_t)k * sizeof(int), cudaMemcpyHostToDevice));
+  InsertStage in;
+  in.x = buf;
+  in.v = buf + (size_t)3 * k;
+  in.w = buf + (size_t)6 * k;
+  in.r = buf + (size_t)9 * k;
+  in.m = buf + (size_t)10 * k;
+  in.dtfm = buf + (size_t)11 * k;
+  in.dtir = buf + (size_t)12 * k;
+  in.type = ibuf;
+  in.tag = ibuf + k;
+  h->kt.kernel_launches += launch_insert_stage(s, in, first, k, h->next_lidx, h->st);
+  CUDA_TRY(h, cudaGetLastError());
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  cudaFree(buf);
+  cudaFree(ibuf);
+  h->next_lidx += k;
+  h->pending_insert += k;
   return DEM_OK;
 }
 
@@ -970,6 +1059,10 @@ int dem_step(dem_handle *h, int nsteps) {
     if (first) {  // step 1 starts from stored forces: initial_integrate only
       h->kt.kernel_launches += launch_particle(h->s, h->lc, kModeInitial, 1, h->st);
       h->kt.kernel_launches += launch_mesh_move(h->s, h->lc, h->st);
+      if (h->pending_insert > 0) {  // staged atoms join now and force a rebuild
+        h->kt.kernel_launches += launch_insert_commit(h->s, h->pending_insert, h->st);
+        h->pending_insert = 0;
+      }
       mark(h, 0);
       h->kt.kernel_launches += launch_decide(h->s, h->st);
       h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 0);

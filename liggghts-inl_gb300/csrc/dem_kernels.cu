@@ -1762,6 +1762,79 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
 }
 
 // ----------------------------------------------------------------------------
+// insertion (dem_insert_atoms): new atoms are staged into the unused slots
+// [first, first + k) of atom buffer 0 between steps and join the system at
+// the next step after its initial integration, with a forced rebuild, as
+// FixInsert::pre_exchange adds them in the reference (src/fix_insert.cpp,
+// pre_exchange with next_reneighbor = the insertion step)
+// ----------------------------------------------------------------------------
+
+__global__ void k_insert_stage(Sys s, InsertStage in, int first, int k, int lidx0) {
+  const AtomArrays &A = s.atoms[0];
+  const size_t nmax = s.nmax;
+  GRID_STRIDE(q, k) {
+    const int i = first + q;
+    A.x[i] = in.x[3 * q]; A.y[i] = in.x[3 * q + 1]; A.z[i] = in.x[3 * q + 2];
+    A.vx[i] = in.v[3 * q]; A.vy[i] = in.v[3 * q + 1]; A.vz[i] = in.v[3 * q + 2];
+    A.wx[i] = in.w[3 * q]; A.wy[i] = in.w[3 * q + 1]; A.wz[i] = in.w[3 * q + 2];
+    A.fx[i] = A.fy[i] = A.fz[i] = 0.0;
+    A.tx[i] = A.ty[i] = A.tz[i] = 0.0;
+    A.xh[i] = A.x[i]; A.yh[i] = A.y[i]; A.zh[i] = A.z[i];
+    A.r[i] = in.r[q]; A.m[i] = in.m[q];
+    A.dtfm[i] = in.dtfm[q]; A.dtir[i] = in.dtir[q];
+    A.type[i] = in.type[q]; A.tag[i] = in.tag[q]; A.lidx[i] = lidx0 + q;
+    for (int w = 0; w < s.nplanes; w++)
+      for (int d = 0; d < 3; d++) A.whist[(size_t)(w * 3 + d) * nmax + i] = 0.0;
+    A.wbits[i] = 0;
+    A.fmx[i] = A.fmy[i] = A.fmz[i] = A.tmx[i] = A.tmy[i] = A.tmz[i] = 0.0;
+    const float4 f = make_float4((float)A.x[i], (float)A.y[i], (float)A.z[i], (float)A.r[i]);
+    s.xf[i] = f;
+    s.xhf[i] = f;
+    for (int m = 0; m < s.nmeshes; m++) {
+      const MeshDev &M = s.meshes[m];
+      M.cand_n[i] = 0;
+      M.nslot[0][i] = 0;
+      M.npart[0][i] = 0;
+      for (int u = 0; u < kMeshMaxCand; u++) {
+        M.slot_tri[0][(size_t)u * nmax + i] = -1;
+        for (int d = 0; d < 3; d++) M.slot_hist[0][(size_t)(3 * u + d) * nmax + i] = 0.0;
+      }
+    }
+  }
+}
+
+// the new atoms get empty rows in the current (old) list, so that the
+// rebuild's history carry-over finds nothing for them
+__global__ void k_insert_commit(Sys s, int k) {
+  __shared__ int n_old;
+  Ctrl *c = s.ctrl;
+  if (c->halt) return;
+  if (threadIdx.x == 0) n_old = c->n;
+  __syncthreads();
+  const PairArrays &L = s.pairs[0];
+  const int r = L.row[n_old], rv = L.rev_start[n_old];
+  for (int q = threadIdx.x; q < k; q += blockDim.x) {
+    L.row[n_old + 1 + q] = r;
+    L.rev_start[n_old + 1 + q] = rv;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    c->n = n_old + k;
+    c->force_rebuild = 1;
+  }
+}
+
+int launch_insert_stage(const Sys &s, const InsertStage &in, int first, int k, int lidx0, cudaStream_t st) {
+  k_insert_stage<<<(k + 127) / 128, 128, 0, st>>>(s, in, first, k, lidx0);
+  return 1;
+}
+
+int launch_insert_commit(const Sys &s, int k, cudaStream_t st) {
+  k_insert_commit<<<1, 256, 0, st>>>(s, k);
+  return 1;
+}
+
+// ----------------------------------------------------------------------------
 // diagnostics (dem_get_diagnostics): deterministic per-block partial sums,
 // added in block order by the host
 // ----------------------------------------------------------------------------

@@ -19,6 +19,12 @@ enum {
 
 // exclusive prefix sum of len ints (len <= 4096*4096 - 1); tmp holds
 // (len+4095)/4096 + 1 ints; gate: skip unless the system rebuilds
+struct InsertStage {  // new atoms, device arrays: x, v, w [3k], the rest [k]
+  const double *x, *v, *w, *r, *m, *dtfm, *dtir;
+  const int *type, *tag;
+};
+int launch_insert_stage(const Sys &s, const InsertStage &in, int first, int k, int lidx0, cudaStream_t st);
+int launch_insert_commit(const Sys &s, int k, cudaStream_t st);
 int launch_diagnostics(const Sys &s, const LaunchCfg &lc, const double lo[3], const double hi[3], double *part_atoms,
                        double *part_walls, unsigned long long *contacts, int nblocks, cudaStream_t st);
 int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, bool gate,

@@ -119,6 +119,8 @@ def load(build=True):
     L.dem_get_kernel_times.argtypes = [P, ctypes.POINTER(DemKernelTimes)]
     L.dem_measure_fp64_peak.argtypes = [ctypes.POINTER(ctypes.c_double)]
     L.dem_get_diagnostics.argtypes = [P, P, P, ctypes.POINTER(DemDiagnostics)]
+    L.dem_set_capacity.argtypes = [P, I, ctypes.c_double, ctypes.c_double]
+    L.dem_insert_atoms.argtypes = [P, I] + [P] * 7
     _lib = L
     return L
 
@@ -210,6 +212,9 @@ class DemSystem:
                 self._check(L.dem_set_mesh_rotation(self.h, len(self._meshkeep) // 3 - 1, _p(org), _p(axv),
                                                     float(ro["period"])))
             self._nodes_shape.append(nodes.shape)
+        if case.get("capacity") is not None:  # (natoms_max, rmin, rmax) for later insertions
+            nmax_, rmin_, rmax_ = case["capacity"]
+            self._check(L.dem_set_capacity(self.h, int(nmax_), float(rmin_), float(rmax_)))
         if "atoms" in case:
             self.upload(case["atoms"])
 
@@ -224,6 +229,14 @@ class DemSystem:
                 (("tag", np.int32), ("type", np.int32), ("x", np.float64), ("v", np.float64),
                  ("omega", np.float64), ("radius", np.float64), ("rmass", np.float64))]
         self._check(load().dem_upload_atoms(self.h, n, *[_p(x) for x in arrs]))
+
+    def insert(self, a):
+        """dem_insert_atoms: atoms (dict as in the case's "atoms") that join
+        at the next step after its initial integration."""
+        arrs = [np.ascontiguousarray(a[k], dtype=t) for k, t in
+                (("tag", np.int32), ("type", np.int32), ("x", np.float64), ("v", np.float64),
+                 ("omega", np.float64), ("radius", np.float64), ("rmass", np.float64))]
+        self._check(load().dem_insert_atoms(self.h, len(arrs[0]), *[_p(x) for x in arrs]))
 
     def set_restart(self, tag_owner, tag_partner, hist, wall_hist=()):
         """Restart contact/wall history (between upload and setup)."""

@@ -3,7 +3,10 @@
 #include "verlet_gb300.h"
 
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
+
+#include <algorithm>
 
 #include "atom.h"
 #include "atom_vec.h"
@@ -13,6 +16,8 @@
 #include "fix.h"
 #include "fix_contact_history.h"
 #include "fix_gravity_gb300.h"
+#include "fix_insert.h"
+#include "fix_particledistribution_discrete.h"
 #include "fix_mesh_surface.h"
 #include "fix_move_mesh_gb300.h"
 #include "fix_nve_sphere_gb300.h"
@@ -29,8 +34,13 @@
 using namespace LAMMPS_NS;
 using namespace FixConst;
 
+/* run_style verlet/gb300 [capacity N]: N atoms of device room for insertion
+   fixes (default: twice the atoms at the first run, at least 10,000 more) */
 VerletGB300::VerletGB300(LAMMPS *lmp, int narg, char **arg)
-    : Verlet(lmp, narg, arg), h_(NULL), pair_(NULL), gravity_(NULL), natoms_(-1), stamp_(0) {}
+    : Verlet(lmp, narg, arg), h_(NULL), pair_(NULL), capacity_(0), gravity_(NULL), natoms_(-1), stamp_(0) {
+  for (int k = 1; k + 1 < narg; k++)
+    if (strcmp(arg[k], "capacity") == 0) capacity_ = atoi(arg[k + 1]);
+}
 
 VerletGB300::~VerletGB300() {
   if (h_) dem_destroy(h_);
@@ -50,6 +60,7 @@ void VerletGB300::collect_styles() {
   if (!pair_) error->all(FLERR, "run_style verlet/gb300 needs pair_style gran/gb300 (run with -sf gb300)");
   walls_.clear();
   movers_.clear();
+  inserts_.clear();
   gravity_ = NULL;
   int nve = 0;
   const int per_step = INITIAL_INTEGRATE | POST_INTEGRATE | PRE_EXCHANGE | PRE_NEIGHBOR | PRE_FORCE |
@@ -75,6 +86,10 @@ void VerletGB300::collect_styles() {
     }
     if (FixMoveMeshGB300 *m = dynamic_cast<FixMoveMeshGB300 *>(f)) {
       movers_.push_back(m);
+      continue;
+    }
+    if (FixInsert *fi = dynamic_cast<FixInsert *>(f)) {  // insert/pack, insert/stream, ...
+      inserts_.push_back(fi);
       continue;
     }
     bool skip = false;
@@ -141,6 +156,22 @@ void VerletGB300::create_device() {
     gravity_->acceleration(cfg.gravity);
   }
   check(dem_create(&cfg, &h_), "dem_create");
+  if (!inserts_.empty()) {
+    // room and radius range for the insertion templates (PairGran::init_one
+    // sizes the cutoff for them the same way)
+    double rmin = 0.0, rmax = 0.0;
+    for (size_t k = 0; k < inserts_.size(); k++) {
+      FixParticledistributionDiscrete *dist = inserts_[k]->get_distribution();
+      rmax = std::max(rmax, inserts_[k]->max_r_bound());
+      if (!dist) continue;
+      for (int t = inserts_[k]->min_type(); t <= inserts_[k]->max_type(); t++) {
+        const double r = dist->min_rad(t);
+        if (r > 0.0 && r < 1000.0) rmin = rmin > 0.0 ? std::min(rmin, r) : r;
+      }
+    }
+    const long cap = capacity_ > 0 ? capacity_ : std::max<long>(2 * atom->natoms, atom->natoms + 10000);
+    check(dem_set_capacity(h_, (int)cap, rmin, rmax), "dem_set_capacity");
+  }
   pair_->upload_params(h_);
   for (size_t w = 0; w < walls_.size(); w++) walls_[w]->upload(h_, atom->ntypes);
   for (size_t k = 0; k < movers_.size(); k++) {
@@ -322,24 +353,91 @@ void VerletGB300::setup_minimal(int) {
   error->all(FLERR, "verlet/gb300 does not run minimizations");
 }
 
+/* FixInsert::pre_exchange of the insertion step s runs on the host with the
+   state of step s-1 (the device has not yet drifted to step s); the new atoms
+   then join the device at step s after its initial integration, with a
+   rebuild (dem_insert_atoms), as the reference adds them.  The only
+   difference: the fix's overlap checks see the positions one drift earlier. */
+void VerletGB300::insert_due(bigint step) {
+  for (size_t k = 0; k < inserts_.size(); k++) {
+    FixInsert *fi = inserts_[k];
+    if (!fi->force_reneighbor || fi->next_reneighbor != step) continue;
+    // fresh ghosts for the fix's overlap checks
+    domain->pbc();
+    domain->reset_box();
+    comm->setup();
+    comm->exchange();
+    comm->borders();
+    const int n0 = atom->nlocal;
+    const bigint ts = update->ntimestep;
+    update->ntimestep = step;
+    fi->pre_exchange();
+    update->ntimestep = ts;
+    const int k_new = atom->nlocal - n0;
+    if (k_new <= 0) continue;
+    std::vector<int> tag(k_new), type(k_new);
+    std::vector<double> x(3 * (size_t)k_new), v(3 * (size_t)k_new), w(3 * (size_t)k_new), r(k_new), m(k_new);
+    for (int q = 0; q < k_new; q++) {
+      const int i = n0 + q;
+      tag[q] = atom->tag[i];
+      type[q] = atom->type[i];
+      r[q] = atom->radius[i];
+      m[q] = atom->rmass[i];
+      for (int d = 0; d < 3; d++) {
+        x[3 * q + d] = atom->x[i][d];
+        v[3 * q + d] = atom->v[i][d];
+        w[3 * q + d] = atom->omega[i][d];
+      }
+    }
+    check(dem_insert_atoms(h_, k_new, &tag[0], &type[0], &x[0], &v[0], &w[0], &r[0], &m[0]), "dem_insert_atoms");
+    natoms_ = atom->natoms;
+  }
+}
+
 void VerletGB300::run(int n) {
   const bigint end = update->ntimestep + n;
   while (update->ntimestep < end) {
     bigint next = end;
     if (output->next > update->ntimestep && output->next < next) next = output->next;
+    // stop one step before an insertion step to stage the new atoms
+    for (size_t k = 0; k < inserts_.size(); k++)
+      if (inserts_[k]->force_reneighbor && inserts_[k]->next_reneighbor > update->ntimestep &&
+          inserts_[k]->next_reneighbor - 1 < next)
+        next = inserts_[k]->next_reneighbor - 1;
     const int k = (int)(next - update->ntimestep);
-    timer->stamp();
-    check(dem_step(h_, k), "dem_step");
-    timer->stamp(TIME_PAIR);
-    update->ntimestep = next;
-    download();
-    sync_meshes(k);
-    stamp_ = host_stamp();
-    if (next == output->next) {
-      ev_set(next);
+    if (k > 0) {
       timer->stamp();
-      output->write(next);
-      timer->stamp(TIME_OUTPUT);
+      check(dem_step(h_, k), "dem_step");
+      timer->stamp(TIME_PAIR);
+      update->ntimestep = next;
+      download();
+      sync_meshes(k);
+      stamp_ = host_stamp();
+      if (next == output->next) {
+        ev_set(next);
+        timer->stamp();
+        output->write(next);
+        timer->stamp(TIME_OUTPUT);
+      }
+    }
+    if (update->ntimestep < end) {
+      insert_due(update->ntimestep + 1);
+      stamp_ = host_stamp();
+      if (k == 0) {  // the insertion step itself
+        timer->stamp();
+        check(dem_step(h_, 1), "dem_step");
+        timer->stamp(TIME_PAIR);
+        update->ntimestep += 1;
+        download();
+        sync_meshes(1);
+        stamp_ = host_stamp();
+        if (update->ntimestep == output->next) {
+          ev_set(update->ntimestep);
+          timer->stamp();
+          output->write(update->ntimestep);
+          timer->stamp(TIME_OUTPUT);
+        }
+      }
     }
   }
 }

@@ -19,10 +19,16 @@
    meshes and calls Output::write, so thermo, dump and restart output see
    the device state at their steps.
 
+   Insertion fixes (insert/pack, insert/stream, ...: FixInsert) run on the
+   host at their insertion steps; the run stops one step before, lets the
+   fix insert, and hands the new atoms to the device (dem_insert_atoms),
+   which adds them at the insertion step after its initial integration.
+   "run_style verlet/gb300 capacity N" reserves device room for N atoms.
+
    Scope (checked in init): one MPI rank, orthogonal box, atom map, pair
    gran/gb300, exactly one nve/sphere/gb300, any number of
-   wall/gran/gb300, gravity/gb300, move/mesh/gb300 (linear), mesh/surface
-   and data-only fixes.  A fix that would run on the host every step is
+   wall/gran/gb300, gravity/gb300, move/mesh/gb300 (linear, rotate),
+   insertion fixes, mesh/surface and data-only fixes.  A fix that would run on the host every step is
    rejected by name: it would silently not run between output steps. */
 
 #ifdef INTEGRATE_CLASS
@@ -62,6 +68,8 @@ class VerletGB300 : public Verlet {
   class PairGranGB300 *pair_;
   std::vector<class FixWallGranGB300 *> walls_;
   std::vector<class FixMoveMeshGB300 *> movers_;
+  std::vector<class FixInsert *> inserts_;
+  long capacity_;
   class FixGravityGB300 *gravity_;
   bigint natoms_;
   uint64_t stamp_;
@@ -75,6 +83,7 @@ class VerletGB300 : public Verlet {
   void create_device();
   void download();
   void sync_meshes(int nsteps);
+  void insert_due(bigint step);
   uint64_t host_stamp() const;
 };
 

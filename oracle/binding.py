@@ -88,6 +88,7 @@ def lib():
         L.orc_get_mesh_nodes.argtypes = [P, ctypes.c_int, P]
         L.orc_set_mesh_rotation.argtypes = [P, ctypes.c_int, P, P, ctypes.c_double]
         L.orc_get_mesh_contacts.argtypes = [P, ctypes.c_int, P, P, P, P]
+        L.orc_insert_atoms.argtypes = [P, ctypes.c_int] + [P] * 7
         L.orc_ncontacts.restype = ctypes.c_longlong
         L.orc_ncontacts.argtypes = [P]
         L.orc_get_wall_forces.argtypes = [P, P]
@@ -236,6 +237,13 @@ class Oracle:
                    hist=np.zeros((n, 3)))
         L.orc_get_mesh_contacts(self.h, int(k), *[_p(out[q]) for q in ("tag", "tri", "slot", "hist")])
         return out
+
+    def insert(self, a):
+        """Atoms (dict as in the case's "atoms") that join at the next step."""
+        arrs = [np.ascontiguousarray(a[k], dtype=t) for k, t in
+                (("tag", np.int32), ("type", np.int32), ("x", np.float64), ("v", np.float64),
+                 ("omega", np.float64), ("radius", np.float64), ("rmass", np.float64))]
+        self._check(lib().orc_insert_atoms(self.h, len(arrs[0]), *[_p(x) for x in arrs]))
 
     def diagnostics(self):
         """Entries with a contact force and the per-wall total forces of the

@@ -51,6 +51,11 @@ typedef struct {
 
 struct orc_sys {
   orc_config cfg;
+  /* atoms staged by orc_insert_atoms: they join at the next step after its
+   * initial integration, with a rebuild at that step (FixInsert) */
+  int npend;
+  int *pend_tag, *pend_type;
+  double *pend_x, *pend_v, *pend_w, *pend_r, *pend_m;
   /* diagnostics of the last force pass: entries with a contact force, and
    * the total force of each wall (planes, then meshes) on the atoms */
   long long ncontacts;
@@ -72,6 +77,7 @@ struct orc_sys {
   int np, npcap;
   int dnum;
   int list_valid;
+  int list_n;      /* atoms the current list was built for (later insertions have no rows) */
 
   /* partner table (FixContactHistory npartner_/partner_/contacthistory_) */
   int *pstart, *ptag;
@@ -122,6 +128,8 @@ void orc_destroy(orc_sys *s) {
   free(s->restlog); free(s->bond);
   free(s->tag); free(s->type); free(s->x); free(s->v); free(s->omega); free(s->f);
   free(s->torque); free(s->radius); free(s->rmass); free(s->xhold); free(s->prow);
+  free(s->pend_tag); free(s->pend_type); free(s->pend_x); free(s->pend_v); free(s->pend_w);
+  free(s->pend_r); free(s->pend_m);
   free(s->nstart); free(s->nj); free(s->nshift); free(s->nflag); free(s->nhist);
   free(s->pstart); free(s->ptag); free(s->phist);
   for (int w = 0; w < s->nplanes; w++) { free(s->planes[w].nlist); free(s->planes[w].hist); }
@@ -401,6 +409,67 @@ int orc_get_mesh_contacts(const orc_sys *s, int k, int *tag, int *tri, int *slot
   return c;
 }
 
+/* FixInsert::pre_exchange (src/fix_insert.cpp): new atoms staged between
+ * runs join at the next step after initial_integrate, and that step rebuilds
+ * (next_reneighbor = the insertion step) */
+int orc_insert_atoms(orc_sys *s, int k, const int *tag, const int *type, const double *x, const double *v,
+                     const double *omega, const double *radius, const double *rmass) {
+  if (k <= 0) return 0;
+  const int m = s->npend + k;
+  s->pend_tag = (int *)xrealloc(s->pend_tag, m * sizeof(int));
+  s->pend_type = (int *)xrealloc(s->pend_type, m * sizeof(int));
+  s->pend_x = (double *)xrealloc(s->pend_x, 3 * (size_t)m * sizeof(double));
+  s->pend_v = (double *)xrealloc(s->pend_v, 3 * (size_t)m * sizeof(double));
+  s->pend_w = (double *)xrealloc(s->pend_w, 3 * (size_t)m * sizeof(double));
+  s->pend_r = (double *)xrealloc(s->pend_r, (size_t)m * sizeof(double));
+  s->pend_m = (double *)xrealloc(s->pend_m, (size_t)m * sizeof(double));
+  const int o = s->npend;
+  memcpy(s->pend_tag + o, tag, k * sizeof(int));
+  memcpy(s->pend_type + o, type, k * sizeof(int));
+  memcpy(s->pend_x + 3 * o, x, 3 * (size_t)k * sizeof(double));
+  memcpy(s->pend_v + 3 * o, v, 3 * (size_t)k * sizeof(double));
+  memcpy(s->pend_w + 3 * o, omega, 3 * (size_t)k * sizeof(double));
+  memcpy(s->pend_r + o, radius, (size_t)k * sizeof(double));
+  memcpy(s->pend_m + o, rmass, (size_t)k * sizeof(double));
+  s->npend = m;
+  return 0;
+}
+
+static void commit_insert(orc_sys *s) {
+  const int n0 = s->n, k = s->npend;
+  grow_atoms(s, n0 + k);
+  for (int q = 0; q < k; q++) {
+    const int i = n0 + q;
+    s->tag[i] = s->pend_tag[q];
+    s->type[i] = s->pend_type[q];
+    for (int d = 0; d < 3; d++) {
+      s->x[3 * i + d] = s->pend_x[3 * q + d];
+      s->v[3 * i + d] = s->pend_v[3 * q + d];
+      s->omega[3 * i + d] = s->pend_w[3 * q + d];
+      s->f[3 * i + d] = 0.0;
+      s->torque[3 * i + d] = 0.0;
+      for (int w = 0; w < s->nplanes; w++) s->planes[w].hist[3 * i + d] = 0.0;
+    }
+    s->radius[i] = s->pend_r[q];
+    s->rmass[i] = s->pend_m[q];
+    s->prow[i] = -1;
+    for (int mm = 0; mm < s->nmeshes; mm++) {
+      orc_mesh *m = &s->meshes[mm];
+      m->nslot[i] = 0;
+      m->npartner[i] = 0;
+      for (int u = 0; u < MESH_MAXSLOT; u++) {
+        m->partner[(size_t)i * MESH_MAXSLOT + u] = -1;
+        m->keep[(size_t)i * MESH_MAXSLOT + u] = 0;
+        m->inter[(size_t)i * MESH_MAXSLOT + u] = 0;
+        for (int d = 0; d < 3; d++) m->hist[3 * ((size_t)i * MESH_MAXSLOT + u) + d] = 0.0;
+      }
+    }
+  }
+  s->n = n0 + k;
+  s->npend = 0;
+  s->next_reneighbor = s->ntimestep;
+}
+
 int orc_set_atoms(orc_sys *s, int n, const int *tag, const int *type, const double *x,
                   const double *v, const double *omega, const double *radius,
                   const double *rmass) {
@@ -545,9 +614,11 @@ static inline int hist_newton(const orc_sys *s, int d) {
 
 static void pre_exchange(orc_sys *s) {
   const int n = s->n, dnum = s->dnum;
+  /* atoms inserted since the last build (FixInsert) are not in the list */
+  const int nl = s->list_valid ? (s->list_n < n ? s->list_n : n) : 0;
   int *cnt = (int *)calloc(n + 1, sizeof(int));
   if (s->list_valid) {
-    for (int i = 0; i < n; i++)
+    for (int i = 0; i < nl; i++)
       for (int p = s->nstart[i]; p < s->nstart[i + 1]; p++)
         if (s->nflag[p]) {
           cnt[i]++;
@@ -563,7 +634,7 @@ static void pre_exchange(orc_sys *s) {
   s->phist = (double *)xrealloc(s->phist, ((size_t)tot * dnum + 1) * sizeof(double));
   memset(cnt, 0, (n + 1) * sizeof(int));
   if (s->list_valid) {
-    for (int i = 0; i < n; i++)
+    for (int i = 0; i < nl; i++)
       for (int p = s->nstart[i]; p < s->nstart[i + 1]; p++)
         if (s->nflag[p]) {
           const double *hist = &s->nhist[(size_t)p * dnum];
@@ -757,6 +828,7 @@ static int neighbor_build(orc_sys *s) {
   s->nstart = nstart; s->nj = nj; s->nshift = nsh; s->nflag = nfl; s->nhist = nh;
   s->np = np; s->npcap = cap;
   s->list_valid = 1;
+  s->list_n = n;
   memcpy(s->xhold, s->x, 3 * (size_t)n * sizeof(double));
   s->ago = 0;
   s->nrebuilds++;
@@ -1754,6 +1826,7 @@ int orc_run(orc_sys *s, int nsteps) {
     for (int k = 0; k < s->nmeshes; k++)
       if (s->meshes[k].moving == 1) mesh_move(s, &s->meshes[k]);
       else if (s->meshes[k].moving == 2) mesh_rotate(s, &s->meshes[k]);
+    if (s->npend > 0) commit_insert(s);
     if (decide(s)) {
       if (rebuild(s)) return -1;
     } else {

@@ -105,6 +105,10 @@ int orc_set_contact_history(orc_sys *s, int nentries, const int *tag_owner,
                             const int *tag_partner, const double *hist);
 int orc_set_wall_history(orc_sys *s, int wall, const double *hist);
 
+/* atoms that join at the next step after its initial integration, with a
+ * rebuild at that step (FixInsert::pre_exchange) */
+int orc_insert_atoms(orc_sys *s, int k, const int *tag, const int *type, const double *x, const double *v,
+                     const double *omega, const double *radius, const double *rmass);
 int orc_setup(orc_sys *s);            /* Verlet::setup */
 int orc_run(orc_sys *s, int nsteps);  /* nsteps iterations of Verlet::run */
 

@@ -165,3 +165,27 @@ def test_oracle_rotating_mesh_matches_reference():
         assert set(gm) == set(rm), st
         assert all(gm[k][0] == rm[k][0] for k in rm), st
     assert o.nrebuilds >= 4
+
+
+def test_oracle_insertion_joins_after_initial_integrate():
+    """orc_insert_atoms: staged atoms join at the next step after its initial
+    integration (they are not drifted at that step), and that step rebuilds."""
+    case, _ = load_golden("dense_hertz")
+    o = Oracle(case)
+    o.setup()
+    o.run(5)
+    nreb = o.nrebuilds
+    n0 = len(o.atoms()["tag"])
+    x = np.array([[1e-3, 1e-3, 0.013]])
+    new = dict(tag=np.array([100000], np.int32), type=np.array([1], np.int32), x=x,
+               v=np.array([[0.0, 0.0, -1.0]]), omega=np.zeros((1, 3)), radius=np.array([0.9e-3]),
+               rmass=np.array([4.0 / 3.0 * np.pi * 0.9e-3 ** 3 * 2500.0]))
+    o.insert(new)
+    o.run(1)
+    a = o.atoms()
+    assert len(a["tag"]) == n0 + 1
+    assert o.nrebuilds == nreb + 1
+    i = int(np.nonzero(a["tag"] == 100000)[0][0])
+    # no drift at the insertion step; the final half-kick used the step's forces
+    assert np.array_equal(a["x"][i], x[0])
+    assert a["v"][i][2] < -1.0
