@@ -16,6 +16,8 @@
 //   sliding (kt^2 |s2|^2 > (mu|Fn|)^2): Ft = -mu|Fn| s2/|s2|, s3 = (mu|Fn|/kt) s2/|s2|
 //   else: Ft = -kt s2 - gamma_t vtr, s3 = s2
 //   F = Fn en + Ft, Ti = -cri (en x Ft), Tj = -crj (en x Ft)
+// For a bonded pair the bond's force replaces Fn en (src/contact_models.h:
+// 228-238): F = Ft here, Fn still caps the friction.
 // Walls: radsum = reff = ri, meff = mi, no j terms.  Without
 // update_history (the setup force pass) s2 = shear.
 // The adjoint is exact for this piecewise-smooth law away from its switch
@@ -28,8 +30,9 @@ struct VjpIn {
   double d[3], vr[3], wi[3], wj[3], sh[3];
   double ri, rj, mi, mj;
   double Y, G, beta, mu, dt;
-  bool upd;   // update_history
+  bool upd;     // update_history
   bool wall;
+  bool bonded;  // a bond (cohesion bond/nonlinear) replaces the normal force
 };
 
 struct VjpBar {  // adjoints of the outputs (in) and of the inputs (out)
@@ -115,7 +118,7 @@ __device__ __forceinline__ void law_forward(const VjpIn &a, LawState &S, double 
   }
   cross3(S.en, S.Ft, S.tor);
   for (int k = 0; k < 3; k++) {
-    F[k] = S.Fn * S.en[k] + S.Ft[k];
+    F[k] = (a.bonded ? 0.0 : S.Fn * S.en[k]) + S.Ft[k];
     Ti[k] = -S.cri * S.tor[k];
     Tj[k] = -S.crj * S.tor[k];
   }
@@ -132,9 +135,9 @@ __device__ void law_vjp(const VjpIn &a, VjpBar &b) {
   double crib = -dot3(S.tor, b.Ti), crjb = -dot3(S.tor, b.Tj);
   cross3(S.Ft, torb, enb);
   cross3(torb, S.en, Ftb);
-  double Fnb = dot3(b.F, S.en);
+  double Fnb = a.bonded ? 0.0 : dot3(b.F, S.en);
   for (int k = 0; k < 3; k++) {
-    enb[k] += S.Fn * b.F[k];
+    enb[k] += a.bonded ? 0.0 : S.Fn * b.F[k];
     Ftb[k] += b.F[k];
   }
   double s2b[3] = {0., 0., 0.}, vtrb[3] = {0., 0., 0.};

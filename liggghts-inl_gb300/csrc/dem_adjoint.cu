@@ -294,6 +294,7 @@ __device__ __forceinline__ VjpIn pair_in(const ADev &s, const double *x, int p, 
   a.mu = s.mu;
   a.dt = s.dt;
   a.wall = false;
+  a.bonded = false;
   return a;
 }
 
@@ -328,6 +329,7 @@ __device__ __forceinline__ bool wall_in(const ADev &s, const double *x, int w, i
   a.mu = s.mu;
   a.dt = s.dt;
   a.wall = true;
+  a.bonded = false;
   return true;
 }
 
