@@ -340,8 +340,9 @@ const char *dem_version(void);
  * N-step run with respect to Young's modulus, restitution, friction and
  * every particle radius, by reverse-mode differentiation of the exact
  * discrete timestep: Verlet::setup + N Verlet steps (src/verlet.cpp:281-389)
- * of FixNVESphere, PairGran Hertz + tangential history (cdf 1, no rolling,
- * no cohesion), FixGravity and FixWallGran primitive planes, one atom type
+ * of FixNVESphere, PairGran Hertz + tangential history (no rolling; with
+ * cohesion bond/nonlinear when dem_adjoint_set_bonds is called, else contact
+ * distance factor 1), FixGravity and FixWallGran primitive planes, one atom type
  * and one material (Yeff/Geff/betaeff of the material against itself,
  * src/global_properties.cpp).  Masses follow the radii: m = 4/3 pi r^3 rho.
  * The neighbour list is rebuilt every `segment` steps, after the drift of
@@ -380,6 +381,16 @@ typedef struct dem_adjoint_loss {
 typedef struct dem_adjoint dem_adjoint;
 int dem_adjoint_create(const dem_adjoint_config *cfg, dem_adjoint **out);
 int dem_adjoint_destroy(dem_adjoint *h);
+/* cohesion bond/nonlinear in the forward model (pair_style gran ... cohesion
+ * bond/nonlinear; CohesionModel<COHESION_BOND_NONLINEAR>, src/
+ * cohesion_model_bond_nonlinear.h:394-992): values holds the 23 properties of
+ * the one type pair in DEM_BOND_* order, st the model's settings (as in
+ * dem_set_bond_params); bonds are created at step tsCreate of the run (the
+ * setup pass is step 0) or always.  Call before dem_adjoint_set_state, which
+ * derives the contact distance factor from the smallest radius.  The
+ * gradients then include the bonds' forces, created, evolved and carried
+ * across rebuilds as the main path does. */
+int dem_adjoint_set_bonds(dem_adjoint *h, const double *values, const dem_bond_settings *st);
 /* initial state (host arrays): x, v, omega n*3, radius n (the radii define the
  * neighbour cells; runs may use radii up to 1 % larger) */
 int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *v, const double *omega,

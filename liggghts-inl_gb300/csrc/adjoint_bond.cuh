@@ -374,8 +374,9 @@ __device__ __forceinline__ void ab_damp_vjp(double x, double v, double c, double
 
 // VJP: Fb/Tib/Tjb the adjoints of the bond's force and torques, houtb those of
 // the history after the evaluation; fills ab (input adjoints, overwritten)
-// and hinb (history adjoints before the evaluation, overwritten)
-__device__ void bond_vjp(const BondArgs &a, const BondPar &P, const double hin[kBondValues], const double Fb[3],
+// and hinb (history adjoints before the evaluation, overwritten); returns the
+// forward's result (kBond*)
+__device__ int bond_vjp(const BondArgs &a, const BondPar &P, const double hin[kBondValues], const double Fb[3],
                          const double Tib[3], const double Tjb[3], const double houtb[kBondValues],
                          BondArgsBar &ab, double hinb[kBondValues]) {
   BondTape T;
@@ -387,11 +388,11 @@ __device__ void bond_vjp(const BondArgs &a, const BondPar &P, const double hin[k
   if (st == kBondNone) {
     for (int k = 0; k < kBondValues; k++) hinb[k] = houtb[k];
     hinb[2] = hinb[3] = hinb[4] = 0.0;
-    return;
+    return st;
   }
   if (!T.evaluated) {  // broken on distance: bondFlag and initial_dist reset
     for (int k = T.created ? 14 : 5; k < kBondValues; k++) hinb[k] = houtb[k];
-    return;
+    return st;
   }
   const int fl = P.flags;
   const double dt = a.dt;
@@ -613,6 +614,7 @@ __device__ void bond_vjp(const BondArgs &a, const BondPar &P, const double hin[k
     rbar += -rinvb * T.rinv * T.rinv;
     for (int k = 0; k < 3; k++) ab.d[k] += T.rinv * enb[k] + rbar * a.d[k] * T.rinv;
   }
+  return st;
 }
 
 }  // namespace gb300

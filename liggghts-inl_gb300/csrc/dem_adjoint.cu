@@ -1,5 +1,6 @@
 // Discrete adjoint of the sphere-DEM timestep (Hertz + tangential history,
-// primitive planes, gravity, nve/sphere) with sqrt(N) checkpointing.
+// cohesion bond/nonlinear, primitive planes, gravity, nve/sphere) with
+// sqrt(N) checkpointing.
 //
 // Forward model: the reference's Verlet step (src/verlet.cpp:281-389) with
 // FixNVESphere (src/fix_nve_sphere.cpp:120-215), PairGran with the Hertz +
@@ -35,6 +36,18 @@
 // old entry carries history.  The backward pass maps the history adjoints
 // back through the same map.
 //
+// With cohesion bond/nonlinear (dem_adjoint_set_bonds) each entry also
+// carries the bond's 28 history values, created, evolved, broken and carried
+// as the main path does (bond_law.cuh, k_pair<..., BOND>): the list cutoff
+// and the carry distance grow by the contact distance factor, pairs within
+// that distance but not touching clear their tangential history and
+// evaluate a bond they hold (or may create), and the bond's force replaces
+// the normal model's force of a touching bonded pair.  Bond values with
+// newtonflag 1 (ft, thetan, thetat) change sign in a flipped carry, as in
+// FixContactHistory::pre_exchange (src/fix_contact_history.cpp:400-410).
+// The backward pass carries their adjoints through the same steps
+// (adjoint_bond.cuh).
+//
 // Reverse-mode arithmetic is deterministic: pair results are gathered per
 // atom in list order (own row, then reverse list), parameter gradients are
 // reduced per block and then summed in block order.
@@ -47,6 +60,7 @@
 #include <vector>
 
 #include "../../include/liggghts_gb300.h"
+#include "adjoint_bond.cuh"
 #include "adjoint_law.cuh"
 #include "dem_device.cuh"
 #include "dem_kernels.h"
@@ -63,8 +77,9 @@ struct AList {
   int *pi = nullptr, *pj = nullptr, *row = nullptr, *rev_start = nullptr, *rev = nullptr;
   int *carry = nullptr;     // old entry e (>= 0), -(e + 2) for a flipped copy, -1 none
   uint8_t *sh = nullptr;    // image code of the partner
-  uint8_t *flag = nullptr;  // entry carries history (carried or touched)
+  uint8_t *flag = nullptr;  // kContact* bits; nonzero: the entry's history is carried
   double *shear = nullptr;  // [3*p+k], evolving
+  double *bond = nullptr;   // [kBondValues*p+k], evolving (bonds only)
 };
 
 struct ADev {
@@ -78,6 +93,12 @@ struct ADev {
   double ppos[8];
   double Y, G, beta, mu;
   double dtf, dtfrot;
+  // cohesion bond/nonlinear: on/off, contact distance factor, parameters of
+  // the one type pair, tsCreateBondnonlinear
+  int bonds;
+  double cdf;
+  BondPar bp;
+  long long ts_create;
   double *x, *v, *w, *F, *T, *r, *m, *ws;  // ws [(w*n + i)*3 + k]
   // list in use
   int np;
@@ -85,9 +106,10 @@ struct ADev {
   const uint8_t *sh;
   uint8_t *flag;
   double *shear;
+  double *bh;  // bond history of the list in use
   // pair outputs of the current force evaluation
   double *pF, *pTi, *pTj;
-  uint8_t *touch;
+  uint8_t *active;  // touching or bonded: the entry's outputs count
   // cells
   int nc[3];
   double csz[3];
@@ -161,7 +183,8 @@ __global__ void ka_cellsort(ADev s) {
 }
 
 // granular half list in input order: local pairs once (owner = lower index),
-// periodic images as directed entries of each owner; cutoff ri + rj + skin
+// periodic images as directed entries of each owner; cutoff
+// (ri + rj) cdf + skin (src/neigh_gran.cpp:580-586)
 template <bool FILL>
 __global__ void ka_pairs(ADev s, int *pi, int *pj, uint8_t *shc, const int *row) {
   AGRID(i, s.n) {
@@ -198,7 +221,7 @@ __global__ void ka_pairs(ADev s, int *pi, int *pj, uint8_t *shc, const int *row)
             double xj[3] = {s.x[3 * j], s.x[3 * j + 1], s.x[3 * j + 2]};
             a_image(s, code, xj);
             const double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
-            const double cs = ri + s.r[j] + s.skin;
+            const double cs = (ri + s.r[j]) * s.cdf + s.skin;
             if (dx * dx + dy * dy + dz * dz > cs * cs) continue;
             if (!FILL) {
               cnt++;
@@ -237,8 +260,9 @@ __global__ void ka_rev_sort(int n, const int *start, int *rev) {
   }
 }
 
-// history carried from the previous list (see the file comment); also sets
-// the new entries' flags
+// history carried from the previous list (see the file comment): pairs within
+// (ri + rj) cdf at the build (src/neigh_gran.cpp:590-620); also sets the new
+// entries' flags
 __global__ void ka_carry(ADev s, AList nw, AList old) {
   AGRID(p, nw.np) {
     const int i = nw.pi[p], j = nw.pj[p], code = nw.sh[p];
@@ -247,7 +271,7 @@ __global__ void ka_carry(ADev s, AList nw, AList old) {
     double xj[3] = {s.x[3 * j], s.x[3 * j + 1], s.x[3 * j + 2]};
     a_image(s, code, xj);
     const double dx = s.x[3 * i] - xj[0], dy = s.x[3 * i + 1] - xj[1], dz = s.x[3 * i + 2] - xj[2];
-    const double rs = s.r[i] + s.r[j];
+    const double rs = (s.r[i] + s.r[j]) * s.cdf;
     if (old.np > 0 && dx * dx + dy * dy + dz * dz < rs * rs) {
       for (int q = old.row[i]; q < old.row[i + 1]; q++)
         if (old.pj[q] == j && old.flag[q]) {
@@ -267,6 +291,11 @@ __global__ void ka_carry(ADev s, AList nw, AList old) {
     nw.carry[p] = e < 0 ? -1 : (sgn > 0 ? e : -(e + 2));
     nw.flag[p] = e >= 0 ? 1 : 0;
     for (int k = 0; k < 3; k++) nw.shear[3 * p + k] = e >= 0 ? sgn * old.shear[3 * e + k] : 0.0;
+    if (s.bonds)
+      for (int k = 0; k < kBondValues; k++) {
+        const double f = (sgn < 0 && k >= 5 && k <= 13) ? -1.0 : 1.0;  // newtonflag 1: ft, thetan, thetat
+        nw.bond[(size_t)kBondValues * p + k] = e >= 0 ? f * old.bond[(size_t)kBondValues * e + k] : 0.0;
+      }
   }
 }
 
@@ -303,6 +332,30 @@ __device__ __forceinline__ bool pair_touch(const VjpIn &a) {
   return dot3(a.d, a.d) < rs * rs;
 }
 
+// within the contact distance (ri + rj) cdf (surfacesClose)
+__device__ __forceinline__ bool pair_band(const ADev &s, const VjpIn &a) {
+  const double rs = a.ri + a.rj;
+  return dot3(a.d, a.d) < s.cdf * s.cdf * rs * rs;
+}
+
+__device__ __forceinline__ BondArgs bond_in(const ADev &s, const VjpIn &a, const double *x, int i,
+                                            long long ntimestep) {
+  BondArgs b;
+  for (int k = 0; k < 3; k++) {
+    b.d[k] = a.d[k];
+    b.vr[k] = a.vr[k];
+    b.wi[k] = a.wi[k];
+    b.wj[k] = a.wj[k];
+    b.xi[k] = x[3 * i + k];
+  }
+  b.ri = a.ri;
+  b.rj = a.rj;
+  b.dt = a.dt;
+  b.upd = a.upd;
+  b.may_create = a.upd && ((s.bp.flags & kBondCreateAlways) || ntimestep == s.ts_create);
+  return b;
+}
+
 // plane w against atom i (FixWallGran primitive: overlap when the distance
 // to the plane is at most the radius); false when not touching
 __device__ __forceinline__ bool wall_in(const ADev &s, const double *x, int w, int i, const double *vh,
@@ -333,29 +386,63 @@ __device__ __forceinline__ bool wall_in(const ADev &s, const double *x, int w, i
   return true;
 }
 
-// pair forces of the current state (vh, wh: the velocities the forces see);
-// tape_sh receives the history before the update
-__global__ void ka_pair_force(ADev s, const double *vh, const double *wh, int upd, double *tape_sh) {
+// pair forces of the current state (vh, wh: the velocities the forces see)
+// at step ntimestep; tape_sh/tape_bh receive the history before the update.
+// The pass follows k_pair<..., BOND> of the main path: touching entries run
+// the contact law (with a bond's force in place of the normal force),
+// entries within the contact distance but apart clear their tangential
+// history and evaluate a bond they hold or may create.
+// BONDS: the system has cohesion bond/nonlinear (a separate instance keeps
+// the registers of the plain contact path low)
+template <bool BONDS>
+__global__ void ka_pair_force(ADev s, const double *vh, const double *wh, int upd, long long ntimestep,
+                              double *tape_sh, double *tape_bh) {
   AGRID(p, s.np) {
     VjpIn a = pair_in(s, s.x, p, vh, wh, s.shear);
     a.upd = upd != 0;
     if (tape_sh)
       for (int k = 0; k < 3; k++) tape_sh[3 * p + k] = a.sh[k];
-    if (!pair_touch(a)) {
-      s.touch[p] = 0;  // history kept (no surfacesClose band with cdf 1)
-      continue;
+    double *bh = BONDS ? s.bh + (size_t)kBondValues * p : nullptr;
+    if (BONDS && tape_bh)
+      for (int k = 0; k < kBondValues; k++) tape_bh[(size_t)kBondValues * p + k] = bh[k];
+    const bool touch = pair_touch(a), band = pair_band(s, a);
+    if (!touch && band) {  // TangentialModel<TANGENTIAL_HISTORY>::surfacesClose
+      for (int k = 0; k < 3; k++) s.shear[3 * p + k] = 0.0;
+      s.flag[p] &= ~kContactTangential;
     }
-    LawState S;
-    double F[3], Ti[3], Tj[3], s3[3];
-    law_forward(a, S, F, Ti, Tj, s3);
-    for (int k = 0; k < 3; k++) {
-      s.pF[3 * p + k] = F[k];
-      s.pTi[3 * p + k] = Ti[k];
-      s.pTj[3 * p + k] = Tj[k];
-      if (upd) s.shear[3 * p + k] = s3[k];
+    int st = kBondNone;
+    double bF[3] = {0., 0., 0.}, bTi[3] = {0., 0., 0.}, bTj[3] = {0., 0., 0.};
+    if (BONDS && (touch || band)) {
+      const BondArgs b = bond_in(s, a, s.x, s.pi[p], ntimestep);
+      double hin[kBondValues], hout[kBondValues];
+      for (int k = 0; k < kBondValues; k++) hin[k] = bh[k];
+      BondTape T;
+      st = bond_fwd(b, s.bp, hin, hout, bF, bTi, bTj, T);
+      for (int k = 0; k < kBondValues; k++) bh[k] = hout[k];
+      if (st == kBondActive) s.flag[p] |= kContactCohesion;
+      if (st == kBondBroken) s.flag[p] &= ~kContactCohesion;
     }
-    if (upd) s.flag[p] = 1;
-    s.touch[p] = 1;
+    const bool bonded = st == kBondActive;
+    if (touch) {
+      a.bonded = bonded;
+      LawState S;
+      double F[3], Ti[3], Tj[3], s3[3];
+      law_forward(a, S, F, Ti, Tj, s3);
+      for (int k = 0; k < 3; k++) {
+        s.pF[3 * p + k] = F[k] + bF[k];
+        s.pTi[3 * p + k] = Ti[k] + bTi[k];
+        s.pTj[3 * p + k] = Tj[k] + bTj[k];
+        if (upd) s.shear[3 * p + k] = s3[k];
+      }
+      s.flag[p] |= kContactNormal | kContactTangential;
+    } else if (bonded) {
+      for (int k = 0; k < 3; k++) {
+        s.pF[3 * p + k] = bF[k];
+        s.pTi[3 * p + k] = bTi[k];
+        s.pTj[3 * p + k] = bTj[k];
+      }
+    }
+    s.active[p] = (touch || bonded) ? 1 : 0;
   }
 }
 
@@ -367,14 +454,14 @@ __global__ void ka_gather(ADev s, const double *vh, const double *wh, int upd, i
   AGRID(i, s.n) {
     double f[3] = {0., 0., 0.}, t[3] = {0., 0., 0.};
     for (int p = s.row[i]; p < s.row[i + 1]; p++)
-      if (s.touch[p])
+      if (s.active[p])
         for (int k = 0; k < 3; k++) {
           f[k] += s.pF[3 * p + k];
           t[k] += s.pTi[3 * p + k];
         }
     for (int q = s.rev_start[i]; q < s.rev_start[i + 1]; q++) {
       const int p = s.rev[q];
-      if (!s.touch[p] || s.sh[p] != kNoShift) continue;
+      if (!s.active[p] || s.sh[p] != kNoShift) continue;
       for (int k = 0; k < 3; k++) {
         f[k] -= s.pF[3 * p + k];
         t[k] += s.pTj[3 * p + k];
@@ -442,6 +529,7 @@ struct ABar {
   double *xb, *vb, *wb, *Fb, *Tb, *rb, *mb, *sb, *wsb;
   // per-entry VJP outputs of the pair law
   double *pd, *pv, *pwi, *pwj, *pri, *prj, *pmi, *pmj, *pth;  // pth [4*p]: Y, G, beta, mu
+  double *bb;   // [kBondValues*p] adjoint of the bond history (bonds only)
   double *wth;  // [4*i] wall parameter adjoints per atom
   double *th;   // [4] accumulated parameter adjoints
 };
@@ -506,42 +594,87 @@ __global__ void kb_walls(ADev s, ABar B, const double *x, const double *vh, cons
   }
 }
 
+// reverse of ka_pair_force for one evaluation at positions x (vh/wh the
+// velocities it saw, sh_before/bh_before the history before it); the input
+// adjoints of each entry go to the per-entry arrays, the history adjoints
+// B.sb/B.bb are replaced by those of the history before the evaluation
+template <bool BONDS>
 __global__ void kb_pairs(ADev s, ABar B, const double *x, const double *vh, const double *wh,
-                         const double *sh_before, int upd) {
+                         const double *sh_before, const double *bh_before, int upd, long long ntimestep) {
   AGRID(p, s.np) {
     VjpIn a = pair_in(s, x, p, vh, wh, sh_before);
     a.upd = upd != 0;
     const int i = s.pi[p], j = s.pj[p];
     const bool local = s.sh[p] == kNoShift;
-    if (!pair_touch(a)) {
-      for (int k = 0; k < 3; k++) B.pd[3 * p + k] = B.pv[3 * p + k] = B.pwi[3 * p + k] = B.pwj[3 * p + k] = 0.0;
-      B.pri[p] = B.prj[p] = B.pmi[p] = B.pmj[p] = 0.0;
-      for (int k = 0; k < 4; k++) B.pth[4 * p + k] = 0.0;
-      continue;  // history unchanged: its adjoint passes through
-    }
-    VjpBar bb;
+    const bool touch = pair_touch(a), band = pair_band(s, a);
+    double Fb[3], Tib[3], Tjb[3];
     for (int k = 0; k < 3; k++) {
-      bb.F[k] = B.Fb[3 * i + k] - (local ? B.Fb[3 * j + k] : 0.0);
-      bb.Ti[k] = B.Tb[3 * i + k];
-      bb.Tj[k] = local ? B.Tb[3 * j + k] : 0.0;
-      bb.s3[k] = upd ? B.sb[3 * p + k] : 0.0;
+      Fb[k] = B.Fb[3 * i + k] - (local ? B.Fb[3 * j + k] : 0.0);
+      Tib[k] = B.Tb[3 * i + k];
+      Tjb[k] = local ? B.Tb[3 * j + k] : 0.0;
     }
-    law_vjp(a, bb);
+    double d[3] = {0., 0., 0.}, vr[3] = {0., 0., 0.}, wi[3] = {0., 0., 0.}, wj[3] = {0., 0., 0.};
+    double ri = 0.0, rj = 0.0, mi = 0.0, mj = 0.0, th[4] = {0., 0., 0., 0.};
+    int st = kBondNone;
+    if (BONDS && (touch || band)) {
+      const BondArgs b = bond_in(s, a, x, i, ntimestep);
+      double hin[kBondValues], houtb[kBondValues], hinb[kBondValues];
+      double *bb = B.bb + (size_t)kBondValues * p;
+      for (int k = 0; k < kBondValues; k++) {
+        hin[k] = bh_before[(size_t)kBondValues * p + k];
+        houtb[k] = bb[k];
+      }
+      BondArgsBar ab;
+      st = bond_vjp(b, s.bp, hin, Fb, Tib, Tjb, houtb, ab, hinb);
+      for (int k = 0; k < kBondValues; k++) bb[k] = hinb[k];
+      for (int k = 0; k < 3; k++) {
+        d[k] += ab.d[k];
+        vr[k] += ab.vr[k];
+        wi[k] += ab.wi[k];
+        wj[k] += ab.wj[k];
+      }
+      ri += ab.ri;
+      rj += ab.rj;
+    }
+    if (touch) {
+      a.bonded = st == kBondActive;
+      VjpBar bb;
+      for (int k = 0; k < 3; k++) {
+        bb.F[k] = Fb[k];
+        bb.Ti[k] = Tib[k];
+        bb.Tj[k] = Tjb[k];
+        bb.s3[k] = upd ? B.sb[3 * p + k] : 0.0;
+      }
+      law_vjp(a, bb);
+      for (int k = 0; k < 3; k++) {
+        d[k] += bb.d[k];
+        vr[k] += bb.vr[k];
+        wi[k] += bb.wi[k];
+        wj[k] += bb.wj[k];  // F_i and T_i depend on w_j for periodic images too
+        B.sb[3 * p + k] = bb.sh[k] + (upd ? 0.0 : B.sb[3 * p + k]);
+      }
+      ri += bb.ri;
+      rj += bb.rj;
+      mi += bb.mi;
+      mj += bb.mj;
+      th[0] = bb.Y;
+      th[1] = bb.G;
+      th[2] = bb.beta;
+      th[3] = bb.mu;
+    } else if (band) {
+      for (int k = 0; k < 3; k++) B.sb[3 * p + k] = 0.0;  // history cleared: no dependence
+    }  // else: history unchanged, its adjoint passes through
     for (int k = 0; k < 3; k++) {
-      B.pd[3 * p + k] = bb.d[k];
-      B.pv[3 * p + k] = bb.vr[k];
-      B.pwi[3 * p + k] = bb.wi[k];
-      B.pwj[3 * p + k] = bb.wj[k];  // F_i and T_i depend on w_j for periodic images too
-      B.sb[3 * p + k] = bb.sh[k] + (upd ? 0.0 : B.sb[3 * p + k]);
+      B.pd[3 * p + k] = d[k];
+      B.pv[3 * p + k] = vr[k];
+      B.pwi[3 * p + k] = wi[k];
+      B.pwj[3 * p + k] = wj[k];
     }
-    B.pri[p] = bb.ri;
-    B.prj[p] = bb.rj;
-    B.pmi[p] = bb.mi;
-    B.pmj[p] = bb.mj;
-    B.pth[4 * p + 0] = bb.Y;
-    B.pth[4 * p + 1] = bb.G;
-    B.pth[4 * p + 2] = bb.beta;
-    B.pth[4 * p + 3] = bb.mu;
+    B.pri[p] = ri;
+    B.prj[p] = rj;
+    B.pmi[p] = mi;
+    B.pmj[p] = mj;
+    for (int k = 0; k < 4; k++) B.pth[4 * p + k] = th[k];
   }
 }
 
@@ -629,14 +762,26 @@ __global__ void kb_accum4(const double *part, int nb, double *acc) {
 
 // history adjoints at a build back to the previous list's entries: direct
 // copies first, then the flipped copies of old local entries (each old entry
-// has at most one source of each kind, so both passes are race-free)
-__global__ void kb_uncarry(int np_new, const int *carry, const double *sb_new, double *sb_old, int flipped) {
+// has at most one source of each kind, so both passes are race-free); bb_new
+// and bb_old (bond values) may be null
+__global__ void kb_uncarry(int np_new, const int *carry, const double *sb_new, double *sb_old, int flipped,
+                           const double *bb_new, double *bb_old) {
   AGRID(p, np_new) {
     const int c = carry[p];
-    if (!flipped && c >= 0)
+    if (!flipped && c >= 0) {
       for (int k = 0; k < 3; k++) sb_old[3 * c + k] += sb_new[3 * p + k];
-    if (flipped && c <= -2)
-      for (int k = 0; k < 3; k++) sb_old[3 * (-c - 2) + k] -= sb_new[3 * p + k];
+      if (bb_new)
+        for (int k = 0; k < kBondValues; k++)
+          bb_old[(size_t)kBondValues * c + k] += bb_new[(size_t)kBondValues * p + k];
+    }
+    if (flipped && c <= -2) {
+      const int e = -c - 2;
+      for (int k = 0; k < 3; k++) sb_old[3 * e + k] -= sb_new[3 * p + k];
+      if (bb_new)
+        for (int k = 0; k < kBondValues; k++)
+          bb_old[(size_t)kBondValues * e + k] +=
+              ((k >= 5 && k <= 13) ? -1.0 : 1.0) * bb_new[(size_t)kBondValues * p + k];
+    }
   }
 }
 
@@ -709,6 +854,7 @@ struct dem_adjoint {
   double *part = nullptr;
   double last_fwd_ms = 0.0, last_bwd_ms = 0.0;
   int last_nseg = 0, last_maxnp = 0;
+  dem_bond_settings bond_settings{};
 };
 
 #define ATRY(h, call)                                                \
@@ -744,7 +890,7 @@ cudaError_t dmalloc(std::vector<void *> &owned, T **p, size_t n) {
 
 struct Checkpoint {
   double *x, *v, *w, *F, *T, *ws;  // state before the segment's first drift
-  double *sh0;                     // the list's history as carried at the build
+  double *sh0, *bh0;               // the list's history as carried at the build
   AList L;
 };
 
@@ -776,6 +922,7 @@ int build_list(dem_adjoint *h, AList &L, const AList &old) {
   AGET(h, L.rev, int, np);
   AGET(h, L.carry, int, np);
   AGET(h, L.shear, double, 3 * (size_t)np);
+  if (s.bonds) AGET(h, L.bond, double, (size_t)kBondValues * np);
   ka_pairs<true><<<grid_of(n), kAB, 0, st>>>(s, L.pi, L.pj, L.sh, L.row);
   ATRY(h, cudaMemsetAsync(h->rcnt, 0, (n + 1) * sizeof(int), st));
   ATRY(h, cudaMemsetAsync(h->rfill, 0, (n + 1) * sizeof(int), st));
@@ -790,8 +937,9 @@ int build_list(dem_adjoint *h, AList &L, const AList &old) {
   return DEM_OK;
 }
 
-void use_list(dem_adjoint *h, const AList &L, double *shear) {
+void use_list(dem_adjoint *h, const AList &L, double *shear, double *bond) {
   ADev &s = h->s;
+  s.bh = bond;
   s.np = L.np;
   s.pi = L.pi;
   s.pj = L.pj;
@@ -811,7 +959,8 @@ int ensure_pairs(dem_adjoint *h, int np) {
   double **d1[] = {&h->B.pri, &h->B.prj, &h->B.pmi, &h->B.pmj};
   for (double **q : d1) ATRY(h, dmalloc(h->owned, q, (size_t)cap));
   ATRY(h, dmalloc(h->owned, &h->B.pth, 4 * (size_t)cap));
-  ATRY(h, dmalloc(h->owned, &h->s.touch, (size_t)cap));
+  if (h->s.bonds) ATRY(h, dmalloc(h->owned, &h->B.bb, (size_t)kBondValues * cap));
+  ATRY(h, dmalloc(h->owned, &h->s.active, (size_t)cap));
   h->pcap = cap;
   return DEM_OK;
 }
@@ -829,11 +978,23 @@ void derive(double E, double nu, double e, double &Y, double &G, double &beta, d
   dbde = (1.0 / e) * (M_PI * M_PI) / std::pow(lg * lg + M_PI * M_PI, 1.5);
 }
 
-void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, double *tape_sh,
-                double *tape_ws, int final_kick, double *wallF) {
+void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, long long ntimestep,
+                double *tape_sh, double *tape_bh, double *tape_ws, int final_kick, double *wallF) {
   ADev &s = h->s;
-  if (s.np > 0) ka_pair_force<<<grid_of(s.np), kAB, 0, h->st>>>(s, vh, wh, upd, tape_sh);
+  if (s.np > 0 && s.bonds)
+    ka_pair_force<true><<<grid_of(s.np), kAB, 0, h->st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
+  else if (s.np > 0)
+    ka_pair_force<false><<<grid_of(s.np), kAB, 0, h->st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
   ka_gather<<<grid_of(h->n), kAB, 0, h->st>>>(s, vh, wh, upd, final_kick, tape_ws, wallF);
+}
+
+void pairs_vjp(dem_adjoint *h, const double *x, const double *vh, const double *wh, const double *sh_before,
+               const double *bh_before, int upd, long long ntimestep) {
+  const ADev &s = h->s;
+  if (s.np > 0 && s.bonds)
+    kb_pairs<true><<<grid_of(s.np), kAB, 0, h->st>>>(s, h->B, x, vh, wh, sh_before, bh_before, upd, ntimestep);
+  else if (s.np > 0)
+    kb_pairs<false><<<grid_of(s.np), kAB, 0, h->st>>>(s, h->B, x, vh, wh, sh_before, bh_before, upd, ntimestep);
 }
 
 void accumulate(dem_adjoint *h, const double *in, int cnt) {
@@ -889,7 +1050,40 @@ int dem_adjoint_create(const dem_adjoint_config *cfg, dem_adjoint **out) {
   // FixNVESphere: dtf = dt/2 (force units 1), dtfrot = dtf / INERTIA (0.4)
   s.dtf = 0.5 * cfg->dt;
   s.dtfrot = s.dtf / 0.4;
+  s.bonds = 0;
+  s.cdf = 1.0;
   *out = h;
+  return DEM_OK;
+}
+
+int dem_adjoint_set_bonds(dem_adjoint *h, const double *values, const dem_bond_settings *st) {
+  if (!h || !values || !st || h->n) return DEM_ERR_BAD_ARG;
+  for (int k = 0; k < kBondTables; k++)
+    if (!std::isfinite(values[k])) return DEM_ERR_BAD_ARG;
+  for (int k = kBondDampFn; k <= kBondDampTt; k++)
+    if (values[k] < 0.0 || values[k] > 1.0) return DEM_ERR_BAD_ARG;
+  if (st->stressBreak && values[kBondKfn2] <= 1e-15) {
+    h->err = "stress breakage needs stiffnessPerUnitAreaK_fn2 > 0";
+    return DEM_ERR_BAD_ARG;
+  }
+  ADev &s = h->s;
+  for (int k = 0; k < kBondTables; k++) s.bp.t[k] = values[k];
+  // the settings as dem_set_bond_params maps them
+  int fl = 0;
+  if (st->stressBreak) fl |= kBondStressBreak;
+  if (st->tensionStress) fl |= kBondTension;
+  if (st->compressionStress) fl |= kBondCompression;
+  if (st->shearStress) fl |= kBondShear;
+  if (st->normalTorqueStress) fl |= kBondNormalTorque;
+  if (st->shearTorqueStress) fl |= kBondShearTorque;
+  if (st->createBondAlways) fl |= kBondCreateAlways;
+  if (st->dampingBond || st->dampingBondSmooth) fl |= kBondDamping;
+  if (st->dampingBondSmooth) fl |= kBondDampingSmooth;
+  if (st->ratioTCBond) fl |= kBondUseRatioTC;
+  s.bp.flags = fl;
+  s.ts_create = (long long)(int)st->tsCreate;
+  s.bonds = values[kBondLambda] >= 1e-15 ? 1 : 0;
+  h->bond_settings = *st;
   return DEM_OK;
 }
 
@@ -914,9 +1108,30 @@ int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *
     if (!(radius[i] > 0.0)) return DEM_ERR_BAD_ARG;
     rmax = std::max(rmax, radius[i]);
   }
+  // contact distance factor of cohesion bond/nonlinear
+  // (neighbor->register_contact_dist_factor, connectToProperties,
+  // src/cohesion_model_bond_nonlinear.h:330-380) from the smallest radius
+  if (s.bonds) {
+    double minrad = radius[0];
+    for (int i = 1; i < n; i++) minrad = std::min(minrad, radius[i]);
+    const dem_bond_settings &bs = h->bond_settings;
+    double one;
+    if (!bs.stressBreak) {
+      one = 1.1 * 0.5 * s.bp.t[kBondMaxDist] / minrad;
+    } else {
+      double stress = s.bp.t[kBondMaxSigma];
+      if (bs.ratioTCBond) stress = std::fmax(stress, stress * s.bp.t[kBondRatioTC]);
+      one = 0.5 * 1.1 * s.bp.t[kBondCreateDist] / minrad + 0.5 * 1.1 * stress / (s.bp.t[kBondKfn2] * minrad);
+    }
+    s.cdf = std::max(1.0, one);
+    if (s.cdf > 10.0) {
+      h->err = "bond distance above 10 particle diameters";
+      return DEM_ERR_BAD_ARG;
+    }
+  }
   // cells at least one neighbour cutoff wide for radii up to 1 % larger
   // than the initial ones
-  const double cut = 2.0 * rmax * 1.01 + s.skin;
+  const double cut = 2.0 * rmax * 1.01 * s.cdf + s.skin;
   long ncell = 1;
   int nc[3];
   for (int d = 0; d < 3; d++) {
@@ -1025,11 +1240,15 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       if (rc) return rc;
       rc = ensure_pairs(h, c.L.np);
       if (rc) return rc;
-      use_list(h, c.L, c.L.shear);
-      force_pass(h, s.v, s.w, 0, nullptr, nullptr, 0, nullptr);  // Verlet::setup
+      use_list(h, c.L, c.L.shear, c.L.bond);
+      force_pass(h, s.v, s.w, 0, 0, nullptr, nullptr, nullptr, 0, nullptr);  // Verlet::setup
       copyd(h, h->xref, s.x, S3);
       AGET(h, c.sh0, double, 3 * (size_t)c.L.np);
       copyd(h, c.sh0, c.L.shear, 3 * (size_t)c.L.np);
+      if (s.bonds) {
+        AGET(h, c.bh0, double, (size_t)kBondValues * c.L.np);
+        copyd(h, c.bh0, c.L.bond, (size_t)kBondValues * c.L.np);
+      }
     }
     copyd(h, c.x, s.x, S3);
     copyd(h, c.v, s.v, S3);
@@ -1046,12 +1265,16 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
         if (rc) return rc;
         rc = ensure_pairs(h, c.L.np);
         if (rc) return rc;
-        use_list(h, c.L, c.L.shear);
+        use_list(h, c.L, c.L.shear, c.L.bond);
         copyd(h, h->xref, s.x, S3);
         AGET(h, c.sh0, double, 3 * (size_t)c.L.np);
         copyd(h, c.sh0, c.L.shear, 3 * (size_t)c.L.np);
+        if (s.bonds) {
+          AGET(h, c.bh0, double, (size_t)kBondValues * c.L.np);
+          copyd(h, c.bh0, c.L.bond, (size_t)kBondValues * c.L.np);
+        }
       }
-      force_pass(h, s.v, s.w, 1, nullptr, nullptr, 1, t == nsteps ? h->wallF : nullptr);
+      force_pass(h, s.v, s.w, 1, t, nullptr, nullptr, nullptr, 1, t == nsteps ? h->wallF : nullptr);
     }
     maxnp = std::max(maxnp, c.L.np);
   }
@@ -1120,6 +1343,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   ATRY(h, cudaMemsetAsync(B.Tb, 0, S3 * sizeof(double), st));
   ATRY(h, cudaMemsetAsync(B.wsb, 0, W3 * sizeof(double), st));
   ATRY(h, cudaMemsetAsync(B.sb, 0, 3 * (size_t)h->pcap * sizeof(double), st));
+  if (s.bonds) ATRY(h, cudaMemsetAsync(B.bb, 0, (size_t)kBondValues * h->pcap * sizeof(double), st));
   ATRY(h, cudaMemsetAsync(B.th, 0, 4 * sizeof(double), st));
   const double fw_seed = use_wall ? loss->w_wallforce * 2.0 * (fw - loss->wallforce_target) : 0.0;
   // tape of one segment
@@ -1133,6 +1357,13 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   AGET(h, tsh, double, 3 * (size_t)maxnp * seg);
   AGET(h, shr, double, 3 * (size_t)maxnp);
   AGET(h, sb_prev, double, 3 * (size_t)maxnp);
+  double *tbh = nullptr, *bhr = nullptr, *bb_prev = nullptr;
+  const size_t NB = kBondValues * (size_t)maxnp;
+  if (s.bonds) {
+    AGET(h, tbh, double, NB * seg);
+    AGET(h, bhr, double, NB);
+    AGET(h, bb_prev, double, NB);
+  }
   for (int k = nseg - 1; k >= 0; k--) {
     Checkpoint &c = cps[k];
     const int first = std::max(1, k * seg), last = std::min(nsteps, (k + 1) * seg - 1);
@@ -1144,7 +1375,8 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     copyd(h, s.T, c.T, S3);
     copyd(h, s.ws, c.ws, W3);
     copyd(h, shr, c.sh0, 3 * (size_t)c.L.np);
-    use_list(h, c.L, shr);
+    if (s.bonds) copyd(h, bhr, c.bh0, (size_t)kBondValues * c.L.np);
+    use_list(h, c.L, shr, bhr);
     for (int t = first; t <= last; t++) {
       const int q = t - first;
       ka_kick_drift<<<grid_of(n), kAB, 0, st>>>(s, nullptr);
@@ -1152,7 +1384,8 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       copyd(h, tx + S3 * q, s.x, S3);
       copyd(h, tvh + S3 * q, s.v, S3);
       copyd(h, twh + S3 * q, s.w, S3);
-      force_pass(h, tvh + S3 * q, twh + S3 * q, 1, tsh + 3 * (size_t)maxnp * q, tws + W3 * q, 1, nullptr);
+      force_pass(h, tvh + S3 * q, twh + S3 * q, 1, t, tsh + 3 * (size_t)maxnp * q, s.bonds ? tbh + NB * q : nullptr,
+                 tws + W3 * q, 1, nullptr);
       copyd(h, tF + S3 * q, s.F, S3);
       copyd(h, tT + S3 * q, s.T, S3);
     }
@@ -1164,7 +1397,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, xs, vh, wh, tws + W3 * q, 1, t == nsteps ? lw : -1,
                                            t == nsteps ? fw_seed : 0.0);
       if (s.np > 0)
-        kb_pairs<<<grid_of(s.np), kAB, 0, st>>>(s, B, xs, vh, wh, tsh + 3 * (size_t)maxnp * q, 1);
+        pairs_vjp(h, xs, vh, wh, tsh + 3 * (size_t)maxnp * q, s.bonds ? tbh + NB * q : nullptr, 1, t);
       const double *Fn = q > 0 ? tF + S3 * (q - 1) : c.F;
       const double *Tn = q > 0 ? tT + S3 * (q - 1) : c.T;
       kb_gather_kick<<<grid_of(n), kAB, 0, st>>>(s, B, Fn, Tn, 1);
@@ -1174,20 +1407,25 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     if (k > 0) {  // history adjoints back through the carry at this build
       const AList &po = cps[k - 1].L;
       ATRY(h, cudaMemsetAsync(sb_prev, 0, 3 * (size_t)std::max(1, po.np) * sizeof(double), st));
+      if (s.bonds)
+        ATRY(h, cudaMemsetAsync(bb_prev, 0, (size_t)kBondValues * std::max(1, po.np) * sizeof(double), st));
       if (c.L.np > 0) {
-        kb_uncarry<<<grid_of(c.L.np), kAB, 0, st>>>(c.L.np, c.L.carry, B.sb, sb_prev, 0);
-        kb_uncarry<<<grid_of(c.L.np), kAB, 0, st>>>(c.L.np, c.L.carry, B.sb, sb_prev, 1);
+        double *bn = s.bonds ? B.bb : nullptr, *bo = s.bonds ? bb_prev : nullptr;
+        kb_uncarry<<<grid_of(c.L.np), kAB, 0, st>>>(c.L.np, c.L.carry, B.sb, sb_prev, 0, bn, bo);
+        kb_uncarry<<<grid_of(c.L.np), kAB, 0, st>>>(c.L.np, c.L.carry, B.sb, sb_prev, 1, bn, bo);
       }
       copyd(h, B.sb, sb_prev, 3 * (size_t)po.np);
+      if (s.bonds) copyd(h, B.bb, bb_prev, (size_t)kBondValues * po.np);
     }
   }
   {  // Verlet::setup force pass: initial state, zero history, no update
     Checkpoint &c = cps[0];
     ATRY(h, cudaMemsetAsync(tws, 0, W3 * sizeof(double), st));
     ATRY(h, cudaMemsetAsync(shr, 0, 3 * (size_t)maxnp * sizeof(double), st));
-    use_list(h, c.L, shr);
+    if (s.bonds) ATRY(h, cudaMemsetAsync(bhr, 0, NB * sizeof(double), st));
+    use_list(h, c.L, shr, bhr);
     kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, c.x, c.v, c.w, tws, 0, -1, 0.0);
-    if (s.np > 0) kb_pairs<<<grid_of(s.np), kAB, 0, st>>>(s, B, c.x, c.v, c.w, shr, 0);
+    pairs_vjp(h, c.x, c.v, c.w, shr, bhr, 0, 0);
     kb_gather_kick<<<grid_of(n), kAB, 0, st>>>(s, B, nullptr, nullptr, 0);
     accumulate(h, B.pth, s.np);
     accumulate(h, B.wth, n);

@@ -1,7 +1,8 @@
 """Discrete adjoint of the sphere-DEM timestep (dem_adjoint_* in the C ABI).
 
 ``DemAdjoint`` owns one adjoint handle: an initial granular state (one atom
-type, one material, primitive planes, gravity) and a run length.  ``loss()``
+type, one material, primitive planes, gravity, optionally cohesion
+bond/nonlinear) and a run length.  ``loss()``
 runs the forward model only; ``gradient()`` also runs the backward pass and
 returns d(loss)/d(E, restitution, friction, radius_i).  ``AdjointLoss`` is a
 ``torch.autograd.Function`` over the same call, so the parameters can sit in
@@ -9,8 +10,9 @@ a torch optimisation loop (the simulation itself runs in the library's CUDA
 kernels, not in torch).
 
 The forward model is the reference's: Verlet::setup, then N Verlet steps of
-FixNVESphere + PairGran (Hertz, tangential history) + FixGravity +
-FixWallGran primitive planes, with the neighbour list rebuilt every
+FixNVESphere + PairGran (Hertz, tangential history, cohesion bond/nonlinear
+when the case has bonds) + FixGravity + FixWallGran primitive planes, with
+the neighbour list rebuilt every
 `segment` steps (neigh_modify every <segment> delay 0 check no).
 """
 import ctypes
@@ -42,6 +44,7 @@ def _bind(L):
     L.dem_adjoint_create.argtypes = [ctypes.POINTER(DemAdjointConfig), ctypes.POINTER(P)]
     L.dem_adjoint_destroy.argtypes = [P]
     L.dem_adjoint_set_state.argtypes = [P, I, P, P, P, P]
+    L.dem_adjoint_set_bonds.argtypes = [P, P, ctypes.POINTER(api.DemBondSettings)]
     L.dem_adjoint_forward.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P]
     L.dem_adjoint_gradient.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P, P, P, P, P]
     L.dem_adjoint_download.argtypes = [P, P, P, P]
@@ -77,8 +80,9 @@ class DemAdjoint:
             raise ValueError("the adjoint covers Hertz without rolling friction")
         if case.get("meshes"):
             raise ValueError("mesh walls are not covered by the adjoint")
+        bonded = case.get("cohesion_model", 0) == 1
         if float(case.get("cdf", 1.0)) != 1.0:
-            raise ValueError("the adjoint needs contact distance factor 1")
+            raise ValueError("the adjoint takes the contact distance factor of its bonds, else 1")
         self.L = _bind(api.load())
         mat = case["material"]
         cfg = DemAdjointConfig()
@@ -106,6 +110,14 @@ class DemAdjoint:
         if rc != 0:
             raise api.DemError("dem_adjoint_create: %s" % api.STATUS.get(rc, rc))
         self.h = h
+        if bonded:
+            b = case["bond"]
+            vals = np.ascontiguousarray(np.asarray(b["tables"], dtype=np.float64)[:, 1, 1])
+            st = api.DemBondSettings()
+            st.tsCreate = float(b["settings"]["tsCreate"])
+            for k in api.BOND_FLAGS:
+                setattr(st, k, int(b["settings"][k]))
+            self._call("dem_adjoint_set_bonds", self.h, api._p(vals), ctypes.byref(st))
         a = case["atoms"]
         self.n = len(a["radius"])
         self.radius = _f64(a["radius"]).copy()
