@@ -411,13 +411,77 @@ def run_ensemble(args):
     print(json.dumps(line))
 
 
+def adjoint_case(seed=2024, n=20000):
+    """configs[4] adjoint: n spheres as the settling columns (r U[0.9, 1.1]
+    mm, jittered 2.2 mm lattice above a floor, 0.05 x 0.05 x 0.3 m box
+    periodic in x/y), one parameter set (E 1e7, e 0.6, mu 0.5), dt 1e-6"""
+    from gb300dem import workloads
+    spacing = 2.2e-3
+    nx = ny = int(0.05 / spacing)
+    nz = (n + nx * ny - 1) // (nx * ny)
+    c = workloads.lattice_case(seed=seed, nx=nx, ny=ny, nz=nz, spacing=spacing, radius=(0.9e-3, 1.1e-3),
+                               density=2500.0, z0=1.2 * 1.1e-3, jitter=0.05 * spacing, E=(1e7,), nu=(0.3,),
+                               rest=((0.6,),), frict=((0.5,),), dt=1e-6, skin=5e-4, zhi=0.3,
+                               pad=(0.05 - nx * spacing, 0.05 - ny * spacing))
+    keep = np.arange(len(c["atoms"]["tag"])) < n
+    c["atoms"] = {k: v[keep] for k, v in c["atoms"].items()}
+    return c
+
+
+def run_adjoint(args):
+    """Cost of one adjoint gradient (forward with checkpoints + backward with
+    replay) of the kinetic energy after `steps` steps, against the plain
+    path's forward run of the same system and steps."""
+    from gb300dem import api
+    from gb300dem.adjoint import DemAdjoint, make_loss
+    n = max(1000, int(round(20000 * args.scale)))
+    steps = args.steps
+    seg = max(1, int(round(steps ** 0.5)))
+    case = adjoint_case(n=n)
+    g = api.DemSystem(case)
+    g.setup()
+    g.step(args.warmup)
+    g.step(steps)
+    plain_ms = g.stats()["last_step_ms"]
+    g.close()
+    eng = DemAdjoint(case)
+    spec = make_loss(w_ke=1.0)
+    modes = {}
+    for mode, name in ((0, "checkpoint_replay"), (1, "recorded")):
+        eng.set_tape(mode)
+        for _ in range(2):  # the first run sizes the arena
+            val, grad = eng.gradient(1e7, 0.6, 0.5, nsteps=steps, segment=seg, loss=spec)
+        tm = eng.times()
+        modes[name] = {"forward_ms": tm["forward_ms"], "backward_ms": tm["backward_ms"],
+                       "total_over_plain_forward": (tm["forward_ms"] + tm["backward_ms"]) / plain_ms,
+                       "backward_over_forward": tm["backward_ms"] / tm["forward_ms"]}
+    eng.close()
+    t = {"forward_ms": modes["recorded"]["forward_ms"], "backward_ms": modes["recorded"]["backward_ms"],
+         "segments": tm["segments"], "max_pairs": tm["max_pairs"]}
+    total = t["forward_ms"] + t["backward_ms"]
+    line = {"metric": "adjoint gradient time / plain forward time", "value": total / plain_ms, "unit": "x",
+            "n_gpus": 1, "steps": steps, "warmup": args.warmup, "higher_is_better": False,
+            "dtype": "f64", "data": "synthetic (seeded)", "impl": "gb300",
+            "config": {"workload": "adjoint%dk" % (n // 1000), "atoms": n, "segment": seg,
+                       "description": "configs[4]: settling-column spheres, one parameter set, "
+                                      "kinetic-energy loss, gradients w.r.t. E, e, mu and every radius"},
+            "plain_forward_ms": plain_ms, "adjoint_forward_ms": t["forward_ms"],
+            "adjoint_backward_ms": t["backward_ms"], "backward_over_forward": t["backward_ms"] / t["forward_ms"],
+            "segments": t["segments"], "max_pairs": t["max_pairs"], "loss": val, "tape_modes": modes,
+            "note": "value: the record taken in the forward pass (tape mode 1); checkpoint_replay: the "
+                    "sqrt(N) checkpoints with the replay of each segment (tape mode 0)",
+            "grad": {"E": grad["E"], "restitution": grad["restitution"], "friction": grad["friction"]}}
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="hopper1m", choices=["hopper1m", "column1m", "ensemble256"])
+    ap.add_argument("--workload", default="hopper1m",
+                    choices=["hopper1m", "column1m", "ensemble256", "adjoint20k"])
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0,
@@ -429,6 +493,8 @@ def main():
         run_reference(args)
     elif args.workload == "ensemble256":
         run_ensemble(args)
+    elif args.workload == "adjoint20k":
+        run_adjoint(args)
     else:
         run_gb300(args)
 

@@ -407,6 +407,19 @@ int dem_adjoint_download(dem_adjoint *h, double *x, double *v, double *omega);
 /* device time of the last run's forward and backward passes, its segment
  * count and largest list */
 int dem_adjoint_times(dem_adjoint *h, double *forward_ms, double *backward_ms, int *segments, int *max_pairs);
+/* where the backward pass takes each step's record (positions, half-step
+ * velocities, history and forces the step's force evaluation saw):
+ *   mode 0: replayed from the segment's checkpoint (memory: one checkpoint
+ *           per segment plus one segment of record, O(sqrt(N)) states);
+ *   mode 1: recorded during the forward pass, no replay (memory: every step);
+ *   mode 2 (default): mode 1 when the whole record fits max_bytes (0: half of
+ *           the device memory free at the run's start), else mode 0.
+ * Both give the same gradients bit for bit; mode 1 saves the replay, about
+ * one forward pass of time. */
+int dem_adjoint_set_tape(dem_adjoint *h, int mode, double max_bytes);
+/* whether the last run recorded its steps in the forward pass (1) or replayed
+ * them (0) */
+int dem_adjoint_tape_recorded(dem_adjoint *h, int *recorded);
 const char *dem_adjoint_last_error(dem_adjoint *h);
 
 #ifdef __cplusplus

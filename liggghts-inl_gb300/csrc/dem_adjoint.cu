@@ -69,7 +69,8 @@ using namespace gb300;
 
 namespace {
 
-constexpr int kAB = 256;
+// threads per block: small blocks spread a 10^4-atom system over every SM
+constexpr int kAB = 128;
 constexpr int kMaxGrid = 152 * 16;
 
 struct AList {
@@ -100,6 +101,13 @@ struct ADev {
   BondPar bp;
   long long ts_create;
   double *x, *v, *w, *F, *T, *r, *m, *ws;  // ws [(w*n + i)*3 + k]
+  // FP32 mirror of the positions and radii (x, y, z, r) for the candidate
+  // tests; fm: the distance margin that covers its rounding
+  float4 *xf;
+  float fm, prdf[3];
+  // per-atom kick constants of the run: ka = dtf/m, kb = dtfrot/(r^2 m) and
+  // the factors of their derivatives ka/m, kb/m, 2 kb/r
+  double *ka, *kb, *kam, *kbm, *kbr;
   // list in use
   int np;
   const int *pi, *pj, *row, *rev_start, *rev;
@@ -132,9 +140,66 @@ __device__ __forceinline__ void a_image(const ADev &s, int code, double xj[3]) {
     if (sv[d]) xj[d] = __dadd_rn(xj[d], sv[d] * s.prd[d]);
 }
 
+// FP32 candidate test of entry p against the contact distance (ri + rj) cdf:
+// false only when the exact FP64 distance is beyond it (fm bounds the
+// rounding of the FP32 mirror and of this arithmetic)
+__device__ __forceinline__ bool pair_candidate(const ADev &s, const float4 *xf, int p) {
+  const float4 a = xf[s.pi[p]], b = xf[s.pj[p]];
+  float bx = b.x, by = b.y, bz = b.z;
+  const int code = s.sh[p];
+  if (code != kNoShift) {
+    bx += (float)(code % 3 - 1) * s.prdf[0];
+    by += (float)((code / 3) % 3 - 1) * s.prdf[1];
+    bz += (float)(code / 9 - 1) * s.prdf[2];
+  }
+  const float dx = a.x - bx, dy = a.y - by, dz = a.z - bz;
+  const float R = (a.w + b.w) * (float)s.cdf + s.fm;
+  return dx * dx + dy * dy + dz * dz <= R * R;
+}
+
 #define AGRID(i, n) for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
+// block-stride loop with the same trip count for every thread of a block (the
+// queue kernels synchronise inside it); blockDim.x == kAB
+#define ABLOCKS(base, n) for (int base = blockIdx.x * kAB; base < (n); base += gridDim.x * kAB)
+
+// Dense work queue of one block.  The FP64 pipe issues per warp, so a warp in
+// which a few lanes run the contact law costs as much as a full one; the
+// threads whose `want` is set place their item in consecutive slots of q (in
+// thread order) and the first `count` threads then run the expensive part on
+// dense warps.  Contains two barriers; the caller synchronises again after
+// consuming q.
+__device__ __forceinline__ int block_queue(bool want, int item, int *q, int *wcnt) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned m = __ballot_sync(0xffffffffu, want);
+  if (lane == 0) wcnt[warp] = __popc(m);
+  __syncthreads();
+  int off = 0, tot = 0;
+#pragma unroll
+  for (int k = 0; k < kAB / 32; k++) {
+    const int v = wcnt[k];
+    off += (k < warp) ? v : 0;
+    tot += v;
+  }
+  if (want) q[off + __popc(m & ((1u << lane) - 1u))] = item;
+  __syncthreads();
+  return tot;
+}
 
 // ---------------------------------------------------------------- list build
+// per-atom kick constants of FixNVESphere (src/fix_nve_sphere.cpp:134-244)
+// for the run's radii and masses
+__global__ void ka_consts(ADev s) {
+  AGRID(i, s.n) {
+    const double m = s.m[i], r = s.r[i];
+    const double a = s.dtf / m, b = s.dtfrot / (r * r * m);
+    s.ka[i] = a;
+    s.kb[i] = b;
+    s.kam[i] = a / m;
+    s.kbm[i] = b / m;
+    s.kbr[i] = 2.0 * b / r;
+  }
+}
+
 // Domain::pbc (src/domain.cpp:550-650) for periodic dimensions
 __global__ void ka_wrap(ADev s) {
   AGRID(i, s.n) {
@@ -148,6 +213,7 @@ __global__ void ka_wrap(ADev s) {
       }
       s.x[3 * i + d] = x;
     }
+    s.xf[i] = make_float4((float)s.x[3 * i], (float)s.x[3 * i + 1], (float)s.x[3 * i + 2], (float)s.r[i]);
   }
 }
 __global__ void ka_cell(ADev s) {
@@ -395,131 +461,197 @@ __device__ __forceinline__ bool wall_in(const ADev &s, const double *x, int w, i
 // BONDS: the system has cohesion bond/nonlinear (a separate instance keeps
 // the registers of the plain contact path low)
 template <bool BONDS>
-__global__ void ka_pair_force(ADev s, const double *vh, const double *wh, int upd, long long ntimestep,
-                              double *tape_sh, double *tape_bh) {
-  AGRID(p, s.np) {
-    VjpIn a = pair_in(s, s.x, p, vh, wh, s.shear);
-    a.upd = upd != 0;
-    if (tape_sh)
-      for (int k = 0; k < 3; k++) tape_sh[3 * p + k] = a.sh[k];
-    double *bh = BONDS ? s.bh + (size_t)kBondValues * p : nullptr;
-    if (BONDS && tape_bh)
-      for (int k = 0; k < kBondValues; k++) tape_bh[(size_t)kBondValues * p + k] = bh[k];
-    const bool touch = pair_touch(a), band = pair_band(s, a);
-    if (!touch && band) {  // TangentialModel<TANGENTIAL_HISTORY>::surfacesClose
-      for (int k = 0; k < 3; k++) s.shear[3 * p + k] = 0.0;
-      s.flag[p] &= ~kContactTangential;
+__global__ void __launch_bounds__(kAB) ka_pair_force(ADev s, const double *vh, const double *wh, int upd,
+                                                     long long ntimestep, double *tape_sh, double *tape_bh) {
+  __shared__ int q[kAB];
+  __shared__ int wcnt[kAB / 32];
+  ABLOCKS(base, s.np) {
+    const int p0 = base + threadIdx.x;
+    bool work = false;
+    if (p0 < s.np) {  // tape and the FP32 candidate test; the rest runs queued
+      if (tape_sh)
+        for (int k = 0; k < 3; k++) tape_sh[3 * p0 + k] = s.shear[3 * p0 + k];
+      if (BONDS && tape_bh)
+        for (int k = 0; k < kBondValues; k++)
+          tape_bh[(size_t)kBondValues * p0 + k] = s.bh[(size_t)kBondValues * p0 + k];
+      work = pair_candidate(s, s.xf, p0);
+      if (!work) s.active[p0] = 0;  // beyond the contact distance: nothing changes
     }
-    int st = kBondNone;
-    double bF[3] = {0., 0., 0.}, bTi[3] = {0., 0., 0.}, bTj[3] = {0., 0., 0.};
-    if (BONDS && (touch || band)) {
-      const BondArgs b = bond_in(s, a, s.x, s.pi[p], ntimestep);
-      double hin[kBondValues], hout[kBondValues];
-      for (int k = 0; k < kBondValues; k++) hin[k] = bh[k];
-      BondTape T;
-      st = bond_fwd(b, s.bp, hin, hout, bF, bTi, bTj, T);
-      for (int k = 0; k < kBondValues; k++) bh[k] = hout[k];
-      if (st == kBondActive) s.flag[p] |= kContactCohesion;
-      if (st == kBondBroken) s.flag[p] &= ~kContactCohesion;
-    }
-    const bool bonded = st == kBondActive;
-    if (touch) {
-      a.bonded = bonded;
-      LawState S;
-      double F[3], Ti[3], Tj[3], s3[3];
-      law_forward(a, S, F, Ti, Tj, s3);
-      for (int k = 0; k < 3; k++) {
-        s.pF[3 * p + k] = F[k] + bF[k];
-        s.pTi[3 * p + k] = Ti[k] + bTi[k];
-        s.pTj[3 * p + k] = Tj[k] + bTj[k];
-        if (upd) s.shear[3 * p + k] = s3[k];
+    const int tot = block_queue(work, p0, q, wcnt);
+    if (threadIdx.x < tot) {
+      const int p = q[threadIdx.x];
+      VjpIn a = pair_in(s, s.x, p, vh, wh, s.shear);
+      a.upd = upd != 0;
+      const bool touch = pair_touch(a), band = pair_band(s, a);
+      if (!touch && band) {  // TangentialModel<TANGENTIAL_HISTORY>::surfacesClose
+        for (int k = 0; k < 3; k++) s.shear[3 * p + k] = 0.0;
+        s.flag[p] &= ~kContactTangential;
       }
-      s.flag[p] |= kContactNormal | kContactTangential;
-    } else if (bonded) {
-      for (int k = 0; k < 3; k++) {
-        s.pF[3 * p + k] = bF[k];
-        s.pTi[3 * p + k] = bTi[k];
-        s.pTj[3 * p + k] = bTj[k];
+      int st = kBondNone;
+      double bF[3] = {0., 0., 0.}, bTi[3] = {0., 0., 0.}, bTj[3] = {0., 0., 0.};
+      if (BONDS && (touch || band)) {
+        double *bh = s.bh + (size_t)kBondValues * p;
+        const BondArgs b = bond_in(s, a, s.x, s.pi[p], ntimestep);
+        double hin[kBondValues], hout[kBondValues];
+        for (int k = 0; k < kBondValues; k++) hin[k] = bh[k];
+        BondTape T;
+        st = bond_fwd(b, s.bp, hin, hout, bF, bTi, bTj, T);
+        for (int k = 0; k < kBondValues; k++) bh[k] = hout[k];
+        if (st == kBondActive) s.flag[p] |= kContactCohesion;
+        if (st == kBondBroken) s.flag[p] &= ~kContactCohesion;
       }
+      const bool bonded = st == kBondActive;
+      if (touch) {
+        a.bonded = bonded;
+        LawState S;
+        double F[3], Ti[3], Tj[3], s3[3];
+        law_forward(a, S, F, Ti, Tj, s3);
+        for (int k = 0; k < 3; k++) {
+          s.pF[3 * p + k] = F[k] + bF[k];
+          s.pTi[3 * p + k] = Ti[k] + bTi[k];
+          s.pTj[3 * p + k] = Tj[k] + bTj[k];
+          if (upd) s.shear[3 * p + k] = s3[k];
+        }
+        s.flag[p] |= kContactNormal | kContactTangential;
+      } else if (bonded) {
+        for (int k = 0; k < 3; k++) {
+          s.pF[3 * p + k] = bF[k];
+          s.pTi[3 * p + k] = bTi[k];
+          s.pTj[3 * p + k] = bTj[k];
+        }
+      }
+      s.active[p] = (touch || bonded) ? 1 : 0;
     }
-    s.active[p] = (touch || bonded) ? 1 : 0;
+    __syncthreads();
   }
 }
 
 // total force/torque per atom: own row, reverse list (local entries), gravity,
 // planes; with final_kick the second half-kick v = vh + a F, w = wh + b T.
-// tape_ws receives the wall history before the update, wallF the wall forces.
-__global__ void ka_gather(ADev s, const double *vh, const double *wh, int upd, int final_kick,
-                          double *tape_ws, double *wallF) {
-  AGRID(i, s.n) {
+// tape_ws receives the wall history before the update, wallF the wall forces,
+// tape_F/tape_T (if set) a copy of the forces and torques.
+__global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const double *wh, int upd,
+                                                 int final_kick, double *tape_ws, double *wallF, double *tape_F,
+                                                 double *tape_T) {
+  __shared__ int q[kAB];
+  __shared__ int wcnt[kAB / 32];
+  __shared__ double sF[3][kAB], sT[3][kAB];
+  ABLOCKS(base, s.n) {
+    const int i = base + threadIdx.x;
+    const bool valid = i < s.n;
     double f[3] = {0., 0., 0.}, t[3] = {0., 0., 0.};
-    for (int p = s.row[i]; p < s.row[i + 1]; p++)
-      if (s.active[p])
+    if (valid) {
+      for (int p = s.row[i]; p < s.row[i + 1]; p++)
+        if (s.active[p])
+          for (int k = 0; k < 3; k++) {
+            f[k] += s.pF[3 * p + k];
+            t[k] += s.pTi[3 * p + k];
+          }
+      for (int qq = s.rev_start[i]; qq < s.rev_start[i + 1]; qq++) {
+        const int p = s.rev[qq];
+        if (!s.active[p] || s.sh[p] != kNoShift) continue;
         for (int k = 0; k < 3; k++) {
-          f[k] += s.pF[3 * p + k];
-          t[k] += s.pTi[3 * p + k];
+          f[k] -= s.pF[3 * p + k];
+          t[k] += s.pTj[3 * p + k];
         }
-    for (int q = s.rev_start[i]; q < s.rev_start[i + 1]; q++) {
-      const int p = s.rev[q];
-      if (!s.active[p] || s.sh[p] != kNoShift) continue;
-      for (int k = 0; k < 3; k++) {
-        f[k] -= s.pF[3 * p + k];
-        t[k] += s.pTj[3 * p + k];
       }
+      if (s.gravity_on)
+        for (int k = 0; k < 3; k++) f[k] += s.m[i] * s.g[k];
     }
-    if (s.gravity_on)
-      for (int k = 0; k < 3; k++) f[k] += s.m[i] * s.g[k];
+    // planes in order; the atoms touching plane w run the law on dense warps
     for (int w = 0; w < s.nplanes; w++) {
-      double *hw = s.ws + ((size_t)w * s.n + i) * 3;
-      if (tape_ws)
-        for (int k = 0; k < 3; k++) tape_ws[((size_t)w * s.n + i) * 3 + k] = hw[k];
-      VjpIn a;
-      if (!wall_in(s, s.x, w, i, vh, wh, s.ws, a)) {
-        for (int k = 0; k < 3; k++) hw[k] = 0.0;  // surfacesClose
-        if (wallF)
-          for (int k = 0; k < 3; k++) wallF[((size_t)w * s.n + i) * 3 + k] = 0.0;
-        continue;
+      bool touch = false;
+      if (valid) {
+        double *hw = s.ws + ((size_t)w * s.n + i) * 3;
+        if (tape_ws)
+          for (int k = 0; k < 3; k++) tape_ws[((size_t)w * s.n + i) * 3 + k] = hw[k];
+        VjpIn a;
+        touch = wall_in(s, s.x, w, i, vh, wh, s.ws, a);
+        if (!touch) {
+          for (int k = 0; k < 3; k++) hw[k] = 0.0;  // surfacesClose
+          if (wallF)
+            for (int k = 0; k < 3; k++) wallF[((size_t)w * s.n + i) * 3 + k] = 0.0;
+        }
       }
-      a.upd = upd != 0;
-      LawState S;
-      double F[3], Ti[3], Tj[3], s3[3];
-      law_forward(a, S, F, Ti, Tj, s3);
-      for (int k = 0; k < 3; k++) {
-        f[k] += F[k];
-        t[k] += Ti[k];
-        if (upd) hw[k] = s3[k];
-        if (wallF) wallF[((size_t)w * s.n + i) * 3 + k] = F[k];
+      const int tot = block_queue(touch, threadIdx.x, q, wcnt);
+      if (threadIdx.x < tot) {
+        const int li = q[threadIdx.x], ii = base + li;
+        VjpIn a;
+        wall_in(s, s.x, w, ii, vh, wh, s.ws, a);
+        a.upd = upd != 0;
+        LawState S;
+        double F[3], Ti[3], Tj[3], s3[3];
+        law_forward(a, S, F, Ti, Tj, s3);
+        double *hw = s.ws + ((size_t)w * s.n + ii) * 3;
+        for (int k = 0; k < 3; k++) {
+          sF[k][li] = F[k];
+          sT[k][li] = Ti[k];
+          if (upd) hw[k] = s3[k];
+          if (wallF) wallF[((size_t)w * s.n + ii) * 3 + k] = F[k];
+        }
       }
+      __syncthreads();
+      if (touch)
+        for (int k = 0; k < 3; k++) {
+          f[k] += sF[k][threadIdx.x];
+          t[k] += sT[k][threadIdx.x];
+        }
+      __syncthreads();
     }
-    const double a = s.dtf / s.m[i];
-    const double b = s.dtfrot / (s.r[i] * s.r[i] * s.m[i]);
-    for (int k = 0; k < 3; k++) {
-      s.F[3 * i + k] = f[k];
-      s.T[3 * i + k] = t[k];
-      if (final_kick) {
-        s.v[3 * i + k] = vh[3 * i + k] + a * f[k];
-        s.w[3 * i + k] = wh[3 * i + k] + b * t[k];
+    if (valid) {
+      const double a = s.ka[i], b = s.kb[i];
+      for (int k = 0; k < 3; k++) {
+        s.F[3 * i + k] = f[k];
+        s.T[3 * i + k] = t[k];
+        if (tape_F) {
+          tape_F[3 * i + k] = f[k];
+          tape_T[3 * i + k] = t[k];
+        }
+        if (final_kick) {
+          s.v[3 * i + k] = vh[3 * i + k] + a * f[k];
+          s.w[3 * i + k] = wh[3 * i + k] + b * t[k];
+        }
       }
     }
   }
 }
 
 // first half-kick and drift (v, w then hold vh, wh); xref: positions at the
-// list build to check the displacement against, or null
-__global__ void ka_kick_drift(ADev s, const double *xref) {
+// list build to check the displacement against, or null; wrap: the periodic
+// wrap of a rebuild step (Domain::pbc, as ka_wrap); tx/tv/tw (if set)
+// receive a copy of the new x, vh, wh
+__global__ void ka_kick_drift(ADev s, const double *xref, int wrap, double *tx, double *tv, double *tw,
+                              float4 *txf) {
   AGRID(i, s.n) {
-    const double a = s.dtf / s.m[i];
-    const double b = s.dtfrot / (s.r[i] * s.r[i] * s.m[i]);
+    const double a = s.ka[i], b = s.kb[i];
     double dsq = 0.0;
     for (int k = 0; k < 3; k++) {
-      s.v[3 * i + k] += a * s.F[3 * i + k];
-      s.w[3 * i + k] += b * s.T[3 * i + k];
-      s.x[3 * i + k] += s.dt * s.v[3 * i + k];
+      const double v = s.v[3 * i + k] + a * s.F[3 * i + k];
+      const double w = s.w[3 * i + k] + b * s.T[3 * i + k];
+      double x = s.x[3 * i + k] + s.dt * v;
       if (xref) {
-        const double e = s.x[3 * i + k] - xref[3 * i + k];
+        const double e = x - xref[3 * i + k];
         dsq += e * e;
       }
+      if (wrap && s.per[k]) {
+        if (x < s.lo[k]) x += s.prd[k];
+        if (x >= s.hi[k]) {
+          x -= s.prd[k];
+          if (x < s.lo[k]) x = s.lo[k];
+        }
+      }
+      s.v[3 * i + k] = v;
+      s.w[3 * i + k] = w;
+      s.x[3 * i + k] = x;
+      if (tx) {
+        tx[3 * i + k] = x;
+        tv[3 * i + k] = v;
+        tw[3 * i + k] = w;
+      }
     }
+    const float4 f4 = make_float4((float)s.x[3 * i], (float)s.x[3 * i + 1], (float)s.x[3 * i + 2], (float)s.r[i]);
+    s.xf[i] = f4;
+    if (txf) txf[i] = f4;
     if (dsq > 0.25 * s.skin * s.skin) s.err[0] = 1;
   }
 }
@@ -534,63 +666,75 @@ struct ABar {
   double *th;   // [4] accumulated parameter adjoints
 };
 
-// second half-kick: v' = vh + a F', w' = wh + b T'
-__global__ void kb_final(ADev s, ABar B, const double *Fn1, const double *Tn1) {
-  AGRID(i, s.n) {
-    const double m = s.m[i], r = s.r[i];
-    const double a = s.dtf / m, b = s.dtfrot / (r * r * m);
-    double fv = 0.0, tw = 0.0;
-    for (int k = 0; k < 3; k++) {
-      B.Fb[3 * i + k] += a * B.vb[3 * i + k];
-      B.Tb[3 * i + k] += b * B.wb[3 * i + k];
-      fv += Fn1[3 * i + k] * B.vb[3 * i + k];
-      tw += Tn1[3 * i + k] * B.wb[3 * i + k];
-    }
-    B.mb[i] += -a / m * fv - b / m * tw;
-    B.rb[i] += -2.0 * b / r * tw;
-  }
-}
-
 // gravity and walls of one force evaluation at positions x; vh/wh the
 // velocities the forces saw, ws_before the wall history before it; seed adds
-// d(loss)/d(normal wall force) on plane seed_w
-__global__ void kb_walls(ADev s, ABar B, const double *x, const double *vh, const double *wh,
-                         const double *ws_before, int upd, int seed_w, double seed) {
-  AGRID(i, s.n) {
-    double th[4] = {0., 0., 0., 0.};
-    if (s.gravity_on)
-      B.mb[i] += s.g[0] * B.Fb[3 * i] + s.g[1] * B.Fb[3 * i + 1] + s.g[2] * B.Fb[3 * i + 2];
-    for (int w = 0; w < s.nplanes; w++) {
-      double *wsb = B.wsb + ((size_t)w * s.n + i) * 3;
-      VjpIn a;
-      if (!wall_in(s, x, w, i, vh, wh, ws_before, a)) {
-        if (upd)
-          for (int k = 0; k < 3; k++) wsb[k] = 0.0;  // history zeroed: no dependence
-        continue;
+// d(loss)/d(normal wall force) on plane seed_w.  Fn1/Tn1 (if set): the
+// forces of this evaluation, whose second half-kick v' = vh + a F',
+// w' = wh + b T' is reversed first.  The wall parameter adjoints add to
+// B.wth.
+__global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x, const double *vh,
+                                                const double *wh, const double *ws_before, int upd, int seed_w,
+                                                double seed, const double *Fn1, const double *Tn1) {
+  __shared__ int q[kAB];
+  __shared__ int wcnt[kAB / 32];
+  ABLOCKS(base, s.n) {
+    const int i = base + threadIdx.x;
+    const bool valid = i < s.n;
+    if (valid) {
+      if (Fn1) {
+        const double a = s.ka[i], b = s.kb[i];
+        double fv = 0.0, tw = 0.0;
+        for (int k = 0; k < 3; k++) {
+          B.Fb[3 * i + k] += a * B.vb[3 * i + k];
+          B.Tb[3 * i + k] += b * B.wb[3 * i + k];
+          fv += Fn1[3 * i + k] * B.vb[3 * i + k];
+          tw += Tn1[3 * i + k] * B.wb[3 * i + k];
+        }
+        B.mb[i] += -s.kam[i] * fv - s.kbm[i] * tw;
+        B.rb[i] += -s.kbr[i] * tw;
       }
-      a.upd = upd != 0;
-      VjpBar bb;
-      for (int k = 0; k < 3; k++) {
-        bb.F[k] = B.Fb[3 * i + k] + (w == seed_w && k == s.pax[w] ? seed : 0.0);
-        bb.Ti[k] = B.Tb[3 * i + k];
-        bb.Tj[k] = 0.0;
-        bb.s3[k] = upd ? wsb[k] : 0.0;
-      }
-      law_vjp(a, bb);
-      for (int k = 0; k < 3; k++) {
-        if (k == s.pax[w]) B.xb[3 * i + k] += bb.d[k];  // off-axis components of d are constants
-        B.vb[3 * i + k] += bb.vr[k];
-        B.wb[3 * i + k] += bb.wi[k];
-        wsb[k] = bb.sh[k] + (upd ? 0.0 : wsb[k]);
-      }
-      B.rb[i] += bb.ri;
-      B.mb[i] += bb.mi;
-      th[0] += bb.Y;
-      th[1] += bb.G;
-      th[2] += bb.beta;
-      th[3] += bb.mu;
+      if (s.gravity_on)
+        B.mb[i] += s.g[0] * B.Fb[3 * i] + s.g[1] * B.Fb[3 * i + 1] + s.g[2] * B.Fb[3 * i + 2];
     }
-    for (int k = 0; k < 4; k++) B.wth[4 * i + k] = th[k];
+    // planes in order; the atoms touching plane w run the VJP on dense warps
+    for (int w = 0; w < s.nplanes; w++) {
+      bool touch = false;
+      if (valid) {
+        VjpIn a;
+        touch = wall_in(s, x, w, i, vh, wh, ws_before, a);
+        if (!touch && upd)
+          for (int k = 0; k < 3; k++) B.wsb[((size_t)w * s.n + i) * 3 + k] = 0.0;  // history zeroed
+      }
+      const int tot = block_queue(touch, threadIdx.x, q, wcnt);
+      if (threadIdx.x < tot) {
+        const int ii = base + q[threadIdx.x];
+        double *wsb = B.wsb + ((size_t)w * s.n + ii) * 3;
+        VjpIn a;
+        wall_in(s, x, w, ii, vh, wh, ws_before, a);
+        a.upd = upd != 0;
+        VjpBar bb;
+        for (int k = 0; k < 3; k++) {
+          bb.F[k] = B.Fb[3 * ii + k] + (w == seed_w && k == s.pax[w] ? seed : 0.0);
+          bb.Ti[k] = B.Tb[3 * ii + k];
+          bb.Tj[k] = 0.0;
+          bb.s3[k] = upd ? wsb[k] : 0.0;
+        }
+        law_vjp(a, bb);
+        for (int k = 0; k < 3; k++) {
+          if (k == s.pax[w]) B.xb[3 * ii + k] += bb.d[k];  // off-axis components of d are constants
+          B.vb[3 * ii + k] += bb.vr[k];
+          B.wb[3 * ii + k] += bb.wi[k];
+          wsb[k] = bb.sh[k] + (upd ? 0.0 : wsb[k]);
+        }
+        B.rb[ii] += bb.ri;
+        B.mb[ii] += bb.mi;
+        B.wth[4 * ii + 0] += bb.Y;
+        B.wth[4 * ii + 1] += bb.G;
+        B.wth[4 * ii + 2] += bb.beta;
+        B.wth[4 * ii + 3] += bb.mu;
+      }
+      __syncthreads();
+    }
   }
 }
 
@@ -599,82 +743,110 @@ __global__ void kb_walls(ADev s, ABar B, const double *x, const double *vh, cons
 // adjoints of each entry go to the per-entry arrays, the history adjoints
 // B.sb/B.bb are replaced by those of the history before the evaluation
 template <bool BONDS>
-__global__ void kb_pairs(ADev s, ABar B, const double *x, const double *vh, const double *wh,
-                         const double *sh_before, const double *bh_before, int upd, long long ntimestep) {
-  AGRID(p, s.np) {
-    VjpIn a = pair_in(s, x, p, vh, wh, sh_before);
-    a.upd = upd != 0;
-    const int i = s.pi[p], j = s.pj[p];
-    const bool local = s.sh[p] == kNoShift;
-    const bool touch = pair_touch(a), band = pair_band(s, a);
-    double Fb[3], Tib[3], Tjb[3];
-    for (int k = 0; k < 3; k++) {
-      Fb[k] = B.Fb[3 * i + k] - (local ? B.Fb[3 * j + k] : 0.0);
-      Tib[k] = B.Tb[3 * i + k];
-      Tjb[k] = local ? B.Tb[3 * j + k] : 0.0;
+__global__ void __launch_bounds__(kAB) kb_pairs(ADev s, ABar B, const double *x, const float4 *xf,
+                                                const double *vh, const double *wh, const double *sh_before,
+                                                const double *bh_before, int upd, long long ntimestep) {
+  __shared__ int q[kAB];
+  __shared__ int wcnt[kAB / 32];
+  ABLOCKS(base, s.np) {
+    const int p0 = base + threadIdx.x;
+    bool work = false;
+    if (p0 < s.np) {  // entries without a law evaluation: no input adjoints
+      bool band = false;
+      if (xf) {  // FP32 candidate test (beyond it: not touching, not in the band)
+        work = pair_candidate(s, xf, p0);
+      } else {
+        const VjpIn a = pair_in(s, x, p0, vh, wh, sh_before);
+        const bool touch = pair_touch(a);
+        band = pair_band(s, a);
+        work = touch || (BONDS && band);
+      }
+      if (!work) {
+        for (int k = 0; k < 3; k++) {
+          B.pd[3 * p0 + k] = B.pv[3 * p0 + k] = B.pwi[3 * p0 + k] = B.pwj[3 * p0 + k] = 0.0;
+          if (band) B.sb[3 * p0 + k] = 0.0;  // history cleared: no dependence
+        }  // else: history unchanged, its adjoint passes through
+        B.pri[p0] = B.prj[p0] = B.pmi[p0] = B.pmj[p0] = 0.0;
+      }
     }
-    double d[3] = {0., 0., 0.}, vr[3] = {0., 0., 0.}, wi[3] = {0., 0., 0.}, wj[3] = {0., 0., 0.};
-    double ri = 0.0, rj = 0.0, mi = 0.0, mj = 0.0, th[4] = {0., 0., 0., 0.};
-    int st = kBondNone;
-    if (BONDS && (touch || band)) {
-      const BondArgs b = bond_in(s, a, x, i, ntimestep);
-      double hin[kBondValues], houtb[kBondValues], hinb[kBondValues];
-      double *bb = B.bb + (size_t)kBondValues * p;
-      for (int k = 0; k < kBondValues; k++) {
-        hin[k] = bh_before[(size_t)kBondValues * p + k];
-        houtb[k] = bb[k];
-      }
-      BondArgsBar ab;
-      st = bond_vjp(b, s.bp, hin, Fb, Tib, Tjb, houtb, ab, hinb);
-      for (int k = 0; k < kBondValues; k++) bb[k] = hinb[k];
+    const int tot = block_queue(work, p0, q, wcnt);
+    if (threadIdx.x < tot) {
+      const int p = q[threadIdx.x];
+      VjpIn a = pair_in(s, x, p, vh, wh, sh_before);
+      a.upd = upd != 0;
+      const int i = s.pi[p], j = s.pj[p];
+      const bool local = s.sh[p] == kNoShift;
+      const bool touch = pair_touch(a), band = pair_band(s, a);
+      double Fb[3], Tib[3], Tjb[3];
       for (int k = 0; k < 3; k++) {
-        d[k] += ab.d[k];
-        vr[k] += ab.vr[k];
-        wi[k] += ab.wi[k];
-        wj[k] += ab.wj[k];
+        Fb[k] = B.Fb[3 * i + k] - (local ? B.Fb[3 * j + k] : 0.0);
+        Tib[k] = B.Tb[3 * i + k];
+        Tjb[k] = local ? B.Tb[3 * j + k] : 0.0;
       }
-      ri += ab.ri;
-      rj += ab.rj;
+      double d[3] = {0., 0., 0.}, vr[3] = {0., 0., 0.}, wi[3] = {0., 0., 0.}, wj[3] = {0., 0., 0.};
+      double ri = 0.0, rj = 0.0, mi = 0.0, mj = 0.0, th[4] = {0., 0., 0., 0.};
+      int st = kBondNone;
+      if (BONDS && (touch || band)) {
+        const BondArgs b = bond_in(s, a, x, i, ntimestep);
+        double hin[kBondValues], houtb[kBondValues], hinb[kBondValues];
+        double *bb = B.bb + (size_t)kBondValues * p;
+        for (int k = 0; k < kBondValues; k++) {
+          hin[k] = bh_before[(size_t)kBondValues * p + k];
+          houtb[k] = bb[k];
+        }
+        BondArgsBar ab;
+        st = bond_vjp(b, s.bp, hin, Fb, Tib, Tjb, houtb, ab, hinb);
+        for (int k = 0; k < kBondValues; k++) bb[k] = hinb[k];
+        for (int k = 0; k < 3; k++) {
+          d[k] += ab.d[k];
+          vr[k] += ab.vr[k];
+          wi[k] += ab.wi[k];
+          wj[k] += ab.wj[k];
+        }
+        ri += ab.ri;
+        rj += ab.rj;
+      }
+      if (touch) {
+        a.bonded = st == kBondActive;
+        VjpBar bb;
+        for (int k = 0; k < 3; k++) {
+          bb.F[k] = Fb[k];
+          bb.Ti[k] = Tib[k];
+          bb.Tj[k] = Tjb[k];
+          bb.s3[k] = upd ? B.sb[3 * p + k] : 0.0;
+        }
+        law_vjp(a, bb);
+        for (int k = 0; k < 3; k++) {
+          d[k] += bb.d[k];
+          vr[k] += bb.vr[k];
+          wi[k] += bb.wi[k];
+          wj[k] += bb.wj[k];  // F_i and T_i depend on w_j for periodic images too
+          B.sb[3 * p + k] = bb.sh[k] + (upd ? 0.0 : B.sb[3 * p + k]);
+        }
+        ri += bb.ri;
+        rj += bb.rj;
+        mi += bb.mi;
+        mj += bb.mj;
+        th[0] = bb.Y;
+        th[1] = bb.G;
+        th[2] = bb.beta;
+        th[3] = bb.mu;
+      } else if (band) {
+        for (int k = 0; k < 3; k++) B.sb[3 * p + k] = 0.0;  // history cleared: no dependence
+      }
+      for (int k = 0; k < 3; k++) {
+        B.pd[3 * p + k] = d[k];
+        B.pv[3 * p + k] = vr[k];
+        B.pwi[3 * p + k] = wi[k];
+        B.pwj[3 * p + k] = wj[k];
+      }
+      B.pri[p] = ri;
+      B.prj[p] = rj;
+      B.pmi[p] = mi;
+      B.pmj[p] = mj;
+      for (int k = 0; k < 4; k++) B.pth[4 * p + k] += th[k];  // summed over the segment's steps
     }
-    if (touch) {
-      a.bonded = st == kBondActive;
-      VjpBar bb;
-      for (int k = 0; k < 3; k++) {
-        bb.F[k] = Fb[k];
-        bb.Ti[k] = Tib[k];
-        bb.Tj[k] = Tjb[k];
-        bb.s3[k] = upd ? B.sb[3 * p + k] : 0.0;
-      }
-      law_vjp(a, bb);
-      for (int k = 0; k < 3; k++) {
-        d[k] += bb.d[k];
-        vr[k] += bb.vr[k];
-        wi[k] += bb.wi[k];
-        wj[k] += bb.wj[k];  // F_i and T_i depend on w_j for periodic images too
-        B.sb[3 * p + k] = bb.sh[k] + (upd ? 0.0 : B.sb[3 * p + k]);
-      }
-      ri += bb.ri;
-      rj += bb.rj;
-      mi += bb.mi;
-      mj += bb.mj;
-      th[0] = bb.Y;
-      th[1] = bb.G;
-      th[2] = bb.beta;
-      th[3] = bb.mu;
-    } else if (band) {
-      for (int k = 0; k < 3; k++) B.sb[3 * p + k] = 0.0;  // history cleared: no dependence
-    }  // else: history unchanged, its adjoint passes through
-    for (int k = 0; k < 3; k++) {
-      B.pd[3 * p + k] = d[k];
-      B.pv[3 * p + k] = vr[k];
-      B.pwi[3 * p + k] = wi[k];
-      B.pwj[3 * p + k] = wj[k];
-    }
-    B.pri[p] = ri;
-    B.prj[p] = rj;
-    B.pmi[p] = mi;
-    B.pmj[p] = mj;
-    for (int k = 0; k < 4; k++) B.pth[4 * p + k] = th[k];
+    __syncthreads();
   }
 }
 
@@ -718,8 +890,7 @@ __global__ void kb_gather_kick(ADev s, ABar B, const double *Fn, const double *T
       B.mb[i] += mb;
       continue;
     }
-    const double m = s.m[i], r = s.r[i];
-    const double a = s.dtf / m, b = s.dtfrot / (r * r * m);
+    const double a = s.ka[i], b = s.kb[i];
     double fv = 0.0, tw = 0.0;
     for (int k = 0; k < 3; k++) {
       vb[k] += s.dt * xb[k];
@@ -731,8 +902,8 @@ __global__ void kb_gather_kick(ADev s, ABar B, const double *Fn, const double *T
       fv += Fn[3 * i + k] * vb[k];
       tw += Tn[3 * i + k] * wb[k];
     }
-    B.rb[i] += rb - 2.0 * b / r * tw;
-    B.mb[i] += mb - a / m * fv - b / m * tw;
+    B.rb[i] += rb - s.kbr[i] * tw;
+    B.mb[i] += mb - s.kam[i] * fv - s.kbm[i] * tw;
   }
 }
 
@@ -855,6 +1026,9 @@ struct dem_adjoint {
   double last_fwd_ms = 0.0, last_bwd_ms = 0.0;
   int last_nseg = 0, last_maxnp = 0;
   dem_bond_settings bond_settings{};
+  int tape_mode = 2;          // 0 replay, 1 record every step, 2 record when it fits
+  double tape_max_bytes = 0;  // budget of mode 2 (0: half the free device memory)
+  int last_recorded = 0;
 };
 
 #define ATRY(h, call)                                                \
@@ -888,10 +1062,21 @@ cudaError_t dmalloc(std::vector<void *> &owned, T **p, size_t n) {
   return e;
 }
 
+// per-step record of one segment: positions, half-step velocities and the
+// history each force evaluation saw, and its forces; ps: entries per step of
+// the pair parts
+struct Tape {
+  double *x = nullptr, *vh = nullptr, *wh = nullptr, *F = nullptr, *T = nullptr, *ws = nullptr;
+  double *sh = nullptr, *bh = nullptr;
+  float4 *xf = nullptr;
+  size_t ps = 0;
+};
+
 struct Checkpoint {
   double *x, *v, *w, *F, *T, *ws;  // state before the segment's first drift
   double *sh0, *bh0;               // the list's history as carried at the build
   AList L;
+  Tape tape;                       // recorded in the forward pass (tape mode), else replayed
 };
 
 // neighbour list of the current positions; old: the previous list (with its
@@ -979,22 +1164,24 @@ void derive(double E, double nu, double e, double &Y, double &G, double &beta, d
 }
 
 void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, long long ntimestep,
-                double *tape_sh, double *tape_bh, double *tape_ws, int final_kick, double *wallF) {
+                double *tape_sh, double *tape_bh, double *tape_ws, int final_kick, double *wallF,
+                double *tape_F = nullptr, double *tape_T = nullptr) {
   ADev &s = h->s;
   if (s.np > 0 && s.bonds)
     ka_pair_force<true><<<grid_of(s.np), kAB, 0, h->st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
   else if (s.np > 0)
     ka_pair_force<false><<<grid_of(s.np), kAB, 0, h->st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
-  ka_gather<<<grid_of(h->n), kAB, 0, h->st>>>(s, vh, wh, upd, final_kick, tape_ws, wallF);
+  ka_gather<<<grid_of(h->n), kAB, 0, h->st>>>(s, vh, wh, upd, final_kick, tape_ws, wallF, tape_F, tape_T);
 }
 
-void pairs_vjp(dem_adjoint *h, const double *x, const double *vh, const double *wh, const double *sh_before,
-               const double *bh_before, int upd, long long ntimestep) {
+void pairs_vjp(dem_adjoint *h, const double *x, const float4 *xf, const double *vh, const double *wh,
+               const double *sh_before, const double *bh_before, int upd, long long ntimestep) {
   const ADev &s = h->s;
   if (s.np > 0 && s.bonds)
-    kb_pairs<true><<<grid_of(s.np), kAB, 0, h->st>>>(s, h->B, x, vh, wh, sh_before, bh_before, upd, ntimestep);
+    kb_pairs<true><<<grid_of(s.np), kAB, 0, h->st>>>(s, h->B, x, xf, vh, wh, sh_before, bh_before, upd, ntimestep);
   else if (s.np > 0)
-    kb_pairs<false><<<grid_of(s.np), kAB, 0, h->st>>>(s, h->B, x, vh, wh, sh_before, bh_before, upd, ntimestep);
+    kb_pairs<false><<<grid_of(s.np), kAB, 0, h->st>>>(s, h->B, x, xf, vh, wh, sh_before, bh_before, upd,
+                                                      ntimestep);
 }
 
 void accumulate(dem_adjoint *h, const double *in, int cnt) {
@@ -1153,10 +1340,21 @@ int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *
   double **d3[] = {&s.x, &s.v, &s.w, &s.F, &s.T, &h->x0, &h->v0, &h->w0, &h->xref,
                    &h->B.xb, &h->B.vb, &h->B.wb, &h->B.Fb, &h->B.Tb};
   for (double **q : d3) ATRY(h, dmalloc(h->owned, q, 3 * (size_t)n));
-  double **d1[] = {&s.r, &s.m, &h->r0, &h->B.rb, &h->B.mb};
+  double **d1[] = {&s.r, &s.m, &h->r0, &h->B.rb, &h->B.mb, &s.ka, &s.kb, &s.kam, &s.kbm, &s.kbr};
   for (double **q : d1) ATRY(h, dmalloc(h->owned, q, (size_t)n));
   const size_t W3 = 3 * (size_t)std::max(1, s.nplanes) * n;
   ATRY(h, dmalloc(h->owned, &s.ws, W3));
+  ATRY(h, dmalloc(h->owned, &s.xf, (size_t)n));
+  // the FP32 mirror's margin: coordinates and image shifts below X in size
+  // round by at most 2^-24 X each, a difference by 4 such roundings; 4e-6 X
+  // is more than ten times the bound on the distance error
+  double X = 0.0, P = 0.0;
+  for (int d = 0; d < 3; d++) {
+    X = std::max(X, std::max(std::fabs(s.lo[d]), std::fabs(s.hi[d])));
+    P = std::max(P, s.prd[d]);
+    s.prdf[d] = (float)s.prd[d];
+  }
+  s.fm = (float)(4e-6 * (X + P));
   ATRY(h, dmalloc(h->owned, &h->B.wsb, W3));
   ATRY(h, dmalloc(h->owned, &h->wallF, W3));
   ATRY(h, dmalloc(h->owned, &h->B.wth, 4 * (size_t)n));
@@ -1211,6 +1409,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   const size_t S3 = 3 * (size_t)n, W3 = 3 * (size_t)std::max(1, s.nplanes) * n;
   ATRY(h, cudaMemcpyAsync(s.r, rr.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
   ATRY(h, cudaMemcpyAsync(s.m, mm.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
+  ka_consts<<<grid_of(n), kAB, 0, st>>>(s);
   copyd(h, s.x, h->x0, S3);
   copyd(h, s.v, h->v0, S3);
   copyd(h, s.w, h->w0, S3);
@@ -1222,6 +1421,16 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   // built after the drift of step kL (k >= 1) or at setup (k = 0)
   const int nseg = nsteps / seg + 1;
   std::vector<Checkpoint> cps(nseg);
+  // tape mode: 1 records every step in the forward pass (no replay), 0
+  // replays each segment from its checkpoint, 2 decides by the budget
+  bool record = h->tape_mode == 1;
+  size_t tape_budget = 0;
+  if (h->tape_mode == 2) {
+    size_t fr = 0, tot = 0;
+    ATRY(h, cudaMemGetInfo(&fr, &tot));
+    const size_t avail = (fr + h->arena.cap) / 2;  // the arena of the previous run is reused
+    tape_budget = h->tape_max_bytes > 0 ? std::min((size_t)h->tape_max_bytes, avail) : avail;
+  }
   int rc;
   AList none;
   int maxnp = 1;
@@ -1250,6 +1459,24 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
         copyd(h, c.bh0, c.L.bond, (size_t)kBondValues * c.L.np);
       }
     }
+    const int nst = last - first + 1;
+    if (k == 0 && h->tape_mode == 2) {
+      // record every step when the whole tape fits the budget (the pair
+      // parts estimated from the first list, with room to grow)
+      const size_t pe = (size_t)(1.5 * cps[0].L.np) + 1024;
+      const size_t per = (5 * S3 + W3 + 2 * (size_t)n + (3 + (s.bonds ? kBondValues : 0)) * pe) * sizeof(double);
+      record = per * (size_t)nsteps <= tape_budget;
+    }
+    if (record && nst > 0) {
+      Tape &T = c.tape;
+      AGET(h, T.x, double, S3 * nst);
+      AGET(h, T.vh, double, S3 * nst);
+      AGET(h, T.wh, double, S3 * nst);
+      AGET(h, T.F, double, S3 * nst);
+      AGET(h, T.T, double, S3 * nst);
+      AGET(h, T.ws, double, W3 * nst);
+      AGET(h, T.xf, float4, (size_t)n * nst);
+    }
     copyd(h, c.x, s.x, S3);
     copyd(h, c.v, s.v, S3);
     copyd(h, c.w, s.w, S3);
@@ -1258,9 +1485,13 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     copyd(h, c.ws, s.ws, W3);
     for (int t = first; t <= last; t++) {
       const bool build = (k > 0 && t == first);
-      ka_kick_drift<<<grid_of(n), kAB, 0, st>>>(s, build ? nullptr : h->xref);
+      const int q = t - first;
+      Tape &T = c.tape;
+      const bool rec = T.x != nullptr;
+      ka_kick_drift<<<grid_of(n), kAB, 0, st>>>(s, build ? nullptr : h->xref, build ? 1 : 0,
+                                                rec ? T.x + S3 * q : nullptr, rec ? T.vh + S3 * q : nullptr,
+                                                rec ? T.wh + S3 * q : nullptr, rec ? T.xf + (size_t)n * q : nullptr);
       if (build) {
-        ka_wrap<<<grid_of(n), kAB, 0, st>>>(s);
         rc = build_list(h, c.L, cps[k - 1].L);
         if (rc) return rc;
         rc = ensure_pairs(h, c.L.np);
@@ -1274,7 +1505,14 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
           copyd(h, c.bh0, c.L.bond, (size_t)kBondValues * c.L.np);
         }
       }
-      force_pass(h, s.v, s.w, 1, t, nullptr, nullptr, nullptr, 1, t == nsteps ? h->wallF : nullptr);
+      if (rec && q == 0) {  // the pair parts, sized by this segment's list
+        T.ps = std::max(1, c.L.np);
+        AGET(h, T.sh, double, 3 * T.ps * nst);
+        if (s.bonds) AGET(h, T.bh, double, kBondValues * T.ps * nst);
+      }
+      force_pass(h, s.v, s.w, 1, t, rec ? T.sh + 3 * T.ps * q : nullptr,
+                 rec && s.bonds ? T.bh + kBondValues * T.ps * q : nullptr, rec ? T.ws + W3 * q : nullptr, 1,
+                 t == nsteps ? h->wallF : nullptr, rec ? T.F + S3 * q : nullptr, rec ? T.T + S3 * q : nullptr);
     }
     maxnp = std::max(maxnp, c.L.np);
   }
@@ -1293,6 +1531,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
   h->last_fwd_ms = ms;
   h->last_nseg = nseg;
+  h->last_recorded = record ? 1 : 0;
   h->last_maxnp = maxnp;
   if (flag) {
     h->err = "an atom moved more than skin/2 from its position at the list build: use shorter segments or a larger skin";
@@ -1345,65 +1584,74 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   ATRY(h, cudaMemsetAsync(B.sb, 0, 3 * (size_t)h->pcap * sizeof(double), st));
   if (s.bonds) ATRY(h, cudaMemsetAsync(B.bb, 0, (size_t)kBondValues * h->pcap * sizeof(double), st));
   ATRY(h, cudaMemsetAsync(B.th, 0, 4 * sizeof(double), st));
+  ATRY(h, cudaMemsetAsync(B.wth, 0, 4 * (size_t)n * sizeof(double), st));
   const double fw_seed = use_wall ? loss->w_wallforce * 2.0 * (fw - loss->wallforce_target) : 0.0;
-  // tape of one segment
-  double *tx, *tvh, *twh, *tF, *tT, *tws, *tsh, *shr, *sb_prev;
-  AGET(h, tx, double, S3 * seg);
-  AGET(h, tvh, double, S3 * seg);
-  AGET(h, twh, double, S3 * seg);
-  AGET(h, tF, double, S3 * seg);
-  AGET(h, tT, double, S3 * seg);
-  AGET(h, tws, double, W3 * seg);
-  AGET(h, tsh, double, 3 * (size_t)maxnp * seg);
+  // the replay's tape of one segment (segments recorded in the forward pass
+  // use their own)
+  Tape shared;
+  shared.ps = (size_t)maxnp;
+  if (!record) {
+    AGET(h, shared.x, double, S3 * seg);
+    AGET(h, shared.vh, double, S3 * seg);
+    AGET(h, shared.wh, double, S3 * seg);
+    AGET(h, shared.F, double, S3 * seg);
+    AGET(h, shared.T, double, S3 * seg);
+    AGET(h, shared.ws, double, W3 * seg);
+    AGET(h, shared.sh, double, 3 * (size_t)maxnp * seg);
+    AGET(h, shared.xf, float4, (size_t)n * seg);
+    if (s.bonds) AGET(h, shared.bh, double, kBondValues * (size_t)maxnp * seg);
+  }
+  double *shr, *sb_prev, *tws0;
   AGET(h, shr, double, 3 * (size_t)maxnp);
   AGET(h, sb_prev, double, 3 * (size_t)maxnp);
-  double *tbh = nullptr, *bhr = nullptr, *bb_prev = nullptr;
+  AGET(h, tws0, double, W3);
+  double *bhr = nullptr, *bb_prev = nullptr;
   const size_t NB = kBondValues * (size_t)maxnp;
   if (s.bonds) {
-    AGET(h, tbh, double, NB * seg);
     AGET(h, bhr, double, NB);
     AGET(h, bb_prev, double, NB);
   }
   for (int k = nseg - 1; k >= 0; k--) {
     Checkpoint &c = cps[k];
     const int first = std::max(1, k * seg), last = std::min(nsteps, (k + 1) * seg - 1);
-    // replay from the checkpoint, recording the tape
-    copyd(h, s.x, c.x, S3);
-    copyd(h, s.v, c.v, S3);
-    copyd(h, s.w, c.w, S3);
-    copyd(h, s.F, c.F, S3);
-    copyd(h, s.T, c.T, S3);
-    copyd(h, s.ws, c.ws, W3);
-    copyd(h, shr, c.sh0, 3 * (size_t)c.L.np);
-    if (s.bonds) copyd(h, bhr, c.bh0, (size_t)kBondValues * c.L.np);
-    use_list(h, c.L, shr, bhr);
-    for (int t = first; t <= last; t++) {
-      const int q = t - first;
-      ka_kick_drift<<<grid_of(n), kAB, 0, st>>>(s, nullptr);
-      if (k > 0 && t == first) ka_wrap<<<grid_of(n), kAB, 0, st>>>(s);
-      copyd(h, tx + S3 * q, s.x, S3);
-      copyd(h, tvh + S3 * q, s.v, S3);
-      copyd(h, twh + S3 * q, s.w, S3);
-      force_pass(h, tvh + S3 * q, twh + S3 * q, 1, t, tsh + 3 * (size_t)maxnp * q, s.bonds ? tbh + NB * q : nullptr,
-                 tws + W3 * q, 1, nullptr);
-      copyd(h, tF + S3 * q, s.F, S3);
-      copyd(h, tT + S3 * q, s.T, S3);
+    const bool recorded = c.tape.x != nullptr;
+    const Tape &T = recorded ? c.tape : shared;
+    const size_t PS = T.ps;
+    if (!recorded) {  // replay from the checkpoint, recording the tape
+      copyd(h, s.x, c.x, S3);
+      copyd(h, s.v, c.v, S3);
+      copyd(h, s.w, c.w, S3);
+      copyd(h, s.F, c.F, S3);
+      copyd(h, s.T, c.T, S3);
+      copyd(h, s.ws, c.ws, W3);
+      copyd(h, shr, c.sh0, 3 * (size_t)c.L.np);
+      if (s.bonds) copyd(h, bhr, c.bh0, (size_t)kBondValues * c.L.np);
     }
-    // reverse over the segment's steps
+    use_list(h, c.L, shr, bhr);
+    for (int t = first; t <= last && !recorded; t++) {
+      const int q = t - first;
+      ka_kick_drift<<<grid_of(n), kAB, 0, st>>>(s, nullptr, (k > 0 && t == first) ? 1 : 0, T.x + S3 * q,
+                                                T.vh + S3 * q, T.wh + S3 * q, T.xf + (size_t)n * q);
+      force_pass(h, T.vh + S3 * q, T.wh + S3 * q, 1, t, T.sh + 3 * PS * q,
+                 s.bonds ? T.bh + kBondValues * PS * q : nullptr, T.ws + W3 * q, 1, nullptr, T.F + S3 * q,
+                 T.T + S3 * q);
+    }
+    // reverse over the segment's steps; the pair parameter adjoints of the
+    // segment's list are summed per entry over its steps, then reduced
+    if (s.np > 0) ATRY(h, cudaMemsetAsync(B.pth, 0, 4 * (size_t)s.np * sizeof(double), st));
     for (int t = last; t >= first; t--) {
       const int q = t - first;
-      const double *xs = tx + S3 * q, *vh = tvh + S3 * q, *wh = twh + S3 * q;
-      kb_final<<<grid_of(n), kAB, 0, st>>>(s, B, tF + S3 * q, tT + S3 * q);
-      kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, xs, vh, wh, tws + W3 * q, 1, t == nsteps ? lw : -1,
-                                           t == nsteps ? fw_seed : 0.0);
+      const double *xs = T.x + S3 * q, *vh = T.vh + S3 * q, *wh = T.wh + S3 * q;
+      kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, xs, vh, wh, T.ws + W3 * q, 1, t == nsteps ? lw : -1,
+                                           t == nsteps ? fw_seed : 0.0, T.F + S3 * q, T.T + S3 * q);
       if (s.np > 0)
-        pairs_vjp(h, xs, vh, wh, tsh + 3 * (size_t)maxnp * q, s.bonds ? tbh + NB * q : nullptr, 1, t);
-      const double *Fn = q > 0 ? tF + S3 * (q - 1) : c.F;
-      const double *Tn = q > 0 ? tT + S3 * (q - 1) : c.T;
+        pairs_vjp(h, xs, T.xf + (size_t)n * q, vh, wh, T.sh + 3 * PS * q,
+                  s.bonds ? T.bh + kBondValues * PS * q : nullptr, 1, t);
+      const double *Fn = q > 0 ? T.F + S3 * (q - 1) : c.F;
+      const double *Tn = q > 0 ? T.T + S3 * (q - 1) : c.T;
       kb_gather_kick<<<grid_of(n), kAB, 0, st>>>(s, B, Fn, Tn, 1);
-      accumulate(h, B.pth, s.np);
-      accumulate(h, B.wth, n);
     }
+    if (k > 0) accumulate(h, B.pth, s.np);  // segment 0: after the setup pass below
     if (k > 0) {  // history adjoints back through the carry at this build
       const AList &po = cps[k - 1].L;
       ATRY(h, cudaMemsetAsync(sb_prev, 0, 3 * (size_t)std::max(1, po.np) * sizeof(double), st));
@@ -1420,15 +1668,15 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   }
   {  // Verlet::setup force pass: initial state, zero history, no update
     Checkpoint &c = cps[0];
-    ATRY(h, cudaMemsetAsync(tws, 0, W3 * sizeof(double), st));
+    ATRY(h, cudaMemsetAsync(tws0, 0, W3 * sizeof(double), st));
     ATRY(h, cudaMemsetAsync(shr, 0, 3 * (size_t)maxnp * sizeof(double), st));
     if (s.bonds) ATRY(h, cudaMemsetAsync(bhr, 0, NB * sizeof(double), st));
     use_list(h, c.L, shr, bhr);
-    kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, c.x, c.v, c.w, tws, 0, -1, 0.0);
-    pairs_vjp(h, c.x, c.v, c.w, shr, bhr, 0, 0);
+    kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, c.x, c.v, c.w, tws0, 0, -1, 0.0, nullptr, nullptr);
+    pairs_vjp(h, c.x, nullptr, c.v, c.w, shr, bhr, 0, 0);
     kb_gather_kick<<<grid_of(n), kAB, 0, st>>>(s, B, nullptr, nullptr, 0);
-    accumulate(h, B.pth, s.np);
-    accumulate(h, B.wth, n);
+    accumulate(h, B.pth, s.np);  // segment 0's steps and the setup pass
+    accumulate(h, B.wth, n);     // every step's wall contacts
   }
   ATRY(h, cudaGetLastError());
   std::vector<double> rb(n), mb(n), th(4);
@@ -1475,6 +1723,19 @@ int dem_adjoint_times(dem_adjoint *h, double *forward_ms, double *backward_ms, i
   if (backward_ms) *backward_ms = h->last_bwd_ms;
   if (segments) *segments = h->last_nseg;
   if (max_pairs) *max_pairs = h->last_maxnp;
+  return DEM_OK;
+}
+
+int dem_adjoint_set_tape(dem_adjoint *h, int mode, double max_bytes) {
+  if (!h || mode < 0 || mode > 2 || !(max_bytes >= 0)) return DEM_ERR_BAD_ARG;
+  h->tape_mode = mode;
+  h->tape_max_bytes = max_bytes;
+  return DEM_OK;
+}
+
+int dem_adjoint_tape_recorded(dem_adjoint *h, int *recorded) {
+  if (!h || !recorded) return DEM_ERR_BAD_ARG;
+  *recorded = h->last_recorded;
   return DEM_OK;
 }
 

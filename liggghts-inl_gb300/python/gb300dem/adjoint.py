@@ -49,6 +49,8 @@ def _bind(L):
     L.dem_adjoint_gradient.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P, P, P, P, P]
     L.dem_adjoint_download.argtypes = [P, P, P, P]
     L.dem_adjoint_times.argtypes = [P, P, P, P, P]
+    L.dem_adjoint_set_tape.argtypes = [P, I, D]
+    L.dem_adjoint_tape_recorded.argtypes = [P, P]
     L.dem_adjoint_last_error.argtypes = [P]
     L.dem_adjoint_last_error.restype = ctypes.c_char_p
     L._adjoint_bound = True
@@ -145,6 +147,18 @@ class DemAdjoint:
                    ctypes.byref(loss or make_loss(w_ke=1.0)), ctypes.byref(out), ctypes.byref(gE),
                    ctypes.byref(ge), ctypes.byref(gmu), api._p(gr))
         return out.value, dict(E=gE.value, restitution=ge.value, friction=gmu.value, radius=gr)
+
+    def set_tape(self, mode, max_bytes=0.0):
+        """Where the backward pass takes each step's record: 0 replay from
+        checkpoints (O(sqrt(N)) memory), 1 record every step in the forward
+        pass, 2 record when it fits max_bytes (default: half the free device
+        memory)."""
+        self._call("dem_adjoint_set_tape", self.h, int(mode), float(max_bytes))
+
+    def tape_recorded(self):
+        r = ctypes.c_int()
+        self._call("dem_adjoint_tape_recorded", self.h, ctypes.byref(r))
+        return bool(r.value)
 
     def final_state(self):
         x, v, w = (np.zeros((self.n, 3)) for _ in range(3))

@@ -196,6 +196,33 @@ def test_adjoint_segment_length_and_determinism():
     eng.close()
 
 
+@pytest.mark.parametrize("bonded", [False, True])
+def test_adjoint_recorded_and_replayed_tapes_agree(bonded):
+    """The backward pass on a record taken in the forward pass and on one
+    replayed from the sqrt(N) checkpoints: the same gradients bit for bit."""
+    from gb300dem.adjoint import DemAdjoint
+    if bonded:
+        import test_adjoint_bonds
+        c = test_adjoint_bonds._case(law="full")
+    else:
+        c = _case()
+    eng = DemAdjoint(c)
+    spec = _spec("ke")
+    out = {}
+    for mode in (0, 1, 2):
+        eng.set_tape(mode)
+        out[mode] = eng.gradient(1e7, 0.6, 0.5, nsteps=NSTEPS, segment=SEG, loss=spec)
+        assert eng.tape_recorded() == (mode != 0), mode  # mode 2: this record fits
+    for mode in (1, 2):
+        assert out[mode][0] == out[0][0]
+        for k in ("E", "restitution", "friction", "radius"):
+            assert np.array_equal(out[mode][1][k], out[0][1][k]), (mode, k)
+    eng.set_tape(2, max_bytes=1e3)  # a budget the record does not fit: replay
+    eng.gradient(1e7, 0.6, 0.5, nsteps=NSTEPS, segment=SEG, loss=spec)
+    assert not eng.tape_recorded()
+    eng.close()
+
+
 def test_adjoint_torch_function():
     torch = pytest.importorskip("torch")
     from gb300dem.adjoint import DemAdjoint, adjoint_loss
