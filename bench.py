@@ -28,6 +28,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 METRIC = "particle-steps/s (1M Hertz/history spheres)"
+METRICS = {"fibres200k": "particle-steps/s (200k bonded fibre spheres)"}
 
 # Per-atom FP64 arithmetic (flop, DFMA = 2) and DRAM bytes (read + write) of
 # one launch, and the FP64 pipe's active fraction, from ncu captures of the
@@ -81,6 +82,29 @@ def workload(name, scale=1.0, seed=2024):
                                 "lattice (2.2 mm, r 0.8-1.2 mm) in a periodic x/y column with a "
                                 "floor plane; configs[1] materials, dt 5e-7",
                     l2="state + neighbour list > L2 (129 MB); no flush needed")
+        return case, desc
+    if name == "fibres200k":
+        # configs[2] material: 20,000 fibres x 10 spheres (200k), r 0.5 mm,
+        # cohesion bond/nonlinear with radiusMultiplier 0.5, tsCreate 1 and
+        # createDistance just above 2r, so intra-fibre touching pairs bond at
+        # step 1; dt 1e-7.  configs[2]'s 40 mm cube cannot hold 200k spheres
+        # of r 0.5 mm (1.6x its volume), so the fibres lie in plywood layers
+        # (workloads.fibre_bed_case) in a 40.8 x 40.8 mm periodic column on a
+        # floor, without the moving top plate.
+        r = 0.5e-3
+        bp = workloads.bond_params(
+            2, [1], tsCreate=1.0, radiusMultiplier=0.5, K_fn1=200.0, Ku_fn1=400.0, Kc_fn1=100.0,
+            K_fn2=1e12, Ku_fn2=2e12, Kc_fn2=5e11, K_ft=5e11, K_tn=5e11, Ku_tn=1e12, Kc_tn=2.5e11,
+            K_tt=5e11, Ku_tt=1e12, Kc_tt=2.5e11, damp_fn=0.05, damp_ft=0.05, damp_tn=0.05,
+            damp_tt=0.05, maxDistance=2 * r * 1.0035, maxSigma=6e6, maxTau=6e6, ratioTC=0.5,
+            createDistance=2 * r * 1.002)
+        case = workloads.fibre_bed_case(seed, max(100, int(round(200_000 * scale)) // 10 * 10), radius=r,
+                                        bond=bp, dt=1e-7, skin=2e-4, vmax=0.05)
+        desc = dict(workload="fibres200k", atoms=int(len(case["atoms"]["tag"])), fibres=case["nfibres"],
+                    description="configs[2] bonded fibres: 10-sphere fibres (r 0.5 mm) in plywood "
+                                "layers, Hertz/history between fibres, cohesion bond/nonlinear within "
+                                "(bonds created at step 1), periodic x/y column on a floor, dt 1e-7",
+                    l2="state + neighbour list + 28-value bond histories > L2 (129 MB); no flush needed")
         return case, desc
     raise SystemExit("unknown workload %s" % name)
 
@@ -204,7 +228,8 @@ def run_reference(args):
     _, desc = workload(args.workload, scale=0.01)
     sample = ("%d independent replicas (one per core) of a %d-atom slice of %s, %d timed steps each"
               % (cores, res[0][0], args.workload, steps))
-    line = {"metric": METRIC, "value": val, "unit": "particle-steps/s", "n_gpus": args.gpus,
+    line = {"metric": METRICS.get(args.workload, METRIC), "value": val, "unit": "particle-steps/s",
+            "n_gpus": args.gpus,
             "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * max(r[2] for r in res) / steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)", "impl": "reference",
@@ -334,7 +359,8 @@ def run_gb300(args):
                "sample": "oracle (CPU restatement, pinned to the reference binary) on a %d-atom slice "
                          "of %s, %d steps, 1 thread" % (res[0][0], args.workload, args.cpu_steps)}
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        line = {"metric": METRICS.get(args.workload, METRIC), "value": value, "unit": "particle-steps/s",
+                "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_ms / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded)", "impl": "gb300",
@@ -481,7 +507,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="hopper1m",
-                    choices=["hopper1m", "column1m", "ensemble256", "adjoint20k"])
+                    choices=["hopper1m", "column1m", "fibres200k", "ensemble256", "adjoint20k"])
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0,

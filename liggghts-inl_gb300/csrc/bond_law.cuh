@@ -40,23 +40,23 @@ __device__ __forceinline__ double bond_tab(const Sys &s, int table, int tp) {
 
 __device__ __forceinline__ double sgn_d(double v) { return (double)((0.0 < v) - (v < 0.0)); }
 
-// vectorProject3D (src/vector_liggghts.h:437-442): onto the normalised `on`
-__device__ __forceinline__ void project3(const double v[3], const double on[3], double out[3]) {
-  const double norm = sqrt(on[0] * on[0] + on[1] * on[1] + on[2] * on[2]);
-  const double inv = (norm == 0.) ? 0. : 1. / norm;
-  const double n0 = on[0] * inv, n1 = on[1] * inv, n2 = on[2] * inv;
-  const double dot = v[0] * n0 + v[1] * n1 + v[2] * n2;
-  out[0] = dot * n0;
-  out[1] = dot * n1;
-  out[2] = dot * n2;
+// vectorProject3D (src/vector_liggghts.h:437-442) onto `on`, given `on`
+// normalised as that function normalises it (n = on/|on|, 0 for on = 0);
+// the model projects three vectors onto the same en, so the normalisation
+// is formed once (same operations, same bits)
+__device__ __forceinline__ void project3_n(const double v[3], const double n[3], double out[3]) {
+  const double dot = v[0] * n[0] + v[1] * n[1] + v[2] * n[2];
+  out[0] = dot * n[0];
+  out[1] = dot * n[1];
+  out[2] = dot * n[2];
 }
 
-// one component of the hysteretic twisting/bending law (:677-761, :792-866)
+// one component of the hysteretic twisting/bending law (:677-761, :792-866);
+// ratio = (ku - k)/(ku + kc), precomputed per type pair
 __device__ __forceinline__ double bond_hyst(double th, double &hmax, double &hmin, double k, double ku,
-                                            double kc, double JI) {
+                                            double kc, double ratio, double JI) {
   if (th > 0.0) hmin = 0.0;
   else if (th < 0.0) hmax = 0.0;
-  const double ratio = (ku - k) / (ku + kc);
   const double c1 = ratio * hmax, c2 = ratio * hmin;
   double t;
   if ((th >= hmax) || (th <= hmin)) t = -k * JI * th;
@@ -104,6 +104,14 @@ __device__ bool bond_nonlinear(const Sys &s, const BondIn &b, double *h, size_t 
   double tht[3] = {h[11 * hs], h[12 * hs], h[13 * hs]};
   const double rinv = 1. / r;
   const double en[3] = {rinv * b.d[0], rinv * b.d[1], rinv * b.d[2]};
+  double enn[3];
+  {
+    const double norm = sqrt(en[0] * en[0] + en[1] * en[1] + en[2] * en[2]);
+    const double inv = (norm == 0.) ? 0. : 1. / norm;
+    enn[0] = en[0] * inv;
+    enn[1] = en[1] * inv;
+    enn[2] = en[2] * inv;
+  }
   const double radi = b.radi, radj = b.radj;
   const double rmin = radi < radj ? radi : radj;
   const double rb = lambda * rmin;
@@ -117,7 +125,7 @@ __device__ bool bond_nonlinear(const Sys &s, const BondIn &b, double *h, size_t 
   // relative velocities (:518-545)
   const double vr[3] = {b.vi[0] - b.vj[0], b.vi[1] - b.vj[1], b.vi[2] - b.vj[2]};
   double vn[3];
-  project3(vr, en, vn);
+  project3_n(vr, enn, vn);
   const double fi_ = radi * radsuminv, fj_ = radj * radsuminv;
   const double wr[3] = {fi_ * b.wi[0] + fj_ * b.wj[0], fi_ * b.wi[1] + fj_ * b.wj[1],
                         fi_ * b.wi[2] + fj_ * b.wj[2]};
@@ -126,7 +134,7 @@ __device__ bool bond_nonlinear(const Sys &s, const BondIn &b, double *h, size_t 
                          (vr[2] - vn[2]) + (b.d[0] * wr[1] - b.d[1] * wr[0])};
   const double wrel[3] = {b.wi[0] - b.wj[0], b.wi[1] - b.wj[1], b.wi[2] - b.wj[2]};
   double wn[3];
-  project3(wrel, en, wn);
+  project3_n(wrel, enn, wn);
   const double wt[3] = {wrel[0] - wn[0], wrel[1] - wn[1], wrel[2] - wn[2]};
   const double minvel = 1e-5 * rmin / dt;
   const bool damping = (fl & kBondDamping) != 0, smooth = (fl & kBondDampingSmooth) != 0;
@@ -145,9 +153,9 @@ __device__ bool bond_nonlinear(const Sys &s, const BondIn &b, double *h, size_t 
     const double k1 = bond_tab(s, kBondKfn1, tp), ku1 = bond_tab(s, kBondKufn1, tp);
     const double kc1 = bond_tab(s, kBondKcfn1, tp), k2 = bond_tab(s, kBondKfn2, tp);
     const double ku2 = bond_tab(s, kBondKufn2, tp), kc2 = bond_tab(s, kBondKcfn2, tp);
-    const double q1 = (ku1 - k1) / (ku1 + kc1);
+    const double q1 = bond_tab(s, kBondRatioFn1, tp);
     const double dc1 = q1 * q1 * dmax;
-    const double dc2 = (ku2 - k2) / (ku2 + kc2) * dmin;
+    const double dc2 = bond_tab(s, kBondRatioFn2, tp) * dmin;
     double f;
     if (disp < dmin) f = k2 * A * disp;
     else if (disp < dc2) f = ku2 * A * disp + (k2 - ku2) * A * dmin;
@@ -171,7 +179,7 @@ __device__ bool bond_nonlinear(const Sys &s, const BondIn &b, double *h, size_t 
   if (fl & kBondShear) {
     const double sc = -bond_tab(s, kBondKft, tp) * A * dt;
     double pr[3];
-    project3(ft, en, pr);
+    project3_n(ft, enn, pr);
     for (int k = 0; k < 3; k++) ft[k] = (ft[k] - pr[k]) + sc * vtr[k];
     if (damping) {
       const double dft = bond_tab(s, kBondDampFt, tp);
@@ -187,10 +195,11 @@ __device__ bool bond_nonlinear(const Sys &s, const BondIn &b, double *h, size_t 
   double tn[3] = {0., 0., 0.}, ntd[3] = {0., 0., 0.};
   if (fl & kBondNormalTorque) {
     const double k = bond_tab(s, kBondKtn, tp), ku = bond_tab(s, kBondKutn, tp), kc = bond_tab(s, kBondKctn, tp);
+    const double ratio = bond_tab(s, kBondRatioTn, tp);
     for (int c = 0; c < 3; c++) {
       thn[c] = thn[c] + dt * wn[c];
       double hmax = h[(15 + c) * hs], hmin = h[(21 + c) * hs];
-      tn[c] = bond_hyst(thn[c], hmax, hmin, k, ku, kc, J);
+      tn[c] = bond_hyst(thn[c], hmax, hmin, k, ku, kc, ratio, J);
       h[(15 + c) * hs] = hmax;
       h[(21 + c) * hs] = hmin;
     }
@@ -201,10 +210,11 @@ __device__ bool bond_nonlinear(const Sys &s, const BondIn &b, double *h, size_t 
   double tt[3] = {0., 0., 0.}, ttd[3] = {0., 0., 0.};
   if (fl & kBondShearTorque) {
     const double k = bond_tab(s, kBondKtt, tp), ku = bond_tab(s, kBondKutt, tp), kc = bond_tab(s, kBondKctt, tp);
+    const double ratio = bond_tab(s, kBondRatioTt, tp);
     for (int c = 0; c < 3; c++) {
       tht[c] = tht[c] + dt * wt[c];
       double hmax = h[(18 + c) * hs], hmin = h[(24 + c) * hs];
-      tt[c] = bond_hyst(tht[c], hmax, hmin, k, ku, kc, I);
+      tt[c] = bond_hyst(tht[c], hmax, hmin, k, ku, kc, ratio, I);
       h[(18 + c) * hs] = hmax;
       h[(24 + c) * hs] = hmin;
     }

@@ -436,8 +436,21 @@ int dem_set_bond_params(dem_handle *h, const double *tables, const dem_bond_sett
     h->allocs_misc.erase(std::remove(h->allocs_misc.begin(), h->allocs_misc.end(), (void *)h->s.bondp),
                          h->allocs_misc.end());
   }
-  CUDA_TRY(h, dalloc(h->allocs_misc, &h->s.bondp, (size_t)kBondTables * m));
-  CUDA_TRY(h, cudaMemcpy(h->s.bondp, tables, (size_t)kBondTables * m * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, dalloc(h->allocs_misc, &h->s.bondp, (size_t)(kBondTables + kBondDerived) * m));
+  {
+    std::vector<double> all(tables, tables + (size_t)kBondTables * m);
+    all.resize((size_t)(kBondTables + kBondDerived) * m);
+    auto T = [&](int t, size_t q) { return tables[(size_t)t * m + q]; };
+    for (size_t q = 0; q < m; q++) {
+      all[(size_t)kBondRatioTn * m + q] = (T(kBondKutn, q) - T(kBondKtn, q)) / (T(kBondKutn, q) + T(kBondKctn, q));
+      all[(size_t)kBondRatioTt * m + q] = (T(kBondKutt, q) - T(kBondKtt, q)) / (T(kBondKutt, q) + T(kBondKctt, q));
+      all[(size_t)kBondRatioFn1 * m + q] =
+          (T(kBondKufn1, q) - T(kBondKfn1, q)) / (T(kBondKufn1, q) + T(kBondKcfn1, q));
+      all[(size_t)kBondRatioFn2 * m + q] =
+          (T(kBondKufn2, q) - T(kBondKfn2, q)) / (T(kBondKufn2, q) + T(kBondKcfn2, q));
+    }
+    CUDA_TRY(h, cudaMemcpy(h->s.bondp, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
+  }
   h->bond_tables.assign(tables, tables + (size_t)kBondTables * m);
   h->bond_settings = *st;
   int fl = 0;

@@ -35,6 +35,12 @@ constexpr int kNoShift = 13;                // shift code of (0,0,0)
 constexpr int kBondValues = 28;
 constexpr int kDnumBond = kDnumShear + kBondValues;
 constexpr int kBondTables = 23;  // per-type-pair tables, DEM_BOND_* order
+// Sys::bondp also holds, after those, per-type-pair ratios of the hysteresis
+// laws that the model forms from the stiffnesses on every evaluation
+// (computed on the host once; IEEE division gives the same bits):
+// (Ku-K)/(Ku+Kc) of twisting, of bending, of compression, of tension
+constexpr int kBondDerived = 4;
+enum { kBondRatioTn = kBondTables, kBondRatioTt, kBondRatioFn1, kBondRatioFn2 };
 enum {
   kBondLambda = 0, kBondKfn1, kBondKufn1, kBondKcfn1, kBondKfn2, kBondKufn2, kBondKcfn2, kBondKft,
   kBondKtn, kBondKutn, kBondKctn, kBondKtt, kBondKutt, kBondKctt, kBondDampFn, kBondDampFt,
@@ -193,7 +199,7 @@ struct Sys {
   float skin_lo2, skin_hi2;
   // cohesion bond/nonlinear (bond = 0: off, dnum = 3)
   int bond, dnum;
-  double *bondp;      // kBondTables matrices of (nt+1)^2
+  double *bondp;      // kBondTables + kBondDerived matrices of (nt+1)^2
   int bond_flags;
   long long bond_ts_create;  // static_cast<int>(tsCreateBondnonlinear)
   int neigh_every, neigh_delay, neigh_check;

@@ -292,6 +292,64 @@ def fibre_case(seed, nfib, nper, radius, box, spacing=(0.999, 1.001), density=10
     return case
 
 
+def fibre_bed_case(seed, n_target, radius=0.5e-3, nper=10, box_xy=(45e-3, 45e-3), along=1.0,
+                   across=1.05, end_gap=1.2, density=1000.0, E=(5e7, 5e7), nu=(0.3, 0.3),
+                   rest=((0.5, 0.5), (0.5, 0.5)), frict=((0.3, 0.3), (0.3, 0.3)), dt=1e-7, skin=2e-4,
+                   vmax=0.05, bond=None):
+    """A bed of straight fibres of nper spheres, built layer by layer (no
+    random placement, so it scales to 10^5-10^6 spheres): in each layer the
+    fibres lie parallel, along x in even layers and along y in odd ones
+    (plywood order).  Spheres of a fibre are along x 2r apart (touching), rows
+    and layers across x 2r apart, and fibre ends end_gap x 2r apart, so with
+    createDistance between 2r and across x 2r only intra-fibre neighbours bond.
+    Periodic in x and y, floor plane of wall type 2 at z = 0, atoms type 1."""
+    rng = np.random.default_rng(seed)
+    d = 2.0 * radius
+    Lx, Ly = box_xy
+    flen = (nper - 1) * along * d + end_gap * d  # fibre pitch along its axis
+    nfx = max(1, int(Lx // flen))
+    nrow = max(1, int(Ly // (across * d)))
+    Lx_eff, Ly_eff = nfx * flen, nrow * across * d
+    L = min(Lx_eff, Ly_eff)
+    nfx = max(1, int(L // flen))
+    nrow = max(1, int(L // (across * d)))
+    L = nfx * flen
+    nrow = int(L // (across * d))
+    per_layer = nfx * nrow * nper
+    nlayer = (n_target + per_layer - 1) // per_layer
+    k = np.arange(nper)
+    pts = []
+    for lay in range(nlayer):
+        z = radius + lay * across * d
+        fx, row = np.meshgrid(np.arange(nfx), np.arange(nrow), indexing="ij")
+        a0 = (fx.ravel()[:, None] * flen + k[None, :] * along * d + 0.5 * end_gap * d)
+        b0 = np.repeat((row.ravel()[:, None] + 0.5) * across * d, nper, axis=1)
+        if lay % 2 == 0:
+            xy = np.stack([a0.ravel(), b0.ravel()], axis=1)
+        else:
+            xy = np.stack([b0.ravel(), a0.ravel()], axis=1)
+        pts.append(np.column_stack([xy, np.full(len(xy), z)]))
+    x = np.concatenate(pts)[:n_target - n_target % nper].astype(np.float64)
+    n = len(x)
+    Lz = radius + nlayer * across * d + 20 * d
+    r = np.full(n, radius)
+    v = rng.uniform(-vmax, vmax, size=(n, 3)) if vmax > 0 else np.zeros((n, 3))
+    case = dict(
+        boxlo=(0.0, 0.0, 0.0), boxhi=(L, L, Lz), periodic=(1, 1, 0), dt=dt, skin=skin, cdf=1.0,
+        neigh=(1, 0, 1), normal_model=0, rolling_model=0, gravity=(0.0, 0.0, -9.81), ntypes=2,
+        charVel=0.0, planes=[(2, 0.0, 2, 0)], cohesion_model=1 if bond is not None else 0,
+        material=dict(E=list(E), nu=list(nu), rest=[list(q) for q in rest],
+                      frict=[list(q) for q in frict], rollfrict=None, density=density),
+        atoms=dict(tag=np.arange(1, n + 1, dtype=np.int32), type=np.ones(n, np.int32), x=x, v=v,
+                   omega=np.zeros((n, 3)), radius=r, rmass=sphere_mass(r, density)),
+        nfibres=n // nper, nper=nper,
+    )
+    if bond is not None:
+        case["bond"] = bond
+    case.update(derive_tables(E, nu, rest, frict, None))
+    return case
+
+
 def plate_mesh(x0, x1, y0, y1, z):
     """Two triangles of a horizontal plate [x0,x1] x [y0,y1] at height z,
     normal +z; nodes[2, 3, 3]."""

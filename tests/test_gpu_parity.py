@@ -229,6 +229,36 @@ def _fibre_case(seed, stress):
                                 gap=1.01, vmax=3.0, wmax=4000.0, bond=bp, skin=1e-4, max_fail=2000)
 
 
+def test_gpu_fibre_bed_matches_oracle():
+    """The bonded fibre bed of the fibres200k bench workload at 2,000 spheres:
+    every intra-fibre pair bonds at step 1 and no other; bond topology, pair
+    sets and forces as the oracle's over 100 steps."""
+    import bench
+    from oracle.binding import Oracle
+    case, _ = bench.workload("fibres200k", scale=0.01)
+    g = _gpu(case)
+    o = Oracle(case)
+    g.setup()
+    o.setup()
+    done = 0
+    for chunk in (1, 9, 90):
+        g.step(chunk)
+        o.run(chunk)
+        done += chunk
+        a, b = sort_by_tag(g.atoms()), sort_by_tag(o.atoms())
+        ftol = FORCE_RTOL if done <= 10 else DIVERGED_RTOL
+        assert max_rel(a["f"], b["f"]) < ftol, (done, max_rel(a["f"], b["f"]))
+        assert max_rel(a["x"], b["x"], scale=_box(case)) < TRAJ_RTOL
+        po = o.pairs()
+        op = canonical_pairs(po["tag_i"], po["tag_j"], po["shift"], po["flag"], po["hist"])
+        gp = _pairs(g)
+        missing, extra, flagmis, hm = compare_pairs(gp, op)
+        assert not missing and not extra and not flagmis, (done, len(missing), len(extra))
+        nb = sum(1 for k in op if op[k][1][0] > 0.5)
+        assert nb == case["nfibres"] * (case["nper"] - 1)
+        assert sum(1 for k in gp if gp[k][1][0] > 0.5) == nb
+
+
 @pytest.mark.parametrize("stress", [0, 1])
 def test_gpu_bonded_fibres_match_oracle(stress):
     """cohesion bond/nonlinear on ~1800 atoms: bond topology (bondFlag, the
