@@ -393,10 +393,10 @@ def run_ensemble(args):
     s0 = float(systems[0]["skin"])
     best, table = ensemble.autotune(systems[: max(2, nsys // 4)], steps=200, warm=20,
                                     blocks_per_sm=(4, 8, 16), cell_scale=(1.0, 1.25),
-                                    skins=(0.6 * s0, s0, 1.5 * s0))
+                                    skins=(0.6 * s0, s0, 1.5 * s0), particle_threads=(128, 256))
     skin = best[2]
     systems = [dict(sy, skin=skin) for sy in systems]
-    e = ensemble.Ensemble(systems, tuning=best[:2])
+    e = ensemble.Ensemble(systems, tuning=(best[0], best[1], best[3]))
     e.setup()
     e.step(args.warmup)
     clocks = Clocks()
@@ -426,13 +426,14 @@ def run_ensemble(args):
                        "description": "settling columns, N_k ~ U[2000, 20000], r U[0.9, 1.1] mm, "
                                       "E log-U[1e6, 1e8] Pa, e U[0.3, 0.95], mu U[0.1, 0.9], box "
                                       "0.05 x 0.05 x 0.3 m periodic x/y, floor, Hertz + history, dt 1e-6",
-                       "tuning": {"blocks_per_sm": best[0], "cell_scale": best[1], "skin": skin},
+                       "tuning": {"blocks_per_sm": best[0], "cell_scale": best[1], "skin": skin,
+                                  "particle_threads": best[3]},
                        "rebuilds_total": st["nrebuilds"]},
             "plain_one_at_a_time": {"value": plain, "unit": "particle-steps/s",
                                     "note": "the same systems, one handle each, run in turn"},
             "ensemble_over_plain": value / plain,
             "autotune": [{"blocks_per_sm": t[0][0], "cell_scale": t[0][1], "skin": t[0][2],
-                          "ms_per_step": t[1]} for t in table],
+                          "particle_threads": t[0][3], "ms_per_step": t[1]} for t in table],
             "clocks": cl}
     print(json.dumps(line))
 

@@ -165,6 +165,10 @@ int dem_set_ensemble(dem_handle *h, int nsys);
  * list is built, hence summation order (rounding only).  Used by the
  * ensemble autotuner. */
 int dem_set_tuning(dem_handle *h, int blocks_per_sm, double cell_scale);
+/* Threads per block of the per-particle kernel (force gather, gravity,
+ * primitive walls, nve/sphere; one particle per thread): 64, 128 or 256
+ * (default).  Results do not depend on it.  Used by the ensemble autotuner. */
+int dem_set_particle_threads(dem_handle *h, int threads);
 
 /* fix mesh/surface FILE type WALL_TYPE + fix wall/gran ... mesh n_meshes 1
  * meshes ID (src/fix_mesh_surface.cpp, src/fix_wall_gran.cpp:803-982):

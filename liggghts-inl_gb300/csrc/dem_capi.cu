@@ -560,6 +560,13 @@ int dem_set_tuning(dem_handle *h, int blocks_per_sm, double cell_scale) {
   return DEM_OK;
 }
 
+int dem_set_particle_threads(dem_handle *h, int threads) {
+  if (!h || (threads != 64 && threads != 128 && threads != 256)) return DEM_ERR_BAD_ARG;
+  h->lc.particle_threads = threads;
+  h->sys_gen++;  // the step graph is rebuilt with the new launch shape
+  return DEM_OK;
+}
+
 int dem_add_mesh(dem_handle *h, int ntri, const double *nodes, int wall_type, int rolling_model,
                  const unsigned char *edge_active, const unsigned char *corner_active, int *mesh_id) {
   if (!h || ntri < 1 || !nodes || wall_type < 1) return DEM_ERR_BAD_ARG;

@@ -2151,8 +2151,7 @@ int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t
 }
 
 template <int NORMAL>
-static void launch_particle_n(const Sys &s, int g, int mode, int shearupdate, cudaStream_t st) {
-  const int B = 256;
+static void launch_particle_n(const Sys &s, int g, int B, int mode, int shearupdate, cudaStream_t st) {
   switch (mode) {
     case kModeInitial: k_particle<NORMAL, false, false, true><<<g, B, 0, st>>>(s, shearupdate); break;
     case kModeGather: k_particle<NORMAL, true, false, false><<<g, B, 0, st>>>(s, shearupdate); break;
@@ -2162,9 +2161,12 @@ static void launch_particle_n(const Sys &s, int g, int mode, int shearupdate, cu
 }
 
 int launch_particle(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, cudaStream_t st) {
-  const int g = grid_for(s.nmax, 256, lc.max_grid);
-  if (s.normal == kHertz) launch_particle_n<kHertz>(s, g, mode, shearupdate, st);
-  else launch_particle_n<kHooke>(s, g, mode, shearupdate, st);
+  // one particle per thread; smaller blocks give the same number of threads
+  // in more, smaller blocks (each particle's sums do not depend on it)
+  const int B = lc.particle_threads;
+  const int g = grid_for(s.nmax, B, lc.max_grid * (256 / B));
+  if (s.normal == kHertz) launch_particle_n<kHertz>(s, g, B, mode, shearupdate, st);
+  else launch_particle_n<kHooke>(s, g, B, mode, shearupdate, st);
   return 1;
 }
 

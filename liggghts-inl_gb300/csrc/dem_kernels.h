@@ -7,7 +7,8 @@
 namespace gb300 {
 
 struct LaunchCfg {
-  int max_grid;  // grid-stride kernels never launch more blocks than this
+  int max_grid;              // grid-stride kernels never launch more blocks of 256 than this
+  int particle_threads = 256;  // threads per block of the per-particle kernel (64, 128, 256)
 };
 
 enum {

@@ -93,6 +93,7 @@ def load(build=True):
     L.dem_add_plane.argtypes = [P, I, ctypes.c_double, I, I, P]
     L.dem_add_plane_per_type.argtypes = [P, I, P, I, P]
     L.dem_set_tuning.argtypes = [P, I, ctypes.c_double]
+    L.dem_set_particle_threads.argtypes = [P, I]
     L.dem_set_ensemble.argtypes = [P, I]
     L.dem_upload_atoms.argtypes = [P, I] + [P] * 7
     L.dem_add_mesh.argtypes = [P, I, P, I, I, P, P, P]
@@ -188,8 +189,10 @@ class DemSystem:
             pt = np.ascontiguousarray(pos_t, dtype=np.float64)
             self._check(L.dem_add_plane_per_type(self.h, int(axis), _p(pt), int(roll), None))
         if case.get("tuning") is not None:
-            bps, cs = case["tuning"]
+            bps, cs = case["tuning"][0], case["tuning"][1]
             self._check(L.dem_set_tuning(self.h, int(bps), float(cs)))
+            if len(case["tuning"]) > 2 and case["tuning"][2] is not None:
+                self._check(L.dem_set_particle_threads(self.h, int(case["tuning"][2])))
         if case.get("ensemble"):
             self._check(L.dem_set_ensemble(self.h, int(case["ensemble"])))
         self._meshkeep = []

@@ -23,10 +23,11 @@ system beyond skin/2 rebuilds every system).  Each system therefore evolves
 exactly as a standalone run of the same model that rebuilds at those steps;
 the rebuild steps are the only coupling.
 
-The autotuner times short runs of the packed ensemble over launch shapes,
-neighbour-cell sizes (dem_set_tuning) and, when asked, the neighbour skin,
-and keeps the fastest.  Launch shape and cell size change no result beyond
-summation order.  The skin changes the rebuild schedule: a pair that
+The autotuner times short runs of the packed ensemble over launch shapes
+(blocks per SM, dem_set_tuning; threads per block of the per-particle
+kernel, dem_set_particle_threads), neighbour-cell sizes and, when asked, the
+neighbour skin, and keeps the fastest.  Launch shape and cell size change no
+result beyond summation order.  The skin changes the rebuild schedule: a pair that
 separates and touches again between two builds keeps its tangential
 history, one rebuilt in between starts afresh (src/neigh_gran.cpp carry-over
 rule), so a tuned skin gives an equally valid but not bit-identical run;
@@ -132,21 +133,23 @@ class Ensemble:
         self.sys.close()
 
 
-def autotune(systems, steps=30, blocks_per_sm=(4, 8, 16), cell_scale=(1.0, 1.25, 1.5), warm=5, skins=None):
+def autotune(systems, steps=30, blocks_per_sm=(4, 8, 16), cell_scale=(1.0, 1.25, 1.5), warm=5, skins=None,
+             particle_threads=(256,)):
     """Times `steps` steps of the packed ensemble for each (blocks_per_sm,
-    cell_scale[, skin]) and returns the fastest as (best, table); best is
-    (blocks_per_sm, cell_scale, skin) with skin None unless skins lists
-    candidates.  The timed steps include the rebuilds they trigger, so a
-    skin is judged by its rebuild rate as well as its list length."""
+    cell_scale, skin, particle_threads) and returns the fastest as (best,
+    table); best is (blocks_per_sm, cell_scale, skin, particle_threads) with
+    skin None unless skins lists candidates.  The timed steps include the
+    rebuilds they trigger, so a skin is judged by its rebuild rate as well as
+    its list length."""
     table = []
-    for bps, cs, sk in itertools.product(blocks_per_sm, cell_scale, skins or (None,)):
-        e = Ensemble(systems, tuning=(bps, cs), skin=sk)
+    for bps, cs, sk, pt in itertools.product(blocks_per_sm, cell_scale, skins or (None,), particle_threads):
+        e = Ensemble(systems, tuning=(bps, cs, pt), skin=sk)
         e.setup()
         e.step(warm)
         t0 = time.perf_counter()
         e.step(steps)
         ms = e.stats()["last_step_ms"]
-        table.append(((bps, cs, sk), ms / steps, time.perf_counter() - t0))
+        table.append(((bps, cs, sk, pt), ms / steps, time.perf_counter() - t0))
         e.close()
     best = min(table, key=lambda r: r[1])[0]
     return best, table

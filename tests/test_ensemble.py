@@ -77,3 +77,23 @@ def test_ensemble_systems_match_standalone_oracle():
             assert hm < 1e-9, (k, done, hm)
     assert e.stats()["nrebuilds"] == done + 1
     e.close()
+
+
+@pytest.mark.gpu
+def test_ensemble_launch_shapes_give_identical_results():
+    """The autotuner's launch-shape knobs (blocks per SM, threads per block of
+    the per-particle kernel) change no result: each particle's sums run in
+    one thread in a fixed order whatever the grid."""
+    from gb300dem import ensemble
+    sy = _systems(n=3)
+    out = []
+    for tuning in ((8, 1.0, 256), (4, 1.0, 128), (16, 1.0, 64)):
+        e = ensemble.Ensemble(sy, tuning=tuning)
+        e.setup()
+        e.step(30)
+        out.append([e.system_atoms(k) for k in range(len(sy))])
+        e.close()
+    for run in out[1:]:
+        for a, b in zip(run, out[0]):
+            for key in ("x", "v", "omega", "f", "torque"):
+                assert np.array_equal(a[key], b[key]), key
