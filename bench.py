@@ -19,6 +19,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -51,7 +52,7 @@ PROFILED_PER_ATOM = {
 def workload(name, scale=1.0, seed=2024):
     from gb300dem import workloads
     if name == "hopper1m":
-        # configs[1]: conical hopper (half-angle 30 deg, top radius 0.25 m,
+        # conical hopper discharge (half-angle 30 deg, top radius 0.25 m,
         # outlet radius 0.03 m, 256 x 64 quads = 32,768 triangles), outlet open,
         # radii U[0.8, 1.2] mm, rho 1500, E 1e7, e 0.5, mu 0.6, CDT rolling 0.3
         # on pairs and wall, dt 5e-7; the lowest 1M sites of a jittered lattice
@@ -62,14 +63,14 @@ def workload(name, scale=1.0, seed=2024):
             dt=5e-7, skin=5e-4, max_atoms=max(1000, int(round(1_000_000 * scale))),
             clearance=-1e-4, z_below=-0.02)
         desc = dict(workload="hopper1m", atoms=int(len(case["atoms"]["tag"])), triangles=32768,
-                    description="configs[1] conical hopper discharge: triangle-mesh cone "
+                    description="1M-sphere conical hopper discharge: triangle-mesh cone "
                                 "(32,768 triangles), outlet open, polydisperse Hertz/history + CDT "
                                 "rolling (pair and wall), jittered lattice (2.2 mm) filling the "
                                 "cone from the outlet up, dt 5e-7",
                     l2="state + neighbour list > L2 (129 MB); no flush needed")
         return case, desc
     if name == "column1m":
-        # configs[1] materials (r U[0.8,1.2] mm, rho 1500, E 1e7, e 0.5, mu 0.6,
+        # the hopper's materials (r U[0.8,1.2] mm, rho 1500, E 1e7, e 0.5, mu 0.6,
         # CDT 0.3), dense jittered lattice in a periodic column with a floor.
         nx = max(4, int(round(100 * scale ** (1 / 3))))
         case = workloads.lattice_case(
@@ -80,14 +81,14 @@ def workload(name, scale=1.0, seed=2024):
         desc = dict(workload="column1m", atoms=int(len(case["atoms"]["tag"])),
                     description="polydisperse Hertz/history + CDT rolling spheres, dense jittered "
                                 "lattice (2.2 mm, r 0.8-1.2 mm) in a periodic x/y column with a "
-                                "floor plane; configs[1] materials, dt 5e-7",
+                                "floor plane; the hopper's materials, dt 5e-7",
                     l2="state + neighbour list > L2 (129 MB); no flush needed")
         return case, desc
     if name == "fibres200k":
-        # configs[2] material: 20,000 fibres x 10 spheres (200k), r 0.5 mm,
+        # bonded-fibre compression material: 20,000 fibres x 10 spheres (200k), r 0.5 mm,
         # cohesion bond/nonlinear with radiusMultiplier 0.5, tsCreate 1 and
         # createDistance just above 2r, so intra-fibre touching pairs bond at
-        # step 1; dt 1e-7.  configs[2]'s 40 mm cube cannot hold 200k spheres
+        # step 1; dt 1e-7.  A 40 mm cube cannot hold 200k spheres
         # of r 0.5 mm (1.6x its volume), so the fibres lie in plywood layers
         # (workloads.fibre_bed_case) in a 40.8 x 40.8 mm periodic column on a
         # floor, without the moving top plate.
@@ -101,7 +102,7 @@ def workload(name, scale=1.0, seed=2024):
         case = workloads.fibre_bed_case(seed, max(100, int(round(200_000 * scale)) // 10 * 10), radius=r,
                                         bond=bp, dt=1e-7, skin=2e-4, vmax=0.05)
         desc = dict(workload="fibres200k", atoms=int(len(case["atoms"]["tag"])), fibres=case["nfibres"],
-                    description="configs[2] bonded fibres: 10-sphere fibres (r 0.5 mm) in plywood "
+                    description="200k bonded fibre spheres: 10-sphere fibres (r 0.5 mm) in plywood "
                                 "layers, Hertz/history between fibres, cohesion bond/nonlinear within "
                                 "(bonds created at step 1), periodic x/y column on a floor, dt 1e-7",
                     l2="state + neighbour list + 28-value bond histories > L2 (129 MB); no flush needed")
@@ -120,11 +121,15 @@ class Clocks:
 
     def __init__(self):
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+        # the samples of the timed region; BENCH_CLOCKS_CSV keeps them in a
+        # file of the caller's choice, else a temporary file is used
+        self.path = os.environ.get("BENCH_CLOCKS_CSV") or os.path.join(
+            tempfile.gettempdir(), "gb300dem_clocks_%d.csv" % os.getpid())
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            if os.path.dirname(self.path):
+                os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
                                        "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
@@ -439,7 +444,7 @@ def run_ensemble(args):
 
 
 def adjoint_case(seed=2024, n=20000):
-    """configs[4] adjoint: n spheres as the settling columns (r U[0.9, 1.1]
+    """Adjoint case: n spheres as the settling columns (r U[0.9, 1.1]
     mm, jittered 2.2 mm lattice above a floor, 0.05 x 0.05 x 0.3 m box
     periodic in x/y), one parameter set (E 1e7, e 0.6, mu 0.5), dt 1e-6"""
     from gb300dem import workloads
@@ -490,7 +495,7 @@ def run_adjoint(args):
             "n_gpus": 1, "steps": steps, "warmup": args.warmup, "higher_is_better": False,
             "dtype": "f64", "data": "synthetic (seeded)", "impl": "gb300",
             "config": {"workload": "adjoint%dk" % (n // 1000), "atoms": n, "segment": seg,
-                       "description": "configs[4]: settling-column spheres, one parameter set, "
+                       "description": "20k settling-column spheres, one parameter set, "
                                       "kinetic-energy loss, gradients w.r.t. E, e, mu and every radius"},
             "plain_forward_ms": plain_ms, "adjoint_forward_ms": t["forward_ms"],
             "adjoint_backward_ms": t["backward_ms"], "backward_over_forward": t["backward_ms"] / t["forward_ms"],
