@@ -346,7 +346,8 @@ const char *dem_version(void);
  * discrete timestep: Verlet::setup + N Verlet steps (src/verlet.cpp:281-389)
  * of FixNVESphere, PairGran Hertz + tangential history (no rolling; with
  * cohesion bond/nonlinear when dem_adjoint_set_bonds is called, else contact
- * distance factor 1), FixGravity and FixWallGran primitive planes, one atom type
+ * distance factor 1), FixGravity and FixWallGran primitive planes and static
+ * triangle meshes (dem_adjoint_add_mesh), one atom type
  * and one material (Yeff/Geff/betaeff of the material against itself,
  * src/global_properties.cpp).  Masses follow the radii: m = 4/3 pi r^3 rho.
  * The neighbour list is rebuilt every `segment` steps, after the drift of
@@ -395,6 +396,15 @@ int dem_adjoint_destroy(dem_adjoint *h);
  * gradients then include the bonds' forces, created, evolved and carried
  * across rebuilds as the main path does. */
 int dem_adjoint_set_bonds(dem_adjoint *h, const double *values, const dem_bond_settings *st);
+/* a static triangle-mesh wall (fix mesh/surface + fix wall/gran ... mesh) of
+ * the atoms' material, nodes[ntri][3][3] as dem_add_mesh; edge/corner
+ * activity NULL = derived from the topology.  At most 4, before
+ * dem_adjoint_set_state.  Contacts follow the reference's sphere-triangle
+ * resolution and FixContactHistoryMesh's history slots
+ * (src/tri_mesh_I.h:65-271, src/fix_contact_history_mesh_I.h:51-216); the
+ * gradients include them. */
+int dem_adjoint_add_mesh(dem_adjoint *h, int ntri, const double *nodes, const unsigned char *edge_active,
+                         const unsigned char *corner_active);
 /* initial state (host arrays): x, v, omega n*3, radius n (the radii define the
  * neighbour cells; runs may use radii up to 1 % larger) */
 int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *v, const double *omega,

@@ -64,6 +64,8 @@
 #include "adjoint_law.cuh"
 #include "dem_device.cuh"
 #include "dem_kernels.h"
+#include "dem_mesh_host.h"
+#include "mesh_device.cuh"
 
 using namespace gb300;
 
@@ -73,6 +75,16 @@ namespace {
 constexpr int kAB = 128;
 constexpr int kMaxGrid = 152 * 16;
 
+constexpr int kAMC = kMeshMaxCand;  // candidate triangles (= history slots) per atom and mesh
+constexpr int kAMeshes = 4;
+
+// one static triangle-mesh wall on the device (geometry of MeshHost)
+struct AMesh {
+  int ntri;
+  const double *tri;  // [t*kTriStride]
+  const int *meta, *cn_start, *cn_list;
+};
+
 struct AList {
   int np = 0;
   int *pi = nullptr, *pj = nullptr, *row = nullptr, *rev_start = nullptr, *rev = nullptr;
@@ -81,6 +93,9 @@ struct AList {
   uint8_t *flag = nullptr;  // kContact* bits; nonzero: the entry's history is carried
   double *shear = nullptr;  // [3*p+k], evolving
   double *bond = nullptr;   // [kBondValues*p+k], evolving (bonds only)
+  // mesh walls: candidates per (mesh, atom) at this build, ascending, and the
+  // slot each slot came from at the build (-1: emptied)
+  int *mcn = nullptr, *mcand = nullptr, *mmap = nullptr;
 };
 
 struct ADev {
@@ -123,7 +138,18 @@ struct ADev {
   double csz[3];
   int ncell;
   int *cell_of, *cell_count, *cell_start, *cell_fill, *order, *pcount;
-  int *err;  // [0]: an atom moved more than skin/2 from its build position
+  int *err;  // [0]: an atom moved more than skin/2 from its build position; [1]: mesh slots exceeded
+  // mesh walls: meshes; FixNeighlistMesh's neighbour threshold (static: skin/2)
+  int nmeshes;
+  AMesh mesh[kAMeshes];
+  double cutneighmax, mtskin;
+  // slot state per (mesh m, atom i), index b = m*n + i: triangle of each slot
+  // (-1 empty), slot histories, occupied slots, slots in use (candidates at
+  // the last build); candidates of the list in use
+  int *mst;     // [b*kAMC + u]
+  double *msh;  // [(b*kAMC + u)*3 + d]
+  int *mnp, *mns;
+  const int *mcn, *mcand;
 };
 
 __device__ __forceinline__ int a_cell_coord(const ADev &s, double x, int d) {
@@ -452,6 +478,368 @@ __device__ __forceinline__ bool wall_in(const ADev &s, const double *x, int w, i
   return true;
 }
 
+// adjoints of the run's state (the mesh reverse below and the reverse kernels)
+struct ABar {
+  double *xb, *vb, *wb, *Fb, *Tb, *rb, *mb, *sb, *wsb;
+  // per-entry VJP outputs of the pair law
+  double *pd, *pv, *pwi, *pwj, *pri, *prj, *pmi, *pmj, *pth;  // pth [4*p]: Y, G, beta, mu
+  double *bb;   // [kBondValues*p] adjoint of the bond history (bonds only)
+  double *wth;  // [4*i] wall parameter adjoints per atom
+  double *th;   // [4] accumulated parameter adjoints
+  double *msb;  // [(b*kAMC + u)*3 + d] adjoints of the mesh slot histories
+};
+
+// ------------------------------------------------------------- mesh walls
+// Static triangle-mesh walls (fix mesh/surface + wall/gran ... mesh): the
+// contact of one atom with its candidate triangles as the main path's
+// sequential mesh_contacts does it (FixWallGran::post_force_mesh,
+// src/fix_wall_gran.cpp:803-982; TriMesh::resolveTriSphereContactBary,
+// src/tri_mesh_I.h:65-271; FixContactHistoryMesh::handleContact,
+// coplanarContactAlready, cleanUpContacts, src/fix_contact_history_mesh_I.h:
+// 51-216), with the slot state per atom and mesh: the triangle of each
+// history slot (-1 empty), the slot histories and the count of occupied
+// slots; the slots in use are the first mcn (the candidate count).
+
+__device__ __forceinline__ bool amesh_coplanar(const AMesh &M, int a, int b) {
+  for (int q = M.cn_start[a]; q < M.cn_start[a + 1]; q++)
+    if (M.cn_list[q] == b) return true;
+  return false;
+}
+
+// the closest feature of a resolved contact, from resolve_tri_sphere's
+// outputs: face (barySign 7), corner (one barycentric weight 1) or edge (the
+// edge between the two nodes with weight); ax: the face normal or the edge's
+// unit vector.  d = centre - closest point then moves with the centre as
+// J = ax ax^T (face), I - ax ax^T (edge), I (corner).
+__device__ __forceinline__ int amesh_feature(const double *g, int bs, const double bary[3], double ax[3]) {
+  if (bs == 7) {
+    for (int k = 0; k < 3; k++) ax[k] = tri_sn(g)[k];
+    return 0;
+  }
+  for (int k = 0; k < 3; k++)
+    if (bary[k] == 1.0 && bary[(k + 1) % 3] == 0.0 && bary[(k + 2) % 3] == 0.0) {
+      ax[0] = ax[1] = ax[2] = 0.0;
+      return 2;
+    }
+  int e = 0;
+  for (int k = 0; k < 3; k++)
+    if (bary[(k + 2) % 3] == 0.0) e = k;  // nodes k and k+1 carry the weight
+  for (int k = 0; k < 3; k++) ax[k] = tri_ev(g, e)[k];
+  return 1;
+}
+
+__device__ __forceinline__ void amesh_contact_in(const ADev &s, int i, const double *vh, const double *wh,
+                                                 const double delta[3], const double hin[3], int upd, VjpIn &a) {
+  for (int k = 0; k < 3; k++) {
+    a.d[k] = -delta[k];
+    a.vr[k] = vh[3 * i + k];  // static mesh: no wall velocity
+    a.wi[k] = wh[3 * i + k];
+    a.wj[k] = 0.0;
+    a.sh[k] = hin[k];
+  }
+  a.ri = s.r[i];
+  a.rj = 0.0;
+  a.mi = s.m[i];
+  a.mj = 0.0;
+  a.Y = s.Y;
+  a.G = s.G;
+  a.beta = s.beta;
+  a.mu = s.mu;
+  a.dt = s.dt;
+  a.upd = upd != 0;
+  a.wall = true;
+  a.bonded = false;
+}
+
+// one evaluation of the slot logic and contact law for atom i and mesh m on
+// the slot state st/sh/np (updated in place); adds the forces to f/t.  rec
+// (if set) receives, per evaluated contact, what the reverse needs.
+struct AMeshRec {
+  int slot, copy, kind, fresh, band;
+  double hin[3], delta[3], ax[3];
+};
+
+__device__ inline int amesh_eval(const ADev &s, int m, int i, const double *x, const double *vh, const double *wh,
+                                 int upd, int *st, double *sh, int &np, double f[3], double t[3], AMeshRec *rec,
+                                 unsigned &keep, bool &bad) {
+  const AMesh &M = s.mesh[m];
+  const size_t base = (size_t)m * s.n + i;
+  const int nc = s.mcn[base];
+  const int *cand = s.mcand + base * kAMC;
+  const double xi[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+  const double radi = s.r[i];
+  const double cdm1 = s.cdf - 1.0;
+  int nr = 0;
+  keep = 0u;
+  for (int q = 0; q < nc; q++) {
+    const int tr = cand[q];
+    const double *g = M.tri + (size_t)tr * kTriStride;
+    double delta[3], bary[3];
+    int bs;
+    const double deltan = resolve_tri_sphere(g, M.meta[tr], radi, xi, delta, bary, bs);
+    if (deltan > s.cutneighmax) continue;
+    if (!(deltan <= 0 || deltan < cdm1 * radi)) continue;
+    int slot = -1, copy = -1;
+    bool fresh = false;
+    for (int u = 0; u < nc; u++)
+      if (st[u] == tr) {
+        slot = u;
+        break;
+      }
+    if (slot >= 0) {
+      keep |= 1u << slot;
+    } else {
+      const bool face = bs == 7;
+      if (face) {  // coplanarContactAlready
+        bool already = false;
+        for (int u = 0; u < nc; u++) {
+          const int p = st[u];
+          if (p >= 0 && p != tr && ((keep >> u) & 1u) && amesh_coplanar(M, p, tr)) already = true;
+        }
+        if (already) continue;
+      }
+      if (np >= nc) {
+        bad = true;
+        continue;
+      }
+      for (int u = 0; u < nc; u++)
+        if (st[u] == -1) {
+          slot = u;
+          break;
+        }
+      st[slot] = tr;
+      keep |= 1u << slot;
+      for (int d = 0; d < 3; d++) sh[3 * slot + d] = 0.0;
+      np++;
+      fresh = true;
+      if (face)  // checkCoplanarContactHistory: the last coplanar partner's history
+        for (int u = 0; u < nc; u++) {
+          const int p = st[u];
+          if (p >= 0 && p != tr && amesh_coplanar(M, p, tr)) {
+            copy = u;
+            for (int d = 0; d < 3; d++) sh[3 * slot + d] = sh[3 * u + d];
+          }
+        }
+    }
+    if (rec) {
+      AMeshRec &R = rec[nr];
+      R.slot = slot;
+      R.copy = copy;
+      R.fresh = fresh ? 1 : 0;
+      R.band = deltan > 0 ? 1 : 0;
+      R.kind = amesh_feature(g, bs, bary, R.ax);
+      for (int d = 0; d < 3; d++) {
+        R.hin[d] = sh[3 * slot + d];
+        R.delta[d] = delta[d];
+      }
+    }
+    nr++;
+    if (deltan > 0) {  // within the contact distance, apart: surfacesClose
+      for (int d = 0; d < 3; d++) sh[3 * slot + d] = 0.0;
+      continue;
+    }
+    VjpIn a;
+    amesh_contact_in(s, i, vh, wh, delta, sh + 3 * slot, upd, a);
+    LawState S;
+    double F[3], Ti[3], Tj[3], s3[3];
+    law_forward(a, S, F, Ti, Tj, s3);
+    for (int d = 0; d < 3; d++) {
+      f[d] += F[d];
+      t[d] += Ti[d];
+      if (upd) sh[3 * slot + d] = s3[d];
+    }
+  }
+  for (int u = 0; u < nc; u++)  // cleanUpContacts
+    if (!((keep >> u) & 1u)) {
+      if (st[u] > -1) np--;
+      st[u] = -1;
+      for (int d = 0; d < 3; d++) sh[3 * u + d] = 0.0;
+    }
+  return nr;
+}
+
+// forward of atom i against every mesh: forces into f/t; the slot state
+// before the evaluation goes to the tape (if set)
+__device__ inline void amesh_forward(const ADev &s, int i, const double *x, const double *vh, const double *wh,
+                                     int upd, double f[3], double t[3], int *tst, double *tsh, int *tnp) {
+  for (int m = 0; m < s.nmeshes; m++) {
+    const size_t base = (size_t)m * s.n + i;
+    int *st = s.mst + base * kAMC;
+    double *sh = s.msh + base * kAMC * 3;
+    int np = s.mnp[base];
+    if (tst) {
+      for (int u = 0; u < kAMC; u++) tst[base * kAMC + u] = st[u];
+      for (int u = 0; u < 3 * kAMC; u++) tsh[base * kAMC * 3 + u] = sh[u];
+      tnp[base] = np;
+    }
+    if (s.mcn[base] == 0) continue;
+    unsigned keep;
+    bool bad = false;
+    amesh_eval(s, m, i, x, vh, wh, upd, st, sh, np, f, t, nullptr, keep, bad);
+    if (bad) s.err[1] = 1;
+    s.mnp[base] = np;
+  }
+}
+
+// reverse of amesh_forward for atom i: Fb/Tb the adjoints of the atom's total
+// force and torque; the slot-history adjoints B.msb (of the state after the
+// evaluation) become those of the state before it (the tape's)
+__device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const double *x, const double *vh,
+                                 const double *wh, int upd, const int *tst, const double *tsh, const int *tnp,
+                                 const double Fb[3], const double Tb[3], double xb[3], double vb[3], double wb[3],
+                                 double &rb, double &mb, double th[4]) {
+  for (int m = 0; m < s.nmeshes; m++) {
+    const size_t base = (size_t)m * s.n + i;
+    const int nc = s.mcn[base];
+    if (nc == 0) continue;
+    int st[kAMC];
+    double sh[3 * kAMC];
+    for (int u = 0; u < kAMC; u++) st[u] = tst[base * kAMC + u];
+    for (int u = 0; u < 3 * kAMC; u++) sh[u] = tsh[base * kAMC * 3 + u];
+    int np = tnp[base];
+    AMeshRec rec[kAMC];
+    unsigned keep;
+    bool bad = false;
+    double f[3] = {0., 0., 0.}, t[3] = {0., 0., 0.};
+    const int nr = amesh_eval(s, m, i, x, vh, wh, upd, st, sh, np, f, t, rec, keep, bad);
+    double *hb = B.msb + base * kAMC * 3;
+    for (int u = 0; u < nc; u++)
+      if (!((keep >> u) & 1u))
+        for (int d = 0; d < 3; d++) hb[3 * u + d] = 0.0;  // cleared: no dependence on the value before
+    for (int r = nr - 1; r >= 0; r--) {
+      const AMeshRec &R = rec[r];
+      const int u = R.slot;
+      if (R.band) {
+        for (int d = 0; d < 3; d++) hb[3 * u + d] = 0.0;
+      } else {
+        VjpIn a;
+        amesh_contact_in(s, i, vh, wh, R.delta, R.hin, upd, a);
+        VjpBar bb;
+        for (int d = 0; d < 3; d++) {
+          bb.F[d] = Fb[d];
+          bb.Ti[d] = Tb[d];
+          bb.Tj[d] = 0.0;
+          bb.s3[d] = upd ? hb[3 * u + d] : 0.0;
+        }
+        law_vjp(a, bb);
+        for (int d = 0; d < 3; d++) hb[3 * u + d] = bb.sh[d] + (upd ? 0.0 : hb[3 * u + d]);
+        // d = centre - closest point
+        if (R.kind == 2) {
+          for (int d = 0; d < 3; d++) xb[d] += bb.d[d];
+        } else {
+          const double pr = R.ax[0] * bb.d[0] + R.ax[1] * bb.d[1] + R.ax[2] * bb.d[2];
+          for (int d = 0; d < 3; d++) xb[d] += R.kind == 0 ? pr * R.ax[d] : bb.d[d] - pr * R.ax[d];
+        }
+        for (int d = 0; d < 3; d++) {
+          vb[d] += bb.vr[d];
+          wb[d] += bb.wi[d];
+        }
+        rb += bb.ri;
+        mb += bb.mi;
+        th[0] += bb.Y;
+        th[1] += bb.G;
+        th[2] += bb.beta;
+        th[3] += bb.mu;
+      }
+      if (R.fresh) {  // the slot was set to zero, or to a coplanar partner's history
+        if (R.copy >= 0)
+          for (int d = 0; d < 3; d++) hb[3 * R.copy + d] += hb[3 * u + d];
+        for (int d = 0; d < 3; d++) hb[3 * u + d] = 0.0;
+      }
+    }
+  }
+}
+
+// FixContactHistoryMesh::sort_contacts (pre_exchange), then the candidates of
+// FixNeighlistMesh::pre_force (TriMesh::resolveTriSphereNeighbuild, every
+// triangle in ascending order), cleanUpContactJumps and the re-paging of the
+// slots, at the positions of a build.  map[s'] receives the slot each new
+// slot came from (-1: emptied), for the reverse pass.
+__device__ __forceinline__ void amesh_swap(int *st, double *sh, int *orig, int a, int b) {
+  const int t = st[a];
+  st[a] = st[b];
+  st[b] = t;
+  const int o = orig[a];
+  orig[a] = orig[b];
+  orig[b] = o;
+  for (int d = 0; d < 3; d++) {
+    const double h = sh[3 * a + d];
+    sh[3 * a + d] = sh[3 * b + d];
+    sh[3 * b + d] = h;
+  }
+}
+
+__global__ void ka_mesh_build(ADev s, int *mcn, int *mcand, int *map) {
+  AGRID(i, s.n) {
+    const double xi[3] = {s.x[3 * i], s.x[3 * i + 1], s.x[3 * i + 2]};
+    const double rS = s.r[i] * s.cdf;
+    for (int m = 0; m < s.nmeshes; m++) {
+      const AMesh &M = s.mesh[m];
+      const size_t base = (size_t)m * s.n + i;
+      int *st = s.mst + base * kAMC;
+      double *sh = s.msh + base * kAMC * 3;
+      int np = s.mnp[base];
+      const int nn = s.mns[base];
+      int orig[kAMC];
+      for (int u = 0; u < kAMC; u++) orig[u] = u;
+      int fe, lf;
+      do {  // sort_contacts
+        fe = lf = -1;
+        for (int j = 0; j < nn; j++) {
+          if (fe == -1 && st[j] == -1) fe = j;
+          if (st[j] >= 0) lf = j;
+        }
+        if (fe > -1 && lf > -1 && fe < lf) amesh_swap(st, sh, orig, fe, lf);
+      } while (fe > -1 && lf > -1 && fe < lf);
+      int nc = 0;
+      int *cand = mcand + base * kAMC;
+      for (int tr = 0; tr < M.ntri; tr++) {
+        if (!tri_sphere_neighbuild(M.tri + (size_t)tr * kTriStride, rS, xi, s.mtskin)) continue;
+        if (nc == kAMC) {
+          s.err[1] = 1;
+          break;
+        }
+        cand[nc++] = tr;
+      }
+      int ip = 0;  // cleanUpContactJumps
+      while (ip < np) {
+        const int tr = st[ip];
+        bool listed = false;
+        for (int q = 0; q < nc; q++) listed |= (cand[q] == tr);
+        if (!listed) {
+          st[ip] = -1;
+          orig[ip] = -1;
+          for (int d = 0; d < 3; d++) sh[3 * ip + d] = 0.0;
+          amesh_swap(st, sh, orig, ip, np - 1);
+          np--;
+        } else {
+          ip++;
+        }
+      }
+      for (int q = np; q < nc; q++) {
+        st[q] = -1;
+        orig[q] = -1;
+        for (int d = 0; d < 3; d++) sh[3 * q + d] = 0.0;
+      }
+      s.mnp[base] = np;
+      s.mns[base] = nc;
+      mcn[base] = nc;
+      for (int u = 0; u < kAMC; u++) map[base * kAMC + u] = u < nc ? orig[u] : -1;
+    }
+  }
+}
+
+// slot-history adjoints back through a build: old[orig] += new[s']
+__global__ void kb_mesh_uncarry(int cnt, const int *map, const double *hb_new, double *hb_old) {
+  AGRID(b, cnt) {  // one (mesh, atom) each
+    for (int u = 0; u < kAMC; u++) {
+      const int o = map[(size_t)b * kAMC + u];
+      if (o >= 0)
+        for (int d = 0; d < 3; d++) hb_old[((size_t)b * kAMC + o) * 3 + d] += hb_new[((size_t)b * kAMC + u) * 3 + d];
+    }
+  }
+}
+
 // pair forces of the current state (vh, wh: the velocities the forces see)
 // at step ntimestep; tape_sh/tape_bh receive the history before the update.
 // The pass follows k_pair<..., BOND> of the main path: touching entries run
@@ -532,7 +920,7 @@ __global__ void __launch_bounds__(kAB) ka_pair_force(ADev s, const double *vh, c
 // tape_F/tape_T (if set) a copy of the forces and torques.
 __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const double *wh, int upd,
                                                  int final_kick, double *tape_ws, double *wallF, double *tape_F,
-                                                 double *tape_T) {
+                                                 double *tape_T, int *tape_mst, double *tape_msh, int *tape_mnp) {
   __shared__ int q[kAB];
   __shared__ int wcnt[kAB / 32];
   __shared__ double sF[3][kAB], sT[3][kAB];
@@ -599,6 +987,7 @@ __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const
       __syncthreads();
     }
     if (valid) {
+      if (s.nmeshes) amesh_forward(s, i, s.x, vh, wh, upd, f, t, tape_mst, tape_msh, tape_mnp);  // after the planes
       const double a = s.ka[i], b = s.kb[i];
       for (int k = 0; k < 3; k++) {
         s.F[3 * i + k] = f[k];
@@ -657,14 +1046,6 @@ __global__ void ka_kick_drift(ADev s, const double *xref, int wrap, double *tx, 
 }
 
 // ------------------------------------------------------------------ backward
-struct ABar {
-  double *xb, *vb, *wb, *Fb, *Tb, *rb, *mb, *sb, *wsb;
-  // per-entry VJP outputs of the pair law
-  double *pd, *pv, *pwi, *pwj, *pri, *prj, *pmi, *pmj, *pth;  // pth [4*p]: Y, G, beta, mu
-  double *bb;   // [kBondValues*p] adjoint of the bond history (bonds only)
-  double *wth;  // [4*i] wall parameter adjoints per atom
-  double *th;   // [4] accumulated parameter adjoints
-};
 
 // gravity and walls of one force evaluation at positions x; vh/wh the
 // velocities the forces saw, ws_before the wall history before it; seed adds
@@ -674,7 +1055,8 @@ struct ABar {
 // B.wth.
 __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x, const double *vh,
                                                 const double *wh, const double *ws_before, int upd, int seed_w,
-                                                double seed, const double *Fn1, const double *Tn1) {
+                                                double seed, const double *Fn1, const double *Tn1,
+                                                const int *tmst, const double *tmsh, const int *tmnp) {
   __shared__ int q[kAB];
   __shared__ int wcnt[kAB / 32];
   ABLOCKS(base, s.n) {
@@ -734,6 +1116,23 @@ __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x,
         B.wth[4 * ii + 3] += bb.mu;
       }
       __syncthreads();
+    }
+    if (valid && s.nmeshes) {  // mesh walls, per atom (the planes' writes are behind the barrier)
+      double Fb[3], Tb[3], xb[3] = {0., 0., 0.}, vb[3] = {0., 0., 0.}, wb[3] = {0., 0., 0.};
+      double rb = 0.0, mb = 0.0, th[4] = {0., 0., 0., 0.};
+      for (int k = 0; k < 3; k++) {
+        Fb[k] = B.Fb[3 * i + k];
+        Tb[k] = B.Tb[3 * i + k];
+      }
+      amesh_vjp(s, B, i, x, vh, wh, upd, tmst, tmsh, tmnp, Fb, Tb, xb, vb, wb, rb, mb, th);
+      for (int k = 0; k < 3; k++) {
+        B.xb[3 * i + k] += xb[k];
+        B.vb[3 * i + k] += vb[k];
+        B.wb[3 * i + k] += wb[k];
+      }
+      B.rb[i] += rb;
+      B.mb[i] += mb;
+      for (int k = 0; k < 4; k++) B.wth[4 * i + k] += th[k];
     }
   }
 }
@@ -1069,12 +1468,16 @@ struct Tape {
   double *x = nullptr, *vh = nullptr, *wh = nullptr, *F = nullptr, *T = nullptr, *ws = nullptr;
   double *sh = nullptr, *bh = nullptr;
   float4 *xf = nullptr;
+  int *mst = nullptr, *mnp = nullptr;  // mesh slot state before each evaluation
+  double *msh = nullptr;
   size_t ps = 0;
 };
 
 struct Checkpoint {
   double *x, *v, *w, *F, *T, *ws;  // state before the segment's first drift
   double *sh0, *bh0;               // the list's history as carried at the build
+  int *mst0, *mnp0;                // mesh slot state at the segment's first force evaluation
+  double *msh0;
   AList L;
   Tape tape;                       // recorded in the forward pass (tape mode), else replayed
 };
@@ -1118,6 +1521,13 @@ int build_list(dem_adjoint *h, AList &L, const AList &old) {
     ka_carry<<<grid_of(np), kAB, 0, st>>>(s, L, old);
   }
   ka_rev_sort<<<grid_of(n), kAB, 0, st>>>(n, L.rev_start, L.rev);
+  if (s.nmeshes) {
+    const size_t nb = (size_t)s.nmeshes * n;
+    AGET(h, L.mcn, int, nb);
+    AGET(h, L.mcand, int, nb * kAMC);
+    AGET(h, L.mmap, int, nb * kAMC);
+    ka_mesh_build<<<grid_of(n), kAB, 0, st>>>(s, L.mcn, L.mcand, L.mmap);
+  }
   ATRY(h, cudaGetLastError());
   return DEM_OK;
 }
@@ -1134,6 +1544,8 @@ void use_list(dem_adjoint *h, const AList &L, double *shear, double *bond) {
   s.rev_start = L.rev_start;
   s.rev = L.rev;
   s.shear = shear;
+  s.mcn = L.mcn;
+  s.mcand = L.mcand;
 }
 
 int ensure_pairs(dem_adjoint *h, int np) {
@@ -1165,13 +1577,15 @@ void derive(double E, double nu, double e, double &Y, double &G, double &beta, d
 
 void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, long long ntimestep,
                 double *tape_sh, double *tape_bh, double *tape_ws, int final_kick, double *wallF,
-                double *tape_F = nullptr, double *tape_T = nullptr) {
+                double *tape_F = nullptr, double *tape_T = nullptr, int *tape_mst = nullptr,
+                double *tape_msh = nullptr, int *tape_mnp = nullptr) {
   ADev &s = h->s;
   if (s.np > 0 && s.bonds)
     ka_pair_force<true><<<grid_of(s.np), kAB, 0, h->st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
   else if (s.np > 0)
     ka_pair_force<false><<<grid_of(s.np), kAB, 0, h->st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
-  ka_gather<<<grid_of(h->n), kAB, 0, h->st>>>(s, vh, wh, upd, final_kick, tape_ws, wallF, tape_F, tape_T);
+  ka_gather<<<grid_of(h->n), kAB, 0, h->st>>>(s, vh, wh, upd, final_kick, tape_ws, wallF, tape_F, tape_T, tape_mst,
+                                               tape_msh, tape_mnp);
 }
 
 void pairs_vjp(dem_adjoint *h, const double *x, const float4 *xf, const double *vh, const double *wh,
@@ -1239,7 +1653,42 @@ int dem_adjoint_create(const dem_adjoint_config *cfg, dem_adjoint **out) {
   s.dtfrot = s.dtf / 0.4;
   s.bonds = 0;
   s.cdf = 1.0;
+  s.nmeshes = 0;
   *out = h;
+  return DEM_OK;
+}
+
+int dem_adjoint_add_mesh(dem_adjoint *h, int ntri, const double *nodes, const unsigned char *edge_active,
+                         const unsigned char *corner_active) {
+  if (!h || h->n || ntri < 1 || !nodes) return DEM_ERR_BAD_ARG;
+  ADev &s = h->s;
+  if (s.nmeshes >= kAMeshes) {
+    h->err = "at most 4 meshes";
+    return DEM_ERR_BAD_ARG;
+  }
+  MeshHost mh;
+  const int rc = mesh_prepare(ntri, nodes, edge_active, corner_active, mh);
+  if (rc != DEM_OK) {
+    h->err = "mesh preparation failed";
+    return rc;
+  }
+  double *tri;
+  int *meta, *cs, *cl;
+  ATRY(h, dmalloc(h->owned, &tri, mh.tri.size()));
+  ATRY(h, dmalloc(h->owned, &meta, mh.meta.size()));
+  ATRY(h, dmalloc(h->owned, &cs, mh.cn_start.size()));
+  ATRY(h, dmalloc(h->owned, &cl, std::max<size_t>(1, mh.cn_list.size())));
+  ATRY(h, cudaMemcpy(tri, mh.tri.data(), mh.tri.size() * sizeof(double), cudaMemcpyHostToDevice));
+  ATRY(h, cudaMemcpy(meta, mh.meta.data(), mh.meta.size() * sizeof(int), cudaMemcpyHostToDevice));
+  ATRY(h, cudaMemcpy(cs, mh.cn_start.data(), mh.cn_start.size() * sizeof(int), cudaMemcpyHostToDevice));
+  if (!mh.cn_list.empty())
+    ATRY(h, cudaMemcpy(cl, mh.cn_list.data(), mh.cn_list.size() * sizeof(int), cudaMemcpyHostToDevice));
+  AMesh &M = s.mesh[s.nmeshes++];
+  M.ntri = ntri;
+  M.tri = tri;
+  M.meta = meta;
+  M.cn_start = cs;
+  M.cn_list = cl;
   return DEM_OK;
 }
 
@@ -1345,6 +1794,19 @@ int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *
   const size_t W3 = 3 * (size_t)std::max(1, s.nplanes) * n;
   ATRY(h, dmalloc(h->owned, &s.ws, W3));
   ATRY(h, dmalloc(h->owned, &s.xf, (size_t)n));
+  // mesh walls: the neighbour cutoff (Neighbor::cutneighmax, (maxrad_i +
+  // maxrad_j) cdf + skin) bounds the contacts considered, and static meshes
+  // take candidates within r cdf + skin/2 (FixNeighlistMesh::pre_force)
+  s.cutneighmax = 2.0 * rmax * s.cdf + s.skin;
+  s.mtskin = 0.5 * s.skin;
+  if (s.nmeshes) {
+    const size_t nb = (size_t)s.nmeshes * n;
+    ATRY(h, dmalloc(h->owned, &s.mst, nb * kAMC));
+    ATRY(h, dmalloc(h->owned, &s.msh, nb * kAMC * 3));
+    ATRY(h, dmalloc(h->owned, &s.mnp, nb));
+    ATRY(h, dmalloc(h->owned, &s.mns, nb));
+    ATRY(h, dmalloc(h->owned, &h->B.msb, nb * kAMC * 3));
+  }
   // the FP32 mirror's margin: coordinates and image shifts below X in size
   // round by at most 2^-24 X each, a difference by 4 such roundings; 4e-6 X
   // is more than ten times the bound on the distance error
@@ -1414,6 +1876,13 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   copyd(h, s.v, h->v0, S3);
   copyd(h, s.w, h->w0, S3);
   ATRY(h, cudaMemsetAsync(s.ws, 0, W3 * sizeof(double), st));
+  const size_t NBM = (size_t)s.nmeshes * n;  // (mesh, atom) slot-state records
+  if (s.nmeshes) {  // no mesh contacts before the setup pass
+    ATRY(h, cudaMemsetAsync(s.mst, 0xff, NBM * kAMC * sizeof(int), st));
+    ATRY(h, cudaMemsetAsync(s.msh, 0, NBM * kAMC * 3 * sizeof(double), st));
+    ATRY(h, cudaMemsetAsync(s.mnp, 0, NBM * sizeof(int), st));
+    ATRY(h, cudaMemsetAsync(s.mns, 0, NBM * sizeof(int), st));
+  }
   ATRY(h, cudaMemsetAsync(s.err, 0, 4 * sizeof(int), st));
   ATRY(h, cudaEventRecord(h->ev[0], st));
   // ------------------------------------------------------------ forward
@@ -1454,6 +1923,14 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       copyd(h, h->xref, s.x, S3);
       AGET(h, c.sh0, double, 3 * (size_t)c.L.np);
       copyd(h, c.sh0, c.L.shear, 3 * (size_t)c.L.np);
+      if (s.nmeshes) {
+        AGET(h, c.mst0, int, NBM * kAMC);
+        AGET(h, c.msh0, double, NBM * kAMC * 3);
+        AGET(h, c.mnp0, int, NBM);
+        ATRY(h, cudaMemcpyAsync(c.mst0, s.mst, NBM * kAMC * sizeof(int), cudaMemcpyDeviceToDevice, st));
+        copyd(h, c.msh0, s.msh, NBM * kAMC * 3);
+        ATRY(h, cudaMemcpyAsync(c.mnp0, s.mnp, NBM * sizeof(int), cudaMemcpyDeviceToDevice, st));
+      }
       if (s.bonds) {
         AGET(h, c.bh0, double, (size_t)kBondValues * c.L.np);
         copyd(h, c.bh0, c.L.bond, (size_t)kBondValues * c.L.np);
@@ -1476,6 +1953,11 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       AGET(h, T.T, double, S3 * nst);
       AGET(h, T.ws, double, W3 * nst);
       AGET(h, T.xf, float4, (size_t)n * nst);
+      if (s.nmeshes) {
+        AGET(h, T.mst, int, NBM * kAMC * nst);
+        AGET(h, T.msh, double, NBM * kAMC * 3 * nst);
+        AGET(h, T.mnp, int, NBM * nst);
+      }
     }
     copyd(h, c.x, s.x, S3);
     copyd(h, c.v, s.v, S3);
@@ -1500,6 +1982,14 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
         copyd(h, h->xref, s.x, S3);
         AGET(h, c.sh0, double, 3 * (size_t)c.L.np);
         copyd(h, c.sh0, c.L.shear, 3 * (size_t)c.L.np);
+        if (s.nmeshes) {
+          AGET(h, c.mst0, int, NBM * kAMC);
+          AGET(h, c.msh0, double, NBM * kAMC * 3);
+          AGET(h, c.mnp0, int, NBM);
+          ATRY(h, cudaMemcpyAsync(c.mst0, s.mst, NBM * kAMC * sizeof(int), cudaMemcpyDeviceToDevice, st));
+          copyd(h, c.msh0, s.msh, NBM * kAMC * 3);
+          ATRY(h, cudaMemcpyAsync(c.mnp0, s.mnp, NBM * sizeof(int), cudaMemcpyDeviceToDevice, st));
+        }
         if (s.bonds) {
           AGET(h, c.bh0, double, (size_t)kBondValues * c.L.np);
           copyd(h, c.bh0, c.L.bond, (size_t)kBondValues * c.L.np);
@@ -1510,15 +2000,19 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
         AGET(h, T.sh, double, 3 * T.ps * nst);
         if (s.bonds) AGET(h, T.bh, double, kBondValues * T.ps * nst);
       }
+      const bool mrec = rec && s.nmeshes;
       force_pass(h, s.v, s.w, 1, t, rec ? T.sh + 3 * T.ps * q : nullptr,
                  rec && s.bonds ? T.bh + kBondValues * T.ps * q : nullptr, rec ? T.ws + W3 * q : nullptr, 1,
-                 t == nsteps ? h->wallF : nullptr, rec ? T.F + S3 * q : nullptr, rec ? T.T + S3 * q : nullptr);
+                 t == nsteps ? h->wallF : nullptr, rec ? T.F + S3 * q : nullptr, rec ? T.T + S3 * q : nullptr,
+                 mrec ? T.mst + NBM * kAMC * q : nullptr, mrec ? T.msh + NBM * kAMC * 3 * q : nullptr,
+                 mrec ? T.mnp + NBM * q : nullptr);
     }
     maxnp = std::max(maxnp, c.L.np);
   }
   ATRY(h, cudaGetLastError());
-  int flag = 0;
+  int flag = 0, mflag = 0;
   ATRY(h, cudaMemcpyAsync(&flag, s.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ATRY(h, cudaMemcpyAsync(&mflag, s.err + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
   std::vector<double> xf(S3), vf(S3), wf(S3), wallf(W3);
   ATRY(h, cudaMemcpyAsync(xf.data(), s.x, S3 * sizeof(double), cudaMemcpyDeviceToHost, st));
   ATRY(h, cudaMemcpyAsync(vf.data(), s.v, S3 * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -1535,6 +2029,10 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   h->last_maxnp = maxnp;
   if (flag) {
     h->err = "an atom moved more than skin/2 from its position at the list build: use shorter segments or a larger skin";
+    return DEM_ERR_BAD_ARG;
+  }
+  if (mflag) {
+    h->err = "an atom has more candidate mesh triangles (or contacts) than its history slots";
     return DEM_ERR_BAD_ARG;
   }
   // loss of the final state
@@ -1600,6 +2098,25 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     AGET(h, shared.sh, double, 3 * (size_t)maxnp * seg);
     AGET(h, shared.xf, float4, (size_t)n * seg);
     if (s.bonds) AGET(h, shared.bh, double, kBondValues * (size_t)maxnp * seg);
+    if (s.nmeshes) {
+      AGET(h, shared.mst, int, NBM * kAMC * seg);
+      AGET(h, shared.msh, double, NBM * kAMC * 3 * seg);
+      AGET(h, shared.mnp, int, NBM * seg);
+    }
+  }
+  // the mesh slot state before the setup pass (empty) and the slot-history
+  // adjoints of the previous list at a build
+  int *mst_e = nullptr, *mnp_e = nullptr;
+  double *msh_e = nullptr, *msb_prev = nullptr;
+  if (s.nmeshes) {
+    AGET(h, mst_e, int, NBM * kAMC);
+    AGET(h, mnp_e, int, NBM);
+    AGET(h, msh_e, double, NBM * kAMC * 3);
+    AGET(h, msb_prev, double, NBM * kAMC * 3);
+    ATRY(h, cudaMemsetAsync(mst_e, 0xff, NBM * kAMC * sizeof(int), st));
+    ATRY(h, cudaMemsetAsync(mnp_e, 0, NBM * sizeof(int), st));
+    ATRY(h, cudaMemsetAsync(msh_e, 0, NBM * kAMC * 3 * sizeof(double), st));
+    ATRY(h, cudaMemsetAsync(B.msb, 0, NBM * kAMC * 3 * sizeof(double), st));
   }
   double *shr, *sb_prev, *tws0;
   AGET(h, shr, double, 3 * (size_t)maxnp);
@@ -1626,6 +2143,11 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       copyd(h, s.ws, c.ws, W3);
       copyd(h, shr, c.sh0, 3 * (size_t)c.L.np);
       if (s.bonds) copyd(h, bhr, c.bh0, (size_t)kBondValues * c.L.np);
+      if (s.nmeshes) {
+        ATRY(h, cudaMemcpyAsync(s.mst, c.mst0, NBM * kAMC * sizeof(int), cudaMemcpyDeviceToDevice, st));
+        copyd(h, s.msh, c.msh0, NBM * kAMC * 3);
+        ATRY(h, cudaMemcpyAsync(s.mnp, c.mnp0, NBM * sizeof(int), cudaMemcpyDeviceToDevice, st));
+      }
     }
     use_list(h, c.L, shr, bhr);
     for (int t = first; t <= last && !recorded; t++) {
@@ -1634,7 +2156,8 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
                                                 T.vh + S3 * q, T.wh + S3 * q, T.xf + (size_t)n * q);
       force_pass(h, T.vh + S3 * q, T.wh + S3 * q, 1, t, T.sh + 3 * PS * q,
                  s.bonds ? T.bh + kBondValues * PS * q : nullptr, T.ws + W3 * q, 1, nullptr, T.F + S3 * q,
-                 T.T + S3 * q);
+                 T.T + S3 * q, s.nmeshes ? T.mst + NBM * kAMC * q : nullptr,
+                 s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr, s.nmeshes ? T.mnp + NBM * q : nullptr);
     }
     // reverse over the segment's steps; the pair parameter adjoints of the
     // segment's list are summed per entry over its steps, then reduced
@@ -1643,7 +2166,10 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       const int q = t - first;
       const double *xs = T.x + S3 * q, *vh = T.vh + S3 * q, *wh = T.wh + S3 * q;
       kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, xs, vh, wh, T.ws + W3 * q, 1, t == nsteps ? lw : -1,
-                                           t == nsteps ? fw_seed : 0.0, T.F + S3 * q, T.T + S3 * q);
+                                           t == nsteps ? fw_seed : 0.0, T.F + S3 * q, T.T + S3 * q,
+                                           s.nmeshes ? T.mst + NBM * kAMC * q : nullptr,
+                                           s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr,
+                                           s.nmeshes ? T.mnp + NBM * q : nullptr);
       if (s.np > 0)
         pairs_vjp(h, xs, T.xf + (size_t)n * q, vh, wh, T.sh + 3 * PS * q,
                   s.bonds ? T.bh + kBondValues * PS * q : nullptr, 1, t);
@@ -1664,6 +2190,11 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       }
       copyd(h, B.sb, sb_prev, 3 * (size_t)po.np);
       if (s.bonds) copyd(h, B.bb, bb_prev, (size_t)kBondValues * po.np);
+      if (s.nmeshes) {
+        ATRY(h, cudaMemsetAsync(msb_prev, 0, NBM * kAMC * 3 * sizeof(double), st));
+        kb_mesh_uncarry<<<grid_of((long)NBM), kAB, 0, st>>>((int)NBM, c.L.mmap, B.msb, msb_prev);
+        copyd(h, B.msb, msb_prev, NBM * kAMC * 3);
+      }
     }
   }
   {  // Verlet::setup force pass: initial state, zero history, no update
@@ -1672,7 +2203,8 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     ATRY(h, cudaMemsetAsync(shr, 0, 3 * (size_t)maxnp * sizeof(double), st));
     if (s.bonds) ATRY(h, cudaMemsetAsync(bhr, 0, NB * sizeof(double), st));
     use_list(h, c.L, shr, bhr);
-    kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, c.x, c.v, c.w, tws0, 0, -1, 0.0, nullptr, nullptr);
+    kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, c.x, c.v, c.w, tws0, 0, -1, 0.0, nullptr, nullptr, mst_e, msh_e,
+                                         mnp_e);
     pairs_vjp(h, c.x, nullptr, c.v, c.w, shr, bhr, 0, 0);
     kb_gather_kick<<<grid_of(n), kAB, 0, st>>>(s, B, nullptr, nullptr, 0);
     accumulate(h, B.pth, s.np);  // segment 0's steps and the setup pass

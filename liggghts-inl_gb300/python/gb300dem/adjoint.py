@@ -1,8 +1,8 @@
 """Discrete adjoint of the sphere-DEM timestep (dem_adjoint_* in the C ABI).
 
 ``DemAdjoint`` owns one adjoint handle: an initial granular state (one atom
-type, one material, primitive planes, gravity, optionally cohesion
-bond/nonlinear) and a run length.  ``loss()``
+type, one material, primitive planes, static triangle meshes, gravity,
+optionally cohesion bond/nonlinear) and a run length.  ``loss()``
 runs the forward model only; ``gradient()`` also runs the backward pass and
 returns d(loss)/d(E, restitution, friction, radius_i).  ``AdjointLoss`` is a
 ``torch.autograd.Function`` over the same call, so the parameters can sit in
@@ -45,6 +45,7 @@ def _bind(L):
     L.dem_adjoint_destroy.argtypes = [P]
     L.dem_adjoint_set_state.argtypes = [P, I, P, P, P, P]
     L.dem_adjoint_set_bonds.argtypes = [P, P, ctypes.POINTER(api.DemBondSettings)]
+    L.dem_adjoint_add_mesh.argtypes = [P, I, P, P, P]
     L.dem_adjoint_forward.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P]
     L.dem_adjoint_gradient.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P, P, P, P, P]
     L.dem_adjoint_download.argtypes = [P, P, P, P]
@@ -80,8 +81,11 @@ class DemAdjoint:
             raise ValueError("the adjoint covers one atom type")
         if case.get("normal_model", 0) != 0 or case.get("rolling_model", 0) != 0:
             raise ValueError("the adjoint covers Hertz without rolling friction")
-        if case.get("meshes"):
-            raise ValueError("mesh walls are not covered by the adjoint")
+        for m in case.get("meshes", []):
+            if m.get("vel") is not None or m.get("rotate") is not None:
+                raise ValueError("the adjoint covers static meshes")
+            if int(m["wall_type"]) != 1 or int(m.get("rolling", 0)) != 0:
+                raise ValueError("the adjoint's meshes are of the atoms' material (wall type 1), no rolling")
         bonded = case.get("cohesion_model", 0) == 1
         if float(case.get("cdf", 1.0)) != 1.0:
             raise ValueError("the adjoint takes the contact distance factor of its bonds, else 1")
@@ -120,6 +124,14 @@ class DemAdjoint:
             for k in api.BOND_FLAGS:
                 setattr(st, k, int(b["settings"][k]))
             self._call("dem_adjoint_set_bonds", self.h, api._p(vals), ctypes.byref(st))
+        self._meshkeep = []
+        for m in case.get("meshes", []):
+            nodes = _f64(m["nodes"])
+            ea, ca = m.get("edge_active"), m.get("corner_active")
+            ea = np.ascontiguousarray(ea, dtype=np.uint8) if ea is not None else None
+            ca = np.ascontiguousarray(ca, dtype=np.uint8) if ca is not None else None
+            self._meshkeep += [nodes, ea, ca]
+            self._call("dem_adjoint_add_mesh", self.h, len(nodes), api._p(nodes), api._p(ea), api._p(ca))
         a = case["atoms"]
         self.n = len(a["radius"])
         self.radius = _f64(a["radius"]).copy()

@@ -196,14 +196,17 @@ def test_adjoint_segment_length_and_determinism():
     eng.close()
 
 
-@pytest.mark.parametrize("bonded", [False, True])
-def test_adjoint_recorded_and_replayed_tapes_agree(bonded):
+@pytest.mark.parametrize("model", ["plain", "bonded", "mesh"])
+def test_adjoint_recorded_and_replayed_tapes_agree(model):
     """The backward pass on a record taken in the forward pass and on one
     replayed from the sqrt(N) checkpoints: the same gradients bit for bit."""
     from gb300dem.adjoint import DemAdjoint
-    if bonded:
+    if model == "bonded":
         import test_adjoint_bonds
         c = test_adjoint_bonds._case(law="full")
+    elif model == "mesh":
+        import test_adjoint_mesh
+        c = test_adjoint_mesh._case(frict=0.9, floor="gapped")
     else:
         c = _case()
     eng = DemAdjoint(c)
