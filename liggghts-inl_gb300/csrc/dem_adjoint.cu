@@ -1,6 +1,6 @@
 // Discrete adjoint of the sphere-DEM timestep (Hertz + tangential history,
-// cohesion bond/nonlinear, primitive planes, gravity, nve/sphere) with
-// sqrt(N) checkpointing.
+// cohesion bond/nonlinear, primitive planes, static triangle-mesh walls,
+// gravity, nve/sphere) with sqrt(N) checkpointing.
 //
 // Forward model: the reference's Verlet step (src/verlet.cpp:281-389) with
 // FixNVESphere (src/fix_nve_sphere.cpp:120-215), PairGran with the Hertz +
