@@ -344,8 +344,9 @@ const char *dem_version(void);
  * N-step run with respect to Young's modulus, restitution, friction and
  * every particle radius, by reverse-mode differentiation of the exact
  * discrete timestep: Verlet::setup + N Verlet steps (src/verlet.cpp:281-389)
- * of FixNVESphere, PairGran Hertz + tangential history (no rolling; with
- * cohesion bond/nonlinear when dem_adjoint_set_bonds is called, else contact
+ * of FixNVESphere, PairGran Hertz + tangential history (CDT rolling friction
+ * when dem_adjoint_set_rolling is called; cohesion bond/nonlinear when
+ * dem_adjoint_set_bonds is called, else contact
  * distance factor 1), FixGravity and FixWallGran primitive planes and static
  * triangle meshes (dem_adjoint_add_mesh), one atom type
  * and one material (Yeff/Geff/betaeff of the material against itself,
@@ -405,6 +406,10 @@ int dem_adjoint_set_bonds(dem_adjoint *h, const double *values, const dem_bond_s
  * gradients include them. */
 int dem_adjoint_add_mesh(dem_adjoint *h, int ntri, const double *nodes, const unsigned char *edge_active,
                          const unsigned char *corner_active);
+/* CDT rolling friction (rolling_friction cdt, RollingModel<ROLLING_CDT>,
+ * src/rolling_model_cdt.h:89-167) with coefficientRollingFriction mur on
+ * pairs and on every wall; before dem_adjoint_set_state. */
+int dem_adjoint_set_rolling(dem_adjoint *h, double mur);
 /* initial state (host arrays): x, v, omega n*3, radius n (the radii define the
  * neighbour cells; runs may use radii up to 1 % larger) */
 int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *v, const double *omega,

@@ -16,6 +16,9 @@
 //   sliding (kt^2 |s2|^2 > (mu|Fn|)^2): Ft = -mu|Fn| s2/|s2|, s3 = (mu|Fn|/kt) s2/|s2|
 //   else: Ft = -kt s2 - gamma_t vtr, s3 = s2
 //   F = Fn en + Ft, Ti = -cri (en x Ft), Tj = -crj (en x Ft)
+// With CDT rolling friction (RollingModel<ROLLING_CDT>, src/rolling_model_cdt.h:
+// 89-167): w = wi - wj (walls: wr), rt = mur kn deltan reff w/|w| projected
+// off en, Ti -= rt, Tj += rt (w = 0: none).
 // For a bonded pair the bond's force replaces Fn en (src/contact_models.h:
 // 228-238): F = Ft here, Fn still caps the friction.
 // Walls: radsum = reff = ri, meff = mi, no j terms.  Without
@@ -33,12 +36,14 @@ struct VjpIn {
   bool upd;     // update_history
   bool wall;
   bool bonded;  // a bond (cohesion bond/nonlinear) replaces the normal force
+  bool rolling;  // CDT rolling friction with coefficient mur
+  double mur;
 };
 
 struct VjpBar {  // adjoints of the outputs (in) and of the inputs (out)
   double F[3], Ti[3], Tj[3], s3[3];
   double d[3], vr[3], wi[3], wj[3], sh[3];
-  double ri, rj, mi, mj, Y, G, beta, mu;
+  double ri, rj, mi, mj, Y, G, beta, mu, mur;
 };
 
 __device__ __forceinline__ void cross3(const double a[3], const double b[3], double c[3]) {
@@ -57,6 +62,7 @@ struct LawState {
   double reff, meff, sv, q, kn, kt, c0, c1, gn, gt, Fn, s1[3], rsht, s2[3], ss, Ffr, u, shat[3];
   double Ft[3], tor[3];
   bool slide;
+  double rw[3], rwsq, rfac;  // rolling: relative spin, |w|^2, mur kn deltan reff / |w|
 };
 
 __device__ __forceinline__ void law_forward(const VjpIn &a, LawState &S, double F[3], double Ti[3],
@@ -122,6 +128,20 @@ __device__ __forceinline__ void law_forward(const VjpIn &a, LawState &S, double 
     Ti[k] = -S.cri * S.tor[k];
     Tj[k] = -S.crj * S.tor[k];
   }
+  S.rwsq = 0.0;
+  if (a.rolling) {
+    for (int k = 0; k < 3; k++) S.rw[k] = a.wall ? S.wr[k] : a.wi[k] - a.wj[k];
+    S.rwsq = dot3(S.rw, S.rw);
+    if (S.rwsq > 0.) {
+      S.rfac = a.mur * S.kn * S.deltan * S.reff / sqrt(S.rwsq);
+      const double we = dot3(S.rw, S.en);
+      for (int k = 0; k < 3; k++) {
+        const double rt = S.rfac * (S.rw[k] - we * S.en[k]);
+        Ti[k] -= rt;
+        Tj[k] += rt;
+      }
+    }
+  }
 }
 
 // b.F/Ti/Tj/s3 hold the output adjoints; fills the input adjoints of b.
@@ -131,9 +151,31 @@ __device__ void law_vjp(const VjpIn &a, VjpBar &b) {
   double F[3], Ti[3], Tj[3], s3[3];
   law_forward(a, S, F, Ti, Tj, s3);
   double torb[3], enb[3], Ftb[3], tmp[3];
+  // rolling friction (the last forward operation): rt = rfac (w - (w.en) en)
+  double rwb[3] = {0., 0., 0.}, renb[3] = {0., 0., 0.};
+  double knb_r = 0.0, deltanb_r = 0.0, reffb_r = 0.0, murb = 0.0;
+  if (a.rolling && S.rwsq > 0.) {
+    double rtb[3], pw[3];
+    const double we = dot3(S.rw, S.en);
+    for (int k = 0; k < 3; k++) {
+      rtb[k] = b.Tj[k] - b.Ti[k];
+      pw[k] = S.rw[k] - we * S.en[k];
+    }
+    const double facb = dot3(rtb, pw), rte = dot3(rtb, S.en);
+    const double iw = 1.0 / sqrt(S.rwsq);
+    for (int k = 0; k < 3; k++) {
+      rwb[k] = S.rfac * (rtb[k] - rte * S.en[k]) - facb * S.rfac * S.rw[k] / S.rwsq;
+      renb[k] = -S.rfac * (rte * S.rw[k] + we * rtb[k]);
+    }
+    murb = facb * S.kn * S.deltan * S.reff * iw;
+    knb_r = facb * a.mur * S.deltan * S.reff * iw;
+    deltanb_r = facb * a.mur * S.kn * S.reff * iw;
+    reffb_r = facb * a.mur * S.kn * S.deltan * iw;
+  }
   for (int k = 0; k < 3; k++) torb[k] = -S.cri * b.Ti[k] - S.crj * b.Tj[k];
   double crib = -dot3(S.tor, b.Ti), crjb = -dot3(S.tor, b.Tj);
   cross3(S.Ft, torb, enb);
+  for (int k = 0; k < 3; k++) enb[k] += renb[k];
   cross3(torb, S.en, Ftb);
   double Fnb = a.bonded ? 0.0 : dot3(b.F, S.en);
   for (int k = 0; k < 3; k++) {
@@ -174,8 +216,8 @@ __device__ void law_vjp(const VjpIn &a, VjpBar &b) {
   } else {
     for (int k = 0; k < 3; k++) b.sh[k] = s2b[k] + shb_direct[k];
   }
-  const double knb = Fnb * S.deltan;
-  double deltanb = Fnb * S.kn;
+  const double knb = Fnb * S.deltan + knb_r;
+  double deltanb = Fnb * S.kn + deltanb_r;
   const double gnb = -Fnb * S.vn;
   double vnb = -Fnb * S.gn;
   const double c0b = gnb * S.q, c1b = gtb * S.q, qb = gnb * S.c0 + gtb * S.c1;
@@ -183,7 +225,7 @@ __device__ void law_vjp(const VjpIn &a, VjpBar &b) {
   double svb = 4.0 / 3.0 * a.Y * knb + 8.0 * a.G * ktb;
   svb += qb / (2.0 * S.q);
   const double wb = svb / (2.0 * S.sv);
-  const double reffb = wb * S.deltan;
+  const double reffb = wb * S.deltan + reffb_r;
   deltanb += wb * S.reff;
   const double betab = c0b * K * sqrt(2.0 * a.Y * S.meff) + c1b * K * sqrt(8.0 * a.G * S.meff);
   Yb += c0b * S.c0 / (2.0 * a.Y);
@@ -192,9 +234,11 @@ __device__ void law_vjp(const VjpIn &a, VjpBar &b) {
   double db[3], wrb[3];
   cross3(S.wr, vtrb, db);
   cross3(vtrb, a.d, wrb);
+  if (a.wall)  // rolling of a wall contact spins with wr
+    for (int k = 0; k < 3; k++) wrb[k] += rwb[k];
   for (int k = 0; k < 3; k++) {
-    b.wi[k] = S.cri * S.rinv * wrb[k];
-    b.wj[k] = a.wall ? 0.0 : S.crj * S.rinv * wrb[k];
+    b.wi[k] = S.cri * S.rinv * wrb[k] + (a.wall ? 0.0 : rwb[k]);
+    b.wj[k] = a.wall ? 0.0 : S.crj * S.rinv * wrb[k] - rwb[k];
   }
   crib += S.rinv * dot3(a.wi, wrb);
   if (!a.wall) crjb += S.rinv * dot3(a.wj, wrb);
@@ -241,6 +285,7 @@ __device__ void law_vjp(const VjpIn &a, VjpBar &b) {
   b.G = Gb;
   b.beta = betab;
   b.mu = mub;
+  b.mur = murb;
   (void)tmp;
 }
 

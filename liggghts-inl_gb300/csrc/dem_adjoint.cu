@@ -108,6 +108,8 @@ struct ADev {
   int pax[8];
   double ppos[8];
   double Y, G, beta, mu;
+  double mur;   // CDT rolling friction coefficient (rolling: on for pairs and walls)
+  int rolling;
   double dtf, dtfrot;
   // cohesion bond/nonlinear: on/off, contact distance factor, parameters of
   // the one type pair, tsCreateBondnonlinear
@@ -416,6 +418,8 @@ __device__ __forceinline__ VjpIn pair_in(const ADev &s, const double *x, int p, 
   a.dt = s.dt;
   a.wall = false;
   a.bonded = false;
+  a.rolling = s.rolling != 0;
+  a.mur = s.mur;
   return a;
 }
 
@@ -475,6 +479,8 @@ __device__ __forceinline__ bool wall_in(const ADev &s, const double *x, int w, i
   a.dt = s.dt;
   a.wall = true;
   a.bonded = false;
+  a.rolling = s.rolling != 0;
+  a.mur = s.mur;
   return true;
 }
 
@@ -549,6 +555,8 @@ __device__ __forceinline__ void amesh_contact_in(const ADev &s, int i, const dou
   a.upd = upd != 0;
   a.wall = true;
   a.bonded = false;
+  a.rolling = s.rolling != 0;
+  a.mur = s.mur;
 }
 
 // one evaluation of the slot logic and contact law for atom i and mesh m on
@@ -1654,7 +1662,16 @@ int dem_adjoint_create(const dem_adjoint_config *cfg, dem_adjoint **out) {
   s.bonds = 0;
   s.cdf = 1.0;
   s.nmeshes = 0;
+  s.rolling = 0;
+  s.mur = 0.0;
   *out = h;
+  return DEM_OK;
+}
+
+int dem_adjoint_set_rolling(dem_adjoint *h, double mur) {
+  if (!h || h->n || !(mur >= 0)) return DEM_ERR_BAD_ARG;
+  h->s.rolling = 1;
+  h->s.mur = mur;
   return DEM_OK;
 }
 

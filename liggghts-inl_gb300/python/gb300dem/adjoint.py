@@ -46,6 +46,7 @@ def _bind(L):
     L.dem_adjoint_set_state.argtypes = [P, I, P, P, P, P]
     L.dem_adjoint_set_bonds.argtypes = [P, P, ctypes.POINTER(api.DemBondSettings)]
     L.dem_adjoint_add_mesh.argtypes = [P, I, P, P, P]
+    L.dem_adjoint_set_rolling.argtypes = [P, D]
     L.dem_adjoint_forward.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P]
     L.dem_adjoint_gradient.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P, P, P, P, P]
     L.dem_adjoint_download.argtypes = [P, P, P, P]
@@ -79,13 +80,18 @@ class DemAdjoint:
     def __init__(self, case):
         if case.get("ntypes", 1) != 1:
             raise ValueError("the adjoint covers one atom type")
-        if case.get("normal_model", 0) != 0 or case.get("rolling_model", 0) != 0:
-            raise ValueError("the adjoint covers Hertz without rolling friction")
+        if case.get("normal_model", 0) != 0:
+            raise ValueError("the adjoint covers Hertz")
+        rolling = case.get("rolling_model", 0)
+        if rolling not in (0, 1):
+            raise ValueError("the adjoint covers no rolling friction or CDT")
+        if any(int(pl[3]) != rolling for pl in case.get("planes", [])):
+            raise ValueError("the adjoint's walls use the pairs' rolling model")
         for m in case.get("meshes", []):
             if m.get("vel") is not None or m.get("rotate") is not None:
                 raise ValueError("the adjoint covers static meshes")
-            if int(m["wall_type"]) != 1 or int(m.get("rolling", 0)) != 0:
-                raise ValueError("the adjoint's meshes are of the atoms' material (wall type 1), no rolling")
+            if int(m["wall_type"]) != 1 or int(m.get("rolling", 0)) != rolling:
+                raise ValueError("the adjoint's meshes are of the atoms' material (wall type 1) and rolling model")
         bonded = case.get("cohesion_model", 0) == 1
         if float(case.get("cdf", 1.0)) != 1.0:
             raise ValueError("the adjoint takes the contact distance factor of its bonds, else 1")
@@ -124,6 +130,8 @@ class DemAdjoint:
             for k in api.BOND_FLAGS:
                 setattr(st, k, int(b["settings"][k]))
             self._call("dem_adjoint_set_bonds", self.h, api._p(vals), ctypes.byref(st))
+        if rolling == 1:
+            self._call("dem_adjoint_set_rolling", self.h, float(mat["rollfrict"][0][0]))
         self._meshkeep = []
         for m in case.get("meshes", []):
             nodes = _f64(m["nodes"])

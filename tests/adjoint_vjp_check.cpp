@@ -25,7 +25,7 @@ struct Rng {
 
 // ------------------------------------------------------------ contact law
 struct LawX {  // the differentiable inputs
-  double d[3], vr[3], wi[3], wj[3], sh[3], ri, rj, mi, mj, Y, G, beta, mu;
+  double d[3], vr[3], wi[3], wj[3], sh[3], ri, rj, mi, mj, Y, G, beta, mu, mur;
 };
 
 double law_value(const VjpIn &base, const LawX &x, const double w[12], int *slide) {
@@ -38,7 +38,7 @@ double law_value(const VjpIn &base, const LawX &x, const double w[12], int *slid
     a.sh[k] = x.sh[k];
   }
   a.ri = x.ri; a.rj = x.rj; a.mi = x.mi; a.mj = x.mj;
-  a.Y = x.Y; a.G = x.G; a.beta = x.beta; a.mu = x.mu;
+  a.Y = x.Y; a.G = x.G; a.beta = x.beta; a.mu = x.mu; a.mur = x.mur;
   LawState S;
   double F[3], Ti[3], Tj[3], s3[3];
   law_forward(a, S, F, Ti, Tj, s3);
@@ -53,11 +53,11 @@ double law_value(const VjpIn &base, const LawX &x, const double w[12], int *slid
 extern "C" {
 
 // ncases random contacts of the given kind (0 pair, 1 wall, 2 bonded pair),
-// with (upd = 1) or without history update; returns the largest relative
+// with (upd = 1) or without history update, with or without CDT rolling; returns the largest relative
 // error of the directional derivative, and in counts[0..1] how many cases
 // stuck / slid, counts[2] the cases skipped because stick/slip switched
 // within the finite-difference step
-double check_law(uint64_t seed, int ncases, int kind, int upd, int *counts) {
+double check_law(uint64_t seed, int ncases, int kind, int upd, int rolling, int *counts) {
   Rng R{seed * 2654435761ULL + 17};
   double worst = 0.0;
   counts[0] = counts[1] = counts[2] = 0;
@@ -67,6 +67,7 @@ double check_law(uint64_t seed, int ncases, int kind, int upd, int *counts) {
     a.upd = upd != 0;
     a.wall = kind == 1;
     a.bonded = kind == 2;
+    a.rolling = rolling != 0;
     a.dt = 1e-6;
     LawX x;
     x.ri = 1e-3 * (0.8 + 0.4 * R.uni());
@@ -88,12 +89,14 @@ double check_law(uint64_t seed, int ncases, int kind, int upd, int *counts) {
     x.G = 4e6 * (0.5 + R.uni());
     x.beta = -0.5 * R.uni() - 0.05;
     x.mu = 0.2 + 0.5 * R.uni();
+    x.mur = 0.1 + 0.4 * R.uni();
     double w[12];
     for (int k = 0; k < 12; k++) w[k] = R.sym();
     // the VJP
     for (int k = 0; k < 3; k++) a.d[k] = x.d[k], a.vr[k] = x.vr[k], a.wi[k] = x.wi[k], a.wj[k] = x.wj[k],
                                 a.sh[k] = x.sh[k];
     a.ri = x.ri; a.rj = x.rj; a.mi = x.mi; a.mj = x.mj; a.Y = x.Y; a.G = x.G; a.beta = x.beta; a.mu = x.mu;
+    a.mur = x.mur;
     LawState S;
     double F[3], Ti[3], Tj[3], s3[3];
     law_forward(a, S, F, Ti, Tj, s3);
@@ -113,13 +116,14 @@ double check_law(uint64_t seed, int ncases, int kind, int upd, int *counts) {
     u.ri = 1e-3 * R.sym(); u.rj = kind == 1 ? 0.0 : 1e-3 * R.sym();
     u.mi = x.mi * R.sym(); u.mj = kind == 1 ? 0.0 : x.mj * R.sym();
     u.Y = x.Y * R.sym(); u.G = x.G * R.sym(); u.beta = 0.3 * R.sym(); u.mu = 0.3 * R.sym();
+    u.mur = rolling ? 0.2 * R.sym() : 0.0;
     double g = 0.0;
     for (int k = 0; k < 3; k++)
       g += b.d[k] * u.d[k] + b.vr[k] * u.vr[k] + b.wi[k] * u.wi[k] + b.wj[k] * u.wj[k] + b.sh[k] * u.sh[k];
     g += b.ri * u.ri + b.rj * u.rj + b.mi * u.mi + b.mj * u.mj + b.Y * u.Y + b.G * u.G + b.beta * u.beta +
-         b.mu * u.mu;
+         b.mu * u.mu + b.mur * u.mur;
     double gabs = fabs(b.ri * u.ri) + fabs(b.rj * u.rj) + fabs(b.mi * u.mi) + fabs(b.mj * u.mj) + fabs(b.Y * u.Y) +
-                  fabs(b.G * u.G) + fabs(b.beta * u.beta) + fabs(b.mu * u.mu);
+                  fabs(b.G * u.G) + fabs(b.beta * u.beta) + fabs(b.mu * u.mu) + fabs(b.mur * u.mur);
     for (int k = 0; k < 3; k++)
       gabs += fabs(b.d[k] * u.d[k]) + fabs(b.vr[k] * u.vr[k]) + fabs(b.wi[k] * u.wi[k]) + fabs(b.wj[k] * u.wj[k]) +
               fabs(b.sh[k] * u.sh[k]);

@@ -26,7 +26,8 @@ NSTEPS = 100
 SEG = 10
 
 
-def _case(E=1e7, rest=0.6, frict=0.5, radius=None, seed=5):
+def _case(E=1e7, rest=0.6, frict=0.5, radius=None, seed=5, rolling=None):
+    """rolling: None, or the CDT rolling-friction coefficient of pairs and walls"""
     from gb300dem import workloads
     sp = 1.97e-3
     nz = 4
@@ -34,9 +35,12 @@ def _case(E=1e7, rest=0.6, frict=0.5, radius=None, seed=5):
     c = workloads.lattice_case(seed=seed, nx=6, ny=6, nz=nz, spacing=sp, radius=(0.99e-3, 1.0e-3),
                                z0=z0, jitter=2e-6, vmax=5e-3, wmax=50.0, E=(E,), nu=(0.3,),
                                rest=((rest,),), frict=((frict,),), dt=1e-6, skin=5e-4,
-                               zhi=z0 + (nz - 1) * sp + 3e-3)
+                               zhi=z0 + (nz - 1) * sp + 3e-3,
+                               rollfrict=((rolling,),) if rolling is not None else None,
+                               rolling_model=1 if rolling is not None else 0)
     top = z0 + (nz - 1) * sp + 0.985e-3
-    c["planes"] = [(2, 0.0, 1, 0), (2, top, 1, 0)]
+    rf = 1 if rolling is not None else 0
+    c["planes"] = [(2, 0.0, 1, rf), (2, top, 1, rf)]
     c["neigh"] = (SEG, 0, 0)
     if radius is not None:
         c["atoms"]["radius"] = np.asarray(radius, dtype=np.float64).copy()
@@ -193,6 +197,49 @@ def test_adjoint_segment_length_and_determinism():
     assert max_rel(g3["radius"], g1["radius"]) < ADJ_RTOL
     t = eng.times()
     assert t["segments"] == NSTEPS // 25 + 1 and t["max_pairs"] > 0
+    eng.close()
+
+
+def _fd4(f, h):
+    return (8.0 * (f(h) - f(-h)) - (f(2 * h) - f(-2 * h))) / (12.0 * h)
+
+
+def test_adjoint_with_cdt_rolling_matches_oracle():
+    """CDT rolling friction on pairs and planes (coefficient 0.002: the
+    rolling torque opposes the relative spin at constant magnitude and flips
+    with it, so a spin reaching zero within the window would make the map
+    non-smooth; at this coefficient no spin does).  Forward against the
+    oracle, gradients against its fourth-order differences."""
+    from gb300dem.adjoint import DemAdjoint
+    E, e, mu, mur = 1e7, 0.6, 0.5, 0.002
+    c = _case(E, e, mu, rolling=mur)
+    r0 = c["atoms"]["radius"].copy()
+    eng = DemAdjoint(c)
+    val, g = eng.gradient(E, e, mu, nsteps=NSTEPS, segment=SEG, loss=_spec("ke"))
+    st = eng.final_state()
+    o = _oracle_final(c)
+    box = float(np.max(np.asarray(c["boxhi"]) - np.asarray(c["boxlo"])))
+    assert max_rel(st["x"], o["x"], scale=box) < TRAJ_RTOL
+    assert max_rel(st["v"], o["v"]) < TRAJ_RTOL
+    assert max_rel(st["omega"], o["omega"]) < TRAJ_RTOL
+    assert np.isclose(val, _oracle_loss(c, "ke"), rtol=1e-8, atol=0)
+    for name, base, key in (("E", E, "E"), ("restitution", e, "rest"), ("friction", mu, "frict")):
+        def f(dv, key=key, base=base):
+            kw = dict(E=E, rest=e, frict=mu, rolling=mur)
+            kw[key] = base + dv
+            return _oracle_loss(_case(**kw), "ke")
+
+        fd = _fd4(f, 1e-4 * base)
+        assert abs(g[name] - fd) <= ADJ_RTOL * abs(fd), (name, g[name], fd)
+    gr = g["radius"]
+    for i in np.argsort(-np.abs(gr))[:4]:
+        def f(dv, i=i):
+            r = r0.copy()
+            r[i] += dv
+            return _oracle_loss(_case(radius=r, rolling=mur), "ke")
+
+        fdi = _fd4(f, 1e-6 * r0[i])
+        assert abs(gr[i] - fdi) <= ADJ_RTOL * abs(fdi), (int(i), gr[i], fdi)
     eng.close()
 
 

@@ -1,8 +1,8 @@
 """The adjoint's per-pair laws against finite differences, on the CPU.
 
 tests/adjoint_vjp_check.cpp compiles the device headers of the adjoint
-(adjoint_law.cuh: Hertz + tangential history for pairs, primitive walls and
-bonded pairs; adjoint_bond.cuh: cohesion bond/nonlinear) for the host and
+(adjoint_law.cuh: Hertz + tangential history, with and without CDT rolling,
+for pairs, walls and bonded pairs; adjoint_bond.cuh: cohesion bond/nonlinear) for the host and
 compares each vector-Jacobian product with a fourth-order central difference
 of the forward law along random directions of all inputs (positions,
 velocities, spins, history, radii, masses, material parameters).  Cases
@@ -38,7 +38,8 @@ def lib(tmp_path_factory):
     assert r.returncode == 0, r.stderr[-3000:]
     L = ctypes.CDLL(out)
     L.check_law.restype = ctypes.c_double
-    L.check_law.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    L.check_law.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                            ctypes.POINTER(ctypes.c_int)]
     L.check_bond.restype = ctypes.c_double
     L.check_bond.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                              ctypes.POINTER(ctypes.c_int)]
@@ -47,10 +48,11 @@ def lib(tmp_path_factory):
 
 @pytest.mark.parametrize("kind", [0, 1, 2], ids=["pair", "wall", "bonded_pair"])
 @pytest.mark.parametrize("upd", [0, 1], ids=["setup_pass", "history_update"])
-def test_contact_law_vjp(lib, kind, upd):
+@pytest.mark.parametrize("rolling", [0, 1], ids=["no_rolling", "cdt_rolling"])
+def test_contact_law_vjp(lib, kind, upd, rolling):
     c = (ctypes.c_int * 3)()
     n = 2000
-    err = lib.check_law(11, n, kind, upd, c)
+    err = lib.check_law(11, n, kind, upd, rolling, c)
     assert c[0] > n // 10 and c[1] > n // 10, "both sticking and sliding contacts must be covered"
     assert c[2] < n // 50
     assert err < VJP_RTOL, err
