@@ -65,6 +65,8 @@ struct LawState {
   double rw[3], rwsq, rfac;  // rolling: relative spin, |w|^2, mur kn deltan reff / |w|
 };
 
+// ROLL = false compiles the rolling part out (kernels of systems without it)
+template <bool ROLL = true>
 __device__ __forceinline__ void law_forward(const VjpIn &a, LawState &S, double F[3], double Ti[3],
                                             double Tj[3], double s3[3]) {
   const double K = -2.0 * 0.91287092917527685576161630466800355658790782499663875;
@@ -129,7 +131,7 @@ __device__ __forceinline__ void law_forward(const VjpIn &a, LawState &S, double 
     Tj[k] = -S.crj * S.tor[k];
   }
   S.rwsq = 0.0;
-  if (a.rolling) {
+  if (ROLL && a.rolling) {
     for (int k = 0; k < 3; k++) S.rw[k] = a.wall ? S.wr[k] : a.wi[k] - a.wj[k];
     S.rwsq = dot3(S.rw, S.rw);
     if (S.rwsq > 0.) {
@@ -145,16 +147,17 @@ __device__ __forceinline__ void law_forward(const VjpIn &a, LawState &S, double 
 }
 
 // b.F/Ti/Tj/s3 hold the output adjoints; fills the input adjoints of b.
+template <bool ROLL = true>
 __device__ void law_vjp(const VjpIn &a, VjpBar &b) {
   const double K = -2.0 * 0.91287092917527685576161630466800355658790782499663875;
   LawState S;
   double F[3], Ti[3], Tj[3], s3[3];
-  law_forward(a, S, F, Ti, Tj, s3);
+  law_forward<ROLL>(a, S, F, Ti, Tj, s3);
   double torb[3], enb[3], Ftb[3], tmp[3];
   // rolling friction (the last forward operation): rt = rfac (w - (w.en) en)
   double rwb[3] = {0., 0., 0.}, renb[3] = {0., 0., 0.};
   double knb_r = 0.0, deltanb_r = 0.0, reffb_r = 0.0, murb = 0.0;
-  if (a.rolling && S.rwsq > 0.) {
+  if (ROLL && a.rolling && S.rwsq > 0.) {
     double rtb[3], pw[3];
     const double we = dot3(S.rw, S.en);
     for (int k = 0; k < 3; k++) {

@@ -567,6 +567,7 @@ struct AMeshRec {
   double hin[3], delta[3], ax[3];
 };
 
+template <bool ROLL>
 __device__ inline int amesh_eval(const ADev &s, int m, int i, const double *x, const double *vh, const double *wh,
                                  int upd, int *st, double *sh, int &np, double f[3], double t[3], AMeshRec *rec,
                                  unsigned &keep, bool &bad) {
@@ -650,7 +651,7 @@ __device__ inline int amesh_eval(const ADev &s, int m, int i, const double *x, c
     amesh_contact_in(s, i, vh, wh, delta, sh + 3 * slot, upd, a);
     LawState S;
     double F[3], Ti[3], Tj[3], s3[3];
-    law_forward(a, S, F, Ti, Tj, s3);
+    law_forward<ROLL>(a, S, F, Ti, Tj, s3);
     for (int d = 0; d < 3; d++) {
       f[d] += F[d];
       t[d] += Ti[d];
@@ -668,6 +669,7 @@ __device__ inline int amesh_eval(const ADev &s, int m, int i, const double *x, c
 
 // forward of atom i against every mesh: forces into f/t; the slot state
 // before the evaluation goes to the tape (if set)
+template <bool ROLL>
 __device__ inline void amesh_forward(const ADev &s, int i, const double *x, const double *vh, const double *wh,
                                      int upd, double f[3], double t[3], int *tst, double *tsh, int *tnp) {
   for (int m = 0; m < s.nmeshes; m++) {
@@ -683,7 +685,7 @@ __device__ inline void amesh_forward(const ADev &s, int i, const double *x, cons
     if (s.mcn[base] == 0) continue;
     unsigned keep;
     bool bad = false;
-    amesh_eval(s, m, i, x, vh, wh, upd, st, sh, np, f, t, nullptr, keep, bad);
+    amesh_eval<ROLL>(s, m, i, x, vh, wh, upd, st, sh, np, f, t, nullptr, keep, bad);
     if (bad) s.err[1] = 1;
     s.mnp[base] = np;
   }
@@ -692,6 +694,7 @@ __device__ inline void amesh_forward(const ADev &s, int i, const double *x, cons
 // reverse of amesh_forward for atom i: Fb/Tb the adjoints of the atom's total
 // force and torque; the slot-history adjoints B.msb (of the state after the
 // evaluation) become those of the state before it (the tape's)
+template <bool ROLL>
 __device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const double *x, const double *vh,
                                  const double *wh, int upd, const int *tst, const double *tsh, const int *tnp,
                                  const double Fb[3], const double Tb[3], double xb[3], double vb[3], double wb[3],
@@ -709,7 +712,7 @@ __device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const doub
     unsigned keep;
     bool bad = false;
     double f[3] = {0., 0., 0.}, t[3] = {0., 0., 0.};
-    const int nr = amesh_eval(s, m, i, x, vh, wh, upd, st, sh, np, f, t, rec, keep, bad);
+    const int nr = amesh_eval<ROLL>(s, m, i, x, vh, wh, upd, st, sh, np, f, t, rec, keep, bad);
     double *hb = B.msb + base * kAMC * 3;
     for (int u = 0; u < nc; u++)
       if (!((keep >> u) & 1u))
@@ -729,7 +732,7 @@ __device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const doub
           bb.Tj[d] = 0.0;
           bb.s3[d] = upd ? hb[3 * u + d] : 0.0;
         }
-        law_vjp(a, bb);
+        law_vjp<ROLL>(a, bb);
         for (int d = 0; d < 3; d++) hb[3 * u + d] = bb.sh[d] + (upd ? 0.0 : hb[3 * u + d]);
         // d = centre - closest point
         if (R.kind == 2) {
@@ -856,7 +859,7 @@ __global__ void kb_mesh_uncarry(int cnt, const int *map, const double *hb_new, d
 // history and evaluate a bond they hold or may create.
 // BONDS: the system has cohesion bond/nonlinear (a separate instance keeps
 // the registers of the plain contact path low)
-template <bool BONDS>
+template <bool BONDS, bool ROLL>
 __global__ void __launch_bounds__(kAB) ka_pair_force(ADev s, const double *vh, const double *wh, int upd,
                                                      long long ntimestep, double *tape_sh, double *tape_bh) {
   __shared__ int q[kAB];
@@ -901,7 +904,7 @@ __global__ void __launch_bounds__(kAB) ka_pair_force(ADev s, const double *vh, c
         a.bonded = bonded;
         LawState S;
         double F[3], Ti[3], Tj[3], s3[3];
-        law_forward(a, S, F, Ti, Tj, s3);
+        law_forward<ROLL>(a, S, F, Ti, Tj, s3);
         for (int k = 0; k < 3; k++) {
           s.pF[3 * p + k] = F[k] + bF[k];
           s.pTi[3 * p + k] = Ti[k] + bTi[k];
@@ -926,6 +929,7 @@ __global__ void __launch_bounds__(kAB) ka_pair_force(ADev s, const double *vh, c
 // planes; with final_kick the second half-kick v = vh + a F, w = wh + b T.
 // tape_ws receives the wall history before the update, wallF the wall forces,
 // tape_F/tape_T (if set) a copy of the forces and torques.
+template <bool ROLL, bool MESH>
 __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const double *wh, int upd,
                                                  int final_kick, double *tape_ws, double *wallF, double *tape_F,
                                                  double *tape_T, int *tape_mst, double *tape_msh, int *tape_mnp) {
@@ -977,7 +981,7 @@ __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const
         a.upd = upd != 0;
         LawState S;
         double F[3], Ti[3], Tj[3], s3[3];
-        law_forward(a, S, F, Ti, Tj, s3);
+        law_forward<ROLL>(a, S, F, Ti, Tj, s3);
         double *hw = s.ws + ((size_t)w * s.n + ii) * 3;
         for (int k = 0; k < 3; k++) {
           sF[k][li] = F[k];
@@ -995,7 +999,7 @@ __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const
       __syncthreads();
     }
     if (valid) {
-      if (s.nmeshes) amesh_forward(s, i, s.x, vh, wh, upd, f, t, tape_mst, tape_msh, tape_mnp);  // after the planes
+      if (MESH) amesh_forward<ROLL>(s, i, s.x, vh, wh, upd, f, t, tape_mst, tape_msh, tape_mnp);  // after the planes
       const double a = s.ka[i], b = s.kb[i];
       for (int k = 0; k < 3; k++) {
         s.F[3 * i + k] = f[k];
@@ -1061,6 +1065,7 @@ __global__ void ka_kick_drift(ADev s, const double *xref, int wrap, double *tx, 
 // forces of this evaluation, whose second half-kick v' = vh + a F',
 // w' = wh + b T' is reversed first.  The wall parameter adjoints add to
 // B.wth.
+template <bool ROLL, bool MESH>
 __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x, const double *vh,
                                                 const double *wh, const double *ws_before, int upd, int seed_w,
                                                 double seed, const double *Fn1, const double *Tn1,
@@ -1109,7 +1114,7 @@ __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x,
           bb.Tj[k] = 0.0;
           bb.s3[k] = upd ? wsb[k] : 0.0;
         }
-        law_vjp(a, bb);
+        law_vjp<ROLL>(a, bb);
         for (int k = 0; k < 3; k++) {
           if (k == s.pax[w]) B.xb[3 * ii + k] += bb.d[k];  // off-axis components of d are constants
           B.vb[3 * ii + k] += bb.vr[k];
@@ -1125,14 +1130,14 @@ __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x,
       }
       __syncthreads();
     }
-    if (valid && s.nmeshes) {  // mesh walls, per atom (the planes' writes are behind the barrier)
+    if (MESH && valid) {  // mesh walls, per atom (the planes' writes are behind the barrier)
       double Fb[3], Tb[3], xb[3] = {0., 0., 0.}, vb[3] = {0., 0., 0.}, wb[3] = {0., 0., 0.};
       double rb = 0.0, mb = 0.0, th[4] = {0., 0., 0., 0.};
       for (int k = 0; k < 3; k++) {
         Fb[k] = B.Fb[3 * i + k];
         Tb[k] = B.Tb[3 * i + k];
       }
-      amesh_vjp(s, B, i, x, vh, wh, upd, tmst, tmsh, tmnp, Fb, Tb, xb, vb, wb, rb, mb, th);
+      amesh_vjp<ROLL>(s, B, i, x, vh, wh, upd, tmst, tmsh, tmnp, Fb, Tb, xb, vb, wb, rb, mb, th);
       for (int k = 0; k < 3; k++) {
         B.xb[3 * i + k] += xb[k];
         B.vb[3 * i + k] += vb[k];
@@ -1149,7 +1154,7 @@ __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x,
 // velocities it saw, sh_before/bh_before the history before it); the input
 // adjoints of each entry go to the per-entry arrays, the history adjoints
 // B.sb/B.bb are replaced by those of the history before the evaluation
-template <bool BONDS>
+template <bool BONDS, bool ROLL>
 __global__ void __launch_bounds__(kAB) kb_pairs(ADev s, ABar B, const double *x, const float4 *xf,
                                                 const double *vh, const double *wh, const double *sh_before,
                                                 const double *bh_before, int upd, long long ntimestep) {
@@ -1222,7 +1227,7 @@ __global__ void __launch_bounds__(kAB) kb_pairs(ADev s, ABar B, const double *x,
           bb.Tj[k] = Tjb[k];
           bb.s3[k] = upd ? B.sb[3 * p + k] : 0.0;
         }
-        law_vjp(a, bb);
+        law_vjp<ROLL>(a, bb);
         for (int k = 0; k < 3; k++) {
           d[k] += bb.d[k];
           vr[k] += bb.vr[k];
@@ -1588,22 +1593,50 @@ void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, lon
                 double *tape_F = nullptr, double *tape_T = nullptr, int *tape_mst = nullptr,
                 double *tape_msh = nullptr, int *tape_mnp = nullptr) {
   ADev &s = h->s;
-  if (s.np > 0 && s.bonds)
-    ka_pair_force<true><<<grid_of(s.np), kAB, 0, h->st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
-  else if (s.np > 0)
-    ka_pair_force<false><<<grid_of(s.np), kAB, 0, h->st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
-  ka_gather<<<grid_of(h->n), kAB, 0, h->st>>>(s, vh, wh, upd, final_kick, tape_ws, wallF, tape_F, tape_T, tape_mst,
-                                               tape_msh, tape_mnp);
+  const int g = grid_of(s.np), ga = grid_of(h->n);
+  const cudaStream_t st = h->st;
+  if (s.np > 0) {
+    if (s.bonds && s.rolling) ka_pair_force<true, true><<<g, kAB, 0, st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
+    else if (s.bonds) ka_pair_force<true, false><<<g, kAB, 0, st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
+    else if (s.rolling) ka_pair_force<false, true><<<g, kAB, 0, st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
+    else ka_pair_force<false, false><<<g, kAB, 0, st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
+  }
+#define A_GATHER(R, M)                                                                                        \
+  ka_gather<R, M><<<ga, kAB, 0, st>>>(s, vh, wh, upd, final_kick, tape_ws, wallF, tape_F, tape_T, tape_mst, tape_msh, \
+                                      tape_mnp)
+  if (s.rolling && s.nmeshes) A_GATHER(true, true);
+  else if (s.rolling) A_GATHER(true, false);
+  else if (s.nmeshes) A_GATHER(false, true);
+  else A_GATHER(false, false);
+#undef A_GATHER
 }
 
 void pairs_vjp(dem_adjoint *h, const double *x, const float4 *xf, const double *vh, const double *wh,
                const double *sh_before, const double *bh_before, int upd, long long ntimestep) {
   const ADev &s = h->s;
-  if (s.np > 0 && s.bonds)
-    kb_pairs<true><<<grid_of(s.np), kAB, 0, h->st>>>(s, h->B, x, xf, vh, wh, sh_before, bh_before, upd, ntimestep);
-  else if (s.np > 0)
-    kb_pairs<false><<<grid_of(s.np), kAB, 0, h->st>>>(s, h->B, x, xf, vh, wh, sh_before, bh_before, upd,
-                                                      ntimestep);
+  if (s.np <= 0) return;
+  const int g = grid_of(s.np);
+#define A_PAIRS(BD, R) \
+  kb_pairs<BD, R><<<g, kAB, 0, h->st>>>(s, h->B, x, xf, vh, wh, sh_before, bh_before, upd, ntimestep)
+  if (s.bonds && s.rolling) A_PAIRS(true, true);
+  else if (s.bonds) A_PAIRS(true, false);
+  else if (s.rolling) A_PAIRS(false, true);
+  else A_PAIRS(false, false);
+#undef A_PAIRS
+}
+
+void walls_vjp(dem_adjoint *h, const double *x, const double *vh, const double *wh, const double *ws_before, int upd,
+               int seed_w, double seed, const double *Fn1, const double *Tn1, const int *tmst, const double *tmsh,
+               const int *tmnp) {
+  const ADev &s = h->s;
+  const int g = grid_of(h->n);
+#define A_WALLS(R, M) \
+  kb_walls<R, M><<<g, kAB, 0, h->st>>>(s, h->B, x, vh, wh, ws_before, upd, seed_w, seed, Fn1, Tn1, tmst, tmsh, tmnp)
+  if (s.rolling && s.nmeshes) A_WALLS(true, true);
+  else if (s.rolling) A_WALLS(true, false);
+  else if (s.nmeshes) A_WALLS(false, true);
+  else A_WALLS(false, false);
+#undef A_WALLS
 }
 
 void accumulate(dem_adjoint *h, const double *in, int cnt) {
@@ -2182,11 +2215,9 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     for (int t = last; t >= first; t--) {
       const int q = t - first;
       const double *xs = T.x + S3 * q, *vh = T.vh + S3 * q, *wh = T.wh + S3 * q;
-      kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, xs, vh, wh, T.ws + W3 * q, 1, t == nsteps ? lw : -1,
-                                           t == nsteps ? fw_seed : 0.0, T.F + S3 * q, T.T + S3 * q,
-                                           s.nmeshes ? T.mst + NBM * kAMC * q : nullptr,
-                                           s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr,
-                                           s.nmeshes ? T.mnp + NBM * q : nullptr);
+      walls_vjp(h, xs, vh, wh, T.ws + W3 * q, 1, t == nsteps ? lw : -1, t == nsteps ? fw_seed : 0.0, T.F + S3 * q,
+                T.T + S3 * q, s.nmeshes ? T.mst + NBM * kAMC * q : nullptr,
+                s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr, s.nmeshes ? T.mnp + NBM * q : nullptr);
       if (s.np > 0)
         pairs_vjp(h, xs, T.xf + (size_t)n * q, vh, wh, T.sh + 3 * PS * q,
                   s.bonds ? T.bh + kBondValues * PS * q : nullptr, 1, t);
@@ -2220,8 +2251,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     ATRY(h, cudaMemsetAsync(shr, 0, 3 * (size_t)maxnp * sizeof(double), st));
     if (s.bonds) ATRY(h, cudaMemsetAsync(bhr, 0, NB * sizeof(double), st));
     use_list(h, c.L, shr, bhr);
-    kb_walls<<<grid_of(n), kAB, 0, st>>>(s, B, c.x, c.v, c.w, tws0, 0, -1, 0.0, nullptr, nullptr, mst_e, msh_e,
-                                         mnp_e);
+    walls_vjp(h, c.x, c.v, c.w, tws0, 0, -1, 0.0, nullptr, nullptr, mst_e, msh_e, mnp_e);
     pairs_vjp(h, c.x, nullptr, c.v, c.w, shr, bhr, 0, 0);
     kb_gather_kick<<<grid_of(n), kAB, 0, st>>>(s, B, nullptr, nullptr, 0);
     accumulate(h, B.pth, s.np);  // segment 0's steps and the setup pass
