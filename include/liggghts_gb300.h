@@ -406,6 +406,12 @@ int dem_adjoint_set_bonds(dem_adjoint *h, const double *values, const dem_bond_s
  * gradients include them. */
 int dem_adjoint_add_mesh(dem_adjoint *h, int ntri, const double *nodes, const unsigned char *edge_active,
                          const unsigned char *corner_active);
+/* fix move/mesh ... linear vx vy vz for mesh mesh_id of the adjoint: the
+ * nodes translate by dt*vel per step and contacts see the wall velocity
+ * (MeshMoverLinear, src/mesh_mover_linear.cpp:95-112); before
+ * dem_adjoint_set_state.  The mesh may not move more than skin/2 between two
+ * list builds (the reference would then force a rebuild). */
+int dem_adjoint_set_mesh_motion(dem_adjoint *h, int mesh_id, const double *vel);
 /* CDT rolling friction (rolling_friction cdt, RollingModel<ROLLING_CDT>,
  * src/rolling_model_cdt.h:89-167) with coefficientRollingFriction mur on
  * pairs and on every wall; before dem_adjoint_set_state. */

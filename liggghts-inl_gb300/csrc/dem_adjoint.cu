@@ -81,8 +81,12 @@ constexpr int kAMeshes = 4;
 // one static triangle-mesh wall on the device (geometry of MeshHost)
 struct AMesh {
   int ntri;
-  const double *tri;  // [t*kTriStride]
+  const double *tri;  // [t*kTriStride], node positions at step 0
   const int *meta, *cn_start, *cn_list;
+  // fix move/mesh ... linear: the nodes translate by dt*vel per step (step t
+  // sees them t*dt*vel away), contacts see the wall velocity vel
+  int moving;
+  double vel[3];
 };
 
 struct AList {
@@ -534,11 +538,14 @@ __device__ __forceinline__ int amesh_feature(const double *g, int bs, const doub
   return 1;
 }
 
+// vw: the wall velocity at the contact (a translating mesh's velocity; 0
+// for a static mesh and in the setup force pass)
 __device__ __forceinline__ void amesh_contact_in(const ADev &s, int i, const double *vh, const double *wh,
-                                                 const double delta[3], const double hin[3], int upd, VjpIn &a) {
+                                                 const double delta[3], const double hin[3], int upd,
+                                                 const double vw[3], VjpIn &a) {
   for (int k = 0; k < 3; k++) {
     a.d[k] = -delta[k];
-    a.vr[k] = vh[3 * i + k];  // static mesh: no wall velocity
+    a.vr[k] = vh[3 * i + k] - vw[k];
     a.wi[k] = wh[3 * i + k];
     a.wj[k] = 0.0;
     a.sh[k] = hin[k];
@@ -567,15 +574,25 @@ struct AMeshRec {
   double hin[3], delta[3], ax[3];
 };
 
+// the atom's position relative to mesh m at step `step` (a translating
+// mesh's geometry is its step-0 geometry shifted by step*dt*vel)
+__device__ __forceinline__ void amesh_rel(const ADev &s, const AMesh &M, long long step, const double *x, int i,
+                                          double xr[3]) {
+  for (int k = 0; k < 3; k++) xr[k] = M.moving ? x[3 * i + k] - (double)step * (s.dt * M.vel[k]) : x[3 * i + k];
+}
+
 template <bool ROLL>
 __device__ inline int amesh_eval(const ADev &s, int m, int i, const double *x, const double *vh, const double *wh,
-                                 int upd, int *st, double *sh, int &np, double f[3], double t[3], AMeshRec *rec,
-                                 unsigned &keep, bool &bad) {
+                                 int upd, long long step, int *st, double *sh, int &np, double f[3], double t[3],
+                                 AMeshRec *rec, unsigned &keep, bool &bad) {
   const AMesh &M = s.mesh[m];
   const size_t base = (size_t)m * s.n + i;
   const int nc = s.mcn[base];
   const int *cand = s.mcand + base * kAMC;
-  const double xi[3] = {x[3 * i], x[3 * i + 1], x[3 * i + 2]};
+  double xi[3];
+  amesh_rel(s, M, step, x, i, xi);
+  const double vw[3] = {M.moving && upd ? M.vel[0] : 0.0, M.moving && upd ? M.vel[1] : 0.0,
+                        M.moving && upd ? M.vel[2] : 0.0};
   const double radi = s.r[i];
   const double cdm1 = s.cdf - 1.0;
   int nr = 0;
@@ -648,7 +665,7 @@ __device__ inline int amesh_eval(const ADev &s, int m, int i, const double *x, c
       continue;
     }
     VjpIn a;
-    amesh_contact_in(s, i, vh, wh, delta, sh + 3 * slot, upd, a);
+    amesh_contact_in(s, i, vh, wh, delta, sh + 3 * slot, upd, vw, a);
     LawState S;
     double F[3], Ti[3], Tj[3], s3[3];
     law_forward<ROLL>(a, S, F, Ti, Tj, s3);
@@ -671,7 +688,8 @@ __device__ inline int amesh_eval(const ADev &s, int m, int i, const double *x, c
 // before the evaluation goes to the tape (if set)
 template <bool ROLL>
 __device__ inline void amesh_forward(const ADev &s, int i, const double *x, const double *vh, const double *wh,
-                                     int upd, double f[3], double t[3], int *tst, double *tsh, int *tnp) {
+                                     int upd, long long step, double f[3], double t[3], int *tst, double *tsh,
+                                     int *tnp) {
   for (int m = 0; m < s.nmeshes; m++) {
     const size_t base = (size_t)m * s.n + i;
     int *st = s.mst + base * kAMC;
@@ -685,7 +703,7 @@ __device__ inline void amesh_forward(const ADev &s, int i, const double *x, cons
     if (s.mcn[base] == 0) continue;
     unsigned keep;
     bool bad = false;
-    amesh_eval<ROLL>(s, m, i, x, vh, wh, upd, st, sh, np, f, t, nullptr, keep, bad);
+    amesh_eval<ROLL>(s, m, i, x, vh, wh, upd, step, st, sh, np, f, t, nullptr, keep, bad);
     if (bad) s.err[1] = 1;
     s.mnp[base] = np;
   }
@@ -696,7 +714,8 @@ __device__ inline void amesh_forward(const ADev &s, int i, const double *x, cons
 // evaluation) become those of the state before it (the tape's)
 template <bool ROLL>
 __device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const double *x, const double *vh,
-                                 const double *wh, int upd, const int *tst, const double *tsh, const int *tnp,
+                                 const double *wh, int upd, long long step, const int *tst, const double *tsh,
+                                 const int *tnp,
                                  const double Fb[3], const double Tb[3], double xb[3], double vb[3], double wb[3],
                                  double &rb, double &mb, double th[4]) {
   for (int m = 0; m < s.nmeshes; m++) {
@@ -712,7 +731,10 @@ __device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const doub
     unsigned keep;
     bool bad = false;
     double f[3] = {0., 0., 0.}, t[3] = {0., 0., 0.};
-    const int nr = amesh_eval<ROLL>(s, m, i, x, vh, wh, upd, st, sh, np, f, t, rec, keep, bad);
+    const int nr = amesh_eval<ROLL>(s, m, i, x, vh, wh, upd, step, st, sh, np, f, t, rec, keep, bad);
+    const AMesh &M = s.mesh[m];
+    const double vw[3] = {M.moving && upd ? M.vel[0] : 0.0, M.moving && upd ? M.vel[1] : 0.0,
+                          M.moving && upd ? M.vel[2] : 0.0};
     double *hb = B.msb + base * kAMC * 3;
     for (int u = 0; u < nc; u++)
       if (!((keep >> u) & 1u))
@@ -724,7 +746,7 @@ __device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const doub
         for (int d = 0; d < 3; d++) hb[3 * u + d] = 0.0;
       } else {
         VjpIn a;
-        amesh_contact_in(s, i, vh, wh, R.delta, R.hin, upd, a);
+        amesh_contact_in(s, i, vh, wh, R.delta, R.hin, upd, vw, a);
         VjpBar bb;
         for (int d = 0; d < 3; d++) {
           bb.F[d] = Fb[d];
@@ -780,12 +802,15 @@ __device__ __forceinline__ void amesh_swap(int *st, double *sh, int *orig, int a
   }
 }
 
-__global__ void ka_mesh_build(ADev s, int *mcn, int *mcand, int *map) {
+__global__ void ka_mesh_build(ADev s, long long step, int *mcn, int *mcand, int *map) {
   AGRID(i, s.n) {
-    const double xi[3] = {s.x[3 * i], s.x[3 * i + 1], s.x[3 * i + 2]};
     const double rS = s.r[i] * s.cdf;
     for (int m = 0; m < s.nmeshes; m++) {
       const AMesh &M = s.mesh[m];
+      double xi[3];
+      amesh_rel(s, M, step, s.x, i, xi);
+      // FixNeighlistMesh: a moving mesh takes candidates within r cdf + skin
+      const double tskin = M.moving ? s.skin : s.mtskin;
       const size_t base = (size_t)m * s.n + i;
       int *st = s.mst + base * kAMC;
       double *sh = s.msh + base * kAMC * 3;
@@ -805,7 +830,7 @@ __global__ void ka_mesh_build(ADev s, int *mcn, int *mcand, int *map) {
       int nc = 0;
       int *cand = mcand + base * kAMC;
       for (int tr = 0; tr < M.ntri; tr++) {
-        if (!tri_sphere_neighbuild(M.tri + (size_t)tr * kTriStride, rS, xi, s.mtskin)) continue;
+        if (!tri_sphere_neighbuild(M.tri + (size_t)tr * kTriStride, rS, xi, tskin)) continue;
         if (nc == kAMC) {
           s.err[1] = 1;
           break;
@@ -932,7 +957,8 @@ __global__ void __launch_bounds__(kAB) ka_pair_force(ADev s, const double *vh, c
 template <bool ROLL, bool MESH>
 __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const double *wh, int upd,
                                                  int final_kick, double *tape_ws, double *wallF, double *tape_F,
-                                                 double *tape_T, int *tape_mst, double *tape_msh, int *tape_mnp) {
+                                                 double *tape_T, int *tape_mst, double *tape_msh, int *tape_mnp,
+                                                 long long ntimestep) {
   __shared__ int q[kAB];
   __shared__ int wcnt[kAB / 32];
   __shared__ double sF[3][kAB], sT[3][kAB];
@@ -999,7 +1025,7 @@ __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const
       __syncthreads();
     }
     if (valid) {
-      if (MESH) amesh_forward<ROLL>(s, i, s.x, vh, wh, upd, f, t, tape_mst, tape_msh, tape_mnp);  // after the planes
+      if (MESH) amesh_forward<ROLL>(s, i, s.x, vh, wh, upd, ntimestep, f, t, tape_mst, tape_msh, tape_mnp);  // after the planes
       const double a = s.ka[i], b = s.kb[i];
       for (int k = 0; k < 3; k++) {
         s.F[3 * i + k] = f[k];
@@ -1069,7 +1095,8 @@ template <bool ROLL, bool MESH>
 __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x, const double *vh,
                                                 const double *wh, const double *ws_before, int upd, int seed_w,
                                                 double seed, const double *Fn1, const double *Tn1,
-                                                const int *tmst, const double *tmsh, const int *tmnp) {
+                                                const int *tmst, const double *tmsh, const int *tmnp,
+                                                long long ntimestep) {
   __shared__ int q[kAB];
   __shared__ int wcnt[kAB / 32];
   ABLOCKS(base, s.n) {
@@ -1137,7 +1164,7 @@ __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x,
         Fb[k] = B.Fb[3 * i + k];
         Tb[k] = B.Tb[3 * i + k];
       }
-      amesh_vjp<ROLL>(s, B, i, x, vh, wh, upd, tmst, tmsh, tmnp, Fb, Tb, xb, vb, wb, rb, mb, th);
+      amesh_vjp<ROLL>(s, B, i, x, vh, wh, upd, ntimestep, tmst, tmsh, tmnp, Fb, Tb, xb, vb, wb, rb, mb, th);
       for (int k = 0; k < 3; k++) {
         B.xb[3 * i + k] += xb[k];
         B.vb[3 * i + k] += vb[k];
@@ -1497,7 +1524,7 @@ struct Checkpoint {
 
 // neighbour list of the current positions; old: the previous list (with its
 // current history and flags) or np = 0
-int build_list(dem_adjoint *h, AList &L, const AList &old) {
+int build_list(dem_adjoint *h, AList &L, const AList &old, long long step) {
   ADev &s = h->s;
   const int n = h->n;
   const cudaStream_t st = h->st;
@@ -1539,7 +1566,7 @@ int build_list(dem_adjoint *h, AList &L, const AList &old) {
     AGET(h, L.mcn, int, nb);
     AGET(h, L.mcand, int, nb * kAMC);
     AGET(h, L.mmap, int, nb * kAMC);
-    ka_mesh_build<<<grid_of(n), kAB, 0, st>>>(s, L.mcn, L.mcand, L.mmap);
+    ka_mesh_build<<<grid_of(n), kAB, 0, st>>>(s, step, L.mcn, L.mcand, L.mmap);
   }
   ATRY(h, cudaGetLastError());
   return DEM_OK;
@@ -1603,7 +1630,7 @@ void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, lon
   }
 #define A_GATHER(R, M)                                                                                        \
   ka_gather<R, M><<<ga, kAB, 0, st>>>(s, vh, wh, upd, final_kick, tape_ws, wallF, tape_F, tape_T, tape_mst, tape_msh, \
-                                      tape_mnp)
+                                      tape_mnp, ntimestep)
   if (s.rolling && s.nmeshes) A_GATHER(true, true);
   else if (s.rolling) A_GATHER(true, false);
   else if (s.nmeshes) A_GATHER(false, true);
@@ -1627,11 +1654,12 @@ void pairs_vjp(dem_adjoint *h, const double *x, const float4 *xf, const double *
 
 void walls_vjp(dem_adjoint *h, const double *x, const double *vh, const double *wh, const double *ws_before, int upd,
                int seed_w, double seed, const double *Fn1, const double *Tn1, const int *tmst, const double *tmsh,
-               const int *tmnp) {
+               const int *tmnp, long long ntimestep) {
   const ADev &s = h->s;
   const int g = grid_of(h->n);
 #define A_WALLS(R, M) \
-  kb_walls<R, M><<<g, kAB, 0, h->st>>>(s, h->B, x, vh, wh, ws_before, upd, seed_w, seed, Fn1, Tn1, tmst, tmsh, tmnp)
+  kb_walls<R, M><<<g, kAB, 0, h->st>>>(s, h->B, x, vh, wh, ws_before, upd, seed_w, seed, Fn1, Tn1, tmst, tmsh, tmnp, \
+                                       ntimestep)
   if (s.rolling && s.nmeshes) A_WALLS(true, true);
   else if (s.rolling) A_WALLS(true, false);
   else if (s.nmeshes) A_WALLS(false, true);
@@ -1701,6 +1729,14 @@ int dem_adjoint_create(const dem_adjoint_config *cfg, dem_adjoint **out) {
   return DEM_OK;
 }
 
+int dem_adjoint_set_mesh_motion(dem_adjoint *h, int mesh_id, const double *vel) {
+  if (!h || h->n || !vel || mesh_id < 0 || mesh_id >= h->s.nmeshes) return DEM_ERR_BAD_ARG;
+  AMesh &M = h->s.mesh[mesh_id];
+  M.moving = 1;
+  for (int k = 0; k < 3; k++) M.vel[k] = vel[k];
+  return DEM_OK;
+}
+
 int dem_adjoint_set_rolling(dem_adjoint *h, double mur) {
   if (!h || h->n || !(mur >= 0)) return DEM_ERR_BAD_ARG;
   h->s.rolling = 1;
@@ -1734,6 +1770,8 @@ int dem_adjoint_add_mesh(dem_adjoint *h, int ntri, const double *nodes, const un
   if (!mh.cn_list.empty())
     ATRY(h, cudaMemcpy(cl, mh.cn_list.data(), mh.cn_list.size() * sizeof(int), cudaMemcpyHostToDevice));
   AMesh &M = s.mesh[s.nmeshes++];
+  M.moving = 0;
+  M.vel[0] = M.vel[1] = M.vel[2] = 0.0;
   M.ntri = ntri;
   M.tri = tri;
   M.meta = meta;
@@ -1964,7 +2002,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     AGET(h, c.ws, double, W3);
     if (k == 0) {
       ka_wrap<<<grid_of(n), kAB, 0, st>>>(s);
-      rc = build_list(h, c.L, none);
+      rc = build_list(h, c.L, none, 0);
       if (rc) return rc;
       rc = ensure_pairs(h, c.L.np);
       if (rc) return rc;
@@ -2024,7 +2062,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
                                                 rec ? T.x + S3 * q : nullptr, rec ? T.vh + S3 * q : nullptr,
                                                 rec ? T.wh + S3 * q : nullptr, rec ? T.xf + (size_t)n * q : nullptr);
       if (build) {
-        rc = build_list(h, c.L, cps[k - 1].L);
+        rc = build_list(h, c.L, cps[k - 1].L, t);
         if (rc) return rc;
         rc = ensure_pairs(h, c.L.np);
         if (rc) return rc;
@@ -2217,7 +2255,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       const double *xs = T.x + S3 * q, *vh = T.vh + S3 * q, *wh = T.wh + S3 * q;
       walls_vjp(h, xs, vh, wh, T.ws + W3 * q, 1, t == nsteps ? lw : -1, t == nsteps ? fw_seed : 0.0, T.F + S3 * q,
                 T.T + S3 * q, s.nmeshes ? T.mst + NBM * kAMC * q : nullptr,
-                s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr, s.nmeshes ? T.mnp + NBM * q : nullptr);
+                s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr, s.nmeshes ? T.mnp + NBM * q : nullptr, t);
       if (s.np > 0)
         pairs_vjp(h, xs, T.xf + (size_t)n * q, vh, wh, T.sh + 3 * PS * q,
                   s.bonds ? T.bh + kBondValues * PS * q : nullptr, 1, t);
@@ -2251,7 +2289,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     ATRY(h, cudaMemsetAsync(shr, 0, 3 * (size_t)maxnp * sizeof(double), st));
     if (s.bonds) ATRY(h, cudaMemsetAsync(bhr, 0, NB * sizeof(double), st));
     use_list(h, c.L, shr, bhr);
-    walls_vjp(h, c.x, c.v, c.w, tws0, 0, -1, 0.0, nullptr, nullptr, mst_e, msh_e, mnp_e);
+    walls_vjp(h, c.x, c.v, c.w, tws0, 0, -1, 0.0, nullptr, nullptr, mst_e, msh_e, mnp_e, 0);
     pairs_vjp(h, c.x, nullptr, c.v, c.w, shr, bhr, 0, 0);
     kb_gather_kick<<<grid_of(n), kAB, 0, st>>>(s, B, nullptr, nullptr, 0);
     accumulate(h, B.pth, s.np);  // segment 0's steps and the setup pass

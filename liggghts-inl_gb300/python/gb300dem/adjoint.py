@@ -47,6 +47,7 @@ def _bind(L):
     L.dem_adjoint_set_bonds.argtypes = [P, P, ctypes.POINTER(api.DemBondSettings)]
     L.dem_adjoint_add_mesh.argtypes = [P, I, P, P, P]
     L.dem_adjoint_set_rolling.argtypes = [P, D]
+    L.dem_adjoint_set_mesh_motion.argtypes = [P, I, P]
     L.dem_adjoint_forward.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P]
     L.dem_adjoint_gradient.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P, P, P, P, P]
     L.dem_adjoint_download.argtypes = [P, P, P, P]
@@ -88,8 +89,8 @@ class DemAdjoint:
         if any(int(pl[3]) != rolling for pl in case.get("planes", [])):
             raise ValueError("the adjoint's walls use the pairs' rolling model")
         for m in case.get("meshes", []):
-            if m.get("vel") is not None or m.get("rotate") is not None:
-                raise ValueError("the adjoint covers static meshes")
+            if m.get("rotate") is not None:
+                raise ValueError("the adjoint covers static and translating meshes")
             if int(m["wall_type"]) != 1 or int(m.get("rolling", 0)) != rolling:
                 raise ValueError("the adjoint's meshes are of the atoms' material (wall type 1) and rolling model")
         bonded = case.get("cohesion_model", 0) == 1
@@ -133,13 +134,17 @@ class DemAdjoint:
         if rolling == 1:
             self._call("dem_adjoint_set_rolling", self.h, float(mat["rollfrict"][0][0]))
         self._meshkeep = []
-        for m in case.get("meshes", []):
+        for mi, m in enumerate(case.get("meshes", [])):
             nodes = _f64(m["nodes"])
             ea, ca = m.get("edge_active"), m.get("corner_active")
             ea = np.ascontiguousarray(ea, dtype=np.uint8) if ea is not None else None
             ca = np.ascontiguousarray(ca, dtype=np.uint8) if ca is not None else None
             self._meshkeep += [nodes, ea, ca]
             self._call("dem_adjoint_add_mesh", self.h, len(nodes), api._p(nodes), api._p(ea), api._p(ca))
+            if m.get("vel") is not None:
+                vel = _f64(m["vel"])
+                self._meshkeep.append(vel)
+                self._call("dem_adjoint_set_mesh_motion", self.h, mi, api._p(vel))
         a = case["atoms"]
         self.n = len(a["radius"])
         self.radius = _f64(a["radius"]).copy()

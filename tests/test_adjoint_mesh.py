@@ -69,11 +69,13 @@ def _case(E=1e7, rest=0.6, frict=0.5, radius=None, seed=5, floor="flat", wmax=50
     top = z0 + (nz - 1) * sp + 0.985e-3
     c["planes"] = [(2, top, 1, 0)]
     lx, ly = c["boxhi"][0], c["boxhi"][1]
-    if floor == "flat":
+    if floor in ("flat", "rising"):
         nodes = floor_mesh(lx, ly, 3, 3)
     else:  # gaps under every other column of bottom atoms: edge contacts beside face contacts
         nodes = gapped_floor(lx, ly, sp, 0.05e-3, 3)
     c["meshes"] = [dict(nodes=nodes, wall_type=1)]
+    if floor == "rising":  # fix move/mesh linear 0 0 0.02: the floor presses into the bed
+        c["meshes"][0]["vel"] = (0.0, 0.0, 0.02)
     c["neigh"] = (SEG, 0, 0)
     if radius is not None:
         c["atoms"]["radius"] = np.asarray(radius, dtype=np.float64).copy()
@@ -217,6 +219,44 @@ def test_adjoint_with_mesh_edges_matches_oracle():
             r = r0.copy()
             r[i] += dv
             return _oracle_loss(_case(frict=mu, radius=r, floor="gapped"), "ke")
+
+        fdi = _fd4(f, 1e-6 * r0[i])
+        assert abs(gr[i] - fdi) <= ADJ_RTOL * abs(fdi), (int(i), gr[i], fdi)
+    eng.close()
+
+
+@pytest.mark.gpu
+def test_adjoint_with_moving_mesh_matches_oracle():
+    """A translating mesh (fix move/mesh linear): the floor rises at 2 cm/s
+    (2 um over the window, far below the skin, so no mesh-forced rebuild),
+    its velocity entering the contacts' relative velocity.  Forward against
+    the oracle, gradients against its differences."""
+    from gb300dem.adjoint import DemAdjoint
+    E, e, mu = 1e7, 0.6, 0.5
+    c = _case(E, e, mu, floor="rising")
+    r0 = c["atoms"]["radius"].copy()
+    eng = DemAdjoint(c)
+    val, g = eng.gradient(E, e, mu, nsteps=NSTEPS, segment=SEG, loss=_spec("ke"))
+    st = eng.final_state()
+    o = sort_by_tag(_oracle(c).atoms())
+    box = float(np.max(np.asarray(c["boxhi"]) - np.asarray(c["boxlo"])))
+    assert max_rel(st["x"], o["x"], scale=box) < TRAJ_RTOL
+    assert max_rel(st["v"], o["v"]) < TRAJ_RTOL
+    assert np.isclose(val, _oracle_loss(c, "ke"), rtol=1e-8, atol=0)
+    for name, base, key in (("E", E, "E"), ("restitution", e, "rest")):
+        def f(dv, key=key, base=base):
+            kw = dict(E=E, rest=e, frict=mu, floor="rising")
+            kw[key] = base + dv
+            return _oracle_loss(_case(**kw), "ke")
+
+        fd = _fd4(f, 1e-4 * base)
+        assert abs(g[name] - fd) <= ADJ_RTOL * abs(fd), (name, g[name], fd)
+    gr = g["radius"]
+    for i in np.argsort(-np.abs(gr))[:4]:
+        def f(dv, i=i):
+            r = r0.copy()
+            r[i] += dv
+            return _oracle_loss(_case(radius=r, floor="rising"), "ke")
 
         fdi = _fd4(f, 1e-6 * r0[i])
         assert abs(gr[i] - fdi) <= ADJ_RTOL * abs(fdi), (int(i), gr[i], fdi)
