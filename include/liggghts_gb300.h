@@ -416,6 +416,9 @@ int dem_adjoint_set_mesh_motion(dem_adjoint *h, int mesh_id, const double *vel);
  * src/rolling_model_cdt.h:89-167) with coefficientRollingFriction mur on
  * pairs and on every wall; before dem_adjoint_set_state. */
 int dem_adjoint_set_rolling(dem_adjoint *h, double mur);
+/* d(loss)/d(coefficientRollingFriction) of the last dem_adjoint_gradient
+ * call (0 without rolling friction) */
+int dem_adjoint_rolling_gradient(dem_adjoint *h, double *grad_mur);
 /* initial state (host arrays): x, v, omega n*3, radius n (the radii define the
  * neighbour cells; runs may use radii up to 1 % larger) */
 int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *v, const double *omega,

@@ -75,6 +75,8 @@ namespace {
 constexpr int kAB = 128;
 constexpr int kMaxGrid = 152 * 16;
 
+// parameter adjoints per entry / atom: Y, G, beta, mu, rolling coefficient
+constexpr int kTh = 5;
 constexpr int kAMC = kMeshMaxCand;  // candidate triangles (= history slots) per atom and mesh
 constexpr int kAMeshes = 4;
 
@@ -492,9 +494,9 @@ __device__ __forceinline__ bool wall_in(const ADev &s, const double *x, int w, i
 struct ABar {
   double *xb, *vb, *wb, *Fb, *Tb, *rb, *mb, *sb, *wsb;
   // per-entry VJP outputs of the pair law
-  double *pd, *pv, *pwi, *pwj, *pri, *prj, *pmi, *pmj, *pth;  // pth [4*p]: Y, G, beta, mu
+  double *pd, *pv, *pwi, *pwj, *pri, *prj, *pmi, *pmj, *pth;  // pth [kTh*p]: Y, G, beta, mu, mur
   double *bb;   // [kBondValues*p] adjoint of the bond history (bonds only)
-  double *wth;  // [4*i] wall parameter adjoints per atom
+  double *wth;  // [kTh*i] wall parameter adjoints per atom
   double *th;   // [4] accumulated parameter adjoints
   double *msb;  // [(b*kAMC + u)*3 + d] adjoints of the mesh slot histories
 };
@@ -717,7 +719,7 @@ __device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const doub
                                  const double *wh, int upd, long long step, const int *tst, const double *tsh,
                                  const int *tnp,
                                  const double Fb[3], const double Tb[3], double xb[3], double vb[3], double wb[3],
-                                 double &rb, double &mb, double th[4]) {
+                                 double &rb, double &mb, double th[kTh]) {
   for (int m = 0; m < s.nmeshes; m++) {
     const size_t base = (size_t)m * s.n + i;
     const int nc = s.mcn[base];
@@ -773,6 +775,7 @@ __device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const doub
         th[1] += bb.G;
         th[2] += bb.beta;
         th[3] += bb.mu;
+        th[4] += bb.mur;
       }
       if (R.fresh) {  // the slot was set to zero, or to a coplanar partner's history
         if (R.copy >= 0)
@@ -1150,16 +1153,17 @@ __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x,
         }
         B.rb[ii] += bb.ri;
         B.mb[ii] += bb.mi;
-        B.wth[4 * ii + 0] += bb.Y;
-        B.wth[4 * ii + 1] += bb.G;
-        B.wth[4 * ii + 2] += bb.beta;
-        B.wth[4 * ii + 3] += bb.mu;
+        B.wth[kTh * ii + 0] += bb.Y;
+        B.wth[kTh * ii + 1] += bb.G;
+        B.wth[kTh * ii + 2] += bb.beta;
+        B.wth[kTh * ii + 3] += bb.mu;
+        B.wth[kTh * ii + 4] += bb.mur;
       }
       __syncthreads();
     }
     if (MESH && valid) {  // mesh walls, per atom (the planes' writes are behind the barrier)
       double Fb[3], Tb[3], xb[3] = {0., 0., 0.}, vb[3] = {0., 0., 0.}, wb[3] = {0., 0., 0.};
-      double rb = 0.0, mb = 0.0, th[4] = {0., 0., 0., 0.};
+      double rb = 0.0, mb = 0.0, th[kTh] = {0., 0., 0., 0., 0.};
       for (int k = 0; k < 3; k++) {
         Fb[k] = B.Fb[3 * i + k];
         Tb[k] = B.Tb[3 * i + k];
@@ -1172,7 +1176,7 @@ __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x,
       }
       B.rb[i] += rb;
       B.mb[i] += mb;
-      for (int k = 0; k < 4; k++) B.wth[4 * i + k] += th[k];
+      for (int k = 0; k < kTh; k++) B.wth[kTh * i + k] += th[k];
     }
   }
 }
@@ -1223,7 +1227,7 @@ __global__ void __launch_bounds__(kAB) kb_pairs(ADev s, ABar B, const double *x,
         Tjb[k] = local ? B.Tb[3 * j + k] : 0.0;
       }
       double d[3] = {0., 0., 0.}, vr[3] = {0., 0., 0.}, wi[3] = {0., 0., 0.}, wj[3] = {0., 0., 0.};
-      double ri = 0.0, rj = 0.0, mi = 0.0, mj = 0.0, th[4] = {0., 0., 0., 0.};
+      double ri = 0.0, rj = 0.0, mi = 0.0, mj = 0.0, th[kTh] = {0., 0., 0., 0., 0.};
       int st = kBondNone;
       if (BONDS && (touch || band)) {
         const BondArgs b = bond_in(s, a, x, i, ntimestep);
@@ -1270,6 +1274,7 @@ __global__ void __launch_bounds__(kAB) kb_pairs(ADev s, ABar B, const double *x,
         th[1] = bb.G;
         th[2] = bb.beta;
         th[3] = bb.mu;
+        th[4] = bb.mur;
       } else if (band) {
         for (int k = 0; k < 3; k++) B.sb[3 * p + k] = 0.0;  // history cleared: no dependence
       }
@@ -1283,7 +1288,7 @@ __global__ void __launch_bounds__(kAB) kb_pairs(ADev s, ABar B, const double *x,
       B.prj[p] = rj;
       B.pmi[p] = mi;
       B.pmj[p] = mj;
-      for (int k = 0; k < 4; k++) B.pth[4 * p + k] += th[k];  // summed over the segment's steps
+      for (int k = 0; k < kTh; k++) B.pth[kTh * p + k] += th[k];  // summed over the segment's steps
     }
     __syncthreads();
   }
@@ -1346,27 +1351,27 @@ __global__ void kb_gather_kick(ADev s, ABar B, const double *Fn, const double *T
   }
 }
 
-// deterministic sum of cnt rows of 4 doubles: per-block partials, then one
+// deterministic sum of cnt rows of kTh doubles: per-block partials, then one
 // thread per component adds them in block order into acc
-__global__ void kb_reduce4(const double *in, int cnt, double *part) {
-  __shared__ double sm[4][kAB];
-  double acc[4] = {0., 0., 0., 0.};
+__global__ void kb_reduce_th(const double *in, int cnt, double *part) {
+  __shared__ double sm[kTh][kAB];
+  double acc[kTh] = {0., 0., 0., 0., 0.};
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x)
-    for (int k = 0; k < 4; k++) acc[k] += in[4 * q + k];
-  for (int k = 0; k < 4; k++) sm[k][threadIdx.x] = acc[k];
+    for (int k = 0; k < kTh; k++) acc[k] += in[kTh * q + k];
+  for (int k = 0; k < kTh; k++) sm[k][threadIdx.x] = acc[k];
   __syncthreads();
   for (int st = kAB / 2; st > 0; st >>= 1) {
     if (threadIdx.x < st)
-      for (int k = 0; k < 4; k++) sm[k][threadIdx.x] += sm[k][threadIdx.x + st];
+      for (int k = 0; k < kTh; k++) sm[k][threadIdx.x] += sm[k][threadIdx.x + st];
     __syncthreads();
   }
   if (threadIdx.x == 0)
-    for (int k = 0; k < 4; k++) part[4 * blockIdx.x + k] = sm[k][0];
+    for (int k = 0; k < kTh; k++) part[kTh * blockIdx.x + k] = sm[k][0];
 }
-__global__ void kb_accum4(const double *part, int nb, double *acc) {
-  if (threadIdx.x >= 4) return;
+__global__ void kb_accum_th(const double *part, int nb, double *acc) {
+  if (threadIdx.x >= kTh) return;
   double v = acc[threadIdx.x];
-  for (int b = 0; b < nb; b++) v += part[4 * b + threadIdx.x];
+  for (int b = 0; b < nb; b++) v += part[kTh * b + threadIdx.x];
   acc[threadIdx.x] = v;
 }
 
@@ -1468,6 +1473,7 @@ struct dem_adjoint {
   int tape_mode = 2;          // 0 replay, 1 record every step, 2 record when it fits
   double tape_max_bytes = 0;  // budget of mode 2 (0: half the free device memory)
   int last_recorded = 0;
+  double last_grad_mur = 0.0;  // d(loss)/d(rolling coefficient) of the last gradient
 };
 
 #define ATRY(h, call)                                                \
@@ -1595,7 +1601,7 @@ int ensure_pairs(dem_adjoint *h, int np) {
   for (double **q : d3) ATRY(h, dmalloc(h->owned, q, 3 * (size_t)cap));
   double **d1[] = {&h->B.pri, &h->B.prj, &h->B.pmi, &h->B.pmj};
   for (double **q : d1) ATRY(h, dmalloc(h->owned, q, (size_t)cap));
-  ATRY(h, dmalloc(h->owned, &h->B.pth, 4 * (size_t)cap));
+  ATRY(h, dmalloc(h->owned, &h->B.pth, kTh * (size_t)cap));
   if (h->s.bonds) ATRY(h, dmalloc(h->owned, &h->B.bb, (size_t)kBondValues * cap));
   ATRY(h, dmalloc(h->owned, &h->s.active, (size_t)cap));
   h->pcap = cap;
@@ -1670,8 +1676,8 @@ void walls_vjp(dem_adjoint *h, const double *x, const double *vh, const double *
 void accumulate(dem_adjoint *h, const double *in, int cnt) {
   if (cnt <= 0) return;
   const int g = std::min(grid_of(cnt), 304);
-  kb_reduce4<<<g, kAB, 0, h->st>>>(in, cnt, h->part);
-  kb_accum4<<<1, 32, 0, h->st>>>(h->part, g, h->B.th);
+  kb_reduce_th<<<g, kAB, 0, h->st>>>(in, cnt, h->part);
+  kb_accum_th<<<1, 32, 0, h->st>>>(h->part, g, h->B.th);
 }
 
 void copyd(dem_adjoint *h, double *dst, const double *src, size_t count) {
@@ -1907,9 +1913,9 @@ int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *
   s.fm = (float)(4e-6 * (X + P));
   ATRY(h, dmalloc(h->owned, &h->B.wsb, W3));
   ATRY(h, dmalloc(h->owned, &h->wallF, W3));
-  ATRY(h, dmalloc(h->owned, &h->B.wth, 4 * (size_t)n));
-  ATRY(h, dmalloc(h->owned, &h->B.th, 4));
-  ATRY(h, dmalloc(h->owned, &h->part, 4 * (size_t)kMaxGrid));
+  ATRY(h, dmalloc(h->owned, &h->B.wth, kTh * (size_t)n));
+  ATRY(h, dmalloc(h->owned, &h->B.th, kTh));
+  ATRY(h, dmalloc(h->owned, &h->part, kTh * (size_t)kMaxGrid));
   ATRY(h, dmalloc(h->owned, &s.cell_of, (size_t)n));
   ATRY(h, dmalloc(h->owned, &s.cell_count, (size_t)ncell + 2));
   ATRY(h, dmalloc(h->owned, &s.cell_start, (size_t)ncell + 2));
@@ -2169,8 +2175,8 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   ATRY(h, cudaMemsetAsync(B.wsb, 0, W3 * sizeof(double), st));
   ATRY(h, cudaMemsetAsync(B.sb, 0, 3 * (size_t)h->pcap * sizeof(double), st));
   if (s.bonds) ATRY(h, cudaMemsetAsync(B.bb, 0, (size_t)kBondValues * h->pcap * sizeof(double), st));
-  ATRY(h, cudaMemsetAsync(B.th, 0, 4 * sizeof(double), st));
-  ATRY(h, cudaMemsetAsync(B.wth, 0, 4 * (size_t)n * sizeof(double), st));
+  ATRY(h, cudaMemsetAsync(B.th, 0, kTh * sizeof(double), st));
+  ATRY(h, cudaMemsetAsync(B.wth, 0, kTh * (size_t)n * sizeof(double), st));
   const double fw_seed = use_wall ? loss->w_wallforce * 2.0 * (fw - loss->wallforce_target) : 0.0;
   // the replay's tape of one segment (segments recorded in the forward pass
   // use their own)
@@ -2249,7 +2255,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     }
     // reverse over the segment's steps; the pair parameter adjoints of the
     // segment's list are summed per entry over its steps, then reduced
-    if (s.np > 0) ATRY(h, cudaMemsetAsync(B.pth, 0, 4 * (size_t)s.np * sizeof(double), st));
+    if (s.np > 0) ATRY(h, cudaMemsetAsync(B.pth, 0, kTh * (size_t)s.np * sizeof(double), st));
     for (int t = last; t >= first; t--) {
       const int q = t - first;
       const double *xs = T.x + S3 * q, *vh = T.vh + S3 * q, *wh = T.wh + S3 * q;
@@ -2296,10 +2302,10 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     accumulate(h, B.wth, n);     // every step's wall contacts
   }
   ATRY(h, cudaGetLastError());
-  std::vector<double> rb(n), mb(n), th(4);
+  std::vector<double> rb(n), mb(n), th(kTh);
   ATRY(h, cudaMemcpyAsync(rb.data(), B.rb, n * sizeof(double), cudaMemcpyDeviceToHost, st));
   ATRY(h, cudaMemcpyAsync(mb.data(), B.mb, n * sizeof(double), cudaMemcpyDeviceToHost, st));
-  ATRY(h, cudaMemcpyAsync(th.data(), B.th, 4 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  ATRY(h, cudaMemcpyAsync(th.data(), B.th, kTh * sizeof(double), cudaMemcpyDeviceToHost, st));
   ATRY(h, cudaEventRecord(h->ev[1], st));
   ATRY(h, cudaStreamSynchronize(st));
   cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
@@ -2308,6 +2314,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   *gE = th[0] * dYdE + th[1] * dGdE;
   *ge = th[2] * dbde;
   *gmu = th[3];
+  h->last_grad_mur = th[4];
   return DEM_OK;
 }
 
@@ -2347,6 +2354,12 @@ int dem_adjoint_set_tape(dem_adjoint *h, int mode, double max_bytes) {
   if (!h || mode < 0 || mode > 2 || !(max_bytes >= 0)) return DEM_ERR_BAD_ARG;
   h->tape_mode = mode;
   h->tape_max_bytes = max_bytes;
+  return DEM_OK;
+}
+
+int dem_adjoint_rolling_gradient(dem_adjoint *h, double *grad_mur) {
+  if (!h || !grad_mur) return DEM_ERR_BAD_ARG;
+  *grad_mur = h->last_grad_mur;
   return DEM_OK;
 }
 

@@ -48,6 +48,7 @@ def _bind(L):
     L.dem_adjoint_add_mesh.argtypes = [P, I, P, P, P]
     L.dem_adjoint_set_rolling.argtypes = [P, D]
     L.dem_adjoint_set_mesh_motion.argtypes = [P, I, P]
+    L.dem_adjoint_rolling_gradient.argtypes = [P, P]
     L.dem_adjoint_forward.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P]
     L.dem_adjoint_gradient.argtypes = [P, D, D, D, P, I, I, ctypes.POINTER(DemAdjointLoss), P, P, P, P, P]
     L.dem_adjoint_download.argtypes = [P, P, P, P]
@@ -171,7 +172,10 @@ class DemAdjoint:
         self._call("dem_adjoint_gradient", self.h, E, restitution, friction, api._p(r), nsteps, segment,
                    ctypes.byref(loss or make_loss(w_ke=1.0)), ctypes.byref(out), ctypes.byref(gE),
                    ctypes.byref(ge), ctypes.byref(gmu), api._p(gr))
-        return out.value, dict(E=gE.value, restitution=ge.value, friction=gmu.value, radius=gr)
+        gmr = D()
+        self._call("dem_adjoint_rolling_gradient", self.h, ctypes.byref(gmr))
+        return out.value, dict(E=gE.value, restitution=ge.value, friction=gmu.value, radius=gr,
+                               rolling_friction=gmr.value)
 
     def set_tape(self, mode, max_bytes=0.0):
         """Where the backward pass takes each step's record: 0 replay from

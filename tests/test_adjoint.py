@@ -231,6 +231,12 @@ def test_adjoint_with_cdt_rolling_matches_oracle():
 
         fd = _fd4(f, 1e-4 * base)
         assert abs(g[name] - fd) <= ADJ_RTOL * abs(fd), (name, g[name], fd)
+
+    def fr(dv):  # the rolling-friction coefficient
+        return _oracle_loss(_case(E, e, mu, rolling=mur + dv), "ke")
+
+    fd = _fd4(fr, 1e-3 * mur)
+    assert abs(g["rolling_friction"] - fd) <= ADJ_RTOL * abs(fd), (g["rolling_friction"], fd)
     gr = g["radius"]
     for i in np.argsort(-np.abs(gr))[:4]:
         def f(dv, i=i):
