@@ -359,8 +359,9 @@ const char *dem_version(void);
  * (DEM_ERR_BAD_ARG otherwise, with a message).  The loss:
  *   w_ke * (translational + rotational kinetic energy)
  * + w_height * (mean z - height_target)^2
- * + w_wallforce * (normal force of plane wall_id on the atoms, summed over
- *                  atoms at the last step - wallforce_target)^2
+ * + w_wallforce * (force of wall wall_id on the atoms, summed over atoms at
+ *                  the last step - wallforce_target)^2: a plane's normal
+ *                  component, a mesh's component wall_axis
  * Gradients are exact for this piecewise-smooth map away from switch
  * points (contacts opening or closing, stick/slip transitions).
  * ------------------------------------------------------------------------ */
@@ -381,7 +382,9 @@ typedef struct dem_adjoint_loss {
   double w_ke;
   double w_height, height_target;
   double w_wallforce, wallforce_target;
-  int wall_id;          /* plane index for the wall-force term, -1 none */
+  int wall_id;          /* wall of the wall-force term, -1 none: planes 0..nplanes-1
+                         * (their normal component), then meshes nplanes.. */
+  int wall_axis;        /* for a mesh: the component (0/1/2) of its total force */
 } dem_adjoint_loss;
 
 typedef struct dem_adjoint dem_adjoint;

@@ -691,7 +691,7 @@ __device__ inline int amesh_eval(const ADev &s, int m, int i, const double *x, c
 template <bool ROLL>
 __device__ inline void amesh_forward(const ADev &s, int i, const double *x, const double *vh, const double *wh,
                                      int upd, long long step, double f[3], double t[3], int *tst, double *tsh,
-                                     int *tnp) {
+                                     int *tnp, double *wallF) {
   for (int m = 0; m < s.nmeshes; m++) {
     const size_t base = (size_t)m * s.n + i;
     int *st = s.mst + base * kAMC;
@@ -702,10 +702,18 @@ __device__ inline void amesh_forward(const ADev &s, int i, const double *x, cons
       for (int u = 0; u < 3 * kAMC; u++) tsh[base * kAMC * 3 + u] = sh[u];
       tnp[base] = np;
     }
-    if (s.mcn[base] == 0) continue;
+    if (s.mcn[base] == 0) {
+      if (wallF)
+        for (int k = 0; k < 3; k++) wallF[(((size_t)s.nplanes + m) * s.n + i) * 3 + k] = 0.0;
+      continue;
+    }
     unsigned keep;
     bool bad = false;
-    amesh_eval<ROLL>(s, m, i, x, vh, wh, upd, step, st, sh, np, f, t, nullptr, keep, bad);
+    double fm[3] = {0., 0., 0.};
+    amesh_eval<ROLL>(s, m, i, x, vh, wh, upd, step, st, sh, np, fm, t, nullptr, keep, bad);
+    for (int k = 0; k < 3; k++) f[k] += fm[k];
+    if (wallF)  // meshes after the planes
+      for (int k = 0; k < 3; k++) wallF[(((size_t)s.nplanes + m) * s.n + i) * 3 + k] = fm[k];
     if (bad) s.err[1] = 1;
     s.mnp[base] = np;
   }
@@ -716,8 +724,8 @@ __device__ inline void amesh_forward(const ADev &s, int i, const double *x, cons
 // evaluation) become those of the state before it (the tape's)
 template <bool ROLL>
 __device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const double *x, const double *vh,
-                                 const double *wh, int upd, long long step, const int *tst, const double *tsh,
-                                 const int *tnp,
+                                 const double *wh, int upd, long long step, int seed_m, int seed_axis, double seed,
+                                 const int *tst, const double *tsh, const int *tnp,
                                  const double Fb[3], const double Tb[3], double xb[3], double vb[3], double wb[3],
                                  double &rb, double &mb, double th[kTh]) {
   for (int m = 0; m < s.nmeshes; m++) {
@@ -751,7 +759,7 @@ __device__ inline void amesh_vjp(const ADev &s, const ABar &B, int i, const doub
         amesh_contact_in(s, i, vh, wh, R.delta, R.hin, upd, vw, a);
         VjpBar bb;
         for (int d = 0; d < 3; d++) {
-          bb.F[d] = Fb[d];
+          bb.F[d] = Fb[d] + (m == seed_m && d == seed_axis ? seed : 0.0);
           bb.Ti[d] = Tb[d];
           bb.Tj[d] = 0.0;
           bb.s3[d] = upd ? hb[3 * u + d] : 0.0;
@@ -1028,7 +1036,7 @@ __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const
       __syncthreads();
     }
     if (valid) {
-      if (MESH) amesh_forward<ROLL>(s, i, s.x, vh, wh, upd, ntimestep, f, t, tape_mst, tape_msh, tape_mnp);  // after the planes
+      if (MESH) amesh_forward<ROLL>(s, i, s.x, vh, wh, upd, ntimestep, f, t, tape_mst, tape_msh, tape_mnp, wallF);
       const double a = s.ka[i], b = s.kb[i];
       for (int k = 0; k < 3; k++) {
         s.F[3 * i + k] = f[k];
@@ -1099,7 +1107,7 @@ __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x,
                                                 const double *wh, const double *ws_before, int upd, int seed_w,
                                                 double seed, const double *Fn1, const double *Tn1,
                                                 const int *tmst, const double *tmsh, const int *tmnp,
-                                                long long ntimestep) {
+                                                long long ntimestep, int seed_axis) {
   __shared__ int q[kAB];
   __shared__ int wcnt[kAB / 32];
   ABLOCKS(base, s.n) {
@@ -1168,7 +1176,8 @@ __global__ void __launch_bounds__(kAB) kb_walls(ADev s, ABar B, const double *x,
         Fb[k] = B.Fb[3 * i + k];
         Tb[k] = B.Tb[3 * i + k];
       }
-      amesh_vjp<ROLL>(s, B, i, x, vh, wh, upd, ntimestep, tmst, tmsh, tmnp, Fb, Tb, xb, vb, wb, rb, mb, th);
+      amesh_vjp<ROLL>(s, B, i, x, vh, wh, upd, ntimestep, seed_w - s.nplanes, seed_axis, seed, tmst, tmsh, tmnp, Fb,
+                      Tb, xb, vb, wb, rb, mb, th);
       for (int k = 0; k < 3; k++) {
         B.xb[3 * i + k] += xb[k];
         B.vb[3 * i + k] += vb[k];
@@ -1660,12 +1669,12 @@ void pairs_vjp(dem_adjoint *h, const double *x, const float4 *xf, const double *
 
 void walls_vjp(dem_adjoint *h, const double *x, const double *vh, const double *wh, const double *ws_before, int upd,
                int seed_w, double seed, const double *Fn1, const double *Tn1, const int *tmst, const double *tmsh,
-               const int *tmnp, long long ntimestep) {
+               const int *tmnp, long long ntimestep, int seed_axis = -1) {
   const ADev &s = h->s;
   const int g = grid_of(h->n);
 #define A_WALLS(R, M) \
   kb_walls<R, M><<<g, kAB, 0, h->st>>>(s, h->B, x, vh, wh, ws_before, upd, seed_w, seed, Fn1, Tn1, tmst, tmsh, tmnp, \
-                                       ntimestep)
+                                       ntimestep, seed_axis)
   if (s.rolling && s.nmeshes) A_WALLS(true, true);
   else if (s.rolling) A_WALLS(true, false);
   else if (s.nmeshes) A_WALLS(false, true);
@@ -1912,7 +1921,7 @@ int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *
   }
   s.fm = (float)(4e-6 * (X + P));
   ATRY(h, dmalloc(h->owned, &h->B.wsb, W3));
-  ATRY(h, dmalloc(h->owned, &h->wallF, W3));
+  ATRY(h, dmalloc(h->owned, &h->wallF, 3 * (size_t)(s.nplanes + kAMeshes) * n));  // planes, then meshes
   ATRY(h, dmalloc(h->owned, &h->B.wth, kTh * (size_t)n));
   ATRY(h, dmalloc(h->owned, &h->B.th, kTh));
   ATRY(h, dmalloc(h->owned, &h->part, kTh * (size_t)kMaxGrid));
@@ -2107,12 +2116,12 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   int flag = 0, mflag = 0;
   ATRY(h, cudaMemcpyAsync(&flag, s.err, sizeof(int), cudaMemcpyDeviceToHost, st));
   ATRY(h, cudaMemcpyAsync(&mflag, s.err + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-  std::vector<double> xf(S3), vf(S3), wf(S3), wallf(W3);
+  const size_t WF = 3 * (size_t)(s.nplanes + s.nmeshes) * n;
+  std::vector<double> xf(S3), vf(S3), wf(S3), wallf(std::max<size_t>(1, WF));
   ATRY(h, cudaMemcpyAsync(xf.data(), s.x, S3 * sizeof(double), cudaMemcpyDeviceToHost, st));
   ATRY(h, cudaMemcpyAsync(vf.data(), s.v, S3 * sizeof(double), cudaMemcpyDeviceToHost, st));
   ATRY(h, cudaMemcpyAsync(wf.data(), s.w, S3 * sizeof(double), cudaMemcpyDeviceToHost, st));
-  if (s.nplanes > 0)
-    ATRY(h, cudaMemcpyAsync(wallf.data(), h->wallF, W3 * sizeof(double), cudaMemcpyDeviceToHost, st));
+  if (WF) ATRY(h, cudaMemcpyAsync(wallf.data(), h->wallF, WF * sizeof(double), cudaMemcpyDeviceToHost, st));
   ATRY(h, cudaEventRecord(h->ev[1], st));
   ATRY(h, cudaStreamSynchronize(st));
   float ms = 0.f;
@@ -2139,9 +2148,14 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   }
   hz /= n;
   const int lw = loss->wall_id;
-  const bool use_wall = lw >= 0 && lw < s.nplanes;
+  const bool use_wall = lw >= 0 && lw < s.nplanes + s.nmeshes;
+  if (lw >= s.nplanes && use_wall && (loss->wall_axis < 0 || loss->wall_axis > 2)) {
+    h->err = "wall_axis must be 0, 1 or 2 for a mesh";
+    return DEM_ERR_BAD_ARG;
+  }
+  const int wax = lw < s.nplanes ? (use_wall ? s.pax[lw] : 0) : loss->wall_axis;
   if (use_wall)
-    for (int i = 0; i < n; i++) fw += wallf[((size_t)lw * n + i) * 3 + s.pax[lw]];
+    for (int i = 0; i < n; i++) fw += wallf[((size_t)lw * n + i) * 3 + wax];
   *loss_out = loss->w_ke * ke + loss->w_height * (hz - loss->height_target) * (hz - loss->height_target) +
               (use_wall ? loss->w_wallforce * (fw - loss->wallforce_target) * (fw - loss->wallforce_target) : 0.0);
   if (!backward) return DEM_OK;
@@ -2261,7 +2275,8 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       const double *xs = T.x + S3 * q, *vh = T.vh + S3 * q, *wh = T.wh + S3 * q;
       walls_vjp(h, xs, vh, wh, T.ws + W3 * q, 1, t == nsteps ? lw : -1, t == nsteps ? fw_seed : 0.0, T.F + S3 * q,
                 T.T + S3 * q, s.nmeshes ? T.mst + NBM * kAMC * q : nullptr,
-                s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr, s.nmeshes ? T.mnp + NBM * q : nullptr, t);
+                s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr, s.nmeshes ? T.mnp + NBM * q : nullptr, t,
+                loss->wall_axis);
       if (s.np > 0)
         pairs_vjp(h, xs, T.xf + (size_t)n * q, vh, wh, T.sh + 3 * PS * q,
                   s.bonds ? T.bh + kBondValues * PS * q : nullptr, 1, t);

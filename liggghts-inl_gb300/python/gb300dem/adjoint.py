@@ -34,7 +34,7 @@ class DemAdjointConfig(ctypes.Structure):
 
 class DemAdjointLoss(ctypes.Structure):
     _fields_ = [("w_ke", D), ("w_height", D), ("height_target", D), ("w_wallforce", D),
-                ("wallforce_target", D), ("wall_id", ctypes.c_int)]
+                ("wallforce_target", D), ("wall_id", ctypes.c_int), ("wall_axis", ctypes.c_int)]
 
 
 def _bind(L):
@@ -62,8 +62,10 @@ def _bind(L):
 
 
 def make_loss(w_ke=0.0, w_height=0.0, height_target=0.0, w_wallforce=0.0, wallforce_target=0.0,
-              wall_id=-1):
-    return DemAdjointLoss(w_ke, w_height, height_target, w_wallforce, wallforce_target, wall_id)
+              wall_id=-1, wall_axis=2):
+    """wall_id: planes first, then meshes; wall_axis: the force component of a
+    mesh (a plane takes its normal)"""
+    return DemAdjointLoss(w_ke, w_height, height_target, w_wallforce, wallforce_target, wall_id, wall_axis)
 
 
 def _f64(a, shape=None):

@@ -92,6 +92,8 @@ def _oracle(case, nsteps=NSTEPS):
 
 
 def _oracle_loss(case, kind):
+    if kind == "wall":  # z force of the floor mesh (walls: the ceiling plane, then the mesh) at the last step
+        return float(_oracle(case).diagnostics()["wall_force"][1][2] ** 2)
     a = sort_by_tag(_oracle(case).atoms())
     if kind == "ke":
         m, r = a["rmass"], a["radius"]
@@ -101,6 +103,8 @@ def _oracle_loss(case, kind):
 
 def _spec(kind):
     from gb300dem.adjoint import make_loss
+    if kind == "wall":
+        return make_loss(w_wallforce=1.0, wallforce_target=0.0, wall_id=1, wall_axis=2)
     return make_loss(w_ke=1.0) if kind == "ke" else make_loss(w_height=1.0, height_target=2.5e-3)
 
 
@@ -257,6 +261,41 @@ def test_adjoint_with_moving_mesh_matches_oracle():
             r = r0.copy()
             r[i] += dv
             return _oracle_loss(_case(radius=r, floor="rising"), "ke")
+
+        fdi = _fd4(f, 1e-6 * r0[i])
+        assert abs(gr[i] - fdi) <= ADJ_RTOL * abs(fdi), (int(i), gr[i], fdi)
+    eng.close()
+
+
+@pytest.mark.gpu
+def test_adjoint_mesh_wallforce_matches_oracle_fd():
+    """The wall-force term on a mesh wall: the squared z force of the floor
+    mesh on the bed at the last step (wall_id counts the planes first, then
+    the meshes).  Its value against the oracle's per-wall force, its
+    gradients against the oracle's differences."""
+    from gb300dem.adjoint import DemAdjoint
+    E, e, mu = 1e7, 0.6, 0.5
+    c = _case(E, e, mu)
+    r0 = c["atoms"]["radius"].copy()
+    eng = DemAdjoint(c)
+    val, g = eng.gradient(E, e, mu, nsteps=NSTEPS, segment=SEG, loss=_spec("wall"))
+    assert val > 0
+    assert np.isclose(val, _oracle_loss(c, "wall"), rtol=1e-8, atol=0)
+    for name, base, key in (("E", E, "E"), ("restitution", e, "rest")):
+        def f(dv, key=key, base=base):
+            kw = dict(E=E, rest=e, frict=mu)
+            kw[key] = base + dv
+            return _oracle_loss(_case(**kw), "wall")
+
+        fd = _fd4(f, 1e-4 * base)
+        assert abs(fd) > 0, name
+        assert abs(g[name] - fd) <= ADJ_RTOL * abs(fd), (name, g[name], fd)
+    gr = g["radius"]
+    for i in np.argsort(-np.abs(gr))[:4]:
+        def f(dv, i=i):
+            r = r0.copy()
+            r[i] += dv
+            return _oracle_loss(_case(radius=r), "wall")
 
         fdi = _fd4(f, 1e-6 * r0[i])
         assert abs(gr[i] - fdi) <= ADJ_RTOL * abs(fdi), (int(i), gr[i], fdi)
