@@ -26,6 +26,17 @@ void PairGranGB300::settings(int nargs, char **args) {
   PairGranProxy::settings(nargs, args);
   args_.assign(args, args + nargs);
 
+  // Force::create_pair names a suffixed style "gran/gb300", but the
+  // reference finds the granular pair by its exact name "gran"
+  // (FixContactHistory::init, src/fix_contact_history.cpp:218;
+  // FixCheckTimestepGran::init, src/fix_check_timestep_gran.cpp:153).  The
+  // style therefore reports the base name, as the class it stands in for.
+  if (force->pair == this && force->pair_style && strcmp(force->pair_style, "gran/gb300") == 0) {
+    delete[] force->pair_style;
+    force->pair_style = new char[5];
+    strcpy(force->pair_style, "gran");
+  }
+
   if (contact_match("normal", "hertz")) normal_ = DEM_NORMAL_HERTZ;
   else if (contact_match("normal", "hooke")) normal_ = DEM_NORMAL_HOOKE;
   else error->all(FLERR, "pair gran/gb300: normal model must be hertz or hooke");

@@ -37,7 +37,8 @@ using namespace FixConst;
 /* run_style verlet/gb300 [capacity N]: N atoms of device room for insertion
    fixes (default: twice the atoms at the first run, at least 10,000 more) */
 VerletGB300::VerletGB300(LAMMPS *lmp, int narg, char **arg)
-    : Verlet(lmp, narg, arg), h_(NULL), pair_(NULL), capacity_(0), gravity_(NULL), natoms_(-1), stamp_(0) {
+    : Verlet(lmp, narg, arg), h_(NULL), pair_(NULL), capacity_(0), gravity_(NULL), nve_(NULL), natoms_(-1),
+      stamp_(0) {
   for (int k = 1; k + 1 < narg; k++)
     if (strcmp(arg[k], "capacity") == 0) capacity_ = atoi(arg[k + 1]);
 }
@@ -62,6 +63,7 @@ void VerletGB300::collect_styles() {
   movers_.clear();
   inserts_.clear();
   gravity_ = NULL;
+  nve_ = NULL;
   int nve = 0;
   const int per_step = INITIAL_INTEGRATE | POST_INTEGRATE | PRE_EXCHANGE | PRE_NEIGHBOR | PRE_FORCE |
                        POST_FORCE | FINAL_INTEGRATE | END_OF_STEP | PRE_INITIAL_INTEGRATE |
@@ -75,7 +77,8 @@ void VerletGB300::collect_styles() {
       walls_.push_back(w);
       continue;
     }
-    if (dynamic_cast<FixNVESphereGB300 *>(f)) {
+    if (FixNVESphereGB300 *nv = dynamic_cast<FixNVESphereGB300 *>(f)) {
+      nve_ = nv;
       nve++;
       continue;
     }
@@ -236,6 +239,12 @@ void VerletGB300::create_device() {
     if (any) check(dem_upload_wall_history(h_, walls_[k]->device_wall_id(), &wh[0]), "dem_upload_wall_history");
   }
   natoms_ = atom->natoms;
+  if (comm->me == 0) {
+    char msg[256];
+    snprintf(msg, sizeof msg, "verlet/gb300: %d atoms, %d walls resident on the GPU\n", n, (int)walls_.size());
+    if (screen) fputs(msg, screen);
+    if (logfile) fputs(msg, logfile);
+  }
 }
 
 /* the device state into the host's local atoms; host atoms the device no
@@ -354,11 +363,18 @@ void VerletGB300::setup_minimal(int) {
 }
 
 /* FixInsert::pre_exchange of the insertion step s runs on the host with the
-   state of step s-1 (the device has not yet drifted to step s); the new atoms
-   then join the device at step s after its initial integration, with a
-   rebuild (dem_insert_atoms), as the reference adds them.  The only
-   difference: the fix's overlap checks see the positions one drift earlier. */
+   state the reference gives it.  In Verlet::run the fix is called after the
+   initial integration of step s, before pbc and the ghost exchange
+   (src/verlet.cpp:298-312), so its overlap checks (FixInsert::load_xnear,
+   local and ghost atoms) see the local atoms drifted to step s and the
+   ghosts still at step s-1.  The host holds the device state of step s-1:
+   the ghosts are built from it, then the local atoms are drifted by the
+   reference's own FixNVESphere::initial_integrate, then the fix inserts.
+   The new atoms join the device at step s after its initial integration,
+   with a rebuild (dem_insert_atoms), as the reference adds them.  The host
+   copy of the existing atoms is overwritten by the next download. */
 void VerletGB300::insert_due(bigint step) {
+  bool drifted = false;
   for (size_t k = 0; k < inserts_.size(); k++) {
     FixInsert *fi = inserts_[k];
     if (!fi->force_reneighbor || fi->next_reneighbor != step) continue;
@@ -371,6 +387,10 @@ void VerletGB300::insert_due(bigint step) {
     const int n0 = atom->nlocal;
     const bigint ts = update->ntimestep;
     update->ntimestep = step;
+    if (!drifted) {
+      nve_->FixNVESphere::initial_integrate(0);
+      drifted = true;
+    }
     fi->pre_exchange();
     update->ntimestep = ts;
     const int k_new = atom->nlocal - n0;

@@ -71,6 +71,7 @@ class VerletGB300 : public Verlet {
   std::vector<class FixInsert *> inserts_;
   long capacity_;
   class FixGravityGB300 *gravity_;
+  class FixNVESphereGB300 *nve_;
   bigint natoms_;
   uint64_t stamp_;
 

@@ -6,10 +6,13 @@
 # files: for every style class, one #include per header that declares it.
 # This script is our own recipe; it does not run the reference's build system.
 #
-# usage: gen_styles.sh REF_SRC_DIR OUT_DIR
+# usage: gen_styles.sh REF_SRC_DIR OUT_DIR [EXTRA_STYLE_DIR]
+# With EXTRA_STYLE_DIR, the style headers found there (the GB300 suffix
+# styles) are registered after the reference's own.
 set -e
 REF="$1"
 OUT="$2"
+EXTRA="$3"
 mkdir -p "$OUT"
 
 style () {   # $1 = search string, $2 = header prefix, $3 = style file suffix
@@ -18,6 +21,11 @@ style () {   # $1 = search string, $2 = header prefix, $3 = style file suffix
   for f in $(cd "$REF" && grep -sl "$1" $2*.h 2>/dev/null); do
     echo "#include \"$f\"" >> "$tmp"
   done
+  if [ -n "$EXTRA" ]; then
+    for f in $(cd "$EXTRA" && grep -sl "$1" $2*.h 2>/dev/null); do
+      echo "#include \"$f\"" >> "$tmp"
+    done
+  fi
   mv "$tmp" "$OUT/style_$3.h"
 }
 

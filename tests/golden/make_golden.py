@@ -91,7 +91,22 @@ def fmt(v):
     return "%.17g" % v
 
 
-def write_inputs(case, d, nsteps, snaps):
+DUMP_COLUMNS = ("id type x y z vx vy vz omegax omegay omegaz fx fy fz tqx tqy tqz radius")
+
+
+def write_inputs(case, d, nsteps, snaps=None, dump_every=None, extra=(), run_style=False):
+    """Writes data.case and in.case (plus mesh STL files) into d.
+
+    snaps: steps at which the snapshot fix of the reference build writes its
+    binary state (golden generation).  dump_every: instead or as well, a
+    "dump custom" of every atom's id, type, x, v, omega, f, torque and
+    radius in %.17g every that many steps, sorted by id (dump.<step>.txt).
+    extra: further input lines placed after the integrator fix (insertion
+    fixes, regions).  run_style: adds "run_style verlet", which selects the
+    reference's default integrator explicitly; under "-sf gb300" that command
+    selects verlet/gb300 (Update::create_integrate, src/update.cpp:342-377),
+    while the integrator LAMMPS creates at start-up is never suffixed
+    (src/update.cpp:103-106)."""
     a = case["atoms"]
     n = len(a["tag"])
     mat = case["material"]
@@ -165,9 +180,17 @@ def write_inputs(case, d, nsteps, snaps):
                         fmt(ro["period"])))
     if not all(case["periodic"]):
         s.append("thermo_modify lost ignore")
-    s += ["fix integr all nve/sphere",
-          "fix snap all oracle/snapshot snap %s" % " ".join(str(t) for t in snaps),
-          "thermo 100", "run %d" % nsteps]
+    s.append("fix integr all nve/sphere")
+    s += list(extra)
+    if snaps is not None:
+        s.append("fix snap all oracle/snapshot snap %s" % " ".join(str(t) for t in snaps))
+    if dump_every:
+        ncol = len(DUMP_COLUMNS.split())
+        s += ["dump dmp all custom %d dump.*.txt %s" % (dump_every, DUMP_COLUMNS),
+              'dump_modify dmp sort id format "%%d %%d%s"' % (" %.17g" * (ncol - 2))]
+    if run_style:
+        s.append("run_style verlet")
+    s += ["thermo 100", "run %d" % nsteps]
     open(os.path.join(d, "in.case"), "w").write("\n".join(s) + "\n")
 
 

@@ -20,7 +20,8 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 STYLES = os.path.join(ROOT, "liggghts-inl_gb300", "styles")
-REF_SRC = os.environ.get("LIGGGHTS_REFERENCE_SRC", "/root/reference/src")
+# the unmodified reference sources as oracle/ref/Makefile stages them
+REF_SRC = os.environ.get("LIGGGHTS_REFERENCE_SRC", os.path.join(ROOT, "oracle", "_ref", "src"))
 
 EXPECTED = {
     "pair_gran_gb300.h": ("PairStyle", "gran/gb300", "PairGranGB300", "PairGranProxy"),
