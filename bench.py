@@ -7,9 +7,9 @@ One bench step = one DEM timestep (Verlet iteration) of the whole system.
 value: device-timed throughput with the state resident in HBM (CUDA events
 on the library's stream around dem_step(K)).  e2e: the same metric through
 the C ABI with host buffers: upload + setup + K steps + download, host
-copies inside the timed region.  --impl reference times the CPU oracle
-(restatement of the reference's path; the reference binary itself is not
-built on the GPU machine) on all host cores.  N>1: independent replicas,
+copies inside the timed region.  --impl reference times the reference
+binary built from the unmodified reference sources (oracle/_ref/lmp_ref) on
+the same workload, one process per host core.  N>1: independent replicas,
 one per rank (the path has no exchange step), "scaling": "weak".
 """
 import argparse
@@ -188,15 +188,62 @@ def _oracle_sample_worker(args):
 
 
 def cpu_sample(name, cores, steps, warm=2, scale=0.01):
-    """Times the oracle on a bounded sample (10k-atom slice of the workload)."""
+    """Times the oracle port (the C restatement) on `cores` independent
+    replicas of the workload at the given scale, one per process."""
     from oracle import binding
     binding.build()
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        res = pool.map(_oracle_sample_worker, [(name, scale, 100 + k, warm, steps) for k in range(cores)])
+        res = pool.map(_oracle_sample_worker, [(name, scale, 2024 + k, warm, steps) for k in range(cores)])
     tot = sum(n * s for n, s, _ in res)
     tmax = max(dt for _, _, dt in res)
     return tot / tmax, res
+
+
+def ref_binary():
+    """The reference binary oracle/ref/Makefile builds from the unmodified
+    reference sources (serial, its own MPI stubs, -O3, the GPU path's contact
+    models compiled in through the reference's whitelist), or None."""
+    p = os.path.join(ROOT, "oracle", "_ref", "lmp_ref")
+    return p if os.path.isfile(p) and os.access(p, os.X_OK) else None
+
+
+def lmp_sample(name, nproc, steps, warm, seed=2024):
+    """Times the reference binary on the full workload: one input script
+    (seeded data file, STL mesh, the reference's own commands), `nproc`
+    independent processes (one per host core), each "run warm" then "run
+    steps"; the timed figure is the reference's "Loop time" of the second
+    run (output off inside it).  Returns (particle-steps/s of all processes
+    over the slowest one's loop time, [(atoms, steps, loop s)])."""
+    import shutil
+    from oracle.lmp_input import write_inputs
+    exe = ref_binary()
+    case, _ = workload(name, seed=seed)
+    n0 = len(case["atoms"]["tag"])
+    top = tempfile.mkdtemp(prefix="lmp_ref_")
+    try:
+        write_inputs(case, top, 0, runs=[warm, steps])
+        files = [f for f in os.listdir(top) if os.path.isfile(os.path.join(top, f))]
+        procs = []
+        for k in range(nproc):
+            d = os.path.join(top, "p%d" % k)
+            os.makedirs(d)
+            for f in files:
+                os.symlink(os.path.join(top, f), os.path.join(d, f))
+            procs.append(subprocess.Popen([exe, "-in", "in.case", "-log", "log.case", "-screen", "screen.case"],
+                                          cwd=d, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL))
+        res = []
+        for k, p in enumerate(procs):
+            rc = p.wait()
+            log = open(os.path.join(top, "p%d" % k, "log.case")).read()
+            loops = [ln.split() for ln in log.splitlines() if ln.startswith("Loop time of")]
+            if rc != 0 or len(loops) < 2:
+                raise RuntimeError("reference run failed (rc %d): %s" % (rc, log[-1500:]))
+            res.append((n0, int(loops[-1][8]), float(loops[-1][3])))
+    finally:
+        shutil.rmtree(top, ignore_errors=True)
+    tot = sum(n * s for n, s, _ in res)
+    return tot / max(t for _, _, t in res), res
 
 
 # ----------------------------------------------------------------------------
@@ -222,30 +269,54 @@ def replica_throughput(dev_ms, atoms, steps, dist=None, device=None):
 # ----------------------------------------------------------------------------
 
 def run_reference(args):
+    """The reference's own CPU implementation of the path on the host cores:
+    the reference binary (oracle/_ref/lmp_ref) on the full workload, one
+    serial process per core (no MPI library on the machine: the build is the
+    reference's serial one against its MPI stubs), beside the C port on one
+    core for the port-to-binary ratio.  Without the binary (no reference
+    sources staged), the port on all cores stands in, kind "port"."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     cores = os.cpu_count() or 1
     steps = max(1, args.steps)
+    warm = max(1, args.warmup)
     t0 = time.perf_counter()
-    val, res = cpu_sample(args.workload, cores, steps, warm=max(1, args.warmup))
+    exe = ref_binary()
+    if exe:
+        val, res = lmp_sample(args.workload, cores, steps, warm)
+        pv, pres = cpu_sample(args.workload, 1, steps, warm=1, scale=1.0)
+        kind = "reference"
+        sample = ("reference binary (oracle/_ref/lmp_ref: unmodified reference sources, serial, -O3, "
+                  "whitelisted contact models) on the full %d-atom %s, %d independent processes "
+                  "(one per core), 'run %d' then the timed 'run %d' (its Loop time)"
+                  % (res[0][0], args.workload, cores, warm, steps))
+        per_proc = statistics.mean(n * s / t for n, s, t in res)
+        port = {"value": pv, "cores": 1, "per_process_binary": per_proc, "port_over_binary": pv / per_proc,
+                "sample": "oracle port (oracle/dem_oracle.c) on the same full workload, 1 thread, "
+                          "%d steps after 1" % steps}
+        config = {"workload": args.workload, "atoms": res[0][0], "processes": cores}
+        ms = 1e3 * max(t for _, _, t in res) / steps
+    else:
+        val, res = cpu_sample(args.workload, cores, steps, warm=warm)
+        kind = "port"
+        sample = ("%d independent replicas (one per core) of a %d-atom slice of %s, %d timed steps each "
+                  "(the reference binary is not built here)" % (cores, res[0][0], args.workload, steps))
+        port = None
+        config = {"workload": args.workload, "sample_atoms": res[0][0], "replicas": cores}
+        ms = 1e3 * max(r[2] for r in res) / steps
     wall = time.perf_counter() - t0
-    _, desc = workload(args.workload, scale=0.01)
-    sample = ("%d independent replicas (one per core) of a %d-atom slice of %s, %d timed steps each"
-              % (cores, res[0][0], args.workload, steps))
     line = {"metric": METRICS.get(args.workload, METRIC), "value": val, "unit": "particle-steps/s",
-            "n_gpus": args.gpus,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * max(r[2] for r in res) / steps,
+            "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "impl": "reference",
-            "config": {"workload": args.workload, "sample_atoms": res[0][0], "replicas": cores},
-            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "data": "synthetic (seeded)", "impl": "reference", "config": config,
+            "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": kind,
                              "sample": sample},
             "e2e": {"value": val, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "note": "CPU restatement of the reference path (oracle/dem_oracle.c, pinned to the "
-                    "reference binary by tests/golden); the reference binary is built only where its "
-                    "sources are present", "wall_s": wall}
+            "wall_s": wall}
+    if port:
+        line["port"] = port
     print(json.dumps(line))
 
 
@@ -283,18 +354,27 @@ def run_gb300(args):
     kp = g.kernel_times()
     g.profile(False)
     # ---- e2e through the C ABI with host buffers
+    # (the caller's host arrays exist before the run, as the reference's
+    # atom->x, atom->v, ... do; the device reads and fills them)
     a = case["atoms"]
     host = {k: np.ascontiguousarray(v) for k, v in a.items()}
     g2 = api.DemSystem({k: v for k, v in case.items() if k != "atoms"})
+    hout = g2.atom_buffers(n)
     t0 = time.perf_counter()
     g2.upload(host)
+    t1 = time.perf_counter()
     g2.setup()
+    t2 = time.perf_counter()
     g2.step(args.steps)
-    out = g2.atoms()
-    e2e_s = time.perf_counter() - t0
+    t3 = time.perf_counter()
+    out = g2.atoms(hout)
+    t4 = time.perf_counter()
+    e2e_s = t4 - t0
     h2d = n * (3 * 3 * 8 + 2 * 8 + 2 * 4)
     d2h = n * (5 * 3 * 8 + 2 * 8 + 2 * 4)
-    assert out["x"].shape == (n, 3)
+    assert out["x"].shape[1] == 3 and len(out["x"]) <= n
+    phases = {"upload_ms": 1e3 * (t1 - t0), "setup_ms": 1e3 * (t2 - t1), "steps_ms": 1e3 * (t3 - t2),
+              "download_ms": 1e3 * (t4 - t3), "host_direct": g2.stats()["host_direct"]}
     e2e, _ = replica_throughput(e2e_s * 1e3, n, args.steps, dist, device="cuda")  # slowest rank
     g2.close()
     # ---- roofline of the dominant kernel
@@ -358,11 +438,17 @@ def run_gb300(args):
     # ---- CPU baseline (oracle port, bounded sample, rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cores = 1
-        v, res = cpu_sample(args.workload, cores, steps=args.cpu_steps, warm=1)
-        cpu = {"value": v, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-               "sample": "oracle (CPU restatement, pinned to the reference binary) on a %d-atom slice "
-                         "of %s, %d steps, 1 thread" % (res[0][0], args.workload, args.cpu_steps)}
+        if ref_binary() and args.scale == 1.0:
+            v, res = lmp_sample(args.workload, 1, args.cpu_steps, 1)
+            cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "reference",
+                   "sample": "reference binary (oracle/_ref/lmp_ref, serial, -O3) on the full %d-atom %s, "
+                             "'run 1' then the timed 'run %d' (its Loop time), 1 process"
+                             % (res[0][0], args.workload, args.cpu_steps)}
+        else:
+            v, res = cpu_sample(args.workload, 1, steps=args.cpu_steps, warm=1)
+            cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+                   "sample": "oracle (CPU restatement, pinned to the reference binary) on a %d-atom slice "
+                             "of %s, %d steps, 1 thread" % (res[0][0], args.workload, args.cpu_steps)}
     if rank == 0:
         line = {"metric": METRICS.get(args.workload, METRIC), "value": value, "unit": "particle-steps/s",
                 "n_gpus": world,
@@ -373,7 +459,8 @@ def run_gb300(args):
                                pairs=npairs, rebuilds_total=st["nrebuilds"]),
                 "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d / args.steps,
                         "d2h_bytes_per_step": d2h / args.steps,
-                        "note": "upload+setup+K steps+download through the C ABI, host buffers"},
+                        "note": "upload+setup+K steps+download through the C ABI, host buffers",
+                        "phases": phases},
                 "gpu_launches": kt["kernel_launches"],
                 "roofline": roof, "cpu_baseline": cpu, "clocks": cl, "wall_s": wall,
                 "kernel_ms_per_step": {"pair": pair_ms, "particle": part_ms, "wall": wall_ms,

@@ -78,6 +78,11 @@ typedef struct dem_stats {
   int device;                  /* CUDA ordinal */
   int pair_capacity;
   double last_step_ms;         /* device time of the last dem_step call */
+  int host_direct;             /* 1: dem_upload_atoms / dem_download_atoms kernels read and write the
+                                  caller's arrays in place (the device reaches pageable host memory
+                                  through the host's page tables); 0: through device staging copies */
+  int mesh_slot_capacity;      /* history slots per atom of the widest mesh (grows on demand, as the
+                                  reference's FixContactHistoryMesh pages do) */
 } dem_stats;
 
 typedef struct dem_handle dem_handle;

@@ -35,7 +35,17 @@ struct dem_handle {
   int device = 0;
   std::string err;
   bool have_params = false, have_atoms = false, setup_done = false;
-  std::vector<void *> allocs_atoms, allocs_pairs, allocs_misc;
+  std::vector<void *> allocs_atoms, allocs_pairs, allocs_misc, allocs_cells;
+  std::vector<void *> allocs_mslots[kMaxMeshes], allocs_tclist[kMaxMeshes];  // grown on overflow
+  // atom transfers: kernels read and write the caller's arrays directly
+  // when the device reaches pageable host memory through the host's page
+  // tables (cudaDevAttrPageableMemoryAccessUsesHostPageTables, Grace
+  // C2C systems); else through this device staging buffer
+  bool host_direct = false;
+  void *stage = nullptr;
+  size_t stage_bytes = 0;
+  UploadCheck *chk = nullptr;       // device: k_upload_atoms results
+  UploadCheck *chk_host = nullptr;  // pinned host copy
   double *diag_buf = nullptr;  // dem_get_diagnostics partial sums
   LaunchCfg lc{152 * 8};
   float last_ms = 0.f;
@@ -131,9 +141,105 @@ static cudaError_t dalloc(std::vector<void *> &list, T **p, size_t n) {
   return e;
 }
 
+// One device allocation carved into 256-byte aligned arrays: a carving
+// function runs once to size the block (base unset), then again to hand out
+// the pointers.  Replaces one cudaMalloc per array.
+struct Arena {
+  char *base = nullptr;
+  size_t off = 0;
+  template <typename T>
+  void take(T **p, size_t n) {
+    off = (off + 255) & ~(size_t)255;
+    if (base) *p = reinterpret_cast<T *>(base + off);
+    off += std::max<size_t>(n, 1) * sizeof(T);
+  }
+  cudaError_t commit(std::vector<void *> &list) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(off, 256));
+    if (e == cudaSuccess) {
+      list.push_back(q);
+      base = static_cast<char *>(q);
+    }
+    off = 0;
+    return e;
+  }
+};
+
 static void free_list(std::vector<void *> &l) {
   for (void *p : l) cudaFree(p);
   l.clear();
+}
+
+// Per-atom candidate lists and history slots of mesh k (the pages of
+// FixContactHistoryMesh) at `cap` per atom.  With keep, the live slots
+// (buffer 0) move to the new arrays and the added rows start empty; the
+// candidate lists are rebuilt by the resumed k_mesh_cand.
+static int alloc_mesh_slots(dem_handle *h, int k, int cap, bool keep) {
+  Sys &s = h->s;
+  MeshDev &M = s.meshes[k];
+  const size_t nmax = s.nmax;
+  MeshDev N = M;
+  std::vector<void *> nl;
+  auto carve = [&](Arena &ar) {
+    ar.take(&N.cand_n, nmax);
+    ar.take(&N.cand, (size_t)cap * nmax);
+    for (int b = 0; b < 2; b++) {
+      ar.take(&N.nslot[b], nmax);
+      ar.take(&N.npart[b], nmax);
+      ar.take(&N.slot_tri[b], (size_t)cap * nmax);
+      ar.take(&N.slot_hist[b], (size_t)3 * cap * nmax);
+    }
+  };
+  Arena ar;
+  carve(ar);
+  CUDA_TRY(h, ar.commit(nl));
+  carve(ar);
+  const size_t old = keep ? (size_t)std::min(M.ccap, cap) : 0;
+  if (keep) {
+    CUDA_TRY(h, cudaMemcpyAsync(N.cand_n, M.cand_n, nmax * sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.nslot[0], M.nslot[0], nmax * sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.npart[0], M.npart[0], nmax * sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.slot_tri[0], M.slot_tri[0], old * nmax * sizeof(int), cudaMemcpyDeviceToDevice,
+                                h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.slot_hist[0], M.slot_hist[0], 3 * old * nmax * sizeof(double),
+                                cudaMemcpyDeviceToDevice, h->st));
+  } else {
+    CUDA_TRY(h, cudaMemsetAsync(N.cand_n, 0, nmax * sizeof(int), h->st));
+    CUDA_TRY(h, cudaMemsetAsync(N.nslot[0], 0, nmax * sizeof(int), h->st));
+    CUDA_TRY(h, cudaMemsetAsync(N.npart[0], 0, nmax * sizeof(int), h->st));
+  }
+  CUDA_TRY(h, cudaMemsetAsync(N.slot_tri[0] + old * nmax, 0xff, ((size_t)cap - old) * nmax * sizeof(int), h->st));
+  CUDA_TRY(h, cudaMemsetAsync(N.slot_hist[0] + 3 * old * nmax, 0, 3 * ((size_t)cap - old) * nmax * sizeof(double),
+                              h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));  // the old arrays are read until here
+  free_list(h->allocs_mslots[k]);
+  h->allocs_mslots[k] = nl;
+  M.cand_n = N.cand_n;
+  M.cand = N.cand;
+  for (int b = 0; b < 2; b++) {
+    M.nslot[b] = N.nslot[b];
+    M.npart[b] = N.npart[b];
+    M.slot_tri[b] = N.slot_tri[b];
+    M.slot_hist[b] = N.slot_hist[b];
+  }
+  M.ccap = cap;
+  h->sys_gen++;
+  return DEM_OK;
+}
+
+// Triangle-to-cell registrations of mesh k (FixNeighlistMesh's per-bin
+// triangle lists) at M.tc_cap entries.
+static int alloc_tc_list(dem_handle *h, int k) {
+  MeshDev &M = h->s.meshes[k];
+  std::vector<void *> nl;
+  int *p = nullptr;
+  CUDA_TRY(h, dalloc(nl, &p, (size_t)M.tc_cap));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  free_list(h->allocs_tclist[k]);
+  h->allocs_tclist[k] = nl;
+  M.tc_list = p;
+  h->sys_gen++;
+  return DEM_OK;
 }
 
 static int alloc_atoms(dem_handle *h, int nmax) {
@@ -141,62 +247,91 @@ static int alloc_atoms(dem_handle *h, int nmax) {
   free_list(h->allocs_atoms);
   h->sys_gen++;
   s.nmax = nmax;
-  auto &L = h->allocs_atoms;
-  for (int b = 0; b < 2; b++) {
-    AtomArrays &A = s.atoms[b];
-    double **d[] = {&A.x, &A.y, &A.z, &A.vx, &A.vy, &A.vz, &A.wx, &A.wy, &A.wz, &A.fx, &A.fy,
-                    &A.fz, &A.tx, &A.ty, &A.tz, &A.r, &A.m, &A.dtfm, &A.dtir, &A.xh, &A.yh, &A.zh};
-    for (double **pp : d) CUDA_TRY(h, dalloc(L, pp, nmax));
-    CUDA_TRY(h, dalloc(L, &A.type, nmax));
-    CUDA_TRY(h, dalloc(L, &A.tag, nmax));
-    CUDA_TRY(h, dalloc(L, &A.lidx, nmax));
-    CUDA_TRY(h, dalloc(L, &A.whist, (size_t)3 * kMaxPlanes * nmax));
-    CUDA_TRY(h, dalloc(L, &A.wbits, nmax));
-    double **fm[] = {&A.fmx, &A.fmy, &A.fmz, &A.tmx, &A.tmy, &A.tmz};
-    for (double **pp : fm) CUDA_TRY(h, dalloc(L, pp, nmax));
-  }
+  auto carve = [&](Arena &ar) {
+    for (int b = 0; b < 2; b++) {
+      AtomArrays &A = s.atoms[b];
+      double **d[] = {&A.x, &A.y, &A.z, &A.vx, &A.vy, &A.vz, &A.wx, &A.wy, &A.wz, &A.fx, &A.fy,
+                      &A.fz, &A.tx, &A.ty, &A.tz, &A.r, &A.m, &A.dtfm, &A.dtir, &A.xh, &A.yh, &A.zh};
+      for (double **pp : d) ar.take(pp, nmax);
+      ar.take(&A.type, nmax);
+      ar.take(&A.tag, nmax);
+      ar.take(&A.lidx, nmax);
+      ar.take(&A.whist, (size_t)3 * kMaxPlanes * nmax);
+      ar.take(&A.wbits, nmax);
+      double **fm[] = {&A.fmx, &A.fmy, &A.fmz, &A.tmx, &A.tmy, &A.tmz};
+      for (double **pp : fm) ar.take(pp, nmax);
+    }
+    for (int b = 0; b < 2; b++) {
+      ar.take(&s.pairs[b].row, nmax + 1);
+      ar.take(&s.pairs[b].rev_start, nmax + 1);
+    }
+    ar.take(&s.perm, nmax);
+    ar.take(&s.xf, nmax);
+    ar.take(&s.xhf, nmax);
+    ar.take(&s.mlist, nmax);
+    ar.take(&s.wforce, (size_t)3 * std::max(1, s.nplanes + s.nmeshes) * nmax);
+    ar.take(&s.order, nmax);
+    ar.take(&s.pcount, nmax + 1);
+    ar.take(&s.rev_count, nmax + 1);
+    ar.take(&s.rev_fill, nmax + 1);
+  };
+  Arena ar;
+  carve(ar);
+  CUDA_TRY(h, ar.commit(h->allocs_atoms));
+  carve(ar);
   for (int b = 0; b < 2; b++) {
     PairArrays &P = s.pairs[b];
-    CUDA_TRY(h, dalloc(L, &P.row, nmax + 1));
-    CUDA_TRY(h, dalloc(L, &P.rev_start, nmax + 1));
-    CUDA_TRY(h, cudaMemset(P.row, 0, (nmax + 1) * sizeof(int)));
-    CUDA_TRY(h, cudaMemset(P.rev_start, 0, (nmax + 1) * sizeof(int)));
+    CUDA_TRY(h, cudaMemsetAsync(P.row, 0, (nmax + 1) * sizeof(int), h->st));
+    CUDA_TRY(h, cudaMemsetAsync(P.rev_start, 0, (nmax + 1) * sizeof(int), h->st));
   }
-  CUDA_TRY(h, dalloc(L, &s.perm, nmax));
-  CUDA_TRY(h, dalloc(L, &s.xf, nmax));
-  CUDA_TRY(h, dalloc(L, &s.xhf, nmax));
-  CUDA_TRY(h, dalloc(L, &s.mlist, nmax));
-  CUDA_TRY(h, dalloc(L, &s.wforce, (size_t)3 * std::max(1, s.nplanes + s.nmeshes) * nmax));
-  CUDA_TRY(h, cudaMemset(s.wforce, 0, (size_t)3 * std::max(1, s.nplanes + s.nmeshes) * nmax * sizeof(double)));
-  CUDA_TRY(h, dalloc(L, &s.order, nmax));
-  CUDA_TRY(h, dalloc(L, &s.pcount, nmax + 1));
-  CUDA_TRY(h, dalloc(L, &s.rev_count, nmax + 1));
-  CUDA_TRY(h, dalloc(L, &s.rev_fill, nmax + 1));
-  CUDA_TRY(h, dalloc(L, &s.cell_count, (size_t)s.ncell + 2));
-  CUDA_TRY(h, dalloc(L, &s.cell_start, (size_t)s.ncell + 2));
-  CUDA_TRY(h, dalloc(L, &s.cell_fill, (size_t)s.ncell + 2));
-  long maxlen = std::max<long>(nmax + 1, s.ncell + 2);
-  CUDA_TRY(h, dalloc(L, &s.scan_tmp, (maxlen + 4095) / 4096 + 1));
+  CUDA_TRY(h, cudaMemsetAsync(s.wforce, 0, (size_t)3 * std::max(1, s.nplanes + s.nmeshes) * nmax * sizeof(double), h->st));
   for (int k = 0; k < s.nmeshes; k++) {
-    MeshDev &M = s.meshes[k];
-    CUDA_TRY(h, dalloc(L, &M.tc_count, (size_t)s.ncell + 2));
-    CUDA_TRY(h, dalloc(L, &M.tc_start, (size_t)s.ncell + 2));
-    CUDA_TRY(h, dalloc(L, &M.tc_fill, (size_t)s.ncell + 2));
-    CUDA_TRY(h, dalloc(L, &M.tc_list, (size_t)M.tc_cap));
-    CUDA_TRY(h, dalloc(L, &M.cand_n, nmax));
-    CUDA_TRY(h, dalloc(L, &M.cand, (size_t)kMeshMaxCand * nmax));
-    for (int b = 0; b < 2; b++) {
-      CUDA_TRY(h, dalloc(L, &M.nslot[b], nmax));
-      CUDA_TRY(h, dalloc(L, &M.npart[b], nmax));
-      CUDA_TRY(h, dalloc(L, &M.slot_tri[b], (size_t)kMeshMaxCand * nmax));
-      CUDA_TRY(h, dalloc(L, &M.slot_hist[b], (size_t)3 * kMeshMaxCand * nmax));
-    }
-    CUDA_TRY(h, cudaMemset(M.cand_n, 0, nmax * sizeof(int)));
-    CUDA_TRY(h, cudaMemset(M.nslot[0], 0, nmax * sizeof(int)));
-    CUDA_TRY(h, cudaMemset(M.npart[0], 0, nmax * sizeof(int)));
-    CUDA_TRY(h, cudaMemset(M.slot_tri[0], 0xff, (size_t)kMeshMaxCand * nmax * sizeof(int)));
-    CUDA_TRY(h, cudaMemset(M.slot_hist[0], 0, (size_t)3 * kMeshMaxCand * nmax * sizeof(double)));
+    int rc = alloc_mesh_slots(h, k, s.meshes[k].ccap, false);
+    if (rc) return rc;
   }
+  return DEM_OK;
+}
+
+// The arrays sized by the neighbour cells and the mesh cell registrations
+// (known once the radius range is): cell counts and starts, the scan's
+// block sums, the triangle-to-cell lists.
+static int alloc_cells(dem_handle *h) {
+  Sys &s = h->s;
+  free_list(h->allocs_cells);
+  auto carve = [&](Arena &ar) {
+    ar.take(&s.cell_count, (size_t)s.ncell + 2);
+    ar.take(&s.cell_start, (size_t)s.ncell + 2);
+    ar.take(&s.cell_fill, (size_t)s.ncell + 2);
+    long maxlen = std::max<long>(s.nmax + 1, s.ncell + 2);
+    ar.take(&s.scan_tmp, (maxlen + 4095) / 4096 + 1);
+    for (int k = 0; k < s.nmeshes; k++) {
+      MeshDev &M = s.meshes[k];
+      ar.take(&M.tc_count, (size_t)s.ncell + 2);
+      ar.take(&M.tc_start, (size_t)s.ncell + 2);
+      ar.take(&M.tc_fill, (size_t)s.ncell + 2);
+    }
+  };
+  Arena ar;
+  carve(ar);
+  CUDA_TRY(h, ar.commit(h->allocs_cells));
+  carve(ar);
+  for (int k = 0; k < s.nmeshes; k++) {
+    int rc = alloc_tc_list(h, k);
+    if (rc) return rc;
+  }
+  h->sys_gen++;
+  return DEM_OK;
+}
+
+// Device staging for atom transfers where the device cannot reach the
+// caller's pageable memory (grown on demand, kept by the handle).
+static int ensure_stage(dem_handle *h, size_t bytes) {
+  if (h->stage_bytes >= bytes) return DEM_OK;
+  if (h->stage) cudaFree(h->stage);
+  h->stage = nullptr;
+  h->stage_bytes = 0;
+  CUDA_TRY(h, cudaMalloc(&h->stage, bytes));
+  h->stage_bytes = bytes;
   return DEM_OK;
 }
 
@@ -205,40 +340,46 @@ static int alloc_pairs(dem_handle *h, int pcap, int keep_np) {
   Sys &s = h->s;
   std::vector<void *> nl;
   PairArrays np_[2];
-  for (int b = 0; b < 2; b++) {
-    PairArrays &P = np_[b];
-    P = s.pairs[b];
-    CUDA_TRY(h, dalloc(nl, &P.i, pcap));
-    CUDA_TRY(h, dalloc(nl, &P.j, pcap));
-    CUDA_TRY(h, dalloc(nl, &P.sh, pcap));
-    CUDA_TRY(h, dalloc(nl, &P.flag, pcap));
-    CUDA_TRY(h, dalloc(nl, &P.hist, (size_t)s.dnum * pcap));
-    CUDA_TRY(h, dalloc(nl, &P.reff, pcap));
-    CUDA_TRY(h, dalloc(nl, &P.c0, pcap));
-    CUDA_TRY(h, dalloc(nl, &P.c1, pcap));
-    CUDA_TRY(h, dalloc(nl, &P.rev, pcap));
-  }
-  double *rF, *rTi, *rTj;
-  uint8_t *act;
-  CUDA_TRY(h, dalloc(nl, &rF, (size_t)3 * pcap));
-  CUDA_TRY(h, dalloc(nl, &rTi, (size_t)3 * pcap));
-  CUDA_TRY(h, dalloc(nl, &rTj, (size_t)3 * pcap));
-  CUDA_TRY(h, dalloc(nl, &act, pcap));
+  double *rF = nullptr, *rTi = nullptr, *rTj = nullptr;
+  uint8_t *act = nullptr;
+  auto carve = [&](Arena &ar) {
+    for (int b = 0; b < 2; b++) {
+      PairArrays &P = np_[b];
+      P = s.pairs[b];
+      ar.take(&P.i, pcap);
+      ar.take(&P.j, pcap);
+      ar.take(&P.sh, pcap);
+      ar.take(&P.flag, pcap);
+      ar.take(&P.hist, (size_t)s.dnum * pcap);
+      ar.take(&P.reff, pcap);
+      ar.take(&P.c0, pcap);
+      ar.take(&P.c1, pcap);
+      ar.take(&P.rev, pcap);
+    }
+    ar.take(&rF, (size_t)3 * pcap);
+    ar.take(&rTi, (size_t)3 * pcap);
+    ar.take(&rTj, (size_t)3 * pcap);
+    ar.take(&act, pcap);
+  };
+  Arena ar;
+  carve(ar);
+  CUDA_TRY(h, ar.commit(nl));
+  carve(ar);
   if (keep_np > 0 && s.pcap > 0) {
     const PairArrays &O = s.pairs[0];
     PairArrays &N = np_[0];
     const size_t k = keep_np;
-    CUDA_TRY(h, cudaMemcpy(N.i, O.i, k * sizeof(int), cudaMemcpyDeviceToDevice));
-    CUDA_TRY(h, cudaMemcpy(N.j, O.j, k * sizeof(int), cudaMemcpyDeviceToDevice));
-    CUDA_TRY(h, cudaMemcpy(N.sh, O.sh, k, cudaMemcpyDeviceToDevice));
-    CUDA_TRY(h, cudaMemcpy(N.flag, O.flag, k * sizeof(int), cudaMemcpyDeviceToDevice));
+    CUDA_TRY(h, cudaMemcpyAsync(N.i, O.i, k * sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.j, O.j, k * sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.sh, O.sh, k, cudaMemcpyDeviceToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.flag, O.flag, k * sizeof(int), cudaMemcpyDeviceToDevice, h->st));
     for (int d = 0; d < s.dnum; d++)
-      CUDA_TRY(h, cudaMemcpy(N.hist + (size_t)d * pcap, O.hist + (size_t)d * s.pcap,
-                             k * sizeof(double), cudaMemcpyDeviceToDevice));
-    CUDA_TRY(h, cudaMemcpy(N.reff, O.reff, k * sizeof(double), cudaMemcpyDeviceToDevice));
-    CUDA_TRY(h, cudaMemcpy(N.c0, O.c0, k * sizeof(double), cudaMemcpyDeviceToDevice));
-    CUDA_TRY(h, cudaMemcpy(N.c1, O.c1, k * sizeof(double), cudaMemcpyDeviceToDevice));
-    CUDA_TRY(h, cudaMemcpy(N.rev, O.rev, k * sizeof(int), cudaMemcpyDeviceToDevice));
+      CUDA_TRY(h, cudaMemcpyAsync(N.hist + (size_t)d * pcap, O.hist + (size_t)d * s.pcap,
+                             k * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.reff, O.reff, k * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.c0, O.c0, k * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.c1, O.c1, k * sizeof(double), cudaMemcpyDeviceToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(N.rev, O.rev, k * sizeof(int), cudaMemcpyDeviceToDevice, h->st));
   }
   free_list(h->allocs_pairs);
   h->allocs_pairs = nl;
@@ -269,9 +410,41 @@ static int recover(dem_handle *h, bool *resumed) {
   Ctrl &c = h->host_ctrl;
   if (c.status == kStatNan) return fail(h, DEM_ERR_NAN, "non-finite particle position");
   if (c.status == kStatMeshSlots)
-    return fail(h, DEM_ERR_CAPACITY, "an atom has more candidate mesh triangles than the per-atom capacity");
-  if (c.status == kStatMeshReg) return fail(h, DEM_ERR_CAPACITY, "mesh triangle-cell registrations overflowed");
+    return fail(h, DEM_ERR_CAPACITY, "a mesh contact found no free history slot (inconsistent slots)");
   if (!c.halt) return DEM_OK;
+  if (c.status == kStatMeshCand || c.status == kStatMeshReg) {
+    // FixContactHistoryMesh pages and FixNeighlistMesh bin lists grow without
+    // a bound in the reference: grow the arrays that overflowed, then finish
+    // the interrupted rebuild from its mesh stages
+    Sys &s = h->s;
+    if (c.status == kStatMeshCand) {
+      const int need = c.mesh_need;
+      for (int k = 0; k < s.nmeshes; k++)
+        if (s.meshes[k].ccap < need) {
+          rc = alloc_mesh_slots(h, k, std::max(need, 2 * s.meshes[k].ccap), true);
+          if (rc) return fail(h, DEM_ERR_CAPACITY, "cannot grow the mesh history slots: " + h->err);
+        }
+      c.mesh_need = 0;
+    } else {
+      for (int k = 0; k < s.nmeshes; k++) {
+        MeshDev &M = s.meshes[k];
+        int tot = 0;
+        CUDA_TRY(h, cudaMemcpyAsync(&tot, M.tc_start + s.ncell, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+        CUDA_TRY(h, cudaStreamSynchronize(h->st));
+        if (tot > M.tc_cap) {
+          M.tc_cap = (int)std::min<long>(2147000000L, (long)tot * 5 / 4 + 4096);
+          rc = alloc_tc_list(h, k);
+          if (rc) return fail(h, DEM_ERR_CAPACITY, "cannot grow the mesh cell registrations: " + h->err);
+        }
+      }
+    }
+    c.halt = 0;
+    c.status = kStatOk;
+    CUDA_TRY(h, cudaMemcpyAsync(h->s.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice, h->st));
+    h->kt.kernel_launches += launch_rebuild(h->s, h->lc, h->st, 2);
+    *resumed = true;
+    return DEM_OK;
+  }
   if (c.status != kStatPairOverflow) return fail(h, DEM_ERR_CUDA, "device halted");
   const int want = (int)std::min<long>(2147000000L, std::max<long>((long)c.np_new * 5 / 4 + 1024, 2L * h->s.pcap));
   rc = alloc_pairs(h, want, c.np);
@@ -322,6 +495,22 @@ int dem_create(const dem_config *cfg, dem_handle **out) {
   }
   h->allocs_misc.push_back(s.ctrl);
   cudaMemset(s.ctrl, 0, sizeof(Ctrl));
+  if (cudaMalloc(&h->chk, sizeof(UploadCheck)) != cudaSuccess ||
+      cudaMallocHost(&h->chk_host, sizeof(UploadCheck)) != cudaSuccess) {
+    delete h;
+    return DEM_ERR_CUDA;
+  }
+  h->allocs_misc.push_back(h->chk);
+  cudaDeviceSynchronize();
+  {  // direct access to the caller's pageable arrays: hardware coherence
+     // through the host page tables only (not software page migration);
+     // LIGGGHTS_GB300_STAGED_COPIES=1 forces the staged copies
+    int pma = 0, hpt = 0;
+    cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, h->device);
+    cudaDeviceGetAttribute(&hpt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, h->device);
+    const char *sc = getenv("LIGGGHTS_GB300_STAGED_COPIES");
+    h->host_direct = pma == 1 && hpt == 1 && !(sc && sc[0] == '1');
+  }
   for (int d = 0; d < 3; d++) {
     s.boxlo[d] = cfg->boxlo[d];
     s.boxhi[d] = cfg->boxhi[d];
@@ -359,6 +548,13 @@ int dem_destroy(dem_handle *h) {
   free_list(h->allocs_pairs);
   free_list(h->allocs_atoms);
   free_list(h->allocs_misc);
+  free_list(h->allocs_cells);
+  for (int k = 0; k < kMaxMeshes; k++) {
+    free_list(h->allocs_mslots[k]);
+    free_list(h->allocs_tclist[k]);
+  }
+  if (h->stage) cudaFree(h->stage);
+  if (h->chk_host) cudaFreeHost(h->chk_host);
   if (h->diag_buf) cudaFree(h->diag_buf);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -410,7 +606,7 @@ int dem_set_pair_params(dem_handle *h, int ntypes, const double *Yeff, const dou
                          h->allocs_misc.end());
   }
   CUDA_TRY(h, dalloc(h->allocs_misc, &h->s.params, tab.size()));
-  CUDA_TRY(h, cudaMemcpy(h->s.params, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpyAsync(h->s.params, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
   h->s.ntypes = ntypes;
   h->s.charVel = charVel;
   h->have_params = true;
@@ -449,7 +645,7 @@ int dem_set_bond_params(dem_handle *h, const double *tables, const dem_bond_sett
       all[(size_t)kBondRatioFn2 * m + q] =
           (T(kBondKufn2, q) - T(kBondKfn2, q)) / (T(kBondKufn2, q) + T(kBondKcfn2, q));
     }
-    CUDA_TRY(h, cudaMemcpy(h->s.bondp, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpyAsync(h->s.bondp, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
   }
   h->bond_tables.assign(tables, tables + (size_t)kBondTables * m);
   h->bond_settings = *st;
@@ -523,7 +719,7 @@ int dem_add_plane_per_type(dem_handle *h, int axis, const double *pos_by_type, i
   if (h->s.nplanes >= kMaxPlanes) return fail(h, DEM_ERR_BAD_ARG, "too many primitive walls");
   double *dpos = nullptr;
   CUDA_TRY(h, dalloc(h->allocs_misc, &dpos, (size_t)h->s.ntypes + 1));
-  CUDA_TRY(h, cudaMemcpy(dpos, pos_by_type, ((size_t)h->s.ntypes + 1) * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpyAsync(dpos, pos_by_type, ((size_t)h->s.ntypes + 1) * sizeof(double), cudaMemcpyHostToDevice, h->st));
   Plane &p = h->s.planes[h->s.nplanes];
   p.axis = axis;
   p.pos = pos_by_type[1];
@@ -580,11 +776,15 @@ int dem_add_mesh(dem_handle *h, int ntri, const double *nodes, int wall_type, in
   M.ntri = ntri;
   M.wall_type = wall_type;
   M.rolling = rolling_model == DEM_ROLLING_CDT ? 1 : 0;
+  // initial candidate triangles per atom; grown on demand.
+  // LIGGGHTS_GB300_MESH_CAND sets a smaller start (tests of the growth path)
+  M.ccap = kMeshCandInit;
+  if (const char *e = getenv("LIGGGHTS_GB300_MESH_CAND")) M.ccap = std::max(1, atoi(e));
   auto &L = h->allocs_misc;
   CUDA_TRY(h, dalloc(L, &M.tri, mh.tri.size()));
-  CUDA_TRY(h, cudaMemcpy(M.tri, mh.tri.data(), mh.tri.size() * sizeof(double), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpyAsync(M.tri, mh.tri.data(), mh.tri.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
   CUDA_TRY(h, dalloc(L, &M.meta, mh.meta.size()));
-  CUDA_TRY(h, cudaMemcpy(M.meta, mh.meta.data(), mh.meta.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpyAsync(M.meta, mh.meta.data(), mh.meta.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
   {
     std::vector<float4> tf(2 * (size_t)ntri);
     for (int t = 0; t < ntri; t++) {
@@ -593,13 +793,13 @@ int dem_add_mesh(dem_handle *h, int ntri, const double *nodes, int wall_type, in
       tf[2 * (size_t)t + 1] = make_float4((float)g[30], (float)g[31], (float)g[32], 0.f);
     }
     CUDA_TRY(h, dalloc(L, &M.trif, tf.size()));
-    CUDA_TRY(h, cudaMemcpy(M.trif, tf.data(), tf.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpyAsync(M.trif, tf.data(), tf.size() * sizeof(float4), cudaMemcpyHostToDevice, h->st));
   }
   CUDA_TRY(h, dalloc(L, &M.cn_start, mh.cn_start.size()));
-  CUDA_TRY(h, cudaMemcpy(M.cn_start, mh.cn_start.data(), mh.cn_start.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpyAsync(M.cn_start, mh.cn_start.data(), mh.cn_start.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
   CUDA_TRY(h, dalloc(L, &M.cn_list, std::max<size_t>(1, mh.cn_list.size())));
   if (!mh.cn_list.empty())
-    CUDA_TRY(h, cudaMemcpy(M.cn_list, mh.cn_list.data(), mh.cn_list.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpyAsync(M.cn_list, mh.cn_list.data(), mh.cn_list.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
   if (mesh_id) *mesh_id = h->s.nmeshes;
   h->mesh_host.push_back(std::move(mh));
   h->s.nmeshes++;
@@ -622,7 +822,7 @@ int dem_set_mesh_motion(dem_handle *h, int mesh_id, const double *vel) {
     const MeshHost &mh = h->mesh_host[mesh_id];
     for (int t = 0; t < M.ntri; t++)
       for (int q = 0; q < 9; q++) nl[(size_t)t * 9 + q] = mh.tri[(size_t)t * kTriStride + q];
-    CUDA_TRY(h, cudaMemcpy(M.node_last, nl.data(), nl.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpyAsync(M.node_last, nl.data(), nl.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
   }
   M.moving = 1;
   M.vel_on = 0;
@@ -658,14 +858,14 @@ int dem_set_mesh_rotation(dem_handle *h, int mesh_id, const double *origin, cons
     M.dx[d] = 0.0;
   }
   CUDA_TRY(h, dalloc(h->allocs_misc, &M.nodev, (size_t)9 * M.ntri));
-  CUDA_TRY(h, cudaMemset(M.nodev, 0, (size_t)9 * M.ntri * sizeof(double)));
+  CUDA_TRY(h, cudaMemsetAsync(M.nodev, 0, (size_t)9 * M.ntri * sizeof(double), h->st));
   if (!M.node_last) {
     CUDA_TRY(h, dalloc(h->allocs_misc, &M.node_last, (size_t)9 * M.ntri));
     std::vector<double> nl((size_t)9 * M.ntri);
     const MeshHost &mh = h->mesh_host[mesh_id];
     for (int t = 0; t < M.ntri; t++)
       for (int q = 0; q < 9; q++) nl[(size_t)t * 9 + q] = mh.tri[(size_t)t * kTriStride + q];
-    CUDA_TRY(h, cudaMemcpy(M.node_last, nl.data(), nl.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpyAsync(M.node_last, nl.data(), nl.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
   }
   M.rotating = 1;
   M.moving = 1;
@@ -679,7 +879,8 @@ int dem_download_mesh_nodes(dem_handle *h, int mesh_id, double *nodes) {
   CUDA_TRY(h, cudaStreamSynchronize(h->st));
   const MeshDev &M = h->s.meshes[mesh_id];
   std::vector<double> g((size_t)kTriStride * M.ntri);
-  CUDA_TRY(h, cudaMemcpy(g.data(), M.tri, g.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  CUDA_TRY(h, cudaMemcpyAsync(g.data(), M.tri, g.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
   for (int t = 0; t < M.ntri; t++)
     for (int q = 0; q < 9; q++) nodes[(size_t)t * 9 + q] = g[(size_t)t * kTriStride + q];
   return DEM_OK;
@@ -701,7 +902,8 @@ int dem_mesh_ncontacts(dem_handle *h, int mesh_id, int *nc) {
   if (rc) return rc;
   const int n = h->host_ctrl.n;
   std::vector<int> np(n);
-  CUDA_TRY(h, cudaMemcpy(np.data(), h->s.meshes[mesh_id].npart[0], n * sizeof(int), cudaMemcpyDeviceToHost));
+  CUDA_TRY(h, cudaMemcpyAsync(np.data(), h->s.meshes[mesh_id].npart[0], n * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
   long t = 0;
   for (int v : np) t += v;
   *nc = (int)t;
@@ -715,12 +917,13 @@ int dem_download_mesh_contacts(dem_handle *h, int mesh_id, int *tag, int *tri, i
   const int n = h->host_ctrl.n;
   const size_t nmax = h->s.nmax;
   const MeshDev &M = h->s.meshes[mesh_id];
-  std::vector<int> ns(n), st((size_t)kMeshMaxCand * nmax), tags(n);
-  std::vector<double> sh((size_t)3 * kMeshMaxCand * nmax);
-  CUDA_TRY(h, cudaMemcpy(ns.data(), M.nslot[0], n * sizeof(int), cudaMemcpyDeviceToHost));
-  CUDA_TRY(h, cudaMemcpy(st.data(), M.slot_tri[0], st.size() * sizeof(int), cudaMemcpyDeviceToHost));
-  CUDA_TRY(h, cudaMemcpy(sh.data(), M.slot_hist[0], sh.size() * sizeof(double), cudaMemcpyDeviceToHost));
-  CUDA_TRY(h, cudaMemcpy(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost));
+  std::vector<int> ns(n), st((size_t)M.ccap * nmax), tags(n);
+  std::vector<double> sh((size_t)3 * M.ccap * nmax);
+  CUDA_TRY(h, cudaMemcpyAsync(ns.data(), M.nslot[0], n * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaMemcpyAsync(st.data(), M.slot_tri[0], st.size() * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaMemcpyAsync(sh.data(), M.slot_hist[0], sh.size() * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaMemcpyAsync(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
   int c = 0;
   for (int i = 0; i < n; i++)
     for (int q = 0; q < ns[i]; q++) {
@@ -743,21 +946,57 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
   if (!h->have_params) return fail(h, DEM_ERR_BAD_ARG, "set pair parameters first");
   Sys &s = h->s;
   if ((long)n > kMaxScan) return fail(h, DEM_ERR_BAD_ARG, "too many atoms for one handle");
-  for (int i = 0; i < n; i++)
-    if (type[i] < 1 || type[i] > s.ntypes) return fail(h, DEM_ERR_BAD_ARG, "atom type out of range");
   for (int w = 0; w < s.nplanes; w++)
     if (s.planes[w].wall_type > s.ntypes) return fail(h, DEM_ERR_BAD_ARG, "wall type out of range");
   for (int k = 0; k < s.nmeshes; k++)
     if (s.meshes[k].wall_type > s.ntypes) return fail(h, DEM_ERR_BAD_ARG, "mesh wall type out of range");
-  for (int i = 0; i < n; i++)
-    if (!(radius[i] > 0.0) || !(rmass[i] > 0.0)) return fail(h, DEM_ERR_BAD_ARG, "radius and rmass must be > 0");
+  if (h->cap_n > 0 && h->cap_n < n) return fail(h, DEM_ERR_CAPACITY, "more atoms than the capacity set");
+  h->have_atoms = false;
+  h->setup_done = false;
+  int rc = alloc_atoms(h, std::max(n, h->cap_n));
+  if (rc) return rc;
+
+  // the caller's arrays into the SoA state, with the checks and the radius
+  // range, in one pass on the device
+  AtomsIn in{tag, type, x, v, omega, radius, rmass};
+  if (!h->host_direct) {
+    const size_t nd = (size_t)n * sizeof(double), ni = (size_t)n * sizeof(int);
+    rc = ensure_stage(h, 11 * nd + 2 * ni);
+    if (rc) return rc;
+    char *p = static_cast<char *>(h->stage);
+    double *dx = reinterpret_cast<double *>(p), *dv = dx + 3 * (size_t)n, *dw = dv + 3 * (size_t)n;
+    double *dr = dw + 3 * (size_t)n, *dm = dr + n;
+    int *dtag = reinterpret_cast<int *>(dm + n), *dtype = dtag + n;
+    CUDA_TRY(h, cudaMemcpyAsync(dx, x, 3 * nd, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(dv, v, 3 * nd, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(dw, omega, 3 * nd, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(dr, radius, nd, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(dm, rmass, nd, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(dtag, tag, ni, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(dtype, type, ni, cudaMemcpyHostToDevice, h->st));
+    in = AtomsIn{dtag, dtype, dx, dv, dw, dr, dm};
+  }
+  UploadCheck *ck = h->chk_host;
+  *ck = UploadCheck{~0ull, 0ull, 0, 0, 0, 0};
+  CUDA_TRY(h, cudaMemcpyAsync(h->chk, ck, sizeof(UploadCheck), cudaMemcpyHostToDevice, h->st));
+  // FixNVESphere's dtf and dtfrotate (src/fix_nve_sphere.cpp:150-178)
+  const double dtf = 0.5 * s.dt * 1.0;
+  const double dtfrotate = dtf / 0.4;
+  h->kt.kernel_launches += launch_upload_atoms(s, in, n, dtf, dtfrotate, h->chk, h->st);
+  CUDA_TRY(h, cudaGetLastError());
+  CUDA_TRY(h, cudaMemcpyAsync(ck, h->chk, sizeof(UploadCheck), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
+  if (ck->bad_type) return fail(h, DEM_ERR_BAD_ARG, "atom type out of range");
+  if (ck->bad_value) return fail(h, DEM_ERR_BAD_ARG, "radius and rmass must be finite and > 0");
+  if (ck->nonfinite) return fail(h, DEM_ERR_NAN, "non-finite position, velocity or angular velocity");
+  double maxrad, minrad;
+  {
+    long long a = (long long)ck->rmax, b = (long long)ck->rmin;
+    std::memcpy(&maxrad, &a, sizeof a);
+    std::memcpy(&minrad, &b, sizeof b);
+  }
   // cutneighmax = (maxrad_i + maxrad_j)*cdf + skin, src/pair_gran.cpp:591-602,
   // src/neighbor.cpp:316-337
-  double maxrad = 0.0, minrad = 1e99;
-  for (int i = 0; i < n; i++) {
-    maxrad = std::max(maxrad, radius[i]);
-    minrad = std::min(minrad, radius[i]);
-  }
   // radii that later insertions may bring (PairGran::init_one takes the
   // insertion templates' radii into maxrad/minrad the same way)
   if (h->cap_rmax > 0.0) maxrad = std::max(maxrad, h->cap_rmax);
@@ -843,9 +1082,10 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
       tot += cells;
     }
     M.tc_cap = (int)std::min<long>(2147000000L, 2 * tot + 4096);
+    // LIGGGHTS_GB300_MESH_REG sets a smaller start (tests of the growth path)
+    if (const char *e = getenv("LIGGGHTS_GB300_MESH_REG")) M.tc_cap = std::max(1, atoi(e));
   }
-  if (h->cap_n > 0 && h->cap_n < n) return fail(h, DEM_ERR_CAPACITY, "more atoms than the capacity set");
-  int rc = alloc_atoms(h, std::max(n, h->cap_n));
+  rc = alloc_cells(h);
   if (rc) return rc;
   h->pending_insert = 0;
   h->next_lidx = n;
@@ -856,45 +1096,12 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
   if (const char *e = getenv("LIGGGHTS_GB300_PAIRS_PER_ATOM")) ppa = std::max(0L, atol(e));
   rc = alloc_pairs(h, (int)std::max<long>(ppa * n, ppa >= 16 ? 4096 : 1), 0);
   if (rc) return rc;
-  // host-side per-atom constants of FixNVESphere (src/fix_nve_sphere.cpp:150-178)
-  const double dtf = 0.5 * s.dt * 1.0;
-  const double dtfrotate = dtf / 0.4;
-  std::vector<double> buf(n);
-  AtomArrays &A = s.atoms[0];
-  auto up3 = [&](const double *src, double *dx, double *dy, double *dz) -> int {
-    double *dst[3] = {dx, dy, dz};
-    for (int d = 0; d < 3; d++) {
-      for (int i = 0; i < n; i++) buf[i] = src[3 * i + d];
-      CUDA_TRY(h, cudaMemcpy(dst[d], buf.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-    }
-    return DEM_OK;
-  };
-  if ((rc = up3(x, A.x, A.y, A.z))) return rc;
-  if ((rc = up3(v, A.vx, A.vy, A.vz))) return rc;
-  if ((rc = up3(omega, A.wx, A.wy, A.wz))) return rc;
-  CUDA_TRY(h, cudaMemcpy(A.r, radius, n * sizeof(double), cudaMemcpyHostToDevice));
-  CUDA_TRY(h, cudaMemcpy(A.m, rmass, n * sizeof(double), cudaMemcpyHostToDevice));
-  CUDA_TRY(h, cudaMemcpy(A.type, type, n * sizeof(int), cudaMemcpyHostToDevice));
-  CUDA_TRY(h, cudaMemcpy(A.tag, tag, n * sizeof(int), cudaMemcpyHostToDevice));
-  {  // the upload order is the caller's local order
-    std::vector<int> li(n);
-    for (int i = 0; i < n; i++) li[i] = i;
-    CUDA_TRY(h, cudaMemcpy(A.lidx, li.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-  }
-  for (int i = 0; i < n; i++) buf[i] = dtf / (rmass[i] * (1. + 0.0));
-  CUDA_TRY(h, cudaMemcpy(A.dtfm, buf.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-  for (int i = 0; i < n; i++) buf[i] = dtfrotate / (radius[i] * radius[i] * rmass[i]);
-  CUDA_TRY(h, cudaMemcpy(A.dtir, buf.data(), n * sizeof(double), cudaMemcpyHostToDevice));
-  double *z3[] = {A.fx, A.fy, A.fz, A.tx, A.ty, A.tz, A.xh, A.yh, A.zh};
-  for (double *p : z3) CUDA_TRY(h, cudaMemset(p, 0, n * sizeof(double)));
-  CUDA_TRY(h, cudaMemset(A.whist, 0, (size_t)3 * kMaxPlanes * n * sizeof(double)));
-  CUDA_TRY(h, cudaMemset(A.wbits, 0, n));
   Ctrl c{};
   c.n = n;
   h->host_ctrl = c;
-  CUDA_TRY(h, cudaMemcpy(s.ctrl, &c, sizeof(Ctrl), cudaMemcpyHostToDevice));
+  CUDA_TRY(h, cudaMemcpyAsync(s.ctrl, &h->host_ctrl, sizeof(Ctrl), cudaMemcpyHostToDevice, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
   h->have_atoms = true;
-  h->setup_done = false;
   return DEM_OK;
 }
 
@@ -945,13 +1152,13 @@ int dem_insert_atoms(dem_handle *h, int k, const int *tag, const int *type, cons
   CUDA_TRY(h, cudaMalloc(&ibuf, (size_t)2 * k * sizeof(int)));
   const double *src[] = {x, v, omega};
   for (int a = 0; a < 3; a++)
-    CUDA_TRY(h, cudaMemcpy(buf + (size_t)3 * k * a, src[a], (size_t)3 * k * sizeof(double), cudaMemcpyHostToDevice));
-  CUDA_TRY(h, cudaMemcpy(buf + (size_t)9 * k, radius, (size_t)k * sizeof(double), cudaMemcpyHostToDevice));
-  CUDA_TRY(h, cudaMemcpy(buf + (size_t)10 * k, rmass, (size_t)k * sizeof(double), cudaMemcpyHostToDevice));
-  CUDA_TRY(h, cudaMemcpy(buf + (size_t)11 * k, dtfm.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice));
-  CUDA_TRY(h, cudaMemcpy(buf + (size_t)12 * k, dtir.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice));
-  CUDA_TRY(h, cudaMemcpy(ibuf, type, (size_t)k * sizeof(int), cudaMemcpyHostToDevice));
-  CUDA_TRY(h, cudaMemcpy(ibuf + k, tag, (size_t)k * sizeof(int), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpyAsync(buf + (size_t)3 * k * a, src[a], (size_t)3 * k * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CUDA_TRY(h, cudaMemcpyAsync(buf + (size_t)9 * k, radius, (size_t)k * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CUDA_TRY(h, cudaMemcpyAsync(buf + (size_t)10 * k, rmass, (size_t)k * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CUDA_TRY(h, cudaMemcpyAsync(buf + (size_t)11 * k, dtfm.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CUDA_TRY(h, cudaMemcpyAsync(buf + (size_t)12 * k, dtir.data(), (size_t)k * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CUDA_TRY(h, cudaMemcpyAsync(ibuf, type, (size_t)k * sizeof(int), cudaMemcpyHostToDevice, h->st));
+  CUDA_TRY(h, cudaMemcpyAsync(ibuf + k, tag, (size_t)k * sizeof(int), cudaMemcpyHostToDevice, h->st));
   InsertStage in;
   in.x = buf;
   in.v = buf + (size_t)3 * k;
@@ -979,7 +1186,8 @@ int dem_upload_contact_history(dem_handle *h, int ne, const int *towner, const i
   if (h->setup_done) return fail(h, DEM_ERR_BAD_ARG, "contact history must precede dem_setup");
   const int n = h->host_ctrl.n;
   std::vector<int> tags(n);
-  CUDA_TRY(h, cudaMemcpy(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost));
+  CUDA_TRY(h, cudaMemcpyAsync(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
   std::vector<std::pair<int, int>> t2i(n);
   for (int i = 0; i < n; i++) t2i[i] = {tags[i], i};
   std::sort(t2i.begin(), t2i.end());
@@ -1014,14 +1222,14 @@ int dem_upload_contact_history(dem_handle *h, int ne, const int *towner, const i
     // each entry is its owner's own partner-list copy: marked as a directed
     // (image) entry so that the first build takes it as it is
     std::vector<uint8_t> dsh(ne, 0);
-    CUDA_TRY(h, cudaMemcpy(L.i, pi.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
-    CUDA_TRY(h, cudaMemcpy(L.j, pj.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
-    CUDA_TRY(h, cudaMemcpy(L.sh, dsh.data(), ne, cudaMemcpyHostToDevice));
-    CUDA_TRY(h, cudaMemcpy(L.flag, fl.data(), ne * sizeof(int), cudaMemcpyHostToDevice));
-    CUDA_TRY(h, cudaMemcpy(L.hist, hh.data(), hh.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpyAsync(L.i, pi.data(), ne * sizeof(int), cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(L.j, pj.data(), ne * sizeof(int), cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(L.sh, dsh.data(), ne, cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(L.flag, fl.data(), ne * sizeof(int), cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(L.hist, hh.data(), hh.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
   }
-  CUDA_TRY(h, cudaMemcpy(L.row, row.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice));
-  CUDA_TRY(h, cudaMemset(L.rev_start, 0, (h->s.nmax + 1) * sizeof(int)));
+  CUDA_TRY(h, cudaMemcpyAsync(L.row, row.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, h->st));
+  CUDA_TRY(h, cudaMemsetAsync(L.rev_start, 0, (h->s.nmax + 1) * sizeof(int), h->st));
   return DEM_OK;
 }
 
@@ -1032,8 +1240,8 @@ int dem_upload_wall_history(dem_handle *h, int wall_id, const double *hist) {
   std::vector<double> hb(n);
   for (int d = 0; d < 3; d++) {
     for (int i = 0; i < n; i++) hb[i] = hist[3 * (size_t)i + d];
-    CUDA_TRY(h, cudaMemcpy(h->s.atoms[0].whist + (size_t)(wall_id * 3 + d) * h->s.nmax, hb.data(),
-                           n * sizeof(double), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpyAsync(h->s.atoms[0].whist + (size_t)(wall_id * 3 + d) * h->s.nmax, hb.data(),
+                           n * sizeof(double), cudaMemcpyHostToDevice, h->st));
   }
   return DEM_OK;
 }
@@ -1219,26 +1427,37 @@ int dem_download_atoms(dem_handle *h, int *tag, int *type, double *x, double *v,
   int rc = read_ctrl(h);
   if (rc) return rc;
   const int n = h->host_ctrl.n;
-  const AtomArrays &A = h->s.atoms[0];
-  std::vector<double> buf(n);
-  auto down3 = [&](double *dst, const double *sx, const double *sy, const double *sz) -> int {
-    if (!dst) return DEM_OK;
-    const double *src[3] = {sx, sy, sz};
-    for (int d = 0; d < 3; d++) {
-      CUDA_TRY(h, cudaMemcpy(buf.data(), src[d], n * sizeof(double), cudaMemcpyDeviceToHost));
-      for (int i = 0; i < n; i++) dst[3 * i + d] = buf[i];
-    }
+  if (n <= 0) return DEM_OK;
+  AtomsOut out{tag, type, x, v, omega, f, torque, radius, rmass};
+  if (h->host_direct) {  // the kernel writes the caller's arrays
+    h->kt.kernel_launches += launch_download_atoms(h->s, out, n, h->st);
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
     return DEM_OK;
-  };
-  if ((rc = down3(x, A.x, A.y, A.z))) return rc;
-  if ((rc = down3(v, A.vx, A.vy, A.vz))) return rc;
-  if ((rc = down3(omega, A.wx, A.wy, A.wz))) return rc;
-  if ((rc = down3(f, A.fx, A.fy, A.fz))) return rc;
-  if ((rc = down3(torque, A.tx, A.ty, A.tz))) return rc;
-  if (radius) CUDA_TRY(h, cudaMemcpy(radius, A.r, n * sizeof(double), cudaMemcpyDeviceToHost));
-  if (rmass) CUDA_TRY(h, cudaMemcpy(rmass, A.m, n * sizeof(double), cudaMemcpyDeviceToHost));
-  if (tag) CUDA_TRY(h, cudaMemcpy(tag, A.tag, n * sizeof(int), cudaMemcpyDeviceToHost));
-  if (type) CUDA_TRY(h, cudaMemcpy(type, A.type, n * sizeof(int), cudaMemcpyDeviceToHost));
+  }
+  const size_t nd = (size_t)n * sizeof(double), ni = (size_t)n * sizeof(int);
+  rc = ensure_stage(h, 17 * nd + 2 * ni);
+  if (rc) return rc;
+  double *p = static_cast<double *>(h->stage);
+  AtomsOut dv{};
+  double *vec[5] = {x, v, omega, f, torque};
+  double **dvec[5] = {&dv.x, &dv.v, &dv.w, &dv.f, &dv.t};
+  for (int k = 0; k < 5; k++)
+    if (vec[k]) *dvec[k] = p + (size_t)3 * n * k;
+  if (radius) dv.r = p + (size_t)15 * n;
+  if (rmass) dv.m = p + (size_t)16 * n;
+  int *ip = reinterpret_cast<int *>(p + (size_t)17 * n);
+  if (tag) dv.tag = ip;
+  if (type) dv.type = ip + n;
+  h->kt.kernel_launches += launch_download_atoms(h->s, dv, n, h->st);
+  CUDA_TRY(h, cudaGetLastError());
+  for (int k = 0; k < 5; k++)
+    if (vec[k]) CUDA_TRY(h, cudaMemcpyAsync(vec[k], *dvec[k], 3 * nd, cudaMemcpyDeviceToHost, h->st));
+  if (radius) CUDA_TRY(h, cudaMemcpyAsync(radius, dv.r, nd, cudaMemcpyDeviceToHost, h->st));
+  if (rmass) CUDA_TRY(h, cudaMemcpyAsync(rmass, dv.m, nd, cudaMemcpyDeviceToHost, h->st));
+  if (tag) CUDA_TRY(h, cudaMemcpyAsync(tag, dv.tag, ni, cudaMemcpyDeviceToHost, h->st));
+  if (type) CUDA_TRY(h, cudaMemcpyAsync(type, dv.type, ni, cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
   return DEM_OK;
 }
 
@@ -1260,13 +1479,14 @@ int dem_download_contacts(dem_handle *h, int *tag_i, int *tag_j, int *shift, int
   std::vector<int> pi(np), pj(np), tags(n), fl(np), li(n);
   std::vector<uint8_t> sh(np);
   if (np) {
-    CUDA_TRY(h, cudaMemcpy(pi.data(), L.i, np * sizeof(int), cudaMemcpyDeviceToHost));
-    CUDA_TRY(h, cudaMemcpy(pj.data(), L.j, np * sizeof(int), cudaMemcpyDeviceToHost));
-    CUDA_TRY(h, cudaMemcpy(sh.data(), L.sh, np, cudaMemcpyDeviceToHost));
-    CUDA_TRY(h, cudaMemcpy(fl.data(), L.flag, np * sizeof(int), cudaMemcpyDeviceToHost));
+    CUDA_TRY(h, cudaMemcpyAsync(pi.data(), L.i, np * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(pj.data(), L.j, np * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(sh.data(), L.sh, np, cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaMemcpyAsync(fl.data(), L.flag, np * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   }
-  CUDA_TRY(h, cudaMemcpy(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost));
-  CUDA_TRY(h, cudaMemcpy(li.data(), h->s.atoms[0].lidx, n * sizeof(int), cudaMemcpyDeviceToHost));
+  CUDA_TRY(h, cudaMemcpyAsync(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaMemcpyAsync(li.data(), h->s.atoms[0].lidx, n * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
   // pairs of two owned atoms are returned as the reference holds them: owned
   // by the atom that comes first in the caller's local order (shear negated
   // when the list holds the other orientation; bond values are kept in that
@@ -1294,8 +1514,9 @@ int dem_download_contacts(dem_handle *h, int *tag_i, int *tag_j, int *shift, int
     const int dnum = h->s.dnum;
     for (int r = 0; r < dnum; r++) {
       const int d = dev_hist_index(h->s, r);
-      CUDA_TRY(h, cudaMemcpy(hb.data(), L.hist + (size_t)d * h->s.pcap, np * sizeof(double),
-                             cudaMemcpyDeviceToHost));
+      CUDA_TRY(h, cudaMemcpyAsync(hb.data(), L.hist + (size_t)d * h->s.pcap, np * sizeof(double),
+                                  cudaMemcpyDeviceToHost, h->st));
+      CUDA_TRY(h, cudaStreamSynchronize(h->st));
       for (int p = 0; p < np; p++) hist[(size_t)p * dnum + r] = (swap[p] && d < kDnumShear) ? -hb[p] : hb[p];
     }
   }
@@ -1309,8 +1530,9 @@ int dem_download_wall_history(dem_handle *h, int wall_id, double *hist) {
   const int n = h->host_ctrl.n;
   std::vector<double> hb(n);
   for (int d = 0; d < 3; d++) {
-    CUDA_TRY(h, cudaMemcpy(hb.data(), h->s.atoms[0].whist + (size_t)(wall_id * 3 + d) * h->s.nmax,
-                           n * sizeof(double), cudaMemcpyDeviceToHost));
+    CUDA_TRY(h, cudaMemcpyAsync(hb.data(), h->s.atoms[0].whist + (size_t)(wall_id * 3 + d) * h->s.nmax,
+                                n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    CUDA_TRY(h, cudaStreamSynchronize(h->st));
     for (int i = 0; i < n; i++) hist[3 * (size_t)i + d] = hb[i];
   }
   return DEM_OK;
@@ -1329,6 +1551,9 @@ int dem_get_stats(dem_handle *h, dem_stats *out) {
   out->device = h->device;
   out->pair_capacity = h->s.pcap;
   out->last_step_ms = h->last_ms;
+  out->host_direct = h->host_direct ? 1 : 0;
+  out->mesh_slot_capacity = 0;
+  for (int k = 0; k < h->s.nmeshes; k++) out->mesh_slot_capacity = std::max(out->mesh_slot_capacity, h->s.meshes[k].ccap);
   return DEM_OK;
 }
 

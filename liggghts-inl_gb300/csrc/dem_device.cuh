@@ -110,6 +110,7 @@ struct Ctrl {
   int mesh_moved;   // a moving mesh node travelled > skin/2 since the last build
   int force_rebuild;  // rebuild at the next decide (FixMesh next_reneighbor)
   int nmlist;         // atoms with candidate mesh triangles (Sys::mlist)
+  int mesh_need;      // most candidate triangles an atom had beyond its mesh's capacity
 };
 
 struct Plane {
@@ -126,10 +127,20 @@ __device__ __forceinline__ double plane_pos(const Plane &pl, int type) {
 
 // Triangle-mesh wall (fix mesh/surface + fix wall/gran mesh).
 constexpr int kMaxMeshes = 4;
-constexpr int kMeshMaxCand = 24;   // candidate triangles (= history slots) per atom
+// Candidate triangles (= history slots) per atom and mesh: the main path
+// starts at kMeshCandInit and doubles MeshDev::ccap when an atom has more
+// (k_mesh_cand halts the rebuild, the host grows the slot arrays and resumes
+// it), as FixContactHistoryMesh grows its per-atom pages without a bound;
+// the adjoint keeps the fixed kMeshMaxCand.
+constexpr int kMeshCandInit = 24;
+constexpr int kMeshMaxCand = 24;
+constexpr int kMeshFastCand = 32;  // k_wall_force's tiled path (32-bit masks); more take the sequential path
+constexpr int kSlotKept = 1 << 30; // mesh_contacts: marks a slot touched in this evaluation
 constexpr int kTriStride = 40;     // doubles of geometry per triangle, see below
-constexpr int kStatMeshSlots = 5;  // Ctrl::status: an atom exceeded kMeshMaxCand
-constexpr int kStatMeshReg = 6;    // Ctrl::status: triangle-cell registrations overflowed
+constexpr int kStatMeshSlots = 5;  // Ctrl::status: a mesh contact found no free slot (inconsistent slots)
+constexpr int kStatMeshReg = 6;    // Ctrl::status: triangle-cell registrations overflowed (halted, grown, resumed)
+constexpr int kStatMeshCand = 7;   // Ctrl::status: an atom has more candidate triangles than ccap (halted, grown,
+                                   // resumed)
 // geometry layout per triangle: node[9] | edgeVec[9] | edgeNorm[9] |
 // edgeLen[3] | surfaceNorm[3] | center[3] | rBound | pad[3]
 // meta per triangle: bits 0-1 obtuse node+1 (0 none), bits 2-4 edge active,
@@ -154,6 +165,7 @@ struct MeshDev {
   int *cn_start, *cn_list;          // coplanar node-neighbours (areCoplanarNodeNeighs)
   int *tc_count, *tc_start, *tc_fill, *tc_list;  // triangles registered per atom cell
   int tc_cap;
+  int ccap;                         // candidate triangles (= history slots) per atom
   int *cand_n, *cand;               // per atom: count, [c*nmax + a] ascending
   int *nslot[2], *npart[2];         // per atom (buffer 0 live, 1 permute scratch)
   int *slot_tri[2];                 // [s*nmax + a], -1 empty

@@ -506,7 +506,7 @@ __global__ void k_tri_fill(Sys s, int k) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
   const MeshDev &M = s.meshes[k];
-  if (M.tc_start[s.ncell] > M.tc_cap) {
+  if (M.tc_start[s.ncell] > M.tc_cap) {  // the host grows tc_list to tc_start[ncell] and resumes
     if (blockIdx.x == 0 && threadIdx.x == 0) {
       c->status = kStatMeshReg;
       c->halt = 1;
@@ -534,30 +534,39 @@ __global__ void k_mesh_cand(Sys s, int k) {
   const AtomArrays &A = s.atoms[0];
   const int n = c->n_new;
   const size_t nmax = s.nmax;
+  const int cap = M.ccap;
   bool over = false;
   GRID_STRIDE(i, n) {
     const double xv[3] = {A.x[i], A.y[i], A.z[i]};
     const int cell = cell_coord(s, xv[0], 0) + s.nc[0] * (cell_coord(s, xv[1], 1) + s.nc[1] * cell_coord(s, xv[2], 2));
     const double rS = __dmul_rn(A.r[i], s.cdf);
-    int cand[kMeshMaxCand];
-    int nc = 0;
+    int *cand = M.cand + i;  // [q*nmax]
+    int nc = 0, need = 0;
     for (int q = M.tc_start[cell]; q < M.tc_start[cell + 1]; q++) {
       const int t = M.tc_list[q];
       if (!tri_sphere_neighbuild(M.tri + (size_t)t * kTriStride, rS, xv, M.tskin)) continue;
-      if (nc == kMeshMaxCand) { over = true; break; }
+      need++;
+      if (nc == cap) continue;  // counted only: the host grows the capacity
       int m = nc++;
-      while (m > 0 && cand[m - 1] > t) { cand[m] = cand[m - 1]; m--; }
-      cand[m] = t;
+      while (m > 0 && cand[(size_t)(m - 1) * nmax] > t) {
+        cand[(size_t)m * nmax] = cand[(size_t)(m - 1) * nmax];
+        m--;
+      }
+      cand[(size_t)m * nmax] = t;
+    }
+    if (need > cap) {  // leave this atom's slots untouched; the rebuild resumes here after growth
+      over = true;
+      atomicMax(&c->mesh_need, need);
+      continue;
     }
     M.cand_n[i] = nc;
-    for (int q = 0; q < nc; q++) M.cand[(size_t)q * nmax + i] = cand[q];
     // cleanUpContactJumps: drop partners whose triangle no longer lists the atom
     int np = M.npart[0][i];
     int ip = 0;
     while (ip < np) {
       const int t = M.slot_tri[0][ip * nmax + i];
       bool listed = false;
-      for (int q = 0; q < nc; q++) listed |= (cand[q] == t);
+      for (int q = 0; q < nc; q++) listed |= (cand[(size_t)q * nmax] == t);
       if (!listed) {
         M.slot_tri[0][ip * nmax + i] = -1;
         for (int d = 0; d < 3; d++) M.slot_hist[0][(3 * ip + d) * nmax + i] = 0.0;
@@ -575,7 +584,7 @@ __global__ void k_mesh_cand(Sys s, int k) {
     M.nslot[0][i] = nc;
   }
   if (over) {
-    c->status = kStatMeshSlots;
+    c->status = kStatMeshCand;
     c->halt = 1;
   }
 }
@@ -1265,9 +1274,15 @@ __device__ __forceinline__ bool mesh_coplanar(const MeshDev &M, int a, int b) {
   return false;
 }
 
-// FixWallGran::post_force_mesh for one atom: its candidate triangles in
-// ascending order with FixContactHistoryMesh's slot semantics (mark, handle,
-// coplanar de-duplication and history copy, clean-up)
+// triangle id of a slot entry (-1: empty), without the kept mark
+__device__ __forceinline__ int slot_tri_of(int v) { return v < 0 ? -1 : (v & ~kSlotKept); }
+
+// The closest-feature contacts of atom i with mesh k, one candidate at a
+// time in ascending triangle order (FixWallGran::post_force_mesh with
+// FixContactHistoryMesh::handleContact, coplanarContactAlready,
+// checkCoplanarContactHistory and cleanUpContacts).  A slot touched in this
+// evaluation carries kSlotKept in slot_tri until the clean-up, so the number
+// of candidates has no fixed bound.
 template <int NORMAL>
 __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, int shearupdate,
                               double v[3], double om[3], double xv[3], double &fx, double &fy,
@@ -1278,7 +1293,6 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
   const size_t nmax = s.nmax;
   int *st = M.slot_tri[0];
   double *sh = M.slot_hist[0];
-  unsigned keep = 0;
   int np = M.npart[0][i];
   const double radi = A.r[i];
   const double cdm1 = s.cdf - 1.0;
@@ -1287,27 +1301,20 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
   // rounding of either side) skip the closest-feature resolution; the
   // resolution would return deltan > 0 and skip them as well
   const double reach = __dmul_rn(__dadd_rn(radi, fmax(0.0, __dmul_rn(cdm1, radi))), 1.0 + 1e-9);
-  // FP32 pass over the candidates: the plane distance in FP32 is within
-  // 5*2^-24*S of the FP64 one (S: sum of the magnitudes of the atom's and
-  // node 0's coordinates), so a candidate farther than reach plus 2^-21*S
-  // is beyond reach in FP64 too; the rest take the FP64 path below in
-  // ascending order (the FP64 pipe then issues only for those)
-  unsigned todo = 0u;
-  {
-    const float4 xa = s.xf[i];
-    const float reach_f = (float)reach * (1.0f + 0x1p-20f);
-    for (int q = 0; q < nc; q++) {
-      const int t = M.cand[(size_t)q * nmax + i];
-      const float4 n0 = M.trif[2 * (size_t)t], sn = M.trif[2 * (size_t)t + 1];
-      const float dn = sn.x * (xa.x - n0.x) + sn.y * (xa.y - n0.y) + sn.z * (xa.z - n0.z);
-      const float mag = fabsf(xa.x) + fabsf(xa.y) + fabsf(xa.z) + fabsf(n0.x) + fabsf(n0.y) + fabsf(n0.z);
-      if (!(fabsf(dn) > reach_f + mag * 0x1p-21f)) todo |= 1u << q;
-    }
-  }
-  while (todo) {
-    const int q = __ffs(todo) - 1;
-    todo &= todo - 1u;
+  // FP32 test first: the plane distance in FP32 is within 5*2^-24*S of the
+  // FP64 one (S: sum of the magnitudes of the atom's and node 0's
+  // coordinates), so a candidate farther than reach plus 2^-21*S is beyond
+  // reach in FP64 too; the rest take the FP64 path below
+  const float4 xa = s.xf[i];
+  const float reach_f = (float)reach * (1.0f + 0x1p-20f);
+  for (int q = 0; q < nc; q++) {
     const int t = M.cand[(size_t)q * nmax + i];
+    {
+      const float4 n0 = M.trif[2 * (size_t)t], sn = M.trif[2 * (size_t)t + 1];
+      const float dnf = sn.x * (xa.x - n0.x) + sn.y * (xa.y - n0.y) + sn.z * (xa.z - n0.z);
+      const float mag = fabsf(xa.x) + fabsf(xa.y) + fabsf(xa.z) + fabsf(n0.x) + fabsf(n0.y) + fabsf(n0.z);
+      if (fabsf(dnf) > reach_f + mag * 0x1p-21f) continue;
+    }
     const double *g = M.tri + (size_t)t * kTriStride;
     {
       const double *sn = tri_sn(g), *n0 = tri_node(g, 0);
@@ -1321,29 +1328,29 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
     if (!(deltan <= 0 || deltan < cdm1 * radi)) continue;
     int slot = -1;
     for (int u = 0; u < nc; u++)
-      if (st[u * nmax + i] == t) { slot = u; break; }
+      if (slot_tri_of(st[u * nmax + i]) == t) { slot = u; break; }
     if (slot >= 0) {
-      keep |= 1u << slot;
+      st[slot * nmax + i] |= kSlotKept;
     } else {
       const bool face = bs == 7;
       if (face) {  // coplanarContactAlready
         bool already = false;
         for (int u = 0; u < nc; u++) {
-          const int p = st[u * nmax + i];
-          if (p >= 0 && p != t && ((keep >> u) & 1u) && mesh_coplanar(M, p, t)) already = true;
+          const int sv = st[u * nmax + i];
+          const int p = slot_tri_of(sv);
+          if (p >= 0 && p != t && (sv & kSlotKept) && mesh_coplanar(M, p, t)) already = true;
         }
         if (already) continue;
       }
       if (np >= nc) { bad = true; continue; }
       for (int u = 0; u < nc; u++)
         if (st[u * nmax + i] == -1) { slot = u; break; }
-      st[slot * nmax + i] = t;
-      keep |= 1u << slot;
+      st[slot * nmax + i] = t | kSlotKept;
       for (int d = 0; d < 3; d++) sh[(3 * slot + d) * nmax + i] = 0.0;
       np++;
       if (face)  // checkCoplanarContactHistory
         for (int u = 0; u < nc; u++) {
-          const int p = st[u * nmax + i];
+          const int p = slot_tri_of(st[u * nmax + i]);
           if (p >= 0 && p != t && mesh_coplanar(M, p, t))
             for (int d = 0; d < 3; d++) sh[(3 * slot + d) * nmax + i] = sh[(3 * u + d) * nmax + i];
         }
@@ -1352,17 +1359,21 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
     if (M.moving && M.vel_on) mesh_vwall(M, t, bary, vwall);
     double cfx = 0., cfy = 0., cfz = 0., ctx = 0., cty = 0., ctz = 0.;
     wall_force<NORMAL>(s, A, i, deltan, delta, vwall, M.wall_type, M.rolling != 0,
-                       sh + (size_t)(3 * slot) * nmax + i, nmax, shearupdate, v, om, cfx, cfy, cfz, ctx, cty, ctz);
+                         sh + (size_t)(3 * slot) * nmax + i, nmax, shearupdate, v, om, cfx, cfy, cfz, ctx, cty, ctz);
     fx += cfx; fy += cfy; fz += cfz;
     tx += ctx; ty += cty; tz += ctz;
     msum[0] += cfx; msum[1] += cfy; msum[2] += cfz;
   }
-  for (int u = 0; u < nc; u++)  // cleanUpContacts
-    if (!((keep >> u) & 1u)) {
-      if (st[u * nmax + i] > -1) np--;
+  for (int u = 0; u < nc; u++) {  // cleanUpContacts
+    const int sv = st[u * nmax + i];
+    if (sv >= 0 && (sv & kSlotKept)) {
+      st[u * nmax + i] = sv & ~kSlotKept;
+    } else {
+      if (sv > -1) np--;
       st[u * nmax + i] = -1;
       for (int d = 0; d < 3; d++) sh[(3 * u + d) * nmax + i] = 0.0;
     }
+  }
   M.npart[0][i] = np;
 }
 
@@ -1457,7 +1468,8 @@ __global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate
       const double radi = valid ? A.r[i] : 0.0;
       const double reach = __dmul_rn(__dadd_rn(radi, fmax(0.0, __dmul_rn(cdm1, radi))), 1.0 + 1e-9);
       unsigned todo = 0u;
-      if (nc > 0) {
+      const bool big = nc > kMeshFastCand;  // beyond the 32-bit masks: sequential path
+      if (nc > 0 && !big) {
         const float4 xa = s.xf[i];
         const float reach_f = (float)reach * (1.0f + 0x1p-20f);
         for (int q = 0; q < nc; q++) {
@@ -1518,12 +1530,12 @@ __global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate
       }
       __syncthreads();
       // ---- C: slot semantics per atom, in candidate order
-      bool fallback = false;
+      bool fallback = big;
       unsigned keep = 0u;
       int np = 0;
-      if (nc > 0) {
+      if (nc > 0 && !big) {
         np = M.npart[0][i];
-        int stl[kMeshMaxCand];
+        int stl[kMeshFastCand];
         for (int u = 0; u < nc; u++) stl[u] = st[u * nmax + i];
         unsigned fresh = 0u;
         for (int e = off; e < off + cnt && !fallback; e++) {
@@ -1802,7 +1814,7 @@ __global__ void k_insert_stage(Sys s, InsertStage in, int first, int k, int lidx
       M.cand_n[i] = 0;
       M.nslot[0][i] = 0;
       M.npart[0][i] = 0;
-      for (int u = 0; u < kMeshMaxCand; u++) {
+      for (int u = 0; u < M.ccap; u++) {
         M.slot_tri[0][(size_t)u * nmax + i] = -1;
         for (int d = 0; d < 3; d++) M.slot_hist[0][(size_t)(3 * u + d) * nmax + i] = 0.0;
       }
@@ -1829,6 +1841,96 @@ __global__ void k_insert_commit(Sys s, int k) {
     c->n = n_old + k;
     c->force_rebuild = 1;
   }
+}
+
+// ----------------------------------------------------------------------------
+// atom transfer: caller AoS <-> device SoA (dem_upload_atoms, dem_download_atoms)
+// ----------------------------------------------------------------------------
+
+__global__ void k_upload_atoms(Sys s, AtomsIn in, int n, double dtf, double dtfrotate, UploadCheck *chk) {
+  const AtomArrays &A = s.atoms[0];
+  const size_t nmax = s.nmax;
+  unsigned long long rmin = ~0ull, rmax = 0ull;
+  int bad_type = 0, bad_value = 0, nonfinite = 0;
+  GRID_STRIDE(i, n) {
+    const double x0 = in.x[3 * i], x1 = in.x[3 * i + 1], x2 = in.x[3 * i + 2];
+    const double v0 = in.v[3 * i], v1 = in.v[3 * i + 1], v2 = in.v[3 * i + 2];
+    const double w0 = in.w[3 * i], w1 = in.w[3 * i + 1], w2 = in.w[3 * i + 2];
+    const double r = in.r[i], m = in.m[i];
+    const int t = in.type[i];
+    bad_type += (t < 1 || t > s.ntypes) ? 1 : 0;
+    const bool okv = r > 0.0 && m > 0.0 && isfinite(r) && isfinite(m);
+    bad_value += okv ? 0 : 1;
+    const bool fin = isfinite(x0) && isfinite(x1) && isfinite(x2) && isfinite(v0) && isfinite(v1) &&
+                     isfinite(v2) && isfinite(w0) && isfinite(w1) && isfinite(w2);
+    nonfinite += fin ? 0 : 1;
+    A.x[i] = x0; A.y[i] = x1; A.z[i] = x2;
+    A.vx[i] = v0; A.vy[i] = v1; A.vz[i] = v2;
+    A.wx[i] = w0; A.wy[i] = w1; A.wz[i] = w2;
+    A.r[i] = r; A.m[i] = m;
+    A.type[i] = t; A.tag[i] = in.tag[i]; A.lidx[i] = i;
+    // FixNVESphere per-atom factors, as its init/initial_integrate form them
+    // (src/fix_nve_sphere.cpp:150-178): dtf/(m*(1+CAdd/rho)) with no added
+    // mass, dtfrotate/(r*r*m)
+    A.dtfm[i] = dtf / (m * (1. + 0.0));
+    A.dtir[i] = dtfrotate / (r * r * m);
+    A.fx[i] = A.fy[i] = A.fz[i] = 0.0;
+    A.tx[i] = A.ty[i] = A.tz[i] = 0.0;
+    A.xh[i] = A.yh[i] = A.zh[i] = 0.0;
+    for (int k = 0; k < 3 * kMaxPlanes; k++) A.whist[(size_t)k * nmax + i] = 0.0;
+    A.wbits[i] = 0;
+    A.fmx[i] = A.fmy[i] = A.fmz[i] = A.tmx[i] = A.tmy[i] = A.tmz[i] = 0.0;
+    if (okv) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(r);
+      rmin = b < rmin ? b : rmin;
+      rmax = b > rmax ? b : rmax;
+    }
+  }
+  // positive doubles order as their bit patterns
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long a = __shfl_down_sync(0xffffffffu, rmin, o);
+    const unsigned long long b = __shfl_down_sync(0xffffffffu, rmax, o);
+    rmin = a < rmin ? a : rmin;
+    rmax = b > rmax ? b : rmax;
+    bad_type += __shfl_down_sync(0xffffffffu, bad_type, o);
+    bad_value += __shfl_down_sync(0xffffffffu, bad_value, o);
+    nonfinite += __shfl_down_sync(0xffffffffu, nonfinite, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (rmin != ~0ull) atomicMin(&chk->rmin, rmin);
+    if (rmax) atomicMax(&chk->rmax, rmax);
+    if (bad_type) atomicAdd(&chk->bad_type, bad_type);
+    if (bad_value) atomicAdd(&chk->bad_value, bad_value);
+    if (nonfinite) atomicAdd(&chk->nonfinite, nonfinite);
+  }
+}
+
+__global__ void k_download_atoms(Sys s, AtomsOut out, int n) {
+  const AtomArrays &A = s.atoms[0];
+  GRID_STRIDE(i, n) {
+    if (out.x) { out.x[3 * i] = A.x[i]; out.x[3 * i + 1] = A.y[i]; out.x[3 * i + 2] = A.z[i]; }
+    if (out.v) { out.v[3 * i] = A.vx[i]; out.v[3 * i + 1] = A.vy[i]; out.v[3 * i + 2] = A.vz[i]; }
+    if (out.w) { out.w[3 * i] = A.wx[i]; out.w[3 * i + 1] = A.wy[i]; out.w[3 * i + 2] = A.wz[i]; }
+    if (out.f) { out.f[3 * i] = A.fx[i]; out.f[3 * i + 1] = A.fy[i]; out.f[3 * i + 2] = A.fz[i]; }
+    if (out.t) { out.t[3 * i] = A.tx[i]; out.t[3 * i + 1] = A.ty[i]; out.t[3 * i + 2] = A.tz[i]; }
+    if (out.r) out.r[i] = A.r[i];
+    if (out.m) out.m[i] = A.m[i];
+    if (out.tag) out.tag[i] = A.tag[i];
+    if (out.type) out.type[i] = A.type[i];
+  }
+}
+
+int launch_upload_atoms(const Sys &s, const AtomsIn &in, int n, double dtf, double dtfrotate, UploadCheck *chk,
+                        cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_upload_atoms<<<std::min((n + 255) / 256, 152 * 16), 256, 0, st>>>(s, in, n, dtf, dtfrotate, chk);
+  return 1;
+}
+
+int launch_download_atoms(const Sys &s, const AtomsOut &out, int n, cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_download_atoms<<<std::min((n + 255) / 256, 152 * 16), 256, 0, st>>>(s, out, n);
+  return 1;
 }
 
 int launch_insert_stage(const Sys &s, const InsertStage &in, int first, int k, int lidx0, cudaStream_t st) {
@@ -1949,6 +2051,9 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
   const int gN = grid_for(s.nmax + 1, B, lc.max_grid);
   const int gC = grid_for(s.ncell + 2, B, lc.max_grid);
   const int gP = grid_for(s.pcap, B, lc.max_grid);
+  // stage 0: the whole rebuild; stage 1: from the pair fill (after the host
+  // grew the pair list); stage 2: from the mesh stages (after it grew mesh
+  // slots or registrations).  Every resumed stage is idempotent.
   if (stage <= 0) {
     k_zero_gated<<<gC, B, 0, st>>>(s, s.cell_count, s.ncell + 2);
     k_zero_gated<<<gC, B, 0, st>>>(s, s.cell_fill, s.ncell + 2);
@@ -1963,15 +2068,16 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
     k_pairs_total<<<1, 1, 0, st>>>(s);
     nl += 1;
   }
-  // stage 1: resumes here after a pair-capacity overflow was fixed by the host
-  k_zero_gated<<<gN, B, 0, st>>>(s, s.rev_count, s.nmax + 1);
-  k_zero_gated<<<gN, B, 0, st>>>(s, s.rev_fill, s.nmax + 1);
-  k_pairs<true><<<gN, B, 0, st>>>(s);
-  k_pair_init<<<gP, B, 0, st>>>(s);
-  nl += 4 + scan_exclusive(s, s.rev_count, s.pairs[1].rev_start, s.nmax + 1, s.scan_tmp, true, st);
-  k_rev_fill<<<gP, B, 0, st>>>(s);
-  k_rev_sort<<<gN, B, 0, st>>>(s);
-  k_copy_pairs<<<grid_for((long)s.pcap > s.nmax + 1 ? s.pcap : s.nmax + 1, B, lc.max_grid), B, 0, st>>>(s);
+  if (stage <= 1) {
+    k_zero_gated<<<gN, B, 0, st>>>(s, s.rev_count, s.nmax + 1);
+    k_zero_gated<<<gN, B, 0, st>>>(s, s.rev_fill, s.nmax + 1);
+    k_pairs<true><<<gN, B, 0, st>>>(s);
+    k_pair_init<<<gP, B, 0, st>>>(s);
+    nl += 4 + scan_exclusive(s, s.rev_count, s.pairs[1].rev_start, s.nmax + 1, s.scan_tmp, true, st);
+    k_rev_fill<<<gP, B, 0, st>>>(s);
+    k_rev_sort<<<gN, B, 0, st>>>(s);
+    k_copy_pairs<<<grid_for((long)s.pcap > s.nmax + 1 ? s.pcap : s.nmax + 1, B, lc.max_grid), B, 0, st>>>(s);
+  }
   for (int k = 0; k < s.nmeshes; k++) {
     const MeshDev &M = s.meshes[k];
     const int gT = grid_for(M.ntri, B, lc.max_grid);

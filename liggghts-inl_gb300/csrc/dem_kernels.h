@@ -25,6 +25,34 @@ struct InsertStage {  // new atoms, device arrays: x, v, w [3k], the rest [k]
   const int *type, *tag;
 };
 int launch_insert_stage(const Sys &s, const InsertStage &in, int first, int k, int lidx0, cudaStream_t st);
+// Atom transfer between the caller's per-atom AoS arrays (atom->x[i][d] as
+// x[3*i+d]) and the device's SoA arrays.  The pointers are either the
+// caller's host arrays (read and written by the kernels themselves where the
+// device reaches pageable host memory through the host's page tables) or
+// device staging copies of them.
+struct AtomsIn {
+  const int *tag, *type;
+  const double *x, *v, *w, *r, *m;
+};
+struct AtomsOut {  // null members are skipped
+  int *tag, *type;
+  double *x, *v, *w, *f, *t, *r, *m;
+};
+struct UploadCheck {         // filled by k_upload_atoms (zero-initialise rmax, counts; rmin = ~0)
+  unsigned long long rmin;   // bit pattern of the smallest positive radius
+  unsigned long long rmax;   // bit pattern of the largest radius
+  int bad_type;              // atoms with a type outside 1..ntypes
+  int bad_value;             // atoms with radius or rmass not finite and > 0
+  int nonfinite;             // atoms with a non-finite position, velocity or angular velocity
+  int pad;
+};
+// SoA state of the first n atoms (buffer 0) from `in`, the nve/sphere
+// per-atom constants dtf/m and dtfrotate/(r^2 m), caller-order indices, and
+// cleared forces, holds, wall histories and mesh slots; `chk` collects the
+// checks and the radius range.
+int launch_upload_atoms(const Sys &s, const AtomsIn &in, int n, double dtf, double dtfrotate, UploadCheck *chk,
+                        cudaStream_t st);
+int launch_download_atoms(const Sys &s, const AtomsOut &out, int n, cudaStream_t st);
 int launch_insert_commit(const Sys &s, int k, cudaStream_t st);
 int launch_diagnostics(const Sys &s, const LaunchCfg &lc, const double lo[3], const double hi[3], double *part_atoms,
                        double *part_walls, unsigned long long *contacts, int nblocks, cudaStream_t st);
@@ -32,7 +60,8 @@ int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, boo
                    cudaStream_t st);
 int launch_decide(const Sys &s, cudaStream_t st);
 int launch_set_rebuild(const Sys &s, int v, cudaStream_t st);
-// stage 0: full rebuild; stage 1: resume after a pair-capacity overflow
+// stage 0: full rebuild; stage 1: resume after a pair-capacity overflow;
+// stage 2: resume after a mesh slot or registration overflow
 int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage);
 int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t st);
 int launch_particle(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, cudaStream_t st);

@@ -55,7 +55,8 @@ class DemStats(ctypes.Structure):
     _fields_ = [("ntimestep", ctypes.c_longlong), ("nrebuilds", ctypes.c_longlong),
                 ("npairs", ctypes.c_longlong), ("nlost", ctypes.c_longlong),
                 ("natoms", ctypes.c_longlong), ("device", ctypes.c_int),
-                ("pair_capacity", ctypes.c_int), ("last_step_ms", ctypes.c_double)]
+                ("pair_capacity", ctypes.c_int), ("last_step_ms", ctypes.c_double),
+                ("host_direct", ctypes.c_int), ("mesh_slot_capacity", ctypes.c_int)]
 
 
 class DemKernelTimes(ctypes.Structure):
@@ -264,15 +265,31 @@ class DemSystem:
         self._check(load().dem_natoms(self.h, ctypes.byref(n)))
         return n.value
 
-    def atoms(self):
-        n = self.natoms()
-        out = dict(tag=np.zeros(n, np.int32), type=np.zeros(n, np.int32),
-                   x=np.zeros((n, 3)), v=np.zeros((n, 3)), omega=np.zeros((n, 3)),
-                   f=np.zeros((n, 3)), torque=np.zeros((n, 3)), radius=np.zeros(n),
-                   rmass=np.zeros(n))
-        self._check(load().dem_download_atoms(self.h, *[_p(out[k]) for k in (
-            "tag", "type", "x", "v", "omega", "f", "torque", "radius", "rmass")]))
+    @staticmethod
+    def atom_buffers(n):
+        """Host arrays for atoms(out=...): the caller's own per-atom arrays,
+        kept across calls as the reference keeps atom->x, atom->v, ..."""
+        out = dict(tag=np.empty(n, np.int32), type=np.empty(n, np.int32),
+                   x=np.empty((n, 3)), v=np.empty((n, 3)), omega=np.empty((n, 3)),
+                   f=np.empty((n, 3)), torque=np.empty((n, 3)), radius=np.empty(n),
+                   rmass=np.empty(n))
+        for a in out.values():  # written once, so the pages exist (np.zeros maps them lazily)
+            a.fill(0)
         return out
+
+    def atoms(self, out=None):
+        """dem_download_atoms into `out` (atom_buffers of at least natoms()
+        rows; new arrays when None or too small); returns the first natoms()
+        rows of each array, in the device's order."""
+        n = self.natoms()
+        if out is None or len(out["tag"]) < n:
+            out = self.atom_buffers(n)
+        keys = ("tag", "type", "x", "v", "omega", "f", "torque", "radius", "rmass")
+        for k in keys:
+            a = out[k]
+            assert a.flags.c_contiguous and a.dtype == (np.int32 if k in ("tag", "type") else np.float64)
+        self._check(load().dem_download_atoms(self.h, *[_p(out[k]) for k in keys]))
+        return {k: out[k][:n] for k in keys}
 
     def pairs(self):
         L = load()

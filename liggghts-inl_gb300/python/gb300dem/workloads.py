@@ -144,6 +144,31 @@ def hopper_case(seed, r_out, r_top, half_angle_deg, n_az, n_ax, spacing, radius=
     return case
 
 
+def fine_floor_case(seed, nx=6, ny=6, nz=2, spacing=2.1e-3, radius=(0.95e-3, 1.05e-3), tri=0.5e-3,
+                    jitter=2e-5, vmax=0.1, wmax=50.0, **kw):
+    """A jittered lattice resting on a finely tessellated floor mesh (squares
+    of `tri`, two triangles each, at z = 0) in a closed box: every atom near
+    the floor has tens of candidate triangles (FixNeighlistMesh), more than
+    a fixed small per-atom page would hold."""
+    c = lattice_case(seed, nx, ny, nz, spacing, radius=radius, z0=0.98 * radius[0], jitter=jitter,
+                     vmax=vmax, wmax=wmax, periodic=(0, 0, 0), plane_z=None, **kw)
+    Lx, Ly = c["boxhi"][0], c["boxhi"][1]
+    mx, my = int(round(Lx / tri)), int(round(Ly / tri))
+    gx, gy = np.linspace(0.0, Lx, mx + 1), np.linspace(0.0, Ly, my + 1)
+    tris = []
+    for i in range(mx):
+        for j in range(my):
+            a = (gx[i], gy[j], 0.0)
+            b = (gx[i + 1], gy[j], 0.0)
+            cc = (gx[i + 1], gy[j + 1], 0.0)
+            d = (gx[i], gy[j + 1], 0.0)
+            tris.append((a, b, cc))
+            tris.append((a, cc, d))
+    c["meshes"] = [dict(nodes=np.asarray(tris, dtype=np.float64), wall_type=1, rolling=c["rolling_model"])]
+    c["boxlo"] = (0.0, 0.0, -2 * radius[1])
+    return c
+
+
 # property/global names of the 23 per-type-pair tables of cohesion
 # bond/nonlinear (src/cohesion_model_bond_nonlinear.h:70-147), in the order
 # the C ABI stacks them (DEM_BOND_* / ORC_BOND_*)

@@ -29,7 +29,7 @@
 #define TRI_LARGE 1000000
 #define MESH_PRECISION 1e-8        /* EPSILON_PRECISION */
 #define MESH_CURVATURE (1. - 0.00001) /* 1 - EPSILON_CURVATURE */
-#define MESH_MAXSLOT 64
+#define MESH_MAXSLOT 128
 
 typedef struct {
   int ntri;

@@ -23,7 +23,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "liggghts-inl_gb300", "python"))
-from gb300dem import workloads  # noqa: E402
+from gb300dem import workloads  # noqa: E402,F401
+sys.path.insert(0, ROOT)
+from oracle.lmp_input import DUMP_COLUMNS, fmt, write_inputs  # noqa: E402,F401
 
 LMP = os.path.join(ROOT, "oracle", "_ref", "lmp_ref")
 
@@ -85,113 +87,6 @@ def cases():
                                         gap=1.01, vmax=3.0, wmax=4000.0, bond=bp),
                    300, [0, 1, 2, 3, 10, 50, 100, 200, 300])
     return c
-
-
-def fmt(v):
-    return "%.17g" % v
-
-
-DUMP_COLUMNS = ("id type x y z vx vy vz omegax omegay omegaz fx fy fz tqx tqy tqz radius")
-
-
-def write_inputs(case, d, nsteps, snaps=None, dump_every=None, extra=(), run_style=False):
-    """Writes data.case and in.case (plus mesh STL files) into d.
-
-    snaps: steps at which the snapshot fix of the reference build writes its
-    binary state (golden generation).  dump_every: instead or as well, a
-    "dump custom" of every atom's id, type, x, v, omega, f, torque and
-    radius in %.17g every that many steps, sorted by id (dump.<step>.txt).
-    extra: further input lines placed after the integrator fix (insertion
-    fixes, regions).  run_style: adds "run_style verlet", which selects the
-    reference's default integrator explicitly; under "-sf gb300" that command
-    selects verlet/gb300 (Update::create_integrate, src/update.cpp:342-377),
-    while the integrator LAMMPS creates at start-up is never suffixed
-    (src/update.cpp:103-106)."""
-    a = case["atoms"]
-    n = len(a["tag"])
-    mat = case["material"]
-    nt = case["ntypes"]
-    lines = ["LIGGGHTS data file (seeded synthetic)", "", "%d atoms" % n, "%d atom types" % nt, ""]
-    for k, ax in enumerate("xyz"):
-        lines.append("%s %s %slo %shi" % (fmt(case["boxlo"][k]), fmt(case["boxhi"][k]), ax, ax))
-    lines += ["", "Atoms", ""]
-    for i in range(n):
-        lines.append("%d %d %s %s %s %s %s" % (a["tag"][i], a["type"][i], fmt(2 * a["radius"][i]),
-                                               fmt(mat["density"]), fmt(a["x"][i, 0]),
-                                               fmt(a["x"][i, 1]), fmt(a["x"][i, 2])))
-    lines += ["", "Velocities", ""]
-    for i in range(n):
-        lines.append("%d %s" % (a["tag"][i], " ".join(fmt(t) for t in
-                                                       list(a["v"][i]) + list(a["omega"][i]))))
-    open(os.path.join(d, "data.case"), "w").write("\n".join(lines) + "\n")
-
-    bnd = " ".join("p" if p else "f" for p in case["periodic"])
-    model = "model %s tangential history" % ("hooke" if case["normal_model"] == 1 else "hertz")
-    if case["rolling_model"] == 1:
-        model += " rolling_friction cdt"
-    bond = case.get("bond") if case.get("cohesion_model", 0) == 1 else None
-    if bond is not None:
-        model += " cohesion bond/nonlinear"
-        for f in workloads.BOND_FLAGS:
-            if bond["settings"][f] != workloads.BOND_DEFAULTS[f]:
-                model += " %s %s" % (workloads.BOND_KEYWORDS[f], "on" if bond["settings"][f] else "off")
-    tpl = lambda m: " ".join(fmt(m[i][j]) for i in range(nt) for j in range(nt))  # noqa: E731
-    s = ["atom_style granular", "atom_modify map array sort 0 0", "boundary %s" % bnd,
-         "newton off", "communicate single vel yes", "units si",
-         "read_data data.case", "neighbor %s bin" % fmt(case["skin"]), "neigh_modify delay 0",
-         "fix m1 all property/global youngsModulus peratomtype %s" % " ".join(fmt(e) for e in mat["E"]),
-         "fix m2 all property/global poissonsRatio peratomtype %s" % " ".join(fmt(e) for e in mat["nu"]),
-         "fix m3 all property/global coefficientRestitution peratomtypepair %d %s" % (nt, tpl(mat["rest"])),
-         "fix m4 all property/global coefficientFriction peratomtypepair %d %s" % (nt, tpl(mat["frict"]))]
-    if case["rolling_model"] == 1:
-        s.append("fix m5 all property/global coefficientRollingFriction peratomtypepair %d %s"
-                 % (nt, tpl(mat["rollfrict"])))
-    if case["normal_model"] == 1:
-        s.append("fix m6 all property/global characteristicVelocity scalar %s" % fmt(case["charVel"]))
-    if bond is not None:
-        for k, name in enumerate(workloads.BOND_TABLES):
-            s.append("fix b%d all property/global %s peratomtypepair %d %s"
-                     % (k, name, nt, tpl(bond["tables"][k][1:, 1:])))
-        s.append("fix bts all property/global tsCreateBondnonlinear scalar %s"
-                 % fmt(bond["settings"]["tsCreate"]))
-    s += ["pair_style gran %s" % model, "pair_coeff * *", "timestep %s" % fmt(case["dt"])]
-    g = case["gravity"]
-    s.append("fix gravi all gravity 9.81 vector 0.0 0.0 -1.0")
-    assert tuple(g) == (0.0, 0.0, -9.81)
-    for k, (axis, pos, wtype, roll) in enumerate(case["planes"]):
-        wm = "model %s tangential history" % ("hooke" if case["normal_model"] == 1 else "hertz")
-        if roll == 1:
-            wm += " rolling_friction cdt"
-        s.append("fix wall%d all wall/gran %s primitive type %d %splane %s"
-                 % (k, wm, wtype, "xyz"[axis], fmt(pos)))
-    for k, m in enumerate(case.get("meshes", [])):
-        workloads.write_stl(os.path.join(d, "mesh%d.stl" % k), m["nodes"])
-        s.append("fix cad%d all mesh/surface file mesh%d.stl type %d" % (k, k, m["wall_type"]))
-        wm = "model %s tangential history" % ("hooke" if case["normal_model"] == 1 else "hertz")
-        if m.get("rolling", 0) == 1:
-            wm += " rolling_friction cdt"
-        s.append("fix mwall%d all wall/gran %s mesh n_meshes 1 meshes cad%d" % (k, wm, k))
-        if m.get("vel") is not None:
-            s.append("fix mv%d all move/mesh mesh cad%d linear %s" % (k, k, " ".join(fmt(v) for v in m["vel"])))
-        if m.get("rotate") is not None:
-            ro = m["rotate"]
-            s.append("fix mv%d all move/mesh mesh cad%d rotate origin %s axis %s period %s"
-                     % (k, k, " ".join(fmt(v) for v in ro["origin"]), " ".join(fmt(v) for v in ro["axis"]),
-                        fmt(ro["period"])))
-    if not all(case["periodic"]):
-        s.append("thermo_modify lost ignore")
-    s.append("fix integr all nve/sphere")
-    s += list(extra)
-    if snaps is not None:
-        s.append("fix snap all oracle/snapshot snap %s" % " ".join(str(t) for t in snaps))
-    if dump_every:
-        ncol = len(DUMP_COLUMNS.split())
-        s += ["dump dmp all custom %d dump.*.txt %s" % (dump_every, DUMP_COLUMNS),
-              'dump_modify dmp sort id format "%%d %%d%s"' % (" %.17g" * (ncol - 2))]
-    if run_style:
-        s.append("run_style verlet")
-    s += ["thermo 100", "run %d" % nsteps]
-    open(os.path.join(d, "in.case"), "w").write("\n".join(s) + "\n")
 
 
 def read_snapshot(path):

@@ -1,0 +1,89 @@
+"""The benchmarked workload (bench.py's hopper1m: 1M polydisperse spheres in
+a 32,768-triangle conical hopper, Hertz/history + CDT rolling on pairs and
+the wall, outlet open, dt 5e-7) under the parity bars.
+
+  * a 20,000-atom slice (the lowest lattice sites, the unchanged cone) over
+    100 steps against the oracle: pair sets and mesh contact sets/slots
+    exact, forces within 1e-11 through step 10 and 1e-7 after, positions
+    within 1e-9 of the box, histories within 1e-9;
+  * the full 1M-atom configuration for its 10,000 steps: runs to the end
+    (the mesh and pair capacities grow as needed), every atom is either in
+    the box or counted lost, no non-finite state.
+"""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from golden_io import (FORCE_RTOL, HIST_RTOL, TRAJ_RTOL, canonical_pairs, compare_pairs, max_rel,
+                       sort_by_tag)
+
+pytestmark = pytest.mark.gpu
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+
+def _mesh_map(mc):
+    return {(int(t), int(tr)): (int(sl), h) for t, tr, sl, h in zip(mc["tag"], mc["tri"], mc["slot"], mc["hist"])}
+
+
+def test_gpu_hopper1m_slice_matches_oracle():
+    import bench
+    from gb300dem.api import DemSystem
+    from oracle.binding import Oracle
+    case, desc = bench.workload("hopper1m", scale=0.02)
+    assert desc["triangles"] == 32768 and len(case["meshes"][0]["nodes"]) == 32768
+    assert len(case["atoms"]["tag"]) == 20000
+    box = float(np.max(np.asarray(case["boxhi"]) - np.asarray(case["boxlo"])))
+    g, o = DemSystem(case), Oracle(case)
+    g.setup()
+    o.setup()
+    done = 0
+    nmesh = 0
+    for st in (0, 1, 10, 50, 100):
+        g.step(st - done)
+        o.run(st - done)
+        done = st
+        a, b = sort_by_tag(g.atoms()), sort_by_tag(o.atoms())
+        assert np.array_equal(a["tag"], b["tag"])
+        tol = FORCE_RTOL if st <= 10 else 1e-7
+        assert max_rel(a["f"], b["f"]) < tol, (st, max_rel(a["f"], b["f"]))
+        assert max_rel(a["torque"], b["torque"]) < tol, st
+        assert max_rel(a["x"], b["x"], scale=box) < TRAJ_RTOL, st
+        assert max_rel(a["v"], b["v"]) < TRAJ_RTOL, st
+        pg, po = g.pairs(), o.pairs()
+        missing, extra, flagmis, hm = compare_pairs(
+            canonical_pairs(pg["tag_i"], pg["tag_j"], pg["shift"], pg["flag"], pg["hist"]),
+            canonical_pairs(po["tag_i"], po["tag_j"], po["shift"], po["flag"], po["hist"]))
+        assert not missing and not extra and not flagmis, st
+        assert hm < HIST_RTOL, st
+        gm, om = _mesh_map(g.mesh_contacts(0)), _mesh_map(o.mesh_contacts(0))
+        assert set(gm) == set(om), st
+        assert all(gm[k][0] == om[k][0] for k in om), "slot layout differs"
+        if om:
+            hs = max(max(np.abs(v[1]).max() for v in om.values()), 1e-300)
+            assert max(np.abs(gm[k][1] - om[k][1]).max() for k in om) / hs < HIST_RTOL
+        nmesh = max(nmesh, len(om))
+    assert nmesh >= 20  # the outer ring of the lattice touches the cone
+    g.close()
+
+
+def test_gpu_hopper1m_full_configuration_runs_to_the_end():
+    import bench
+    from gb300dem.api import DemSystem
+    case, _ = bench.workload("hopper1m")
+    n0 = len(case["atoms"]["tag"])
+    g = DemSystem(case)
+    g.setup()
+    for _ in range(10):
+        g.step(1000)
+    st = g.stats()
+    assert st["ntimestep"] == 10000
+    a = g.atoms()
+    assert st["natoms"] + st["nlost"] == n0
+    assert np.all(np.isfinite(a["x"])) and np.all(np.isfinite(a["v"]))
+    lo, hi = np.asarray(case["boxlo"]), np.asarray(case["boxhi"])
+    assert np.all(a["x"] >= lo) and np.all(a["x"] <= hi)
+    print("hopper1m 10000 steps: atoms %d lost %d rebuilds %d mesh slots %d"
+          % (st["natoms"], st["nlost"], st["nrebuilds"], st["mesh_slot_capacity"]))
+    g.close()

@@ -1,0 +1,95 @@
+"""Mesh wall capacities that grow on demand, as the reference's do.
+
+FixContactHistoryMesh keeps per-atom pages of partner triangles and
+histories without a fixed bound (src/fix_contact_history_mesh.cpp:278-285),
+and FixNeighlistMesh's per-bin triangle lists grow the same way.  On the GPU
+an atom with more candidate triangles than the per-atom slot capacity, or a
+mesh whose triangle-to-cell registrations outgrow their array, halts the
+neighbour rebuild; the host grows the arrays and resumes the rebuild from its
+mesh stages.  The results must not depend on where the capacities start:
+the same bits with the smallest start as with the default, through the graph
+and through the host loop, and equal to the oracle on a floor where every
+atom has tens of candidate triangles (more than the tiled wall kernel's
+32-candidate masks, so those atoms take the sequential contact path).
+"""
+import numpy as np
+import pytest
+
+from golden_io import FORCE_RTOL, HIST_RTOL, TRAJ_RTOL, load_golden, max_rel, sort_by_tag
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(case, steps, monkeypatch, env):
+    from gb300dem.api import DemSystem
+    for k in ("LIGGGHTS_GB300_MESH_CAND", "LIGGGHTS_GB300_MESH_REG", "LIGGGHTS_GB300_NO_GRAPH"):
+        monkeypatch.delenv(k, raising=False)
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    g = DemSystem(case)
+    for k in env:
+        monkeypatch.delenv(k, raising=False)
+    g.setup()
+    out = []
+    for st in steps:
+        g.step(st)
+        a = {k: v.copy() for k, v in sort_by_tag(g.atoms()).items()}
+        out.append((a, g.mesh_contacts(0), g.stats()))
+    g.close()
+    return out
+
+
+def _same(r0, r1):
+    for (a0, m0, _), (a1, m1, _) in zip(r0, r1):
+        for k in a0:
+            assert np.array_equal(a0[k], a1[k]), k
+        for k in m0:
+            assert np.array_equal(m0[k], m1[k]), k
+
+
+@pytest.mark.parametrize("env", [{"LIGGGHTS_GB300_MESH_CAND": "1"}, {"LIGGGHTS_GB300_MESH_REG": "1"},
+                                 {"LIGGGHTS_GB300_MESH_CAND": "2", "LIGGGHTS_GB300_MESH_REG": "8",
+                                  "LIGGGHTS_GB300_NO_GRAPH": "1"}])
+@pytest.mark.parametrize("name", ["hopper_mesh_cdt", "mixer_rotate", "fibre_press"])
+def test_mesh_capacity_growth_gives_identical_runs(name, env, monkeypatch):
+    case, _ = load_golden(name)
+    ref = _run(case, [1, 30, 150], monkeypatch, {})
+    got = _run(case, [1, 30, 150], monkeypatch, env)
+    _same(ref, got)
+    if "LIGGGHTS_GB300_MESH_CAND" in env:
+        assert got[-1][2]["mesh_slot_capacity"] > int(env["LIGGGHTS_GB300_MESH_CAND"])
+
+
+def test_fine_floor_many_candidates_match_oracle(monkeypatch):
+    """0.4 mm floor triangles under 1 mm spheres: the slot capacity grows
+    past the initial 24 and past the tiled path's 32; forces, positions and
+    the mesh contact set, slots and histories equal the oracle's."""
+    from gb300dem import workloads
+    from oracle.binding import Oracle
+    case = workloads.fine_floor_case(71, tri=0.4e-3)
+    box = float(np.max(np.asarray(case["boxhi"]) - np.asarray(case["boxlo"])))
+    from gb300dem.api import DemSystem
+    monkeypatch.delenv("LIGGGHTS_GB300_MESH_CAND", raising=False)
+    g, o = DemSystem(case), Oracle(case)
+    g.setup()
+    o.setup()
+    assert g.stats()["mesh_slot_capacity"] > 32
+    done = 0
+    for st in (0, 1, 5, 10, 50, 100):
+        g.step(st - done)
+        o.run(st - done)
+        done = st
+        a, b = sort_by_tag(g.atoms()), sort_by_tag(o.atoms())
+        assert np.array_equal(a["tag"], b["tag"])
+        tol = FORCE_RTOL if st <= 10 else 1e-7
+        assert max_rel(a["f"], b["f"]) < tol, (st, max_rel(a["f"], b["f"]))
+        assert max_rel(a["torque"], b["torque"]) < tol, st
+        assert max_rel(a["x"], b["x"], scale=box) < TRAJ_RTOL, st
+        gm, om = g.mesh_contacts(0), o.mesh_contacts(0)
+        kg = {(int(t), int(tr)): (int(sl), h) for t, tr, sl, h in zip(gm["tag"], gm["tri"], gm["slot"], gm["hist"])}
+        ko = {(int(t), int(tr)): (int(sl), h) for t, tr, sl, h in zip(om["tag"], om["tri"], om["slot"], om["hist"])}
+        assert set(kg) == set(ko) and len(ko) >= 30, st
+        assert all(kg[k][0] == ko[k][0] for k in ko), "slot layout differs"
+        hs = max([np.abs(v[1]).max() for v in ko.values()] + [1e-300])
+        assert max(np.abs(kg[k][1] - ko[k][1]).max() for k in ko) / hs < HIST_RTOL
+    g.close()
