@@ -31,18 +31,27 @@ import numpy as np  # noqa: E402
 METRIC = "particle-steps/s (1M Hertz/history spheres)"
 METRICS = {"fibres200k": "particle-steps/s (200k bonded fibre spheres)"}
 
-# Per-atom FP64 arithmetic (flop, DFMA = 2) and DRAM bytes (read + write) of
-# one launch, and the FP64 pipe's active fraction, from ncu captures of the
-# workload at 500k atoms (profiles/k_pair_pf_hopper1m_500k.md,
-# profiles/k_particle_hopper1m_500k.md, profiles/k_wall_force_hopper1m_500k.md).
-PROFILED_PER_ATOM = {
-    "hopper1m": {"pair": {"fp64_flop": 81.6, "dram_bytes": 422.2, "fp64_pipe_active": 0.714},
-                 "particle": {"fp64_flop": 38.7, "dram_bytes": 395.5, "fp64_pipe_active": 0.745},
-                 "wall": {"fp64_flop": 0.256, "dram_bytes": 10.0, "fp64_pipe_active": 0.072},
-                 # touching fraction of the list entries: contact-side additions in
-                 # k_particle (6 per side) over the list length, same capture
-                 "touch_frac": 0.14},
+# Per-unit figures of the two step kernels (the roofline multiplies them by
+# the run's own atoms n, list entries E and touching entries C):
+#   k_pair_pf   bytes: 100 per atom (x, v, omega, r as doubles, type, the
+#               FP32 position copy), 10 per list entry (i, j, image code,
+#               active flag), 152 per touching entry (reff, c0, c1; history
+#               read and written; flag read and written; F, Ti, Tj written);
+#               FP64: flop per touching entry (DADD + DMUL + 2 DFMA, ncu);
+#   k_particle  bytes: 273 per atom (x, v, omega, f, torque read and
+#               written, dtfm, dtir, holds, rows, the FP32 copy), 5 per list
+#               entry (active flag, reverse index), 96 per touching entry (F
+#               read by both atoms, Ti and Tj by one each);
+#               FP64: flop per atom (gravity, two half-kicks, drift, wall
+#               sums) plus 12 per touching entry (two sides of six adds).
+KERNEL_UNITS = {
+    "pair": {"bytes_atom": 100, "bytes_entry": 10, "bytes_contact": 152, "flop_contact": 204.0},
+    "particle": {"bytes_atom": 273, "bytes_entry": 5, "bytes_contact": 96, "flop_atom": 34.0,
+                 "flop_contact": 12.0},
 }
+# DRAM bytes (read + write) per atom of one launch, from the ncu capture of
+# the workload (hopper1m at 500k atoms)
+DRAM_PER_ATOM = {"hopper1m": {"pair": 422.2, "particle": 395.5}}
 
 
 # ----------------------------------------------------------------------------
@@ -82,6 +91,26 @@ def workload(name, scale=1.0, seed=2024):
                     description="polydisperse Hertz/history + CDT rolling spheres, dense jittered "
                                 "lattice (2.2 mm, r 0.8-1.2 mm) in a periodic x/y column with a "
                                 "floor plane; the hopper's materials, dt 5e-7",
+                    l2="state + neighbour list > L2 (129 MB); no flush needed")
+        return case, desc
+    if name == "dense1m":
+        # the dense regime: 1M spheres of the hopper's materials (r U[0.97,
+        # 1.03] mm, rho 1500, E 1e7, e 0.5, mu 0.6, CDT 0.3 on pairs and
+        # floor) collapsed from an FCC lattice (nearest neighbours 2.04 mm)
+        # onto a floor in a periodic x/y column, settled on the GPU for
+        # 16,000 steps at dt 5e-6, then restarted from that state (atoms,
+        # contact and wall histories through the restart-data path) and timed
+        # at the hopper's dt 5e-7: about five touching contacts per sphere
+        nx = max(4, int(round(100 * scale ** 0.5)))
+        case = workloads.packed_bed_case(
+            seed, nx, nx, 25, dnn=2.04e-3, radius=(0.97e-3, 1.03e-3), density=1500.0, dt=5e-6,
+            E=(1e7,), nu=(0.45,), rest=((0.5,),), frict=((0.6,),), rollfrict=((0.3,),), rolling_model=1,
+            skin=5e-4)
+        desc = dict(workload="dense1m", atoms=int(len(case["atoms"]["tag"])), settle_steps=16000,
+                    settle_dt=5e-6, dt=5e-7,
+                    description="1M polydisperse Hertz/history + CDT spheres settled into a dense bed "
+                                "(FCC start, 16,000 steps at dt 5e-6 on the GPU, restarted with its "
+                                "contact history), periodic x/y column on a floor, timed at dt 5e-7",
                     l2="state + neighbour list > L2 (129 MB); no flush needed")
         return case, desc
     if name == "fibres200k":
@@ -208,7 +237,7 @@ def ref_binary():
     return p if os.path.isfile(p) and os.access(p, os.X_OK) else None
 
 
-def lmp_sample(name, nproc, steps, warm, seed=2024):
+def lmp_sample(name, nproc, steps, warm, seed=2024, case=None):
     """Times the reference binary on the full workload: one input script
     (seeded data file, STL mesh, the reference's own commands), `nproc`
     independent processes (one per host core), each "run warm" then "run
@@ -218,7 +247,8 @@ def lmp_sample(name, nproc, steps, warm, seed=2024):
     import shutil
     from oracle.lmp_input import write_inputs
     exe = ref_binary()
-    case, _ = workload(name, seed=seed)
+    if case is None:
+        case, _ = workload(name, seed=seed)
     n0 = len(case["atoms"]["tag"])
     top = tempfile.mkdtemp(prefix="lmp_ref_")
     try:
@@ -320,6 +350,20 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def settle_bed(case, desc):
+    """The dense workload's preparation (outside every timed region): the
+    bed settles on the GPU at desc["settle_dt"], then its state becomes the
+    restart data of the timed run at desc["dt"]."""
+    from gb300dem import api, workloads
+    g = api.DemSystem(dict(case, dt=desc["settle_dt"]))
+    g.setup()
+    g.step(desc["settle_steps"])
+    ck, to, tp, hh, walls = workloads.restart_state(g, case)
+    g.close()
+    ck["dt"] = desc["dt"]
+    return ck, (to, tp, hh, walls)
+
+
 def run_gb300(args):
     from gb300dem import api
     rank = int(os.environ.get("RANK", "0"))
@@ -331,8 +375,13 @@ def run_gb300(args):
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
     case, desc = workload(args.workload, scale=args.scale, seed=2024 + rank)
+    restart = None
+    if desc.get("settle_steps"):
+        case, restart = settle_bed(case, desc)
     n = len(case["atoms"]["tag"])
     g = api.DemSystem(case)
+    if restart:
+        g.set_restart(*restart)
     g.setup()
     g.step(args.warmup)
     # ---- headline: device-timed K steps, state resident
@@ -362,6 +411,8 @@ def run_gb300(args):
     hout = g2.atom_buffers(n)
     t0 = time.perf_counter()
     g2.upload(host)
+    if restart:
+        g2.set_restart(*restart)
     t1 = time.perf_counter()
     g2.setup()
     t2 = time.perf_counter()
@@ -386,48 +437,48 @@ def run_gb300(args):
     part_ms = kp["particle_ms"] / max(1, kp["particle_launches"])
     neigh_ms = kp["neigh_ms"] / max(1, kp["neigh_stages"])
     tot_ms = pair_ms + part_ms + neigh_ms + wall_ms
-    # algorithmic bytes: pair kernel reads each atom's x,r,v,omega,type once
-    # (92 B), each list entry's i,j,shift (9 B) + active flag write (1 B);
-    # each touching entry: meff,reff (16 B), history r/w (48 B), flags r/w
-    # (8 B), results (72 B).
-    ncontact = int(kp.get("ncontacts", 0)) or None
-    fp64 = None
+    # ---- roofline of the dominant kernel from this run's own counts: atoms
+    # n, list entries E, touching entries C (dem_get_diagnostics after the
+    # timed steps), times the per-unit figures of KERNEL_UNITS
     try:
         fp64_peak = api.fp64_peak_tflops()
     except Exception:
         fp64_peak = None
-    frac_touch = PROFILED_PER_ATOM.get(args.workload, {}).get("touch_frac", 0.5)
-    pair_bytes = n * 92 + npairs * 10 + frac_touch * npairs * 144
-    part_bytes = n * (15 * 8 * 2 + 8 * 4 + 1) + npairs * (4 + 1 + 72) + frac_touch * npairs * 4
+    ncontact = int(g.diagnostics()["ncontacts"])
+    E, C = int(npairs), ncontact
+    ku = KERNEL_UNITS
+    pair_bytes = n * ku["pair"]["bytes_atom"] + E * ku["pair"]["bytes_entry"] + C * ku["pair"]["bytes_contact"]
+    part_bytes = (n * ku["particle"]["bytes_atom"] + E * ku["particle"]["bytes_entry"]
+                  + C * ku["particle"]["bytes_contact"])
+    pair_flop = C * ku["pair"]["flop_contact"]
+    part_flop = n * ku["particle"]["flop_atom"] + C * ku["particle"]["flop_contact"]
     dom = "pair" if pair_ms >= part_ms else "particle"
     dom_bytes = pair_bytes if dom == "pair" else part_bytes
+    dom_flop = pair_flop if dom == "pair" else part_flop
     dom_ms = pair_ms if dom == "pair" else part_ms
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    # Binding roof: the FP64 pipe.  FP64 arithmetic per atom and DRAM bytes
-    # per atom of each kernel come from one ncu capture of the same workload
-    # at 500k atoms (DADD + DMUL + 2 DFMA thread instructions; dram read +
-    # write), scaled to this run by the atom count.
-    per_atom = PROFILED_PER_ATOM.get(args.workload, {}).get(dom)
+    traffic = DRAM_PER_ATOM.get(args.workload, {}).get(dom)
     hbm_roof = {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": per_atom["dram_bytes"] * n if per_atom else None,
+                "traffic": traffic * n if traffic else None,
                 "algorithmic_bytes_per_launch": dom_bytes,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
-    if per_atom and fp64_peak:
-        flops = per_atom["fp64_flop"] * n
-        ach_tf = flops / (dom_ms * 1e-3) / 1e12
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks.get("hbm_gbs")
+                else "6800 GB/s (of fallback: no MEASURED_PEAKS.json)"}
+    if fp64_peak:
+        ach_tf = dom_flop / (dom_ms * 1e-3) / 1e12
         roof = {"kernel": "k_pair_pf" if dom == "pair" else "k_particle", "bound": "fp64",
                 "achieved": ach_tf, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach_tf / fp64_peak,
                 "traffic": hbm_roof["traffic"],
                 "peak_source": "FP64 FMA peak measured live on this GPU (dem_measure_fp64_peak), "
                                "of measured",
-                "fp64_flop_per_launch": flops, "hbm": hbm_roof,
-                "fp64_pipe_active_ncu": per_atom.get("fp64_pipe_active"),
-                "note": "flop counts DADD/DMUL + 2*DFMA; the FP64 pipe also issues compares, "
-                        "conversions and the idle lanes of partly active warps, so pipe-active "
-                        "(ncu) exceeds achieved/peak"}
+                "fp64_flop_per_launch": dom_flop, "hbm": hbm_roof,
+                "note": "flop counts DADD/DMUL + 2*DFMA per unit (ncu) times this run's units; the "
+                        "FP64 pipe also issues compares, conversions and the idle lanes of partly "
+                        "active warps, so its active fraction exceeds achieved/peak"}
     else:
         roof = dict(hbm_roof, kernel="k_pair_pf" if dom == "pair" else "k_particle", bound="hbm")
     roof.update({"avg_launch_ms": dom_ms,
+                 "units": {"atoms": n, "list_entries": E, "touching_entries": C,
+                           "touching_per_atom": C / max(1, n)},
                  "shares": {"pair": pair_ms / tot_ms, "particle": part_ms / tot_ms,
                             "wall": wall_ms / tot_ms, "neigh": neigh_ms / tot_ms},
                  "shares_note": "host-queued profiled run (kernels serialised, rebuild stage as "
@@ -439,11 +490,13 @@ def run_gb300(args):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         if ref_binary() and args.scale == 1.0:
-            v, res = lmp_sample(args.workload, 1, args.cpu_steps, 1)
+            v, res = lmp_sample(args.workload, 1, args.cpu_steps, 1, case=case if restart else None)
             cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "reference",
-                   "sample": "reference binary (oracle/_ref/lmp_ref, serial, -O3) on the full %d-atom %s, "
+                   "sample": "reference binary (oracle/_ref/lmp_ref, serial, -O3) on the full %d-atom %s%s, "
                              "'run 1' then the timed 'run %d' (its Loop time), 1 process"
-                             % (res[0][0], args.workload, args.cpu_steps)}
+                             % (res[0][0], args.workload,
+                                " (the settled positions, read_data without contact history)" if restart else "",
+                                args.cpu_steps)}
         else:
             v, res = cpu_sample(args.workload, 1, steps=args.cpu_steps, warm=1)
             cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "port",
@@ -600,7 +653,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="hopper1m",
-                    choices=["hopper1m", "column1m", "fibres200k", "ensemble256", "adjoint20k"])
+                    choices=["hopper1m", "column1m", "dense1m", "fibres200k", "ensemble256", "adjoint20k"])
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0,

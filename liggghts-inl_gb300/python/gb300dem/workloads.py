@@ -144,6 +144,60 @@ def hopper_case(seed, r_out, r_top, half_angle_deg, n_az, n_ax, spacing, radius=
     return case
 
 
+def packed_bed_case(seed, nx, ny, nz, dnn=2.04e-3, radius=(0.97e-3, 1.03e-3), density=1500.0, dt=5e-6,
+                    **kw):
+    """Spheres on a face-centred cubic lattice (nearest-neighbour distance
+    dnn, just above the mean diameter) in a box periodic in x/y above a floor:
+    under gravity the polydisperse lattice collapses into a dense random bed
+    with about five touching contacts per sphere.  4*nx*ny*nz spheres."""
+    rng = np.random.default_rng(seed)
+    a = dnn * math.sqrt(2.0)  # edge of the cubic FCC cell
+    basis = np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.0], [0.5, 0.0, 0.5], [0.0, 0.5, 0.5]])
+    ii, jj, kk = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    cells = np.stack([ii.ravel(), jj.ravel(), kk.ravel()], 1).astype(np.float64)
+    x = ((cells[:, None, :] + basis[None]) * a).reshape(-1, 3)
+    x[:, 2] += radius[1] * 1.05
+    n = len(x)
+    c = lattice_case(seed, 1, 1, 1, 1.0, radius=radius, density=density, dt=dt, **kw)
+    r = rng.uniform(radius[0], radius[1], n)
+    c["boxhi"] = (nx * a, ny * a, float(x[:, 2].max() + 6 * radius[1]))
+    c["atoms"] = dict(tag=np.arange(1, n + 1, dtype=np.int32), type=np.ones(n, np.int32), x=x,
+                      v=np.zeros((n, 3)), omega=np.zeros((n, 3)), radius=r, rmass=sphere_mass(r, density))
+    return c
+
+
+def restart_state(sys_, case):
+    """A resident system's state as the reference's restart data: atoms,
+    the per-atom partner lists with their contact history (one entry per
+    touching side; FixContactHistory::pre_exchange writes both sides of a
+    pair of two owned atoms, the partner's with the newton sign) and the
+    primitive-wall histories.  Returns (case with those atoms, owner tags,
+    partner tags, histories, wall histories)."""
+    a = sys_.atoms()
+    ck = dict(case)
+    ck["atoms"] = {k: np.array(a[k]) for k in ("tag", "type", "x", "v", "omega", "radius", "rmass")}
+    p = sys_.pairs()
+    on = p["flag"] != 0
+    ti, tj, sh, hs = p["tag_i"][on], p["tag_j"][on], p["shift"][on], p["hist"][on]
+    own = ~np.any(sh != 0, axis=1)
+    # sign of each history value in the partner's copy (the newtonflag of
+    # add_history_value): the shear flips; of the 28 bond values, ft,
+    # thetan and thetat (5..13) flip
+    if hs.shape[1] == 3:
+        sgn = -np.ones(3)
+    else:
+        sgn = np.ones(hs.shape[1])
+        sgn[5:14] = -1.0
+        sgn[28:31] = -1.0
+    to = np.concatenate([ti, tj[own]]).astype(np.int32)
+    tp = np.concatenate([tj, ti[own]]).astype(np.int32)
+    hh = np.concatenate([hs, hs[own] * sgn[None, :]])
+    order = np.argsort(a["tag"], kind="stable")
+    walls = [np.asarray(sys_.wall_history(w))[order] for w in range(len(case.get("planes", [])))]
+    ck["atoms"] = {k: v[order] for k, v in ck["atoms"].items()}
+    return ck, to, tp, hh, walls
+
+
 def fine_floor_case(seed, nx=6, ny=6, nz=2, spacing=2.1e-3, radius=(0.95e-3, 1.05e-3), tri=0.5e-3,
                     jitter=2e-5, vmax=0.1, wmax=50.0, **kw):
     """A jittered lattice resting on a finely tessellated floor mesh (squares

@@ -57,7 +57,10 @@ def test_mesh_capacity_growth_gives_identical_runs(name, env, monkeypatch):
     got = _run(case, [1, 30, 150], monkeypatch, env)
     _same(ref, got)
     if "LIGGGHTS_GB300_MESH_CAND" in env:
-        assert got[-1][2]["mesh_slot_capacity"] > int(env["LIGGGHTS_GB300_MESH_CAND"])
+        cap = got[-1][2]["mesh_slot_capacity"]
+        assert cap >= int(env["LIGGGHTS_GB300_MESH_CAND"])
+        if name == "hopper_mesh_cdt":  # atoms there have several candidate facets: the slots grew
+            assert cap > int(env["LIGGGHTS_GB300_MESH_CAND"])
 
 
 def test_fine_floor_many_candidates_match_oracle(monkeypatch):
