@@ -145,6 +145,16 @@ int dem_set_bond_params(dem_handle *h, const double *tables, const dem_bond_sett
 int dem_add_plane(dem_handle *h, int axis, double pos, int wall_type, int rolling_model,
                   int *wall_id);
 
+/* fix wall/gran ... primitive type T xcylinder|ycylinder|zcylinder R C1 C2
+ * (FixWallGran with PrimitiveWall Cylinder<dim>, src/primitive_wall_definitions.h:
+ * 69-71,155-200): a cylinder of radius R about the axis 0/1/2 through the point
+ * whose coordinates along (axis+1)%3 and (axis+2)%3 are C1, C2.  Contact from
+ * inside and from outside, the reference's neighbour rule and history.  Walls
+ * share one id sequence (planes and cylinders in the order they are added,
+ * then meshes).  Returns the wall id through *wall_id (may be NULL). */
+int dem_add_cylinder(dem_handle *h, int axis, double radius, double center1, double center2, int wall_type,
+                     int rolling_model, int *wall_id);
+
 /* A primitive plane whose position depends on the atom's type (pos_by_type,
  * ntypes+1 entries, entry 0 unused) and whose wall type is the atom's own
  * type: the floors of independent systems stacked into one handle (the
@@ -323,9 +333,13 @@ int dem_get_kernel_times(dem_handle *h, dem_kernel_times *out);
  * synchronises it before returning.
  * Scratch lives in one fixed static device array (about 11 MB per GPU that
  * loads the library, kept until exit); limits: n <= 32768 atoms,
- * npairs <= 131072, ntypes <= 15, else DEM_ERR_BAD_ARG.  The first call on a
- * device looks up that array's device address and should come before any
- * stream capture on that device.  Calls share the array: calls that overlap
+ * npairs <= 131072, ntypes <= 15, else DEM_ERR_BAD_ARG; so is an entry of an
+ * atom with itself without an image shift.  CUDA loads a module's static
+ * arrays lazily by default (CUDA_MODULE_LOADING=LAZY): the first call on a
+ * device is when the ~11 MB is taken, so a caller that must not allocate
+ * mid-run makes one call at start-up (npairs = 0 suffices) or sets
+ * CUDA_MODULE_LOADING=EAGER; that first call should also come before any
+ * stream capture on the device.  Calls share the array: calls that overlap
  * on the GPU race and must be serialised by the caller. */
 int dem_contact_forces_noalloc(int n, const double *x, const double *v, const double *omega,
                                const double *radius, const double *rmass, const int *type,

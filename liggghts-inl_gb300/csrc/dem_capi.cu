@@ -700,8 +700,32 @@ int dem_add_plane(dem_handle *h, int axis, double pos, int wall_type, int rollin
   if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "add walls before uploading atoms");
   if (h->s.nplanes >= kMaxPlanes) return fail(h, DEM_ERR_BAD_ARG, "too many primitive walls");
   Plane &p = h->s.planes[h->s.nplanes];
+  p = Plane{};
   p.axis = axis;
   p.pos = pos;
+  p.pos_t = nullptr;
+  p.wall_type = wall_type;
+  p.rolling = rolling_model == DEM_ROLLING_CDT ? 1 : 0;
+  if (wall_id) *wall_id = h->s.nplanes;
+  h->s.nplanes++;
+  h->sys_gen++;
+  return DEM_OK;
+}
+
+int dem_add_cylinder(dem_handle *h, int axis, double radius, double center1, double center2, int wall_type,
+                     int rolling_model, int *wall_id) {
+  if (!h || axis < 0 || axis > 2 || wall_type < 1 || !(radius > 0.0) || !std::isfinite(radius) ||
+      !std::isfinite(center1) || !std::isfinite(center2))
+    return DEM_ERR_BAD_ARG;
+  if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "add walls before uploading atoms");
+  if (h->s.nplanes >= kMaxPlanes) return fail(h, DEM_ERR_BAD_ARG, "too many primitive walls");
+  Plane &p = h->s.planes[h->s.nplanes];
+  p = Plane{};
+  p.axis = axis;
+  p.pos = radius;
+  p.kind = 1;
+  p.c1 = center1;
+  p.c2 = center2;
   p.pos_t = nullptr;
   p.wall_type = wall_type;
   p.rolling = rolling_model == DEM_ROLLING_CDT ? 1 : 0;
@@ -721,6 +745,7 @@ int dem_add_plane_per_type(dem_handle *h, int axis, const double *pos_by_type, i
   CUDA_TRY(h, dalloc(h->allocs_misc, &dpos, (size_t)h->s.ntypes + 1));
   CUDA_TRY(h, cudaMemcpyAsync(dpos, pos_by_type, ((size_t)h->s.ntypes + 1) * sizeof(double), cudaMemcpyHostToDevice, h->st));
   Plane &p = h->s.planes[h->s.nplanes];
+  p = Plane{};
   p.axis = axis;
   p.pos = pos_by_type[1];
   p.pos_t = dpos;
@@ -1188,13 +1213,13 @@ int dem_upload_contact_history(dem_handle *h, int ne, const int *towner, const i
   std::vector<int> tags(n);
   CUDA_TRY(h, cudaMemcpyAsync(tags.data(), h->s.atoms[0].tag, n * sizeof(int), cudaMemcpyDeviceToHost, h->st));
   CUDA_TRY(h, cudaStreamSynchronize(h->st));
-  std::vector<std::pair<int, int>> t2i(n);
-  for (int i = 0; i < n; i++) t2i[i] = {tags[i], i};
-  std::sort(t2i.begin(), t2i.end());
-  auto find = [&](int t) -> int {
-    auto it = std::lower_bound(t2i.begin(), t2i.end(), std::make_pair(t, -1));
-    return (it != t2i.end() && it->first == t) ? it->second : -1;
-  };
+  // tag -> local index, as the reference's atom map array (Atom::map_set)
+  int maxtag = 0;
+  for (int i = 0; i < n; i++) maxtag = std::max(maxtag, tags[i]);
+  std::vector<int> t2i((size_t)maxtag + 1, -1);
+  for (int i = 0; i < n; i++)
+    if (tags[i] >= 0) t2i[tags[i]] = i;
+  auto find = [&](int t) -> int { return (t >= 0 && t <= maxtag) ? t2i[t] : -1; };
   std::vector<int> oi(ne), oj(ne), row(n + 1, 0);
   for (int k = 0; k < ne; k++) {
     oi[k] = find(towner[k]);
@@ -1210,12 +1235,12 @@ int dem_upload_contact_history(dem_handle *h, int ne, const int *towner, const i
   const size_t P = h->s.pcap;
   const int dnum = h->s.dnum;
   std::vector<int> pi(ne), pj(ne), fl(ne, 1), fill(row.begin(), row.end() - 1);
-  std::vector<double> hh((size_t)dnum * P, 0.0);
+  std::vector<double> hh((size_t)dnum * ne);  // [d*ne + p]: one block per history value
   for (int k = 0; k < ne; k++) {
     const int p = fill[oi[k]]++;
     pi[p] = oi[k];
     pj[p] = oj[k];
-    for (int r = 0; r < dnum; r++) hh[dev_hist_index(h->s, r) * P + p] = hist[(size_t)k * dnum + r];
+    for (int r = 0; r < dnum; r++) hh[(size_t)dev_hist_index(h->s, r) * ne + p] = hist[(size_t)k * dnum + r];
   }
   const PairArrays &L = h->s.pairs[0];
   if (ne) {
@@ -1226,7 +1251,9 @@ int dem_upload_contact_history(dem_handle *h, int ne, const int *towner, const i
     CUDA_TRY(h, cudaMemcpyAsync(L.j, pj.data(), ne * sizeof(int), cudaMemcpyHostToDevice, h->st));
     CUDA_TRY(h, cudaMemcpyAsync(L.sh, dsh.data(), ne, cudaMemcpyHostToDevice, h->st));
     CUDA_TRY(h, cudaMemcpyAsync(L.flag, fl.data(), ne * sizeof(int), cudaMemcpyHostToDevice, h->st));
-    CUDA_TRY(h, cudaMemcpyAsync(L.hist, hh.data(), hh.size() * sizeof(double), cudaMemcpyHostToDevice, h->st));
+    for (int d = 0; d < dnum; d++)
+      CUDA_TRY(h, cudaMemcpyAsync(L.hist + (size_t)d * P, hh.data() + (size_t)d * ne, (size_t)ne * sizeof(double),
+                                  cudaMemcpyHostToDevice, h->st));
   }
   CUDA_TRY(h, cudaMemcpyAsync(L.row, row.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, h->st));
   CUDA_TRY(h, cudaMemsetAsync(L.rev_start, 0, (h->s.nmax + 1) * sizeof(int), h->st));

@@ -113,9 +113,14 @@ struct Ctrl {
   int mesh_need;      // most candidate triangles an atom had beyond its mesh's capacity
 };
 
+// Primitive wall of fix wall/gran (src/primitive_wall_definitions.h): a
+// plane normal to `axis` at pos, or a cylinder about `axis` of radius pos
+// through (c1, c2) in the coordinates (axis+1)%3, (axis+2)%3.
 struct Plane {
   int axis;
   double pos;
+  int kind;           // 0: plane, 1: cylinder
+  double c1, c2;
   int wall_type;      // 0: the wall takes each atom's own type (per-type planes)
   int rolling;
   const double *pos_t;  // per-atom-type position [ntypes+1] (stacked ensembles) or nullptr

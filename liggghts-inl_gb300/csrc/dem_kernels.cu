@@ -278,9 +278,18 @@ __global__ void k_permute(Sys s) {
     for (int w = 0; w < s.nplanes; w++) {
       for (int d = 0; d < 3; d++)
         B.whist[(size_t)(w * 3 + d) * s.nmax + i] = A.whist[(size_t)(w * 3 + d) * s.nmax + o];
-      const double pos = s.planes[w].axis == 0 ? x : (s.planes[w].axis == 1 ? y : z);
-      const double dMax = r + s.skin;
-      const double dist = pos - plane_pos(s.planes[w], A.type[o]);
+      const Plane &pl = s.planes[w];
+      const double dMax = __dadd_rn(r, s.skin);
+      if (pl.kind == 1) {
+        // Cylinder<dim>::resolveNeighlist (src/primitive_wall_definitions.h:192-198)
+        const double xo[3] = {x, y, z};
+        const double dy = __dadd_rn(xo[(pl.axis + 1) % 3], -pl.c1), dz = __dadd_rn(xo[(pl.axis + 2) % 3], -pl.c2);
+        const double dist = __dadd_rn(__dsqrt_rn(__dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dz, dz))), -pl.pos);
+        if (dMax < dist || -dMax < dist) bits |= (uint8_t)(1u << w);
+        continue;
+      }
+      const double pos = pl.axis == 0 ? x : (pl.axis == 1 ? y : z);
+      const double dist = pos - plane_pos(pl, A.type[o]);
       const double absdist = (dist > 0.0) ? dist : -dist;
       if (absdist <= dMax) bits |= (uint8_t)(1u << w);
     }
@@ -1233,16 +1242,38 @@ __device__ __forceinline__ void plane_contact(const Sys &s, const AtomArrays &A,
   const double ppos = plane_pos(pl, A.type[i]);
   double delta[3];
   double deltan;
-  // Plane<dim>::resolveContact, src/primitive_wall_definitions.h:123-140
-  if (xv[ax] > ppos) {
+  if (pl.kind == 1) {
+    // Cylinder<dim>::resolveContact, src/primitive_wall_definitions.h:170-190,
+    // in the reference's operations and order
+    const double dy = __dadd_rn(xv[ay], -pl.c1), dz = __dadd_rn(xv[az], -pl.c2);
+    const double dist = __dsqrt_rn(__dadd_rn(__dmul_rn(dy, dy), __dmul_rn(dz, dz)));
+    if (dist < 1e-13 && dist > -1e-13) {  // compDouble(dist, 0.0)
+      delta[0] = delta[1] = delta[2] = 0.;
+      deltan = 0.0;
+    } else if (dist > ppos) {
+      deltan = __dadd_rn(__dadd_rn(dist, -ppos), -radi);
+      const double fact = __ddiv_rn(__dadd_rn(dist, -ppos), dist);
+      delta[ax] = 0.;
+      delta[ay] = __dmul_rn(-dy, fact);
+      delta[az] = __dmul_rn(-dz, fact);
+    } else {
+      deltan = __dadd_rn(__dadd_rn(ppos, -dist), -radi);
+      const double fact = __ddiv_rn(__dadd_rn(ppos, -dist), dist);
+      delta[ax] = 0.;
+      delta[ay] = __dmul_rn(dy, fact);
+      delta[az] = __dmul_rn(dz, fact);
+    }
+  } else if (xv[ax] > ppos) {  // Plane<dim>::resolveContact, src/primitive_wall_definitions.h:123-140
     delta[ax] = ppos - xv[ax];
     deltan = xv[ax] - ppos - radi;
   } else {
     delta[ax] = ppos - xv[ax];
     deltan = ppos - xv[ax] - radi;
   }
-  delta[ay] = 0.;
-  delta[az] = 0.;
+  if (pl.kind == 0) {
+    delta[ay] = 0.;
+    delta[az] = 0.;
+  }
   if (deltan > s.cutneighmax) return;
   double *h = A.whist + (size_t)(w * 3) * s.nmax + i;
   const size_t hs = s.nmax;
@@ -2104,21 +2135,38 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
 cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st, cudaStream_t st2,
                              cudaGraphExec_t *exec, int *kernels_per_step, int *kernels_per_rebuild) {
   cudaGraph_t g = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  // every failure leaves through here: end a capture still open on either
+  // stream (its graph belongs to g), destroy the events and the graph
+  auto fail = [&](cudaError_t err) -> cudaError_t {
+    const cudaStream_t qs[2] = {st, st2};
+    for (cudaStream_t q : qs) {
+      cudaStreamCaptureStatus cs0 = cudaStreamCaptureStatusNone;
+      if (cudaStreamIsCapturing(q, &cs0) == cudaSuccess && cs0 != cudaStreamCaptureStatusNone) {
+        cudaGraph_t part = nullptr;
+        cudaStreamEndCapture(q, &part);
+      }
+    }
+    if (fork) cudaEventDestroy(fork);
+    if (join) cudaEventDestroy(join);
+    if (g) cudaGraphDestroy(g);
+    return err;
+  };
   cudaError_t e = cudaGraphCreate(&g, 0);
-  if (e != cudaSuccess) return e;
+  if (e != cudaSuccess) return fail(e);
   cudaGraphConditionalHandle hloop, hreb;
-  if ((e = cudaGraphConditionalHandleCreate(&hloop, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
-  if ((e = cudaGraphConditionalHandleCreate(&hreb, g, 0, cudaGraphCondAssignDefault)) != cudaSuccess) return e;
+  if ((e = cudaGraphConditionalHandleCreate(&hloop, g, 1, cudaGraphCondAssignDefault)) != cudaSuccess) return fail(e);
+  if ((e = cudaGraphConditionalHandleCreate(&hreb, g, 0, cudaGraphCondAssignDefault)) != cudaSuccess) return fail(e);
   cudaGraphNodeParams wp = {};
   wp.type = cudaGraphNodeTypeConditional;
   wp.conditional.handle = hloop;
   wp.conditional.type = cudaGraphCondTypeWhile;
   wp.conditional.size = 1;
   cudaGraphNode_t wnode;
-  if ((e = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp)) != cudaSuccess) return e;
+  if ((e = cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp)) != cudaSuccess) return fail(e);
   cudaGraph_t body = wp.conditional.phGraph_out[0];
   if ((e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-    return e;
+    return fail(e);
   int k = launch_particle(s, lc, kModeGatherFinalInitial, 1, st);
   k += launch_mesh_move(s, lc, st);
   k_decide_loop<<<1, 1, 0, st>>>(s, hreb, hloop);
@@ -2127,40 +2175,41 @@ cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st,
   const cudaGraphNode_t *deps = nullptr;
   size_t nd = 0;
   cudaGraph_t cg;
-  if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &nd)) != cudaSuccess) return e;
+  if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &nd)) != cudaSuccess) return fail(e);
   cudaGraphNodeParams ip = {};
   ip.type = cudaGraphNodeTypeConditional;
   ip.conditional.handle = hreb;
   ip.conditional.type = cudaGraphCondTypeIf;
   ip.conditional.size = 1;
   cudaGraphNode_t inode;
-  if ((e = cudaGraphAddNode(&inode, cg, deps, nullptr, nd, &ip)) != cudaSuccess) return e;
+  if ((e = cudaGraphAddNode(&inode, cg, deps, nullptr, nd, &ip)) != cudaSuccess) return fail(e);
   cudaGraph_t rbody = ip.conditional.phGraph_out[0];
   if ((e = cudaStreamUpdateCaptureDependencies(st, &inode, nullptr, 1, cudaStreamSetCaptureDependencies)) != cudaSuccess)
-    return e;
+    return fail(e);
   // the pair kernel and the wall kernel of the step run side by side
-  cudaEvent_t fork = nullptr, join = nullptr;
   const bool walls = s.nmeshes > 0 || s.nplanes > 0;
   if (walls) {
-    if ((e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming)) != cudaSuccess) return e;
-    if ((e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming)) != cudaSuccess) return e;
-    if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(st2, fork, 0)) != cudaSuccess) return e;
+    if ((e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+    if ((e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+    if ((e = cudaEventRecord(fork, st)) != cudaSuccess) return fail(e);
+    if ((e = cudaStreamWaitEvent(st2, fork, 0)) != cudaSuccess) return fail(e);
     k += launch_wall_force(s, lc, 1, st2);
-    if ((e = cudaEventRecord(join, st2)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(join, st2)) != cudaSuccess) return fail(e);
   }
   k += launch_pair(s, lc, 1, st);
-  if (walls && (e = cudaStreamWaitEvent(st, join, 0)) != cudaSuccess) return e;
+  if (walls && (e = cudaStreamWaitEvent(st, join, 0)) != cudaSuccess) return fail(e);
   cudaGraph_t out = nullptr;
-  if ((e = cudaStreamEndCapture(st, &out)) != cudaSuccess) return e;
+  if ((e = cudaStreamEndCapture(st, &out)) != cudaSuccess) return fail(e);
   if (fork) cudaEventDestroy(fork);
   if (join) cudaEventDestroy(join);
+  fork = join = nullptr;
   if ((e = cudaStreamBeginCaptureToGraph(st2, rbody, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-    return e;
+    return fail(e);
   const int kr = launch_rebuild(s, lc, st2, 0);
-  if ((e = cudaStreamEndCapture(st2, &out)) != cudaSuccess) return e;
+  if ((e = cudaStreamEndCapture(st2, &out)) != cudaSuccess) return fail(e);
   e = cudaGraphInstantiate(exec, g, 0);
   cudaGraphDestroy(g);
+  g = nullptr;
   *kernels_per_step = k;
   *kernels_per_rebuild = kr;
   return e;

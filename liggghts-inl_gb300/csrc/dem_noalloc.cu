@@ -16,10 +16,16 @@
 // two host threads) race and must be serialised by the caller.  Each call
 // clears what it accumulates before use, so results never depend on the
 // previous call.
+//
+// When the array is taken: CUDA loads a module's device code and its static
+// arrays lazily by default (CUDA_MODULE_LOADING=LAZY), i.e. on the first
+// call on each device, which therefore takes the ~11 MB then.  A caller that
+// must not see that happen mid-run makes one call at start-up (any valid
+// input, npairs = 0 is enough) or runs with CUDA_MODULE_LOADING=EAGER; later
+// calls take no device memory.
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <mutex>
 
 #include "../../include/liggghts_gb300.h"
 #include "contact_law.cuh"
@@ -82,12 +88,12 @@ __global__ void na_pairs(NaArgs a) {
   const double *params = reinterpret_cast<const double *>(a.base + kOffParams);
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < a.np; p += gridDim.x * blockDim.x) {
     const int i = a.pi[p], j = a.pj[p];
-    if (i < 0 || i >= a.n || j < 0 || j >= a.n || (p > 0 && a.pi[p - 1] > i)) {
-      atomicExch(na_int(a, kOffFlag), 1);  // out of range or not sorted by owner
+    const int sx = a.shift[3 * p], sy = a.shift[3 * p + 1], sz = a.shift[3 * p + 2];
+    if (i < 0 || i >= a.n || j < 0 || j >= a.n || (p > 0 && a.pi[p - 1] > i) || (i == j && !sx && !sy && !sz)) {
+      atomicExch(na_int(a, kOffFlag), 1);  // out of range, not sorted by owner, or an atom with itself
       active[p] = 0;
       continue;
     }
-    const int sx = a.shift[3 * p], sy = a.shift[3 * p + 1], sz = a.shift[3 * p + 2];
     double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
     if (sx) xj = __dadd_rn(xj, sx * a.prd[0]);
     if (sy) yj = __dadd_rn(yj, sy * a.prd[1]);
@@ -219,20 +225,14 @@ __global__ void na_gather(NaArgs a) {
   }
 }
 
-// device address of the scratch array, looked up once per device with that
-// device current (the host-side symbol is only a stand-in, not an address)
-std::mutex g_na_mutex;
-unsigned char *g_na_base[64] = {};
-
-int scratch_address(int dev, unsigned char **out) {
-  std::lock_guard<std::mutex> lk(g_na_mutex);
-  if (dev < 0 || dev >= 64) return DEM_ERR_BAD_ARG;
-  if (!g_na_base[dev]) {
-    void *ptr = nullptr;
-    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return DEM_ERR_CUDA;
-    g_na_base[dev] = static_cast<unsigned char *>(ptr);
-  }
-  *out = g_na_base[dev];
+// Device address of the scratch array on the current device.  The name
+// g_noalloc_scratch in host code is only a stand-in for the symbol, not an
+// address; the lookup is repeated on every call (cheap once the module is
+// loaded), so a device reset or a new context never leaves a stale address.
+int scratch_address(unsigned char **out) {
+  void *ptr = nullptr;
+  if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return DEM_ERR_CUDA;
+  *out = static_cast<unsigned char *>(ptr);
   return DEM_OK;
 }
 
@@ -258,8 +258,10 @@ extern "C" int dem_contact_forces_noalloc(int n, const double *x, const double *
   if (cfg->cohesion_model != DEM_COHESION_OFF) return DEM_ERR_UNSUPPORTED;  // 3 history values per pair
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return DEM_ERR_NO_DEVICE;
+  // an error left by earlier, unrelated work is not this call's
+  (void)cudaGetLastError();
   unsigned char *base = nullptr;
-  int rc = scratch_address(dev, &base);
+  int rc = scratch_address(&base);
   if (rc) return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // material table into the scratch (host -> device copy, no allocation)
@@ -294,10 +296,10 @@ extern "C" int dem_contact_forces_noalloc(int n, const double *x, const double *
   na_scan<<<1, 1024, 0, st>>>(reinterpret_cast<int *>(base + kOffRevStart), n + 1);
   na_rev_fill<<<gp, B, 0, st>>>(a);
   na_gather<<<gn, B, 0, st>>>(a);
+  if (cudaGetLastError() != cudaSuccess) return DEM_ERR_CUDA;  // launches of this call
   int flag = 0;
   if (cudaMemcpyAsync(&flag, base + kOffFlag, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
     return DEM_ERR_CUDA;
   if (cudaStreamSynchronize(st) != cudaSuccess) return DEM_ERR_CUDA;
-  if (cudaGetLastError() != cudaSuccess) return DEM_ERR_CUDA;
   return flag ? DEM_ERR_BAD_ARG : DEM_OK;
 }

@@ -91,6 +91,8 @@ class DemAdjoint:
             raise ValueError("the adjoint covers no rolling friction or CDT")
         if any(int(pl[3]) != rolling for pl in case.get("planes", [])):
             raise ValueError("the adjoint's walls use the pairs' rolling model")
+        if case.get("cylinders"):
+            raise ValueError("the adjoint covers primitive planes and meshes, not cylinders")
         for m in case.get("meshes", []):
             if m.get("rotate") is not None:
                 raise ValueError("the adjoint covers static and translating meshes")

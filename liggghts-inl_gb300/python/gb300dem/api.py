@@ -92,6 +92,7 @@ def load(build=True):
     L.dem_set_bond_params.argtypes = [P, P, ctypes.POINTER(DemBondSettings)]
     L.dem_derive_hertz_tables.argtypes = [I] + [P] * 7
     L.dem_add_plane.argtypes = [P, I, ctypes.c_double, I, I, P]
+    L.dem_add_cylinder.argtypes = [P, I, ctypes.c_double, ctypes.c_double, ctypes.c_double, I, I, P]
     L.dem_add_plane_per_type.argtypes = [P, I, P, I, P]
     L.dem_set_tuning.argtypes = [P, I, ctypes.c_double]
     L.dem_set_particle_threads.argtypes = [P, I]
@@ -186,6 +187,9 @@ class DemSystem:
             self._check(L.dem_set_bond_params(self.h, _p(bt), ctypes.byref(st)))
         for (axis, pos, wtype, roll) in case.get("planes", []):
             self._check(L.dem_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll), None))
+        for (axis, rad, c1, c2, wtype, roll) in case.get("cylinders", []):
+            self._check(L.dem_add_cylinder(self.h, int(axis), float(rad), float(c1), float(c2), int(wtype),
+                                           int(roll), None))
         for (axis, pos_t, roll) in case.get("planes_per_type", []):
             pt = np.ascontiguousarray(pos_t, dtype=np.float64)
             self._check(L.dem_add_plane_per_type(self.h, int(axis), _p(pt), int(roll), None))

@@ -193,9 +193,59 @@ def restart_state(sys_, case):
     tp = np.concatenate([tj, ti[own]]).astype(np.int32)
     hh = np.concatenate([hs, hs[own] * sgn[None, :]])
     order = np.argsort(a["tag"], kind="stable")
-    walls = [np.asarray(sys_.wall_history(w))[order] for w in range(len(case.get("planes", [])))]
+    nprim = len(case.get("planes", [])) + len(case.get("cylinders", []))
+    walls = [np.asarray(sys_.wall_history(w))[order] for w in range(nprim)]
     ck["atoms"] = {k: v[order] for k, v in ck["atoms"].items()}
     return ck, to, tp, hh, walls
+
+
+def silo_case(seed, R=8e-3, nz=6, spacing=2.05e-3, radius=(0.9e-3, 1.0e-3), bar=(1.5e-3, 7e-3),
+              vmax=0.5, wmax=80.0, **kw):
+    """A jittered lattice filling a vertical cylinder (fix wall/gran
+    primitive zcylinder R 0 0: contacts from inside) on a floor plane, with a
+    horizontal bar through the bed (xcylinder of radius bar[0] at height
+    bar[1]: contacts from outside), closed box."""
+    rng = np.random.default_rng(seed)
+    rmax = radius[1]
+    m = int(2 * R / spacing) + 1
+    g = (np.arange(m) - (m - 1) / 2.0) * spacing
+    pts = []
+    for k in range(nz):
+        z = rmax + k * spacing
+        for x0 in g:
+            for y0 in g:
+                if math.hypot(x0, y0) + rmax > R - spacing:
+                    continue
+                if math.hypot(y0, z - bar[1]) < bar[0] + spacing:
+                    continue
+                pts.append((x0, y0, z))
+        # a ring just inside the wall (overlapping it slightly)
+        nr = int(2 * math.pi * (R - rmax) / spacing)
+        for q in range(nr):
+            t = 2 * math.pi * (q + 0.5 * (k % 2)) / nr
+            pts.append(((R - 0.97 * rmax) * math.cos(t), (R - 0.97 * rmax) * math.sin(t), z))
+    # a row resting on the bar (touching it from outside)
+    zb = bar[1] + bar[0] + 0.97 * rmax
+    for x0 in g[1:-1]:
+        pts.append((x0, 0.0, zb))
+    x = np.asarray(pts, dtype=np.float64)
+    keep = np.ones(len(x), bool)
+    for a in range(len(x)):  # drop lattice sites that overlap a ring or bar atom
+        if keep[a]:
+            d = np.linalg.norm(x[a + 1:] - x[a], axis=1)
+            keep[a + 1:][d < 0.95 * spacing] = False
+    x = x[keep]
+    x += rng.uniform(-0.01 * spacing, 0.01 * spacing, size=x.shape)
+    n = len(x)
+    c = lattice_case(seed, 1, 1, 1, 1.0, radius=radius, periodic=(0, 0, 0), **kw)
+    r = rng.uniform(radius[0], radius[1], size=n) if radius[0] != radius[1] else np.full(n, radius[0])
+    c["boxlo"] = (-R - 4 * rmax, -R - 4 * rmax, -2 * rmax)
+    c["boxhi"] = (R + 4 * rmax, R + 4 * rmax, float(x[:, 2].max() + 6 * rmax))
+    c["cylinders"] = [(2, R, 0.0, 0.0, 1, c["rolling_model"]), (0, bar[0], 0.0, bar[1], 1, c["rolling_model"])]
+    c["atoms"] = dict(tag=np.arange(1, n + 1, dtype=np.int32), type=np.ones(n, np.int32), x=x,
+                      v=rng.uniform(-vmax, vmax, size=(n, 3)), omega=rng.uniform(-wmax, wmax, size=(n, 3)),
+                      radius=r, rmass=sphere_mass(r, c["material"]["density"]))
+    return c
 
 
 def fine_floor_case(seed, nx=6, ny=6, nz=2, spacing=2.1e-3, radius=(0.95e-3, 1.05e-3), tri=0.5e-3,

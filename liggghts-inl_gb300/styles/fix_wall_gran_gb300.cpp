@@ -20,18 +20,30 @@ using namespace LAMMPS_NS;
    (src/fix_wall_gran.cpp:149-300); the keywords the device needs are read
    again here from the same argument list */
 FixWallGranGB300::FixWallGranGB300(LAMMPS *lmp, int narg, char **arg)
-    : FixWallGran(lmp, narg, arg), primitive_(false), axis_(-1), pos_(0.0), wall_type_(0),
+    : FixWallGran(lmp, narg, arg), primitive_(false), cylinder_(false), axis_(-1), pos_(0.0), c1_(0.0), c2_(0.0),
+      wall_type_(0),
       rolling_(DEM_ROLLING_OFF), device_wall_id_(-1) {
   for (int k = 3; k < narg; k++) {
     if (strcmp(arg[k], "primitive") == 0 && k + 4 < narg && strcmp(arg[k + 1], "type") == 0) {
+      // primitive type T {x,y,z}plane P | {x,y,z}cylinder R C1 C2
+      // (PRIMITIVE_WALL_DEFINITIONS::wallString/numArgs, src/primitive_wall_definitions.h:74-94)
       primitive_ = true;
       wall_type_ = atoi(arg[k + 2]);
       const char *ws = arg[k + 3];
-      if (strcmp(ws, "xplane") == 0) axis_ = 0;
-      else if (strcmp(ws, "yplane") == 0) axis_ = 1;
-      else if (strcmp(ws, "zplane") == 0) axis_ = 2;
-      else error->all(FLERR, "fix wall/gran/gb300: primitive walls must be xplane, yplane or zplane");
+      const char *names[] = {"xplane", "yplane", "zplane", "xcylinder", "ycylinder", "zcylinder"};
+      int kind = -1;
+      for (int q = 0; q < 6; q++)
+        if (strcmp(ws, names[q]) == 0) kind = q;
+      if (kind < 0) error->all(FLERR, "fix wall/gran/gb300: primitive walls must be planes or cylinders");
+      axis_ = kind % 3;
+      cylinder_ = kind >= 3;
+      if (cylinder_ && k + 6 >= narg) error->all(FLERR, "fix wall/gran/gb300: a cylinder takes R C1 C2");
       pos_ = atof(arg[k + 4]);
+      if (cylinder_) {
+        c1_ = atof(arg[k + 5]);
+        c2_ = atof(arg[k + 6]);
+        k += 2;
+      }
       k += 4;
     } else if (strcmp(arg[k], "meshes") == 0) {
       for (int q = k + 1; q < narg && modify->find_fix(arg[q]) >= 0; q++) mesh_ids_.push_back(arg[q]);
@@ -55,8 +67,9 @@ void FixWallGranGB300::upload(dem_handle *h, int) {
   else error->all(FLERR, "fix wall/gran/gb300: rolling_friction must be off or cdt");
 
   if (primitive_) {
-    if (dem_add_plane(h, axis_, pos_, wall_type_, rolling_, &device_wall_id_) != DEM_OK)
-      error->all(FLERR, dem_last_error(h));
+    const int rc = cylinder_ ? dem_add_cylinder(h, axis_, pos_, c1_, c2_, wall_type_, rolling_, &device_wall_id_)
+                             : dem_add_plane(h, axis_, pos_, wall_type_, rolling_, &device_wall_id_);
+    if (rc != DEM_OK) error->all(FLERR, dem_last_error(h));
     return;
   }
   device_mesh_ids_.clear();

@@ -49,8 +49,10 @@ class FixWallGranGB300 : public FixWallGran {
 
  private:
   bool primitive_;
+  bool cylinder_;   // primitive {x,y,z}cylinder R C1 C2 (else a plane)
   int axis_;
-  double pos_;
+  double pos_;      // plane position, or cylinder radius
+  double c1_, c2_;  // cylinder centre along (axis+1)%3, (axis+2)%3
   int wall_type_;
   int rolling_;
   std::vector<std::string> mesh_ids_;

@@ -68,6 +68,8 @@ def lib():
         L.orc_set_pair_params.argtypes = [P, ctypes.c_int] + [P] * 6 + [ctypes.c_double]
         L.orc_set_bond_params.argtypes = [P, P, ctypes.POINTER(OrcBondSettings)]
         L.orc_add_plane.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.orc_add_cylinder.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                       ctypes.c_int, ctypes.c_int]
         L.orc_set_atoms.argtypes = [P, ctypes.c_int] + [P] * 7
         L.orc_setup.argtypes = [P]
         L.orc_run.argtypes = [P, ctypes.c_int]
@@ -142,6 +144,8 @@ class Oracle:
             self._check(L.orc_set_bond_params(self.h, _p(bt), ctypes.byref(st)))
         for (axis, pos, wtype, roll) in case.get("planes", []):
             L.orc_add_plane(self.h, int(axis), float(pos), int(wtype), int(roll))
+        for (axis, rad, c1, c2, wtype, roll) in case.get("cylinders", []):
+            L.orc_add_cylinder(self.h, int(axis), float(rad), float(c1), float(c2), int(wtype), int(roll))
         self.nmesh = 0
         self._mesh_nodes = []
         for m in case.get("meshes", []):

@@ -41,7 +41,9 @@
 
 typedef struct {
   int axis;
-  double pos;
+  double pos;        /* plane: position on the axis; cylinder: radius */
+  int kind;          /* 0: plane, 1: cylinder about the axis through (c1, c2) */
+  double c1, c2;     /* cylinder centre: coordinates (axis+1)%3 and (axis+2)%3 */
   int wall_type;
   int rolling_model;
   int *nlist;        /* PrimitiveWall neighbour list (atom indices) */
@@ -187,6 +189,18 @@ int orc_add_plane(orc_sys *s, int axis, double pos, int wall_type, int rolling_m
   orc_plane *w = &s->planes[s->nplanes++];
   memset(w, 0, sizeof *w);
   w->axis = axis; w->pos = pos; w->wall_type = wall_type; w->rolling_model = rolling_model;
+  return 0;
+}
+
+/* FixWallGran primitive xcylinder/ycylinder/zcylinder R c1 c2
+   (src/primitive_wall_definitions.h:69-71,155-200: param[0] radius,
+   param[1], param[2] the centre's coordinates along (axis+1)%3, (axis+2)%3) */
+int orc_add_cylinder(orc_sys *s, int axis, double radius, double c1, double c2, int wall_type, int rolling_model) {
+  if (s->nplanes >= 8) { snprintf(s->err, sizeof s->err, "too many primitive walls"); return -1; }
+  orc_plane *w = &s->planes[s->nplanes++];
+  memset(w, 0, sizeof *w);
+  w->axis = axis; w->pos = radius; w->kind = 1; w->c1 = c1; w->c2 = c2;
+  w->wall_type = wall_type; w->rolling_model = rolling_model;
   return 0;
 }
 
@@ -843,8 +857,16 @@ static void plane_neighbors(orc_sys *s) {
     orc_plane *pl = &s->planes[w];
     if (pl->nncap < s->n) { pl->nncap = s->n; pl->nlist = (int *)xrealloc(pl->nlist, s->n * sizeof(int)); }
     pl->nn = 0;
+    const int ay = (pl->axis + 1) % 3, az = (pl->axis + 2) % 3;
     for (int i = 0; i < s->n; i++) {
       double dMax = s->radius[i] + s->cfg.skin;
+      if (pl->kind == 1) {
+        /* Cylinder<dim>::resolveNeighlist (src/primitive_wall_definitions.h:192-198) */
+        double dy = s->x[3 * i + ay] - pl->c1, dz = s->x[3 * i + az] - pl->c2;
+        double dist = sqrt(dy * dy + dz * dz) - pl->pos;
+        if (dMax < dist || -dMax < dist) pl->nlist[pl->nn++] = i;
+        continue;
+      }
       double dist = s->x[3 * i + pl->axis] - pl->pos;
       double absdist = (dist > 0.0) ? dist : -dist;
       if (absdist <= dMax) pl->nlist[pl->nn++] = i;
@@ -1506,7 +1528,23 @@ static void plane_post_force(orc_sys *s, orc_plane *pl, int shearupdate) {
     double deltan;
     const double *pos = &s->x[3 * ip];
     const int ax = pl->axis, ay = (ax + 1) % 3, az = (ax + 2) % 3;
-    if (pos[ax] > pl->pos) {
+    if (pl->kind == 1) {
+      /* Cylinder<dim>::resolveContact (src/primitive_wall_definitions.h:170-190) */
+      const double dy = pos[ay] - pl->c1, dz = pos[az] - pl->c2;
+      const double dist = sqrt(dy * dy + dz * dz);
+      if (dist < 1e-13 && dist > -1e-13) { /* compDouble(dist, 0.0) */
+        delta[0] = delta[1] = delta[2] = 0.;
+        deltan = 0.0;
+      } else if (dist > pl->pos) {
+        deltan = dist - pl->pos - sd.radi;
+        const double fact = (dist - pl->pos) / dist;
+        delta[ax] = 0.; delta[ay] = -dy * fact; delta[az] = -dz * fact;
+      } else {
+        deltan = pl->pos - dist - sd.radi;
+        const double fact = (pl->pos - dist) / dist;
+        delta[ax] = 0.; delta[ay] = +dy * fact; delta[az] = +dz * fact;
+      }
+    } else if (pos[ax] > pl->pos) {
       delta[ax] = pl->pos - pos[ax]; delta[ay] = 0.; delta[az] = 0.;
       deltan = pos[ax] - pl->pos - sd.radi;
     } else {

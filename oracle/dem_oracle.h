@@ -79,6 +79,7 @@ int orc_set_bond_params(orc_sys *s, const double *tables, const orc_bond_setting
 
 /* fix wall/gran ... primitive type WTYPE {x,y,z}plane POS (axis 0/1/2). */
 int orc_add_plane(orc_sys *s, int axis, double pos, int wall_type, int rolling_model);
+int orc_add_cylinder(orc_sys *s, int axis, double radius, double c1, double c2, int wall_type, int rolling_model);
 
 /* fix mesh/surface + fix wall/gran mesh: nodes[ntri*9], element id = index.
  * edge_active/corner_active[ntri*3]: the reference's flags, or NULL to derive

@@ -99,6 +99,13 @@ def write_inputs(case, d, nsteps, snaps=None, dump_every=None, extra=(), run_sty
             wm += " rolling_friction cdt"
         s.append("fix wall%d all wall/gran %s primitive type %d %splane %s"
                  % (k, wm, wtype, "xyz"[axis], fmt(pos)))
+    npl = len(case["planes"])
+    for k, (axis, rad, c1, c2, wtype, roll) in enumerate(case.get("cylinders", [])):
+        wm = "model %s tangential history" % ("hooke" if case["normal_model"] == 1 else "hertz")
+        if roll == 1:
+            wm += " rolling_friction cdt"
+        s.append("fix wall%d all wall/gran %s primitive type %d %scylinder %s %s %s"
+                 % (npl + k, wm, wtype, "xyz"[axis], fmt(rad), fmt(c1), fmt(c2)))
     for k, m in enumerate(case.get("meshes", [])):
         workloads.write_stl(os.path.join(d, "mesh%d.stl" % k), m["nodes"])
         s.append("fix cad%d all mesh/surface file mesh%d.stl type %d" % (k, k, m["wall_type"]))

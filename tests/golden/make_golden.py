@@ -73,6 +73,12 @@ def cases():
         53, nx=8, ny=8, nz=3, spacing=2.2e-3, radius=(0.95e-3, 1.0e-3), blade_half_len=6e-3,
         blade_height=7e-3, period=0.02, z0=1.0e-3, jitter=2e-5, vmax=0.5, wmax=50.0),
         600, [0, 1, 2, 10, 50, 100, 200, 300, 400, 500, 600])
+    # a cylindrical silo (primitive zcylinder, contacts from inside) on a floor
+    # plane with a horizontal bar through the bed (primitive xcylinder,
+    # contacts from outside), CDT rolling on pairs and walls
+    c["silo_cyl"] = (workloads.silo_case(
+        81, rolling_model=1, rollfrict=((0.3,),), E=(1e7,), nu=(0.3,), rest=((0.6,),), frict=((0.5,),),
+        density=2000.0), 500, [0, 1, 2, 10, 50, 100, 200, 300, 500])
     # fibres of bonded spheres (cohesion bond/nonlinear), floor of wall type 2
     for name, seed, stress in (("fibre_bond", 41, 0), ("fibre_bond_stress", 43, 1)):
         r = 0.5e-3

@@ -21,7 +21,7 @@ from golden_io import (DIVERGED_RTOL, FORCE_RTOL, HIST_RTOL, TRAJ_RTOL, canonica
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["dense_hertz", "poly_cdt", "hooke", "fibre_bond", "fibre_bond_stress"]
+CASES = ["dense_hertz", "poly_cdt", "hooke", "fibre_bond", "fibre_bond_stress", "silo_cyl"]
 
 
 def _gpu(case):
@@ -65,8 +65,11 @@ def test_gpu_matches_reference_snapshots(name):
         assert not missing and not extra, (name, st, len(missing), len(extra))
         assert all(gp[k][0] == rp[k][0] for k in rp), "contact flags differ"
         assert hm < (HIST_RTOL if st <= 100 else 1e-6), (name, st, hm)
-        wh = g.wall_history(0)[np.argsort(g.atoms()["tag"], kind="stable")]
-        assert max_rel(wh, r["wall0_hist"]) < (HIST_RTOL if st <= 100 else 1e-6)
+        order = np.argsort(g.atoms()["tag"], kind="stable")
+        nw = len([k for k in r if k.startswith("wall") and k.endswith("_hist")])
+        for w in range(nw):  # planes, then cylinders
+            wh = g.wall_history(w)[order]
+            assert max_rel(wh, r["wall%d_hist" % w]) < (HIST_RTOL if st <= 100 else 1e-6), (name, st, w)
     assert g.nrebuilds >= 2
 
 

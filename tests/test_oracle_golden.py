@@ -11,7 +11,7 @@ from golden_io import (FORCE_RTOL, HIST_RTOL, canonical_pairs, compare_pairs, lo
                        max_rel, sort_by_tag)
 from oracle.binding import Oracle
 
-CASES = ["dense_hertz", "poly_cdt", "hooke", "fibre_bond", "fibre_bond_stress"]
+CASES = ["dense_hertz", "poly_cdt", "hooke", "fibre_bond", "fibre_bond_stress", "silo_cyl"]
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -42,8 +42,11 @@ def test_oracle_matches_reference(name):
         assert not flagmis
         assert all(gp[k][0] == rp[k][0] for k in rp), "contact flag bits differ"
         assert hm < (HIST_RTOL if st <= 100 else 1e-8)
-        wh = o.wall_history(0)[np.argsort(o.atoms()["tag"], kind="stable")]
-        assert max_rel(wh, r["wall0_hist"]) < (HIST_RTOL if st <= 100 else 1e-8)
+        order = np.argsort(o.atoms()["tag"], kind="stable")
+        nw = len([k for k in r if k.startswith("wall") and k.endswith("_hist")])
+        for w in range(nw):  # planes, then cylinders
+            wh = o.wall_history(w)[order]
+            assert max_rel(wh, r["wall%d_hist" % w]) < (HIST_RTOL if st <= 100 else 1e-8), (name, st, w)
     assert o.nrebuilds >= 2, "fixture must exercise history carry-over across rebuilds"
 
 

@@ -100,7 +100,7 @@ def _run(case, extra, d, suffix):
 
 
 CASES = ["dense_hertz", "poly_cdt", "hooke", "hopper_mesh_cdt", "fibre_bond", "fibre_press",
-         "mixer_rotate", "insert_pack"]
+         "mixer_rotate", "silo_cyl", "insert_pack"]
 
 
 @needs_binary
