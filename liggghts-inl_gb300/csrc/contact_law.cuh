@@ -17,7 +17,10 @@
 //     the pow() of the reference is evaluated once per neighbour build;
 //   * Coulomb test kt|s| > mu|Fn| on squares; sqrt and division only when
 //     the contact slides; shear = -Ft/kt as shear*ratio;
-//   * 1/r and 1/|w_roll| as rsqrt.
+//   * 1/r and 1/|w_roll| as rsqrt;
+//   * 4/3 Yeff and 8 Geff from the type table; (cri, crj)/r formed once;
+//     the rolling torque folded into the torque products (one rounding
+//     fewer).
 // The quantities that decide the contact set (rsq, radsum) and the overlap
 // deltan = radsum - sqrt(rsq) are formed exactly as in the reference.
 #pragma once
@@ -27,8 +30,15 @@ namespace gb300 {
 
 enum { kHertz = 0, kHooke = 1 };
 
+// Per type pair: Yeff, Geff, betaeff, coeffFrict, coeffRollFrict,
+// coeffRestLog, and the Hertz stiffness prefactors 4/3 Yeff and 8 Geff
+// (formed on the host as the reference forms them inside its law, so kn and
+// kt keep their bits).  The table stacks kTypeTables matrices of (nt+1)^2.
+constexpr int kTypeTables = 8;
+
 struct TypePair {
   double Y, G, beta, mu, mur, restlog;
+  double Y43, G8;
 };
 
 __device__ __forceinline__ TypePair load_typepair(const double *__restrict__ params, int nt,
@@ -42,7 +52,17 @@ __device__ __forceinline__ TypePair load_typepair(const double *__restrict__ par
   t.mu = __ldg(params + 3 * m + k);
   t.mur = __ldg(params + 4 * m + k);
   t.restlog = __ldg(params + 5 * m + k);
+  t.Y43 = __ldg(params + 6 * m + k);
+  t.G8 = __ldg(params + 7 * m + k);
   return t;
+}
+
+// host side: the two derived matrices from Yeff and Geff
+inline void derive_type_tables(int m, double *tab) {
+  for (int q = 0; q < m; q++) {
+    tab[6 * m + q] = 4. / 3. * tab[q];
+    tab[7 * m + q] = 8. * tab[m + q];
+  }
 }
 
 // Per-pair constants of the normal law.  Hertz: (Kn, Kt) damping prefactors;
@@ -109,9 +129,10 @@ __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &
   } else {
     cri = c.radi - 0.5 * deltan;
     crj = c.radj - 0.5 * deltan;
-    wr1 = (cri * c.wi[0] + crj * c.wj[0]) * c.rinv;
-    wr2 = (cri * c.wi[1] + crj * c.wj[1]) * c.rinv;
-    wr3 = (cri * c.wi[2] + crj * c.wj[2]) * c.rinv;
+    const double ai = cri * c.rinv, aj = crj * c.rinv;
+    wr1 = ai * c.wi[0] + aj * c.wj[0];
+    wr2 = ai * c.wi[1] + aj * c.wj[1];
+    wr3 = ai * c.wi[2] + aj * c.wj[2];
   }
   const double vtr1 = vt1 - (dz * wr2 - dy * wr3);
   const double vtr2 = vt2 - (dx * wr3 - dz * wr1);
@@ -122,8 +143,8 @@ __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &
   if (NORMAL == kHertz) {
     const double sqrtval = sqrt(c.reff * deltan);
     const double q = sqrt(sqrtval);
-    kn = 4. / 3. * tp.Y * sqrtval;
-    kt = 8. * tp.G * sqrtval;
+    kn = tp.Y43 * sqrtval;
+    kt = tp.G8 * sqrtval;
     gamman = c.c0 * q;
     gammat = c.c1 * q;
   } else {
@@ -173,29 +194,9 @@ __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &
   const double tor1 = eny * Ft3 - enz * Ft2;
   const double tor2 = enz * Ft1 - enx * Ft3;
   const double tor3 = enx * Ft2 - eny * Ft1;
-  if (base) {
-    o.F[0] = base->F[0] + Ft1;
-    o.F[1] = base->F[1] + Ft2;
-    o.F[2] = base->F[2] + Ft3;
-    o.Ti[0] = base->Ti[0] + -cri * tor1;
-    o.Ti[1] = base->Ti[1] + -cri * tor2;
-    o.Ti[2] = base->Ti[2] + -cri * tor3;
-    o.Tj[0] = base->Tj[0] + -crj * tor1;
-    o.Tj[1] = base->Tj[1] + -crj * tor2;
-    o.Tj[2] = base->Tj[2] + -crj * tor3;
-  } else {
-    o.F[0] = Fn * enx + Ft1;
-    o.F[1] = Fn * eny + Ft2;
-    o.F[2] = Fn * enz + Ft3;
-    o.Ti[0] = -cri * tor1;
-    o.Ti[1] = -cri * tor2;
-    o.Ti[2] = -cri * tor3;
-    o.Tj[0] = -crj * tor1;
-    o.Tj[1] = -crj * tor2;
-    o.Tj[2] = -crj * tor3;
-  }
-
-  // ---- rolling friction, constant directional torque
+  // rolling friction, constant directional torque: rt, taken from Ti and
+  // given to Tj (folded into their products below)
+  double rt1 = 0., rt2 = 0., rt3 = 0.;
   if (rolling) {
     double w1, w2, w3;
     if (WALL) {
@@ -208,20 +209,37 @@ __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &
       w3 = c.wi[2] - c.wj[2];
     }
     const double wsq = w1 * w1 + w2 * w2 + w3 * w3;
-    if (wsq > 0.) {
+    if (__double_as_longlong(wsq) != 0) {  // wsq > 0 (a sum of squares: +0 or positive)
       const double fac = tp.mur * kn * deltan * c.reff * rsqrt(wsq);
-      double rt1 = fac * w1, rt2 = fac * w2, rt3 = fac * w3;
+      rt1 = fac * w1;
+      rt2 = fac * w2;
+      rt3 = fac * w3;
       const double rtd = rt1 * enx + rt2 * eny + rt3 * enz;
       rt1 -= enx * rtd;
       rt2 -= eny * rtd;
       rt3 -= enz * rtd;
-      o.Ti[0] -= rt1;
-      o.Ti[1] -= rt2;
-      o.Ti[2] -= rt3;
-      o.Tj[0] += rt1;
-      o.Tj[1] += rt2;
-      o.Tj[2] += rt3;
     }
+  }
+  if (base) {
+    o.F[0] = base->F[0] + Ft1;
+    o.F[1] = base->F[1] + Ft2;
+    o.F[2] = base->F[2] + Ft3;
+    o.Ti[0] = base->Ti[0] + (-cri * tor1 - rt1);
+    o.Ti[1] = base->Ti[1] + (-cri * tor2 - rt2);
+    o.Ti[2] = base->Ti[2] + (-cri * tor3 - rt3);
+    o.Tj[0] = base->Tj[0] + (-crj * tor1 + rt1);
+    o.Tj[1] = base->Tj[1] + (-crj * tor2 + rt2);
+    o.Tj[2] = base->Tj[2] + (-crj * tor3 + rt3);
+  } else {
+    o.F[0] = Fn * enx + Ft1;
+    o.F[1] = Fn * eny + Ft2;
+    o.F[2] = Fn * enz + Ft3;
+    o.Ti[0] = -cri * tor1 - rt1;
+    o.Ti[1] = -cri * tor2 - rt2;
+    o.Ti[2] = -cri * tor3 - rt3;
+    o.Tj[0] = -crj * tor1 + rt1;
+    o.Tj[1] = -crj * tor2 + rt2;
+    o.Tj[2] = -crj * tor3 + rt3;
   }
 }
 

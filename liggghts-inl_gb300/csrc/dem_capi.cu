@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/liggghts_gb300.h"
+#include "contact_law.cuh"
 #include "dem_device.cuh"
 #include "dem_kernels.h"
 #include "dem_mesh_host.h"
@@ -476,8 +477,10 @@ int dem_create(const dem_config *cfg, dem_handle **out) {
   h->cfg = *cfg;
   cudaGetDevice(&h->device);
   cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, h->device) == cudaSuccess)
+  if (cudaGetDeviceProperties(&prop, h->device) == cudaSuccess) {
     h->lc.max_grid = prop.multiProcessorCount * 8;
+    h->lc.sms = prop.multiProcessorCount;
+  }
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&h->ev0) != cudaSuccess || cudaEventCreate(&h->ev1) != cudaSuccess) {
@@ -596,10 +599,11 @@ int dem_set_pair_params(dem_handle *h, int ntypes, const double *Yeff, const dou
   if (h->cfg.normal_model == DEM_NORMAL_HERTZ && !betaeff) return fail(h, DEM_ERR_BAD_ARG, "betaeff required");
   if (h->cfg.normal_model == DEM_NORMAL_HOOKE && !coeffRestLog) return fail(h, DEM_ERR_BAD_ARG, "coeffRestLog required");
   const int m = (ntypes + 1) * (ntypes + 1);
-  std::vector<double> tab(6 * (size_t)m, 0.0);
+  std::vector<double> tab(kTypeTables * (size_t)m, 0.0);
   const double *src[6] = {Yeff, Geff, betaeff, coeffFrict, coeffRollFrict, coeffRestLog};
   for (int k = 0; k < 6; k++)
     if (src[k]) std::memcpy(&tab[(size_t)k * m], src[k], m * sizeof(double));
+  derive_type_tables(m, tab.data());
   if (h->s.params) {
     cudaFree(h->s.params);
     h->allocs_misc.erase(std::remove(h->allocs_misc.begin(), h->allocs_misc.end(), (void *)h->s.params),

@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <stdint.h>
 
 #include "bond_law.cuh"
@@ -1119,8 +1120,8 @@ __device__ __forceinline__ void pair_entry(const Sys &s, int q, int shearupdate)
   s.active[q] = 1;
 }
 
-template <int NORMAL, bool ROLL>
-__global__ void __launch_bounds__(kPairTile, 3) k_pair_pf(Sys s, int shearupdate) {
+template <int NORMAL, bool ROLL, int MINB>
+__global__ void __launch_bounds__(kPairTile, MINB) k_pair_pf(Sys s, int shearupdate) {
   __shared__ int q[2 * kPairTile];
   __shared__ int wcnt[kPairTile / 32];
   __shared__ int qn_s;
@@ -2286,12 +2287,34 @@ int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t
     return 1;
   }
   if (s.cdf == 1.0) {
-    if (s.normal == kHertz) {
-      if (s.rolling) k_pair_pf<kHertz, true><<<g, B, 0, st>>>(s, shearupdate);
-      else k_pair_pf<kHertz, false><<<g, B, 0, st>>>(s, shearupdate);
+    // blocks per SM the kernel is compiled for (registers: 80 at 3, 64 at
+    // 4 with some spilling) and the grid: LIGGGHTS_GB300_PAIR_MINB (3 or 4),
+    // LIGGGHTS_GB300_PAIR_GRID (0: up to 8 blocks per SM, 1: one resident
+    // wave, the tiles taken grid-stride); results do not depend on either
+    static int minb = -1, wave = 0;
+    if (minb < 0) {
+      const char *e = getenv("LIGGGHTS_GB300_PAIR_MINB");
+      minb = (e && atoi(e) == 4) ? 4 : 3;
+      const char *w = getenv("LIGGGHTS_GB300_PAIR_GRID");
+      wave = (w && atoi(w) == 1) ? 1 : 0;
+    }
+    const int gp = wave ? std::min(g, lc.sms * minb) : g;
+    if (minb == 4) {
+      if (s.normal == kHertz) {
+        if (s.rolling) k_pair_pf<kHertz, true, 4><<<gp, B, 0, st>>>(s, shearupdate);
+        else k_pair_pf<kHertz, false, 4><<<gp, B, 0, st>>>(s, shearupdate);
+      } else {
+        if (s.rolling) k_pair_pf<kHooke, true, 4><<<gp, B, 0, st>>>(s, shearupdate);
+        else k_pair_pf<kHooke, false, 4><<<gp, B, 0, st>>>(s, shearupdate);
+      }
     } else {
-      if (s.rolling) k_pair_pf<kHooke, true><<<g, B, 0, st>>>(s, shearupdate);
-      else k_pair_pf<kHooke, false><<<g, B, 0, st>>>(s, shearupdate);
+      if (s.normal == kHertz) {
+        if (s.rolling) k_pair_pf<kHertz, true, 3><<<gp, B, 0, st>>>(s, shearupdate);
+        else k_pair_pf<kHertz, false, 3><<<gp, B, 0, st>>>(s, shearupdate);
+      } else {
+        if (s.rolling) k_pair_pf<kHooke, true, 3><<<gp, B, 0, st>>>(s, shearupdate);
+        else k_pair_pf<kHooke, false, 3><<<gp, B, 0, st>>>(s, shearupdate);
+      }
     }
     return 1;
   }

@@ -9,6 +9,7 @@ namespace gb300 {
 struct LaunchCfg {
   int max_grid;              // grid-stride kernels never launch more blocks of 256 than this
   int particle_threads = 256;  // threads per block of the per-particle kernel (64, 128, 256)
+  int sms = 152;               // multiprocessors of the device
 };
 
 enum {

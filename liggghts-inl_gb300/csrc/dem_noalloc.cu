@@ -37,7 +37,7 @@ using namespace gb300;
 constexpr int kNaMaxAtoms = 32768;
 constexpr int kNaMaxPairs = 131072;
 constexpr int kNaMaxTypes = 15;
-constexpr int kNaParams = 6 * (kNaMaxTypes + 1) * (kNaMaxTypes + 1);
+constexpr int kNaParams = kTypeTables * (kNaMaxTypes + 1) * (kNaMaxTypes + 1);
 
 // byte offsets of the sub-arrays inside the scratch array (256-byte aligned)
 constexpr size_t al(size_t b) { return (b + 255) / 256 * 256; }
@@ -270,7 +270,9 @@ extern "C" int dem_contact_forces_noalloc(int n, const double *x, const double *
   const double *src[6] = {Yeff, Geff, betaeff, coeffFrict, coeffRollFrict, coeffRestLog};
   for (int k = 0; k < 6; k++)
     for (int q = 0; q < m; q++) tab[k * m + q] = src[k] ? src[k][q] : 0.0;
-  if (cudaMemcpyAsync(base + kOffParams, tab, sizeof(double) * 6 * m, cudaMemcpyHostToDevice, st) != cudaSuccess)
+  derive_type_tables(m, tab);
+  if (cudaMemcpyAsync(base + kOffParams, tab, sizeof(double) * kTypeTables * m, cudaMemcpyHostToDevice, st) !=
+      cudaSuccess)
     return DEM_ERR_CUDA;
   NaArgs a;
   a.n = n;

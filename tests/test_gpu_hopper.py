@@ -36,8 +36,9 @@ def test_gpu_hopper1m_slice_matches_oracle(rolling):
     oracle itself, started from positions one ulp away, differs by ~7 % in
     torques at step 2 and ~1e-5 in forces by step 5 (without rolling: 1e-13
     through step 100).  With CDT the forces after step 1 are therefore held
-    to 10x that sensitivity, measured in the same test; the sets, slots and
-    positions keep their exact/1e-9 bars."""
+    to 10x the spread of three oracle runs started one ulp away (up, down,
+    mixed), measured in the same test; the sets, slots and positions keep
+    their exact/1e-9 bars."""
     import bench
     from gb300dem.api import DemSystem
     from oracle.binding import Oracle
@@ -48,26 +49,44 @@ def test_gpu_hopper1m_slice_matches_oracle(rolling):
         case = dict(case, rolling_model=0, meshes=[dict(m, rolling=0) for m in case["meshes"]])
     else:
         assert case["rolling_model"] == 1 and case["meshes"][0]["rolling"] == 1
-    cp = dict(case, atoms={k: v.copy() for k, v in case["atoms"].items()})
-    cp["atoms"]["x"] = np.nextafter(cp["atoms"]["x"], np.inf)
+    # oracle runs from positions one ulp away (up, down, mixed): their
+    # spread is how far the reference's own result is determined
+    rng = np.random.default_rng(5)
+    perturbed = []
+    for how in ("up", "down", "mixed") if rolling == "cdt" else ():
+        cp = dict(case, atoms={k: v.copy() for k, v in case["atoms"].items()})
+        x0 = cp["atoms"]["x"]
+        if how == "up":
+            cp["atoms"]["x"] = np.nextafter(x0, np.inf)
+        elif how == "down":
+            cp["atoms"]["x"] = np.nextafter(x0, -np.inf)
+        else:
+            cp["atoms"]["x"] = np.where(rng.random(x0.shape) < 0.5, np.nextafter(x0, np.inf),
+                                        np.nextafter(x0, -np.inf))
+        perturbed.append(Oracle(cp))
     box = float(np.max(np.asarray(case["boxhi"]) - np.asarray(case["boxlo"])))
-    g, o, op = DemSystem(case), Oracle(case), Oracle(cp)
-    for x in (g, o, op):
+    g, o = DemSystem(case), Oracle(case)
+    for x in [g, o] + perturbed:
         x.setup()
     done = 0
     nmesh = 0
     for st in (0, 1, 2, 5, 10, 50, 100):
         g.step(st - done)
-        o.run(st - done)
-        op.run(st - done)
+        for x in [o] + perturbed:
+            x.run(st - done)
         done = st
-        a, b, bp = sort_by_tag(g.atoms()), sort_by_tag(o.atoms()), sort_by_tag(op.atoms())
+        a, b = sort_by_tag(g.atoms()), sort_by_tag(o.atoms())
+        bps = [sort_by_tag(x.atoms()) for x in perturbed]
         assert np.array_equal(a["tag"], b["tag"])
         for k in ("f", "torque"):
             if rolling == "off":
                 tol = FORCE_RTOL if st <= 10 else 1e-9
+            elif st <= 1:
+                tol = FORCE_RTOL
             else:
-                tol = FORCE_RTOL if st <= 1 else max(FORCE_RTOL, 10 * max_rel(bp[k], b[k]))
+                runs = [b] + bps
+                spread = max(max_rel(u[k], w[k]) for q, u in enumerate(runs) for w in runs[q + 1:])
+                tol = max(FORCE_RTOL, 10 * spread)
             assert max_rel(a[k], b[k]) < tol, (st, k, max_rel(a[k], b[k]), tol)
         assert max_rel(a["x"], b["x"], scale=box) < TRAJ_RTOL, st
         if rolling == "off":
