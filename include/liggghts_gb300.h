@@ -168,10 +168,16 @@ int dem_add_plane_per_type(dem_handle *h, int axis, const double *pos_by_type, i
  * type k+1 (each system one material, the type-pair tables' diagonal), its
  * walls are per-type planes (dem_add_plane_per_type).  Every system keeps
  * its own coordinates; its neighbour cells form their own block, so no pair
- * crosses systems.  All systems advance together in one step loop; a
- * neighbour rebuild, decided over all atoms, rebuilds every system.  After
- * dem_set_pair_params (ntypes == nsys), before dem_upload_atoms; no meshes. */
+ * crosses systems.  All systems advance together in one step loop; each
+ * system takes its own neighbour decision (Neighbor::decide with the
+ * every/delay/check settings, src/neighbor.cpp:1362-1378), as it would
+ * running alone: a system that does not rebuild keeps its atom order, list
+ * and histories while others rebuild.  After dem_set_pair_params
+ * (ntypes == nsys), before dem_upload_atoms; no meshes. */
 int dem_set_ensemble(dem_handle *h, int nsys);
+/* Neighbour list builds of each ensemble system (Neighbor::ncalls of that
+ * system run alone, including the setup build): counts[nsys]. */
+int dem_ensemble_rebuilds(dem_handle *h, int *counts);
 
 /* Launch shape and neighbour-cell size, set before dem_upload_atoms:
  * grid-stride kernels use at most blocks_per_sm blocks per SM (default 8);

@@ -768,7 +768,27 @@ int dem_set_ensemble(dem_handle *h, int nsys) {
   if (h->have_atoms) return fail(h, DEM_ERR_BAD_ARG, "declare the ensemble before uploading atoms");
   if (h->s.nmeshes > 0) return fail(h, DEM_ERR_UNSUPPORTED, "mesh walls are not supported in ensembles");
   h->ens_nsys = nsys;
+  // per-system neighbour decisions: moved, rebuild, ago, build count [nsys]
+  // and the systems' first atoms [nsys+1]
+  int *buf = nullptr;
+  CUDA_TRY(h, dalloc(h->allocs_misc, &buf, (size_t)5 * nsys + 1));
+  CUDA_TRY(h, cudaMemsetAsync(buf, 0, ((size_t)5 * nsys + 1) * sizeof(int), h->st));
+  Sys &s = h->s;
+  s.nsys = nsys;
+  s.sys_moved = buf;
+  s.sys_reb = buf + nsys;
+  s.sys_ago = buf + 2 * nsys;
+  s.sys_nreb = buf + 3 * nsys;
+  s.sys_start = buf + 4 * nsys;
   h->sys_gen++;
+  return DEM_OK;
+}
+
+int dem_ensemble_rebuilds(dem_handle *h, int *counts) {
+  if (!h || !counts || h->ens_nsys < 1) return DEM_ERR_BAD_ARG;
+  CUDA_TRY(h, cudaMemcpyAsync(counts, h->s.sys_nreb, (size_t)h->ens_nsys * sizeof(int), cudaMemcpyDeviceToHost,
+                              h->st));
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));
   return DEM_OK;
 }
 

@@ -203,6 +203,14 @@ struct Sys {
   // batched ensemble: independent systems, system k = atom type k+1, each
   // with its own block of ens_ncell neighbour cells (0: one system)
   int ens_ncell;
+  // per-system neighbour decisions of an ensemble (system k alone runs its
+  // own Neighbor::decide): nsys systems, [nsys] each, sys_start [nsys+1]
+  int nsys;          // 0: one system
+  int *sys_moved;    // an atom of system k moved more than skin/2 (this step)
+  int *sys_reb;      // system k rebuilds at this step
+  int *sys_ago;      // steps since system k's last build
+  int *sys_start;    // first atom of system k (atoms are grouped by system after every build)
+  int *sys_nreb;     // builds of system k
   double csz[3];
   double boxlo[3], boxhi[3], prd[3];
   int periodic[3];

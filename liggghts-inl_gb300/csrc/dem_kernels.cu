@@ -82,10 +82,25 @@ __device__ __forceinline__ int cell_coord(const Sys &s, double x, int d) {
 // rebuild at this step (FixMesh::next_reneighbor) comes before the
 // ago/every/delay/check logic.  A moving mesh that travelled more than skin/2
 // on a step without rebuild forces one at the next step.
+// An ensemble decides per system, as each system running alone would; the
+// rebuild stage runs when any system rebuilds, and the others keep their
+// atom order, list and histories.
 __device__ __forceinline__ int decide_rebuild(const Sys &s, Ctrl *c) {
   int reb = 0;
   if (c->force_rebuild) {
     reb = 1;
+    for (int k = 0; k < s.nsys; k++) {
+      s.sys_reb[k] = 1;
+      s.sys_moved[k] = 0;
+    }
+  } else if (s.nsys) {
+    for (int k = 0; k < s.nsys; k++) {
+      const int ago = ++s.sys_ago[k];
+      const int r = (ago >= s.neigh_delay && ago % s.neigh_every == 0) ? (s.neigh_check ? s.sys_moved[k] : 1) : 0;
+      s.sys_reb[k] = r;
+      s.sys_moved[k] = 0;
+      reb |= r;
+    }
   } else {
     c->ago++;
     if (c->ago >= s.neigh_delay && c->ago % s.neigh_every == 0) reb = s.neigh_check ? c->moved : 1;
@@ -96,6 +111,9 @@ __device__ __forceinline__ int decide_rebuild(const Sys &s, Ctrl *c) {
   c->moved = 0;
   return reb;
 }
+
+// this atom's system rebuilds at the current rebuild stage
+__device__ __forceinline__ bool sys_rebuilds(const Sys &s, int type) { return s.nsys == 0 || s.sys_reb[type - 1]; }
 
 __global__ void k_decide(Sys s) {
   Ctrl *c = s.ctrl;
@@ -126,6 +144,10 @@ __global__ void k_set_rebuild(Sys s, int v) {
   if (s.ctrl->halt) return;
   s.ctrl->rebuild = v;
   s.ctrl->moved = 0;
+  for (int k = 0; k < s.nsys; k++) {
+    s.sys_reb[k] = v;
+    s.sys_moved[k] = 0;
+  }
 }
 
 __global__ void k_zero_gated(Sys s, int *a, int n) {
@@ -194,6 +216,12 @@ __global__ void k_cell_count(Sys s) {
   const AtomArrays &A = s.atoms[0];
   const int n = c->n;
   GRID_STRIDE(i, n) {
+    if (!sys_rebuilds(s, A.type[i])) {  // kept in order, in its system's first cell
+      const int cell = (A.type[i] - 1) * s.ens_ncell;
+      s.pcount[i] = cell;
+      atomicAdd(&s.cell_count[cell], 1);
+      continue;
+    }
     double xv[3] = {A.x[i], A.y[i], A.z[i]};
     bool lost = false;
 #pragma unroll
@@ -224,9 +252,12 @@ __global__ void k_cell_scatter(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
   const int n = c->n;
+  const AtomArrays &A = s.atoms[0];
   GRID_STRIDE(i, n) {
     const int cell = s.pcount[i];
-    const int slot = s.cell_start[cell] + atomicAdd(&s.cell_fill[cell], 1);
+    int slot;
+    if (!sys_rebuilds(s, A.type[i])) slot = s.cell_start[cell] + (i - s.sys_start[A.type[i] - 1]);
+    else slot = s.cell_start[cell] + atomicAdd(&s.cell_fill[cell], 1);
     s.order[slot] = i;
   }
 }
@@ -236,6 +267,7 @@ __global__ void k_cell_sort(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
   GRID_STRIDE(cell, s.ncell) {
+    if (s.nsys && !s.sys_reb[cell / s.ens_ncell]) continue;  // already in order
     const int b = s.cell_start[cell], e = s.cell_start[cell + 1];
     for (int k = b + 1; k < e; k++) {
       const int v = s.order[k];
@@ -265,9 +297,14 @@ __global__ void k_permute(Sys s) {
   GRID_STRIDE(i, n) {
     const int o = s.order[i];
     s.perm[i] = o;
+    const bool reb = sys_rebuilds(s, A.type[o]);
     const double x = A.x[o], y = A.y[o], z = A.z[o];
     B.x[i] = x; B.y[i] = y; B.z[i] = z;
-    B.xh[i] = x; B.yh[i] = y; B.zh[i] = z;
+    if (reb) {
+      B.xh[i] = x; B.yh[i] = y; B.zh[i] = z;
+    } else {  // a system that does not rebuild keeps its holds
+      B.xh[i] = A.xh[o]; B.yh[i] = A.yh[o]; B.zh[i] = A.zh[o];
+    }
     B.vx[i] = A.vx[o]; B.vy[i] = A.vy[o]; B.vz[i] = A.vz[o];
     B.wx[i] = A.wx[o]; B.wy[i] = A.wy[o]; B.wz[i] = A.wz[o];
     B.fx[i] = A.fx[o]; B.fy[i] = A.fy[o]; B.fz[i] = A.fz[o];
@@ -294,7 +331,7 @@ __global__ void k_permute(Sys s) {
       const double absdist = (dist > 0.0) ? dist : -dist;
       if (absdist <= dMax) bits |= (uint8_t)(1u << w);
     }
-    B.wbits[i] = bits;
+    B.wbits[i] = reb ? bits : A.wbits[o];
     for (int k = 0; k < s.nmeshes; k++) {  // FixContactHistoryMesh per-atom slots travel too
       const MeshDev &M = s.meshes[k];
       const int ns = M.nslot[0][o];
@@ -326,7 +363,8 @@ __global__ void k_copy_atoms(Sys s) {
     A.type[i] = B.type[i]; A.tag[i] = B.tag[i]; A.lidx[i] = B.lidx[i];
     const float4 xf = make_float4((float)B.x[i], (float)B.y[i], (float)B.z[i], (float)B.r[i]);
     s.xf[i] = xf;
-    s.xhf[i] = xf;  // xhold = x at this build (k_permute)
+    // xhold = x at this build (k_permute), or kept by a system that did not rebuild
+    s.xhf[i] = sys_rebuilds(s, B.type[i]) ? xf : make_float4((float)B.xh[i], (float)B.yh[i], (float)B.zh[i], xf.w);
     for (int w = 0; w < s.nplanes; w++)
       for (int d = 0; d < 3; d++)
         A.whist[(size_t)(w * 3 + d) * s.nmax + i] = B.whist[(size_t)(w * 3 + d) * s.nmax + i];
@@ -672,6 +710,27 @@ __global__ void k_pairs(Sys s) {
       s.pcount[i] = 0;
       continue;
     }
+    if (!sys_rebuilds(s, A.type[i])) {
+      // a system that does not rebuild keeps its entries, in their order,
+      // with partners renumbered by its block's shift (pairs never cross
+      // systems); k_pair_init copies their history from the source entry
+      const int sy = A.type[i] - 1;
+      const int o = s.perm[i];
+      const int eb = L.row[o], ee = L.row[o + 1];
+      if (!FILL) {
+        s.pcount[i] = ee - eb;
+        continue;
+      }
+      const int shift = s.cell_start[sy * s.ens_ncell] - s.sys_start[sy];
+      int out = M.row[i];
+      for (int e = eb; e < ee; e++, out++) {
+        M.i[out] = i;
+        M.j[out] = L.j[e] + shift;
+        M.sh[out] = L.sh[e];
+        M.rev[out] = e;
+      }
+      continue;
+    }
     const double xi = A.x[i], yi = A.y[i], zi = A.z[i];
     const double radi = A.r[i];
     const int ci[3] = {cell_coord(s, xi, 0), cell_coord(s, yi, 1), cell_coord(s, zi, 2)};
@@ -744,6 +803,7 @@ __global__ void k_pairs(Sys s) {
             M.i[p] = i;
             M.j[p] = j;
             M.sh[p] = (uint8_t)code;
+            if (s.nsys) M.rev[p] = -1;  // a fresh entry (source of copied ones: see above)
           }
         }
       }
@@ -770,6 +830,16 @@ __global__ void k_pair_init(Sys s) {
   const int np = c->np_new;
   GRID_STRIDE(p, np) {
     const int i = M.i[p], j = M.j[p], code = M.sh[p];
+    const int src = s.nsys ? M.rev[p] : -1;
+    if (src >= 0) {  // kept entry of a system that does not rebuild: as it was
+      M.flag[p] = L.flag[src];
+      for (int d = 0; d < s.dnum; d++) M.hist[(size_t)d * s.pcap + p] = L.hist[(size_t)d * s.pcap + src];
+      M.reff[p] = L.reff[src];
+      M.c0[p] = L.c0[src];
+      M.c1[p] = L.c1[src];
+      if (code == kNoShift) atomicAdd(&s.rev_count[j], 1);
+      continue;
+    }
     double xj = A.x[j], yj = A.y[j], zj = A.z[j];
     image(s, code, xj, yj, zj);
     const double rsq = rsq_rn(__dadd_rn(A.x[i], -xj), __dadd_rn(A.y[i], -yj), __dadd_rn(A.z[i], -zj));
@@ -886,6 +956,14 @@ __global__ void k_finish_rebuild(Sys s) {
   c->np = c->np_new;
   c->nrebuilds++;
   c->ago = 0;
+  for (int k = 0; k < s.nsys; k++) {
+    if (s.sys_reb[k]) {
+      s.sys_nreb[k]++;
+      s.sys_ago[k] = 0;
+    }
+    s.sys_start[k] = s.cell_start[k * s.ens_ncell];
+  }
+  if (s.nsys) s.sys_start[s.nsys] = s.cell_start[s.ncell];
 }
 
 // ----------------------------------------------------------------------------
@@ -1789,14 +1867,17 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
         const float4 hf = s.xhf[i];
         const float ex = nf.x - hf.x, ey = nf.y - hf.y, ez = nf.z - hf.z;
         const float rf2 = ex * ex + ey * ey + ez * ez;
+        bool mv = false;
         if (rf2 > s.skin_hi2) {
-          moved = true;
+          mv = true;
         } else if (rf2 > s.skin_lo2) {
           const double dx = __dadd_rn(xv[0], -A.xh[i]);
           const double dy = __dadd_rn(xv[1], -A.yh[i]);
           const double dz = __dadd_rn(xv[2], -A.zh[i]);
-          if (rsq_rn(dx, dy, dz) > trigger) moved = true;
+          if (rsq_rn(dx, dy, dz) > trigger) mv = true;
         }
+        if (mv && s.nsys) s.sys_moved[A.type[i] - 1] = 1;  // this atom's system (ensembles)
+        moved |= mv;
         // a non-finite coordinate converts to a non-finite float (so does one
         // beyond the FP32 range, which no granular box reaches)
         if (!(isfinite(nf.x) && isfinite(nf.y) && isfinite(nf.z))) bad = true;

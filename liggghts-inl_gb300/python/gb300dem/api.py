@@ -97,6 +97,7 @@ def load(build=True):
     L.dem_set_tuning.argtypes = [P, I, ctypes.c_double]
     L.dem_set_particle_threads.argtypes = [P, I]
     L.dem_set_ensemble.argtypes = [P, I]
+    L.dem_ensemble_rebuilds.argtypes = [P, P]
     L.dem_upload_atoms.argtypes = [P, I] + [P] * 7
     L.dem_add_mesh.argtypes = [P, I, P, I, I, P, P, P]
     L.dem_mesh_topology.argtypes = [I, P, P, P]

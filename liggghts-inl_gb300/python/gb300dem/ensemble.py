@@ -117,6 +117,13 @@ class Ensemble:
     def stats(self):
         return self.sys.stats()
 
+    def rebuilds(self):
+        """Neighbour list builds of every system (dem_ensemble_rebuilds)."""
+        from .api import _p, load
+        out = np.zeros(self.layout["nsys"], np.int32)
+        self.sys._check(load().dem_ensemble_rebuilds(self.sys.h, _p(out)))
+        return out
+
     def system_atoms(self, k):
         """Atoms of system k with its own tags and coordinates (sorted by tag)."""
         a = self.sys.atoms()

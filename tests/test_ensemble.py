@@ -1,11 +1,11 @@
 """Batched ensemble runner (gb300dem.ensemble): packing on the CPU, and on
 the GPU each packed system against the oracle running that system alone.
 
-The ensemble decides neighbour rebuilds for all systems together; with
-`neigh_modify every 1 check no` (a rebuild every step) the schedule is the
-same as each system's own, so every system must match its standalone run:
-forces within FORCE_RTOL per step while the trajectories agree to rounding,
-pair sets bit-exact."""
+Every system takes its own neighbour decision, as it would alone, so under
+the default `neigh_modify every 1 delay 0 check yes` as well as with a
+rebuild every step (`check no`) every system must match its standalone run:
+its rebuild count, forces within FORCE_RTOL per step while the trajectories
+agree to rounding, pair sets bit-exact and histories within 1e-9."""
 import numpy as np
 import pytest
 
@@ -42,17 +42,21 @@ def test_pack_layout():
 
 
 @pytest.mark.gpu
-def test_ensemble_systems_match_standalone_oracle():
+@pytest.mark.parametrize("neigh", [(1, 0, 0), (1, 0, 1)])
+def test_ensemble_systems_match_standalone_oracle(neigh):
     from gb300dem import ensemble
     from oracle.binding import Oracle
-    sy = _systems()
+    sy = _systems(neigh=neigh)
+    if neigh[2]:  # faster systems rebuild more often than slower ones
+        for k, s in enumerate(sy):
+            s["atoms"]["v"] *= 1.0 + 3.0 * k
     e = ensemble.Ensemble(sy)
     e.setup()
     orcs = [Oracle(s) for s in sy]
     for o in orcs:
         o.setup()
     done = 0
-    for chunk in (1, 4, 5, 20):
+    for chunk in ((1, 4, 5, 20) if not neigh[2] else (1, 4, 5, 20, 70)):
         e.step(chunk)
         for o in orcs:
             o.run(chunk)
@@ -75,7 +79,12 @@ def test_ensemble_systems_match_standalone_oracle():
             missing, extra, flagmis, hm = compare_pairs(gp, op)
             assert not missing and not extra and not flagmis, (k, done)
             assert hm < 1e-9, (k, done, hm)
-    assert e.stats()["nrebuilds"] == done + 1
+        reb = e.rebuilds()
+        assert [int(r) for r in reb] == [o.nrebuilds for o in orcs], (done, reb, [o.nrebuilds for o in orcs])
+    if not neigh[2]:
+        assert e.stats()["nrebuilds"] == done + 1
+    else:  # the systems' schedules differ
+        assert len(set(int(r) for r in e.rebuilds())) > 1
     e.close()
 
 
