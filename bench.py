@@ -114,26 +114,29 @@ def workload(name, scale=1.0, seed=2024):
                     l2="state + neighbour list > L2 (129 MB); no flush needed")
         return case, desc
     if name == "fibres200k":
-        # bonded-fibre compression material: 20,000 fibres x 10 spheres (200k), r 0.5 mm,
-        # cohesion bond/nonlinear with radiusMultiplier 0.5, tsCreate 1 and
-        # createDistance just above 2r, so intra-fibre touching pairs bond at
-        # step 1; dt 1e-7.  A 40 mm cube cannot hold 200k spheres
-        # of r 0.5 mm (1.6x its volume), so the fibres lie in plywood layers
-        # (workloads.fibre_bed_case) in a 40.8 x 40.8 mm periodic column on a
-        # floor, without the moving top plate.
+        # bonded-fibre compression: 20,000 fibres x 10 spheres (200k), r 0.5 mm,
+        # cohesion bond/nonlinear for an elastoplastic bond material (elastic
+        # 1e9 Pa, yield strain 0.01, hardening ratio 0.1; the tables from
+        # workloads.elastoplastic_bond_params), bond radius ratio 0.5,
+        # tsCreate 1 and createDistance just above 2r, so intra-fibre touching
+        # pairs bond at step 1; Hertz between fibres; a two-triangle lid moving
+        # down at 0.05 m/s; dt 1e-7.  A 40 mm cube cannot hold 200k spheres of
+        # r 0.5 mm (1.6x its volume), so the fibres lie in plywood layers
+        # (workloads.fibre_bed_case) in a closed 40.8 x 40.8 mm box.
         r = 0.5e-3
-        bp = workloads.bond_params(
-            2, [1], tsCreate=1.0, radiusMultiplier=0.5, K_fn1=200.0, Ku_fn1=400.0, Kc_fn1=100.0,
-            K_fn2=1e12, Ku_fn2=2e12, Kc_fn2=5e11, K_ft=5e11, K_tn=5e11, Ku_tn=1e12, Kc_tn=2.5e11,
-            K_tt=5e11, Ku_tt=1e12, Kc_tt=2.5e11, damp_fn=0.05, damp_ft=0.05, damp_tn=0.05,
-            damp_tt=0.05, maxDistance=2 * r * 1.0035, maxSigma=6e6, maxTau=6e6, ratioTC=0.5,
-            createDistance=2 * r * 1.002)
+        bp = workloads.elastoplastic_bond_params(
+            2, [1], E=1e9, yield_strain=0.01, hardening=0.1, radius=r, lam=0.5, nu=0.3, tsCreate=1.0,
+            damp_fn=0.05, damp_ft=0.05, damp_tn=0.05, damp_tt=0.05, maxDistance=2 * r * 1.0035,
+            maxSigma=6e6, maxTau=6e6, ratioTC=0.5, createDistance=2 * r * 1.002)
         case = workloads.fibre_bed_case(seed, max(100, int(round(200_000 * scale)) // 10 * 10), radius=r,
-                                        bond=bp, dt=1e-7, skin=2e-4, vmax=0.05)
+                                        bond=bp, dt=1e-7, skin=2e-4, vmax=0.05, plate_vel=(0.0, 0.0, -0.05),
+                                        plate_gap=0.0)
         desc = dict(workload="fibres200k", atoms=int(len(case["atoms"]["tag"])), fibres=case["nfibres"],
                     description="200k bonded fibre spheres: 10-sphere fibres (r 0.5 mm) in plywood "
                                 "layers, Hertz/history between fibres, cohesion bond/nonlinear within "
-                                "(bonds created at step 1), periodic x/y column on a floor, dt 1e-7",
+                                "(elastoplastic bond: 1e9 Pa, yield strain 0.01, hardening 0.1; bonds "
+                                "created at step 1), closed box with a lid pressing down at 0.05 m/s, "
+                                "dt 1e-7",
                     l2="state + neighbour list + 28-value bond histories > L2 (129 MB); no flush needed")
         return case, desc
     raise SystemExit("unknown workload %s" % name)

