@@ -341,7 +341,7 @@ static int alloc_pairs(dem_handle *h, int pcap, int keep_np) {
   Sys &s = h->s;
   std::vector<void *> nl;
   PairArrays np_[2];
-  double *rF = nullptr, *rTi = nullptr, *rTj = nullptr;
+  double *rres = nullptr;
   uint8_t *act = nullptr;
   auto carve = [&](Arena &ar) {
     for (int b = 0; b < 2; b++) {
@@ -357,9 +357,7 @@ static int alloc_pairs(dem_handle *h, int pcap, int keep_np) {
       ar.take(&P.c1, pcap);
       ar.take(&P.rev, pcap);
     }
-    ar.take(&rF, (size_t)3 * pcap);
-    ar.take(&rTi, (size_t)3 * pcap);
-    ar.take(&rTj, (size_t)3 * pcap);
+    ar.take(&rres, (size_t)kResStride * pcap);
     ar.take(&act, pcap);
   };
   Arena ar;
@@ -386,9 +384,7 @@ static int alloc_pairs(dem_handle *h, int pcap, int keep_np) {
   h->allocs_pairs = nl;
   s.pairs[0] = np_[0];
   s.pairs[1] = np_[1];
-  s.resF = rF;
-  s.resTi = rTi;
-  s.resTj = rTj;
+  s.res = rres;
   s.active = act;
   s.pcap = pcap;
   h->sys_gen++;

@@ -177,6 +177,8 @@ struct MeshDev {
   double *slot_hist[2];             // [(s*3+d)*nmax + a]
 };
 
+constexpr int kResStride = 12;  // doubles per pair-result record
+
 struct Sys {
   AtomArrays atoms[2];
   PairArrays pairs[2];
@@ -187,7 +189,9 @@ struct Sys {
   int *order;       // slot -> old (before the per-cell sort)
   int *pcount;      // per-atom pair counts [nmax+1]
   int *rev_count, *rev_fill;  // [nmax+1]
-  double *resF, *resTi, *resTj;  // [3*pcap]
+  // pair results, one 96-byte record per list entry (three whole 32-byte
+  // sectors): F[3], Ti[3], Tj[3], 3 doubles of padding; [kResStride*pcap]
+  double *res;
   uint8_t *active;  // [pcap]
   int *scan_tmp;
   float4 *xf;       // FP32 copy (x, y, z, r) of the atoms, refreshed by every drift

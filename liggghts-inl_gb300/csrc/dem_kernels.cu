@@ -984,6 +984,17 @@ constexpr int kPairTile = 256;
 // with three 128-thread blocks, 0.35 ms with four; 64-thread tiles 0.40 ms).
 constexpr int kBandTile = 128;
 
+// the entry's result record: three whole 32-byte sectors in one go
+__device__ __forceinline__ void store_result(const Sys &s, int q, const ContactOut &o) {
+  double2 *r = reinterpret_cast<double2 *>(s.res + (size_t)kResStride * q);
+  r[0] = make_double2(o.F[0], o.F[1]);
+  r[1] = make_double2(o.F[2], o.Ti[0]);
+  r[2] = make_double2(o.Ti[1], o.Ti[2]);
+  r[3] = make_double2(o.Tj[0], o.Tj[1]);
+  r[4] = make_double2(o.Tj[2], 0.0);
+  r[5] = make_double2(0.0, 0.0);
+}
+
 template <int NORMAL, bool ROLL, bool BOND>
 __global__ void __launch_bounds__(kBandTile, 4) k_pair(Sys s, int shearupdate) {
   __shared__ int q_p[kBandTile];
@@ -1129,9 +1140,7 @@ __global__ void __launch_bounds__(kBandTile, 4) k_pair(Sys s, int shearupdate) {
         }
       }
       if (touch || bonded) {
-        s.resF[q] = o.F[0]; s.resF[P + q] = o.F[1]; s.resF[2 * P + q] = o.F[2];
-        s.resTi[q] = o.Ti[0]; s.resTi[P + q] = o.Ti[1]; s.resTi[2 * P + q] = o.Ti[2];
-        s.resTj[q] = o.Tj[0]; s.resTj[P + q] = o.Tj[1]; s.resTj[2 * P + q] = o.Tj[2];
+        store_result(s, q, o);
         s.active[q] = 1;
       }
     }
@@ -1192,9 +1201,7 @@ __device__ __forceinline__ void pair_entry(const Sys &s, int q, int shearupdate)
     L.hist[2 * P + q] = sh3[2];
   }
   L.flag[q] |= (kContactNormal | kContactTangential);
-  s.resF[q] = o.F[0]; s.resF[P + q] = o.F[1]; s.resF[2 * P + q] = o.F[2];
-  s.resTi[q] = o.Ti[0]; s.resTi[P + q] = o.Ti[1]; s.resTi[2 * P + q] = o.Ti[2];
-  s.resTj[q] = o.Tj[0]; s.resTj[P + q] = o.Tj[1]; s.resTj[2 * P + q] = o.Tj[2];
+  store_result(s, q, o);
   s.active[q] = 1;
 }
 
@@ -1761,37 +1768,40 @@ __device__ __forceinline__ void gather_contacts(const Sys &s, const PairArrays &
     for (int t = 0; t < cnt; t++) {
       int p;
       unsigned long long sg;
-      const double *T;
+      int to;  // offset of the torque in the record: Ti (own row) or Tj (partner)
       if (om) {
         p = pb + __ffs(om) - 1;
         om &= om - 1u;
         sg = 0ull;
-        T = s.resTi;
+        to = 3;
       } else {
         p = L.rev[rb + __ffs(rm) - 1];
         rm &= rm - 1u;
         sg = 0x8000000000000000ull;
-        T = s.resTj;
+        to = 6;
       }
-      fx += __longlong_as_double(__double_as_longlong(s.resF[p]) ^ sg);
-      fy += __longlong_as_double(__double_as_longlong(s.resF[P + p]) ^ sg);
-      fz += __longlong_as_double(__double_as_longlong(s.resF[2 * P + p]) ^ sg);
-      tx += T[p];
-      ty += T[P + p];
-      tz += T[2 * P + p];
+      const double *r = s.res + (size_t)kResStride * p;
+      fx += __longlong_as_double(__double_as_longlong(r[0]) ^ sg);
+      fy += __longlong_as_double(__double_as_longlong(r[1]) ^ sg);
+      fz += __longlong_as_double(__double_as_longlong(r[2]) ^ sg);
+      tx += r[to];
+      ty += r[to + 1];
+      tz += r[to + 2];
     }
     return;
   }
   for (int p = pb; p < pe; p++) {  // lists longer than 32 entries
     if (!s.active[p]) continue;
-    fx += s.resF[p]; fy += s.resF[P + p]; fz += s.resF[2 * P + p];
-    tx += s.resTi[p]; ty += s.resTi[P + p]; tz += s.resTi[2 * P + p];
+    const double *r = s.res + (size_t)kResStride * p;
+    fx += r[0]; fy += r[1]; fz += r[2];
+    tx += r[3]; ty += r[4]; tz += r[5];
   }
   for (int k = rb; k < re; k++) {
     const int p = L.rev[k];
     if (!s.active[p]) continue;
-    fx -= s.resF[p]; fy -= s.resF[P + p]; fz -= s.resF[2 * P + p];
-    tx += s.resTj[p]; ty += s.resTj[P + p]; tz += s.resTj[2 * P + p];
+    const double *r = s.res + (size_t)kResStride * p;
+    fx -= r[0]; fy -= r[1]; fz -= r[2];
+    tx += r[6]; ty += r[7]; tz += r[8];
   }
 }
 
@@ -1829,8 +1839,12 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
         fx += A.fmx[i]; fy += A.fmy[i]; fz += A.fmz[i];
         tx += A.tmx[i]; ty += A.tmy[i]; tz += A.tmz[i];
       }
-      A.fx[i] = fx; A.fy[i] = fy; A.fz[i] = fz;
-      A.tx[i] = tx; A.ty[i] = ty; A.tz[i] = tz;
+      // the sums are kept for the download and the next call's first
+      // step; inside a run (FINAL && INITIAL) nothing reads them
+      if (!(FINAL && INITIAL)) {
+        A.fx[i] = fx; A.fy[i] = fy; A.fz[i] = fz;
+        A.tx[i] = tx; A.ty[i] = ty; A.tz[i] = tz;
+      }
     } else {
       fx = A.fx[i]; fy = A.fy[i]; fz = A.fz[i];
       tx = A.tx[i]; ty = A.ty[i]; tz = A.tz[i];
@@ -1839,8 +1853,18 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
       // FixNVESphere half-kicks and drift as fused multiply-adds: one FP64
       // instruction each (the FP64 pipe bounds this kernel on GB300); the
       // single rounding moves positions by at most an ulp from the reference.
+      // The final half-kick of step n and the initial one of step n+1 use
+      // the same force: fused into one FMA with 2*dtfm (2*dtir), exact
+      // scalings, one rounding instead of two.
       const double dtfm = A.dtfm[i], dtir = A.dtir[i];
-      if (FINAL) {
+      if (FINAL && INITIAL) {
+        v[0] = fma(2.0 * dtfm, fx, v[0]);
+        v[1] = fma(2.0 * dtfm, fy, v[1]);
+        v[2] = fma(2.0 * dtfm, fz, v[2]);
+        om[0] = fma(2.0 * dtir, tx, om[0]);
+        om[1] = fma(2.0 * dtir, ty, om[1]);
+        om[2] = fma(2.0 * dtir, tz, om[2]);
+      } else if (FINAL || INITIAL) {
         v[0] = fma(dtfm, fx, v[0]);
         v[1] = fma(dtfm, fy, v[1]);
         v[2] = fma(dtfm, fz, v[2]);
@@ -1849,17 +1873,12 @@ __global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
         om[2] = fma(dtir, tz, om[2]);
       }
       if (INITIAL) {
-        v[0] = fma(dtfm, fx, v[0]);
-        v[1] = fma(dtfm, fy, v[1]);
-        v[2] = fma(dtfm, fz, v[2]);
         xv[0] = fma(dtv, v[0], xv[0]);
         xv[1] = fma(dtv, v[1], xv[1]);
         xv[2] = fma(dtv, v[2], xv[2]);
-        om[0] = fma(dtir, tx, om[0]);
-        om[1] = fma(dtir, ty, om[1]);
-        om[2] = fma(dtir, tz, om[2]);
         A.x[i] = xv[0]; A.y[i] = xv[1]; A.z[i] = xv[2];
-        const float4 nf = make_float4((float)xv[0], (float)xv[1], (float)xv[2], (float)A.r[i]);
+        // the FP32 radius of the copy does not change: no conversion
+        const float4 nf = make_float4((float)xv[0], (float)xv[1], (float)xv[2], s.xf[i].w);
         s.xf[i] = nf;
         // Neighbor::check_distance (src/neighbor.cpp:1426-1466) with an FP32
         // prefilter: only displacements within the rounding band of skin/2
