@@ -84,31 +84,34 @@ __device__ __forceinline__ int cell_coord(const Sys &s, double x, int d) {
 // on a step without rebuild forces one at the next step.
 // An ensemble decides per system, as each system running alone would; the
 // rebuild stage runs when any system rebuilds, and the others keep their
-// atom order, list and histories.
+// atom order, list and histories.  Called by every thread of a single
+// block (one thread per system at a time); the result is the block's.
 __device__ __forceinline__ int decide_rebuild(const Sys &s, Ctrl *c) {
-  int reb = 0;
-  if (c->force_rebuild) {
-    reb = 1;
-    for (int k = 0; k < s.nsys; k++) {
-      s.sys_reb[k] = 1;
-      s.sys_moved[k] = 0;
-    }
-  } else if (s.nsys) {
-    for (int k = 0; k < s.nsys; k++) {
+  const int force = c->force_rebuild;
+  int r_any = 0;
+  for (int k = threadIdx.x; k < s.nsys; k += blockDim.x) {
+    int r = 1;
+    if (!force) {
       const int ago = ++s.sys_ago[k];
-      const int r = (ago >= s.neigh_delay && ago % s.neigh_every == 0) ? (s.neigh_check ? s.sys_moved[k] : 1) : 0;
-      s.sys_reb[k] = r;
-      s.sys_moved[k] = 0;
-      reb |= r;
+      r = (ago >= s.neigh_delay && ago % s.neigh_every == 0) ? (s.neigh_check ? s.sys_moved[k] : 1) : 0;
     }
-  } else {
-    c->ago++;
-    if (c->ago >= s.neigh_delay && c->ago % s.neigh_every == 0) reb = s.neigh_check ? c->moved : 1;
+    s.sys_reb[k] = r;
+    s.sys_moved[k] = 0;
+    r_any |= r;
   }
-  c->force_rebuild = reb ? 0 : c->mesh_moved;
-  c->mesh_moved = 0;
-  c->rebuild = reb;
-  c->moved = 0;
+  int reb = __syncthreads_or(r_any);
+  if (threadIdx.x == 0) {
+    if (force) {
+      reb = 1;
+    } else if (!s.nsys) {
+      c->ago++;
+      if (c->ago >= s.neigh_delay && c->ago % s.neigh_every == 0) reb = s.neigh_check ? c->moved : 1;
+    }
+    c->force_rebuild = reb ? 0 : c->mesh_moved;
+    c->mesh_moved = 0;
+    c->rebuild = reb;
+    c->moved = 0;
+  }
   return reb;
 }
 
@@ -118,7 +121,7 @@ __device__ __forceinline__ bool sys_rebuilds(const Sys &s, int type) { return s.
 __global__ void k_decide(Sys s) {
   Ctrl *c = s.ctrl;
   if (c->halt) return;
-  c->ntimestep++;
+  if (threadIdx.x == 0) c->ntimestep++;
   decide_rebuild(s, c);
 }
 
@@ -127,24 +130,30 @@ __global__ void k_decide(Sys s) {
 __global__ void k_decide_loop(Sys s, cudaGraphConditionalHandle hreb, cudaGraphConditionalHandle hloop) {
   Ctrl *c = s.ctrl;
   if (c->halt) {
-    cudaGraphSetConditional(hreb, 0);
-    cudaGraphSetConditional(hloop, 0);
+    if (threadIdx.x == 0) {
+      cudaGraphSetConditional(hreb, 0);
+      cudaGraphSetConditional(hloop, 0);
+    }
     return;
   }
-  c->ntimestep++;
+  if (threadIdx.x == 0) c->ntimestep++;
   const int reb = decide_rebuild(s, c);
-  c->loop_left--;
-  cudaGraphSetConditional(hreb, reb ? 1u : 0u);
-  cudaGraphSetConditional(hloop, c->loop_left > 0 ? 1u : 0u);
+  if (threadIdx.x == 0) {
+    c->loop_left--;
+    cudaGraphSetConditional(hreb, reb ? 1u : 0u);
+    cudaGraphSetConditional(hloop, c->loop_left > 0 ? 1u : 0u);
+  }
 }
 
 __global__ void k_set_loop(Sys s, int n) { s.ctrl->loop_left = n; }
 
 __global__ void k_set_rebuild(Sys s, int v) {
   if (s.ctrl->halt) return;
-  s.ctrl->rebuild = v;
-  s.ctrl->moved = 0;
-  for (int k = 0; k < s.nsys; k++) {
+  if (threadIdx.x == 0) {
+    s.ctrl->rebuild = v;
+    s.ctrl->moved = 0;
+  }
+  for (int k = threadIdx.x; k < s.nsys; k += blockDim.x) {
     s.sys_reb[k] = v;
     s.sys_moved[k] = 0;
   }
@@ -215,11 +224,13 @@ __global__ void k_cell_count(Sys s) {
   if (gated(c)) return;
   const AtomArrays &A = s.atoms[0];
   const int n = c->n;
+  // a system that does not rebuild keeps its atoms in order in its first
+  // cell: its count is set once, not added per atom
+  GRID_STRIDE(k, s.nsys)
+    if (!s.sys_reb[k]) s.cell_count[k * s.ens_ncell] = s.sys_start[k + 1] - s.sys_start[k];
   GRID_STRIDE(i, n) {
-    if (!sys_rebuilds(s, A.type[i])) {  // kept in order, in its system's first cell
-      const int cell = (A.type[i] - 1) * s.ens_ncell;
-      s.pcount[i] = cell;
-      atomicAdd(&s.cell_count[cell], 1);
+    if (!sys_rebuilds(s, A.type[i])) {
+      s.pcount[i] = (A.type[i] - 1) * s.ens_ncell;
       continue;
     }
     double xv[3] = {A.x[i], A.y[i], A.z[i]};
@@ -951,19 +962,22 @@ __global__ void k_copy_pairs(Sys s) {
 __global__ void k_finish_rebuild(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
-  c->lost += c->lost_step;
-  c->n = c->n_new;
-  c->np = c->np_new;
-  c->nrebuilds++;
-  c->ago = 0;
-  for (int k = 0; k < s.nsys; k++) {
+  for (int k = threadIdx.x; k < s.nsys; k += blockDim.x) {
     if (s.sys_reb[k]) {
       s.sys_nreb[k]++;
       s.sys_ago[k] = 0;
     }
     s.sys_start[k] = s.cell_start[k * s.ens_ncell];
   }
-  if (s.nsys) s.sys_start[s.nsys] = s.cell_start[s.ncell];
+  __syncthreads();  // every thread has read the gate before it changes
+  if (threadIdx.x == 0) {
+    if (s.nsys) s.sys_start[s.nsys] = s.cell_start[s.ncell];
+    c->lost += c->lost_step;
+    c->n = c->n_new;
+    c->np = c->np_new;
+    c->nrebuilds++;
+    c->ago = 0;
+  }
 }
 
 // ----------------------------------------------------------------------------
@@ -2177,6 +2191,9 @@ int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, boo
   return 1;
 }
 
+// one block: one thread per ensemble system (up to 256 at a time)
+static inline int sys_threads(const Sys &s) { return s.nsys > 32 ? 256 : 32; }
+
 int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage) {
   int nl = 0;
   const int B = 256;
@@ -2225,7 +2242,7 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
     k_wall_list<<<gN, B, 0, st>>>(s);
     nl++;
   }
-  k_finish_rebuild<<<1, 1, 0, st>>>(s);
+  k_finish_rebuild<<<1, sys_threads(s), 0, st>>>(s);
   return nl + 4;
 }
 
@@ -2270,7 +2287,7 @@ cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st,
     return fail(e);
   int k = launch_particle(s, lc, kModeGatherFinalInitial, 1, st);
   k += launch_mesh_move(s, lc, st);
-  k_decide_loop<<<1, 1, 0, st>>>(s, hreb, hloop);
+  k_decide_loop<<<1, sys_threads(s), 0, st>>>(s, hreb, hloop);
   k++;
   cudaStreamCaptureStatus cs;
   const cudaGraphNode_t *deps = nullptr;
@@ -2363,11 +2380,11 @@ int launch_set_loop(const Sys &s, int n, cudaStream_t st) {
 }
 
 int launch_decide(const Sys &s, cudaStream_t st) {
-  k_decide<<<1, 1, 0, st>>>(s);
+  k_decide<<<1, sys_threads(s), 0, st>>>(s);
   return 1;
 }
 int launch_set_rebuild(const Sys &s, int v, cudaStream_t st) {
-  k_set_rebuild<<<1, 1, 0, st>>>(s, v);
+  k_set_rebuild<<<1, sys_threads(s), 0, st>>>(s, v);
   return 1;
 }
 

@@ -213,7 +213,8 @@ def test_adjoint_c5_size_matches_oracle_fd():
     """20,000 spheres, a 100-step window with sqrt(N) checkpoints: the
     kinetic-energy gradients with respect to E, restitution, friction and
     eight sampled radii match the oracle's central differences within 1e-6
-    (steps: 1e-6 relative, friction 1e-5 where its difference has converged)."""
+    (steps: 1e-6 relative; friction 1e-5 and radii 3e-6, where those
+    differences have converged)."""
     from gb300dem.adjoint import DemAdjoint
     E, e, mu = 1e7, 0.6, 0.5
     c = _c5_case()
@@ -233,7 +234,7 @@ def test_adjoint_c5_size_matches_oracle_fd():
     r0 = c["atoms"]["radius"]
     gr = g["radius"]
     for i in (0, 1234, 4567, 8000, 11111, 14000, 17777, 19999):
-        h = 1e-6 * r0[i]
+        h = 3e-6 * r0[i]  # where the quotient of the 20,000-term loss is settled (rounding scatter ~6e-7 at 1e-6)
         rp, rm = r0.copy(), r0.copy()
         rp[i] += h
         rm[i] -= h

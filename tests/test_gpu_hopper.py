@@ -39,7 +39,8 @@ def test_gpu_hopper1m_slice_matches_oracle(rolling):
     held to 10x the spread of three oracle runs started one ulp away (up,
     down, mixed), measured in the same test; later, when the rounding of
     every step has been amplified, the comparison rests on the exact pair
-    and mesh sets and slots and on positions within 1e-9 of the box."""
+    and mesh sets and slots, with positions within 1e-9 of the box or 10x
+    the runs' spread."""
     import bench
     from gb300dem.api import DemSystem
     from oracle.binding import Oracle
@@ -91,7 +92,12 @@ def test_gpu_hopper1m_slice_matches_oracle(rolling):
                 spread = max(max_rel(u[k], w[k]) for q, u in enumerate(runs) for w in runs[q + 1:])
                 tol = max(FORCE_RTOL, 10 * spread)
             assert max_rel(a[k], b[k]) < tol, (st, k, max_rel(a[k], b[k]), tol)
-        assert max_rel(a["x"], b["x"], scale=box) < TRAJ_RTOL, st
+        xtol = TRAJ_RTOL
+        if rolling == "cdt" and st > 10:  # the same chaotic growth: within 10x the oracle runs' spread
+            runs = [b] + bps
+            xtol = max(TRAJ_RTOL, 10 * max(max_rel(u["x"], w["x"], scale=box)
+                                           for q, u in enumerate(runs) for w in runs[q + 1:]))
+        assert max_rel(a["x"], b["x"], scale=box) < xtol, (st, max_rel(a["x"], b["x"], scale=box), xtol)
         if rolling == "off":
             assert max_rel(a["v"], b["v"]) < TRAJ_RTOL, st
         pg, po = g.pairs(), o.pairs()
