@@ -83,6 +83,10 @@ typedef struct dem_stats {
                                   through the host's page tables); 0: through device staging copies */
   int mesh_slot_capacity;      /* history slots per atom of the widest mesh (grows on demand, as the
                                   reference's FixContactHistoryMesh pages do) */
+  int ens_inplace_builds;      /* ensembles: builds that rebuilt only the rebuilding systems' atoms and
+                                  list segments, every other system left in place */
+  int ens_relayout_builds;     /* ensembles: builds in place for the atoms whose list was laid out anew
+                                  (a rebuilding system outgrew its segment) */
 } dem_stats;
 
 typedef struct dem_handle dem_handle;

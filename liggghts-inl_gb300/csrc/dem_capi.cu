@@ -265,6 +265,12 @@ static int alloc_atoms(dem_handle *h, int nmax) {
     for (int b = 0; b < 2; b++) {
       ar.take(&s.pairs[b].row, nmax + 1);
       ar.take(&s.pairs[b].rev_start, nmax + 1);
+      if (s.nsys) {  // ensembles: row ends (segmented list)
+        ar.take(&s.pairs[b].rowe, nmax + 1);
+        ar.take(&s.pairs[b].reve, nmax + 1);
+      } else {
+        s.pairs[b].rowe = s.pairs[b].reve = nullptr;
+      }
     }
     ar.take(&s.perm, nmax);
     ar.take(&s.xf, nmax);
@@ -284,6 +290,10 @@ static int alloc_atoms(dem_handle *h, int nmax) {
     PairArrays &P = s.pairs[b];
     CUDA_TRY(h, cudaMemsetAsync(P.row, 0, (nmax + 1) * sizeof(int), h->st));
     CUDA_TRY(h, cudaMemsetAsync(P.rev_start, 0, (nmax + 1) * sizeof(int), h->st));
+    if (P.rowe) {
+      CUDA_TRY(h, cudaMemsetAsync(P.rowe, 0, (nmax + 1) * sizeof(int), h->st));
+      CUDA_TRY(h, cudaMemsetAsync(P.reve, 0, (nmax + 1) * sizeof(int), h->st));
+    }
   }
   CUDA_TRY(h, cudaMemsetAsync(s.wforce, 0, (size_t)3 * std::max(1, s.nplanes + s.nmeshes) * nmax * sizeof(double), h->st));
   for (int k = 0; k < s.nmeshes; k++) {
@@ -765,17 +775,32 @@ int dem_set_ensemble(dem_handle *h, int nsys) {
   if (h->s.nmeshes > 0) return fail(h, DEM_ERR_UNSUPPORTED, "mesh walls are not supported in ensembles");
   h->ens_nsys = nsys;
   // per-system neighbour decisions: moved, rebuild, ago, build count [nsys]
-  // and the systems' first atoms [nsys+1]
+  // and the systems' first atoms [nsys+1]; list segments: start [nsys+1],
+  // used [nsys]; the in-place rebuild's compaction: rlist [nsys], rpre and
+  // cpre [nsys+1]
+  const size_t nbuf = (size_t)10 * nsys + 4;
   int *buf = nullptr;
-  CUDA_TRY(h, dalloc(h->allocs_misc, &buf, (size_t)5 * nsys + 1));
-  CUDA_TRY(h, cudaMemsetAsync(buf, 0, ((size_t)5 * nsys + 1) * sizeof(int), h->st));
+  CUDA_TRY(h, dalloc(h->allocs_misc, &buf, nbuf));
+  CUDA_TRY(h, cudaMemsetAsync(buf, 0, nbuf * sizeof(int), h->st));
   Sys &s = h->s;
   s.nsys = nsys;
   s.sys_moved = buf;
   s.sys_reb = buf + nsys;
   s.sys_ago = buf + 2 * nsys;
   s.sys_nreb = buf + 3 * nsys;
-  s.sys_start = buf + 4 * nsys;
+  s.sys_start = buf + 4 * nsys;            // [nsys+1]
+  s.seg_start = buf + 5 * nsys + 1;        // [nsys+1]
+  s.seg_used = buf + 6 * nsys + 2;         // [nsys]
+  s.rlist = buf + 7 * nsys + 2;            // [nsys]
+  s.rpre = buf + 8 * nsys + 2;             // [nsys+1]
+  s.cpre = buf + 9 * nsys + 3;             // [nsys+1]
+  // LIGGGHTS_GB300_ENS_FULL=1 takes the whole-list path at every rebuild;
+  // LIGGGHTS_GB300_ENS_SLACK sets the segments' unused share in percent
+  // (default 12; 0 makes every growth re-lay the list): both for tests
+  const char *ef = getenv("LIGGGHTS_GB300_ENS_FULL");
+  s.ens_full = (ef && atoi(ef) != 0) ? 1 : 0;
+  const char *es = getenv("LIGGGHTS_GB300_ENS_SLACK");
+  s.ens_slack = es ? std::max(0, std::min(400, atoi(es))) : 12;
   h->sys_gen++;
   return DEM_OK;
 }
@@ -1277,6 +1302,11 @@ int dem_upload_contact_history(dem_handle *h, int ne, const int *towner, const i
   }
   CUDA_TRY(h, cudaMemcpyAsync(L.row, row.data(), (n + 1) * sizeof(int), cudaMemcpyHostToDevice, h->st));
   CUDA_TRY(h, cudaMemsetAsync(L.rev_start, 0, (h->s.nmax + 1) * sizeof(int), h->st));
+  if (L.rowe) {  // ensembles: the rows' ends (no segments before the first build)
+    CUDA_TRY(h, cudaMemcpyAsync(L.rowe, row.data() + 1, n * sizeof(int), cudaMemcpyHostToDevice, h->st));
+    CUDA_TRY(h, cudaMemsetAsync(L.reve, 0, (h->s.nmax + 1) * sizeof(int), h->st));
+  }
+  CUDA_TRY(h, cudaStreamSynchronize(h->st));  // the host vectors go out of scope
   return DEM_OK;
 }
 
@@ -1512,7 +1542,9 @@ int dem_npairs(dem_handle *h, int *npairs, int *dnum) {
   if (!h) return DEM_ERR_BAD_ARG;
   int rc = read_ctrl(h);
   if (rc) return rc;
-  if (npairs) *npairs = h->host_ctrl.np;
+  // ensembles: the entries in use (the segments' unused entries are not part
+  // of the list)
+  if (npairs) *npairs = h->s.nsys ? h->host_ctrl.np_live : h->host_ctrl.np;
   if (dnum) *dnum = h->s.dnum;
   return DEM_OK;
 }
@@ -1545,16 +1577,22 @@ int dem_download_contacts(dem_handle *h, int *tag_i, int *tag_j, int *shift, int
       std::swap(pi[p], pj[p]);
     }
   }
+  // output slot of each entry: ensembles skip their segments' unused entries
+  std::vector<int> slot(np);
+  int nout = 0;
+  for (int p = 0; p < np; p++) slot[p] = sh[p] == kHole ? -1 : nout++;
   for (int p = 0; p < np; p++) {
-    if (tag_i) tag_i[p] = tags[pi[p]];
-    if (tag_j) tag_j[p] = tags[pj[p]];
+    const int o = slot[p];
+    if (o < 0) continue;
+    if (tag_i) tag_i[o] = tags[pi[p]];
+    if (tag_j) tag_j[o] = tags[pj[p]];
     if (shift) {
       const int c = sh[p];
-      shift[3 * p] = c % 3 - 1;
-      shift[3 * p + 1] = (c / 3) % 3 - 1;
-      shift[3 * p + 2] = c / 9 - 1;
+      shift[3 * o] = c % 3 - 1;
+      shift[3 * o + 1] = (c / 3) % 3 - 1;
+      shift[3 * o + 2] = c / 9 - 1;
     }
-    if (flag) flag[p] = fl[p];
+    if (flag) flag[o] = fl[p];
   }
   if (hist && np) {
     std::vector<double> hb(np);
@@ -1564,7 +1602,8 @@ int dem_download_contacts(dem_handle *h, int *tag_i, int *tag_j, int *shift, int
       CUDA_TRY(h, cudaMemcpyAsync(hb.data(), L.hist + (size_t)d * h->s.pcap, np * sizeof(double),
                                   cudaMemcpyDeviceToHost, h->st));
       CUDA_TRY(h, cudaStreamSynchronize(h->st));
-      for (int p = 0; p < np; p++) hist[(size_t)p * dnum + r] = (swap[p] && d < kDnumShear) ? -hb[p] : hb[p];
+      for (int p = 0; p < np; p++)
+        if (slot[p] >= 0) hist[(size_t)slot[p] * dnum + r] = (swap[p] && d < kDnumShear) ? -hb[p] : hb[p];
     }
   }
   return DEM_OK;
@@ -1592,13 +1631,15 @@ int dem_get_stats(dem_handle *h, dem_stats *out) {
   const Ctrl &c = h->host_ctrl;
   out->ntimestep = c.ntimestep;
   out->nrebuilds = c.nrebuilds;
-  out->npairs = c.np;
+  out->npairs = h->s.nsys ? c.np_live : c.np;
   out->nlost = c.lost;
   out->natoms = c.n;
   out->device = h->device;
   out->pair_capacity = h->s.pcap;
   out->last_step_ms = h->last_ms;
   out->host_direct = h->host_direct ? 1 : 0;
+  out->ens_inplace_builds = c.ens_inplace;
+  out->ens_relayout_builds = c.ens_relayout;
   out->mesh_slot_capacity = 0;
   for (int k = 0; k < h->s.nmeshes; k++) out->mesh_slot_capacity = std::max(out->mesh_slot_capacity, h->s.meshes[k].ccap);
   return DEM_OK;

@@ -90,7 +90,15 @@ struct PairArrays {
   int *row;                 // [nmax+1] CSR offsets by owner
   int *rev_start;           // [nmax+1] offsets of pairs where the atom is partner
   int *rev;                 // pair ids, ascending per partner
+  // ensembles: per-atom ends of the owner row and of the partner list
+  // [nmax+1] (each system's entries lie in its own segment, followed by
+  // unused entries, so row[i+1] is not the end of a system's last atom)
+  int *rowe, *reve;
 };
+
+// shift code of an unused list entry inside an ensemble system's segment
+// (i = j = -1, flag 0; the pair kernels skip it, no row covers it)
+constexpr int kHole = 255;
 
 struct Ctrl {
   int n;            // atoms
@@ -111,6 +119,15 @@ struct Ctrl {
   int force_rebuild;  // rebuild at the next decide (FixMesh next_reneighbor)
   int nmlist;         // atoms with candidate mesh triangles (Sys::mlist)
   int mesh_need;      // most candidate triangles an atom had beyond its mesh's capacity
+  // ensemble rebuilds (see k_ens_plan): pmode 1 rebuilds only the rebuilding
+  // systems' atoms in place; lmode 1 also keeps every other system's list
+  // segment where it is; nR systems rebuild, with nra atoms and ncr entries
+  // of segment capacity between them
+  int pmode, lmode, nR, nra, ncr;
+  int seg_ok;         // the list is laid out in per-system segments
+  int np_live;        // entries in use (ensembles: np less the unused entries)
+  int ens_inplace;    // ensemble builds in place (atoms and list)
+  int ens_relayout;   // ensemble builds in place for the atoms, list re-laid
 };
 
 // Primitive wall of fix wall/gran (src/primitive_wall_definitions.h): a
@@ -215,6 +232,13 @@ struct Sys {
   int *sys_ago;      // steps since system k's last build
   int *sys_start;    // first atom of system k (atoms are grouped by system after every build)
   int *sys_nreb;     // builds of system k
+  // list segments: system k's entries lie in [seg_start[k], seg_start[k+1]),
+  // the first seg_used[k] in use; a rebuild that keeps the other systems in
+  // place compacts the rebuilding ones into rlist (rpre/cpre: their prefix
+  // sums of atoms and of segment capacity) [nsys+1] each
+  int *seg_start, *seg_used, *rlist, *rpre, *cpre;
+  int ens_full;      // 1: every ensemble rebuild takes the whole-list path
+  int ens_slack;     // unused entries a segment gets, percent of its entries (plus 64; 0: none)
   double csz[3];
   double boxlo[3], boxhi[3], prd[3];
   int periodic[3];

@@ -179,9 +179,15 @@ __device__ __forceinline__ int warp_incl_scan(int x) {
 }
 
 // out[k] = sum(in[0..k-1]) within the block's 4096 items; bsum[block] = total.
+// gate: 0 always runs; 1 only while the system rebuilds; 2 also not in an
+// ensemble rebuild that keeps the other systems in place (Ctrl::pmode)
+__device__ __forceinline__ bool scan_gated(const Ctrl *c, int gate) {
+  return gate && (gated(c) || (gate == 2 && c->pmode));
+}
+
 __global__ void __launch_bounds__(1024) k_scan_blocks(Sys s, const int *__restrict__ in, int *out,
                                                       int len, int *bsum, int gate) {
-  if (gate && gated(s.ctrl)) return;
+  if (scan_gated(s.ctrl, gate)) return;
   __shared__ int wsum[32];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
   const long base = (long)blockIdx.x * 4096 + 4 * t;
@@ -206,7 +212,7 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(Sys s, const int *__restri
 }
 
 __global__ void k_scan_add(Sys s, int *out, int len, const int *__restrict__ bsum, int gate) {
-  if (gate && gated(s.ctrl)) return;
+  if (scan_gated(s.ctrl, gate)) return;
   const int add = bsum[blockIdx.x];
   const long base = (long)blockIdx.x * 4096;
   for (int k = threadIdx.x; k < 4096; k += blockDim.x)
@@ -214,15 +220,377 @@ __global__ void k_scan_add(Sys s, int *out, int len, const int *__restrict__ bsu
 }
 
 // ----------------------------------------------------------------------------
+// ensemble rebuilds that keep the other systems in place
+// ----------------------------------------------------------------------------
+//
+// A rebuild of an ensemble where only some systems rebuild (Ctrl::pmode)
+// runs the rebuild kernels over those systems' atoms, cells and list
+// segments alone, through compact indices: atom t of the rebuilding systems
+// (prefix sums rpre over rlist), cell u (ens_ncell per system), segment
+// entry u (prefix sums cpre of the segments' capacities).  Every other
+// system keeps its atoms, cells, list entries, histories and holds where
+// they are.  The whole-list path runs instead when a rebuilding system loses
+// atoms (the systems behind it would move), and its list layout (Ctrl::lmode
+// 0) when a rebuilding system's entries outgrow its segment.  Both paths
+// give the same atom order, entries and values for every system.
+
+// largest q in [0, n) with pre[q] <= t (pre ascending from 0, pre[n] > t)
+__device__ __forceinline__ int seg_find(const int *pre, int n, int t) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// atom of compact index t (t < nra); systems keep their ranges in pmode
+__device__ __forceinline__ int ens_atom(const Sys &s, const Ctrl *c, int t) {
+  const int q = seg_find(s.rpre, c->nR, t);
+  return s.sys_start[s.rlist[q]] + (t - s.rpre[q]);
+}
+
+// list entry of compact segment index u (u < ncr)
+__device__ __forceinline__ int ens_entry(const Sys &s, const Ctrl *c, int u) {
+  const int q = seg_find(s.cpre, c->nR, u);
+  return s.seg_start[s.rlist[q]] + (u - s.cpre[q]);
+}
+
+// cell of compact index u (u < nR * ens_ncell)
+__device__ __forceinline__ int ens_cell(const Sys &s, int u) {
+  return s.rlist[u / s.ens_ncell] * s.ens_ncell + u % s.ens_ncell;
+}
+
+__device__ __forceinline__ bool ens_partial(const Sys &s, const Ctrl *c) { return s.nsys && c->pmode; }
+__device__ __forceinline__ bool ens_list_partial(const Sys &s, const Ctrl *c) { return s.nsys && c->lmode; }
+
+// exclusive block-wide prefix sum of one int per thread (blockDim.x a
+// multiple of 32); *tot = the block's total
+__device__ int block_excl_scan(int v, int *tot) {
+  __shared__ int ws[32];
+  __shared__ int wt;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int incl = warp_incl_scan(v);
+  if (lane == 31) ws[w] = incl;
+  __syncthreads();
+  if (w == 0) {
+    const int y = warp_incl_scan(lane < nw ? ws[lane] : 0);
+    if (lane < nw) ws[lane] = y;
+    if (lane == 31) wt = y;
+  }
+  __syncthreads();
+  const int ex = incl - v + (w ? ws[w - 1] : 0);
+  *tot = wt;
+  __syncthreads();  // ws and wt are reused by the next call
+  return ex;
+}
+
+// out[i] = base + sum(in[b..i)) for i in [b, e), and out_end[i] = out[i] +
+// in[i] when out_end is set, by one block of 1024 threads in chunks of 4096;
+// returns the range's total (every thread)
+__device__ int block_range_scan(const int *__restrict__ in, int b, int e, int base, int *out, int *out_end) {
+  __shared__ int wsum[32];
+  __shared__ int carry;
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  if (t == 0) carry = base;
+  __syncthreads();
+  for (int c0 = b; c0 < e; c0 += 4096) {
+    const int i0 = c0 + 4 * t;
+    int v[4], tot = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      v[k] = (i0 + k < e) ? in[i0 + k] : 0;
+      tot += v[k];
+    }
+    const int incl = warp_incl_scan(tot);
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    if (w == 0) wsum[lane] = warp_incl_scan(wsum[lane]);
+    __syncthreads();
+    int run = carry + incl - tot + (w ? wsum[w - 1] : 0);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (i0 + k < e) {
+        out[i0 + k] = run;
+        if (out_end) out_end[i0 + k] = run + v[k];
+      }
+      run += v[k];
+    }
+    __syncthreads();  // every thread has read carry and wsum
+    if (t == 1023) carry = run;
+    __syncthreads();
+  }
+  const int total = carry - base;
+  __syncthreads();
+  return total;
+}
+
+// Domain::pbc (src/domain.cpp:550-600) of one atom's position, in place;
+// true when the atom is then outside the box in any dimension, which
+// CommBrick::exchange deletes (src/comm_brick.cpp:784-808)
+__device__ __forceinline__ bool pbc_wrap(const Sys &s, double xv[3]) {
+  bool lost = false;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (s.periodic[d]) {
+      if (xv[d] < s.boxlo[d]) xv[d] = __dadd_rn(xv[d], s.prd[d]);
+      if (xv[d] >= s.boxhi[d]) {
+        xv[d] = __dadd_rn(xv[d], -s.prd[d]);
+        if (xv[d] < s.boxlo[d]) xv[d] = s.boxlo[d];
+      }
+    }
+    if (xv[d] < s.boxlo[d] || xv[d] >= s.boxhi[d]) lost = true;
+  }
+  return lost;
+}
+
+// Compacts the rebuilding systems and picks the path: in place (pmode 1)
+// when the list is in segments, some system does not rebuild and the
+// whole-list path is not forced.  One block.
+__global__ void k_ens_plan(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  __shared__ int cr, ca, cc;
+  if (threadIdx.x == 0) cr = ca = cc = 0;
+  __syncthreads();
+  for (int b = 0; b < s.nsys; b += blockDim.x) {
+    const int k = b + threadIdx.x;
+    const int r = k < s.nsys ? s.sys_reb[k] : 0;
+    const int na = r ? s.sys_start[k + 1] - s.sys_start[k] : 0;
+    const int ne = r ? s.seg_start[k + 1] - s.seg_start[k] : 0;
+    int tr, ta, te;
+    const int xr = block_excl_scan(r, &tr);
+    const int xa = block_excl_scan(na, &ta);
+    const int xe = block_excl_scan(ne, &te);
+    if (r) {
+      s.rlist[cr + xr] = k;
+      s.rpre[cr + xr] = ca + xa;
+      s.cpre[cr + xr] = cc + xe;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      cr += tr;
+      ca += ta;
+      cc += te;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    s.rpre[cr] = ca;
+    s.cpre[cr] = cc;
+    c->nR = cr;
+    c->nra = ca;
+    c->ncr = cc;
+    const int part = (c->seg_ok && !s.ens_full && cr < s.nsys) ? 1 : 0;
+    c->pmode = part;
+    c->lmode = part;
+    c->np_new = c->np;
+  }
+}
+
+// in-place path: a rebuilding system that loses an atom moves every system
+// behind it, so the whole-list path takes this rebuild
+__global__ void k_ens_lost(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c) || !c->pmode) return;
+  const AtomArrays &A = s.atoms[0];
+  GRID_STRIDE(t, c->nra) {
+    const int i = ens_atom(s, c, t);
+    double xv[3] = {A.x[i], A.y[i], A.z[i]};
+    if (pbc_wrap(s, xv)) {
+      c->pmode = 0;
+      c->lmode = 0;
+    }
+  }
+}
+
+__global__ void k_ens_zero_cells(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  if (c->pmode) {
+    const int tot = c->nR * s.ens_ncell;
+    GRID_STRIDE(u, tot) {
+      const int cell = ens_cell(s, u);
+      s.cell_count[cell] = 0;
+      s.cell_fill[cell] = 0;
+    }
+  } else {
+    GRID_STRIDE(u, s.ncell + 2) {
+      s.cell_count[u] = 0;
+      s.cell_fill[u] = 0;
+    }
+  }
+}
+
+// the in-place path's block-per-system prefix sums
+enum { kEnsScanCells = 0, kEnsScanRowsPartial = 1, kEnsScanRowsFull = 2, kEnsScanRev = 3 };
+
+// atoms of system k after this rebuild's cell sort: [lo, hi)
+__device__ __forceinline__ void ens_range(const Sys &s, int k, int &lo, int &hi) {
+  lo = s.cell_start[k * s.ens_ncell];
+  hi = s.cell_start[(k + 1) * s.ens_ncell];
+}
+
+__global__ void __launch_bounds__(1024) k_ens_scan(Sys s, int what) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const PairArrays &M = s.pairs[1];
+  bool all = false;
+  if (what == kEnsScanCells || what == kEnsScanRowsPartial) {
+    if (!(what == kEnsScanCells ? c->pmode : c->lmode)) return;
+  } else if (what == kEnsScanRowsFull) {
+    if (c->lmode) return;
+    all = true;
+  } else {
+    all = !c->lmode;
+  }
+  const int nlist = all ? s.nsys : c->nR;
+  for (int q = blockIdx.x; q < nlist; q += gridDim.x) {
+    const int k = all ? q : s.rlist[q];
+    int lo, hi;
+    if (what == kEnsScanCells) {
+      // the system's cells, from its first atom (its range is unchanged)
+      block_range_scan(s.cell_count, k * s.ens_ncell, (k + 1) * s.ens_ncell, s.sys_start[k], s.cell_start, nullptr);
+      continue;
+    }
+    ens_range(s, k, lo, hi);
+    if (what == kEnsScanRev) {
+      block_range_scan(s.rev_count, lo, hi, s.seg_start[k], M.rev_start, M.reve);
+      continue;
+    }
+    // owner rows: into the system's own segment, or relative (the layout
+    // kernel places the segments) on the whole-list path
+    const int base = what == kEnsScanRowsPartial ? s.seg_start[k] : 0;
+    const int used = block_range_scan(s.pcount, lo, hi, base, M.row, M.rowe);
+    if (threadIdx.x == 0) {
+      s.seg_used[k] = used;
+      if (what == kEnsScanRowsPartial && used > s.seg_start[k + 1] - s.seg_start[k]) c->lmode = 0;
+    }
+  }
+}
+
+// in place for the atoms, whole list for the entries: the systems that do
+// not rebuild keep their atoms where they are (perm = identity) and count
+// their current rows
+__global__ void k_ens_kept(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c) || !c->pmode || c->lmode) return;
+  const AtomArrays &A = s.atoms[0];
+  const PairArrays &L = s.pairs[0];
+  GRID_STRIDE(i, c->n) {
+    if (s.sys_reb[A.type[i] - 1]) continue;
+    s.pcount[i] = L.rowe[i] - L.row[i];
+    s.perm[i] = i;
+  }
+}
+
+// whole-list path: every system gets a segment of its entries plus slack
+// (ens_slack percent and 64 more; none with ens_slack 0), so that later
+// rebuilds of it alone stay in place while it grows.  One block.
+__global__ void k_ens_layout(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c) || c->lmode) return;
+  __shared__ int run;
+  if (threadIdx.x == 0) run = 0;
+  __syncthreads();
+  for (int b = 0; b < s.nsys; b += blockDim.x) {
+    const int k = b + threadIdx.x;
+    int cap = 0;
+    if (k < s.nsys) {
+      const long u = s.seg_used[k];
+      cap = (int)(u + (u * s.ens_slack) / 100 + (s.ens_slack ? 64 : 0));
+    }
+    int tot;
+    const int x = block_excl_scan(cap, &tot);
+    if (k < s.nsys) s.seg_start[k] = run + x;
+    __syncthreads();
+    if (threadIdx.x == 0) run += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    s.seg_start[s.nsys] = run;
+    c->np_new = run;
+  }
+}
+
+// whole-list path: relative rows into the system's segment
+__global__ void k_ens_rows_base(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c) || c->lmode) return;
+  const AtomArrays &A = s.atoms[0];
+  const PairArrays &M = s.pairs[1];
+  GRID_STRIDE(i, c->n_new) {
+    const int b = s.seg_start[A.type[i] - 1];
+    M.row[i] += b;
+    M.rowe[i] += b;
+  }
+}
+
+__global__ void k_ens_zero_rev(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  if (c->lmode) {
+    GRID_STRIDE(t, c->nra) {
+      const int i = ens_atom(s, c, t);
+      s.rev_count[i] = 0;
+      s.rev_fill[i] = 0;
+    }
+  } else {
+    GRID_STRIDE(i, s.nmax + 1) {
+      s.rev_count[i] = 0;
+      s.rev_fill[i] = 0;
+    }
+  }
+}
+
+// unused entries at the end of each (rebuilt) segment
+__global__ void k_ens_holes(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const PairArrays &M = s.pairs[1];
+  const bool part = c->lmode;
+  const int nlist = part ? c->nR : s.nsys;
+  for (int q = blockIdx.x; q < nlist; q += gridDim.x) {
+    const int k = part ? s.rlist[q] : q;
+    for (int p = s.seg_start[k] + s.seg_used[k] + threadIdx.x; p < s.seg_start[k + 1]; p += blockDim.x) {
+      M.i[p] = -1;
+      M.j[p] = -1;
+      M.sh[p] = (uint8_t)kHole;
+      M.flag[p] = 0;
+    }
+  }
+}
+
+// ----------------------------------------------------------------------------
 // rebuild: pbc wrap, cell sort, permutation
 // ----------------------------------------------------------------------------
 
-// Domain::pbc (src/domain.cpp:550-600) then CommBrick::exchange deletion of
-// atoms outside the box in any dimension (src/comm_brick.cpp:784-808).
+// Domain::pbc then CommBrick::exchange deletion of atoms outside the box
+// (pbc_wrap), and the atoms' neighbour cells.
+__device__ __forceinline__ void cell_count_atom(const Sys &s, const AtomArrays &A, int i) {
+  double xv[3] = {A.x[i], A.y[i], A.z[i]};
+  const bool lost = pbc_wrap(s, xv);
+  A.x[i] = xv[0];
+  A.y[i] = xv[1];
+  A.z[i] = xv[2];
+  int cell = s.ncell;
+  if (!lost) {
+    const int cx = cell_coord(s, xv[0], 0), cy = cell_coord(s, xv[1], 1), cz = cell_coord(s, xv[2], 2);
+    cell = cx + s.nc[0] * (cy + s.nc[1] * cz) + (s.ens_ncell ? (A.type[i] - 1) * s.ens_ncell : 0);
+  }
+  s.pcount[i] = cell;  // reused as per-atom cell id until the pair count
+  atomicAdd(&s.cell_count[cell], 1);
+}
+
 __global__ void k_cell_count(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
   const AtomArrays &A = s.atoms[0];
+  if (ens_partial(s, c)) {
+    GRID_STRIDE(t, c->nra) cell_count_atom(s, A, ens_atom(s, c, t));
+    return;
+  }
   const int n = c->n;
   // a system that does not rebuild keeps its atoms in order in its first
   // cell: its count is set once, not added per atom
@@ -233,37 +601,23 @@ __global__ void k_cell_count(Sys s) {
       s.pcount[i] = (A.type[i] - 1) * s.ens_ncell;
       continue;
     }
-    double xv[3] = {A.x[i], A.y[i], A.z[i]};
-    bool lost = false;
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      if (s.periodic[d]) {
-        if (xv[d] < s.boxlo[d]) xv[d] = __dadd_rn(xv[d], s.prd[d]);
-        if (xv[d] >= s.boxhi[d]) {
-          xv[d] = __dadd_rn(xv[d], -s.prd[d]);
-          if (xv[d] < s.boxlo[d]) xv[d] = s.boxlo[d];
-        }
-      }
-      if (xv[d] < s.boxlo[d] || xv[d] >= s.boxhi[d]) lost = true;
-    }
-    A.x[i] = xv[0];
-    A.y[i] = xv[1];
-    A.z[i] = xv[2];
-    int cell = s.ncell;
-    if (!lost) {
-      const int cx = cell_coord(s, xv[0], 0), cy = cell_coord(s, xv[1], 1), cz = cell_coord(s, xv[2], 2);
-      cell = cx + s.nc[0] * (cy + s.nc[1] * cz) + (s.ens_ncell ? (A.type[i] - 1) * s.ens_ncell : 0);
-    }
-    s.pcount[i] = cell;  // reused as per-atom cell id until the pair count
-    atomicAdd(&s.cell_count[cell], 1);
+    cell_count_atom(s, A, i);
   }
 }
 
 __global__ void k_cell_scatter(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
-  const int n = c->n;
   const AtomArrays &A = s.atoms[0];
+  if (ens_partial(s, c)) {
+    GRID_STRIDE(t, c->nra) {
+      const int i = ens_atom(s, c, t);
+      const int cell = s.pcount[i];
+      s.order[s.cell_start[cell] + atomicAdd(&s.cell_fill[cell], 1)] = i;
+    }
+    return;
+  }
+  const int n = c->n;
   GRID_STRIDE(i, n) {
     const int cell = s.pcount[i];
     int slot;
@@ -274,22 +628,33 @@ __global__ void k_cell_scatter(Sys s) {
 }
 
 // canonical order inside every cell: ascending previous index
+__device__ __forceinline__ void cell_sort_one(const Sys &s, int cell) {
+  const int b = s.cell_start[cell], e = s.cell_start[cell + 1];
+  for (int k = b + 1; k < e; k++) {
+    const int v = s.order[k];
+    int m = k - 1;
+    while (m >= b && s.order[m] > v) {
+      s.order[m + 1] = s.order[m];
+      m--;
+    }
+    s.order[m + 1] = v;
+  }
+}
+
 __global__ void k_cell_sort(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
-  GRID_STRIDE(cell, s.ncell) {
-    if (s.nsys && !s.sys_reb[cell / s.ens_ncell]) continue;  // already in order
-    const int b = s.cell_start[cell], e = s.cell_start[cell + 1];
-    for (int k = b + 1; k < e; k++) {
-      const int v = s.order[k];
-      int m = k - 1;
-      while (m >= b && s.order[m] > v) {
-        s.order[m + 1] = s.order[m];
-        m--;
-      }
-      s.order[m + 1] = v;
+  if (ens_partial(s, c)) {
+    const int tot = c->nR * s.ens_ncell;
+    GRID_STRIDE(u, tot) cell_sort_one(s, ens_cell(s, u));
+  } else {
+    GRID_STRIDE(cell, s.ncell) {
+      if (s.nsys && !s.sys_reb[cell / s.ens_ncell]) continue;  // already in order
+      cell_sort_one(s, cell);
     }
   }
+  // (in place, cell_start[ncell] is the atom count of the last whole build
+  // and no atom is lost)
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     c->n_new = s.cell_start[s.ncell];
     c->nmlist = 0;
@@ -299,13 +664,8 @@ __global__ void k_cell_sort(Sys s) {
 
 // gather atoms into the new order (buffer 1), xhold = x, primitive-wall
 // neighbour lists (PrimitiveWall::buildNeighList, src/primitive_wall.h:129-138)
-__global__ void k_permute(Sys s) {
-  Ctrl *c = s.ctrl;
-  if (gated(c)) return;
-  const AtomArrays &A = s.atoms[0];
-  const AtomArrays &B = s.atoms[1];
-  const int n = c->n_new;
-  GRID_STRIDE(i, n) {
+__device__ __forceinline__ void permute_atom(const Sys &s, const AtomArrays &A, const AtomArrays &B, int i) {
+  {
     const int o = s.order[i];
     s.perm[i] = o;
     const bool reb = sys_rebuilds(s, A.type[o]);
@@ -357,13 +717,21 @@ __global__ void k_permute(Sys s) {
   }
 }
 
-__global__ void k_copy_atoms(Sys s) {
+__global__ void k_permute(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
   const AtomArrays &A = s.atoms[0];
   const AtomArrays &B = s.atoms[1];
+  if (ens_partial(s, c)) {
+    GRID_STRIDE(t, c->nra) permute_atom(s, A, B, ens_atom(s, c, t));
+    return;
+  }
   const int n = c->n_new;
-  GRID_STRIDE(i, n) {
+  GRID_STRIDE(i, n) permute_atom(s, A, B, i);
+}
+
+__device__ __forceinline__ void copy_atom(const Sys &s, const AtomArrays &A, const AtomArrays &B, int i) {
+  {
     A.x[i] = B.x[i]; A.y[i] = B.y[i]; A.z[i] = B.z[i];
     A.xh[i] = B.xh[i]; A.yh[i] = B.yh[i]; A.zh[i] = B.zh[i];
     A.vx[i] = B.vx[i]; A.vy[i] = B.vy[i]; A.vz[i] = B.vz[i];
@@ -392,6 +760,19 @@ __global__ void k_copy_atoms(Sys s) {
       }
     }
   }
+}
+
+__global__ void k_copy_atoms(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const AtomArrays &A = s.atoms[0];
+  const AtomArrays &B = s.atoms[1];
+  if (ens_partial(s, c)) {
+    GRID_STRIDE(t, c->nra) copy_atom(s, A, B, ens_atom(s, c, t));
+    return;
+  }
+  const int n = c->n_new;
+  GRID_STRIDE(i, n) copy_atom(s, A, B, i);
 }
 
 // ----------------------------------------------------------------------------
@@ -648,15 +1029,23 @@ __global__ void k_mesh_cand(Sys s, int k) {
   }
 }
 
+// end of atom i's owner row and of its partner list
+__device__ __forceinline__ int row_end(const Sys &s, const PairArrays &L, int i) {
+  return s.nsys ? L.rowe[i] : L.row[i + 1];
+}
+__device__ __forceinline__ int rev_end(const Sys &s, const PairArrays &L, int i) {
+  return s.nsys ? L.reve[i] : L.rev_start[i + 1];
+}
+
 // Entry of the old list for the atom pair (owner o, partner q) in old
 // indices: o's own row first, then the entries where o was the partner
 // (flip = true).  Only flagged entries carry history (pre_exchange keeps
 // those).  Returns -1 when none.
-__device__ __forceinline__ int find_old(const PairArrays &L, int o, int q, bool &flip) {
+__device__ __forceinline__ int find_old(const Sys &s, const PairArrays &L, int o, int q, bool &flip) {
   flip = false;
-  for (int k = L.row[o]; k < L.row[o + 1]; k++)
+  for (int k = L.row[o]; k < row_end(s, L, o); k++)
     if (L.j[k] == q && L.flag[k] != 0) return k;
-  for (int k = L.rev_start[o]; k < L.rev_start[o + 1]; k++) {
+  for (int k = L.rev_start[o]; k < rev_end(s, L, o); k++) {
     const int e = L.rev[k];
     if (L.i[e] == q && L.flag[e] != 0) {
       flip = true;
@@ -708,29 +1097,19 @@ __global__ void __launch_bounds__(256) k_wall_list(Sys s) {
 // ----------------------------------------------------------------------------
 
 template <bool FILL>
-__global__ void k_pairs(Sys s) {
-  Ctrl *c = s.ctrl;
-  if (gated(c)) return;
-  const AtomArrays &A = s.atoms[0];
-  const PairArrays &L = s.pairs[0];  // old list (old atom order)
-  const PairArrays &M = s.pairs[1];  // new list
-  const int n = c->n_new;
-  const int total = FILL ? n : s.nmax + 1;
-  GRID_STRIDE(i, total) {
-    if (!FILL && i >= n) {
-      s.pcount[i] = 0;
-      continue;
-    }
+__device__ __forceinline__ void pairs_atom(const Sys &s, const AtomArrays &A, const PairArrays &L,
+                                           const PairArrays &M, int i) {
+  {
     if (!sys_rebuilds(s, A.type[i])) {
       // a system that does not rebuild keeps its entries, in their order,
       // with partners renumbered by its block's shift (pairs never cross
       // systems); k_pair_init copies their history from the source entry
       const int sy = A.type[i] - 1;
       const int o = s.perm[i];
-      const int eb = L.row[o], ee = L.row[o + 1];
+      const int eb = L.row[o], ee = row_end(s, L, o);
       if (!FILL) {
         s.pcount[i] = ee - eb;
-        continue;
+        return;
       }
       const int shift = s.cell_start[sy * s.ens_ncell] - s.sys_start[sy];
       int out = M.row[i];
@@ -740,7 +1119,7 @@ __global__ void k_pairs(Sys s) {
         M.sh[out] = L.sh[e];
         M.rev[out] = e;
       }
-      continue;
+      return;
     }
     const double xi = A.x[i], yi = A.y[i], zi = A.z[i];
     const double radi = A.r[i];
@@ -751,7 +1130,7 @@ __global__ void k_pairs(Sys s) {
     const float hi_f = 1.0f + s.pf_margin, lo_f = 1.0f - s.pf_margin;
     int cnt = 0;
     int out = FILL ? M.row[i] : 0;
-    const int out_end = FILL ? M.row[i + 1] : 0;
+    const int out_end = FILL ? row_end(s, M, i) : 0;
     for (int oz = -1; oz <= 1; oz++) {
       for (int oy = -1; oy <= 1; oy++) {
         for (int ox = -1; ox <= 1; ox++) {
@@ -823,6 +1202,30 @@ __global__ void k_pairs(Sys s) {
   }
 }
 
+template <bool FILL>
+__global__ void k_pairs(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const AtomArrays &A = s.atoms[0];
+  const PairArrays &L = s.pairs[0];  // old list (old atom order)
+  const PairArrays &M = s.pairs[1];  // new list
+  // count: in place for the rebuilding systems' atoms (pmode); fill: also
+  // in place for their segments (lmode)
+  if (FILL ? ens_list_partial(s, c) : ens_partial(s, c)) {
+    GRID_STRIDE(t, c->nra) pairs_atom<FILL>(s, A, L, M, ens_atom(s, c, t));
+    return;
+  }
+  const int n = c->n_new;
+  const int total = FILL ? n : s.nmax + 1;
+  GRID_STRIDE(i, total) {
+    if (!FILL && i >= n) {
+      s.pcount[i] = 0;
+      continue;
+    }
+    pairs_atom<FILL>(s, A, L, M, i);
+  }
+}
+
 // Per new list entry (one thread each, dense): exact distance, history
 // carry-over, per-pair contact constants, reverse-list count.  The carry-over
 // is the reference's (pre_exchange partner lists + the lookup of
@@ -832,15 +1235,12 @@ __global__ void k_pairs(Sys s) {
 // values registered with newtonflag 1 change sign.  The shear is then
 // expressed in the list's own orientation; history is carried only when the
 // pair is within radsum*cdf at the build.
-__global__ void k_pair_init(Sys s) {
-  Ctrl *c = s.ctrl;
-  if (gated(c)) return;
-  const AtomArrays &A = s.atoms[0];
-  const PairArrays &L = s.pairs[0];  // old list (old atom order)
-  const PairArrays &M = s.pairs[1];  // new list
-  const int np = c->np_new;
-  GRID_STRIDE(p, np) {
-    const int i = M.i[p], j = M.j[p], code = M.sh[p];
+__device__ __forceinline__ void pair_init_entry(const Sys &s, const AtomArrays &A, const PairArrays &L,
+                                                const PairArrays &M, int p) {
+  {
+    const int code = M.sh[p];
+    if (code == kHole) return;  // an unused entry of an ensemble segment
+    const int i = M.i[p], j = M.j[p];
     const int src = s.nsys ? M.rev[p] : -1;
     if (src >= 0) {  // kept entry of a system that does not rebuild: as it was
       M.flag[p] = L.flag[src];
@@ -849,7 +1249,7 @@ __global__ void k_pair_init(Sys s) {
       M.c0[p] = L.c0[src];
       M.c1[p] = L.c1[src];
       if (code == kNoShift) atomicAdd(&s.rev_count[j], 1);
-      continue;
+      return;
     }
     double xj = A.x[j], yj = A.y[j], zj = A.z[j];
     image(s, code, xj, yj, zj);
@@ -862,7 +1262,7 @@ __global__ void k_pair_init(Sys s) {
     if (rsq < __dmul_rn(radsum, radsum)) {
       const bool rj = s.bond && code == kNoShift && A.lidx[i] > A.lidx[j];
       bool fl;
-      e = rj ? find_old(L, s.perm[j], s.perm[i], fl) : find_old(L, s.perm[i], s.perm[j], fl);
+      e = rj ? find_old(s, L, s.perm[j], s.perm[i], fl) : find_old(s, L, s.perm[i], s.perm[j], fl);
       ssign = (fl ? -1.0 : 1.0) * (rj ? -1.0 : 1.0);
       quirk = s.bond && e >= 0 && !rj && code != kNoShift && L.sh[e] == kNoShift && A.lidx[i] > A.lidx[j];
     }
@@ -888,11 +1288,26 @@ __global__ void k_pair_init(Sys s) {
   }
 }
 
+__global__ void k_pair_init(Sys s) {
+  Ctrl *c = s.ctrl;
+  if (gated(c)) return;
+  const AtomArrays &A = s.atoms[0];
+  const PairArrays &L = s.pairs[0];  // old list (old atom order)
+  const PairArrays &M = s.pairs[1];  // new list
+  if (ens_list_partial(s, c)) {
+    GRID_STRIDE(u, c->ncr) pair_init_entry(s, A, L, M, ens_entry(s, c, u));
+    return;
+  }
+  const int np = c->np_new;
+  GRID_STRIDE(p, np) pair_init_entry(s, A, L, M, p);
+}
+
 // after the pair-count scan: capacity check; halts on overflow
 __global__ void k_pairs_total(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
-  const int np = s.pairs[1].row[s.nmax];
+  // ensembles: the segments' extent (k_ens_plan or k_ens_layout)
+  const int np = s.nsys ? c->np_new : s.pairs[1].row[s.nmax];
   c->np_new = np;
   if (np > s.pcap) {
     c->status = kStatPairOverflow;
@@ -901,15 +1316,34 @@ __global__ void k_pairs_total(Sys s) {
   }
 }
 
+__device__ __forceinline__ void rev_fill_entry(const Sys &s, const PairArrays &M, int p) {
+  if (M.sh[p] != kNoShift) return;  // image entries and unused ones
+  const int j = M.j[p];
+  M.rev[M.rev_start[j] + atomicAdd(&s.rev_fill[j], 1)] = p;
+}
+
 __global__ void k_rev_fill(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
   const PairArrays &M = s.pairs[1];
+  if (ens_list_partial(s, c)) {
+    GRID_STRIDE(u, c->ncr) rev_fill_entry(s, M, ens_entry(s, c, u));
+    return;
+  }
   const int np = c->np_new;
-  GRID_STRIDE(p, np) {
-    if (M.sh[p] != kNoShift) continue;
-    const int j = M.j[p];
-    M.rev[M.rev_start[j] + atomicAdd(&s.rev_fill[j], 1)] = p;
+  GRID_STRIDE(p, np) rev_fill_entry(s, M, p);
+}
+
+__device__ __forceinline__ void rev_sort_atom(const Sys &s, const PairArrays &M, int i) {
+  const int b = M.rev_start[i], e = rev_end(s, M, i);
+  for (int k = b + 1; k < e; k++) {
+    const int v = M.rev[k];
+    int m = k - 1;
+    while (m >= b && M.rev[m] > v) {
+      M.rev[m + 1] = M.rev[m];
+      m--;
+    }
+    M.rev[m + 1] = v;
   }
 }
 
@@ -917,18 +1351,32 @@ __global__ void k_rev_sort(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
   const PairArrays &M = s.pairs[1];
+  if (ens_list_partial(s, c)) {
+    GRID_STRIDE(t, c->nra) rev_sort_atom(s, M, ens_atom(s, c, t));
+    return;
+  }
   const int n = c->n_new;
-  GRID_STRIDE(i, n) {
-    const int b = M.rev_start[i], e = M.rev_start[i + 1];
-    for (int k = b + 1; k < e; k++) {
-      const int v = M.rev[k];
-      int m = k - 1;
-      while (m >= b && M.rev[m] > v) {
-        M.rev[m + 1] = M.rev[m];
-        m--;
-      }
-      M.rev[m + 1] = v;
-    }
+  GRID_STRIDE(i, n) rev_sort_atom(s, M, i);
+}
+
+__device__ __forceinline__ void copy_entry(const Sys &s, const PairArrays &L, const PairArrays &M, int p) {
+  L.i[p] = M.i[p];
+  L.j[p] = M.j[p];
+  L.sh[p] = M.sh[p];
+  L.flag[p] = M.flag[p];
+  for (int d = 0; d < s.dnum; d++) L.hist[(size_t)d * s.pcap + p] = M.hist[(size_t)d * s.pcap + p];
+  L.reff[p] = M.reff[p];
+  L.c0[p] = M.c0[p];
+  L.c1[p] = M.c1[p];
+  L.rev[p] = M.rev[p];
+}
+
+__device__ __forceinline__ void copy_rows(const Sys &s, const PairArrays &L, const PairArrays &M, int i) {
+  L.row[i] = M.row[i];
+  L.rev_start[i] = M.rev_start[i];
+  if (s.nsys) {
+    L.rowe[i] = M.rowe[i];
+    L.reve[i] = M.reve[i];
   }
 }
 
@@ -937,44 +1385,49 @@ __global__ void k_copy_pairs(Sys s) {
   if (gated(c)) return;
   const PairArrays &L = s.pairs[0];
   const PairArrays &M = s.pairs[1];
+  if (ens_list_partial(s, c)) {  // the rebuilt segments (with their unused entries) and rows
+    GRID_STRIDE(u, c->ncr) copy_entry(s, L, M, ens_entry(s, c, u));
+    GRID_STRIDE(t, c->nra) copy_rows(s, L, M, ens_atom(s, c, t));
+    return;
+  }
   const int np = c->np_new;
   const int nrow = s.nmax + 1;
   const int tot = np > nrow ? np : nrow;
   GRID_STRIDE(p, tot) {
-    if (p < np) {
-      L.i[p] = M.i[p];
-      L.j[p] = M.j[p];
-      L.sh[p] = M.sh[p];
-      L.flag[p] = M.flag[p];
-      for (int d = 0; d < s.dnum; d++) L.hist[(size_t)d * s.pcap + p] = M.hist[(size_t)d * s.pcap + p];
-      L.reff[p] = M.reff[p];
-      L.c0[p] = M.c0[p];
-      L.c1[p] = M.c1[p];
-      L.rev[p] = M.rev[p];
-    }
-    if (p < nrow) {
-      L.row[p] = M.row[p];
-      L.rev_start[p] = M.rev_start[p];
-    }
+    if (p < np) copy_entry(s, L, M, p);
+    if (p < nrow) copy_rows(s, L, M, p);
   }
 }
 
 __global__ void k_finish_rebuild(Sys s) {
   Ctrl *c = s.ctrl;
   if (gated(c)) return;
+  int live = 0;
   for (int k = threadIdx.x; k < s.nsys; k += blockDim.x) {
     if (s.sys_reb[k]) {
       s.sys_nreb[k]++;
       s.sys_ago[k] = 0;
     }
     s.sys_start[k] = s.cell_start[k * s.ens_ncell];
+    live += s.seg_used[k];
   }
+  int tot = 0;
+  if (s.nsys) block_excl_scan(live, &tot);
   __syncthreads();  // every thread has read the gate before it changes
   if (threadIdx.x == 0) {
-    if (s.nsys) s.sys_start[s.nsys] = s.cell_start[s.ncell];
+    if (s.nsys) {
+      s.sys_start[s.nsys] = s.cell_start[s.ncell];
+      c->seg_ok = 1;
+      c->np_live = tot;
+      if (c->pmode) {
+        if (c->lmode) c->ens_inplace++;
+        else c->ens_relayout++;
+      }
+    }
     c->lost += c->lost_step;
     c->n = c->n_new;
     c->np = c->np_new;
+    if (!s.nsys) c->np_live = c->np_new;
     c->nrebuilds++;
     c->ago = 0;
   }
@@ -1030,9 +1483,10 @@ __global__ void __launch_bounds__(kBandTile, 4) k_pair(Sys s, int shearupdate) {
     const int p = base + threadIdx.x;
     bool queue = false;
     double delx = 0., dely = 0., delz = 0., rsq = 0.;
-    if (p < np) {
+    const int code = p < np ? L.sh[p] : kHole;
+    if (code == kHole && p < np) s.active[p] = 0;  // an unused entry of an ensemble segment
+    if (code != kHole) {
       const int i = L.i[p], j = L.j[p];
-      const int code = L.sh[p];
       double xj = A.x[j], yj = A.y[j], zj = A.z[j];
       image(s, code, xj, yj, zj);
       delx = __dadd_rn(A.x[i], -xj);
@@ -1236,8 +1690,8 @@ __global__ void __launch_bounds__(kPairTile, MINB) k_pair_pf(Sys s, int shearupd
   for (int base = blockIdx.x * kPairTile; base < np; base += gridDim.x * kPairTile) {
     const int p = base + threadIdx.x;
     bool maybe = false;
-    if (p < np) {
-      const int code = L.sh[p];
+    const int code = p < np ? L.sh[p] : kHole;
+    if (code != kHole) {
       const float4 a = s.xf[L.i[p]], b = s.xf[L.j[p]];
       float sx = 0.f, sy = 0.f, sz = 0.f;
       if (code != kNoShift) {
@@ -1248,8 +1702,8 @@ __global__ void __launch_bounds__(kPairTile, MINB) k_pair_pf(Sys s, int shearupd
       const float fx = a.x - (b.x + sx), fy = a.y - (b.y + sy), fz = a.z - (b.z + sz);
       const float rs = a.w + b.w;
       maybe = !(fx * fx + fy * fy + fz * fz > rs * rs * hi_f);
-      if (!maybe) s.active[p] = 0;
     }
+    if (!maybe && p < np) s.active[p] = 0;
     const unsigned m = __ballot_sync(0xffffffffu, maybe);
     if (lane == 0) wcnt[warp] = __popc(m);
     __syncthreads();
@@ -1772,8 +2226,8 @@ __global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate
 // a + (-b) is exactly a - b) and Tj instead of Ti.
 __device__ __forceinline__ void gather_contacts(const Sys &s, const PairArrays &L, size_t P, int i, double &fx,
                                                 double &fy, double &fz, double &tx, double &ty, double &tz) {
-  const int pb = L.row[i], pe = L.row[i + 1];
-  const int rb = L.rev_start[i], re = L.rev_start[i + 1];
+  const int pb = L.row[i], pe = row_end(s, L, i);
+  const int rb = L.rev_start[i], re = rev_end(s, L, i);
   if (pe - pb <= 32 && re - rb <= 32) {
     unsigned om = 0u, rm = 0u;
     for (int k = 0; k < pe - pb; k++) om |= (s.active[pb + k] ? 1u : 0u) << k;
@@ -2178,7 +2632,7 @@ static inline int grid_for(long n, int block, int cap) {
   return (int)g;
 }
 
-int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, bool gate,
+int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, int gate,
                    cudaStream_t st) {
   const int nb = (len + 4095) / 4096;
   k_scan_blocks<<<nb, 1024, 0, st>>>(s, in, out, len, tmp, gate);
@@ -2194,7 +2648,59 @@ int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, boo
 // one block: one thread per ensemble system (up to 256 at a time)
 static inline int sys_threads(const Sys &s) { return s.nsys > 32 ? 256 : 32; }
 
+// Ensemble rebuild: in place for the rebuilding systems where that is
+// possible (see k_ens_plan), else the whole list; the kernels of both paths
+// are launched and each runs the path that Ctrl selects.  Stage 1 resumes
+// after a pair-capacity overflow (whole-list path only).
+static int launch_rebuild_ens(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage) {
+  int nl = 0;
+  const int B = 256;
+  const int gN = grid_for(s.nmax + 1, B, lc.max_grid);
+  const int gC = grid_for(s.ncell + 2, B, lc.max_grid);
+  const int gP = grid_for(s.pcap, B, lc.max_grid);
+  const int gS = std::max(1, std::min(s.nsys, 2 * lc.sms));  // a block per system
+  const int T = sys_threads(s);
+  if (stage <= 0) {
+    k_ens_plan<<<1, T, 0, st>>>(s);
+    k_ens_lost<<<gN, B, 0, st>>>(s);
+    k_ens_zero_cells<<<gC, B, 0, st>>>(s);
+    k_cell_count<<<gN, B, 0, st>>>(s);
+    nl += 4 + scan_exclusive(s, s.cell_count, s.cell_start, s.ncell + 2, s.scan_tmp, 2, st);
+    k_ens_scan<<<gS, 1024, 0, st>>>(s, kEnsScanCells);
+    k_cell_scatter<<<gN, B, 0, st>>>(s);
+    k_cell_sort<<<gC, B, 0, st>>>(s);
+    k_permute<<<gN, B, 0, st>>>(s);
+    k_copy_atoms<<<gN, B, 0, st>>>(s);
+    k_pairs<false><<<gN, B, 0, st>>>(s);
+    k_ens_scan<<<gS, 1024, 0, st>>>(s, kEnsScanRowsPartial);
+    k_ens_kept<<<gN, B, 0, st>>>(s);
+    k_ens_scan<<<gS, 1024, 0, st>>>(s, kEnsScanRowsFull);
+    k_ens_layout<<<1, T, 0, st>>>(s);
+    k_ens_rows_base<<<gN, B, 0, st>>>(s);
+    k_pairs_total<<<1, 1, 0, st>>>(s);
+    nl += 13;
+  }
+  if (stage <= 1) {
+    k_ens_zero_rev<<<gN, B, 0, st>>>(s);
+    k_ens_holes<<<gS, B, 0, st>>>(s);
+    k_pairs<true><<<gN, B, 0, st>>>(s);
+    k_pair_init<<<gP, B, 0, st>>>(s);
+    k_ens_scan<<<gS, 1024, 0, st>>>(s, kEnsScanRev);
+    k_rev_fill<<<gP, B, 0, st>>>(s);
+    k_rev_sort<<<gN, B, 0, st>>>(s);
+    k_copy_pairs<<<grid_for((long)s.pcap > s.nmax + 1 ? s.pcap : s.nmax + 1, B, lc.max_grid), B, 0, st>>>(s);
+    nl += 8;
+  }
+  if (s.nplanes > 0) {
+    k_wall_list<<<gN, B, 0, st>>>(s);
+    nl++;
+  }
+  k_finish_rebuild<<<1, T, 0, st>>>(s);
+  return nl + 1;
+}
+
 int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage) {
+  if (s.nsys) return launch_rebuild_ens(s, lc, st, stage);
   int nl = 0;
   const int B = 256;
   const int gN = grid_for(s.nmax + 1, B, lc.max_grid);

@@ -19,8 +19,6 @@ enum {
   kModeGatherFinalInitial = 3,  // sum forces + final(n) + initial(n+1) (steady state)
 };
 
-// exclusive prefix sum of len ints (len <= 4096*4096 - 1); tmp holds
-// (len+4095)/4096 + 1 ints; gate: skip unless the system rebuilds
 struct InsertStage {  // new atoms, device arrays: x, v, w [3k], the rest [k]
   const double *x, *v, *w, *r, *m, *dtfm, *dtir;
   const int *type, *tag;
@@ -57,7 +55,10 @@ int launch_download_atoms(const Sys &s, const AtomsOut &out, int n, cudaStream_t
 int launch_insert_commit(const Sys &s, int k, cudaStream_t st);
 int launch_diagnostics(const Sys &s, const LaunchCfg &lc, const double lo[3], const double hi[3], double *part_atoms,
                        double *part_walls, unsigned long long *contacts, int nblocks, cudaStream_t st);
-int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, bool gate,
+// exclusive prefix sum of len ints (len <= 4096*4096 - 1); tmp holds
+// (len+4095)/4096 + 1 ints; gate 0: always; 1: only while the system
+// rebuilds; 2: not in an ensemble rebuild that keeps other systems in place
+int scan_exclusive(const Sys &s, const int *in, int *out, int len, int *tmp, int gate,
                    cudaStream_t st);
 int launch_decide(const Sys &s, cudaStream_t st);
 int launch_set_rebuild(const Sys &s, int v, cudaStream_t st);

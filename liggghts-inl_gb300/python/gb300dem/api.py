@@ -56,7 +56,8 @@ class DemStats(ctypes.Structure):
                 ("npairs", ctypes.c_longlong), ("nlost", ctypes.c_longlong),
                 ("natoms", ctypes.c_longlong), ("device", ctypes.c_int),
                 ("pair_capacity", ctypes.c_int), ("last_step_ms", ctypes.c_double),
-                ("host_direct", ctypes.c_int), ("mesh_slot_capacity", ctypes.c_int)]
+                ("host_direct", ctypes.c_int), ("mesh_slot_capacity", ctypes.c_int),
+                ("ens_inplace_builds", ctypes.c_int), ("ens_relayout_builds", ctypes.c_int)]
 
 
 class DemKernelTimes(ctypes.Structure):

@@ -106,3 +106,67 @@ def test_ensemble_launch_shapes_give_identical_results():
         for a, b in zip(run, out[0]):
             for key in ("x", "v", "omega", "f", "torque"):
                 assert np.array_equal(a[key], b[key]), key
+
+
+def _run_modes(sy, monkeypatch, chunks):
+    """The same ensemble under three rebuild settings: the whole-list path
+    at every build (LIGGGHTS_GB300_ENS_FULL), the default (in place where
+    possible), and segments without slack (LIGGGHTS_GB300_ENS_SLACK=0: a
+    rebuilding system that gains one entry re-lays the list)."""
+    from gb300dem import ensemble
+    runs = {}
+    for name, env in (("full", {"LIGGGHTS_GB300_ENS_FULL": "1"}), ("inplace", {}),
+                      ("noslack", {"LIGGGHTS_GB300_ENS_SLACK": "0"})):
+        for key in ("LIGGGHTS_GB300_ENS_FULL", "LIGGGHTS_GB300_ENS_SLACK"):
+            monkeypatch.delenv(key, raising=False)
+        for key, v in env.items():
+            monkeypatch.setenv(key, v)
+        e = ensemble.Ensemble(sy)
+        for key in env:
+            monkeypatch.delenv(key, raising=False)
+        e.setup()
+        out = []
+        for chunk in chunks:
+            e.step(chunk)
+            out.append(([e.system_atoms(k) for k in range(len(sy))], e.sys.pairs(), e.rebuilds().copy(),
+                        e.stats()))
+        e.close()
+        runs[name] = out
+    return runs
+
+
+@pytest.mark.gpu
+def test_ensemble_in_place_rebuilds_match_whole_list_rebuilds(monkeypatch):
+    """A build where only some systems rebuild runs over those systems'
+    atoms, cells and list segments alone; the others stay where they are.
+    That must change no bit: atoms, forces, pair sets, histories and the
+    per-system build counts equal those of the whole-list path at every
+    build, with the segments re-laid out (no slack) or not, and through a
+    build at which a rebuilding system loses an atom (the whole-list path
+    takes that one: the systems behind it move)."""
+    sy = _systems(n=6, neigh=(1, 0, 1))
+    for k, s in enumerate(sy):  # fast enough that new pairs form and segments overflow
+        s["atoms"]["v"] *= 4.0 * (1.0 + 3.0 * k)
+    # an atom of system 3 leaves through the open top of its box
+    zhi = sy[3]["boxhi"][2]
+    sy[3]["atoms"]["x"][0] = (sy[3]["atoms"]["x"][0, 0], sy[3]["atoms"]["x"][0, 1], zhi - 1e-4)
+    sy[3]["atoms"]["v"][0] = (0.0, 0.0, 20.0)
+    runs = _run_modes(sy, monkeypatch, (7, 30, 63))
+    ref = runs["full"]
+    for name in ("inplace", "noslack"):
+        for (atoms, pairs, reb, st), (ratoms, rpairs, rreb, rst) in zip(runs[name], ref):
+            assert np.array_equal(reb, rreb), name
+            assert st["natoms"] == rst["natoms"] and st["nlost"] == rst["nlost"], name
+            assert st["npairs"] == rst["npairs"], name
+            for a, b in zip(atoms, ratoms):
+                for key in ("tag", "x", "v", "omega", "f", "torque"):
+                    assert np.array_equal(a[key], b[key]), (name, key)
+            for key in rpairs:
+                assert np.array_equal(pairs[key], rpairs[key]), (name, key)
+    assert ref[-1][3]["nlost"] >= 1
+    assert ref[-1][3]["ens_inplace_builds"] == 0 and ref[-1][3]["ens_relayout_builds"] == 0
+    last = runs["inplace"][-1][3]
+    assert last["ens_inplace_builds"] > 10, last
+    assert runs["noslack"][-1][3]["ens_relayout_builds"] > 0
+    # the schedules differ between systems, so most builds leave some system out
+    assert len(set(int(r) for r in runs["inplace"][-1][2])) > 1
