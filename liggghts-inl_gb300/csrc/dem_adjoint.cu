@@ -1466,6 +1466,11 @@ struct dem_adjoint {
   Arena arena;                // per-run checkpoints, lists and tape
   cudaStream_t st = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  // the backward pass's replays run on st2, beside the reverse sweeps on st:
+  // evq[b] = the replay into tape b is done, evq[2 + b] = the reverse sweep
+  // over tape b is done
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t evq[4] = {nullptr, nullptr, nullptr, nullptr};
   std::string err;
   double *x0 = nullptr, *v0 = nullptr, *w0 = nullptr, *r0 = nullptr;  // initial state
   double rmax0 = 0.0;
@@ -1587,8 +1592,7 @@ int build_list(dem_adjoint *h, AList &L, const AList &old, long long step) {
   return DEM_OK;
 }
 
-void use_list(dem_adjoint *h, const AList &L, double *shear, double *bond) {
-  ADev &s = h->s;
+void use_list_on(ADev &s, const AList &L, double *shear, double *bond) {
   s.bh = bond;
   s.np = L.np;
   s.pi = L.pi;
@@ -1602,6 +1606,8 @@ void use_list(dem_adjoint *h, const AList &L, double *shear, double *bond) {
   s.mcn = L.mcn;
   s.mcand = L.mcand;
 }
+
+void use_list(dem_adjoint *h, const AList &L, double *shear, double *bond) { use_list_on(h->s, L, shear, bond); }
 
 int ensure_pairs(dem_adjoint *h, int np) {
   if (np <= h->pcap) return DEM_OK;
@@ -1630,13 +1636,12 @@ void derive(double E, double nu, double e, double &Y, double &G, double &beta, d
   dbde = (1.0 / e) * (M_PI * M_PI) / std::pow(lg * lg + M_PI * M_PI, 1.5);
 }
 
-void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, long long ntimestep,
-                double *tape_sh, double *tape_bh, double *tape_ws, int final_kick, double *wallF,
-                double *tape_F = nullptr, double *tape_T = nullptr, int *tape_mst = nullptr,
-                double *tape_msh = nullptr, int *tape_mnp = nullptr) {
-  ADev &s = h->s;
-  const int g = grid_of(s.np), ga = grid_of(h->n);
-  const cudaStream_t st = h->st;
+// one force evaluation of state s on stream st
+void force_pass_on(const ADev &s, cudaStream_t st, const double *vh, const double *wh, int upd,
+                   long long ntimestep, double *tape_sh, double *tape_bh, double *tape_ws, int final_kick,
+                   double *wallF, double *tape_F = nullptr, double *tape_T = nullptr, int *tape_mst = nullptr,
+                   double *tape_msh = nullptr, int *tape_mnp = nullptr) {
+  const int g = grid_of(s.np), ga = grid_of(s.n);
   if (s.np > 0) {
     if (s.bonds && s.rolling) ka_pair_force<true, true><<<g, kAB, 0, st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
     else if (s.bonds) ka_pair_force<true, false><<<g, kAB, 0, st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
@@ -1651,6 +1656,14 @@ void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, lon
   else if (s.nmeshes) A_GATHER(false, true);
   else A_GATHER(false, false);
 #undef A_GATHER
+}
+
+void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, long long ntimestep,
+                double *tape_sh, double *tape_bh, double *tape_ws, int final_kick, double *wallF,
+                double *tape_F = nullptr, double *tape_T = nullptr, int *tape_mst = nullptr,
+                double *tape_msh = nullptr, int *tape_mnp = nullptr) {
+  force_pass_on(h->s, h->st, vh, wh, upd, ntimestep, tape_sh, tape_bh, tape_ws, final_kick, wallF, tape_F, tape_T,
+                tape_mst, tape_msh, tape_mnp);
 }
 
 void pairs_vjp(dem_adjoint *h, const double *x, const float4 *xf, const double *vh, const double *wh,
@@ -1689,9 +1702,11 @@ void accumulate(dem_adjoint *h, const double *in, int cnt) {
   kb_accum_th<<<1, 32, 0, h->st>>>(h->part, g, h->B.th);
 }
 
-void copyd(dem_adjoint *h, double *dst, const double *src, size_t count) {
-  if (count) cudaMemcpyAsync(dst, src, count * sizeof(double), cudaMemcpyDeviceToDevice, h->st);
+void copyd_on(cudaStream_t st, double *dst, const double *src, size_t count) {
+  if (count) cudaMemcpyAsync(dst, src, count * sizeof(double), cudaMemcpyDeviceToDevice, st);
 }
+
+void copyd(dem_adjoint *h, double *dst, const double *src, size_t count) { copyd_on(h->st, dst, src, count); }
 
 }  // namespace
 
@@ -1711,8 +1726,11 @@ int dem_adjoint_create(const dem_adjoint_config *cfg, dem_adjoint **out) {
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return DEM_ERR_NO_DEVICE;
   dem_adjoint *h = new dem_adjoint();
   h->cfg = *cfg;
-  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&h->ev[0]) != cudaSuccess || cudaEventCreate(&h->ev[1]) != cudaSuccess) {
+  bool ok = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaStreamCreateWithFlags(&h->st2, cudaStreamNonBlocking) == cudaSuccess &&
+            cudaEventCreate(&h->ev[0]) == cudaSuccess && cudaEventCreate(&h->ev[1]) == cudaSuccess;
+  for (cudaEvent_t &e : h->evq) ok = ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  if (!ok) {
     dem_adjoint_destroy(h);
     return DEM_ERR_CUDA;
   }
@@ -1829,11 +1847,15 @@ int dem_adjoint_set_bonds(dem_adjoint *h, const double *values, const dem_bond_s
 int dem_adjoint_destroy(dem_adjoint *h) {
   if (!h) return DEM_ERR_BAD_ARG;
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->st2) cudaStreamSynchronize(h->st2);
   h->arena.release();
   for (void *p : h->owned) cudaFree(p);
   for (cudaEvent_t e : h->ev)
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : h->evq)
+    if (e) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
+  if (h->st2) cudaStreamDestroy(h->st2);
   delete h;
   return DEM_OK;
 }
@@ -2192,26 +2214,84 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
   ATRY(h, cudaMemsetAsync(B.th, 0, kTh * sizeof(double), st));
   ATRY(h, cudaMemsetAsync(B.wth, 0, kTh * (size_t)n * sizeof(double), st));
   const double fw_seed = use_wall ? loss->w_wallforce * 2.0 * (fw - loss->wallforce_target) : 0.0;
-  // the replay's tape of one segment (segments recorded in the forward pass
-  // use their own)
-  Tape shared;
-  shared.ps = (size_t)maxnp;
+  // Replay (tape mode 0): segment k-1 is replayed from its checkpoint on
+  // the second stream, with its own state s2 and into one of two tapes,
+  // while the reverse sweep of segment k reads the other tape on the
+  // handle's stream.  (Segments recorded in the forward pass use their own
+  // tape.)
+  Tape shared[2];
+  ADev s2 = s;
+  double *shr2 = nullptr, *bhr2 = nullptr;
   if (!record) {
-    AGET(h, shared.x, double, S3 * seg);
-    AGET(h, shared.vh, double, S3 * seg);
-    AGET(h, shared.wh, double, S3 * seg);
-    AGET(h, shared.F, double, S3 * seg);
-    AGET(h, shared.T, double, S3 * seg);
-    AGET(h, shared.ws, double, W3 * seg);
-    AGET(h, shared.sh, double, 3 * (size_t)maxnp * seg);
-    AGET(h, shared.xf, float4, (size_t)n * seg);
-    if (s.bonds) AGET(h, shared.bh, double, kBondValues * (size_t)maxnp * seg);
-    if (s.nmeshes) {
-      AGET(h, shared.mst, int, NBM * kAMC * seg);
-      AGET(h, shared.msh, double, NBM * kAMC * 3 * seg);
-      AGET(h, shared.mnp, int, NBM * seg);
+    for (Tape &tp : shared) {
+      tp.ps = (size_t)maxnp;
+      AGET(h, tp.x, double, S3 * seg);
+      AGET(h, tp.vh, double, S3 * seg);
+      AGET(h, tp.wh, double, S3 * seg);
+      AGET(h, tp.F, double, S3 * seg);
+      AGET(h, tp.T, double, S3 * seg);
+      AGET(h, tp.ws, double, W3 * seg);
+      AGET(h, tp.sh, double, 3 * (size_t)maxnp * seg);
+      AGET(h, tp.xf, float4, (size_t)n * seg);
+      if (s.bonds) AGET(h, tp.bh, double, kBondValues * (size_t)maxnp * seg);
+      if (s.nmeshes) {
+        AGET(h, tp.mst, int, NBM * kAMC * seg);
+        AGET(h, tp.msh, double, NBM * kAMC * 3 * seg);
+        AGET(h, tp.mnp, int, NBM * seg);
+      }
     }
+    // the replay's own positions, velocities, forces, wall and slot
+    // histories, FP32 mirror, pair outputs and carried histories
+    AGET(h, s2.x, double, S3);
+    AGET(h, s2.v, double, S3);
+    AGET(h, s2.w, double, S3);
+    AGET(h, s2.F, double, S3);
+    AGET(h, s2.T, double, S3);
+    AGET(h, s2.ws, double, W3);
+    AGET(h, s2.xf, float4, (size_t)n);
+    AGET(h, s2.pF, double, 3 * (size_t)maxnp);
+    AGET(h, s2.pTi, double, 3 * (size_t)maxnp);
+    AGET(h, s2.pTj, double, 3 * (size_t)maxnp);
+    AGET(h, s2.active, uint8_t, (size_t)maxnp);
+    if (s.nmeshes) {
+      AGET(h, s2.mst, int, NBM * kAMC);
+      AGET(h, s2.msh, double, NBM * kAMC * 3);
+      AGET(h, s2.mnp, int, NBM);
+    }
+    AGET(h, shr2, double, 3 * (size_t)maxnp);
+    if (s.bonds) AGET(h, bhr2, double, kBondValues * (size_t)maxnp);
   }
+  // replay of segment k into tape T on the second stream, recording the
+  // positions, half-step velocities, histories and forces of every step
+  auto replay = [&](int k, Tape &T) {
+    Checkpoint &c = cps[k];
+    const int first = std::max(1, k * seg), last = std::min(nsteps, (k + 1) * seg - 1);
+    const cudaStream_t q2 = h->st2;
+    copyd_on(q2, s2.x, c.x, S3);
+    copyd_on(q2, s2.v, c.v, S3);
+    copyd_on(q2, s2.w, c.w, S3);
+    copyd_on(q2, s2.F, c.F, S3);
+    copyd_on(q2, s2.T, c.T, S3);
+    copyd_on(q2, s2.ws, c.ws, W3);
+    copyd_on(q2, shr2, c.sh0, 3 * (size_t)c.L.np);
+    if (s.bonds) copyd_on(q2, bhr2, c.bh0, (size_t)kBondValues * c.L.np);
+    if (s.nmeshes) {
+      cudaMemcpyAsync(s2.mst, c.mst0, NBM * kAMC * sizeof(int), cudaMemcpyDeviceToDevice, q2);
+      copyd_on(q2, s2.msh, c.msh0, NBM * kAMC * 3);
+      cudaMemcpyAsync(s2.mnp, c.mnp0, NBM * sizeof(int), cudaMemcpyDeviceToDevice, q2);
+    }
+    use_list_on(s2, c.L, shr2, bhr2);
+    const size_t PS = T.ps;
+    for (int t = first; t <= last; t++) {
+      const int q = t - first;
+      ka_kick_drift<<<grid_of(n), kAB, 0, q2>>>(s2, nullptr, (k > 0 && t == first) ? 1 : 0, T.x + S3 * q,
+                                                T.vh + S3 * q, T.wh + S3 * q, T.xf + (size_t)n * q);
+      force_pass_on(s2, q2, T.vh + S3 * q, T.wh + S3 * q, 1, t, T.sh + 3 * PS * q,
+                    s.bonds ? T.bh + kBondValues * PS * q : nullptr, T.ws + W3 * q, 1, nullptr, T.F + S3 * q,
+                    T.T + S3 * q, s.nmeshes ? T.mst + NBM * kAMC * q : nullptr,
+                    s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr, s.nmeshes ? T.mnp + NBM * q : nullptr);
+    }
+  };
   // the mesh slot state before the setup pass (empty) and the slot-history
   // adjoints of the previous list at a build
   int *mst_e = nullptr, *mnp_e = nullptr;
@@ -2236,37 +2316,26 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     AGET(h, bhr, double, NB);
     AGET(h, bb_prev, double, NB);
   }
+  const bool replayed = !record;
+  if (replayed) {  // the last segment's replay; each earlier one is queued a segment ahead
+    ATRY(h, cudaEventRecord(h->evq[2], st));  // the state above is in place before the replays start
+    ATRY(h, cudaStreamWaitEvent(h->st2, h->evq[2], 0));
+    replay(nseg - 1, shared[(nseg - 1) & 1]);
+    ATRY(h, cudaEventRecord(h->evq[(nseg - 1) & 1], h->st2));
+  }
   for (int k = nseg - 1; k >= 0; k--) {
     Checkpoint &c = cps[k];
     const int first = std::max(1, k * seg), last = std::min(nsteps, (k + 1) * seg - 1);
-    const bool recorded = c.tape.x != nullptr;
-    const Tape &T = recorded ? c.tape : shared;
+    if (replayed && k >= 1) {
+      // segment k-1 into the tape of segment k+1, once that one's reverse sweep is done
+      if (k + 1 < nseg) ATRY(h, cudaStreamWaitEvent(h->st2, h->evq[2 + ((k + 1) & 1)], 0));
+      replay(k - 1, shared[(k - 1) & 1]);
+      ATRY(h, cudaEventRecord(h->evq[(k - 1) & 1], h->st2));
+    }
+    if (replayed) ATRY(h, cudaStreamWaitEvent(st, h->evq[k & 1], 0));
+    const Tape &T = replayed ? shared[k & 1] : c.tape;
     const size_t PS = T.ps;
-    if (!recorded) {  // replay from the checkpoint, recording the tape
-      copyd(h, s.x, c.x, S3);
-      copyd(h, s.v, c.v, S3);
-      copyd(h, s.w, c.w, S3);
-      copyd(h, s.F, c.F, S3);
-      copyd(h, s.T, c.T, S3);
-      copyd(h, s.ws, c.ws, W3);
-      copyd(h, shr, c.sh0, 3 * (size_t)c.L.np);
-      if (s.bonds) copyd(h, bhr, c.bh0, (size_t)kBondValues * c.L.np);
-      if (s.nmeshes) {
-        ATRY(h, cudaMemcpyAsync(s.mst, c.mst0, NBM * kAMC * sizeof(int), cudaMemcpyDeviceToDevice, st));
-        copyd(h, s.msh, c.msh0, NBM * kAMC * 3);
-        ATRY(h, cudaMemcpyAsync(s.mnp, c.mnp0, NBM * sizeof(int), cudaMemcpyDeviceToDevice, st));
-      }
-    }
     use_list(h, c.L, shr, bhr);
-    for (int t = first; t <= last && !recorded; t++) {
-      const int q = t - first;
-      ka_kick_drift<<<grid_of(n), kAB, 0, st>>>(s, nullptr, (k > 0 && t == first) ? 1 : 0, T.x + S3 * q,
-                                                T.vh + S3 * q, T.wh + S3 * q, T.xf + (size_t)n * q);
-      force_pass(h, T.vh + S3 * q, T.wh + S3 * q, 1, t, T.sh + 3 * PS * q,
-                 s.bonds ? T.bh + kBondValues * PS * q : nullptr, T.ws + W3 * q, 1, nullptr, T.F + S3 * q,
-                 T.T + S3 * q, s.nmeshes ? T.mst + NBM * kAMC * q : nullptr,
-                 s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr, s.nmeshes ? T.mnp + NBM * q : nullptr);
-    }
     // reverse over the segment's steps; the pair parameter adjoints of the
     // segment's list are summed per entry over its steps, then reduced
     if (s.np > 0) ATRY(h, cudaMemsetAsync(B.pth, 0, kTh * (size_t)s.np * sizeof(double), st));
@@ -2303,6 +2372,7 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
         copyd(h, B.msb, msb_prev, NBM * kAMC * 3);
       }
     }
+    if (replayed) ATRY(h, cudaEventRecord(h->evq[2 + (k & 1)], st));
   }
   {  // Verlet::setup force pass: initial state, zero history, no update
     Checkpoint &c = cps[0];

@@ -25,6 +25,7 @@ namespace {
 constexpr int kCheckEvery = 256;
 // the two-level exclusive scan covers 4096 * 4096 items
 constexpr long kMaxScan = 4096L * 4096L - 2;
+static_assert(kMaxScan < (1L << 24), "the neighbour stash packs atom indices in 24 bits");
 constexpr long kMaxCells = 16000000L;
 }  // namespace
 
@@ -276,6 +277,7 @@ static int alloc_atoms(dem_handle *h, int nmax) {
     ar.take(&s.xf, nmax);
     ar.take(&s.xhf, nmax);
     ar.take(&s.mlist, nmax);
+    ar.take(&s.stash, (size_t)kStash * nmax);
     ar.take(&s.wforce, (size_t)3 * std::max(1, s.nplanes + s.nmeshes) * nmax);
     ar.take(&s.order, nmax);
     ar.take(&s.pcount, nmax + 1);
@@ -1122,7 +1124,13 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
     s.nc[d] = std::max(s.periodic[d] ? 3 : 1, s.nc[d] / 2);
     ncell = (long)s.nc[0] * s.nc[1] * s.nc[2];
   }
-  for (int d = 0; d < 3; d++) s.csz[d] = s.prd[d] / s.nc[d];
+  for (int d = 0; d < 3; d++) {
+    s.csz[d] = s.prd[d] / s.nc[d];
+    s.icsz[d] = 1.0 / s.csz[d];
+    s.prdf[d] = (float)s.prd[d];
+  }
+  s.cdff = (float)s.cdf;
+  s.skinf = (float)s.skin;
   s.ens_ncell = h->ens_nsys > 0 ? (int)ncell : 0;
   s.ncell = (int)(ncell * nsys);
   // FixNeighlistMesh::pre_force distmax/skin (static meshes), src/fix_neighlist_mesh.cpp:249-264

@@ -195,6 +195,9 @@ struct MeshDev {
 };
 
 constexpr int kResStride = 12;  // doubles per pair-result record
+// list entries per atom that the neighbour count pass keeps for the fill
+// pass (Sys::stash): partner | image code << 24 (atom indices stay below 2^24)
+constexpr int kStash = 16;
 
 struct Sys {
   AtomArrays atoms[2];
@@ -214,6 +217,7 @@ struct Sys {
   float4 *xf;       // FP32 copy (x, y, z, r) of the atoms, refreshed by every drift
   float4 *xhf;      // FP32 copy of x at the last neighbour build (displacement prefilter)
   int *mlist;       // atoms with candidate mesh triangles [nmax]
+  int *stash;       // [kStash*nmax]: entries found by the count pass, see kStash
   double *wforce;   // [(w*3+d)*nmax + i]: force of wall w (planes, then meshes) on listed
                     // atom i at the last force evaluation (diagnostics)
   // parameters
@@ -240,7 +244,11 @@ struct Sys {
   int ens_full;      // 1: every ensemble rebuild takes the whole-list path
   int ens_slack;     // unused entries a segment gets, percent of its entries (plus 64; 0: none)
   double csz[3];
+  double icsz[3];     // 1/csz: an atom's cell is floor((x - boxlo) * icsz)
   double boxlo[3], boxhi[3], prd[3];
+  // FP32 copies for the prefilters (a double-to-float conversion issues on
+  // the FP64 pipe, so none is made inside a loop)
+  float prdf[3], cdff, skinf;
   int periodic[3];
   double dt, skin, cdf, cutneighmax;
   double ghost_slab;  // cutneighmax/2 + skin/2: CommBrick slab_offset of the ghost band

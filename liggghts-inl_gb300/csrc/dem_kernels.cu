@@ -67,8 +67,11 @@ __device__ __forceinline__ bool ghost_exists(const Sys &s, const AtomArrays &A, 
   return true;
 }
 
+// The cells are wider than the neighbour cutoff by a relative 1e-9 at least,
+// far above the rounding of this product, so atoms within the cutoff are
+// never more than one cell apart; every kernel bins through this function.
 __device__ __forceinline__ int cell_coord(const Sys &s, double x, int d) {
-  int c = (int)((x - s.boxlo[d]) / s.csz[d]);
+  int c = (int)((x - s.boxlo[d]) * s.icsz[d]);
   c = c < 0 ? 0 : c;
   c = c >= s.nc[d] ? s.nc[d] - 1 : c;
   return c;
@@ -1093,7 +1096,10 @@ __global__ void __launch_bounds__(256) k_wall_list(Sys s) {
 
 // ----------------------------------------------------------------------------
 // rebuild: granular half list (Neighbor::granular_bin_no_newton,
-// src/neigh_gran.cpp:485-644), 27-cell stencil with periodic images.
+// src/neigh_gran.cpp:485-644), 27-cell stencil with periodic images.  The
+// count pass keeps each atom's first kStash entries (partner and image code
+// in one int); the fill pass copies them into the atom's row, and searches
+// again only for atoms with more.
 // ----------------------------------------------------------------------------
 
 template <bool FILL>
@@ -1121,12 +1127,25 @@ __device__ __forceinline__ void pairs_atom(const Sys &s, const AtomArrays &A, co
       }
       return;
     }
+    if (FILL) {  // the count pass kept the atom's entries unless it had more than kStash
+      const int beg = M.row[i], ne = row_end(s, M, i) - beg;
+      if (ne <= kStash) {
+        for (int e = 0; e < ne; e++) {
+          const int v = s.stash[(size_t)e * s.nmax + i];
+          M.i[beg + e] = i;
+          M.j[beg + e] = v & 0xffffff;
+          M.sh[beg + e] = (uint8_t)(v >> 24);
+          if (s.nsys) M.rev[beg + e] = -1;  // a fresh entry (source of copied ones: see above)
+        }
+        return;
+      }
+    }
     const double xi = A.x[i], yi = A.y[i], zi = A.z[i];
     const double radi = A.r[i];
     const int ci[3] = {cell_coord(s, xi, 0), cell_coord(s, yi, 1), cell_coord(s, zi, 2)};
     const float4 pi = s.xf[i];
     const int cell_base = s.ens_ncell ? (A.type[i] - 1) * s.ens_ncell : 0;
-    const float cdff = (float)s.cdf, skinf = (float)s.skin;
+    const float cdff = s.cdff, skinf = s.skinf;
     const float hi_f = 1.0f + s.pf_margin, lo_f = 1.0f - s.pf_margin;
     int cnt = 0;
     int out = FILL ? M.row[i] : 0;
@@ -1155,7 +1174,7 @@ __device__ __forceinline__ void pairs_atom(const Sys &s, const AtomArrays &A, co
           const int code = (sv[0] + 1) + 3 * (sv[1] + 1) + 9 * (sv[2] + 1);
           const int cell = cc[0] + s.nc[0] * (cc[1] + s.nc[1] * cc[2]) + cell_base;
           const int jb = s.cell_start[cell], je = s.cell_start[cell + 1];
-          const float sxf = sv[0] * (float)s.prd[0], syf = sv[1] * (float)s.prd[1], szf = sv[2] * (float)s.prd[2];
+          const float sxf = sv[0] * s.prdf[0], syf = sv[1] * s.prdf[1], szf = sv[2] * s.prdf[2];
           for (int j = jb; j < je; j++) {
             if (code == kNoShift && j <= i) continue;
             // FP32 prefilter of rsq <= (radsum*cdf + skin)^2: candidates
@@ -1171,6 +1190,7 @@ __device__ __forceinline__ void pairs_atom(const Sys &s, const AtomArrays &A, co
             if (code != kNoShift && !ghost_exists(s, A, j, sv)) continue;
             const bool clear_in = rsqf < cs2f * lo_f;
             if (!FILL && clear_in) {
+              if (cnt < kStash) s.stash[(size_t)cnt * s.nmax + i] = j | (code << 24);
               cnt++;
               continue;
             }
@@ -1185,6 +1205,7 @@ __device__ __forceinline__ void pairs_atom(const Sys &s, const AtomArrays &A, co
             const double cs = __dadd_rn(radsum, s.skin);
             if (!(rsq <= __dmul_rn(cs, cs))) continue;
             if (!FILL) {
+              if (cnt < kStash) s.stash[(size_t)cnt * s.nmax + i] = j | (code << 24);
               cnt++;
               continue;
             }
@@ -1684,7 +1705,7 @@ __global__ void __launch_bounds__(kPairTile, MINB) k_pair_pf(Sys s, int shearupd
   const int np = c->np;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float hi_f = 1.0f + s.pf_margin_touch;
-  const float px = (float)s.prd[0], py = (float)s.prd[1], pz = (float)s.prd[2];
+  const float px = s.prdf[0], py = s.prdf[1], pz = s.prdf[2];
   if (threadIdx.x == 0) qn_s = 0;
   __syncthreads();
   for (int base = blockIdx.x * kPairTile; base < np; base += gridDim.x * kPairTile) {
