@@ -2005,11 +2005,15 @@ __device__ void mesh_contacts(const Sys &s, const AtomArrays &A, int i, int k, i
 //      since that copy depends on the order of the contact updates;
 //   D  per contact: the contact law with the slot's history;
 //   E  per atom: contact forces summed in candidate order, slot clean-up.
-// A tile whose queue would exceed kWallCap entries runs the sequential path
-// for all its atoms.  Both paths give the same result.
+// A tile whose queue would exceed its capacity (cap entries, a launch
+// parameter) runs the sequential path for all its atoms.  Both paths give
+// the same result.  The queue lives in dynamic shared memory, kWallQ bytes
+// per entry: a smaller cap leaves room for more blocks beside the pair
+// kernel that runs concurrently.
 constexpr int kWallTile = 64;
-constexpr int kWallCap = 16 * kWallTile;
+constexpr int kWallCapDefault = 6;  // queue entries per tile atom (LIGGGHTS_GB300_WALL_CAP)
 constexpr int kWallRes = 7;  // doubles per queued candidate: deltan, delta[3], vwall[3]; then F[3], T[3]
+constexpr int kWallQ = kWallRes * 8 + 4 + 2;  // result doubles, state int, atom and candidate bytes
 
 __device__ __forceinline__ int wall_tile_scan(int v, int &total, int *wsum) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -2032,10 +2036,12 @@ __device__ __forceinline__ int wall_tile_scan(int v, int &total, int *wsum) {
 }
 
 template <int NORMAL>
-__global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate) {
-  extern __shared__ double wres[];             // [kWallCap * kWallRes]
-  __shared__ unsigned char qa[kWallCap], qq[kWallCap];
-  __shared__ int qst[kWallCap];                // bit 0 touching, bit 1 face, bits 8+: contact slot + 1
+__global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate, int cap) {
+  extern __shared__ double wres[];             // [cap * kWallRes], then qst, qa, qq
+  int *qst = reinterpret_cast<int *>(wres + (size_t)cap * kWallRes);  // bit 0 touching, bit 1 face,
+                                                                       // bits 8+: contact slot + 1
+  unsigned char *qa = reinterpret_cast<unsigned char *>(qst + cap);
+  unsigned char *qq = qa + cap;
   __shared__ int wsum[kWallTile / 32];
   Ctrl *c = s.ctrl;
   if (c->halt) return;
@@ -2091,7 +2097,7 @@ __global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate
       const int off = wall_tile_scan(cnt, total, wsum);
       double msum[3] = {0., 0., 0.};
       double *const wf = s.wforce + (size_t)(3 * (s.nplanes + k)) * nmax;
-      if (total > kWallCap) {  // sequential path for this tile
+      if (total > cap) {  // sequential path for this tile
         if (nc > 0) mesh_contacts<NORMAL>(s, A, i, k, shearupdate, v, om, xv, fx, fy, fz, tx, ty, tz, meshbad, msum);
         if (valid)
           for (int d = 0; d < 3; d++) wf[(size_t)d * nmax + i] = msum[d];
@@ -2867,24 +2873,28 @@ int launch_wall_force(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaSt
   if (s.nmeshes == 0 && s.nplanes == 0) return 0;
   int lo = 0, hi = 0;
   cudaDeviceGetStreamPriorityRange(&lo, &hi);
+  // queue entries per tile: LIGGGHTS_GB300_WALL_CAP per atom (1..16)
+  static int cap_per_atom = 0;
+  if (!cap_per_atom) {
+    const char *e = getenv("LIGGGHTS_GB300_WALL_CAP");
+    cap_per_atom = e ? std::max(1, std::min(16, atoi(e))) : kWallCapDefault;
+    const int bytes = cap_per_atom * kWallTile * kWallQ;
+    cudaFuncSetAttribute(k_wall_force<kHertz>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_wall_force<kHooke>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  }
+  const int cap = cap_per_atom * kWallTile;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid_for(s.nmax, kWallTile, 2 * lc.max_grid));
   cfg.blockDim = dim3(kWallTile);
-  cfg.dynamicSmemBytes = (size_t)kWallCap * kWallRes * sizeof(double);
-  static bool smem_set = false;  // more than the 48 KB default of dynamic shared memory
-  if (!smem_set) {
-    cudaFuncSetAttribute(k_wall_force<kHertz>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.dynamicSmemBytes);
-    cudaFuncSetAttribute(k_wall_force<kHooke>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cfg.dynamicSmemBytes);
-    smem_set = true;
-  }
+  cfg.dynamicSmemBytes = (size_t)cap * kWallQ;
   cfg.stream = st;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributePriority;
   attr[0].val.priority = hi;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (s.normal == kHertz) cudaLaunchKernelEx(&cfg, k_wall_force<kHertz>, s, shearupdate);
-  else cudaLaunchKernelEx(&cfg, k_wall_force<kHooke>, s, shearupdate);
+  if (s.normal == kHertz) cudaLaunchKernelEx(&cfg, k_wall_force<kHertz>, s, shearupdate, cap);
+  else cudaLaunchKernelEx(&cfg, k_wall_force<kHooke>, s, shearupdate, cap);
   return 1;
 }
 
