@@ -2247,45 +2247,60 @@ __global__ void __launch_bounds__(kWallTile) k_wall_force(Sys s, int shearupdate
 // instruction, so additions inside a loop over all list entries cost one
 // issue per entry of the warp's longest row, active or not.  Here a first,
 // integer-only pass collects the active entries of up to 32 entries per list
-// as bit masks; one loop over the set bits then does the FP64 additions, so a
-// warp issues them only as often as its busiest atom has contacts.  A reverse
-// contribution adds the negated force (sign bit flipped on the integer pipe:
-// a + (-b) is exactly a - b) and Tj instead of Ti.
-__device__ __forceinline__ void gather_contacts(const Sys &s, const PairArrays &L, size_t P, int i, double &fx,
-                                                double &fy, double &fz, double &tx, double &ty, double &tz) {
+// as bit masks (gather_masks); one loop over the set bits then does the FP64
+// additions (gather_sum).  A reverse contribution adds the negated force
+// (sign bit flipped on the integer pipe: a + (-b) is exactly a - b) and Tj
+// instead of Ti.  k_particle hands the loops of a block's atoms to its
+// threads sorted by contact count, so that a warp's lanes run loops of equal
+// length (see there).
+__device__ __forceinline__ bool gather_masks(const Sys &s, const PairArrays &L, int i, int &pb, int &rb,
+                                             unsigned &om, unsigned &rm) {
+  pb = L.row[i];
+  rb = L.rev_start[i];
+  const int pe = row_end(s, L, i), re = rev_end(s, L, i);
+  if (pe - pb > 32 || re - rb > 32) return false;
+  om = 0u;
+  rm = 0u;
+  for (int k = 0; k < pe - pb; k++) om |= (s.active[pb + k] ? 1u : 0u) << k;
+  for (int k = 0; k < re - rb; k++) rm |= (s.active[L.rev[rb + k]] ? 1u : 0u) << k;
+  return true;
+}
+
+__device__ __forceinline__ void gather_sum(const Sys &s, const PairArrays &L, int pb, int rb, unsigned om,
+                                           unsigned rm, double &fx, double &fy, double &fz, double &tx, double &ty,
+                                           double &tz) {
+  const int cnt = __popc(om) + __popc(rm);
+  for (int t = 0; t < cnt; t++) {
+    int p;
+    unsigned long long sg;
+    int to;  // offset of the torque in the record: Ti (own row) or Tj (partner)
+    if (om) {
+      p = pb + __ffs(om) - 1;
+      om &= om - 1u;
+      sg = 0ull;
+      to = 3;
+    } else {
+      p = L.rev[rb + __ffs(rm) - 1];
+      rm &= rm - 1u;
+      sg = 0x8000000000000000ull;
+      to = 6;
+    }
+    const double *r = s.res + (size_t)kResStride * p;
+    fx += __longlong_as_double(__double_as_longlong(r[0]) ^ sg);
+    fy += __longlong_as_double(__double_as_longlong(r[1]) ^ sg);
+    fz += __longlong_as_double(__double_as_longlong(r[2]) ^ sg);
+    tx += r[to];
+    ty += r[to + 1];
+    tz += r[to + 2];
+  }
+}
+
+// lists longer than 32 entries: one pass over every entry
+__device__ __forceinline__ void gather_long(const Sys &s, const PairArrays &L, int i, double &fx, double &fy,
+                                            double &fz, double &tx, double &ty, double &tz) {
   const int pb = L.row[i], pe = row_end(s, L, i);
   const int rb = L.rev_start[i], re = rev_end(s, L, i);
-  if (pe - pb <= 32 && re - rb <= 32) {
-    unsigned om = 0u, rm = 0u;
-    for (int k = 0; k < pe - pb; k++) om |= (s.active[pb + k] ? 1u : 0u) << k;
-    for (int k = 0; k < re - rb; k++) rm |= (s.active[L.rev[rb + k]] ? 1u : 0u) << k;
-    const int cnt = __popc(om) + __popc(rm);
-    for (int t = 0; t < cnt; t++) {
-      int p;
-      unsigned long long sg;
-      int to;  // offset of the torque in the record: Ti (own row) or Tj (partner)
-      if (om) {
-        p = pb + __ffs(om) - 1;
-        om &= om - 1u;
-        sg = 0ull;
-        to = 3;
-      } else {
-        p = L.rev[rb + __ffs(rm) - 1];
-        rm &= rm - 1u;
-        sg = 0x8000000000000000ull;
-        to = 6;
-      }
-      const double *r = s.res + (size_t)kResStride * p;
-      fx += __longlong_as_double(__double_as_longlong(r[0]) ^ sg);
-      fy += __longlong_as_double(__double_as_longlong(r[1]) ^ sg);
-      fz += __longlong_as_double(__double_as_longlong(r[2]) ^ sg);
-      tx += r[to];
-      ty += r[to + 1];
-      tz += r[to + 2];
-    }
-    return;
-  }
-  for (int p = pb; p < pe; p++) {  // lists longer than 32 entries
+  for (int p = pb; p < pe; p++) {
     if (!s.active[p]) continue;
     const double *r = s.res + (size_t)kResStride * p;
     fx += r[0]; fy += r[1]; fz += r[2];
@@ -2300,36 +2315,110 @@ __device__ __forceinline__ void gather_contacts(const Sys &s, const PairArrays &
   }
 }
 
+// the block-level sort of k_particle's gather: loops of up to kGatherKeys-1
+// contacts by count, longer ones together in the last key
+constexpr int kGatherKeys = 32;
+constexpr int kParticleMaxThreads = 256;
+
+// Per atom: force gather, gravity, wall totals, nve/sphere, FP32 copy,
+// displacement check.  The gather runs in three block-wide phases, because a
+// warp's contact loops issue their FP64 additions once per contact of its
+// busiest atom: (1) every thread forms its atom's start sums (gravity) and
+// contact masks; (2) the atoms with contacts are sorted by their contact
+// count in shared memory; (3) thread t runs the loop of the t-th atom in that
+// order, so that a warp's lanes run loops of equal length, and the sums go
+// back to the owner.  Each atom's sum keeps its order and its one thread, so
+// the result does not depend on the sort or the launch shape.
 template <int NORMAL, bool GATHER, bool FINAL, bool INITIAL>
-__global__ void __launch_bounds__(256) k_particle(Sys s, int shearupdate) {
+__global__ void __launch_bounds__(kParticleMaxThreads, 4) k_particle(Sys s, int shearupdate) {
+  __shared__ double gsum[GATHER ? 6 : 1][GATHER ? kParticleMaxThreads : 1];
+  __shared__ int gpb[GATHER ? kParticleMaxThreads : 1], grb[GATHER ? kParticleMaxThreads : 1];
+  __shared__ unsigned gom[GATHER ? kParticleMaxThreads : 1], grm[GATHER ? kParticleMaxThreads : 1];
+  __shared__ short gsorted[GATHER ? kParticleMaxThreads : 1];
+  __shared__ int gcount[kGatherKeys], gfill[kGatherKeys], gstart[kGatherKeys], gnq;
   Ctrl *c = s.ctrl;
   if (c->halt) return;
   const AtomArrays &A = s.atoms[0];
   const PairArrays &L = s.pairs[0];
   const int n = c->n;
-  const size_t P = s.pcap;
   const double dtv = s.dt;
   const double trigger = 0.25 * s.skin * s.skin;
+  const int tid = threadIdx.x;
   bool moved = false, bad = false;
-  GRID_STRIDE(i, n) {
-    double fx, fy, fz, tx, ty, tz;
-    double v[3] = {A.vx[i], A.vy[i], A.vz[i]};
-    double om[3] = {A.wx[i], A.wy[i], A.wz[i]};
-    double xv[3] = {A.x[i], A.y[i], A.z[i]};
+  for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+    const int i = base + tid;
+    const bool valid = i < n;
+    double fx = 0.0, fy = 0.0, fz = 0.0, tx = 0.0, ty = 0.0, tz = 0.0;
+    double v[3] = {0.0, 0.0, 0.0}, om[3] = {0.0, 0.0, 0.0}, xv[3] = {0.0, 0.0, 0.0};
+    if (valid) {
+      v[0] = A.vx[i]; v[1] = A.vy[i]; v[2] = A.vz[i];
+      om[0] = A.wx[i]; om[1] = A.wy[i]; om[2] = A.wz[i];
+      xv[0] = A.x[i]; xv[1] = A.y[i]; xv[2] = A.z[i];
+    }
     if (GATHER) {
       // FixGravity::post_force (src/fix_gravity.cpp:329-337) adds m*g after
       // the pair forces; starting the sum from it instead changes only the
       // rounding order and saves three FP64 additions
-      if (s.gravity_on) {
+      if (valid && s.gravity_on) {
         const double massone = A.m[i];
         fx = __dmul_rn(massone, s.g[0]);
         fy = __dmul_rn(massone, s.g[1]);
         fz = __dmul_rn(massone, s.g[2]);
-      } else {
-        fx = fy = fz = 0.0;
       }
-      tx = ty = tz = 0.0;
-      gather_contacts(s, L, P, i, fx, fy, fz, tx, ty, tz);
+      // (1) masks; lists longer than 32 entries are summed here by the owner
+      int key = 0;
+      if (tid < kGatherKeys) {
+        gcount[tid] = 0;
+        gfill[tid] = 0;
+      }
+      if (valid) {
+        int pb, rb;
+        unsigned mo, mr;
+        if (gather_masks(s, L, i, pb, rb, mo, mr)) {
+          const int cnt = __popc(mo) + __popc(mr);
+          if (cnt) {
+            key = cnt < kGatherKeys ? cnt : kGatherKeys - 1;
+            gpb[tid] = pb;
+            grb[tid] = rb;
+            gom[tid] = mo;
+            grm[tid] = mr;
+            gsum[0][tid] = fx; gsum[1][tid] = fy; gsum[2][tid] = fz;
+            gsum[3][tid] = tx; gsum[4][tid] = ty; gsum[5][tid] = tz;
+          }
+        } else {
+          gather_long(s, L, i, fx, fy, fz, tx, ty, tz);
+        }
+      }
+      __syncthreads();
+      // (2) counting sort of the block's atoms with contacts by their count
+      if (key) atomicAdd(&gcount[key], 1);
+      __syncthreads();
+      if (tid < 32) {
+        const int v0 = tid < kGatherKeys ? gcount[tid] : 0;
+        const int inc = warp_incl_scan(v0);
+        if (tid < kGatherKeys) gstart[tid] = inc - v0;
+        if (tid == 31) gnq = inc;
+      }
+      __syncthreads();
+      if (key) gsorted[gstart[key] + atomicAdd(&gfill[key], 1)] = (short)tid;
+      __syncthreads();
+      // (3) the loops, one atom per thread in sorted order
+      if (tid < gnq) {
+        const int a = gsorted[tid];
+        double sx = gsum[0][a], sy = gsum[1][a], sz = gsum[2][a];
+        double qx = gsum[3][a], qy = gsum[4][a], qz = gsum[5][a];
+        gather_sum(s, L, gpb[a], grb[a], gom[a], grm[a], sx, sy, sz, qx, qy, qz);
+        gsum[0][a] = sx; gsum[1][a] = sy; gsum[2][a] = sz;
+        gsum[3][a] = qx; gsum[4][a] = qy; gsum[5][a] = qz;
+      }
+      __syncthreads();
+      if (key) {
+        fx = gsum[0][tid]; fy = gsum[1][tid]; fz = gsum[2][tid];
+        tx = gsum[3][tid]; ty = gsum[4][tid]; tz = gsum[5][tid];
+      }
+    }
+    if (!valid) continue;
+    if (GATHER) {
       if (A.wbits[i] & 0x80u) {  // walls, computed by k_wall_force for this step
         fx += A.fmx[i]; fy += A.fmy[i]; fz += A.fmz[i];
         tx += A.tmx[i]; ty += A.tmy[i]; tz += A.tmz[i];
