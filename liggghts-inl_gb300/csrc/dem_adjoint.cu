@@ -965,11 +965,21 @@ __global__ void __launch_bounds__(kAB) ka_pair_force(ADev s, const double *vh, c
 // planes; with final_kick the second half-kick v = vh + a F, w = wh + b T.
 // tape_ws receives the wall history before the update, wallF the wall forces,
 // tape_F/tape_T (if set) a copy of the forces and torques.
+// The next step's first half-kick and drift (ka_kick_drift without a wrap),
+// fused into the gather of a step when both lie in one segment: xref and the
+// t* records as there, nk = 1 to do it.
+struct NextKick {
+  const double *xref;
+  double *tx, *tv, *tw;
+  float4 *txf;
+  int on;
+};
+
 template <bool ROLL, bool MESH>
 __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const double *wh, int upd,
                                                  int final_kick, double *tape_ws, double *wallF, double *tape_F,
                                                  double *tape_T, int *tape_mst, double *tape_msh, int *tape_mnp,
-                                                 long long ntimestep) {
+                                                 long long ntimestep, NextKick nk) {
   __shared__ int q[kAB];
   __shared__ int wcnt[kAB / 32];
   __shared__ double sF[3][kAB], sT[3][kAB];
@@ -978,18 +988,48 @@ __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const
     const bool valid = i < s.n;
     double f[3] = {0., 0., 0.}, t[3] = {0., 0., 0.};
     if (valid) {
-      for (int p = s.row[i]; p < s.row[i + 1]; p++)
-        if (s.active[p])
+      // own row, then the local partner entries, each in ascending order; the
+      // active entries of lists of up to 32 are collected as bit masks first,
+      // so that the FP64 additions issue once per contact of the warp's
+      // busiest atom rather than once per entry of its longest list
+      const int pb = s.row[i], pe = s.row[i + 1], rb = s.rev_start[i], re = s.rev_start[i + 1];
+      if (pe - pb <= 32 && re - rb <= 32) {
+        unsigned mo = 0u, mr = 0u;
+        for (int k = 0; k < pe - pb; k++) mo |= (s.active[pb + k] ? 1u : 0u) << k;
+        for (int k = 0; k < re - rb; k++) {
+          const int p = s.rev[rb + k];
+          mr |= ((s.active[p] && s.sh[p] == kNoShift) ? 1u : 0u) << k;
+        }
+        while (mo) {
+          const int p = pb + __ffs(mo) - 1;
+          mo &= mo - 1u;
           for (int k = 0; k < 3; k++) {
             f[k] += s.pF[3 * p + k];
             t[k] += s.pTi[3 * p + k];
           }
-      for (int qq = s.rev_start[i]; qq < s.rev_start[i + 1]; qq++) {
-        const int p = s.rev[qq];
-        if (!s.active[p] || s.sh[p] != kNoShift) continue;
-        for (int k = 0; k < 3; k++) {
-          f[k] -= s.pF[3 * p + k];
-          t[k] += s.pTj[3 * p + k];
+        }
+        while (mr) {
+          const int p = s.rev[rb + __ffs(mr) - 1];
+          mr &= mr - 1u;
+          for (int k = 0; k < 3; k++) {
+            f[k] -= s.pF[3 * p + k];
+            t[k] += s.pTj[3 * p + k];
+          }
+        }
+      } else {
+        for (int p = pb; p < pe; p++)
+          if (s.active[p])
+            for (int k = 0; k < 3; k++) {
+              f[k] += s.pF[3 * p + k];
+              t[k] += s.pTi[3 * p + k];
+            }
+        for (int qq = rb; qq < re; qq++) {
+          const int p = s.rev[qq];
+          if (!s.active[p] || s.sh[p] != kNoShift) continue;
+          for (int k = 0; k < 3; k++) {
+            f[k] -= s.pF[3 * p + k];
+            t[k] += s.pTj[3 * p + k];
+          }
         }
       }
       if (s.gravity_on)
@@ -1049,6 +1089,30 @@ __global__ void __launch_bounds__(kAB) ka_gather(ADev s, const double *vh, const
           s.v[3 * i + k] = vh[3 * i + k] + a * f[k];
           s.w[3 * i + k] = wh[3 * i + k] + b * t[k];
         }
+      }
+      if (nk.on) {  // the next step's first half-kick and drift, as ka_kick_drift
+        double dsq = 0.0;
+        for (int k = 0; k < 3; k++) {
+          const double v = s.v[3 * i + k] + a * f[k];
+          const double w = s.w[3 * i + k] + b * t[k];
+          const double x = s.x[3 * i + k] + s.dt * v;
+          if (nk.xref) {
+            const double e = x - nk.xref[3 * i + k];
+            dsq += e * e;
+          }
+          s.v[3 * i + k] = v;
+          s.w[3 * i + k] = w;
+          s.x[3 * i + k] = x;
+          if (nk.tx) {
+            nk.tx[3 * i + k] = x;
+            nk.tv[3 * i + k] = v;
+            nk.tw[3 * i + k] = w;
+          }
+        }
+        const float4 f4 = make_float4((float)s.x[3 * i], (float)s.x[3 * i + 1], (float)s.x[3 * i + 2], (float)s.r[i]);
+        s.xf[i] = f4;
+        if (nk.txf) nk.txf[i] = f4;
+        if (dsq > 0.25 * s.skin * s.skin) s.err[0] = 1;
       }
     }
   }
@@ -1640,7 +1704,7 @@ void derive(double E, double nu, double e, double &Y, double &G, double &beta, d
 void force_pass_on(const ADev &s, cudaStream_t st, const double *vh, const double *wh, int upd,
                    long long ntimestep, double *tape_sh, double *tape_bh, double *tape_ws, int final_kick,
                    double *wallF, double *tape_F = nullptr, double *tape_T = nullptr, int *tape_mst = nullptr,
-                   double *tape_msh = nullptr, int *tape_mnp = nullptr) {
+                   double *tape_msh = nullptr, int *tape_mnp = nullptr, NextKick nk = NextKick{}) {
   const int g = grid_of(s.np), ga = grid_of(s.n);
   if (s.np > 0) {
     if (s.bonds && s.rolling) ka_pair_force<true, true><<<g, kAB, 0, st>>>(s, vh, wh, upd, ntimestep, tape_sh, tape_bh);
@@ -1650,7 +1714,7 @@ void force_pass_on(const ADev &s, cudaStream_t st, const double *vh, const doubl
   }
 #define A_GATHER(R, M)                                                                                        \
   ka_gather<R, M><<<ga, kAB, 0, st>>>(s, vh, wh, upd, final_kick, tape_ws, wallF, tape_F, tape_T, tape_mst, tape_msh, \
-                                      tape_mnp, ntimestep)
+                                      tape_mnp, ntimestep, nk)
   if (s.rolling && s.nmeshes) A_GATHER(true, true);
   else if (s.rolling) A_GATHER(true, false);
   else if (s.nmeshes) A_GATHER(false, true);
@@ -1661,9 +1725,9 @@ void force_pass_on(const ADev &s, cudaStream_t st, const double *vh, const doubl
 void force_pass(dem_adjoint *h, const double *vh, const double *wh, int upd, long long ntimestep,
                 double *tape_sh, double *tape_bh, double *tape_ws, int final_kick, double *wallF,
                 double *tape_F = nullptr, double *tape_T = nullptr, int *tape_mst = nullptr,
-                double *tape_msh = nullptr, int *tape_mnp = nullptr) {
+                double *tape_msh = nullptr, int *tape_mnp = nullptr, NextKick nk = NextKick{}) {
   force_pass_on(h->s, h->st, vh, wh, upd, ntimestep, tape_sh, tape_bh, tape_ws, final_kick, wallF, tape_F, tape_T,
-                tape_mst, tape_msh, tape_mnp);
+                tape_mst, tape_msh, tape_mnp, nk);
 }
 
 void pairs_vjp(dem_adjoint *h, const double *x, const float4 *xf, const double *vh, const double *wh,
@@ -2095,9 +2159,11 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
       const int q = t - first;
       Tape &T = c.tape;
       const bool rec = T.x != nullptr;
-      ka_kick_drift<<<grid_of(n), kAB, 0, st>>>(s, build ? nullptr : h->xref, build ? 1 : 0,
-                                                rec ? T.x + S3 * q : nullptr, rec ? T.vh + S3 * q : nullptr,
-                                                rec ? T.wh + S3 * q : nullptr, rec ? T.xf + (size_t)n * q : nullptr);
+      if (t == first)  // later steps of the segment: kicked and drifted by the previous gather
+        ka_kick_drift<<<grid_of(n), kAB, 0, st>>>(s, build ? nullptr : h->xref, build ? 1 : 0,
+                                                  rec ? T.x + S3 * q : nullptr, rec ? T.vh + S3 * q : nullptr,
+                                                  rec ? T.wh + S3 * q : nullptr,
+                                                  rec ? T.xf + (size_t)n * q : nullptr);
       if (build) {
         rc = build_list(h, c.L, cps[k - 1].L, t);
         if (rc) return rc;
@@ -2126,11 +2192,22 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
         if (s.bonds) AGET(h, T.bh, double, kBondValues * T.ps * nst);
       }
       const bool mrec = rec && s.nmeshes;
+      NextKick nk{};
+      if (t < last) {
+        nk.on = 1;
+        nk.xref = h->xref;
+        if (rec) {
+          nk.tx = T.x + S3 * (q + 1);
+          nk.tv = T.vh + S3 * (q + 1);
+          nk.tw = T.wh + S3 * (q + 1);
+          nk.txf = T.xf + (size_t)n * (q + 1);
+        }
+      }
       force_pass(h, s.v, s.w, 1, t, rec ? T.sh + 3 * T.ps * q : nullptr,
                  rec && s.bonds ? T.bh + kBondValues * T.ps * q : nullptr, rec ? T.ws + W3 * q : nullptr, 1,
                  t == nsteps ? h->wallF : nullptr, rec ? T.F + S3 * q : nullptr, rec ? T.T + S3 * q : nullptr,
                  mrec ? T.mst + NBM * kAMC * q : nullptr, mrec ? T.msh + NBM * kAMC * 3 * q : nullptr,
-                 mrec ? T.mnp + NBM * q : nullptr);
+                 mrec ? T.mnp + NBM * q : nullptr, nk);
     }
     maxnp = std::max(maxnp, c.L.np);
   }
@@ -2284,12 +2361,21 @@ static int adj_run(dem_adjoint *h, double E, double e, double mu, const double *
     const size_t PS = T.ps;
     for (int t = first; t <= last; t++) {
       const int q = t - first;
-      ka_kick_drift<<<grid_of(n), kAB, 0, q2>>>(s2, nullptr, (k > 0 && t == first) ? 1 : 0, T.x + S3 * q,
-                                                T.vh + S3 * q, T.wh + S3 * q, T.xf + (size_t)n * q);
+      if (t == first)  // later steps: kicked and drifted by the previous gather
+        ka_kick_drift<<<grid_of(n), kAB, 0, q2>>>(s2, nullptr, k > 0 ? 1 : 0, T.x + S3 * q, T.vh + S3 * q,
+                                                  T.wh + S3 * q, T.xf + (size_t)n * q);
+      NextKick nk{};
+      if (t < last) {
+        nk.on = 1;
+        nk.tx = T.x + S3 * (q + 1);
+        nk.tv = T.vh + S3 * (q + 1);
+        nk.tw = T.wh + S3 * (q + 1);
+        nk.txf = T.xf + (size_t)n * (q + 1);
+      }
       force_pass_on(s2, q2, T.vh + S3 * q, T.wh + S3 * q, 1, t, T.sh + 3 * PS * q,
                     s.bonds ? T.bh + kBondValues * PS * q : nullptr, T.ws + W3 * q, 1, nullptr, T.F + S3 * q,
                     T.T + S3 * q, s.nmeshes ? T.mst + NBM * kAMC * q : nullptr,
-                    s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr, s.nmeshes ? T.mnp + NBM * q : nullptr);
+                    s.nmeshes ? T.msh + NBM * kAMC * 3 * q : nullptr, s.nmeshes ? T.mnp + NBM * q : nullptr, nk);
     }
   };
   // the mesh slot state before the setup pass (empty) and the slot-history

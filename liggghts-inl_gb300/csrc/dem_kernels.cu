@@ -70,6 +70,9 @@ __device__ __forceinline__ bool ghost_exists(const Sys &s, const AtomArrays &A, 
 // The cells are wider than the neighbour cutoff by a relative 1e-9 at least,
 // far above the rounding of this product, so atoms within the cutoff are
 // never more than one cell apart; every kernel bins through this function.
+// FP32 image shift -1, 0 or +1 times the period, by selection (no conversion)
+__device__ __forceinline__ float fshift(int sv, float prd) { return sv == 0 ? 0.0f : (sv > 0 ? prd : -prd); }
+
 __device__ __forceinline__ int cell_coord(const Sys &s, double x, int d) {
   int c = (int)((x - s.boxlo[d]) * s.icsz[d]);
   c = c < 0 ? 0 : c;
@@ -1174,7 +1177,8 @@ __device__ __forceinline__ void pairs_atom(const Sys &s, const AtomArrays &A, co
           const int code = (sv[0] + 1) + 3 * (sv[1] + 1) + 9 * (sv[2] + 1);
           const int cell = cc[0] + s.nc[0] * (cc[1] + s.nc[1] * cc[2]) + cell_base;
           const int jb = s.cell_start[cell], je = s.cell_start[cell + 1];
-          const float sxf = sv[0] * s.prdf[0], syf = sv[1] * s.prdf[1], szf = sv[2] * s.prdf[2];
+          // image shifts by selection: an int-to-float conversion would issue on the FP64 pipe
+          const float sxf = fshift(sv[0], s.prdf[0]), syf = fshift(sv[1], s.prdf[1]), szf = fshift(sv[2], s.prdf[2]);
           for (int j = jb; j < je; j++) {
             if (code == kNoShift && j <= i) continue;
             // FP32 prefilter of rsq <= (radsum*cdf + skin)^2: candidates
@@ -1716,9 +1720,9 @@ __global__ void __launch_bounds__(kPairTile, MINB) k_pair_pf(Sys s, int shearupd
       const float4 a = s.xf[L.i[p]], b = s.xf[L.j[p]];
       float sx = 0.f, sy = 0.f, sz = 0.f;
       if (code != kNoShift) {
-        sx = (code % 3 - 1) * px;
-        sy = ((code / 3) % 3 - 1) * py;
-        sz = (code / 9 - 1) * pz;
+        sx = fshift(code % 3 - 1, px);
+        sy = fshift((code / 3) % 3 - 1, py);
+        sz = fshift(code / 9 - 1, pz);
       }
       const float fx = a.x - (b.x + sx), fy = a.y - (b.y + sy), fz = a.z - (b.z + sz);
       const float rs = a.w + b.w;
@@ -2345,6 +2349,13 @@ __global__ void __launch_bounds__(kParticleMaxThreads, 4) k_particle(Sys s, int 
   const double trigger = 0.25 * s.skin * s.skin;
   const int tid = threadIdx.x;
   bool moved = false, bad = false;
+  if (GATHER) {
+    if (tid < kGatherKeys) {
+      gcount[tid] = 0;
+      gfill[tid] = 0;
+    }
+    __syncthreads();
+  }
   for (int base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
     const int i = base + tid;
     const bool valid = i < n;
@@ -2365,12 +2376,9 @@ __global__ void __launch_bounds__(kParticleMaxThreads, 4) k_particle(Sys s, int 
         fy = __dmul_rn(massone, s.g[1]);
         fz = __dmul_rn(massone, s.g[2]);
       }
-      // (1) masks; lists longer than 32 entries are summed here by the owner
+      // (1) masks and counts; lists longer than 32 entries are summed here
+      // by the owner (gcount and gfill are zero: cleared after the last use)
       int key = 0;
-      if (tid < kGatherKeys) {
-        gcount[tid] = 0;
-        gfill[tid] = 0;
-      }
       if (valid) {
         int pb, rb;
         unsigned mo, mr;
@@ -2389,7 +2397,6 @@ __global__ void __launch_bounds__(kParticleMaxThreads, 4) k_particle(Sys s, int 
           gather_long(s, L, i, fx, fy, fz, tx, ty, tz);
         }
       }
-      __syncthreads();
       // (2) counting sort of the block's atoms with contacts by their count
       if (key) atomicAdd(&gcount[key], 1);
       __syncthreads();
@@ -2402,6 +2409,10 @@ __global__ void __launch_bounds__(kParticleMaxThreads, 4) k_particle(Sys s, int 
       __syncthreads();
       if (key) gsorted[gstart[key] + atomicAdd(&gfill[key], 1)] = (short)tid;
       __syncthreads();
+      if (tid < kGatherKeys) {  // read by no one until the next block of atoms counts
+        gcount[tid] = 0;
+        gfill[tid] = 0;
+      }
       // (3) the loops, one atom per thread in sorted order
       if (tid < gnq) {
         const int a = gsorted[tid];
