@@ -176,8 +176,12 @@ int dem_add_plane_per_type(dem_handle *h, int axis, const double *pos_by_type, i
  * system takes its own neighbour decision (Neighbor::decide with the
  * every/delay/check settings, src/neighbor.cpp:1362-1378), as it would
  * running alone: a system that does not rebuild keeps its atom order, list
- * and histories while others rebuild.  After dem_set_pair_params
- * (ntypes == nsys), before dem_upload_atoms; no meshes. */
+ * and histories while others rebuild.  The list is laid out in one segment
+ * per system with unused entries at its end, so that a build touches only
+ * the rebuilding systems (dem_stats.ens_inplace_builds); dem_npairs and
+ * dem_download_contacts leave the unused entries out.  After
+ * dem_set_pair_params (ntypes == nsys), before dem_upload_atoms; no meshes,
+ * no insertion. */
 int dem_set_ensemble(dem_handle *h, int nsys);
 /* Neighbour list builds of each ensemble system (Neighbor::ncalls of that
  * system run alone, including the setup build): counts[nsys]. */

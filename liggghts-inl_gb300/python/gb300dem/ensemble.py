@@ -18,10 +18,12 @@ bandwidth-bound one:
     at its own height, with wall type = the atom's type;
   * tags are offset per system so that they stay unique.
 
-A neighbour rebuild is decided for the ensemble as a whole (any atom of any
-system beyond skin/2 rebuilds every system).  Each system therefore evolves
-exactly as a standalone run of the same model that rebuilds at those steps;
-the rebuild steps are the only coupling.
+Each system takes its own neighbour decision, as it would running alone
+(Neighbor::decide, src/neighbor.cpp:1362-1378): a system rebuilds when one
+of its own atoms moved beyond skin/2, and the others keep their atom order,
+list entries and histories.  A build touches only the rebuilding systems'
+atoms and list segments.  Each system therefore evolves exactly as its
+standalone run, rebuild steps included; the systems do not interact.
 
 The autotuner times short runs of the packed ensemble over launch shapes
 (blocks per SM, dem_set_tuning; threads per block of the per-particle
