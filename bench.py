@@ -197,6 +197,79 @@ class Clocks:
                 "samples": len(sm)}
 
 
+class NvmlClocks:
+    """SM clock and clock-event reasons sampled through NVML (libnvidia-ml,
+    read-only queries) by a thread that polls every half millisecond while
+    the timed region runs, so that even a few-millisecond region has
+    samples.  The region's dem_step is a ctypes call, which releases the
+    GIL.  Falls back to the nvidia-smi sampler (Clocks) where NVML cannot be
+    loaded."""
+    # nvmlClocksEventReasons bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self):
+        import ctypes
+        self.ct = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        idx = 0
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0].strip()
+        if vis.isdigit():
+            idx = int(vis)
+        cnt = ctypes.c_uint(0)
+        self.lib.nvmlDeviceGetCount_v2(ctypes.byref(cnt))
+        if idx >= cnt.value:
+            idx = 0
+        self.h = ctypes.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(idx), ctypes.byref(self.h)) != 0:
+            raise RuntimeError("nvmlDeviceGetHandleByIndex failed")
+        self.get_reasons = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.samples, self.reasons = [], set()
+        self.thread, self.stop_flag = None, False
+
+    def _sample(self):
+        ct = self.ct
+        clk, rs = ct.c_uint(0), ct.c_ulonglong(0)
+        if self.lib.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk)) == 0:  # NVML_CLOCK_SM
+            self.samples.append(float(clk.value))
+        if self.get_reasons(self.h, ct.byref(rs)) == 0:
+            for bit, name in self.REASONS.items():
+                if rs.value & bit:
+                    self.reasons.add(name)
+
+    def _run(self):
+        while not self.stop_flag:
+            self._sample()
+            time.sleep(0.0005)
+
+    def start(self):
+        import threading
+        self._sample()
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.thread.start()
+
+    def stop(self):
+        self.stop_flag = True
+        self.thread.join(timeout=5)
+        self._sample()
+        mx = self.ct.c_uint(0)
+        self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, self.ct.byref(mx))
+        if not self.samples:
+            return None
+        return {"sm_mhz": statistics.median(self.samples), "sm_max_mhz": float(mx.value),
+                "reasons": sorted(self.reasons), "samples": len(self.samples), "source": "nvml"}
+
+
+def clock_sampler():
+    try:
+        return NvmlClocks()
+    except Exception:
+        return Clocks()
+
+
 def measured_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -390,7 +463,7 @@ def run_gb300(args):
     # ---- headline: device-timed K steps, state resident
     if dist:
         dist.barrier()
-    clocks = Clocks()
+    clocks = clock_sampler()
     clocks.start()
     g.profile(False)
     t0 = time.perf_counter()
@@ -547,7 +620,7 @@ def run_ensemble(args):
     e = ensemble.Ensemble(systems, tuning=(best[0], best[1], best[3]))
     e.setup()
     e.step(args.warmup)
-    clocks = Clocks()
+    clocks = clock_sampler()
     clocks.start()
     e.step(args.steps)
     cl = clocks.stop()
