@@ -141,8 +141,15 @@ __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &
   // ---- normal model
   double kn, kt, gamman, gammat;
   if (NORMAL == kHertz) {
-    const double sqrtval = sqrt(c.reff * deltan);
-    const double q = sqrt(sqrtval);
+    // sqrt(reff*deltan) and its square root from two reciprocal square
+    // roots (x^-1/2, then (x^-1/2)^-1/2 = x^1/4): within an ulp or two of
+    // the correctly rounded sqrt, with fewer FP64 instructions and no divide
+    // (zero for a contact at zero overlap, as sqrt(0) gives)
+    const double xr = c.reff * deltan;
+    const bool pos = xr > 0.0;
+    const double rs = rsqrt(pos ? xr : 1.0);
+    const double sqrtval = pos ? xr * rs : 0.0;
+    const double q = pos ? rsqrt(rs) : 0.0;
     kn = tp.Y43 * sqrtval;
     kt = tp.G8 * sqrtval;
     gamman = c.c0 * q;
@@ -170,9 +177,11 @@ __device__ __forceinline__ void contact_law(const ContactIn &c, const TypePair &
   double Ft1, Ft2, Ft3;
   const double ss = s0 * s0 + s1 * s1 + s2 * s2;
   const double Ft_friction = tp.mu * fabs(Fn);
-  if (kt * kt * ss > Ft_friction * Ft_friction) {
-    // sliding (ss > 0 here): cap the spring force at mu|Fn|
-    const double ratio = Ft_friction * rsqrt(ss) / kt;
+  const double kt2ss = kt * kt * ss;
+  if (kt2ss > Ft_friction * Ft_friction) {
+    // sliding (ss > 0 here): cap the spring force at mu|Fn|;
+    // mu|Fn| / (kt |shear|) with one reciprocal square root, no divide
+    const double ratio = Ft_friction * rsqrt(kt2ss);
     Ft1 = -(kt * s0) * ratio;
     Ft2 = -(kt * s1) * ratio;
     Ft3 = -(kt * s2) * ratio;
