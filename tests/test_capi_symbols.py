@@ -67,3 +67,36 @@ def test_host_table_derivation_matches_reference_formulas():
     assert L.dem_derive_hertz_tables(2, p(Ea), p(nua), p(ea), p(Y), p(G), p(B), p(R)) == 0
     assert np.array_equal(Y, ref["Yeff"]) and np.array_equal(G, ref["Geff"])
     assert np.array_equal(B, ref["betaeff"]) and np.array_equal(R, ref["coeffRestLog"])
+
+
+def test_ctypes_structures_match_the_header_layout(tmp_path):
+    """Every struct of include/liggghts_gb300.h that the ctypes binding
+    mirrors has the header's size and field offsets: a C program built with
+    gcc from the header prints them, field names taken from the binding."""
+    import shutil
+    import subprocess
+    from gb300dem import adjoint
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        import pytest
+        pytest.skip("no C compiler")
+    mirrors = {"dem_config": api.DemConfig, "dem_bond_settings": api.DemBondSettings,
+               "dem_stats": api.DemStats, "dem_kernel_times": api.DemKernelTimes,
+               "dem_diagnostics": api.DemDiagnostics, "dem_adjoint_config": adjoint.DemAdjointConfig,
+               "dem_adjoint_loss": adjoint.DemAdjointLoss}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "liggghts_gb300.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (cname, cname))
+        for fname, _ in py._fields_:
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (cname, fname, cname, fname))
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    for cname, py in mirrors.items():
+        assert int(got[cname]) == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(got["%s.%s" % (cname, fname)]) == getattr(py, fname).offset, (cname, fname)
