@@ -29,6 +29,7 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 METRIC = "particle-steps/s (1M Hertz/history spheres)"
+REF_MAX_STEPS = 100  # timed steps per reference process (--impl reference)
 METRICS = {"fibres200k": "particle-steps/s (200k bonded fibre spheres)"}
 
 # Per-unit figures of the two step kernels (the roofline multiplies them by
@@ -385,8 +386,11 @@ def run_reference(args):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    steps = max(1, args.steps)
-    warm = max(1, args.warmup)
+    # a bounded sample: at most REF_MAX_STEPS timed steps of the full
+    # workload per process (the metric is a rate), so that a long K still
+    # ends within a few minutes
+    steps = max(1, min(args.steps, REF_MAX_STEPS))
+    warm = max(1, min(args.warmup, 5))
     t0 = time.perf_counter()
     exe = ref_binary()
     if exe:
@@ -413,7 +417,8 @@ def run_reference(args):
         ms = 1e3 * max(r[2] for r in res) / steps
     wall = time.perf_counter() - t0
     line = {"metric": METRICS.get(args.workload, METRIC), "value": val, "unit": "particle-steps/s",
-            "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup, "ms_per_step": ms,
+            "n_gpus": args.gpus, "steps": args.steps, "timed_steps_per_process": steps,
+            "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)", "impl": "reference", "config": config,
             "cpu_baseline": {"value": val, "unit": "particle-steps/s", "cores": cores, "kind": kind,
