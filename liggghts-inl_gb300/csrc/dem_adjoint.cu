@@ -127,7 +127,7 @@ struct ADev {
   // FP32 mirror of the positions and radii (x, y, z, r) for the candidate
   // tests; fm: the distance margin that covers its rounding
   float4 *xf;
-  float fm, prdf[3];
+  float fm, prdf[3], cdff;  // cdff: (float)cdf
   // per-atom kick constants of the run: ka = dtf/m, kb = dtfrot/(r^2 m) and
   // the factors of their derivatives ka/m, kb/m, 2 kb/r
   double *ka, *kb, *kam, *kbm, *kbr;
@@ -171,7 +171,7 @@ __device__ __forceinline__ void a_image(const ADev &s, int code, double xj[3]) {
   if (code == kNoShift) return;
   const int sv[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
   for (int d = 0; d < 3; d++)
-    if (sv[d]) xj[d] = __dadd_rn(xj[d], sv[d] * s.prd[d]);
+    if (sv[d]) xj[d] = __dadd_rn(xj[d], sv[d] > 0 ? s.prd[d] : -s.prd[d]);  // by selection: no FP64 convert
 }
 
 // FP32 candidate test of entry p against the contact distance (ri + rj) cdf:
@@ -182,12 +182,14 @@ __device__ __forceinline__ bool pair_candidate(const ADev &s, const float4 *xf, 
   float bx = b.x, by = b.y, bz = b.z;
   const int code = s.sh[p];
   if (code != kNoShift) {
-    bx += (float)(code % 3 - 1) * s.prdf[0];
-    by += (float)((code / 3) % 3 - 1) * s.prdf[1];
-    bz += (float)(code / 9 - 1) * s.prdf[2];
+    // shifts by selection (no conversions)
+    const int sx = code % 3 - 1, sy = (code / 3) % 3 - 1, sz = code / 9 - 1;
+    bx += sx == 0 ? 0.f : (sx > 0 ? s.prdf[0] : -s.prdf[0]);
+    by += sy == 0 ? 0.f : (sy > 0 ? s.prdf[1] : -s.prdf[1]);
+    bz += sz == 0 ? 0.f : (sz > 0 ? s.prdf[2] : -s.prdf[2]);
   }
   const float dx = a.x - bx, dy = a.y - by, dz = a.z - bz;
-  const float R = (a.w + b.w) * (float)s.cdf + s.fm;
+  const float R = (a.w + b.w) * s.cdff + s.fm;
   return dx * dx + dy * dy + dz * dz <= R * R;
 }
 
@@ -1819,6 +1821,7 @@ int dem_adjoint_create(const dem_adjoint_config *cfg, dem_adjoint **out) {
   s.dtfrot = s.dtf / 0.4;
   s.bonds = 0;
   s.cdf = 1.0;
+  s.cdff = 1.0f;
   s.nmeshes = 0;
   s.rolling = 0;
   s.mur = 0.0;
@@ -1949,6 +1952,7 @@ int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *
       one = 0.5 * 1.1 * s.bp.t[kBondCreateDist] / minrad + 0.5 * 1.1 * stress / (s.bp.t[kBondKfn2] * minrad);
     }
     s.cdf = std::max(1.0, one);
+    s.cdff = (float)s.cdf;
     if (s.cdf > 10.0) {
       h->err = "bond distance above 10 particle diameters";
       return DEM_ERR_BAD_ARG;

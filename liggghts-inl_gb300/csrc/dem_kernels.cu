@@ -45,9 +45,11 @@ __device__ __forceinline__ void image(const Sys &s, int code, double &xj, double
   if (code == kNoShift) return;
   int sx, sy, sz;
   shift_decode(code, sx, sy, sz);
-  if (sx) xj = __dadd_rn(xj, sx * s.prd[0]);
-  if (sy) yj = __dadd_rn(yj, sy * s.prd[1]);
-  if (sz) zj = __dadd_rn(zj, sz * s.prd[2]);
+  // +-prd by selection: sx * prd would convert sx to FP64 and multiply on
+  // the FP64 pipe (and the compiler hoists that out of candidate loops)
+  if (sx) xj = __dadd_rn(xj, sx > 0 ? s.prd[0] : -s.prd[0]);
+  if (sy) yj = __dadd_rn(yj, sy > 0 ? s.prd[1] : -s.prd[1]);
+  if (sz) zj = __dadd_rn(zj, sz > 0 ? s.prd[2] : -s.prd[2]);
 }
 
 // Whether the periodic image of j (shift sv) exists as a ghost atom:
@@ -1105,6 +1107,57 @@ __global__ void __launch_bounds__(256) k_wall_list(Sys s) {
 // again only for atoms with more.
 // ----------------------------------------------------------------------------
 
+// One run of candidates [jb, je) of the cell-sorted order, all with image
+// code `code` (shift sv): FP32 prefilter of rsq <= (radsum*cdf + skin)^2;
+// candidates clearly outside (or clearly inside) by more than the bound of
+// the FP32 rounding are decided without FP64; the rest, and every entry the
+// fill pass writes, use the exact FP64 test.
+template <bool FILL>
+__device__ __forceinline__ void pairs_scan(const Sys &s, const AtomArrays &A, const PairArrays &M, int i,
+                                           const float4 &pi, double xi, double yi, double zi, double radi,
+                                           float cdff, float skinf, float hi_f, float lo_f, int jb, int je,
+                                           int code, const int sv[3], int &cnt, int &out, int out_end) {
+  // image shifts by selection: an int-to-float conversion would issue on the FP64 pipe
+  const float sxf = fshift(sv[0], s.prdf[0]), syf = fshift(sv[1], s.prdf[1]), szf = fshift(sv[2], s.prdf[2]);
+  for (int j = jb; j < je; j++) {
+    if (code == kNoShift && j <= i) continue;
+    const float4 pj = s.xf[j];
+    const float fx = pi.x - (pj.x + sxf), fy = pi.y - (pj.y + syf), fz = pi.z - (pj.z + szf);
+    const float rsqf = fx * fx + fy * fy + fz * fz;
+    const float csf = (pi.w + pj.w) * cdff + skinf;
+    const float cs2f = csf * csf;
+    if (rsqf > cs2f * hi_f) continue;
+    if (code != kNoShift && !ghost_exists(s, A, j, sv)) continue;
+    const bool clear_in = rsqf < cs2f * lo_f;
+    if (!FILL && clear_in) {
+      if (cnt < kStash) s.stash[(size_t)cnt * s.nmax + i] = j | (code << 24);
+      cnt++;
+      continue;
+    }
+    double xj = A.x[j], yj = A.y[j], zj = A.z[j];
+    image(s, code, xj, yj, zj);
+    const double delx = __dadd_rn(xi, -xj);
+    const double dely = __dadd_rn(yi, -yj);
+    const double delz = __dadd_rn(zi, -zj);
+    const double rsq = rsq_rn(delx, dely, delz);
+    const double radj = A.r[j];
+    const double radsum = __dmul_rn(__dadd_rn(radi, radj), s.cdf);
+    const double cs = __dadd_rn(radsum, s.skin);
+    if (!(rsq <= __dmul_rn(cs, cs))) continue;
+    if (!FILL) {
+      if (cnt < kStash) s.stash[(size_t)cnt * s.nmax + i] = j | (code << 24);
+      cnt++;
+      continue;
+    }
+    if (out >= out_end) continue;  // count and fill passes agree; guard only
+    const int p = out++;
+    M.i[p] = i;
+    M.j[p] = j;
+    M.sh[p] = (uint8_t)code;
+    if (s.nsys) M.rev[p] = -1;  // a fresh entry (source of copied ones: see pairs_atom)
+  }
+}
+
 template <bool FILL>
 __device__ __forceinline__ void pairs_atom(const Sys &s, const AtomArrays &A, const PairArrays &L,
                                            const PairArrays &M, int i) {
@@ -1153,73 +1206,60 @@ __device__ __forceinline__ void pairs_atom(const Sys &s, const AtomArrays &A, co
     int cnt = 0;
     int out = FILL ? M.row[i] : 0;
     const int out_end = FILL ? row_end(s, M, i) : 0;
-    for (int oz = -1; oz <= 1; oz++) {
-      for (int oy = -1; oy <= 1; oy++) {
-        for (int ox = -1; ox <= 1; ox++) {
-          const int o[3] = {ox, oy, oz};
-          int cc[3], sv[3] = {0, 0, 0};
-          bool skip = false;
+    // per dimension: the neighbour coordinate, image shift and validity of
+    // the offsets -1, 0, +1
+    int nb[3][3], sv3[3][3];
+    bool ok3[3][3];
 #pragma unroll
-          for (int d = 0; d < 3; d++) {
-            cc[d] = ci[d] + o[d];
-            if (s.nc[d] == 1 && o[d] != 0) skip = true;
-            if (cc[d] < 0) {
-              if (!s.periodic[d]) skip = true;
-              cc[d] += s.nc[d];
-              sv[d] = -1;
-            } else if (cc[d] >= s.nc[d]) {
-              if (!s.periodic[d]) skip = true;
-              cc[d] -= s.nc[d];
-              sv[d] = 1;
-            }
-          }
-          if (skip) continue;
-          const int code = (sv[0] + 1) + 3 * (sv[1] + 1) + 9 * (sv[2] + 1);
-          const int cell = cc[0] + s.nc[0] * (cc[1] + s.nc[1] * cc[2]) + cell_base;
-          const int jb = s.cell_start[cell], je = s.cell_start[cell + 1];
-          // image shifts by selection: an int-to-float conversion would issue on the FP64 pipe
-          const float sxf = fshift(sv[0], s.prdf[0]), syf = fshift(sv[1], s.prdf[1]), szf = fshift(sv[2], s.prdf[2]);
-          for (int j = jb; j < je; j++) {
-            if (code == kNoShift && j <= i) continue;
-            // FP32 prefilter of rsq <= (radsum*cdf + skin)^2: candidates
-            // clearly outside (or clearly inside) by more than the bound of
-            // the FP32 rounding are decided without FP64; the rest, and
-            // every entry the fill pass writes, use the exact FP64 test.
-            const float4 pj = s.xf[j];
-            const float fx = pi.x - (pj.x + sxf), fy = pi.y - (pj.y + syf), fz = pi.z - (pj.z + szf);
-            const float rsqf = fx * fx + fy * fy + fz * fz;
-            const float csf = (pi.w + pj.w) * cdff + skinf;
-            const float cs2f = csf * csf;
-            if (rsqf > cs2f * hi_f) continue;
-            if (code != kNoShift && !ghost_exists(s, A, j, sv)) continue;
-            const bool clear_in = rsqf < cs2f * lo_f;
-            if (!FILL && clear_in) {
-              if (cnt < kStash) s.stash[(size_t)cnt * s.nmax + i] = j | (code << 24);
-              cnt++;
-              continue;
-            }
-            double xj = A.x[j], yj = A.y[j], zj = A.z[j];
-            image(s, code, xj, yj, zj);
-            const double delx = __dadd_rn(xi, -xj);
-            const double dely = __dadd_rn(yi, -yj);
-            const double delz = __dadd_rn(zi, -zj);
-            const double rsq = rsq_rn(delx, dely, delz);
-            const double radj = A.r[j];
-            const double radsum = __dmul_rn(__dadd_rn(radi, radj), s.cdf);
-            const double cs = __dadd_rn(radsum, s.skin);
-            if (!(rsq <= __dmul_rn(cs, cs))) continue;
-            if (!FILL) {
-              if (cnt < kStash) s.stash[(size_t)cnt * s.nmax + i] = j | (code << 24);
-              cnt++;
-              continue;
-            }
-            if (out >= out_end) continue;  // count and fill passes agree; guard only
-            const int p = out++;
-            M.i[p] = i;
-            M.j[p] = j;
-            M.sh[p] = (uint8_t)code;
-            if (s.nsys) M.rev[p] = -1;  // a fresh entry (source of copied ones: see above)
-          }
+    for (int d = 0; d < 3; d++) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        const int o = k - 1;
+        int cc = ci[d] + o, sv = 0;
+        bool ok = !(s.nc[d] == 1 && o != 0);
+        if (cc < 0) {
+          ok = ok && s.periodic[d];
+          cc += s.nc[d];
+          sv = -1;
+        } else if (cc >= s.nc[d]) {
+          ok = ok && s.periodic[d];
+          cc -= s.nc[d];
+          sv = 1;
+        }
+        nb[d][k] = cc;
+        sv3[d][k] = sv;
+        ok3[d][k] = ok;
+      }
+    }
+    // the 27 cells in the stencil's order (z, then y, then x offsets): along
+    // x the unwrapped cells of a row are consecutive, so their atoms are one
+    // contiguous run of the cell-sorted order, scanned in one loop (the same
+    // candidates in the same order as cell by cell); a cell that wraps
+    // around a periodic x boundary is scanned alone, with its image shift
+    const bool lwrap = ok3[0][0] && sv3[0][0] != 0, rwrap = ok3[0][2] && sv3[0][2] != 0;
+    const int x0 = (ok3[0][0] && !lwrap) ? nb[0][0] : nb[0][1];
+    const int x1 = (ok3[0][2] && !rwrap) ? nb[0][2] : nb[0][1];
+#pragma unroll
+    for (int kz = 0; kz < 3; kz++) {
+#pragma unroll
+      for (int ky = 0; ky < 3; ky++) {
+        if (!ok3[2][kz] || !ok3[1][ky]) continue;
+        const int rowb = s.nc[0] * (nb[1][ky] + s.nc[1] * nb[2][kz]) + cell_base;
+        const int syz = 3 * (sv3[1][ky] + 1) + 9 * (sv3[2][kz] + 1);
+        if (lwrap) {
+          const int sv[3] = {-1, sv3[1][ky], sv3[2][kz]};
+          pairs_scan<FILL>(s, A, M, i, pi, xi, yi, zi, radi, cdff, skinf, hi_f, lo_f, s.cell_start[rowb + nb[0][0]],
+                           s.cell_start[rowb + nb[0][0] + 1], syz, sv, cnt, out, out_end);
+        }
+        {
+          const int sv[3] = {0, sv3[1][ky], sv3[2][kz]};
+          pairs_scan<FILL>(s, A, M, i, pi, xi, yi, zi, radi, cdff, skinf, hi_f, lo_f, s.cell_start[rowb + x0],
+                           s.cell_start[rowb + x1 + 1], 1 + syz, sv, cnt, out, out_end);
+        }
+        if (rwrap) {
+          const int sv[3] = {1, sv3[1][ky], sv3[2][kz]};
+          pairs_scan<FILL>(s, A, M, i, pi, xi, yi, zi, radi, cdff, skinf, hi_f, lo_f, s.cell_start[rowb + nb[0][2]],
+                           s.cell_start[rowb + nb[0][2] + 1], 2 + syz, sv, cnt, out, out_end);
         }
       }
     }

@@ -95,9 +95,9 @@ __global__ void na_pairs(NaArgs a) {
       continue;
     }
     double xj = a.x[3 * j], yj = a.x[3 * j + 1], zj = a.x[3 * j + 2];
-    if (sx) xj = __dadd_rn(xj, sx * a.prd[0]);
-    if (sy) yj = __dadd_rn(yj, sy * a.prd[1]);
-    if (sz) zj = __dadd_rn(zj, sz * a.prd[2]);
+    if (sx) xj = __dadd_rn(xj, sx > 0 ? a.prd[0] : -a.prd[0]);  // +-prd by selection, as the
+    if (sy) yj = __dadd_rn(yj, sy > 0 ? a.prd[1] : -a.prd[1]);  // resident path's image()
+    if (sz) zj = __dadd_rn(zj, sz > 0 ? a.prd[2] : -a.prd[2]);
     const double delx = __dadd_rn(a.x[3 * i], -xj);
     const double dely = __dadd_rn(a.x[3 * i + 1], -yj);
     const double delz = __dadd_rn(a.x[3 * i + 2], -zj);
