@@ -127,7 +127,7 @@ struct ADev {
   // FP32 mirror of the positions and radii (x, y, z, r) for the candidate
   // tests; fm: the distance margin that covers its rounding
   float4 *xf;
-  float fm, prdf[3], cdff;  // cdff: (float)cdf
+  float fm, prdf[3];
   // per-atom kick constants of the run: ka = dtf/m, kb = dtfrot/(r^2 m) and
   // the factors of their derivatives ka/m, kb/m, 2 kb/r
   double *ka, *kb, *kam, *kbm, *kbr;
@@ -171,7 +171,7 @@ __device__ __forceinline__ void a_image(const ADev &s, int code, double xj[3]) {
   if (code == kNoShift) return;
   const int sv[3] = {code % 3 - 1, (code / 3) % 3 - 1, code / 9 - 1};
   for (int d = 0; d < 3; d++)
-    if (sv[d]) xj[d] = __dadd_rn(xj[d], sv[d] > 0 ? s.prd[d] : -s.prd[d]);  // by selection: no FP64 convert
+    if (sv[d]) xj[d] = __dadd_rn(xj[d], sv[d] * s.prd[d]);
 }
 
 // FP32 candidate test of entry p against the contact distance (ri + rj) cdf:
@@ -182,14 +182,12 @@ __device__ __forceinline__ bool pair_candidate(const ADev &s, const float4 *xf, 
   float bx = b.x, by = b.y, bz = b.z;
   const int code = s.sh[p];
   if (code != kNoShift) {
-    // shifts by selection (no conversions)
-    const int sx = code % 3 - 1, sy = (code / 3) % 3 - 1, sz = code / 9 - 1;
-    bx += sx == 0 ? 0.f : (sx > 0 ? s.prdf[0] : -s.prdf[0]);
-    by += sy == 0 ? 0.f : (sy > 0 ? s.prdf[1] : -s.prdf[1]);
-    bz += sz == 0 ? 0.f : (sz > 0 ? s.prdf[2] : -s.prdf[2]);
+    bx += (float)(code % 3 - 1) * s.prdf[0];
+    by += (float)((code / 3) % 3 - 1) * s.prdf[1];
+    bz += (float)(code / 9 - 1) * s.prdf[2];
   }
   const float dx = a.x - bx, dy = a.y - by, dz = a.z - bz;
-  const float R = (a.w + b.w) * s.cdff + s.fm;
+  const float R = (a.w + b.w) * (float)s.cdf + s.fm;
   return dx * dx + dy * dy + dz * dz <= R * R;
 }
 
@@ -287,6 +285,37 @@ __global__ void ka_cellsort(ADev s) {
 // granular half list in input order: local pairs once (owner = lower index),
 // periodic images as directed entries of each owner; cutoff
 // (ri + rj) cdf + skin (src/neigh_gran.cpp:580-586)
+// candidates [qb, qe) of the cell-sorted order (s.order), all with image
+// code `code`
+template <bool FILL>
+__device__ __forceinline__ void ka_scan(const ADev &s, int i, const double xi[3], double ri, int qb, int qe,
+                                        int code, int &cnt, int &out, int out_end, int *pi, int *pj,
+                                        uint8_t *shc) {
+  for (int q = qb; q < qe; q++) {
+    const int j = s.order[q];
+    if (code == kNoShift && j <= i) continue;
+    double xj[3] = {s.x[3 * j], s.x[3 * j + 1], s.x[3 * j + 2]};
+    a_image(s, code, xj);
+    const double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
+    const double cs = (ri + s.r[j]) * s.cdf + s.skin;
+    if (dx * dx + dy * dy + dz * dz > cs * cs) continue;
+    if (!FILL) {
+      cnt++;
+      continue;
+    }
+    if (out >= out_end) continue;
+    pi[out] = i;
+    pj[out] = j;
+    shc[out] = (uint8_t)code;
+    out++;
+  }
+}
+
+// The 27 cells in the stencil's order (z, then y, then x offsets); along x
+// the unwrapped cells of a row are consecutive cells, whose atoms form one
+// contiguous run of the cell-sorted order, scanned in one loop (the same
+// candidates in the same order as cell by cell); a cell that wraps around a
+// periodic x boundary is scanned alone, with its image shift.
 template <bool FILL>
 __global__ void ka_pairs(ADev s, int *pi, int *pj, uint8_t *shc, const int *row) {
   AGRID(i, s.n) {
@@ -296,46 +325,48 @@ __global__ void ka_pairs(ADev s, int *pi, int *pj, uint8_t *shc, const int *row)
     for (int d = 0; d < 3; d++) ci[d] = a_cell_coord(s, xi[d], d);
     int cnt = 0, out = FILL ? row[i] : 0;
     const int out_end = FILL ? row[i + 1] : 0;
-    for (int oz = -1; oz <= 1; oz++)
-      for (int oy = -1; oy <= 1; oy++)
-        for (int ox = -1; ox <= 1; ox++) {
-          const int o[3] = {ox, oy, oz};
-          int cc[3], sv[3] = {0, 0, 0};
-          bool skip = false;
-          for (int d = 0; d < 3; d++) {
-            cc[d] = ci[d] + o[d];
-            if (cc[d] < 0) {
-              if (!s.per[d]) skip = true;
-              cc[d] += s.nc[d];
-              sv[d] = -1;
-            } else if (cc[d] >= s.nc[d]) {
-              if (!s.per[d]) skip = true;
-              cc[d] -= s.nc[d];
-              sv[d] = 1;
-            }
-          }
-          if (skip) continue;
-          const int code = (sv[0] + 1) + 3 * (sv[1] + 1) + 9 * (sv[2] + 1);
-          const int cell = cc[0] + s.nc[0] * (cc[1] + s.nc[1] * cc[2]);
-          for (int q = s.cell_start[cell]; q < s.cell_start[cell + 1]; q++) {
-            const int j = s.order[q];
-            if (code == kNoShift && j <= i) continue;
-            double xj[3] = {s.x[3 * j], s.x[3 * j + 1], s.x[3 * j + 2]};
-            a_image(s, code, xj);
-            const double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
-            const double cs = (ri + s.r[j]) * s.cdf + s.skin;
-            if (dx * dx + dy * dy + dz * dz > cs * cs) continue;
-            if (!FILL) {
-              cnt++;
-              continue;
-            }
-            if (out >= out_end) continue;
-            pi[out] = i;
-            pj[out] = j;
-            shc[out] = (uint8_t)code;
-            out++;
-          }
+    int nb[3][3], sv3[3][3];
+    bool ok3[3][3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        int cc = ci[d] + k - 1, sv = 0;
+        bool ok = true;
+        if (cc < 0) {
+          ok = s.per[d] != 0;
+          cc += s.nc[d];
+          sv = -1;
+        } else if (cc >= s.nc[d]) {
+          ok = s.per[d] != 0;
+          cc -= s.nc[d];
+          sv = 1;
         }
+        nb[d][k] = cc;
+        sv3[d][k] = sv;
+        ok3[d][k] = ok;
+      }
+    }
+    const bool lwrap = ok3[0][0] && sv3[0][0] != 0, rwrap = ok3[0][2] && sv3[0][2] != 0;
+    const int x0 = (ok3[0][0] && !lwrap) ? nb[0][0] : nb[0][1];
+    const int x1 = (ok3[0][2] && !rwrap) ? nb[0][2] : nb[0][1];
+#pragma unroll
+    for (int kz = 0; kz < 3; kz++) {
+#pragma unroll
+      for (int ky = 0; ky < 3; ky++) {
+        if (!ok3[2][kz] || !ok3[1][ky]) continue;
+        const int rowb = s.nc[0] * (nb[1][ky] + s.nc[1] * nb[2][kz]);
+        const int syz = 3 * (sv3[1][ky] + 1) + 9 * (sv3[2][kz] + 1);
+        if (lwrap)
+          ka_scan<FILL>(s, i, xi, ri, s.cell_start[rowb + nb[0][0]], s.cell_start[rowb + nb[0][0] + 1], syz, cnt,
+                        out, out_end, pi, pj, shc);
+        ka_scan<FILL>(s, i, xi, ri, s.cell_start[rowb + x0], s.cell_start[rowb + x1 + 1], 1 + syz, cnt, out,
+                      out_end, pi, pj, shc);
+        if (rwrap)
+          ka_scan<FILL>(s, i, xi, ri, s.cell_start[rowb + nb[0][2]], s.cell_start[rowb + nb[0][2] + 1], 2 + syz,
+                        cnt, out, out_end, pi, pj, shc);
+      }
+    }
     if (!FILL) s.pcount[i] = cnt;
   }
 }
@@ -1821,7 +1852,6 @@ int dem_adjoint_create(const dem_adjoint_config *cfg, dem_adjoint **out) {
   s.dtfrot = s.dtf / 0.4;
   s.bonds = 0;
   s.cdf = 1.0;
-  s.cdff = 1.0f;
   s.nmeshes = 0;
   s.rolling = 0;
   s.mur = 0.0;
@@ -1952,7 +1982,6 @@ int dem_adjoint_set_state(dem_adjoint *h, int n, const double *x, const double *
       one = 0.5 * 1.1 * s.bp.t[kBondCreateDist] / minrad + 0.5 * 1.1 * stress / (s.bp.t[kBondKfn2] * minrad);
     }
     s.cdf = std::max(1.0, one);
-    s.cdff = (float)s.cdf;
     if (s.cdf > 10.0) {
       h->err = "bond distance above 10 particle diameters";
       return DEM_ERR_BAD_ARG;
