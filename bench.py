@@ -486,8 +486,13 @@ def run_gb300(args):
     # ---- e2e through the C ABI with host buffers
     # (the caller's host arrays exist before the run, as the reference's
     # atom->x, atom->v, ... do; the device reads and fills them)
+    # The caller's arrays are written by the host just before (as the
+    # reference's atom->x, atom->v, ... are), not the workload's arrays that
+    # the first upload above already read: pages the device has read may be
+    # migrating to its memory (access-counter migration), which made the
+    # read of those same pages 1.6 to 10.5 ms from run to run
     a = case["atoms"]
-    host = {k: np.ascontiguousarray(v) for k, v in a.items()}
+    host = {k: np.array(v, copy=True, order="C") for k, v in a.items()}
     g2 = api.DemSystem({k: v for k, v in case.items() if k != "atoms"})
     hout = g2.atom_buffers(n)
     t0 = time.perf_counter()
