@@ -329,7 +329,9 @@ def lmp_sample(name, nproc, steps, warm, seed=2024, case=None):
     n0 = len(case["atoms"]["tag"])
     top = tempfile.mkdtemp(prefix="lmp_ref_")
     try:
-        write_inputs(case, top, 0, runs=[warm, steps])
+        # the reference's own spatial sort on (its default, "sort 1000 0"):
+        # its fastest setting; the parity runs keep the atoms' order instead
+        write_inputs(case, top, 0, runs=[warm, steps], atom_sort="1000 0")
         files = [f for f in os.listdir(top) if os.path.isfile(os.path.join(top, f))]
         procs = []
         for k in range(nproc):
@@ -398,8 +400,8 @@ def run_reference(args):
         pv, pres = cpu_sample(args.workload, 1, steps, warm=1, scale=1.0)
         kind = "reference"
         sample = ("reference binary (oracle/_ref/lmp_ref: unmodified reference sources, serial, -O3, "
-                  "whitelisted contact models) on the full %d-atom %s, %d independent processes "
-                  "(one per core), 'run %d' then the timed 'run %d' (its Loop time)"
+                  "whitelisted contact models, atom_modify sort 1000 0) on the full %d-atom %s, %d "
+                  "independent processes (one per core), 'run %d' then the timed 'run %d' (its Loop time)"
                   % (res[0][0], args.workload, cores, warm, steps))
         per_proc = statistics.mean(n * s / t for n, s, t in res)
         port = {"value": pv, "cores": 1, "per_process_binary": per_proc, "port_over_binary": pv / per_proc,
@@ -578,7 +580,8 @@ def run_gb300(args):
         if ref_binary() and args.scale == 1.0:
             v, res = lmp_sample(args.workload, 1, args.cpu_steps, 1, case=case if restart else None)
             cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "reference",
-                   "sample": "reference binary (oracle/_ref/lmp_ref, serial, -O3) on the full %d-atom %s%s, "
+                   "sample": "reference binary (oracle/_ref/lmp_ref, serial, -O3, sort 1000 0) on the full "
+                             "%d-atom %s%s, "
                              "'run 1' then the timed 'run %d' (its Loop time), 1 process"
                              % (res[0][0], args.workload,
                                 " (the settled positions, read_data without contact history)" if restart else "",

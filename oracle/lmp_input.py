@@ -28,7 +28,8 @@ def fmt(v):
 DUMP_COLUMNS = ("id type x y z vx vy vz omegax omegay omegaz fx fy fz tqx tqy tqz radius")
 
 
-def write_inputs(case, d, nsteps, snaps=None, dump_every=None, extra=(), run_style=False, runs=None):
+def write_inputs(case, d, nsteps, snaps=None, dump_every=None, extra=(), run_style=False, runs=None,
+                 atom_sort="0 0"):
     """Writes data.case and in.case (plus mesh STL files) into d.
 
     snaps: steps at which the snapshot fix of the reference build writes its
@@ -41,7 +42,10 @@ def write_inputs(case, d, nsteps, snaps=None, dump_every=None, extra=(), run_sty
     selects verlet/gb300 (Update::create_integrate, src/update.cpp:342-377),
     while the integrator LAMMPS creates at start-up is never suffixed
     (src/update.cpp:103-106).  runs: several consecutive "run" commands
-    (for instance a warm-up and a timed run) in place of "run nsteps"."""
+    (for instance a warm-up and a timed run) in place of "run nsteps".
+    atom_sort: the "atom_modify sort" frequency and bin size: "0 0" for the
+    parity runs (the atoms keep their order), "1000 0" (the reference's
+    default, its fastest setting) for timing."""
     a = case["atoms"]
     n = len(a["tag"])
     mat = case["material"]
@@ -71,7 +75,7 @@ def write_inputs(case, d, nsteps, snaps=None, dump_every=None, extra=(), run_sty
             if bond["settings"][f] != workloads.BOND_DEFAULTS[f]:
                 model += " %s %s" % (workloads.BOND_KEYWORDS[f], "on" if bond["settings"][f] else "off")
     tpl = lambda m: " ".join(fmt(m[i][j]) for i in range(nt) for j in range(nt))  # noqa: E731
-    s = ["atom_style granular", "atom_modify map array sort 0 0", "boundary %s" % bnd,
+    s = ["atom_style granular", "atom_modify map array sort %s" % atom_sort, "boundary %s" % bnd,
          "newton off", "communicate single vel yes", "units si",
          "read_data data.case", "neighbor %s bin" % fmt(case["skin"]), "neigh_modify delay 0",
          "fix m1 all property/global youngsModulus peratomtype %s" % " ".join(fmt(e) for e in mat["E"]),
