@@ -51,8 +51,9 @@ KERNEL_UNITS = {
                  "flop_contact": 12.0},
 }
 # DRAM bytes (read + write) per atom of one launch, from the ncu capture of
-# the workload (hopper1m at 500k atoms)
-DRAM_PER_ATOM = {"hopper1m": {"pair": 422.2, "particle": 395.5}}
+# the workload (hopper1m at 500k atoms: k_pair_pf 131.0 MB read + 19.7 MB
+# written, k_particle 106.8 + 13.3 MB)
+DRAM_PER_ATOM = {"hopper1m": {"pair": 301.3, "particle": 240.2}}
 
 
 # ----------------------------------------------------------------------------
