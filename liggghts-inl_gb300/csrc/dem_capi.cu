@@ -258,7 +258,7 @@ static int alloc_atoms(dem_handle *h, int nmax) {
       ar.take(&A.type, nmax);
       ar.take(&A.tag, nmax);
       ar.take(&A.lidx, nmax);
-      ar.take(&A.whist, (size_t)3 * kMaxPlanes * nmax);
+      ar.take(&A.whist, (size_t)3 * std::max(1, s.nplanes) * nmax);  // walls are added before atoms
       ar.take(&A.wbits, nmax);
       double **fm[] = {&A.fmx, &A.fmy, &A.fmz, &A.tmx, &A.tmy, &A.tmz};
       for (double **pp : fm) ar.take(pp, nmax);
@@ -1151,8 +1151,8 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
           a = std::min(a, mh.tri[(size_t)t * kTriStride + 3 * q + d]);
           b = std::max(b, mh.tri[(size_t)t * kTriStride + 3 * q + d]);
         }
-        auto cc = [&](double x) {
-          long c = (long)((x - s.boxlo[d]) / s.csz[d]);
+        auto cc = [&](double x) {  // an estimate: the rebuild grows the list if it is short
+          long c = (long)((x - s.boxlo[d]) * s.icsz[d]);
           return std::min<long>(std::max<long>(c, 0), s.nc[d] - 1);
         };
         cells *= cc(b + M.distmax) - cc(a - M.distmax) + 1 + (M.moving ? 2 : 0);

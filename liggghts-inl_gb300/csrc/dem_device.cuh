@@ -128,6 +128,7 @@ struct Ctrl {
   int np_live;        // entries in use (ensembles: np less the unused entries)
   int ens_inplace;    // ensemble builds in place (atoms and list)
   int ens_relayout;   // ensemble builds in place for the atoms, list re-laid
+  int pdone;          // blocks of k_particle done (the last one decides; graph steps)
 };
 
 // Primitive wall of fix wall/gran (src/primitive_wall_definitions.h): a

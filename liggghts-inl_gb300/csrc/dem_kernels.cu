@@ -93,7 +93,9 @@ __device__ __forceinline__ int cell_coord(const Sys &s, double x, int d) {
 // An ensemble decides per system, as each system running alone would; the
 // rebuild stage runs when any system rebuilds, and the others keep their
 // atom order, list and histories.  Called by every thread of a single
-// block (one thread per system at a time); the result is the block's.
+// block (one thread per system at a time); the result is the block's.  The
+// displacement flags are read past L1 (the last block of k_particle decides
+// while the flags other blocks set may sit stale in its SM's L1).
 __device__ __forceinline__ int decide_rebuild(const Sys &s, Ctrl *c) {
   const int force = c->force_rebuild;
   int r_any = 0;
@@ -101,7 +103,8 @@ __device__ __forceinline__ int decide_rebuild(const Sys &s, Ctrl *c) {
     int r = 1;
     if (!force) {
       const int ago = ++s.sys_ago[k];
-      r = (ago >= s.neigh_delay && ago % s.neigh_every == 0) ? (s.neigh_check ? s.sys_moved[k] : 1) : 0;
+      r = (ago >= s.neigh_delay && ago % s.neigh_every == 0) ? (s.neigh_check ? __ldcg(&s.sys_moved[k]) : 1)
+                                                             : 0;
     }
     s.sys_reb[k] = r;
     s.sys_moved[k] = 0;
@@ -113,7 +116,7 @@ __device__ __forceinline__ int decide_rebuild(const Sys &s, Ctrl *c) {
       reb = 1;
     } else if (!s.nsys) {
       c->ago++;
-      if (c->ago >= s.neigh_delay && c->ago % s.neigh_every == 0) reb = s.neigh_check ? c->moved : 1;
+      if (c->ago >= s.neigh_delay && c->ago % s.neigh_every == 0) reb = s.neigh_check ? __ldcg(&c->moved) : 1;
     }
     c->force_rebuild = reb ? 0 : c->mesh_moved;
     c->mesh_moved = 0;
@@ -686,8 +689,9 @@ __device__ __forceinline__ void permute_atom(const Sys &s, const AtomArrays &A, 
     }
     B.vx[i] = A.vx[o]; B.vy[i] = A.vy[o]; B.vz[i] = A.vz[o];
     B.wx[i] = A.wx[o]; B.wy[i] = A.wy[o]; B.wz[i] = A.wz[o];
-    B.fx[i] = A.fx[o]; B.fy[i] = A.fy[o]; B.fz[i] = A.fz[o];
-    B.tx[i] = A.tx[o]; B.ty[i] = A.ty[o]; B.tz[i] = A.tz[o];
+    // f and torque are not moved: a rebuild comes after the step's initial
+    // integration, and the step's gather writes them again before they are
+    // read (they are live only between dem_step calls)
     const double r = A.r[o];
     B.r[i] = r; B.m[i] = A.m[o]; B.dtfm[i] = A.dtfm[o]; B.dtir[i] = A.dtir[o];
     B.type[i] = A.type[o]; B.tag[i] = A.tag[o]; B.lidx[i] = A.lidx[o];
@@ -744,8 +748,6 @@ __device__ __forceinline__ void copy_atom(const Sys &s, const AtomArrays &A, con
     A.xh[i] = B.xh[i]; A.yh[i] = B.yh[i]; A.zh[i] = B.zh[i];
     A.vx[i] = B.vx[i]; A.vy[i] = B.vy[i]; A.vz[i] = B.vz[i];
     A.wx[i] = B.wx[i]; A.wy[i] = B.wy[i]; A.wz[i] = B.wz[i];
-    A.fx[i] = B.fx[i]; A.fy[i] = B.fy[i]; A.fz[i] = B.fz[i];
-    A.tx[i] = B.tx[i]; A.ty[i] = B.ty[i]; A.tz[i] = B.tz[i];
     A.r[i] = B.r[i]; A.m[i] = B.m[i]; A.dtfm[i] = B.dtfm[i]; A.dtir[i] = B.dtir[i];
     A.type[i] = B.type[i]; A.tag[i] = B.tag[i]; A.lidx[i] = B.lidx[i];
     const float4 xf = make_float4((float)B.x[i], (float)B.y[i], (float)B.z[i], (float)B.r[i]);
@@ -2377,15 +2379,31 @@ constexpr int kParticleMaxThreads = 256;
 // order, so that a warp's lanes run loops of equal length, and the sums go
 // back to the owner.  Each atom's sum keeps its order and its one thread, so
 // the result does not depend on the sort or the launch shape.
+// Graph steps without moving meshes: the last block of k_particle to finish
+// takes the step's rebuild decision and sets the loop's conditionals, as
+// k_decide_loop does after it otherwise (one node and one dependency fewer
+// per step).
+struct LoopCond {
+  int on;
+  cudaGraphConditionalHandle hreb, hloop;
+};
+
 template <int NORMAL, bool GATHER, bool FINAL, bool INITIAL>
-__global__ void __launch_bounds__(kParticleMaxThreads, 4) k_particle(Sys s, int shearupdate) {
+__global__ void __launch_bounds__(kParticleMaxThreads, 4) k_particle(Sys s, int shearupdate, LoopCond lp) {
   __shared__ double gsum[GATHER ? 6 : 1][GATHER ? kParticleMaxThreads : 1];
   __shared__ int gpb[GATHER ? kParticleMaxThreads : 1], grb[GATHER ? kParticleMaxThreads : 1];
   __shared__ unsigned gom[GATHER ? kParticleMaxThreads : 1], grm[GATHER ? kParticleMaxThreads : 1];
   __shared__ short gsorted[GATHER ? kParticleMaxThreads : 1];
   __shared__ int gcount[kGatherKeys], gfill[kGatherKeys], gstart[kGatherKeys], gnq;
+  __shared__ int last_block;
   Ctrl *c = s.ctrl;
-  if (c->halt) return;
+  if (c->halt) {
+    if (lp.on && blockIdx.x == 0 && threadIdx.x == 0) {
+      cudaGraphSetConditional(lp.hreb, 0);
+      cudaGraphSetConditional(lp.hloop, 0);
+    }
+    return;
+  }
   const AtomArrays &A = s.atoms[0];
   const PairArrays &L = s.pairs[0];
   const int n = c->n;
@@ -2549,6 +2567,27 @@ __global__ void __launch_bounds__(kParticleMaxThreads, 4) k_particle(Sys s, int 
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) {
     atomicExch(&c->status, kStatNan);
   }
+  if (lp.on) {  // the last block to finish decides (k_decide_loop's work)
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      last_block = atomicAdd(&c->pdone, 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (last_block) {
+      __threadfence();
+      if (threadIdx.x == 0) {
+        c->pdone = 0;
+        c->ntimestep++;
+      }
+      const int reb = decide_rebuild(s, c);
+      if (threadIdx.x == 0) {
+        c->loop_left--;
+        cudaGraphSetConditional(lp.hreb, reb ? 1u : 0u);
+        cudaGraphSetConditional(lp.hloop, c->loop_left > 0 ? 1u : 0u);
+      }
+    }
+  }
 }
 
 // ----------------------------------------------------------------------------
@@ -2648,7 +2687,7 @@ __global__ void k_upload_atoms(Sys s, AtomsIn in, int n, double dtf, double dtfr
     A.fx[i] = A.fy[i] = A.fz[i] = 0.0;
     A.tx[i] = A.ty[i] = A.tz[i] = 0.0;
     A.xh[i] = A.yh[i] = A.zh[i] = 0.0;
-    for (int k = 0; k < 3 * kMaxPlanes; k++) A.whist[(size_t)k * nmax + i] = 0.0;
+    for (int k = 0; k < 3 * s.nplanes; k++) A.whist[(size_t)k * nmax + i] = 0.0;
     A.wbits[i] = 0;
     A.fmx[i] = A.fmy[i] = A.fmz[i] = A.tmx[i] = A.tmy[i] = A.tmz[i] = 0.0;
     if (okv) {
@@ -2948,7 +2987,12 @@ int launch_rebuild(const Sys &s, const LaunchCfg &lc, cudaStream_t st, int stage
 // Builds the executable graph of `steps 2..n` of dem_step:
 //   WHILE(loop) { k_particle(gather+final+initial) -> k_decide_loop ->
 //                 IF(rebuild) { rebuild kernels } -> k_pair }
+// (without moving meshes, the last block of k_particle decides instead of
+// k_decide_loop)
 // The host sets ctrl->loop_left with launch_set_loop() before each launch.
+static int launch_particle_lp(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, const LoopCond &lp,
+                              cudaStream_t st);
+
 cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st, cudaStream_t st2,
                              cudaGraphExec_t *exec, int *kernels_per_step, int *kernels_per_rebuild) {
   cudaGraph_t g = nullptr;
@@ -2984,10 +3028,17 @@ cudaError_t build_step_graph(const Sys &s, const LaunchCfg &lc, cudaStream_t st,
   cudaGraph_t body = wp.conditional.phGraph_out[0];
   if ((e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
     return fail(e);
-  int k = launch_particle(s, lc, kModeGatherFinalInitial, 1, st);
-  k += launch_mesh_move(s, lc, st);
-  k_decide_loop<<<1, sys_threads(s), 0, st>>>(s, hreb, hloop);
-  k++;
+  bool moving = false;
+  for (int m = 0; m < s.nmeshes; m++) moving |= s.meshes[m].moving != 0;
+  int k = 0;
+  if (moving) {  // the mesh moves between the particle kernel and the decision
+    k += launch_particle(s, lc, kModeGatherFinalInitial, 1, st);
+    k += launch_mesh_move(s, lc, st);
+    k_decide_loop<<<1, sys_threads(s), 0, st>>>(s, hreb, hloop);
+    k++;
+  } else {
+    k += launch_particle_lp(s, lc, kModeGatherFinalInitial, 1, LoopCond{1, hreb, hloop}, st);
+  }
   cudaStreamCaptureStatus cs;
   const cudaGraphNode_t *deps = nullptr;
   size_t nd = 0;
@@ -3151,23 +3202,31 @@ int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t
 }
 
 template <int NORMAL>
-static void launch_particle_n(const Sys &s, int g, int B, int mode, int shearupdate, cudaStream_t st) {
+static void launch_particle_n(const Sys &s, int g, int B, int mode, int shearupdate, const LoopCond &lp,
+                              cudaStream_t st) {
   switch (mode) {
-    case kModeInitial: k_particle<NORMAL, false, false, true><<<g, B, 0, st>>>(s, shearupdate); break;
-    case kModeGather: k_particle<NORMAL, true, false, false><<<g, B, 0, st>>>(s, shearupdate); break;
-    case kModeGatherFinal: k_particle<NORMAL, true, true, false><<<g, B, 0, st>>>(s, shearupdate); break;
-    case kModeGatherFinalInitial: k_particle<NORMAL, true, true, true><<<g, B, 0, st>>>(s, shearupdate); break;
+    case kModeInitial: k_particle<NORMAL, false, false, true><<<g, B, 0, st>>>(s, shearupdate, lp); break;
+    case kModeGather: k_particle<NORMAL, true, false, false><<<g, B, 0, st>>>(s, shearupdate, lp); break;
+    case kModeGatherFinal: k_particle<NORMAL, true, true, false><<<g, B, 0, st>>>(s, shearupdate, lp); break;
+    case kModeGatherFinalInitial:
+      k_particle<NORMAL, true, true, true><<<g, B, 0, st>>>(s, shearupdate, lp);
+      break;
   }
 }
 
-int launch_particle(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, cudaStream_t st) {
+static int launch_particle_lp(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, const LoopCond &lp,
+                              cudaStream_t st) {
   // one particle per thread; smaller blocks give the same number of threads
   // in more, smaller blocks (each particle's sums do not depend on it)
   const int B = lc.particle_threads;
   const int g = grid_for(s.nmax, B, lc.max_grid * (256 / B));
-  if (s.normal == kHertz) launch_particle_n<kHertz>(s, g, B, mode, shearupdate, st);
-  else launch_particle_n<kHooke>(s, g, B, mode, shearupdate, st);
+  if (s.normal == kHertz) launch_particle_n<kHertz>(s, g, B, mode, shearupdate, lp, st);
+  else launch_particle_n<kHooke>(s, g, B, mode, shearupdate, lp, st);
   return 1;
+}
+
+int launch_particle(const Sys &s, const LaunchCfg &lc, int mode, int shearupdate, cudaStream_t st) {
+  return launch_particle_lp(s, lc, mode, shearupdate, LoopCond{0, 0, 0}, st);
 }
 
 }  // namespace gb300
