@@ -1529,11 +1529,106 @@ __device__ __forceinline__ void store_result(const Sys &s, int q, const ContactO
   r[5] = make_double2(0.0, 0.0);
 }
 
+// Phase 2 of k_pair for one queued entry q (delx, dely, delz, rsq_q from
+// its exact test): the bond law, the contact law, the result record
+template <int NORMAL, bool ROLL, bool BOND>
+__device__ __forceinline__ void band_entry(const Sys &s, int q, double delx, double dely, double delz,
+                                           double rsq_q, int shearupdate, long long ntimestep) {
+  const AtomArrays &A = s.atoms[0];
+  const PairArrays &L = s.pairs[0];
+  const size_t P = s.pcap;
+  const int i = L.i[q], j = L.j[q];
+  ContactIn ci;
+  ci.d[0] = delx;
+  ci.d[1] = dely;
+  ci.d[2] = delz;
+  ci.radi = A.r[i];
+  ci.radj = A.r[j];
+  ci.radsum = __dadd_rn(ci.radi, ci.radj);
+  ci.vr[0] = A.vx[i] - A.vx[j];
+  ci.vr[1] = A.vy[i] - A.vy[j];
+  ci.vr[2] = A.vz[i] - A.vz[j];
+  ci.wi[0] = A.wx[i]; ci.wi[1] = A.wy[i]; ci.wi[2] = A.wz[i];
+  ci.wj[0] = A.wx[j]; ci.wj[1] = A.wy[j]; ci.wj[2] = A.wz[j];
+  const bool touch = !BOND || rsq_q < __dmul_rn(ci.radsum, ci.radsum);
+  ContactOut bo;
+  bool bonded = false;
+  if (BOND) {
+    // evaluated in the reference's orientation: owner = lower lidx
+    // (periodic entries are directed and always owned by i)
+    const bool rev = L.sh[q] == kNoShift && A.lidx[i] > A.lidx[j];
+    const int a = rev ? j : i, b = rev ? i : j;
+    const double sg = rev ? -1.0 : 1.0;
+    BondIn bi;
+    bi.d[0] = sg * ci.d[0]; bi.d[1] = sg * ci.d[1]; bi.d[2] = sg * ci.d[2];
+    bi.rsq = rsq_q;
+    bi.radi = A.r[a];
+    bi.radj = A.r[b];
+    bi.vi[0] = A.vx[a]; bi.vi[1] = A.vy[a]; bi.vi[2] = A.vz[a];
+    bi.vj[0] = A.vx[b]; bi.vj[1] = A.vy[b]; bi.vj[2] = A.vz[b];
+    bi.wi[0] = A.wx[a]; bi.wi[1] = A.wy[a]; bi.wi[2] = A.wz[a];
+    bi.wj[0] = A.wx[b]; bi.wj[1] = A.wy[b]; bi.wj[2] = A.wz[b];
+    bi.xi[0] = A.x[a]; bi.xi[1] = A.y[a]; bi.xi[2] = A.z[a];
+    bi.tp = A.type[a] * (s.ntypes + 1) + A.type[b];
+    ContactOut bc;
+    bonded = bond_nonlinear(s, bi, L.hist + 3 * P + q, P, L.flag + q, shearupdate != 0, ntimestep, bc);
+    if (bonded) {  // back to the list's orientation (i owns the entry)
+      for (int k = 0; k < 3; k++) {
+        bo.F[k] = sg * bc.F[k];
+        bo.Ti[k] = rev ? bc.Tj[k] : bc.Ti[k];
+        bo.Tj[k] = rev ? bc.Ti[k] : bc.Tj[k];
+      }
+    }
+  }
+  ContactOut o;
+  if (touch) {
+    // r from 1/r: within an ulp of sqrt(rsq), which moves the overlap
+    // radsum - r by ~1e-13 of itself
+    ci.rinv = rsqrt(rsq_q);
+    ci.r = rsq_q * ci.rinv;
+    ci.reff = L.reff[q];
+    ci.c0 = L.c0[q];
+    ci.c1 = L.c1[q];
+    ci.en[0] = ci.d[0] * ci.rinv;
+    ci.en[1] = ci.d[1] * ci.rinv;
+    ci.en[2] = ci.d[2] * ci.rinv;
+    ci.deltan_wall = 0.0;
+    const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], A.type[j]);
+    double sh3[3] = {L.hist[q], L.hist[P + q], L.hist[2 * P + q]};
+    contact_law<NORMAL, false>(ci, tp, s.dt, s.tdamp, s.limitf, ROLL, shearupdate != 0, sh3, o,
+                               (BOND && bonded) ? &bo : nullptr);
+    if (shearupdate) {
+      L.hist[q] = sh3[0];
+      L.hist[P + q] = sh3[1];
+      L.hist[2 * P + q] = sh3[2];
+    }
+    L.flag[q] |= (kContactNormal | kContactTangential);
+  } else {
+    for (int k = 0; k < 3; k++) {
+      o.F[k] = bo.F[k];
+      o.Ti[k] = bo.Ti[k];
+      o.Tj[k] = bo.Tj[k];
+    }
+  }
+  if (touch || bonded) {
+    store_result(s, q, o);
+    s.active[q] = 1;
+  }
+}
+
+// Phase 1 runs per lane on 32 consecutive entries of a warp at a time; the
+// entries that need phase 2 wait in the warp's shared-memory queue (with
+// their exact test's delta and rsq) until 32 have gathered, so the bond and
+// contact laws run on full warps.  The warps' remainders merge into one
+// block batch at the end.  Each entry's result goes to its own slot and
+// depends on no other entry, so the order changes no value.
 template <int NORMAL, bool ROLL, bool BOND>
 __global__ void __launch_bounds__(kBandTile, 4) k_pair(Sys s, int shearupdate) {
-  __shared__ int q_p[kBandTile];
-  __shared__ double q_d[4][kBandTile];
-  __shared__ int wcnt[kBandTile / 32];
+  __shared__ int q_p[kBandTile / 32][64];
+  __shared__ double q_d[kBandTile / 32][4][64];
+  __shared__ int rest_p[kBandTile];
+  __shared__ double rest_d[4][kBandTile];
+  __shared__ int nrest;
   Ctrl *c = s.ctrl;
   if (c->halt) return;
   const AtomArrays &A = s.atoms[0];
@@ -1542,12 +1637,17 @@ __global__ void __launch_bounds__(kBandTile, 4) k_pair(Sys s, int shearupdate) {
   const size_t P = s.pcap;
   const double cdm = s.cdf * s.cdf;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
+  int *qp = q_p[warp];
+  double(*qd)[64] = q_d[warp];
   // cohesion bond/nonlinear: a bond can be created in this pass
   const long long ntimestep = BOND ? c->ntimestep : 0;
   const bool may_create = BOND && shearupdate &&
                           ((s.bond_flags & kBondCreateAlways) || ntimestep == s.bond_ts_create);
-  for (int base = blockIdx.x * kBandTile; base < np; base += gridDim.x * kBandTile) {
-    const int p = base + threadIdx.x;
+  int qn = 0;  // the same in every lane
+  const long stride = (long)gridDim.x * kBandTile;
+  for (long base = (long)blockIdx.x * kBandTile + warp * 32; base < np; base += stride) {
+    const int p = (int)base + lane;
     bool queue = false;
     double delx = 0., dely = 0., delz = 0., rsq = 0.;
     const int code = p < np ? L.sh[p] : kHole;
@@ -1580,107 +1680,56 @@ __global__ void __launch_bounds__(kBandTile, 4) k_pair(Sys s, int shearupdate) {
       }
     }
     const unsigned m = __ballot_sync(0xffffffffu, queue);
-    if (lane == 0) wcnt[warp] = __popc(m);
-    __syncthreads();
-    int off = 0, tot = 0;
-#pragma unroll
-    for (int k = 0; k < kBandTile / 32; k++) {
-      const int v = wcnt[k];
-      off += (k < warp) ? v : 0;
-      tot += v;
-    }
     if (queue) {
-      const int slot = off + __popc(m & ((1u << lane) - 1u));
-      q_p[slot] = p;
-      q_d[0][slot] = delx;
-      q_d[1][slot] = dely;
-      q_d[2][slot] = delz;
-      q_d[3][slot] = rsq;
+      const int slot = qn + __popc(m & below);
+      qp[slot] = p;
+      qd[0][slot] = delx;
+      qd[1][slot] = dely;
+      qd[2][slot] = delz;
+      qd[3][slot] = rsq;
     }
-    __syncthreads();
-    if (threadIdx.x < tot) {
-      const int q = q_p[threadIdx.x];
-      const int i = L.i[q], j = L.j[q];
-      ContactIn ci;
-      ci.d[0] = q_d[0][threadIdx.x];
-      ci.d[1] = q_d[1][threadIdx.x];
-      ci.d[2] = q_d[2][threadIdx.x];
-      const double rsq_q = q_d[3][threadIdx.x];
-      ci.radi = A.r[i];
-      ci.radj = A.r[j];
-      ci.radsum = __dadd_rn(ci.radi, ci.radj);
-      ci.vr[0] = A.vx[i] - A.vx[j];
-      ci.vr[1] = A.vy[i] - A.vy[j];
-      ci.vr[2] = A.vz[i] - A.vz[j];
-      ci.wi[0] = A.wx[i]; ci.wi[1] = A.wy[i]; ci.wi[2] = A.wz[i];
-      ci.wj[0] = A.wx[j]; ci.wj[1] = A.wy[j]; ci.wj[2] = A.wz[j];
-      const bool touch = !BOND || rsq_q < __dmul_rn(ci.radsum, ci.radsum);
-      ContactOut bo;
-      bool bonded = false;
-      if (BOND) {
-        // evaluated in the reference's orientation: owner = lower lidx
-        // (periodic entries are directed and always owned by i)
-        const bool rev = L.sh[q] == kNoShift && A.lidx[i] > A.lidx[j];
-        const int a = rev ? j : i, b = rev ? i : j;
-        const double sg = rev ? -1.0 : 1.0;
-        BondIn bi;
-        bi.d[0] = sg * ci.d[0]; bi.d[1] = sg * ci.d[1]; bi.d[2] = sg * ci.d[2];
-        bi.rsq = rsq_q;
-        bi.radi = A.r[a];
-        bi.radj = A.r[b];
-        bi.vi[0] = A.vx[a]; bi.vi[1] = A.vy[a]; bi.vi[2] = A.vz[a];
-        bi.vj[0] = A.vx[b]; bi.vj[1] = A.vy[b]; bi.vj[2] = A.vz[b];
-        bi.wi[0] = A.wx[a]; bi.wi[1] = A.wy[a]; bi.wi[2] = A.wz[a];
-        bi.wj[0] = A.wx[b]; bi.wj[1] = A.wy[b]; bi.wj[2] = A.wz[b];
-        bi.xi[0] = A.x[a]; bi.xi[1] = A.y[a]; bi.xi[2] = A.z[a];
-        bi.tp = A.type[a] * (s.ntypes + 1) + A.type[b];
-        ContactOut bc;
-        bonded = bond_nonlinear(s, bi, L.hist + 3 * P + q, P, L.flag + q, shearupdate != 0, ntimestep, bc);
-        if (bonded) {  // back to the list's orientation (i owns the entry)
-          for (int k = 0; k < 3; k++) {
-            bo.F[k] = sg * bc.F[k];
-            bo.Ti[k] = rev ? bc.Tj[k] : bc.Ti[k];
-            bo.Tj[k] = rev ? bc.Ti[k] : bc.Tj[k];
-          }
-        }
+    qn += __popc(m);
+    __syncwarp();
+    if (qn >= 32) {
+      band_entry<NORMAL, ROLL, BOND>(s, qp[lane], qd[0][lane], qd[1][lane], qd[2][lane], qd[3][lane], shearupdate,
+                                     ntimestep);
+      const int rem = qn - 32;
+      __syncwarp();
+      int vp = 0;
+      double v0 = 0., v1 = 0., v2 = 0., v3 = 0.;
+      if (lane < rem) {
+        vp = qp[32 + lane];
+        v0 = qd[0][32 + lane];
+        v1 = qd[1][32 + lane];
+        v2 = qd[2][32 + lane];
+        v3 = qd[3][32 + lane];
       }
-      ContactOut o;
-      if (touch) {
-        // r from 1/r: within an ulp of sqrt(rsq), which moves the overlap
-        // radsum - r by ~1e-13 of itself
-        ci.rinv = rsqrt(rsq_q);
-        ci.r = rsq_q * ci.rinv;
-        ci.reff = L.reff[q];
-        ci.c0 = L.c0[q];
-        ci.c1 = L.c1[q];
-        ci.en[0] = ci.d[0] * ci.rinv;
-        ci.en[1] = ci.d[1] * ci.rinv;
-        ci.en[2] = ci.d[2] * ci.rinv;
-        ci.deltan_wall = 0.0;
-        const TypePair tp = load_typepair(s.params, s.ntypes, A.type[i], A.type[j]);
-        double sh3[3] = {L.hist[q], L.hist[P + q], L.hist[2 * P + q]};
-        contact_law<NORMAL, false>(ci, tp, s.dt, s.tdamp, s.limitf, ROLL, shearupdate != 0, sh3, o,
-                                   (BOND && bonded) ? &bo : nullptr);
-        if (shearupdate) {
-          L.hist[q] = sh3[0];
-          L.hist[P + q] = sh3[1];
-          L.hist[2 * P + q] = sh3[2];
-        }
-        L.flag[q] |= (kContactNormal | kContactTangential);
-      } else {
-        for (int k = 0; k < 3; k++) {
-          o.F[k] = bo.F[k];
-          o.Ti[k] = bo.Ti[k];
-          o.Tj[k] = bo.Tj[k];
-        }
+      __syncwarp();
+      if (lane < rem) {
+        qp[lane] = vp;
+        qd[0][lane] = v0;
+        qd[1][lane] = v1;
+        qd[2][lane] = v2;
+        qd[3][lane] = v3;
       }
-      if (touch || bonded) {
-        store_result(s, q, o);
-        s.active[q] = 1;
-      }
+      qn = rem;
+      __syncwarp();
     }
-    __syncthreads();
   }
+  // the warps' remainders (at most 31 each) into one block batch
+  if (threadIdx.x == 0) nrest = 0;
+  __syncthreads();
+  int at = 0;
+  if (lane == 0 && qn) at = atomicAdd(&nrest, qn);
+  at = __shfl_sync(0xffffffffu, at, 0);
+  if (lane < qn) {
+    rest_p[at + lane] = qp[lane];
+    for (int k = 0; k < 4; k++) rest_d[k][at + lane] = qd[k][lane];
+  }
+  __syncthreads();
+  if (threadIdx.x < nrest)
+    band_entry<NORMAL, ROLL, BOND>(s, rest_p[threadIdx.x], rest_d[0][threadIdx.x], rest_d[1][threadIdx.x],
+                                   rest_d[2][threadIdx.x], rest_d[3][threadIdx.x], shearupdate, ntimestep);
 }
 
 // Pair forces without cohesion and with contact distance factor 1 (an entry
