@@ -1504,18 +1504,18 @@ __global__ void k_finish_rebuild(Sys s) {
 // pair forces: one thread per half-list entry, results to the pair buffer
 // ----------------------------------------------------------------------------
 
-// Each block walks tiles of 256 list entries.  Phase 1 (all lanes): the exact
-// contact test rsq < radsum^2.  Touching entries are compacted into a shared
-// queue (warp ballots + block prefix), so phase 2 runs the FP64 contact law
-// on dense warps: non-touching entries cost no FP64 issue slots.  Results go
-// to the entry's own slot p, so the processing order never changes a value.
+// The pair kernels test list entries per lane (phase 1) and queue the ones
+// that need the FP64 laws in a per-warp shared-memory queue (warp ballots),
+// so phase 2 runs on full warps: entries that need nothing cost no FP64
+// issue slots.  Results go to the entry's own slot, so the processing order
+// never changes a value.  kPairTile is k_pair_pf's block size.
 constexpr int kPairTile = 256;
 
-// The general kernel carries the bond law.  Tiles of 128 threads capped at
-// 128 registers (a few spilled) let four blocks share an SM, so one block's
-// FP64 work overlaps the others' waits at the tile barrier (measured on the
-// 200k bonded fibre bed: 0.55 ms with one 256-thread block per SM, 0.41 ms
-// with three 128-thread blocks, 0.35 ms with four; 64-thread tiles 0.40 ms).
+// The general kernel carries the bond law.  Blocks of 128 threads capped at
+// 128 registers (a few spilled) let four blocks share an SM (measured on the
+// 200k bonded fibre bed with one queue per tile: 0.55 ms with one 256-thread
+// block per SM, 0.41 ms with three 128-thread blocks, 0.35 ms with four;
+// 64-thread tiles 0.40 ms; with per-warp queues 0.27 ms).
 constexpr int kBandTile = 128;
 
 // the entry's result record: three whole 32-byte sectors in one go
