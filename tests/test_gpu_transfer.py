@@ -91,3 +91,32 @@ def test_upload_rejects_bad_atoms(field, idx, value, status, staged, monkeypatch
     g.step(5)
     assert np.all(np.isfinite(g.atoms()["x"]))
     g.close()
+
+
+def test_download_of_some_arrays_over_several_tiles():
+    """The download kernel writes each 3-vector through a shared-memory tile
+    of 256 atoms.  A caller may pass null for arrays it does not want: those
+    are left alone and the others come back as in the full download (700
+    atoms after 25 steps with rebuilds: three tiles, the last one partial)."""
+    import ctypes
+    from gb300dem import api, workloads
+    case = workloads.lattice_case(seed=3, nx=10, ny=10, nz=7, spacing=1.97e-3, radius=(0.9e-3, 1.05e-3),
+                                  z0=1.0e-3, jitter=3e-5, vmax=1.0, wmax=80.0)
+    g = api.DemSystem(case)
+    g.setup()
+    g.step(25)
+    full = {k: v.copy() for k, v in g.atoms().items()}
+    n = g.natoms()
+    assert n == 700
+    keys = ("tag", "type", "x", "v", "omega", "f", "torque", "radius", "rmass")
+    L = api.load()
+    for sel in (("x", "f"), ("v", "torque", "radius"), ("omega", "tag", "rmass", "type"), ()):
+        out = {k: np.full_like(full[k], -7) for k in keys}
+        ptrs = [out[k].ctypes.data_as(ctypes.c_void_p) if k in sel else None for k in keys]
+        assert L.dem_download_atoms(g.h, *ptrs) == 0
+        for k in keys:
+            if k in sel:
+                assert np.array_equal(out[k], full[k]), (sel, k)
+            else:
+                assert np.all(out[k] == -7), (sel, k)
+    g.close()
