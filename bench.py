@@ -489,15 +489,30 @@ def run_gb300(args):
     # ---- e2e through the C ABI with host buffers
     # (the caller's host arrays exist before the run, as the reference's
     # atom->x, atom->v, ... do; the device reads and fills them)
-    # The caller's arrays are written by the host just before (as the
-    # reference's atom->x, atom->v, ... are), not the workload's arrays that
-    # the first upload above already read: pages the device has read may be
-    # migrating to its memory (access-counter migration), which made the
-    # read of those same pages 1.6 to 10.5 ms from run to run
+    # The caller's arrays are in pinned (page-locked) host memory, allocated
+    # and filled before the timed region.  Pageable arrays go through the
+    # same calls (the kernels reach them through the host page tables), but
+    # their transfer time depends on the pages' history: 1 to 16 ms for the
+    # 144 MB of a download, against the pinned arrays' steady rate.
+    import torch
+    pinned = []
+
+    def _pinned(shape, dtype):
+        tt = {np.dtype(np.float64): torch.float64, np.dtype(np.int32): torch.int32}[np.dtype(dtype)]
+        t = torch.empty(shape, dtype=tt, pin_memory=True)
+        pinned.append(t)
+        return t.numpy()
+
     a = case["atoms"]
-    host = {k: np.array(v, copy=True, order="C") for k, v in a.items()}
+    host = {}
+    for k, v in a.items():
+        host[k] = _pinned(v.shape, v.dtype)
+        host[k][...] = v
     g2 = api.DemSystem({k: v for k, v in case.items() if k != "atoms"})
-    hout = g2.atom_buffers(n)
+    hout = {}
+    for k, v in g2.atom_buffers(n).items():
+        hout[k] = _pinned(v.shape, v.dtype)
+        hout[k].fill(0)
     t0 = time.perf_counter()
     g2.upload(host)
     if restart:
@@ -602,7 +617,7 @@ def run_gb300(args):
                                pairs=npairs, rebuilds_total=st["nrebuilds"]),
                 "e2e": {"value": e2e, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d / args.steps,
                         "d2h_bytes_per_step": d2h / args.steps,
-                        "note": "upload+setup+K steps+download through the C ABI, host buffers",
+                        "note": "upload+setup+K steps+download through the C ABI, pinned host buffers",
                         "phases": phases},
                 "gpu_launches": kt["kernel_launches"],
                 "roofline": roof, "cpu_baseline": cpu, "clocks": cl, "wall_s": wall,
