@@ -3209,14 +3209,16 @@ int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t
   if (s.cdf == 1.0) {
     // blocks per SM the kernel is compiled for (registers: 80 at 3, 64 at
     // 4 with some spilling) and the grid: LIGGGHTS_GB300_PAIR_MINB (3 or 4,
-    // default 4: the kernel ran 10 % faster on the 1M hopper),
+    // default 3: with the per-warp queues the graph step ran 2 % faster on
+    // the 1M hopper and 1.5 % on the dense bed than at 4),
     // LIGGGHTS_GB300_PAIR_GRID (0: up to 8 blocks per SM, the default, which
     // leaves room for the wall kernel beside it; 1: one resident wave, the
-    // tiles taken grid-stride); results do not depend on either
+    // tiles taken grid-stride: the pair kernel alone runs faster, the step
+    // slower); results do not depend on either
     static int minb = -1, wave = 0;
     if (minb < 0) {
       const char *e = getenv("LIGGGHTS_GB300_PAIR_MINB");
-      minb = (e && atoi(e) == 3) ? 3 : 4;
+      minb = (e && atoi(e) == 4) ? 4 : 3;
       const char *w = getenv("LIGGGHTS_GB300_PAIR_GRID");
       wave = (w && atoi(w) == 1) ? 1 : 0;
     }
