@@ -287,13 +287,27 @@ __global__ void ka_cellsort(ADev s) {
 // (ri + rj) cdf + skin (src/neigh_gran.cpp:580-586)
 // candidates [qb, qe) of the cell-sorted order (s.order), all with image
 // code `code`
+// A candidate farther in FP32 (the mirror xf, refreshed by every drift and
+// wrap) than the cutoff plus fm, the bound of the mirror's rounding and of
+// this arithmetic, is beyond the exact cutoff too: it skips the FP64 test.
 template <bool FILL>
-__device__ __forceinline__ void ka_scan(const ADev &s, int i, const double xi[3], double ri, int qb, int qe,
-                                        int code, int &cnt, int &out, int out_end, int *pi, int *pj,
-                                        uint8_t *shc) {
+__device__ __forceinline__ void ka_scan(const ADev &s, int i, const double xi[3], double ri, float4 fi,
+                                        float cdff, float skinm, int qb, int qe, int code, int &cnt, int &out,
+                                        int out_end, int *pi, int *pj, uint8_t *shc) {
+  float sxf = 0.f, syf = 0.f, szf = 0.f;
+  if (code != kNoShift) {
+    const int sx = code % 3 - 1, sy = (code / 3) % 3 - 1, sz = code / 9 - 1;
+    sxf = sx == 0 ? 0.f : (sx > 0 ? s.prdf[0] : -s.prdf[0]);
+    syf = sy == 0 ? 0.f : (sy > 0 ? s.prdf[1] : -s.prdf[1]);
+    szf = sz == 0 ? 0.f : (sz > 0 ? s.prdf[2] : -s.prdf[2]);
+  }
   for (int q = qb; q < qe; q++) {
     const int j = s.order[q];
     if (code == kNoShift && j <= i) continue;
+    const float4 b = s.xf[j];
+    const float fx = fi.x - (b.x + sxf), fy = fi.y - (b.y + syf), fz = fi.z - (b.z + szf);
+    const float rf = (fi.w + b.w) * cdff + skinm;
+    if (fx * fx + fy * fy + fz * fz > rf * rf) continue;
     double xj[3] = {s.x[3 * j], s.x[3 * j + 1], s.x[3 * j + 2]};
     a_image(s, code, xj);
     const double dx = xi[0] - xj[0], dy = xi[1] - xj[1], dz = xi[2] - xj[2];
@@ -318,9 +332,11 @@ __device__ __forceinline__ void ka_scan(const ADev &s, int i, const double xi[3]
 // periodic x boundary is scanned alone, with its image shift.
 template <bool FILL>
 __global__ void ka_pairs(ADev s, int *pi, int *pj, uint8_t *shc, const int *row) {
+  const float cdff = (float)s.cdf, skinm = (float)s.skin + s.fm;
   AGRID(i, s.n) {
     const double xi[3] = {s.x[3 * i], s.x[3 * i + 1], s.x[3 * i + 2]};
     const double ri = s.r[i];
+    const float4 fi = s.xf[i];
     int ci[3];
     for (int d = 0; d < 3; d++) ci[d] = a_cell_coord(s, xi[d], d);
     int cnt = 0, out = FILL ? row[i] : 0;
@@ -358,13 +374,13 @@ __global__ void ka_pairs(ADev s, int *pi, int *pj, uint8_t *shc, const int *row)
         const int rowb = s.nc[0] * (nb[1][ky] + s.nc[1] * nb[2][kz]);
         const int syz = 3 * (sv3[1][ky] + 1) + 9 * (sv3[2][kz] + 1);
         if (lwrap)
-          ka_scan<FILL>(s, i, xi, ri, s.cell_start[rowb + nb[0][0]], s.cell_start[rowb + nb[0][0] + 1], syz, cnt,
-                        out, out_end, pi, pj, shc);
-        ka_scan<FILL>(s, i, xi, ri, s.cell_start[rowb + x0], s.cell_start[rowb + x1 + 1], 1 + syz, cnt, out,
-                      out_end, pi, pj, shc);
+          ka_scan<FILL>(s, i, xi, ri, fi, cdff, skinm, s.cell_start[rowb + nb[0][0]],
+                        s.cell_start[rowb + nb[0][0] + 1], syz, cnt, out, out_end, pi, pj, shc);
+        ka_scan<FILL>(s, i, xi, ri, fi, cdff, skinm, s.cell_start[rowb + x0], s.cell_start[rowb + x1 + 1],
+                      1 + syz, cnt, out, out_end, pi, pj, shc);
         if (rwrap)
-          ka_scan<FILL>(s, i, xi, ri, s.cell_start[rowb + nb[0][2]], s.cell_start[rowb + nb[0][2] + 1], 2 + syz,
-                        cnt, out, out_end, pi, pj, shc);
+          ka_scan<FILL>(s, i, xi, ri, fi, cdff, skinm, s.cell_start[rowb + nb[0][2]],
+                        s.cell_start[rowb + nb[0][2] + 1], 2 + syz, cnt, out, out_end, pi, pj, shc);
       }
     }
     if (!FILL) s.pcount[i] = cnt;
