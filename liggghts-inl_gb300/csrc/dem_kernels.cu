@@ -3208,20 +3208,22 @@ int launch_pair(const Sys &s, const LaunchCfg &lc, int shearupdate, cudaStream_t
   }
   if (s.cdf == 1.0) {
     // blocks per SM the kernel is compiled for (registers: 80 at 3, 64 at
-    // 4 with some spilling) and the grid: LIGGGHTS_GB300_PAIR_MINB (3 or 4,
-    // default 3: with the per-warp queues the graph step ran 2 % faster on
-    // the 1M hopper and 1.5 % on the dense bed than at 4),
+    // 4 with some spilling): 3 with mesh walls, whose wall kernel runs
+    // beside this one (the 1M hopper's graph step 2 % faster than at 4),
+    // else 4 (the 256-system ensemble 12 % faster than at 3; the dense bed
+    // 1.6 % slower); LIGGGHTS_GB300_PAIR_MINB 3 or 4 sets it.  The grid:
     // LIGGGHTS_GB300_PAIR_GRID (0: up to 8 blocks per SM, the default, which
     // leaves room for the wall kernel beside it; 1: one resident wave, the
     // tiles taken grid-stride: the pair kernel alone runs faster, the step
-    // slower); results do not depend on either
-    static int minb = -1, wave = 0;
-    if (minb < 0) {
+    // slower).  Results do not depend on either.
+    static int env_minb = -1, wave = 0;
+    if (env_minb < 0) {
       const char *e = getenv("LIGGGHTS_GB300_PAIR_MINB");
-      minb = (e && atoi(e) == 4) ? 4 : 3;
+      env_minb = (e && (atoi(e) == 3 || atoi(e) == 4)) ? atoi(e) : 0;
       const char *w = getenv("LIGGGHTS_GB300_PAIR_GRID");
       wave = (w && atoi(w) == 1) ? 1 : 0;
     }
+    const int minb = env_minb ? env_minb : (s.nmeshes > 0 ? 3 : 4);
     const int gp = wave ? std::min(g, lc.sms * minb) : g;
     if (minb == 4) {
       if (s.normal == kHertz) {
