@@ -557,6 +557,10 @@ def run_gb300(args):
     pair_flop = C * ku["pair"]["flop_contact"]
     part_flop = n * ku["particle"]["flop_atom"] + C * ku["particle"]["flop_contact"]
     dom = "pair" if pair_ms >= part_ms else "particle"
+    # the pair kernel that runs: k_pair_pf (contact distance factor 1, no
+    # cohesion) or k_pair (bonds, or a larger contact distance)
+    bonded = bool(case.get("bond")) or float(case.get("cdf", 1.0)) != 1.0
+    pair_kernel = "k_pair" if bonded else "k_pair_pf"
     dom_bytes = pair_bytes if dom == "pair" else part_bytes
     dom_flop = pair_flop if dom == "pair" else part_flop
     dom_ms = pair_ms if dom == "pair" else part_ms
@@ -569,7 +573,7 @@ def run_gb300(args):
                 else "6800 GB/s (of fallback: no MEASURED_PEAKS.json)"}
     if fp64_peak:
         ach_tf = dom_flop / (dom_ms * 1e-3) / 1e12
-        roof = {"kernel": "k_pair_pf" if dom == "pair" else "k_particle", "bound": "fp64",
+        roof = {"kernel": pair_kernel if dom == "pair" else "k_particle", "bound": "fp64",
                 "achieved": ach_tf, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach_tf / fp64_peak,
                 "traffic": hbm_roof["traffic"],
                 "peak_source": "FP64 FMA peak measured live on this GPU (dem_measure_fp64_peak), "
@@ -577,9 +581,11 @@ def run_gb300(args):
                 "fp64_flop_per_launch": dom_flop, "hbm": hbm_roof,
                 "note": "flop counts DADD/DMUL + 2*DFMA per unit (ncu) times this run's units; the "
                         "FP64 pipe also issues compares, conversions and the idle lanes of partly "
-                        "active warps, so its active fraction exceeds achieved/peak"}
+                        "active warps, so its active fraction exceeds achieved/peak"
+                        + ("; k_pair: the contact law's flops only, not the bond law's"
+                           if bonded and dom == "pair" else "")}
     else:
-        roof = dict(hbm_roof, kernel="k_pair_pf" if dom == "pair" else "k_particle", bound="hbm")
+        roof = dict(hbm_roof, kernel=pair_kernel if dom == "pair" else "k_particle", bound="hbm")
     roof.update({"avg_launch_ms": dom_ms,
                  "units": {"atoms": n, "list_entries": E, "touching_entries": C,
                            "touching_per_atom": C / max(1, n)},
