@@ -276,7 +276,10 @@ int dem_upload_wall_history(dem_handle *h, int wall_id, const double *hist);
 int dem_setup(dem_handle *h);
 int dem_step(dem_handle *h, int nsteps);
 
-/* Atoms come back in the device's current (cell-sorted) order with their tags. */
+/* Atoms come back in the device's current (cell-sorted) order with their tags.
+ * Any array pointer may be NULL: that array is not written.  Page-locked
+ * arrays transfer at a steady rate; pageable ones through the host page
+ * tables, at a rate that depends on the pages' history. */
 int dem_natoms(dem_handle *h, int *n);
 int dem_download_atoms(dem_handle *h, int *tag, int *type, double *x, double *v, double *omega,
                        double *f, double *torque, double *radius, double *rmass);
