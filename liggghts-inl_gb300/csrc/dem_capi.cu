@@ -872,6 +872,15 @@ int dem_add_mesh(dem_handle *h, int ntri, const double *nodes, int wall_type, in
   CUDA_TRY(h, dalloc(L, &M.cn_list, std::max<size_t>(1, mh.cn_list.size())));
   if (!mh.cn_list.empty())
     CUDA_TRY(h, cudaMemcpyAsync(M.cn_list, mh.cn_list.data(), mh.cn_list.size() * sizeof(int), cudaMemcpyHostToDevice, h->st));
+  // bounding boxes for the cell-registration estimate of each upload
+  mh.bbox.resize(6 * (size_t)ntri);
+  for (int t = 0; t < ntri; t++) {
+    const double *g = &mh.tri[(size_t)t * kTriStride];
+    for (int d = 0; d < 3; d++) {
+      mh.bbox[6 * (size_t)t + d] = std::min(g[d], std::min(g[3 + d], g[6 + d]));
+      mh.bbox[6 * (size_t)t + 3 + d] = std::max(g[d], std::max(g[3 + d], g[6 + d]));
+    }
+  }
   if (mesh_id) *mesh_id = h->s.nmeshes;
   h->mesh_host.push_back(std::move(mh));
   h->s.nmeshes++;
@@ -1146,11 +1155,7 @@ int dem_upload_atoms(dem_handle *h, int n, const int *tag, const int *type, cons
     for (int t = 0; t < mh.ntri; t++) {
       long cells = 1;
       for (int d = 0; d < 3; d++) {
-        double a = mh.tri[(size_t)t * kTriStride + d], b = a;
-        for (int q = 1; q < 3; q++) {
-          a = std::min(a, mh.tri[(size_t)t * kTriStride + 3 * q + d]);
-          b = std::max(b, mh.tri[(size_t)t * kTriStride + 3 * q + d]);
-        }
+        const double a = mh.bbox[6 * (size_t)t + d], b = mh.bbox[6 * (size_t)t + 3 + d];
         auto cc = [&](double x) {  // an estimate: the rebuild grows the list if it is short
           long c = (long)((x - s.boxlo[d]) * s.icsz[d]);
           return std::min<long>(std::max<long>(c, 0), s.nc[d] - 1);

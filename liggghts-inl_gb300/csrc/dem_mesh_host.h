@@ -11,6 +11,7 @@ struct MeshHost {
   std::vector<int> meta;       // obtuse index + edge/corner activity bits
   std::vector<uint8_t> edge_active, corner_active;  // [t*3]
   std::vector<int> cn_start, cn_list;               // coplanar node-neighbours
+  std::vector<double> bbox;    // [t*6]: lower then upper corner of each triangle (initial mesh)
 };
 
 // Geometry, topology (unless edge/corner activity are given) and coplanar
